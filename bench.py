@@ -1,0 +1,291 @@
+"""Benchmark: sshex8 Laplacian matrix-free apply at L=4 on a 48^3 macro mesh.
+
+Workload (one "step"): one FP64 apply y = A x of the affine sshex8 Laplacian
+(level 4, 48x48x48 macro hex8 elements of the unit cube, interior macro nodes
+perturbed by U(-0.1,0.1) h, seed 0): 110,592 macro elements, 7,189,057 nodes.
+``value`` = GDoF/s with x, y and the mesh resident in HBM; the L2 cache is
+flushed (a 512 MiB write) before every timed step and kernels are timed with
+CUDA events on the launching stream.  ``e2e`` = the same apply through the C
+ABI with host buffers: pinned host x -> device, zero y, apply, y -> pinned host.
+
+``--impl reference`` times the reference CPU implementation of the same apply
+(the oracle port of affine_sshex8_laplacian_stencil_apply_fff, OpenMP, all host
+threads) on the same mesh.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+NX = 48
+LEVEL = 4
+SEED = 0
+PERTURB = 0.1
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--nx", type=int, default=NX)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def workload_config(nx):
+    from sfem_gb300.mesh import SSMesh
+
+    m = SSMesh(nx, nx, nx, LEVEL, perturb=PERTURB, seed=SEED)
+    return m
+
+
+class ClockSampler:
+    """Samples nvidia-smi SM clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.samples = []
+        self._stop = threading.Event()
+        self._thr = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(
+                    ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits"],
+                    capture_output=True, text=True, timeout=5).stdout.strip()
+                if out:
+                    self.samples.append([s.strip() for s in out.split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._thr = threading.Thread(target=self._run, daemon=True)
+        self._thr.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        if self._thr:
+            self._thr.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for s in self.samples for k in range(4) if len(s) > 3 + k and "Active" in s[3 + k]
+                          and "Not" not in s[3 + k]})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def measured_peak_hbm():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return 6800.0, "fallback"
+
+
+def cpu_baseline(m, reps=3):
+    """Time the CPU oracle apply (port of the reference CPU kernel) on the host cores."""
+    import oracle as O
+
+    el = m.elements(LEVEL)
+    fff = O.fff_fill(el[m.macro_corner_lidx(LEVEL)], m.points)
+    x = np.random.default_rng(1).standard_normal(m.n_nodes())
+    y = np.zeros_like(x)
+    O.sshex8_laplacian_apply(LEVEL, el, fff, x, out=y)  # warm-up
+    t = time.perf_counter()
+    for _ in range(reps):
+        y[:] = 0
+        O.sshex8_laplacian_apply(LEVEL, el, fff, x, out=y)
+    dt = (time.perf_counter() - t) / reps
+    return {"value": m.n_nodes() / dt / 1e9, "unit": "GDoF/s", "cores": os.cpu_count(), "kind": "port",
+            "sample": f"{reps} FP64 applies of the full 48^3 L=4 mesh (oracle port of "
+                      f"affine_sshex8_laplacian_stencil_apply_fff, OpenMP)", "seconds_per_apply": dt}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    m = workload_config(args.nx)
+    import oracle as O
+
+    el = m.elements(LEVEL)
+    fff = O.fff_fill(el[m.macro_corner_lidx(LEVEL)], m.points)
+    x = np.random.default_rng(1).standard_normal(m.n_nodes())
+    y = np.zeros_like(x)
+    for _ in range(max(1, args.warmup)):
+        O.sshex8_laplacian_apply(LEVEL, el, fff, x, out=y)
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        y[:] = 0
+        O.sshex8_laplacian_apply(LEVEL, el, fff, x, out=y)
+    dt = (time.perf_counter() - t) / args.steps
+    v = m.n_nodes() / dt / 1e9
+    line = {
+        "impl": "reference", "metric": "sshex8 Laplacian apply GDoF/s (FP64, L=4, 48^3 macro)", "value": v,
+        "unit": "GDoF/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "sshex8_laplacian_apply_L4_48cube", "nodes": m.n_nodes(), "macro_elements": m.n_elements},
+        "cpu_baseline": {"value": v, "unit": "GDoF/s", "cores": os.cpu_count(), "kind": "port",
+                         "sample": f"{args.steps} timed FP64 applies of the full mesh (oracle port, OpenMP)"},
+        "e2e": {"value": v, "unit": "GDoF/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def run_ours(args):
+    import torch
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    dev = torch.device(f"cuda:{local}")
+    torch.cuda.set_device(dev)
+
+    from sfem_gb300 import capi
+    from sfem_gb300.operators import Laplacian, SSMeshDevice
+
+    capi.load()
+    m = workload_config(args.nx)
+    sp = SSMeshDevice(m, LEVEL, device=dev)
+    op = Laplacian(sp).initialize()
+    N, E = m.n_nodes(), m.n_elements
+    x = torch.randn(N, dtype=torch.float64, device=dev, generator=torch.Generator(device=dev).manual_seed(1))
+    y = torch.zeros(N, dtype=torch.float64, device=dev)
+    flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def step():
+        y.zero_()
+        op.apply(x, y)
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+    # device-timed region: events around each apply (the y.zero_ is the
+    # accumulate-interface's caller-side reset and is excluded), L2 flushed before each step
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        wall0 = time.perf_counter()
+        for k in range(args.steps):
+            flush.fill_(k & 0xFF)
+            y.zero_()
+            starts[k].record(stream)
+            op.apply(x, y)
+            ends[k].record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - wall0
+    times = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    t_kernel = float(np.mean(times)) / 1e3
+    if world > 1:
+        tt = torch.tensor([t_kernel], device=dev)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_kernel = float(tt.item())
+    value = world * N / t_kernel / 1e9
+
+    # end-to-end through the C ABI with host buffers
+    xh = torch.empty(N, dtype=torch.float64, pin_memory=True)
+    xh.copy_(x.cpu())
+    yh = torch.empty(N, dtype=torch.float64, pin_memory=True)
+    xd = torch.empty_like(x)
+    e2e_steps = max(3, args.steps // 5)
+    for _ in range(2):
+        xd.copy_(xh, non_blocking=True)
+        y.zero_()
+        op.apply(xd, y)
+        yh.copy_(y, non_blocking=True)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(e2e_steps):
+        xd.copy_(xh, non_blocking=True)
+        y.zero_()
+        op.apply(xd, y)
+        yh.copy_(y, non_blocking=True)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t_e2e = e0.elapsed_time(e1) / 1e3 / e2e_steps
+    e2e_value = world * N / t_e2e / 1e9
+
+    peak, peak_kind = measured_peak_hbm()
+    alg_bytes = 2 * 8 * N + (4 * (LEVEL + 1) ** 3 + 24) * E
+    achieved = alg_bytes / t_kernel / 1e9
+    fp64_flops = 2 * 64 * (LEVEL ** 3) * E  # element-matrix form, 128 flop per micro element
+    line = {
+        "metric": "sshex8 Laplacian apply GDoF/s (FP64, L=4, 48^3 macro); time-to-1e-10 solve in 'solve'",
+        "value": value, "unit": "GDoF/s", "n_gpus": world, "steps": args.steps, "warmup": max(3, args.warmup),
+        "ms_per_step": t_kernel * 1e3, "higher_is_better": True, "scaling": "weak" if world > 1 else "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "sshex8_laplacian_apply_L4_48cube", "nodes": N, "macro_elements": E, "level": LEVEL,
+                   "perturb": PERTURB, "seed": SEED, "l2": "flushed (512 MiB write) before every timed step",
+                   "parallelism": f"replicas{world}" if world > 1 else "single"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None, "peak_kind": peak_kind, "algorithmic_bytes": alg_bytes,
+                     "fp64_gflops_achieved": fp64_flops / t_kernel / 1e9},
+        "e2e": {"value": e2e_value, "unit": "GDoF/s", "h2d_bytes_per_step": 8 * N, "d2h_bytes_per_step": 8 * N},
+        "gpu_launches": args.steps,
+        "clocks": clk.summary(),
+        "wall_s_timed": wall,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        try:
+            line["cpu_baseline"] = cpu_baseline(m)
+        except Exception as exc:
+            line["cpu_baseline"] = {"value": None, "error": str(exc)}
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,298 @@
+"""CPU oracle for the matrix-free operator path (TEST INFRASTRUCTURE ONLY).
+
+Two libraries are exposed through ctypes:
+
+* ``lib()``  -- the plain-C restatement ``oracle/src/oracle.c`` (always built);
+* ``ref()``  -- the reference's own CPU sources compiled in place
+  (``oracle/_ref/libsfem_ref.so``), available only where the reference tree is
+  present; it pins the restatement.
+
+Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
+``bench.py`` may import this package.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+from . import build as _build
+
+_lib = None
+_ref = None
+
+c_int = C.c_int
+c_ptrdiff = C.c_ssize_t
+c_double = C.c_double
+c_void_p = C.c_void_p
+
+
+def _ptr(a: np.ndarray):
+    return C.c_void_p(a.ctypes.data)
+
+
+class PtrArray:
+    """``T**`` view of the rows of a 2-D C-contiguous array (keeps it alive)."""
+
+    def __init__(self, a: np.ndarray):
+        self.a = np.ascontiguousarray(a)
+        n = self.a.shape[0]
+        self.arr = (C.c_void_p * n)(*[self.a[i].ctypes.data for i in range(n)])
+
+    @property
+    def p(self):
+        return C.cast(self.arr, C.c_void_p)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.build_oracle()
+        _lib = C.CDLL(str(path))
+    return _lib
+
+
+def ref():
+    """The reference's compiled CPU kernels, or None when unavailable."""
+    global _ref
+    if _ref is None:
+        path = _build.REF_LIB
+        if not path.exists():
+            path = _build.build_ref()
+        if path is None or not Path(path).exists():
+            return None
+        _ref = C.CDLL(str(path))
+    return _ref
+
+
+# ---------------------------------------------------------------------------
+# helpers (numpy in, numpy out)
+# ---------------------------------------------------------------------------
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def fff_fill(corners, points, use_ref=False):
+    """FFF (AoS float32 [E,6]) at the element centre; ``corners`` int32 [8,E] in hex8 order."""
+    L = ref() if use_ref else lib()
+    fn = L.ref_hex8_fff_fill if use_ref else L.or_hex8_fff_fill
+    E = corners.shape[1]
+    out = np.zeros((E, 6), dtype=np.float32)
+    ca, pa = PtrArray(corners.astype(np.int32)), PtrArray(_f32(points))
+    fn(c_ptrdiff(E), ca.p, pa.p, _ptr(out))
+    return out
+
+
+def adjugate_fill(corners, points, use_ref=False):
+    L = ref() if use_ref else lib()
+    fn = L.ref_hex8_adjugate_and_det_fill if use_ref else L.or_hex8_adjugate_and_det_fill
+    E = corners.shape[1]
+    adj = np.zeros((E, 9), dtype=np.float32)
+    det = np.zeros(E, dtype=np.float32)
+    ca, pa = PtrArray(corners.astype(np.int32)), PtrArray(_f32(points))
+    fn(c_ptrdiff(E), ca.p, pa.p, _ptr(adj), _ptr(det))
+    return adj, det
+
+
+def laplacian_matrix(fff6, use_ref=False):
+    A = np.zeros(64)
+    f = _f64(fff6)
+    if use_ref:
+        ref().ref_hex8_laplacian_matrix_fff_integral(_ptr(f), _ptr(A))
+    else:
+        lib().or_hex8_laplacian_matrix(_ptr(f), _ptr(A))
+    return A.reshape(8, 8)
+
+
+def elasticity_matrix(mu, lam, adj9, det, use_ref=False):
+    K = np.zeros(576)
+    a = _f64(adj9)
+    if use_ref:
+        ref().ref_hex8_linear_elasticity_matrix(c_double(mu), c_double(lam), _ptr(a), c_double(det), _ptr(K))
+    else:
+        lib().or_hex8_linear_elasticity_matrix(c_double(mu), c_double(lam), _ptr(a), c_double(det), _ptr(K))
+    return K.reshape(24, 24)
+
+
+def sshex8_laplacian_apply(L, elements, fff_aos, u, out=None, use_ref=False):
+    """values += A u for the affine sshex8 Laplacian (float32 AoS FFF)."""
+    E = elements.shape[1]
+    u = _f64(u)
+    out = np.zeros_like(u) if out is None else out
+    ea = PtrArray(elements.astype(np.int32))
+    f = _f32(fff_aos)
+    if use_ref:
+        ref().affine_sshex8_laplacian_stencil_apply_fff(c_int(L), c_ptrdiff(E), ea.p, _ptr(f), _ptr(u), _ptr(out))
+    else:
+        lib().or_sshex8_laplacian_apply(c_int(L), c_ptrdiff(E), ea.p, _ptr(f), _ptr(u), _ptr(out))
+    return out
+
+
+def hex8_laplacian_apply(elements, fff_aos, u, out=None, use_ref=False):
+    E = elements.shape[1]
+    u = _f64(u)
+    out = np.zeros_like(u) if out is None else out
+    ea = PtrArray(elements.astype(np.int32))
+    f = _f32(fff_aos)
+    if use_ref:
+        ref().hex8_laplacian_apply_opt(c_ptrdiff(E), ea.p, _ptr(f), _ptr(u), _ptr(out))
+    else:
+        lib().or_hex8_laplacian_apply(c_ptrdiff(E), ea.p, _ptr(f), _ptr(u), _ptr(out))
+    return out
+
+
+def laplacian_diag(L, elements, fff_aos, n, points=None, use_ref=False):
+    """Operator diagonal.  L == 0 means plain hex8 (hex8 corner order)."""
+    E = elements.shape[1]
+    out = np.zeros(n)
+    ea = PtrArray(elements.astype(np.int32))
+    if use_ref:
+        pa = PtrArray(_f32(points))
+        if L == 0:
+            ref().hex8_laplacian_diag(c_ptrdiff(E), c_ptrdiff(n), ea.p, pa.p, _ptr(out))
+        else:
+            ref().affine_sshex8_laplacian_diag(c_int(L), c_ptrdiff(E), ea.p, pa.p, _ptr(out))
+    else:
+        lib().or_laplacian_diag(c_int(L), c_ptrdiff(E), ea.p, _ptr(_f32(fff_aos)), _ptr(out))
+    return out
+
+
+def linear_elasticity_apply(L, elements, adj_aos, det, mu, lam, u, out=None, use_ref=False):
+    """out += K u (interleaved xyz).  L == 0 means plain hex8 (hex8 corner order)."""
+    E = elements.shape[1]
+    u = _f64(u)
+    out = np.zeros_like(u) if out is None else out
+    ea = PtrArray(elements.astype(np.int32))
+    a, d = _f32(adj_aos), _f32(det)
+    if use_ref:
+        if L == 0:
+            raise NotImplementedError
+        ref().affine_sshex8_linear_elasticity_apply_macro_adjugate(
+            c_int(L), c_ptrdiff(E), c_ptrdiff(u.size // 3), ea.p, c_void_p(0), _ptr(a), _ptr(d), c_double(mu),
+            c_double(lam), c_ptrdiff(3), C.c_void_p(u.ctypes.data), C.c_void_p(u.ctypes.data + 8),
+            C.c_void_p(u.ctypes.data + 16), c_ptrdiff(3), C.c_void_p(out.ctypes.data),
+            C.c_void_p(out.ctypes.data + 8), C.c_void_p(out.ctypes.data + 16))
+    else:
+        lib().or_linear_elasticity_apply(c_int(L), c_ptrdiff(E), ea.p, _ptr(a), _ptr(d), c_double(mu), c_double(lam),
+                                         _ptr(u), _ptr(out))
+    return out
+
+
+def linear_elasticity_block_diag(L, elements, adj_aos, det, mu, lam, n_nodes):
+    E = elements.shape[1]
+    d3 = np.zeros(3 * n_nodes)
+    b6 = np.zeros(6 * n_nodes)
+    ea = PtrArray(elements.astype(np.int32))
+    lib().or_linear_elasticity_block_diag_sym(c_int(L), c_ptrdiff(E), ea.p, _ptr(_f32(adj_aos)), _ptr(_f32(det)),
+                                             c_double(mu), c_double(lam), _ptr(d3), _ptr(b6))
+    return d3, b6
+
+
+def ref_linear_elasticity_diag(L, elements, points, mu, lam, n_nodes):
+    E = elements.shape[1]
+    out = np.zeros(3 * n_nodes)
+    ea, pa = PtrArray(elements.astype(np.int32)), PtrArray(_f32(points))
+    b = out.ctypes.data
+    ref().affine_sshex8_linear_elasticity_diag(c_int(L), c_ptrdiff(E), c_ptrdiff(n_nodes), ea.p, pa.p, c_double(mu),
+                                               c_double(lam), c_ptrdiff(3), c_void_p(b), c_void_p(b + 8),
+                                               c_void_p(b + 16))
+    return out
+
+
+def ref_linear_elasticity_block_diag(L, elements, points, mu, lam, n_nodes):
+    E = elements.shape[1]
+    out = np.zeros(6 * n_nodes)
+    ea, pa = PtrArray(elements.astype(np.int32)), PtrArray(_f32(points))
+    b = out.ctypes.data
+    ref().affine_sshex8_linear_elasticity_block_diag_sym(
+        c_int(L), c_ptrdiff(E), c_ptrdiff(n_nodes), ea.p, pa.p, c_double(mu), c_double(lam), c_ptrdiff(6),
+        *[c_void_p(b + 8 * k) for k in range(6)])
+    return out
+
+
+def incidence_count(L, elements, n, use_ref=False):
+    E = elements.shape[1]
+    out = np.zeros(n, dtype=np.uint16)
+    ea = PtrArray(elements.astype(np.int32))
+    if use_ref:
+        ref().sshex8_element_node_incidence_count(c_int(L), c_int(1), c_ptrdiff(E), ea.p, _ptr(out))
+    else:
+        lib().or_incidence_count(c_int(L), c_ptrdiff(E), ea.p, _ptr(out))
+    return out
+
+
+def prolongate(from_level, from_elements, to_level, to_elements, vec, x_coarse, n_fine, use_ref=False):
+    E = to_elements.shape[1]
+    out = np.zeros(n_fine * vec)
+    fa, ta = PtrArray(from_elements.astype(np.int32)), PtrArray(to_elements.astype(np.int32))
+    xc = _f64(x_coarse)
+    if use_ref:
+        if from_level == 1:
+            ref().sshex8_hierarchical_prolongation(c_int(to_level), c_ptrdiff(E), ta.p, c_int(vec), _ptr(xc), _ptr(out))
+        else:
+            ref().sshex8_prolongate(c_ptrdiff(E), c_int(from_level), c_int(1), fa.p, c_int(to_level), c_int(1), ta.p,
+                                    c_int(vec), _ptr(xc), _ptr(out))
+    else:
+        rc = lib().or_sshex8_prolongate(c_ptrdiff(E), c_int(from_level), fa.p, c_int(to_level), ta.p, c_int(vec),
+                                        _ptr(xc), _ptr(out))
+        assert rc == 0
+    return out
+
+
+def restrict(from_level, from_elements, count, to_level, to_elements, vec, x_fine, n_coarse, use_ref=False):
+    E = from_elements.shape[1]
+    out = np.zeros(n_coarse * vec)
+    fa, ta = PtrArray(from_elements.astype(np.int32)), PtrArray(to_elements.astype(np.int32))
+    xf = _f64(x_fine)
+    cnt = np.ascontiguousarray(count, dtype=np.uint16)
+    if use_ref:
+        if to_level == 1:
+            ref().sshex8_hierarchical_restriction(c_int(from_level), c_ptrdiff(E), fa.p, _ptr(cnt), c_int(vec),
+                                                  _ptr(xf), _ptr(out))
+        else:
+            ref().sshex8_restrict(c_ptrdiff(E), c_int(from_level), c_int(1), fa.p, _ptr(cnt), c_int(to_level), c_int(1),
+                                  ta.p, c_int(vec), _ptr(xf), _ptr(out))
+    else:
+        rc = lib().or_sshex8_restrict(c_ptrdiff(E), c_int(from_level), fa.p, _ptr(cnt), c_int(to_level), ta.p,
+                                      c_int(vec), _ptr(xf), _ptr(out))
+        assert rc == 0
+    return out
+
+
+def crs_sym_spmv(rowptr, colidx, diag, offdiag, x):
+    n = diag.size
+    y = np.zeros(n)
+    lib().or_crs_sym_spmv(c_ptrdiff(n), _ptr(np.ascontiguousarray(rowptr, np.int32)),
+                          _ptr(np.ascontiguousarray(colidx, np.int32)), _ptr(_f64(diag)), _ptr(_f64(offdiag)),
+                          _ptr(_f64(x)), _ptr(y))
+    return y
+
+
+def bsr_sym_spmv(bs, rowptr, colidx, diag_sym, offdiag, x):
+    nb = rowptr.size - 1
+    y = np.zeros(nb * bs)
+    lib().or_bsr_sym_spmv(c_ptrdiff(nb), c_int(bs), _ptr(np.ascontiguousarray(rowptr, np.int32)),
+                          _ptr(np.ascontiguousarray(colidx, np.int32)), _ptr(_f64(diag_sym)), _ptr(_f64(offdiag)),
+                          _ptr(_f64(x)), _ptr(y))
+    return y
+
+
+def hex8_laplacian_crs_sym(elements, fff_aos, rowptr, colidx, n, use_ref=False, points=None):
+    E = elements.shape[1]
+    diag = np.zeros(n)
+    off = np.zeros(colidx.size)
+    ea = PtrArray(elements.astype(np.int32))
+    rp, ci = np.ascontiguousarray(rowptr, np.int32), np.ascontiguousarray(colidx, np.int32)
+    if use_ref:
+        pa = PtrArray(_f32(points))
+        ref().hex8_laplacian_crs_sym(c_ptrdiff(E), c_ptrdiff(n), ea.p, pa.p, _ptr(rp), _ptr(ci), _ptr(diag), _ptr(off))
+    else:
+        lib().or_hex8_laplacian_crs_sym(c_ptrdiff(E), ea.p, _ptr(_f32(fff_aos)), _ptr(rp), _ptr(ci), _ptr(diag),
+                                        _ptr(off))
+    return diag, off

@@ -1,0 +1,98 @@
+"""Build recipes for the CPU oracle (test infrastructure only).
+
+* ``build_oracle()`` compiles the plain-C restatement ``oracle/src/oracle.c``
+  into ``oracle/_build/liboracle.so`` (works on any host with gcc + OpenMP).
+* ``build_ref()`` compiles the reference's own CPU operator sources, read in
+  place from the reference tree (never copied), together with the small type
+  shim in ``oracle/shim`` and the wrapper ``oracle/ref/ref_extras.cpp`` into
+  ``oracle/_ref/libsfem_ref.so``.  It is skipped when the reference tree is
+  absent (e.g. on a machine that only runs the tests).
+"""
+
+from __future__ import annotations
+
+import os
+import subprocess
+from concurrent.futures import ThreadPoolExecutor
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+REF_ROOT = Path(os.environ.get("SFEM_REFERENCE_ROOT", "/root/reference"))
+
+ORACLE_LIB = HERE / "_build" / "liboracle.so"
+REF_LIB = HERE / "_ref" / "libsfem_ref.so"
+
+# reference sources on the operator path (read in place)
+REF_SOURCES = [
+    "operators/hex8/hex8_laplacian.cpp",
+    "operators/hex8/hex8_fff.cpp",
+    "operators/sshex8/sshex8_laplacian.cpp",
+    "operators/sshex8/sshex8_interpolate.cpp",
+    "operators/sshex8/sshex8_linear_elasticity.cpp",
+    "operators/hex8/hex8_linear_elasticity.cpp",
+]
+REF_INCLUDES = [
+    "base",
+    "operators",
+    "operators/hex8",
+    "operators/sshex8",
+    "operators/stencil",
+    "operators/tet4",
+    "operators/beam2",
+    "algebra",
+    "algebra/openmp",
+    "frontend/ops/generated",
+]
+
+
+def _run(cmd):
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("command failed: " + " ".join(cmd) + "\n" + r.stdout + r.stderr)
+
+
+def _stale(target: Path, sources) -> bool:
+    if not target.exists():
+        return True
+    t = target.stat().st_mtime
+    return any(Path(s).stat().st_mtime > t for s in sources)
+
+
+def build_oracle(force: bool = False) -> Path:
+    srcs = [HERE / "src" / "oracle.c"]
+    if force or _stale(ORACLE_LIB, srcs):
+        ORACLE_LIB.parent.mkdir(parents=True, exist_ok=True)
+        _run(["gcc", "-O2", "-fopenmp", "-fPIC", "-shared", "-o", str(ORACLE_LIB)] + [str(s) for s in srcs] + ["-lm"])
+    return ORACLE_LIB
+
+
+def reference_available() -> bool:
+    return (REF_ROOT / "operators" / "sshex8" / "sshex8_laplacian.cpp").exists()
+
+
+def build_ref(force: bool = False):
+    if not reference_available():
+        return None
+    srcs = [REF_ROOT / s for s in REF_SOURCES] + [HERE / "ref" / "ref_extras.cpp"]
+    if not (force or _stale(REF_LIB, srcs)):
+        return REF_LIB
+    objdir = HERE / "_ref" / "obj"
+    objdir.mkdir(parents=True, exist_ok=True)
+    inc = ["-I" + str(HERE / "shim")] + ["-I" + str(REF_ROOT / d) for d in REF_INCLUDES]
+    flags = ["g++", "-std=c++17", "-O2", "-fopenmp", "-fPIC", "-DNDEBUG", "-w"] + inc
+
+    def compile_one(src: Path):
+        obj = objdir / (src.stem + ".o")
+        if force or _stale(obj, [src]):
+            _run(flags + ["-c", str(src), "-o", str(obj)])
+        return obj
+
+    with ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 2)) as ex:
+        objs = list(ex.map(compile_one, srcs))
+    _run(["g++", "-shared", "-fopenmp", "-o", str(REF_LIB)] + [str(o) for o in objs])
+    return REF_LIB
+
+
+if __name__ == "__main__":
+    print(build_oracle(force=True))
+    print(build_ref(force=True))

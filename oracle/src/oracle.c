@@ -1,0 +1,589 @@
+/*
+ * CPU oracle: a plain-C restatement of the reference's (zulianp/sfem) CPU
+ * algorithms on the matrix-free operator path.  TEST INFRASTRUCTURE ONLY:
+ * the parity tests, smoke() and bench.py's CPU-baseline leg are the only
+ * users; the product never links or calls this file.
+ *
+ * Conventions follow the reference's CPU path:
+ *   real_t = double (vectors, accumulation), geom_t = jacobian_t = float
+ *   (coordinates and cached geometry), idx_t = int32 (cmake/SFEMNumbers.cmake:5-14);
+ *   connectivity is SoA elements[v][e]; the CPU FFF / adjugate caches are AoS
+ *   (fff[e*6+d], adj[e*9+d]) as in operators/hex8/hex8_fff.cpp:31-33.
+ *
+ * Element matrices are derived here from the tensor-product structure of the
+ * Q1 basis on [0,1]^3 (exact integration of the affine-element bilinear
+ * forms); the reference uses generated closed forms with the same values.
+ * The oracle is pinned against the reference's own compiled sources by the
+ * CPU test-suite (oracle/_ref, built from the reference tree).
+ */
+#include <math.h>
+#include <stddef.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+typedef int32_t idx_t;
+typedef float geom_t;
+typedef float jacobian_t;
+
+/* standard hex8 corner order (operators/sshex8/sshex8.hpp:53-62) */
+static const int C8[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0}, {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
+
+static inline int lidx(int L, int x, int y, int z) { return z * (L + 1) * (L + 1) + y * (L + 1) + x; }
+
+static inline void atomic_add(double *p, double v) {
+#pragma omp atomic update
+    *p += v;
+}
+
+/* ------------------------------------------------------------------------ */
+/* 1D integrals of the linear basis psi0 = 1-t, psi1 = t on [0,1]           */
+/* ------------------------------------------------------------------------ */
+static inline double m1(int a, int b) { return a == b ? 1.0 / 3.0 : 1.0 / 6.0; }  /* int psi_a psi_b   */
+static inline double k1(int a, int b) { return a == b ? 1.0 : -1.0; }             /* int psi'_a psi'_b */
+static inline double g1(int a, int b) { (void)b; return a ? 0.5 : -0.5; }         /* int psi'_a psi_b  */
+
+/* int d_p phi_c d_q phi_e over the unit cube (p, q in 0..2) */
+static double grad_integral(int c, int e, int p, int q) {
+    double r = 1.0;
+    for (int d = 0; d < 3; d++) {
+        const int a = C8[c][d], b = C8[e][d];
+        if (d == p && d == q)
+            r *= k1(a, b);
+        else if (d == p)
+            r *= g1(a, b);
+        else if (d == q)
+            r *= g1(b, a);
+        else
+            r *= m1(a, b);
+    }
+    return r;
+}
+
+static double I_table[8][8][3][3];
+static int I_ready = 0;
+static void ensure_tables(void) {
+    if (I_ready) return;
+#pragma omp critical(oracle_tables)
+    {
+        if (!I_ready) {
+            for (int c = 0; c < 8; c++)
+                for (int e = 0; e < 8; e++)
+                    for (int p = 0; p < 3; p++)
+                        for (int q = 0; q < 3; q++) I_table[c][e][p][q] = grad_integral(c, e, p, q);
+            I_ready = 1;
+        }
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Geometry                                                                 */
+/* ------------------------------------------------------------------------ */
+
+/* Jacobian J[i][p] = d x_i / d xi_p of the trilinear map at (qx,qy,qz).
+ * The reference evaluates it at the element centre (hex8_inline_cpu.hpp:13-73, :90-150). */
+static void hex8_jacobian(const double *x, const double *y, const double *z, double qx, double qy, double qz,
+                          double J[3][3]) {
+    const double q[3] = {qx, qy, qz};
+    const double *X[3] = {x, y, z};
+    for (int i = 0; i < 3; i++)
+        for (int p = 0; p < 3; p++) J[i][p] = 0;
+    for (int c = 0; c < 8; c++) {
+        double w[3], dw[3];
+        for (int d = 0; d < 3; d++) {
+            w[d] = C8[c][d] ? q[d] : 1 - q[d];
+            dw[d] = C8[c][d] ? 1.0 : -1.0;
+        }
+        const double dphi[3] = {dw[0] * w[1] * w[2], w[0] * dw[1] * w[2], w[0] * w[1] * dw[2]};
+        for (int i = 0; i < 3; i++)
+            for (int p = 0; p < 3; p++) J[i][p] += X[i][c] * dphi[p];
+    }
+}
+
+/* adj = det(J) J^{-1} (row-major), det = det(J) */
+static void adjugate_det(const double J[3][3], double adj[9], double *det) {
+    adj[0] = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+    adj[1] = J[0][2] * J[2][1] - J[0][1] * J[2][2];
+    adj[2] = J[0][1] * J[1][2] - J[0][2] * J[1][1];
+    adj[3] = J[1][2] * J[2][0] - J[1][0] * J[2][2];
+    adj[4] = J[0][0] * J[2][2] - J[0][2] * J[2][0];
+    adj[5] = J[0][2] * J[1][0] - J[0][0] * J[1][2];
+    adj[6] = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+    adj[7] = J[0][1] * J[2][0] - J[0][0] * J[2][1];
+    adj[8] = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+    *det = J[0][0] * adj[0] + J[0][1] * adj[3] + J[0][2] * adj[6];
+}
+
+/* FFF = det(J) J^{-1} J^{-T}, symmetric, stored (00,01,02,11,12,22)
+ * (operators/hex8/hex8_inline_cpu.hpp:13-73). */
+static void fff_from_jacobian(const double J[3][3], double fff[6]) {
+    double adj[9], det;
+    adjugate_det(J, adj, &det);
+    /* J^{-1} = adj/det ;  FFF = det * Jinv Jinv^T = (adj adj^T) / det */
+    double G[3][3];
+    for (int p = 0; p < 3; p++)
+        for (int q = 0; q < 3; q++) {
+            double s = 0;
+            for (int k = 0; k < 3; k++) s += adj[3 * p + k] * adj[3 * q + k];
+            G[p][q] = s / det;
+        }
+    fff[0] = G[0][0];
+    fff[1] = G[0][1];
+    fff[2] = G[0][2];
+    fff[3] = G[1][1];
+    fff[4] = G[1][2];
+    fff[5] = G[2][2];
+}
+
+static void gather_corners(ptrdiff_t e, idx_t **corners, geom_t **points, double x[8], double y[8], double z[8]) {
+    for (int v = 0; v < 8; v++) {
+        const idx_t n = corners[v][e];
+        x[v] = points[0][n];
+        y[v] = points[1][n];
+        z[v] = points[2][n];
+    }
+}
+
+/* hex8_fff_fill (operators/hex8/hex8_fff.cpp:5-37): corners in hex8 order. */
+int or_hex8_fff_fill(ptrdiff_t nelements, idx_t **corners, geom_t **points, jacobian_t *fff) {
+#pragma omp parallel for
+    for (ptrdiff_t e = 0; e < nelements; e++) {
+        double x[8], y[8], z[8], J[3][3], f[6];
+        gather_corners(e, corners, points, x, y, z);
+        hex8_jacobian(x, y, z, 0.5, 0.5, 0.5, J);
+        fff_from_jacobian(J, f);
+        for (int d = 0; d < 6; d++) fff[e * 6 + d] = (jacobian_t)f[d];
+    }
+    return 0;
+}
+
+/* macro adjugate + determinant cache (hex8_adjugate_and_det at the centre,
+ * operators/hex8/hex8_inline_cpu.hpp:90; frontend/ops/sfem_LinearElasticity.cpp:252-289). */
+int or_hex8_adjugate_and_det_fill(ptrdiff_t nelements, idx_t **corners, geom_t **points, jacobian_t *adjugate,
+                                  jacobian_t *determinant) {
+#pragma omp parallel for
+    for (ptrdiff_t e = 0; e < nelements; e++) {
+        double x[8], y[8], z[8], J[3][3], adj[9], det;
+        gather_corners(e, corners, points, x, y, z);
+        hex8_jacobian(x, y, z, 0.5, 0.5, 0.5, J);
+        adjugate_det(J, adj, &det);
+        for (int d = 0; d < 9; d++) adjugate[e * 9 + d] = (jacobian_t)adj[d];
+        determinant[e] = (jacobian_t)det;
+    }
+    return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Laplacian                                                                */
+/* ------------------------------------------------------------------------ */
+
+/* 8x8 Q1 Laplacian element matrix from the FFF of the (sub-)element
+ * (operators/hex8/hex8_laplacian_inline_cpu.hpp:213). */
+void or_hex8_laplacian_matrix(const double fff[6], double A[64]) {
+    ensure_tables();
+    const double F[3][3] = {{fff[0], fff[1], fff[2]}, {fff[1], fff[3], fff[4]}, {fff[2], fff[4], fff[5]}};
+    for (int c = 0; c < 8; c++)
+        for (int e = 0; e < 8; e++) {
+            double s = 0;
+            for (int p = 0; p < 3; p++)
+                for (int q = 0; q < 3; q++) s += F[p][q] * I_table[c][e][p][q];
+            A[c * 8 + e] = s;
+        }
+}
+
+static void sshex8_micro_nodes(int L, int xi, int yi, int zi, int lev[8]) {
+    for (int c = 0; c < 8; c++) lev[c] = lidx(L, xi + C8[c][0], yi + C8[c][1], zi + C8[c][2]);
+}
+
+/* Affine sshex8 Laplacian apply, values += A u.
+ * Same operator as affine_sshex8_laplacian_stencil_apply_fff
+ * (operators/sshex8/sshex8_laplacian.cpp:698-769): one metric per macro
+ * element, sub-FFF = FFF / L (:19-28), applied micro element by micro element
+ * as sshex8_apply_element_matrix (operators/sshex8/sshex8.hpp:44-86). */
+int or_sshex8_laplacian_apply(int L, ptrdiff_t nelements, idx_t **elements, const jacobian_t *fff, const double *u,
+                              double *values) {
+    const int nxe = (L + 1) * (L + 1) * (L + 1);
+#pragma omp parallel
+    {
+        double *eu = (double *)malloc(nxe * sizeof(double));
+        double *ev = (double *)malloc(nxe * sizeof(double));
+        idx_t *idx = (idx_t *)malloc(nxe * sizeof(idx_t));
+#pragma omp for
+        for (ptrdiff_t e = 0; e < nelements; e++) {
+            double sub[6], A[64];
+            const double h = 1.0 / L;
+            for (int d = 0; d < 6; d++) sub[d] = (double)fff[e * 6 + d] * h;
+            or_hex8_laplacian_matrix(sub, A);
+            for (int v = 0; v < nxe; v++) {
+                idx[v] = elements[v][e];
+                eu[v] = u[idx[v]];
+                ev[v] = 0;
+            }
+            for (int zi = 0; zi < L; zi++)
+                for (int yi = 0; yi < L; yi++)
+                    for (int xi = 0; xi < L; xi++) {
+                        int lev[8];
+                        sshex8_micro_nodes(L, xi, yi, zi, lev);
+                        for (int i = 0; i < 8; i++) {
+                            double acc = 0;
+                            for (int j = 0; j < 8; j++) acc += A[i * 8 + j] * eu[lev[j]];
+                            ev[lev[i]] += acc;
+                        }
+                    }
+            for (int v = 0; v < nxe; v++) atomic_add(&values[idx[v]], ev[v]);
+        }
+        free(eu);
+        free(ev);
+        free(idx);
+    }
+    return 0;
+}
+
+/* hex8_laplacian_apply_opt (operators/hex8/hex8_laplacian.cpp:309-345);
+ * elements in hex8 corner order. */
+int or_hex8_laplacian_apply(ptrdiff_t nelements, idx_t **elements, const jacobian_t *fff, const double *u,
+                            double *values) {
+#pragma omp parallel for
+    for (ptrdiff_t e = 0; e < nelements; e++) {
+        double f[6], A[64], eu[8];
+        for (int d = 0; d < 6; d++) f[d] = fff[e * 6 + d];
+        or_hex8_laplacian_matrix(f, A);
+        for (int v = 0; v < 8; v++) eu[v] = u[elements[v][e]];
+        for (int i = 0; i < 8; i++) {
+            double acc = 0;
+            for (int j = 0; j < 8; j++) acc += A[i * 8 + j] * eu[j];
+            atomic_add(&values[elements[i][e]], acc);
+        }
+    }
+    return 0;
+}
+
+/* affine_sshex8_laplacian_diag (operators/sshex8/sshex8_laplacian.cpp:333-435)
+ * and hex8_laplacian_diag (operators/hex8/hex8_laplacian.cpp:262-307), from
+ * the cached FFF.  L == 0 selects the plain hex8 corner ordering. */
+int or_laplacian_diag(int L, ptrdiff_t nelements, idx_t **elements, const jacobian_t *fff, double *diag) {
+    const int Lm = L > 0 ? L : 1;
+#pragma omp parallel for
+    for (ptrdiff_t e = 0; e < nelements; e++) {
+        double sub[6], A[64];
+        for (int d = 0; d < 6; d++) sub[d] = (double)fff[e * 6 + d] / Lm;
+        or_hex8_laplacian_matrix(sub, A);
+        if (L == 0) {
+            for (int i = 0; i < 8; i++) atomic_add(&diag[elements[i][e]], A[i * 9]);
+            continue;
+        }
+        for (int zi = 0; zi < L; zi++)
+            for (int yi = 0; yi < L; yi++)
+                for (int xi = 0; xi < L; xi++) {
+                    int lev[8];
+                    sshex8_micro_nodes(L, xi, yi, zi, lev);
+                    for (int i = 0; i < 8; i++) atomic_add(&diag[elements[lev[i]][e]], A[i * 9]);
+                }
+    }
+    return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Linear elasticity                                                        */
+/* ------------------------------------------------------------------------ */
+
+/* 24x24 element matrix, row/col index = component*8 + node, from the
+ * (sub-)adjugate and determinant (operators/hex8/hex8_linear_elasticity_inline_cpu.hpp:207).
+ * K[(a,i),(b,j)] = int mu (grad phi_a . grad phi_b) delta_ij + mu d_j phi_a d_i phi_b
+ *                      + lambda d_i phi_a d_j phi_b  dx,  grad phi = adj^T grad_ref phi / det. */
+void or_hex8_linear_elasticity_matrix(double mu, double lambda, const double adj[9], double det, double K[576]) {
+    ensure_tables();
+    double AA[3][3];
+    for (int p = 0; p < 3; p++)
+        for (int q = 0; q < 3; q++) {
+            double s = 0;
+            for (int k = 0; k < 3; k++) s += adj[3 * p + k] * adj[3 * q + k];
+            AA[p][q] = s;
+        }
+    const double inv_det = 1.0 / det;
+    for (int i = 0; i < 3; i++)
+        for (int a = 0; a < 8; a++)
+            for (int j = 0; j < 3; j++)
+                for (int b = 0; b < 8; b++) {
+                    double s = 0;
+                    for (int p = 0; p < 3; p++)
+                        for (int q = 0; q < 3; q++) {
+                            const double I = I_table[a][b][p][q];
+                            double w = mu * adj[3 * p + j] * adj[3 * q + i] + lambda * adj[3 * p + i] * adj[3 * q + j];
+                            if (i == j) w += mu * AA[p][q];
+                            s += I * w;
+                        }
+                    K[(i * 8 + a) * 24 + (j * 8 + b)] = s * inv_det;
+                }
+}
+
+static void sub_adjugate(const jacobian_t *adjugate, const jacobian_t *determinant, ptrdiff_t e, int L, double adj[9],
+                         double *det) {
+    const double h = 1.0 / L;
+    for (int d = 0; d < 9; d++) adj[d] = (double)adjugate[e * 9 + d] * (h * h);
+    *det = (double)determinant[e] * (h * h * h);
+}
+
+/* affine_sshex8_linear_elasticity_apply_macro_adjugate (operators/sshex8/sshex8_linear_elasticity.cpp:275-424):
+ * sub-adjugate = adj h^2, sub-det = det h^3 (operators/sshex8/sshex8.hpp:26-42);
+ * u and out are interleaved with stride 3 (ux = u, uy = u+1, uz = u+2).
+ * L == 0 selects a plain hex8 mesh (affine_hex8_linear_elasticity_apply_adjugate,
+ * operators/hex8/hex8_linear_elasticity.cpp:458). */
+int or_linear_elasticity_apply(int L, ptrdiff_t nelements, idx_t **elements, const jacobian_t *adjugate,
+                               const jacobian_t *determinant, double mu, double lambda, const double *u, double *out) {
+    const int Lm = L > 0 ? L : 1;
+    const int nxe = (Lm + 1) * (Lm + 1) * (Lm + 1);
+#pragma omp parallel
+    {
+        double *eu = (double *)malloc(3 * nxe * sizeof(double));
+        double *ev = (double *)malloc(3 * nxe * sizeof(double));
+        idx_t *idx = (idx_t *)malloc(nxe * sizeof(idx_t));
+        double *K = (double *)malloc(576 * sizeof(double));
+#pragma omp for
+        for (ptrdiff_t e = 0; e < nelements; e++) {
+            double adj[9], det;
+            sub_adjugate(adjugate, determinant, e, Lm, adj, &det);
+            or_hex8_linear_elasticity_matrix(mu, lambda, adj, det, K);
+            if (L == 0) {
+                double ue[24], oe[24];
+                for (int v = 0; v < 8; v++)
+                    for (int d = 0; d < 3; d++) ue[d * 8 + v] = u[3 * (ptrdiff_t)elements[v][e] + d];
+                for (int i = 0; i < 24; i++) {
+                    double s = 0;
+                    for (int j = 0; j < 24; j++) s += K[i * 24 + j] * ue[j];
+                    oe[i] = s;
+                }
+                for (int v = 0; v < 8; v++)
+                    for (int d = 0; d < 3; d++) atomic_add(&out[3 * (ptrdiff_t)elements[v][e] + d], oe[d * 8 + v]);
+                continue;
+            }
+            for (int v = 0; v < nxe; v++) {
+                idx[v] = elements[v][e];
+                for (int d = 0; d < 3; d++) {
+                    eu[d * nxe + v] = u[3 * (ptrdiff_t)idx[v] + d];
+                    ev[d * nxe + v] = 0;
+                }
+            }
+            for (int zi = 0; zi < L; zi++)
+                for (int yi = 0; yi < L; yi++)
+                    for (int xi = 0; xi < L; xi++) {
+                        int lev[8];
+                        double ue[24];
+                        sshex8_micro_nodes(L, xi, yi, zi, lev);
+                        for (int d = 0; d < 3; d++)
+                            for (int v = 0; v < 8; v++) ue[d * 8 + v] = eu[d * nxe + lev[v]];
+                        for (int i = 0; i < 24; i++) {
+                            double s = 0;
+                            for (int j = 0; j < 24; j++) s += K[i * 24 + j] * ue[j];
+                            ev[(i / 8) * nxe + lev[i % 8]] += s;
+                        }
+                    }
+            for (int v = 0; v < nxe; v++)
+                for (int d = 0; d < 3; d++) atomic_add(&out[3 * (ptrdiff_t)idx[v] + d], ev[d * nxe + v]);
+        }
+        free(eu);
+        free(ev);
+        free(idx);
+        free(K);
+    }
+    return 0;
+}
+
+/* Diagonal (3 per node, interleaved) and symmetric 3x3 block diagonal
+ * (6 per node: 00,01,02,11,12,22, interleaved)
+ * (operators/sshex8/sshex8_linear_elasticity.cpp:971-1257). L == 0: plain hex8. */
+int or_linear_elasticity_block_diag_sym(int L, ptrdiff_t nelements, idx_t **elements, const jacobian_t *adjugate,
+                                        const jacobian_t *determinant, double mu, double lambda, double *diag3,
+                                        double *block6) {
+    const int Lm = L > 0 ? L : 1;
+    static const int bi[6] = {0, 0, 0, 1, 1, 2}, bj[6] = {0, 1, 2, 1, 2, 2};
+#pragma omp parallel
+    {
+        double *K = (double *)malloc(576 * sizeof(double));
+#pragma omp for
+        for (ptrdiff_t e = 0; e < nelements; e++) {
+            double adj[9], det;
+            sub_adjugate(adjugate, determinant, e, Lm, adj, &det);
+            or_hex8_linear_elasticity_matrix(mu, lambda, adj, det, K);
+            const int nmicro = L > 0 ? L * L * L : 1;
+            for (int m = 0; m < nmicro; m++) {
+                int lev[8];
+                if (L > 0) {
+                    const int xi = m % L, yi = (m / L) % L, zi = m / (L * L);
+                    sshex8_micro_nodes(L, xi, yi, zi, lev);
+                } else {
+                    for (int v = 0; v < 8; v++) lev[v] = v;
+                }
+                for (int a = 0; a < 8; a++) {
+                    const ptrdiff_t n = elements[lev[a]][e];
+                    if (diag3)
+                        for (int d = 0; d < 3; d++) atomic_add(&diag3[3 * n + d], K[(d * 8 + a) * 24 + d * 8 + a]);
+                    if (block6)
+                        for (int k = 0; k < 6; k++)
+                            atomic_add(&block6[6 * n + k], K[(bi[k] * 8 + a) * 24 + bj[k] * 8 + a]);
+                }
+            }
+        }
+        free(K);
+    }
+    return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Transfer operators                                                       */
+/* ------------------------------------------------------------------------ */
+
+/* sshex8_element_node_incidence_count (operators/sshex8/sshex8_interpolate.cpp:239-257) */
+int or_incidence_count(int L, ptrdiff_t nelements, idx_t **elements, uint16_t *count) {
+    const int nxe = (L + 1) * (L + 1) * (L + 1);
+    for (int v = 0; v < nxe; v++)
+        for (ptrdiff_t e = 0; e < nelements; e++) count[elements[v][e]]++;
+    return 0;
+}
+
+/* Nested prolongation, to = P from (overwrite), trilinear in each macro element
+ * (sshex8_prolongate, operators/sshex8/sshex8_interpolate.cpp:259-558; with
+ * from_level == 1 and the macro corners of to_elements this is
+ * sshex8_hierarchical_prolongation, :129-237).  vec_size components interleaved. */
+int or_sshex8_prolongate(ptrdiff_t nelements, int from_level, idx_t **from_elements, int to_level,
+                         idx_t **to_elements, int vec_size, const double *from, double *to) {
+    if (to_level % from_level) return 1;
+    const int s = to_level / from_level;
+#pragma omp parallel for
+    for (ptrdiff_t e = 0; e < nelements; e++) {
+        for (int zi = 0; zi <= to_level; zi++)
+            for (int yi = 0; yi <= to_level; yi++)
+                for (int xi = 0; xi <= to_level; xi++) {
+                    const int cx = xi / s < from_level ? xi / s : from_level - 1;
+                    const int cy = yi / s < from_level ? yi / s : from_level - 1;
+                    const int cz = zi / s < from_level ? zi / s : from_level - 1;
+                    const double tx = (double)(xi - cx * s) / s, ty = (double)(yi - cy * s) / s,
+                                 tz = (double)(zi - cz * s) / s;
+                    const ptrdiff_t gid = to_elements[lidx(to_level, xi, yi, zi)][e];
+                    for (int d = 0; d < vec_size; d++) {
+                        double acc = 0;
+                        for (int c = 0; c < 8; c++) {
+                            const double w = (C8[c][0] ? tx : 1 - tx) * (C8[c][1] ? ty : 1 - ty) * (C8[c][2] ? tz : 1 - tz);
+                            if (w == 0) continue;
+                            const ptrdiff_t src =
+                                    from_elements[lidx(from_level, cx + C8[c][0], cy + C8[c][1], cz + C8[c][2])][e];
+                            acc += w * from[src * vec_size + d];
+                        }
+                        to[gid * vec_size + d] = acc;
+                    }
+                }
+    }
+    return 0;
+}
+
+/* Restriction R = P^T with the fine input divided by the element-node incidence
+ * count (sshex8_restrict, operators/sshex8/sshex8_interpolate.cpp:633-760;
+ * sshex8_hierarchical_restriction, :12-127).  to += R from. */
+int or_sshex8_restrict(ptrdiff_t nelements, int from_level, idx_t **from_elements, const uint16_t *count,
+                       int to_level, idx_t **to_elements, int vec_size, const double *from, double *to) {
+    if (from_level % to_level) return 1;
+    const int s = from_level / to_level;
+#pragma omp parallel for
+    for (ptrdiff_t e = 0; e < nelements; e++) {
+        for (int zi = 0; zi <= from_level; zi++)
+            for (int yi = 0; yi <= from_level; yi++)
+                for (int xi = 0; xi <= from_level; xi++) {
+                    const int cx = xi / s < to_level ? xi / s : to_level - 1;
+                    const int cy = yi / s < to_level ? yi / s : to_level - 1;
+                    const int cz = zi / s < to_level ? zi / s : to_level - 1;
+                    const double tx = (double)(xi - cx * s) / s, ty = (double)(yi - cy * s) / s,
+                                 tz = (double)(zi - cz * s) / s;
+                    const ptrdiff_t gid = from_elements[lidx(from_level, xi, yi, zi)][e];
+                    for (int d = 0; d < vec_size; d++) {
+                        const double val = from[gid * vec_size + d] / count[gid];
+                        for (int c = 0; c < 8; c++) {
+                            const double w = (C8[c][0] ? tx : 1 - tx) * (C8[c][1] ? ty : 1 - ty) * (C8[c][2] ? tz : 1 - tz);
+                            if (w == 0) continue;
+                            const ptrdiff_t dst = to_elements[lidx(to_level, cx + C8[c][0], cy + C8[c][1], cz + C8[c][2])][e];
+                            atomic_add(&to[dst * vec_size + d], w * val);
+                        }
+                    }
+                }
+    }
+    return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Symmetric sparse formats                                                 */
+/* ------------------------------------------------------------------------ */
+
+/* y = (D + U + U^T) x with D the diagonal and U the strict upper triangle in
+ * CRS (CRSSymSpMV, algebra/sfem_crs_sym_SpMV.hpp:8-91).  y is overwritten. */
+int or_crs_sym_spmv(ptrdiff_t n, const idx_t *rowptr, const idx_t *colidx, const double *diag, const double *offdiag,
+                    const double *x, double *y) {
+    for (ptrdiff_t i = 0; i < n; i++) y[i] = diag[i] * x[i];
+    for (ptrdiff_t i = 0; i < n; i++)
+        for (idx_t k = rowptr[i]; k < rowptr[i + 1]; k++) {
+            const idx_t j = colidx[k];
+            y[i] += offdiag[k] * x[j];
+            y[j] += offdiag[k] * x[i];
+        }
+    return 0;
+}
+
+/* Symmetric block CRS, block size bs: diagonal blocks stored as the bs(bs+1)/2
+ * upper entries per row, off-diagonal blocks (strict upper) full bs*bs row-major
+ * (BCRSSymSpMV, algebra/sfem_bcrs_sym_SpMV.hpp:9-279; values are kept AoS here). */
+int or_bsr_sym_spmv(ptrdiff_t nb, int bs, const idx_t *rowptr, const idx_t *colidx, const double *diag_sym,
+                    const double *offdiag, const double *x, double *y) {
+    const int nsym = bs * (bs + 1) / 2;
+    for (ptrdiff_t i = 0; i < nb; i++) {
+        const double *D = &diag_sym[i * nsym];
+        int k = 0;
+        double Df[16];
+        for (int a = 0; a < bs; a++)
+            for (int b = a; b < bs; b++, k++) {
+                Df[a * bs + b] = D[k];
+                Df[b * bs + a] = D[k];
+            }
+        for (int a = 0; a < bs; a++) {
+            double s = 0;
+            for (int b = 0; b < bs; b++) s += Df[a * bs + b] * x[i * bs + b];
+            y[i * bs + a] = s;
+        }
+    }
+    for (ptrdiff_t i = 0; i < nb; i++)
+        for (idx_t k = rowptr[i]; k < rowptr[i + 1]; k++) {
+            const idx_t j = colidx[k];
+            const double *B = &offdiag[(ptrdiff_t)k * bs * bs];
+            for (int a = 0; a < bs; a++)
+                for (int b = 0; b < bs; b++) {
+                    y[i * bs + a] += B[a * bs + b] * x[j * bs + b];
+                    y[j * bs + b] += B[a * bs + b] * x[i * bs + a];
+                }
+        }
+    return 0;
+}
+
+/* Symmetric CRS assembly of the hex8 Laplacian from the FFF cache: diag and
+ * strict upper triangle on a given graph (hex8_laplacian_crs_sym,
+ * operators/hex8/hex8_laplacian.cpp:148-221).  rowptr/colidx hold only the
+ * strict upper part (col > row), sorted. */
+int or_hex8_laplacian_crs_sym(ptrdiff_t nelements, idx_t **elements, const jacobian_t *fff, const idx_t *rowptr,
+                              const idx_t *colidx, double *diag, double *offdiag) {
+#pragma omp parallel for
+    for (ptrdiff_t e = 0; e < nelements; e++) {
+        double f[6], A[64];
+        idx_t ev[8];
+        for (int d = 0; d < 6; d++) f[d] = fff[e * 6 + d];
+        or_hex8_laplacian_matrix(f, A);
+        for (int v = 0; v < 8; v++) ev[v] = elements[v][e];
+        for (int i = 0; i < 8; i++) {
+            atomic_add(&diag[ev[i]], A[i * 9]);
+            for (int j = 0; j < 8; j++) {
+                if (ev[j] <= ev[i]) continue;
+                for (idx_t k = rowptr[ev[i]]; k < rowptr[ev[i] + 1]; k++)
+                    if (colidx[k] == ev[j]) {
+                        atomic_add(&offdiag[k], A[i * 8 + j]);
+                        break;
+                    }
+            }
+        }
+    }
+    return 0;
+}

@@ -1,0 +1,368 @@
+// Matrix-free Laplacian on hex8 and semi-structured hex8 (sshex8) meshes, sm_103a.
+//
+// Operator (reference: affine_sshex8_laplacian_stencil_apply_fff,
+// operators/sshex8/sshex8_laplacian.cpp:698-769, and hex8_laplacian_apply_opt,
+// operators/hex8/hex8_laplacian.cpp:309-345): one metric (FFF, 6 floats) per
+// macro element, sub-metric FFF/L for each of the L^3 micro elements, element
+// matrix A = sum_m f_m W_m with the exact Q1 integrals W_m, y += A x.
+#include <cstdio>
+
+#include "common.cuh"
+#include "laplacian_kernels.cuh"
+
+namespace sfem_gb300 {
+
+// ------------------------------------------------------------------ geometry
+
+__device__ inline void hex8_center_jacobian(const double *x, const double *y, const double *z, double J[3][3]) {
+    // d x_i / d xi_p at (1/2,1/2,1/2) of the trilinear map
+    for (int i = 0; i < 3; i++)
+        for (int p = 0; p < 3; p++) J[i][p] = 0;
+    const double *X[3] = {x, y, z};
+#pragma unroll
+    for (int c = 0; c < 8; c++) {
+        const double dphi[3] = {(c8x(c) ? 0.25 : -0.25), (c8y(c) ? 0.25 : -0.25), (c8z(c) ? 0.25 : -0.25)};
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int p = 0; p < 3; p++) J[i][p] += X[i][c] * dphi[p];
+    }
+}
+
+__device__ inline double adjugate_det(const double J[3][3], double adj[9]) {
+    adj[0] = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+    adj[1] = J[0][2] * J[2][1] - J[0][1] * J[2][2];
+    adj[2] = J[0][1] * J[1][2] - J[0][2] * J[1][1];
+    adj[3] = J[1][2] * J[2][0] - J[1][0] * J[2][2];
+    adj[4] = J[0][0] * J[2][2] - J[0][2] * J[2][0];
+    adj[5] = J[0][2] * J[1][0] - J[0][0] * J[1][2];
+    adj[6] = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+    adj[7] = J[0][1] * J[2][0] - J[0][0] * J[2][1];
+    adj[8] = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+    return J[0][0] * adj[0] + J[0][1] * adj[3] + J[0][2] * adj[6];
+}
+
+__global__ void hex8_geometry_kernel(ptrdiff_t nelements, const idx_t *const *corners, const float *const *points,
+                                     ptrdiff_t stride, float *fff, float *adjugate, float *determinant) {
+    for (ptrdiff_t e = blockIdx.x * (ptrdiff_t)blockDim.x + threadIdx.x; e < nelements;
+         e += (ptrdiff_t)gridDim.x * blockDim.x) {
+        double x[8], y[8], z[8];
+#pragma unroll
+        for (int v = 0; v < 8; v++) {
+            const idx_t n = corners[v][e];
+            x[v] = points[0][n];
+            y[v] = points[1][n];
+            z[v] = points[2][n];
+        }
+        double J[3][3], adj[9];
+        hex8_center_jacobian(x, y, z, J);
+        const double det = adjugate_det(J, adj);
+        if (fff) {
+            double G[6];
+            const int pq[6][2] = {{0, 0}, {0, 1}, {0, 2}, {1, 1}, {1, 2}, {2, 2}};
+#pragma unroll
+            for (int m = 0; m < 6; m++) {
+                const int p = pq[m][0], q = pq[m][1];
+                G[m] = (adj[3 * p] * adj[3 * q] + adj[3 * p + 1] * adj[3 * q + 1] + adj[3 * p + 2] * adj[3 * q + 2]) / det;
+                fff[m * stride + e] = (float)G[m];
+            }
+        }
+        if (adjugate) {
+#pragma unroll
+            for (int d = 0; d < 9; d++) adjugate[d * stride + e] = (float)adj[d];
+            determinant[e] = (float)det;
+        }
+    }
+}
+
+// ------------------------------------------------------------------ tables
+
+__constant__ LapTable kLap = LapTable();
+__constant__ LapTableF kLapF = LapTableF();
+
+// ------------------------------------------------------------------ hex8 apply
+
+// One thread per element: coalesced SoA index / FFF loads, 8 gathers, 8 atomic scatters.
+template <typename T>
+__global__ void __launch_bounds__(128) hex8_laplacian_apply_kernel(ptrdiff_t nelements, const idx_t *const *elements,
+                                                                   ptrdiff_t fff_stride, const float *fff, const T *x,
+                                                                   T *y) {
+    for (ptrdiff_t e = blockIdx.x * (ptrdiff_t)blockDim.x + threadIdx.x; e < nelements;
+         e += (ptrdiff_t)gridDim.x * blockDim.x) {
+        idx_t ev[8];
+        T u[8], f[6];
+#pragma unroll
+        for (int v = 0; v < 8; v++) ev[v] = elements[v][e];
+#pragma unroll
+        for (int m = 0; m < 6; m++) f[m] = (T)fff[m * fff_stride + e];
+#pragma unroll
+        for (int v = 0; v < 8; v++) u[v] = x[ev[v]];
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+            T acc = 0;
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+                T a = 0;
+#pragma unroll
+                for (int m = 0; m < 6; m++) a += f[m] * lap_w<T>(i * 8 + j, m);
+                acc += a * u[j];
+            }
+            atomicAdd(&y[ev[i]], acc);
+        }
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(128) hex8_laplacian_diag_kernel(ptrdiff_t nelements, const idx_t *const *elements,
+                                                                  ptrdiff_t fff_stride, const float *fff, T *diag) {
+    for (ptrdiff_t e = blockIdx.x * (ptrdiff_t)blockDim.x + threadIdx.x; e < nelements;
+         e += (ptrdiff_t)gridDim.x * blockDim.x) {
+        T f[6];
+#pragma unroll
+        for (int m = 0; m < 6; m++) f[m] = (T)fff[m * fff_stride + e];
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+            T a = 0;
+#pragma unroll
+            for (int m = 0; m < 6; m++) a += f[m] * lap_w<T>(i * 9, m);
+            atomicAdd(&diag[elements[i][e]], a);
+        }
+    }
+}
+
+// ------------------------------------------------------------------ sshex8 apply
+
+// v1: one warp per macro element.  Lanes compute the element matrix entries
+// (A = sum_m (fff_m / L) W_m), gather the (L+1)^3 micro-grid values into shared
+// memory, apply the 8x8 element matrix per micro element with shared-memory
+// accumulation, then scatter: nodes strictly inside the macro element are owned
+// (plain read-modify-write), surface nodes are shared (atomicAdd).
+template <typename T, int L>
+__global__ void __launch_bounds__(128) sshex8_laplacian_apply_warp_kernel(ptrdiff_t nelements,
+                                                                          const idx_t *const *elements,
+                                                                          ptrdiff_t fff_stride, const float *fff,
+                                                                          const T *x, T *y) {
+    constexpr int N1 = L + 1;
+    constexpr int NXE = N1 * N1 * N1;
+    constexpr int NM = L * L * L;
+    constexpr int WPB = 4;
+    constexpr int NR = (NXE + 31) / 32;
+    __shared__ T xs[WPB][NXE];
+    __shared__ T ys[WPB][NXE];
+    __shared__ T As[WPB][64];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    T *xw = xs[warp];
+    T *yw = ys[warp];
+    T *Aw = As[warp];
+    const T h = T(1) / T(L);
+
+    for (ptrdiff_t e = (ptrdiff_t)blockIdx.x * WPB + warp; e < nelements; e += (ptrdiff_t)gridDim.x * WPB) {
+        T f = 0;
+        if (lane < 6) f = (T)fff[lane * fff_stride + e] * h;
+        T sub[6];
+#pragma unroll
+        for (int m = 0; m < 6; m++) sub[m] = __shfl_sync(0xffffffffu, f, m);
+#pragma unroll
+        for (int k = lane; k < 64; k += 32) {
+            T a = 0;
+#pragma unroll
+            for (int m = 0; m < 6; m++) a += sub[m] * lap_w<T>(k, m);
+            Aw[k] = a;
+        }
+
+        idx_t gi[NR];
+#pragma unroll
+        for (int r = 0; r < NR; r++) {
+            const int l = lane + 32 * r;
+            if (l < NXE) {
+                gi[r] = elements[l][e];
+                xw[l] = x[gi[r]];
+                yw[l] = 0;
+            }
+        }
+        __syncwarp();
+
+        for (int m = lane; m < NM; m += 32) {
+            const int xi = m % L, yi = (m / L) % L, zi = m / (L * L);
+            int v[8];
+            T u[8];
+#pragma unroll
+            for (int c = 0; c < 8; c++) {
+                v[c] = lidx(L, xi + c8x(c), yi + c8y(c), zi + c8z(c));
+                u[c] = xw[v[c]];
+            }
+#pragma unroll
+            for (int i = 0; i < 8; i++) {
+                T acc = 0;
+#pragma unroll
+                for (int j = 0; j < 8; j++) acc += Aw[i * 8 + j] * u[j];
+                atomicAdd(&yw[v[i]], acc);
+            }
+        }
+        __syncwarp();
+
+#pragma unroll
+        for (int r = 0; r < NR; r++) {
+            const int l = lane + 32 * r;
+            if (l < NXE) {
+                const int xi = l % N1, yi = (l / N1) % N1, zi = l / (N1 * N1);
+                const bool interior = xi > 0 && xi < L && yi > 0 && yi < L && zi > 0 && zi < L;
+                const T val = yw[l];
+                if (interior)
+                    y[gi[r]] += val;
+                else
+                    atomicAdd(&y[gi[r]], val);
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// Diagonal: node value = sum over the micro elements of this macro element that
+// contain it of A[a][a] (a = the node's corner in that micro element).
+template <typename T, int L>
+__global__ void __launch_bounds__(128) sshex8_laplacian_diag_kernel(ptrdiff_t nelements, const idx_t *const *elements,
+                                                                    ptrdiff_t fff_stride, const float *fff, T *diag) {
+    constexpr int N1 = L + 1;
+    constexpr int NXE = N1 * N1 * N1;
+    constexpr int WPB = 4;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const T h = T(1) / T(L);
+    for (ptrdiff_t e = (ptrdiff_t)blockIdx.x * WPB + warp; e < nelements; e += (ptrdiff_t)gridDim.x * WPB) {
+        T sub[6];
+#pragma unroll
+        for (int m = 0; m < 6; m++) sub[m] = (T)fff[m * fff_stride + e] * h;
+        T Ad[8];
+#pragma unroll
+        for (int a = 0; a < 8; a++) {
+            T s = 0;
+#pragma unroll
+            for (int m = 0; m < 6; m++) s += sub[m] * lap_w<T>(a * 9, m);
+            Ad[a] = s;
+        }
+        for (int l = lane; l < NXE; l += 32) {
+            const int xi = l % N1, yi = (l / N1) % N1, zi = l / (N1 * N1);
+            T s = 0;
+#pragma unroll
+            for (int a = 0; a < 8; a++) {
+                const bool ok = (c8x(a) ? xi > 0 : xi < L) && (c8y(a) ? yi > 0 : yi < L) && (c8z(a) ? zi > 0 : zi < L);
+                if (ok) s += Ad[a];
+            }
+            const bool interior = xi > 0 && xi < L && yi > 0 && yi < L && zi > 0 && zi < L;
+            const idx_t g = elements[l][e];
+            if (interior)
+                diag[g] += s;
+            else
+                atomicAdd(&diag[g], s);
+        }
+    }
+}
+
+// ------------------------------------------------------------------ dispatch
+
+template <typename T>
+static int laplacian_apply_tpl(int element_type, ptrdiff_t nelements, idx_t **elements, ptrdiff_t fff_stride,
+                               const float *fff, const T *x, T *y, cudaStream_t s) {
+    if (nelements <= 0) return SFEM_GB300_SUCCESS;
+    if (element_type == SFEM_GB300_HEX8) {
+        hex8_laplacian_apply_kernel<T><<<grid_for(nelements, 128), 128, 0, s>>>(nelements, elements, fff_stride, fff, x, y);
+        return check_launch("cu_laplacian_apply(HEX8)");
+    }
+    const int L = element_type - SFEM_GB300_SSHEX8_BASE;
+    const int blocks = grid_for((nelements + 3) / 4, 1, kNumSMs * 64);
+#define SFEM_LAP_CASE(LL)                                                                                     \
+    case LL:                                                                                                  \
+        sshex8_laplacian_apply_warp_kernel<T, LL><<<blocks, 128, 0, s>>>(nelements, elements, fff_stride, fff, x, y); \
+        return check_launch("cu_laplacian_apply(SSHEX8)");
+    switch (L) {
+        SFEM_LAP_CASE(1)
+        SFEM_LAP_CASE(2)
+        SFEM_LAP_CASE(3)
+        SFEM_LAP_CASE(4)
+        SFEM_LAP_CASE(6)
+        SFEM_LAP_CASE(8)
+        default:
+            return set_error("cu_laplacian_apply: unsupported element type %d", element_type);
+    }
+#undef SFEM_LAP_CASE
+}
+
+template <typename T>
+static int laplacian_diag_tpl(int element_type, ptrdiff_t nelements, idx_t **elements, ptrdiff_t fff_stride,
+                              const float *fff, T *diag, cudaStream_t s) {
+    if (nelements <= 0) return SFEM_GB300_SUCCESS;
+    if (element_type == SFEM_GB300_HEX8) {
+        hex8_laplacian_diag_kernel<T><<<grid_for(nelements, 128), 128, 0, s>>>(nelements, elements, fff_stride, fff, diag);
+        return check_launch("cu_laplacian_diag(HEX8)");
+    }
+    const int L = element_type - SFEM_GB300_SSHEX8_BASE;
+    const int blocks = grid_for((nelements + 3) / 4, 1, kNumSMs * 64);
+#define SFEM_LAP_CASE(LL)                                                                                   \
+    case LL:                                                                                                \
+        sshex8_laplacian_diag_kernel<T, LL><<<blocks, 128, 0, s>>>(nelements, elements, fff_stride, fff, diag); \
+        return check_launch("cu_laplacian_diag(SSHEX8)");
+    switch (L) {
+        SFEM_LAP_CASE(1)
+        SFEM_LAP_CASE(2)
+        SFEM_LAP_CASE(3)
+        SFEM_LAP_CASE(4)
+        SFEM_LAP_CASE(6)
+        SFEM_LAP_CASE(8)
+        default:
+            return set_error("cu_laplacian_diag: unsupported element type %d", element_type);
+    }
+#undef SFEM_LAP_CASE
+}
+
+}  // namespace sfem_gb300
+
+using namespace sfem_gb300;
+
+extern "C" int sfem_gb300_hex8_fff_fill(ptrdiff_t nelements, idx_t **corners, float **points, ptrdiff_t fff_stride,
+                                        float *fff, void *stream) {
+    if (nelements <= 0) return SFEM_GB300_SUCCESS;
+    hex8_geometry_kernel<<<grid_for(nelements, 128), 128, 0, stream_of(stream)>>>(nelements, corners, points,
+                                                                                  fff_stride, fff, nullptr, nullptr);
+    return check_launch("sfem_gb300_hex8_fff_fill");
+}
+
+extern "C" int sfem_gb300_hex8_adjugate_fill(ptrdiff_t nelements, idx_t **corners, float **points,
+                                             ptrdiff_t jacobian_stride, float *adjugate, float *determinant,
+                                             void *stream) {
+    if (nelements <= 0) return SFEM_GB300_SUCCESS;
+    hex8_geometry_kernel<<<grid_for(nelements, 128), 128, 0, stream_of(stream)>>>(
+            nelements, corners, points, jacobian_stride, nullptr, adjugate, determinant);
+    return check_launch("sfem_gb300_hex8_adjugate_fill");
+}
+
+extern "C" int cu_laplacian_apply(int element_type, ptrdiff_t nelements, idx_t **elements, ptrdiff_t fff_stride,
+                                  const void *fff, int real_type_xy, const void *x, void *y, void *stream) {
+    const cudaStream_t s = stream_of(stream);
+    switch (real_type_xy) {
+        case SFEM_GB300_REAL_DEFAULT:
+        case SFEM_GB300_FLOAT64:
+            return laplacian_apply_tpl<double>(element_type, nelements, elements, fff_stride, (const float *)fff,
+                                               (const double *)x, (double *)y, s);
+        case SFEM_GB300_FLOAT32:
+            return laplacian_apply_tpl<float>(element_type, nelements, elements, fff_stride, (const float *)fff,
+                                              (const float *)x, (float *)y, s);
+        default:
+            return set_error("cu_laplacian_apply: unsupported real type %d", real_type_xy);
+    }
+}
+
+extern "C" int cu_laplacian_diag(int element_type, ptrdiff_t nelements, idx_t **elements, ptrdiff_t fff_stride,
+                                 const void *fff, int real_type_diag, void *diag, void *stream) {
+    const cudaStream_t s = stream_of(stream);
+    switch (real_type_diag) {
+        case SFEM_GB300_REAL_DEFAULT:
+        case SFEM_GB300_FLOAT64:
+            return laplacian_diag_tpl<double>(element_type, nelements, elements, fff_stride, (const float *)fff,
+                                              (double *)diag, s);
+        case SFEM_GB300_FLOAT32:
+            return laplacian_diag_tpl<float>(element_type, nelements, elements, fff_stride, (const float *)fff,
+                                             (float *)diag, s);
+        default:
+            return set_error("cu_laplacian_diag: unsupported real type %d", real_type_diag);
+    }
+}
