@@ -75,11 +75,6 @@ __global__ void hex8_geometry_kernel(ptrdiff_t nelements, const idx_t *const *co
     }
 }
 
-// ------------------------------------------------------------------ tables
-
-__constant__ LapTable kLap = LapTable();
-__constant__ LapTableF kLapF = LapTableF();
-
 // ------------------------------------------------------------------ hex8 apply
 
 // One thread per element: coalesced SoA index / FFF loads, 8 gathers, 8 atomic scatters.

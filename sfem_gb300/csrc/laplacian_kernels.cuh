@@ -24,8 +24,9 @@ struct LapTableF {
     }
 };
 
-extern __constant__ LapTable kLap;
-extern __constant__ LapTableF kLapF;
+// one copy per translation unit (whole-program compilation, no -rdc)
+static __constant__ LapTable kLap = LapTable();
+static __constant__ LapTableF kLapF = LapTableF();
 
 template <typename T>
 __device__ __forceinline__ T lap_w(int k, int m);

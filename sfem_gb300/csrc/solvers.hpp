@@ -1,0 +1,476 @@
+// Device-resident host solver layer: C++ mirror of the reference's solver
+// templates on top of the sfem_gb300 C ABI.
+//
+//   Operator<T>            algebra/sfem_Operator.hpp:13-33   (apply(x, y), rows, cols)
+//   ConjugateGradient<T>   algebra/sfem_cg.hpp:79-453        (PCG; stop on sqrt(rtz)/sqrt(rtz0))
+//   Chebyshev3<T>          algebra/sfem_Chebyshev3.hpp:56-312 + PowerMethod (sfem_PowerMethod.hpp:12-55)
+//   ShiftableJacobi<T>     algebra/sfem_ShiftableJacobi.hpp:15-65
+//   StationaryIteration<T> algebra/sfem_Stationary.hpp:19-133
+//   Multigrid<T>           algebra/sfem_Multigrid.hpp:27-354 (V/W cycle)
+//
+// All vectors live on the GPU; scalars produced by reductions stay on the
+// device and feed the fused update kernels directly.  The host reads one
+// scalar per Krylov iteration (the convergence test), like the reference's
+// device BLAS does for every dot.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <functional>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "sfem_gb300.h"
+
+namespace sfem_gb300 {
+
+template <typename T>
+constexpr int real_type_v = sizeof(T) == 8 ? SFEM_GB300_FLOAT64 : SFEM_GB300_FLOAT32;
+
+#define SFEM_GB300_CHECK(expr)                  \
+    do {                                        \
+        if ((expr) != SFEM_GB300_SUCCESS) {     \
+            return SFEM_GB300_FAILURE;          \
+        }                                       \
+    } while (0)
+
+#define SFEM_GB300_CUDA(expr)                                                                                   \
+    do {                                                                                                        \
+        cudaError_t _e = (expr);                                                                                \
+        if (_e != cudaSuccess) return set_error("%s:%d: %s", __FILE__, __LINE__, cudaGetErrorString(_e)); \
+    } while (0)
+
+int set_error(const char *fmt, ...);
+
+// -------------------------------------------------------------------------- buffers
+
+// Owning device buffer.
+template <typename T>
+struct DeviceBuffer {
+    T *ptr{nullptr};
+    ptrdiff_t n{0};
+    DeviceBuffer() = default;
+    explicit DeviceBuffer(ptrdiff_t size) { resize(size); }
+    DeviceBuffer(const DeviceBuffer &) = delete;
+    DeviceBuffer &operator=(const DeviceBuffer &) = delete;
+    ~DeviceBuffer() { release(); }
+    void release() {
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        n = 0;
+    }
+    int resize(ptrdiff_t size) {
+        if (size == n && ptr) return 0;
+        release();
+        n = size;
+        if (size > 0 && cudaMalloc((void **)&ptr, size * sizeof(T)) != cudaSuccess) {
+            ptr = nullptr;
+            n = 0;
+            return set_error("cudaMalloc of %zd bytes failed", (size_t)(size * sizeof(T)));
+        }
+        return 0;
+    }
+    T *data() const { return ptr; }
+};
+
+// Stream + reduction workspace + device/pinned scalar slots shared by the solvers of one hierarchy.
+struct Context {
+    cudaStream_t stream{0};
+    void *workspace{nullptr};
+    double *d_scalars{nullptr};
+    double *h_scalars{nullptr};
+    int n_slots{0};
+    int next_slot{0};
+
+    static std::shared_ptr<Context> create(cudaStream_t s, int n_slots = 256) {
+        auto c = std::make_shared<Context>();
+        c->stream = s;
+        c->n_slots = n_slots;
+        if (cudaMalloc(&c->workspace, sfem_gb300_reduce_workspace_size()) != cudaSuccess) return nullptr;
+        if (cudaMemset(c->workspace, 0, sfem_gb300_reduce_workspace_size()) != cudaSuccess) return nullptr;
+        if (cudaMalloc((void **)&c->d_scalars, n_slots * sizeof(double)) != cudaSuccess) return nullptr;
+        if (cudaMemset(c->d_scalars, 0, n_slots * sizeof(double)) != cudaSuccess) return nullptr;
+        if (cudaMallocHost((void **)&c->h_scalars, n_slots * sizeof(double)) != cudaSuccess) return nullptr;
+        return c;
+    }
+    ~Context() {
+        if (workspace) cudaFree(workspace);
+        if (d_scalars) cudaFree(d_scalars);
+        if (h_scalars) cudaFreeHost(h_scalars);
+    }
+    // Reserve k consecutive device scalar slots.
+    double *slots(int k) {
+        if (next_slot + k > n_slots) return nullptr;
+        double *p = d_scalars + next_slot;
+        next_slot += k;
+        return p;
+    }
+    void *sp() { return stream ? (void *)&stream : nullptr; }
+    // Copy one device scalar to the host (synchronizes the stream).
+    double read(const double *d) {
+        const int k = (int)(d - d_scalars);
+        cudaMemcpyAsync(h_scalars + k, d, sizeof(double), cudaMemcpyDeviceToHost, stream);
+        cudaStreamSynchronize(stream);
+        return h_scalars[k];
+    }
+};
+
+// BLAS<T> on the device (algebra/sfem_tpl_blas.hpp:11-35) through the C ABI.
+template <typename T>
+struct Blas {
+    std::shared_ptr<Context> ctx;
+    static constexpr int rt = real_type_v<T>;
+    int zeros(ptrdiff_t n, T *x) const {
+        return n > 0 && cudaMemsetAsync(x, 0, n * sizeof(T), ctx->stream) != cudaSuccess ? set_error("memset") : 0;
+    }
+    int copy(ptrdiff_t n, const T *src, T *dst) const {
+        return n > 0 && cudaMemcpyAsync(dst, src, n * sizeof(T), cudaMemcpyDeviceToDevice, ctx->stream) != cudaSuccess
+                       ? set_error("memcpy")
+                       : 0;
+    }
+    int values(ptrdiff_t n, T v, T *x) const { return sfem_gb300_values(rt, n, v, x, ctx->sp()); }
+    int axpby(ptrdiff_t n, T a, const T *x, T b, T *y) const { return sfem_gb300_axpby(rt, n, a, x, b, y, ctx->sp()); }
+    int axpy(ptrdiff_t n, T a, const T *x, T *y) const { return sfem_gb300_axpy(rt, n, a, x, y, ctx->sp()); }
+    int zaxpby(ptrdiff_t n, T a, const T *x, T b, const T *y, T *z) const {
+        return sfem_gb300_zaxpby(rt, n, a, x, b, y, z, ctx->sp());
+    }
+    int scal(ptrdiff_t n, T a, T *x) const { return sfem_gb300_scal(rt, n, a, x, ctx->sp()); }
+    int reciprocal(ptrdiff_t n, T a, T *x) const { return sfem_gb300_reciprocal(rt, n, a, x, ctx->sp()); }
+    int xypaz(ptrdiff_t n, const T *x, const T *y, T a, T *z) const { return sfem_gb300_xypaz(rt, n, x, y, a, z, ctx->sp()); }
+    int dot(ptrdiff_t n, const T *x, const T *y, double *d_result) const {
+        return sfem_gb300_dot(rt, n, x, y, ctx->workspace, d_result, ctx->sp());
+    }
+    int norm2(ptrdiff_t n, const T *x, double *d_result) const {
+        return sfem_gb300_norm2(rt, n, x, ctx->workspace, d_result, ctx->sp());
+    }
+};
+
+// -------------------------------------------------------------------------- operators
+
+// algebra/sfem_Operator.hpp:13-33.  Linear operators accumulate (y += A x);
+// solvers used as operators take (b, x) with x as the initial guess.
+template <typename T>
+class Operator {
+public:
+    virtual ~Operator() = default;
+    virtual int apply(const T *x, T *y) = 0;
+    virtual ptrdiff_t rows() const = 0;
+    virtual ptrdiff_t cols() const = 0;
+    // true if apply overwrites y instead of accumulating
+    virtual bool overwrites_output() const { return false; }
+};
+
+template <typename T>
+class LambdaOperator final : public Operator<T> {
+public:
+    ptrdiff_t r{0}, c{0};
+    bool overwrites{false};
+    std::function<int(const T *, T *)> fn;
+    int apply(const T *x, T *y) override { return fn(x, y); }
+    ptrdiff_t rows() const override { return r; }
+    ptrdiff_t cols() const override { return c; }
+    bool overwrites_output() const override { return overwrites; }
+};
+
+template <typename T>
+std::shared_ptr<Operator<T>> make_op(ptrdiff_t rows, ptrdiff_t cols, std::function<int(const T *, T *)> fn,
+                                     bool overwrites = false) {
+    auto op = std::make_shared<LambdaOperator<T>>();
+    op->r = rows;
+    op->c = cols;
+    op->fn = std::move(fn);
+    op->overwrites = overwrites;
+    return op;
+}
+
+// -------------------------------------------------------------------------- solvers
+
+template <typename T>
+class Solver : public Operator<T> {
+public:
+    int iterations_{0};
+    virtual int iterations() const { return iterations_; }
+};
+
+// PowerMethod (algebra/sfem_PowerMethod.hpp:18-55): largest eigenvalue by normalised power iteration.
+template <typename T>
+double power_method_max_eigenvalue(const Blas<T> &blas, Operator<T> &op, int max_it, double tol, ptrdiff_t n,
+                                   T *ev, T *work, double *d_slot) {
+    const int max_it_odd = max_it + (max_it % 2 == 0);
+    blas.zeros(n, work);
+    op.apply(ev, work);
+    blas.norm2(n, work, d_slot);
+    double nrm = blas.ctx->read(d_slot);
+    blas.scal(n, T(1.0 / nrm), work);
+    T *vecs[2] = {ev, work};
+    double lambda = 0, lambda_old = 0;
+    for (int k = 0; k < max_it_odd; k++) {
+        T *w = vecs[k % 2];
+        T *v = vecs[(k + 1) % 2];
+        blas.zeros(n, w);
+        op.apply(v, w);
+        blas.norm2(n, w, d_slot);
+        lambda = blas.ctx->read(d_slot);
+        blas.scal(n, T(1.0 / lambda), w);
+        if (std::fabs(lambda - lambda_old) <= tol && k % 2 == 0) break;
+        lambda_old = lambda;
+    }
+    return lambda;
+}
+
+// Chebyshev3 (algebra/sfem_Chebyshev3.hpp:183-302).
+template <typename T>
+class Chebyshev3 final : public Solver<T> {
+public:
+    Blas<T> blas;
+    std::shared_ptr<Operator<T>> op;
+    DeviceBuffer<T> p, temp;
+    double eig_max{0}, scale_eig_max{1.02}, scale_eig_min{0.06};
+    int max_it{3};
+    bool initial_guess_zero{false};
+    int eigen_max_it{1000};
+    double eigen_tol{1e-6};
+
+    int init(const T *guess) {
+        const ptrdiff_t n = op->rows();
+        SFEM_GB300_CHECK(p.resize(n));
+        SFEM_GB300_CHECK(temp.resize(n));
+        blas.copy(n, guess, temp.ptr);
+        double *slot = blas.ctx->slots(1);
+        eig_max = power_method_max_eigenvalue(blas, *op, eigen_max_it, eigen_tol, n, temp.ptr, p.ptr, slot);
+        return 0;
+    }
+    int init_with_ones() {
+        DeviceBuffer<T> ones(op->rows());
+        blas.values(op->rows(), T(1), ones.ptr);
+        return init(ones.ptr);
+    }
+    int apply(const T *b, T *x) override {
+        const ptrdiff_t n = op->rows();
+        if (max_it <= 0) return 0;
+        const double emax = eig_max * scale_eig_max;
+        const double emin = scale_eig_min * emax;
+        const double eavg = (emin + emax) / 2, ediff = (emin - emax) / 2;
+        double alpha = 1.0 / eavg, beta = 0, dea = 0;
+        if (initial_guess_zero) {
+            blas.zaxpby(n, T(-1), b, T(0), b, p.ptr);
+        } else {
+            if (!op->overwrites_output()) blas.zeros(n, p.ptr);
+            op->apply(x, p.ptr);
+            blas.axpy(n, T(-1), b, p.ptr);
+        }
+        blas.axpy(n, T(-alpha), p.ptr, x);
+        this->iterations_ = 1;
+        for (; this->iterations_ < max_it; this->iterations_++) {
+            dea = ediff * alpha;
+            beta = (this->iterations_ == 1 ? 0.5 : 0.25) * dea * dea;
+            alpha = 1.0 / (eavg - beta / alpha);
+            if (!op->overwrites_output()) blas.zeros(n, temp.ptr);
+            op->apply(x, temp.ptr);
+            SFEM_GB300_CHECK(sfem_gb300_chebyshev_update(real_type_v<T>, n, alpha, beta, b, temp.ptr, p.ptr, x,
+                                                         blas.ctx->sp()));
+        }
+        return 0;
+    }
+    ptrdiff_t rows() const override { return op->rows(); }
+    ptrdiff_t cols() const override { return op->cols(); }
+};
+
+// ShiftableJacobi (algebra/sfem_ShiftableJacobi.hpp:15-65): x += omega D^{-1} b.
+template <typename T>
+class Jacobi final : public Solver<T> {
+public:
+    Blas<T> blas;
+    DeviceBuffer<T> inv_diag;
+    double relaxation{1.0};
+    int set_diag(const T *diag, ptrdiff_t n) {
+        SFEM_GB300_CHECK(inv_diag.resize(n));
+        blas.copy(n, diag, inv_diag.ptr);
+        return blas.reciprocal(n, T(relaxation), inv_diag.ptr);
+    }
+    int apply(const T *b, T *x) override { return blas.xypaz(inv_diag.n, inv_diag.ptr, b, T(1), x); }
+    ptrdiff_t rows() const override { return inv_diag.n; }
+    ptrdiff_t cols() const override { return inv_diag.n; }
+};
+
+// StationaryIteration (algebra/sfem_Stationary.hpp:19-133): x += P (b - A x), max_it sweeps.
+template <typename T>
+class Stationary final : public Solver<T> {
+public:
+    Blas<T> blas;
+    std::shared_ptr<Operator<T>> op, precond;
+    DeviceBuffer<T> r;
+    int max_it{3};
+    int apply(const T *b, T *x) override {
+        const ptrdiff_t n = op->rows();
+        SFEM_GB300_CHECK(r.resize(n));
+        for (this->iterations_ = 0; this->iterations_ < max_it; this->iterations_++) {
+            if (!op->overwrites_output()) blas.zeros(n, r.ptr);
+            op->apply(x, r.ptr);
+            blas.axpby(n, T(1), b, T(-1), r.ptr);
+            precond->apply(r.ptr, x);
+        }
+        return 0;
+    }
+    ptrdiff_t rows() const override { return op->rows(); }
+    ptrdiff_t cols() const override { return op->cols(); }
+};
+
+// ConjugateGradient (algebra/sfem_cg.hpp:79-453).  With a preconditioner the
+// stopping test is the reference's: sqrt(rtz) < atol or sqrt(rtz)/sqrt(rtz0) < rtol.
+template <typename T>
+class ConjugateGradient final : public Solver<T> {
+public:
+    Blas<T> blas;
+    std::shared_ptr<Operator<T>> op, precond;
+    DeviceBuffer<T> r, z, p, Ap;
+    int max_it{10000};
+    double atol{1e-30}, rtol{1e-10};
+    bool verbose{false};
+    double last_rel{0};
+    // slots: 0 rtz_new, 1 rtz_old, 2 ptAp, 3 rr
+    double *s{nullptr};
+
+    int apply(const T *b, T *x) override {
+        const ptrdiff_t n = op->rows();
+        if (!s) s = blas.ctx->slots(4);
+        if (!s) return set_error("ConjugateGradient: out of scalar slots");
+        SFEM_GB300_CHECK(r.resize(n));
+        SFEM_GB300_CHECK(p.resize(n));
+        SFEM_GB300_CHECK(Ap.resize(n));
+        if (precond) SFEM_GB300_CHECK(z.resize(n));
+        const cudaStream_t st = blas.ctx->stream;
+        (void)st;
+        if (!op->overwrites_output()) blas.zeros(n, r.ptr);
+        op->apply(x, r.ptr);
+        blas.axpby(n, T(1), b, T(-1), r.ptr);  // r = b - A x
+        T *zz = r.ptr;
+        if (precond) {
+            if (!precond->overwrites_output()) blas.zeros(n, z.ptr);
+            precond->apply(r.ptr, z.ptr);
+            zz = z.ptr;
+        }
+        blas.copy(n, zz, p.ptr);
+        blas.dot(n, r.ptr, zz, &s[0]);
+        const double rtz0 = blas.ctx->read(&s[0]);
+        last_rel = 1;
+        this->iterations_ = 0;
+        if (rtz0 == 0) return 0;
+        const double norm0 = std::sqrt(std::fabs(rtz0));
+        for (this->iterations_ = 0; this->iterations_ < max_it;) {
+            if (!op->overwrites_output()) blas.zeros(n, Ap.ptr);
+            op->apply(p.ptr, Ap.ptr);
+            blas.dot(n, p.ptr, Ap.ptr, &s[2]);
+            if (precond) {
+                SFEM_GB300_CHECK(sfem_gb300_cg_update_x_r(real_type_v<T>, n, &s[0], &s[2], p.ptr, Ap.ptr, x, r.ptr,
+                                                          nullptr, nullptr, blas.ctx->sp()));
+                if (!precond->overwrites_output()) blas.zeros(n, z.ptr);
+                precond->apply(r.ptr, z.ptr);
+                cudaMemcpyAsync(&s[1], &s[0], sizeof(double), cudaMemcpyDeviceToDevice, blas.ctx->stream);
+                blas.dot(n, r.ptr, z.ptr, &s[0]);
+            } else {
+                cudaMemcpyAsync(&s[1], &s[0], sizeof(double), cudaMemcpyDeviceToDevice, blas.ctx->stream);
+                SFEM_GB300_CHECK(sfem_gb300_cg_update_x_r(real_type_v<T>, n, &s[1], &s[2], p.ptr, Ap.ptr, x, r.ptr,
+                                                          blas.ctx->workspace, &s[0], blas.ctx->sp()));
+            }
+            this->iterations_++;
+            const double rtz = blas.ctx->read(&s[0]);
+            const double anorm = std::sqrt(std::fabs(rtz));
+            last_rel = anorm / norm0;
+            if (verbose) printf("cg %d: %g %g\n", this->iterations_, anorm, last_rel);
+            if (anorm < atol || last_rel < rtol || rtz == 0) return 0;
+            if (!std::isfinite(rtz)) return set_error("ConjugateGradient: non-finite residual");
+            SFEM_GB300_CHECK(sfem_gb300_cg_update_p(real_type_v<T>, n, &s[0], &s[1], zz, p.ptr, blas.ctx->sp()));
+        }
+        return set_error("ConjugateGradient: no convergence in %d iterations (rel %g)", max_it, last_rel);
+    }
+    ptrdiff_t rows() const override { return op->rows(); }
+    ptrdiff_t cols() const override { return op->cols(); }
+};
+
+// Multigrid (algebra/sfem_Multigrid.hpp:27-354).  Level 0 is the finest.
+template <typename T>
+class Multigrid final : public Solver<T> {
+public:
+    struct Level {
+        std::shared_ptr<Operator<T>> op, smoother, prolongation /* from next coarser */, restriction /* to coarser */;
+        DeviceBuffer<T> rhs, sol, work;
+    };
+    Blas<T> blas;
+    std::vector<Level> levels;
+    int max_it{1};
+    int cycle_type{1};
+    double atol{1e-30};
+    double *s{nullptr};
+    bool wrap_input{true};
+    double norm_residual0{0}, norm_residual{0};
+
+    void add_level(std::shared_ptr<Operator<T>> op, std::shared_ptr<Operator<T>> smoother,
+                   std::shared_ptr<Operator<T>> prolongation, std::shared_ptr<Operator<T>> restriction) {
+        Level l;
+        l.op = op;
+        l.smoother = smoother;
+        l.prolongation = prolongation;
+        l.restriction = restriction;
+        levels.push_back(std::move(l));
+    }
+    int ensure_init() {
+        if (!s) s = blas.ctx->slots(1);
+        for (size_t i = 0; i < levels.size(); i++) {
+            const ptrdiff_t n = levels[i].op->rows();
+            if (i > 0 || !wrap_input) {
+                SFEM_GB300_CHECK(levels[i].rhs.resize(n));
+                SFEM_GB300_CHECK(levels[i].sol.resize(n));
+            }
+            SFEM_GB300_CHECK(levels[i].work.resize(n));
+        }
+        return 0;
+    }
+    // returns 1 if converged
+    int cycle(int l, const T *rhs, T *sol) {
+        Level &L = levels[l];
+        const ptrdiff_t n = L.op->rows();
+        if (l == (int)levels.size() - 1) {
+            blas.zeros(n, sol);
+            L.smoother->apply(rhs, sol);
+            return 0;
+        }
+        Level &C = levels[l + 1];
+        const ptrdiff_t nc = C.op->rows();
+        for (int k = 0; k < cycle_type; k++) {
+            L.smoother->apply(rhs, sol);
+            if (!L.op->overwrites_output()) blas.zeros(n, L.work.ptr);
+            L.op->apply(sol, L.work.ptr);
+            blas.axpby(n, T(1), rhs, T(-1), L.work.ptr);
+            if (l == 0 && atol > 0) {
+                blas.norm2(n, L.work.ptr, s);
+                norm_residual = blas.ctx->read(s);
+                if (this->iterations_ == 0) norm_residual0 = norm_residual;
+                if (norm_residual < atol) return 1;
+            }
+            blas.zeros(nc, C.rhs.ptr);
+            L.restriction->apply(L.work.ptr, C.rhs.ptr);
+            blas.zeros(nc, C.sol.ptr);
+            cycle(l + 1, C.rhs.ptr, C.sol.ptr);
+            blas.zeros(n, L.work.ptr);
+            C.prolongation->apply(C.sol.ptr, L.work.ptr);
+            blas.axpby(n, T(1), L.work.ptr, T(1), sol);
+            L.smoother->apply(rhs, sol);
+        }
+        return 0;
+    }
+    int apply(const T *b, T *x) override {
+        SFEM_GB300_CHECK(ensure_init());
+        for (this->iterations_ = 0; this->iterations_ < max_it; this->iterations_++) {
+            if (cycle(0, b, x)) break;
+        }
+        return 0;
+    }
+    ptrdiff_t rows() const override { return levels[0].op->rows(); }
+    ptrdiff_t cols() const override { return levels[0].op->cols(); }
+};
+
+}  // namespace sfem_gb300
