@@ -75,6 +75,68 @@ int cu_laplacian_apply(int element_type, ptrdiff_t nelements, sfem_gb300_idx_t *
 int cu_laplacian_diag(int element_type, ptrdiff_t nelements, sfem_gb300_idx_t **elements, ptrdiff_t fff_stride,
                       const void *fff, int real_type_diag, void *diag, void *stream);
 
+/* ------------------------------------------------------- linear elasticity */
+
+/* out += K u for the affine hex8 / sshex8 linear-elasticity operator with
+ * interleaved vectors (u[3*node + d]) and SoA float adjugate (9 x stride) /
+ * determinant (stride).  Replaces cu_linear_elasticity_apply
+ * (operators/cuda/cu_linear_elasticity.hpp:15) / cu_affine_hex8_linear_elasticity_apply
+ * (operators/hex8/cuda/cu_hex8_linear_elasticity.cu:181). */
+int sfem_gb300_linear_elasticity_apply(int element_type, ptrdiff_t nelements, sfem_gb300_idx_t **elements,
+                                       ptrdiff_t jacobian_stride, const float *adjugate, const float *determinant,
+                                       double mu, double lambda, int real_type, const void *u, void *out,
+                                       void *stream);
+
+/* The reference's exact sshex8 entry point (operators/sshex8/cuda/cu_sshex8_linear_elasticity.cu:1730-1748);
+ * only the interleaved layout (u_stride = out_stride = 3, uy = ux + 1, uz = ux + 2) is accepted. */
+int cu_affine_sshex8_linear_elasticity_apply(int level, ptrdiff_t nelements, sfem_gb300_idx_t **elements,
+                                             ptrdiff_t jacobian_stride, const void *jacobian_adjugate,
+                                             const void *jacobian_determinant, double mu, double lambda,
+                                             int real_type, ptrdiff_t u_stride, const void *ux, const void *uy,
+                                             const void *uz, ptrdiff_t out_stride, void *outx, void *outy, void *outz,
+                                             void *stream);
+
+/* diag3 += diagonal (3 per node) and/or block6 += symmetric 3x3 block diagonal
+ * (00,01,02,11,12,22 per node); either may be NULL.  Replaces
+ * cu_affine_sshex8_linear_elasticity_diag / _block_diag_sym
+ * (operators/sshex8/cuda/cu_sshex8_linear_elasticity.cu:1938, :2171). */
+int sfem_gb300_linear_elasticity_block_diag(int element_type, ptrdiff_t nelements, sfem_gb300_idx_t **elements,
+                                            ptrdiff_t jacobian_stride, const float *adjugate, const float *determinant,
+                                            double mu, double lambda, int real_type, void *diag3, void *block6,
+                                            void *stream);
+
+/* block6 <- omega * inverse(block6) per node; Dirichlet nodes become identity
+ * (algebra/cuda/sfem_cuda_ShiftableJacobi.cu:14-100). */
+int sfem_gb300_block3_invert(int real_type, ptrdiff_t n_nodes, void *block6, double omega, ptrdiff_t n_dirichlet,
+                             const int32_t *dirichlet_nodes, void *stream);
+/* x += B r per node with symmetric 3x3 blocks B (block Jacobi step). */
+int sfem_gb300_block3_apply(int real_type, ptrdiff_t n_nodes, const void *block6, const void *r, void *x, void *stream);
+
+/* ------------------------------------------------------ multigrid transfer */
+
+/* to = P from: nested trilinear prolongation inside each macro element from
+ * level from_level to to_level (to_level % from_level == 0), vec_size
+ * interleaved components.  Both connectivities are in sshex8 lidx order (for
+ * level 1 pass the macro corners in lidx order).  Output overwritten.
+ * Replaces sshex8_prolongate / sshex8_hierarchical_prolongation
+ * (operators/sshex8/sshex8_interpolate.cpp:259, :129) and smesh's device path. */
+int sfem_gb300_sshex8_prolongate(ptrdiff_t nelements, int from_level, sfem_gb300_idx_t **from_elements, int to_level,
+                                 sfem_gb300_idx_t **to_elements, int vec_size, int real_type, const void *from,
+                                 void *to, void *stream);
+
+/* to += R from with R = P^T and the fine input divided by the element-node
+ * incidence count.  Replaces sshex8_restrict / sshex8_hierarchical_restriction
+ * (operators/sshex8/sshex8_interpolate.cpp:633, :12). */
+int sfem_gb300_sshex8_restrict(ptrdiff_t nelements, int from_level, sfem_gb300_idx_t **from_elements,
+                               const uint16_t *from_element_to_node_incidence_count, int to_level,
+                               sfem_gb300_idx_t **to_elements, int vec_size, int real_type, const void *from, void *to,
+                               void *stream);
+
+/* count[node] += number of macro elements containing the node (count zeroed by the caller).
+ * Replaces sshex8_element_node_incidence_count (operators/sshex8/sshex8_interpolate.cpp:239). */
+int sfem_gb300_sshex8_element_node_incidence_count(int level, ptrdiff_t nelements, sfem_gb300_idx_t **elements,
+                                                   uint16_t *count, void *stream);
+
 /* ------------------------------------------------------------ vector BLAS */
 /* Device-vector kernels of the BLAS<T> seam (algebra/sfem_tpl_blas.hpp:11-35;
  * CUDA_BLAS, algebra/cuda/sfem_cuda_blas.hpp:55-77).  real_type selects
@@ -132,6 +194,72 @@ int sfem_gb300_constraint_nodes_to_value(int real_type, ptrdiff_t n_nodes, const
 /* Precision conversion dst = (dst_type) src, and y += alpha (double) x for float x. */
 int sfem_gb300_convert(ptrdiff_t n, int src_type, const void *src, int dst_type, void *dst, void *stream);
 int sfem_gb300_axpy_f32_to_f64(ptrdiff_t n, double alpha, const float *x, double *y, void *stream);
+
+/* ------------------------------------------------- operators and solvers */
+/* Opaque handles (void *) over the device solver layer, mirroring the
+ * reference's frontend factories (frontend/sfem_API.hpp: create_cg :143,
+ * create_shiftable_jacobi :180, create_stationary :247, create_cheb3 :287,
+ * create_mg :323) and Operator<T>::apply (algebra/sfem_Operator.hpp:13-33).
+ * The caller owns every device array passed in and keeps it alive while the
+ * handle exists; handles own their work vectors.  Every handle is released
+ * with sfem_gb300_handle_destroy.  Linear operators accumulate (y += A x);
+ * solvers take (b, x) with x as the initial guess. */
+
+/* Stream (pointer to cudaStream_t or NULL) + reduction workspace shared by the handles built on it. */
+int sfem_gb300_context_create(void *stream, void **context);
+int sfem_gb300_handle_destroy(void *handle);
+
+/* Function-level Laplacian: y += A x, then y[c] = x[c] on Dirichlet nodes
+ * (Function::apply + copy_constrained_dofs, frontend/sfem_Function.cpp:481-496). */
+int sfem_gb300_laplacian_op_create(void *context, int real_type, int element_type, ptrdiff_t nelements,
+                                   sfem_gb300_idx_t **elements, ptrdiff_t fff_stride, const float *fff,
+                                   ptrdiff_t n_nodes, ptrdiff_t n_dirichlet, const int32_t *dirichlet_nodes,
+                                   void **op);
+/* Function-level linear elasticity (3 dofs/node, all components fixed on Dirichlet nodes). */
+int sfem_gb300_elasticity_op_create(void *context, int real_type, int element_type, ptrdiff_t nelements,
+                                    sfem_gb300_idx_t **elements, ptrdiff_t jacobian_stride, const float *adjugate,
+                                    const float *determinant, double mu, double lambda, ptrdiff_t n_nodes,
+                                    ptrdiff_t n_dirichlet, const int32_t *dirichlet_nodes, void **op);
+/* Prolongation (coarse level -> fine level) then zero fine Dirichlet dofs
+ * (algebra/mg/sfem_GeometricMultigrid.cpp:54-66). */
+int sfem_gb300_prolongation_op_create(void *context, int real_type, ptrdiff_t nelements, int from_level,
+                                      sfem_gb300_idx_t **from_elements, ptrdiff_t n_from, int to_level,
+                                      sfem_gb300_idx_t **to_elements, ptrdiff_t n_to, int vec_size,
+                                      ptrdiff_t n_dirichlet_to, const int32_t *dirichlet_to, void **op);
+/* Restriction (fine -> coarse) then zero coarse Dirichlet dofs (:38-52). */
+int sfem_gb300_restriction_op_create(void *context, int real_type, ptrdiff_t nelements, int from_level,
+                                     sfem_gb300_idx_t **from_elements, const uint16_t *count, ptrdiff_t n_from,
+                                     int to_level, sfem_gb300_idx_t **to_elements, ptrdiff_t n_to, int vec_size,
+                                     ptrdiff_t n_dirichlet_to, const int32_t *dirichlet_to, void **op);
+int sfem_gb300_op_apply(void *op, const void *x, void *y);
+int sfem_gb300_op_size(void *op, ptrdiff_t *rows, ptrdiff_t *cols);
+
+/* Jacobi smoother x += relaxation D^-1 b (ShiftableJacobi, algebra/sfem_ShiftableJacobi.hpp:15-65). */
+int sfem_gb300_jacobi_create(void *context, int real_type, ptrdiff_t n, const void *diag, double relaxation,
+                             void **solver);
+/* 3x3 block Jacobi x += B b with block6 already inverted by sfem_gb300_block3_invert
+ * (ShiftableBlockSymJacobi, algebra/sfem_ShiftableJacobi.hpp:67-155). */
+int sfem_gb300_block_jacobi_create(void *context, int real_type, ptrdiff_t n_nodes, const void *inv_block6,
+                                   void **solver);
+/* Stationary iteration x += P (b - A x), max_it sweeps (algebra/sfem_Stationary.hpp:19-133). */
+int sfem_gb300_stationary_create(void *context, void *op, void *precond, int max_it, void **solver);
+/* Chebyshev3 smoother; runs the power method from a vector of ones at creation
+ * (algebra/sfem_Chebyshev3.hpp:56-312, algebra/sfem_PowerMethod.hpp:18-55). */
+int sfem_gb300_chebyshev3_create(void *context, void *op, int max_it, double scale_eig_max, double scale_eig_min,
+                                 int eigen_max_it, double eigen_tol, void **solver);
+int sfem_gb300_chebyshev3_eig_max(void *solver, double *eig_max);
+int sfem_gb300_chebyshev3_set_eig_max(void *solver, double eig_max);
+/* (Preconditioned) conjugate gradient (algebra/sfem_cg.hpp:79-453); precond may be NULL. */
+int sfem_gb300_cg_create(void *context, void *op, void *precond, int max_it, double rtol, double atol, void **solver);
+int sfem_gb300_cg_set_verbose(void *solver, int verbose);
+/* Multigrid V/W cycle (algebra/sfem_Multigrid.hpp:27-354); levels added finest first. */
+int sfem_gb300_mg_create(void *context, int real_type, int max_it, int cycle_type, void **solver);
+int sfem_gb300_mg_add_level(void *mg, void *op, void *smoother, void *prolongation, void *restriction);
+/* FP64 iterative refinement around a float inner solver (no reference counterpart):
+ * r = b - A x in double, d = inner(r/|r|) in float, x += |r| d, until |r| <= rtol |b|. */
+int sfem_gb300_ir_create(void *context, void *op64, void *inner32, int max_it, double rtol, void **solver);
+int sfem_gb300_solver_apply(void *solver, const void *b, void *x);
+int sfem_gb300_solver_stats(void *solver, int *iterations, double *last_relative);
 
 #ifdef __cplusplus
 }

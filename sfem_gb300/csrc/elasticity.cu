@@ -1,0 +1,373 @@
+// Matrix-free linear elasticity (3 dofs per node, interleaved u[3*node+d]) on
+// hex8 and sshex8 meshes, sm_103a.
+//
+// Operator (reference: affine_sshex8_linear_elasticity_apply_macro_adjugate,
+// operators/sshex8/sshex8_linear_elasticity.cpp:275-424): one adjugate (9
+// floats) and determinant per macro element; sub-adjugate = adj h^2 and
+// sub-det = det h^3 with h = 1/L (operators/sshex8/sshex8.hpp:26-42); the 24x24
+// element stiffness K (row/column = component*8 + corner) is applied to every
+// micro element.  K[(i,a),(j,b)] = 1/det sum_pq I_ab^pq (mu adj_pj adj_qi +
+// lambda adj_pi adj_qj + delta_ij mu (adj adj^T)_pq), I_ab^pq the exact Q1
+// integrals of d_p phi_a d_q phi_b on the unit cube.
+#include "common.cuh"
+
+namespace sfem_gb300 {
+
+struct GradTable {
+    double I[8][8][3][3];
+    constexpr GradTable() : I() {
+        for (int a = 0; a < 8; a++)
+            for (int b = 0; b < 8; b++)
+                for (int p = 0; p < 3; p++)
+                    for (int q = 0; q < 3; q++) I[a][b][p][q] = q1_grad_integral(a, b, p, q);
+    }
+};
+static __constant__ GradTable kGrad = GradTable();
+
+// sshex8 lidx of the hex8 corner c at level 1 (used when a hex8 mesh is given in hex8 order)
+__host__ __device__ constexpr int hex8_corner_of_lidx1(int l) {
+    return l == 0 ? 0 : l == 1 ? 1 : l == 2 ? 3 : l == 3 ? 2 : l == 4 ? 4 : l == 5 ? 5 : l == 6 ? 7 : 6;
+}
+
+// Entry k (0..575) of the 24x24 element matrix from sub-adjugate / sub-det.
+template <typename T>
+__device__ __forceinline__ T elasticity_entry(int k, const T adj[9], const T AA[9], T inv_det, T mu, T lambda) {
+    const int row = k / 24, col = k % 24;
+    const int i = row / 8, a = row % 8, j = col / 8, b = col % 8;
+    T s = 0;
+#pragma unroll
+    for (int p = 0; p < 3; p++)
+#pragma unroll
+        for (int q = 0; q < 3; q++) {
+            T w = mu * adj[3 * p + j] * adj[3 * q + i] + lambda * adj[3 * p + i] * adj[3 * q + j];
+            if (i == j) w += mu * AA[3 * p + q];
+            s += (T)kGrad.I[a][b][p][q] * w;
+        }
+    return s * inv_det;
+}
+
+template <typename T>
+__device__ __forceinline__ void load_sub_adjugate(const float *adjugate, const float *determinant, ptrdiff_t stride,
+                                                  ptrdiff_t e, int L, T adj[9], T AA[9], T &inv_det) {
+    const T h = T(1) / T(L);
+#pragma unroll
+    for (int d = 0; d < 9; d++) adj[d] = (T)adjugate[d * stride + e] * (h * h);
+    const T det = (T)determinant[e] * (h * h * h);
+    inv_det = T(1) / det;
+#pragma unroll
+    for (int p = 0; p < 3; p++)
+#pragma unroll
+        for (int q = 0; q < 3; q++) AA[3 * p + q] = adj[3 * p] * adj[3 * q] + adj[3 * p + 1] * adj[3 * q + 1] + adj[3 * p + 2] * adj[3 * q + 2];
+}
+
+// v1: one warp per macro element.  The warp builds K (576 entries) in shared
+// memory, stages the (L+1)^3 x 3 micro-grid values, lanes apply K per micro
+// element with shared-memory accumulation, then scatter (owned interior nodes
+// plain, shared surface nodes atomic).  HEX8 = plain hex8 mesh in hex8 corner order.
+template <typename T, int L, bool HEX8>
+__global__ void __launch_bounds__(64) elasticity_apply_warp_kernel(ptrdiff_t nelements, const idx_t *const *elements,
+                                                                   ptrdiff_t stride, const float *adjugate,
+                                                                   const float *determinant, T mu, T lambda,
+                                                                   const T *__restrict__ x, T *__restrict__ y) {
+    constexpr int N1 = L + 1;
+    constexpr int NXE = N1 * N1 * N1;
+    constexpr int NM = L * L * L;
+    constexpr int WPB = 2;
+    constexpr int NR = (NXE + 31) / 32;
+    __shared__ T Ks[WPB][576];
+    __shared__ T xs[WPB][3 * NXE];
+    __shared__ T ys[WPB][3 * NXE];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    T *K = Ks[warp];
+    T *xw = xs[warp];
+    T *yw = ys[warp];
+    for (ptrdiff_t e = (ptrdiff_t)blockIdx.x * WPB + warp; e < nelements; e += (ptrdiff_t)gridDim.x * WPB) {
+        T adj[9], AA[9], inv_det;
+        load_sub_adjugate<T>(adjugate, determinant, stride, e, L, adj, AA, inv_det);
+        for (int k = lane; k < 576; k += 32) K[k] = elasticity_entry<T>(k, adj, AA, inv_det, mu, lambda);
+        idx_t gi[NR];
+#pragma unroll
+        for (int r = 0; r < NR; r++) {
+            const int l = lane + 32 * r;
+            if (l < NXE) {
+                gi[r] = elements[HEX8 ? hex8_corner_of_lidx1(l) : l][e];
+#pragma unroll
+                for (int d = 0; d < 3; d++) {
+                    xw[d * NXE + l] = x[3 * (ptrdiff_t)gi[r] + d];
+                    yw[d * NXE + l] = 0;
+                }
+            }
+        }
+        __syncwarp();
+        for (int m = lane; m < NM; m += 32) {
+            const int xi = m % L, yi = (m / L) % L, zi = m / (L * L);
+            int v[8];
+            T u[24];
+#pragma unroll
+            for (int c = 0; c < 8; c++) {
+                v[c] = lidx(L, xi + c8x(c), yi + c8y(c), zi + c8z(c));
+#pragma unroll
+                for (int d = 0; d < 3; d++) u[d * 8 + c] = xw[d * NXE + v[c]];
+            }
+#pragma unroll 4
+            for (int i = 0; i < 24; i++) {
+                T acc = 0;
+#pragma unroll
+                for (int j = 0; j < 24; j++) acc += K[i * 24 + j] * u[j];
+                atomicAdd(&yw[(i / 8) * NXE + v[i % 8]], acc);
+            }
+        }
+        __syncwarp();
+#pragma unroll
+        for (int r = 0; r < NR; r++) {
+            const int l = lane + 32 * r;
+            if (l < NXE) {
+                const int xi = l % N1, yi = (l / N1) % N1, zi = l / (N1 * N1);
+                const bool interior = xi > 0 && xi < L && yi > 0 && yi < L && zi > 0 && zi < L;
+#pragma unroll
+                for (int d = 0; d < 3; d++) {
+                    const T val = yw[d * NXE + l];
+                    T *dst = &y[3 * (ptrdiff_t)gi[r] + d];
+                    if (interior)
+                        *dst += val;
+                    else
+                        atomicAdd(dst, val);
+                }
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// Diagonal (diag3: 3 per node) and symmetric 3x3 block diagonal (block6: 00,01,02,11,12,22 per node).
+template <typename T, int L, bool HEX8>
+__global__ void __launch_bounds__(64) elasticity_block_diag_kernel(ptrdiff_t nelements, const idx_t *const *elements,
+                                                                   ptrdiff_t stride, const float *adjugate,
+                                                                   const float *determinant, T mu, T lambda, T *diag3,
+                                                                   T *block6) {
+    constexpr int N1 = L + 1;
+    constexpr int NXE = N1 * N1 * N1;
+    constexpr int WPB = 2;
+    __shared__ T Bs[WPB][8][6];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int bi[6] = {0, 0, 0, 1, 1, 2}, bj[6] = {0, 1, 2, 1, 2, 2};
+    for (ptrdiff_t e = (ptrdiff_t)blockIdx.x * WPB + warp; e < nelements; e += (ptrdiff_t)gridDim.x * WPB) {
+        T adj[9], AA[9], inv_det;
+        load_sub_adjugate<T>(adjugate, determinant, stride, e, L, adj, AA, inv_det);
+        for (int k = lane; k < 48; k += 32) {
+            const int a = k / 6, c = k % 6;
+            Bs[warp][a][c] = elasticity_entry<T>((bi[c] * 8 + a) * 24 + bj[c] * 8 + a, adj, AA, inv_det, mu, lambda);
+        }
+        __syncwarp();
+        for (int l = lane; l < NXE; l += 32) {
+            const int xi = l % N1, yi = (l / N1) % N1, zi = l / (N1 * N1);
+            T s[6] = {0, 0, 0, 0, 0, 0};
+#pragma unroll
+            for (int a = 0; a < 8; a++) {
+                const bool ok = (c8x(a) ? xi > 0 : xi < L) && (c8y(a) ? yi > 0 : yi < L) && (c8z(a) ? zi > 0 : zi < L);
+                if (ok)
+#pragma unroll
+                    for (int c = 0; c < 6; c++) s[c] += Bs[warp][a][c];
+            }
+            const ptrdiff_t g = elements[HEX8 ? hex8_corner_of_lidx1(l) : l][e];
+            const bool interior = xi > 0 && xi < L && yi > 0 && yi < L && zi > 0 && zi < L;
+            if (diag3) {
+                const T dv[3] = {s[0], s[3], s[5]};
+                for (int d = 0; d < 3; d++) {
+                    if (interior)
+                        diag3[3 * g + d] += dv[d];
+                    else
+                        atomicAdd(&diag3[3 * g + d], dv[d]);
+                }
+            }
+            if (block6) {
+                for (int c = 0; c < 6; c++) {
+                    if (interior)
+                        block6[6 * g + c] += s[c];
+                    else
+                        atomicAdd(&block6[6 * g + c], s[c]);
+                }
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// In-place inversion of symmetric 3x3 blocks (6 per node) scaled by omega, with
+// Dirichlet nodes set to identity (inverse3_inplace_apply_AoS + mask3_apply,
+// algebra/cuda/sfem_cuda_ShiftableJacobi.cu:14-100).
+template <typename T>
+__global__ void block_inverse_kernel(ptrdiff_t n_nodes, T *block6, T omega) {
+    for (ptrdiff_t i = blockIdx.x * (ptrdiff_t)blockDim.x + threadIdx.x; i < n_nodes; i += (ptrdiff_t)gridDim.x * blockDim.x) {
+        T *b = &block6[6 * i];
+        const T a00 = b[0], a01 = b[1], a02 = b[2], a11 = b[3], a12 = b[4], a22 = b[5];
+        const T c00 = a11 * a22 - a12 * a12, c01 = a02 * a12 - a01 * a22, c02 = a01 * a12 - a02 * a11;
+        const T c11 = a00 * a22 - a02 * a02, c12 = a01 * a02 - a00 * a12, c22 = a00 * a11 - a01 * a01;
+        const T det = a00 * c00 + a01 * c01 + a02 * c02;
+        const T s = det != T(0) ? omega / det : T(0);
+        b[0] = c00 * s;
+        b[1] = c01 * s;
+        b[2] = c02 * s;
+        b[3] = c11 * s;
+        b[4] = c12 * s;
+        b[5] = c22 * s;
+    }
+}
+
+template <typename T>
+__global__ void block_identity_kernel(ptrdiff_t nn, const idx_t *nodes, T *block6) {
+    for (ptrdiff_t i = blockIdx.x * (ptrdiff_t)blockDim.x + threadIdx.x; i < nn; i += (ptrdiff_t)gridDim.x * blockDim.x) {
+        T *b = &block6[6 * (ptrdiff_t)nodes[i]];
+        b[0] = 1;
+        b[1] = 0;
+        b[2] = 0;
+        b[3] = 1;
+        b[4] = 0;
+        b[5] = 1;
+    }
+}
+
+// x += B r for symmetric 3x3 blocks B (block Jacobi step)
+template <typename T>
+__global__ void block_apply_kernel(ptrdiff_t n_nodes, const T *__restrict__ block6, const T *__restrict__ r,
+                                   T *__restrict__ x) {
+    for (ptrdiff_t i = blockIdx.x * (ptrdiff_t)blockDim.x + threadIdx.x; i < n_nodes; i += (ptrdiff_t)gridDim.x * blockDim.x) {
+        const T *b = &block6[6 * i];
+        const T r0 = r[3 * i], r1 = r[3 * i + 1], r2 = r[3 * i + 2];
+        x[3 * i] += b[0] * r0 + b[1] * r1 + b[2] * r2;
+        x[3 * i + 1] += b[1] * r0 + b[3] * r1 + b[4] * r2;
+        x[3 * i + 2] += b[2] * r0 + b[4] * r1 + b[5] * r2;
+    }
+}
+
+template <typename T>
+static int elasticity_apply_tpl(int element_type, ptrdiff_t nelements, idx_t **elements, ptrdiff_t stride,
+                                const float *adj, const float *det, T mu, T lambda, const T *x, T *y, cudaStream_t s) {
+    if (nelements <= 0) return SFEM_GB300_SUCCESS;
+    const int blocks = grid_for((nelements + 1) / 2, 1, kNumSMs * 64);
+    if (element_type == SFEM_GB300_HEX8) {
+        elasticity_apply_warp_kernel<T, 1, true><<<blocks, 64, 0, s>>>(nelements, elements, stride, adj, det, mu,
+                                                                       lambda, x, y);
+        return check_launch("sfem_gb300_linear_elasticity_apply(HEX8)");
+    }
+    const int L = element_type - SFEM_GB300_SSHEX8_BASE;
+#define SFEM_EL_CASE(LL)                                                                                             \
+    case LL:                                                                                                         \
+        elasticity_apply_warp_kernel<T, LL, false><<<blocks, 64, 0, s>>>(nelements, elements, stride, adj, det, mu, \
+                                                                         lambda, x, y);                              \
+        return check_launch("sfem_gb300_linear_elasticity_apply(SSHEX8)");
+    switch (L) {
+        SFEM_EL_CASE(1)
+        SFEM_EL_CASE(2)
+        SFEM_EL_CASE(3)
+        SFEM_EL_CASE(4)
+        default:
+            return set_error("sfem_gb300_linear_elasticity_apply: unsupported element type %d", element_type);
+    }
+#undef SFEM_EL_CASE
+}
+
+template <typename T>
+static int elasticity_diag_tpl(int element_type, ptrdiff_t nelements, idx_t **elements, ptrdiff_t stride,
+                               const float *adj, const float *det, T mu, T lambda, T *diag3, T *block6, cudaStream_t s) {
+    if (nelements <= 0) return SFEM_GB300_SUCCESS;
+    const int blocks = grid_for((nelements + 1) / 2, 1, kNumSMs * 64);
+    if (element_type == SFEM_GB300_HEX8) {
+        elasticity_block_diag_kernel<T, 1, true><<<blocks, 64, 0, s>>>(nelements, elements, stride, adj, det, mu,
+                                                                       lambda, diag3, block6);
+        return check_launch("sfem_gb300_linear_elasticity_block_diag(HEX8)");
+    }
+    const int L = element_type - SFEM_GB300_SSHEX8_BASE;
+#define SFEM_EL_CASE(LL)                                                                                             \
+    case LL:                                                                                                         \
+        elasticity_block_diag_kernel<T, LL, false><<<blocks, 64, 0, s>>>(nelements, elements, stride, adj, det, mu, \
+                                                                         lambda, diag3, block6);                     \
+        return check_launch("sfem_gb300_linear_elasticity_block_diag(SSHEX8)");
+    switch (L) {
+        SFEM_EL_CASE(1)
+        SFEM_EL_CASE(2)
+        SFEM_EL_CASE(3)
+        SFEM_EL_CASE(4)
+        default:
+            return set_error("sfem_gb300_linear_elasticity_block_diag: unsupported element type %d", element_type);
+    }
+#undef SFEM_EL_CASE
+}
+
+}  // namespace sfem_gb300
+
+using namespace sfem_gb300;
+
+extern "C" int sfem_gb300_linear_elasticity_apply(int element_type, ptrdiff_t nelements, idx_t **elements,
+                                                  ptrdiff_t jacobian_stride, const float *adjugate,
+                                                  const float *determinant, double mu, double lambda, int real_type,
+                                                  const void *u, void *out, void *stream) {
+    const cudaStream_t s = stream_of(stream);
+    if (real_type == SFEM_GB300_FLOAT32)
+        return elasticity_apply_tpl<float>(element_type, nelements, elements, jacobian_stride, adjugate, determinant,
+                                           (float)mu, (float)lambda, (const float *)u, (float *)out, s);
+    if (real_type == SFEM_GB300_FLOAT64 || real_type == SFEM_GB300_REAL_DEFAULT)
+        return elasticity_apply_tpl<double>(element_type, nelements, elements, jacobian_stride, adjugate, determinant,
+                                            mu, lambda, (const double *)u, (double *)out, s);
+    return set_error("sfem_gb300_linear_elasticity_apply: unsupported real type %d", real_type);
+}
+
+extern "C" int cu_affine_sshex8_linear_elasticity_apply(int level, ptrdiff_t nelements, idx_t **elements,
+                                                        ptrdiff_t jacobian_stride, const void *jacobian_adjugate,
+                                                        const void *jacobian_determinant, double mu, double lambda,
+                                                        int real_type, ptrdiff_t u_stride, const void *ux,
+                                                        const void *uy, const void *uz, ptrdiff_t out_stride,
+                                                        void *outx, void *outy, void *outz, void *stream) {
+    // Interleaved xyz vectors only: ux = u, uy = u + 1, uz = u + 2 with stride 3.
+    const size_t es = real_type == SFEM_GB300_FLOAT32 ? 4 : 8;
+    if (u_stride != 3 || out_stride != 3 || (const char *)uy != (const char *)ux + es ||
+        (const char *)uz != (const char *)ux + 2 * es || (char *)outy != (char *)outx + es ||
+        (char *)outz != (char *)outx + 2 * es)
+        return set_error("cu_affine_sshex8_linear_elasticity_apply: only interleaved (stride 3) vectors are supported");
+    return sfem_gb300_linear_elasticity_apply(SFEM_GB300_SSHEX8(level), nelements, elements, jacobian_stride,
+                                              (const float *)jacobian_adjugate, (const float *)jacobian_determinant, mu,
+                                              lambda, real_type, ux, outx, stream);
+}
+
+extern "C" int sfem_gb300_linear_elasticity_block_diag(int element_type, ptrdiff_t nelements, idx_t **elements,
+                                                       ptrdiff_t jacobian_stride, const float *adjugate,
+                                                       const float *determinant, double mu, double lambda,
+                                                       int real_type, void *diag3, void *block6, void *stream) {
+    const cudaStream_t s = stream_of(stream);
+    if (real_type == SFEM_GB300_FLOAT32)
+        return elasticity_diag_tpl<float>(element_type, nelements, elements, jacobian_stride, adjugate, determinant,
+                                          (float)mu, (float)lambda, (float *)diag3, (float *)block6, s);
+    if (real_type == SFEM_GB300_FLOAT64 || real_type == SFEM_GB300_REAL_DEFAULT)
+        return elasticity_diag_tpl<double>(element_type, nelements, elements, jacobian_stride, adjugate, determinant,
+                                           mu, lambda, (double *)diag3, (double *)block6, s);
+    return set_error("sfem_gb300_linear_elasticity_block_diag: unsupported real type %d", real_type);
+}
+
+extern "C" int sfem_gb300_block3_invert(int real_type, ptrdiff_t n_nodes, void *block6, double omega,
+                                        ptrdiff_t n_dirichlet, const int32_t *dirichlet_nodes, void *stream) {
+    const cudaStream_t s = stream_of(stream);
+    if (n_nodes <= 0) return SFEM_GB300_SUCCESS;
+    if (real_type == SFEM_GB300_FLOAT32) {
+        if (n_dirichlet > 0)
+            block_identity_kernel<float><<<grid_for(n_dirichlet, 256), 256, 0, s>>>(n_dirichlet, dirichlet_nodes, (float *)block6);
+        block_inverse_kernel<float><<<grid_for(n_nodes, 256), 256, 0, s>>>(n_nodes, (float *)block6, (float)omega);
+    } else {
+        if (n_dirichlet > 0)
+            block_identity_kernel<double><<<grid_for(n_dirichlet, 256), 256, 0, s>>>(n_dirichlet, dirichlet_nodes, (double *)block6);
+        block_inverse_kernel<double><<<grid_for(n_nodes, 256), 256, 0, s>>>(n_nodes, (double *)block6, omega);
+    }
+    return check_launch("sfem_gb300_block3_invert");
+}
+
+extern "C" int sfem_gb300_block3_apply(int real_type, ptrdiff_t n_nodes, const void *block6, const void *r, void *x,
+                                       void *stream) {
+    const cudaStream_t s = stream_of(stream);
+    if (n_nodes <= 0) return SFEM_GB300_SUCCESS;
+    if (real_type == SFEM_GB300_FLOAT32)
+        block_apply_kernel<float><<<grid_for(n_nodes, 256), 256, 0, s>>>(n_nodes, (const float *)block6,
+                                                                         (const float *)r, (float *)x);
+    else
+        block_apply_kernel<double><<<grid_for(n_nodes, 256), 256, 0, s>>>(n_nodes, (const double *)block6,
+                                                                          (const double *)r, (double *)x);
+    return check_launch("sfem_gb300_block3_apply");
+}

@@ -1,0 +1,630 @@
+// C ABI object layer over the device solver templates: operators (Laplacian,
+// linear elasticity, transfer), smoothers and solvers as opaque handles, composed
+// the way the reference's frontend composes them (frontend/sfem_API.hpp:
+// create_cg :143, create_shiftable_jacobi :180, create_stationary :247,
+// create_cheb3 :287, create_mg :323, create_hierarchical_prolongation :409,
+// create_hierarchical_restriction :575) and as drivers/mgsolve.cpp:128-330 uses them.
+#include <cstdarg>
+#include <cstring>
+#include <memory>
+#include <string>
+
+#include "common.cuh"
+#include "solvers.hpp"
+
+namespace sfem_gb300 {
+
+struct Handle {
+    int real_type{SFEM_GB300_FLOAT64};
+    std::string kind;
+    std::shared_ptr<Context> ctx;
+    std::shared_ptr<Operator<double>> d;
+    std::shared_ptr<Operator<float>> f;
+    // typed views for kind-specific calls
+    std::shared_ptr<void> impl;
+    ptrdiff_t rows() const { return d ? d->rows() : (f ? f->rows() : 0); }
+    ptrdiff_t cols() const { return d ? d->cols() : (f ? f->cols() : 0); }
+};
+
+static bool is_f32(int rt) { return rt == SFEM_GB300_FLOAT32; }
+
+// ---------------------------------------------------------------- operators
+
+// Function-level Laplacian: y += A x, then y[c] = x[c] on Dirichlet nodes
+// (Function::apply + copy_constrained_dofs, frontend/sfem_Function.cpp:481-496).
+template <typename T>
+class LaplacianOp final : public Operator<T> {
+public:
+    std::shared_ptr<Context> ctx;
+    int element_type{0};
+    ptrdiff_t nelements{0}, n_nodes{0}, fff_stride{0}, n_dirichlet{0};
+    idx_t **elements{nullptr};
+    const float *fff{nullptr};
+    const idx_t *dirichlet{nullptr};
+    int apply(const T *x, T *y) override {
+        SFEM_GB300_CHECK(cu_laplacian_apply(element_type, nelements, elements, fff_stride, fff, real_type_v<T>, x, y,
+                                            ctx->sp()));
+        return sfem_gb300_constraint_nodes_copy(real_type_v<T>, n_dirichlet, dirichlet, 1, 0, x, y, ctx->sp());
+    }
+    ptrdiff_t rows() const override { return n_nodes; }
+    ptrdiff_t cols() const override { return n_nodes; }
+};
+
+// Function-level linear elasticity (3 dofs per node, interleaved), Dirichlet on all components.
+template <typename T>
+class ElasticityOp final : public Operator<T> {
+public:
+    std::shared_ptr<Context> ctx;
+    int element_type{0};
+    ptrdiff_t nelements{0}, n_nodes{0}, jac_stride{0}, n_dirichlet{0};
+    idx_t **elements{nullptr};
+    const float *adjugate{nullptr}, *determinant{nullptr};
+    double mu{1}, lambda{1};
+    const idx_t *dirichlet{nullptr};
+    int apply(const T *x, T *y) override {
+        SFEM_GB300_CHECK(sfem_gb300_linear_elasticity_apply(element_type, nelements, elements, jac_stride, adjugate,
+                                                            determinant, mu, lambda, real_type_v<T>, x, y, ctx->sp()));
+        for (int c = 0; c < 3; c++)
+            SFEM_GB300_CHECK(
+                    sfem_gb300_constraint_nodes_copy(real_type_v<T>, n_dirichlet, dirichlet, 3, c, x, y, ctx->sp()));
+        return 0;
+    }
+    ptrdiff_t rows() const override { return 3 * n_nodes; }
+    ptrdiff_t cols() const override { return 3 * n_nodes; }
+};
+
+// Prolongation (overwrites y) followed by zeroing the fine Dirichlet dofs
+// (algebra/mg/sfem_GeometricMultigrid.cpp:54-66).
+template <typename T>
+class ProlongationOp final : public Operator<T> {
+public:
+    std::shared_ptr<Context> ctx;
+    ptrdiff_t nelements{0}, n_from{0}, n_to{0}, n_dirichlet{0};
+    int from_level{0}, to_level{0}, vec{1};
+    idx_t **from_elements{nullptr}, **to_elements{nullptr};
+    const idx_t *dirichlet{nullptr};
+    int apply(const T *x, T *y) override {
+        SFEM_GB300_CHECK(sfem_gb300_sshex8_prolongate(nelements, from_level, from_elements, to_level, to_elements, vec,
+                                                      real_type_v<T>, x, y, ctx->sp()));
+        for (int c = 0; c < vec; c++)
+            SFEM_GB300_CHECK(
+                    sfem_gb300_constraint_nodes_to_value(real_type_v<T>, n_dirichlet, dirichlet, vec, c, 0.0, y, ctx->sp()));
+        return 0;
+    }
+    ptrdiff_t rows() const override { return vec * n_to; }
+    ptrdiff_t cols() const override { return vec * n_from; }
+    bool overwrites_output() const override { return true; }
+};
+
+// Restriction (accumulates into y) followed by zeroing the coarse Dirichlet dofs
+// (algebra/mg/sfem_GeometricMultigrid.cpp:38-52).
+template <typename T>
+class RestrictionOp final : public Operator<T> {
+public:
+    std::shared_ptr<Context> ctx;
+    ptrdiff_t nelements{0}, n_from{0}, n_to{0}, n_dirichlet{0};
+    int from_level{0}, to_level{0}, vec{1};
+    idx_t **from_elements{nullptr}, **to_elements{nullptr};
+    const uint16_t *count{nullptr};
+    const idx_t *dirichlet{nullptr};
+    int apply(const T *x, T *y) override {
+        SFEM_GB300_CHECK(sfem_gb300_sshex8_restrict(nelements, from_level, from_elements, count, to_level, to_elements,
+                                                    vec, real_type_v<T>, x, y, ctx->sp()));
+        for (int c = 0; c < vec; c++)
+            SFEM_GB300_CHECK(
+                    sfem_gb300_constraint_nodes_to_value(real_type_v<T>, n_dirichlet, dirichlet, vec, c, 0.0, y, ctx->sp()));
+        return 0;
+    }
+    ptrdiff_t rows() const override { return vec * n_to; }
+    ptrdiff_t cols() const override { return vec * n_from; }
+};
+
+template <typename T>
+std::shared_ptr<Operator<T>> &op_of(Handle *h);
+template <>
+std::shared_ptr<Operator<double>> &op_of<double>(Handle *h) {
+    return h->d;
+}
+template <>
+std::shared_ptr<Operator<float>> &op_of<float>(Handle *h) {
+    return h->f;
+}
+
+template <typename T>
+Blas<T> blas_of(const std::shared_ptr<Context> &ctx) {
+    Blas<T> b;
+    b.ctx = ctx;
+    return b;
+}
+
+// Iterative refinement (no reference counterpart): outer loop in double with the
+// double operator, inner solve in float on the normalised residual.
+//   r = b - A x ; d = inner(r / |r|) ; x += |r| d ; until |r| <= rtol |b|.
+class IterativeRefinement final : public Solver<double> {
+public:
+    std::shared_ptr<Context> ctx;
+    std::shared_ptr<Operator<double>> op;
+    std::shared_ptr<Operator<float>> inner;
+    DeviceBuffer<double> r;
+    DeviceBuffer<float> r32, d32;
+    int max_it{50};
+    double rtol{1e-10}, atol{0};
+    double last_rel{0};
+    double *s{nullptr};
+    int apply(const double *b, double *x) override {
+        const ptrdiff_t n = op->rows();
+        if (!s) s = ctx->slots(2);
+        SFEM_GB300_CHECK(r.resize(n));
+        SFEM_GB300_CHECK(r32.resize(n));
+        SFEM_GB300_CHECK(d32.resize(n));
+        Blas<double> bd = blas_of<double>(ctx);
+        bd.norm2(n, b, &s[1]);
+        const double bnorm = ctx->read(&s[1]);
+        for (this->iterations_ = 0;; this->iterations_++) {
+            bd.zeros(n, r.ptr);
+            SFEM_GB300_CHECK(op->apply(x, r.ptr));
+            bd.axpby(n, 1.0, b, -1.0, r.ptr);
+            bd.norm2(n, r.ptr, &s[0]);
+            const double rnorm = ctx->read(&s[0]);
+            last_rel = bnorm > 0 ? rnorm / bnorm : rnorm;
+            if (rnorm <= rtol * bnorm || rnorm <= atol || rnorm == 0) return 0;
+            if (!std::isfinite(rnorm)) return set_error("IterativeRefinement: non-finite residual");
+            if (this->iterations_ >= max_it) return set_error("IterativeRefinement: no convergence (rel %g)", last_rel);
+            bd.scal(n, 1.0 / rnorm, r.ptr);
+            SFEM_GB300_CHECK(sfem_gb300_convert(n, SFEM_GB300_FLOAT64, r.ptr, SFEM_GB300_FLOAT32, r32.ptr, ctx->sp()));
+            cudaMemsetAsync(d32.ptr, 0, n * sizeof(float), ctx->stream);
+            inner->apply(r32.ptr, d32.ptr);  // inner may stop at its own max_it: refinement absorbs it
+            SFEM_GB300_CHECK(sfem_gb300_axpy_f32_to_f64(n, rnorm, d32.ptr, x, ctx->sp()));
+        }
+    }
+    ptrdiff_t rows() const override { return op->rows(); }
+    ptrdiff_t cols() const override { return op->cols(); }
+};
+
+}  // namespace sfem_gb300
+
+using namespace sfem_gb300;
+
+typedef Handle sfem_gb300_handle;
+
+#define H(p) reinterpret_cast<Handle *>(p)
+
+extern "C" {
+
+int sfem_gb300_context_create(void *stream, void **out) {
+    cudaStream_t s = stream_of(stream);
+    auto ctx = Context::create(s);
+    if (!ctx) return set_error("sfem_gb300_context_create: allocation failed");
+    auto *h = new Handle();
+    h->kind = "context";
+    h->ctx = ctx;
+    *out = h;
+    return SFEM_GB300_SUCCESS;
+}
+
+int sfem_gb300_handle_destroy(void *handle) {
+    delete H(handle);
+    return SFEM_GB300_SUCCESS;
+}
+
+int sfem_gb300_laplacian_op_create(void *context, int real_type, int element_type, ptrdiff_t nelements,
+                                   idx_t **elements, ptrdiff_t fff_stride, const float *fff, ptrdiff_t n_nodes,
+                                   ptrdiff_t n_dirichlet, const int32_t *dirichlet_nodes, void **out) {
+    auto *c = H(context);
+    auto *h = new Handle();
+    h->kind = "laplacian";
+    h->ctx = c->ctx;
+    h->real_type = is_f32(real_type) ? SFEM_GB300_FLOAT32 : SFEM_GB300_FLOAT64;
+    auto fill = [&](auto op) {
+        op->ctx = c->ctx;
+        op->element_type = element_type;
+        op->nelements = nelements;
+        op->elements = elements;
+        op->fff_stride = fff_stride;
+        op->fff = fff;
+        op->n_nodes = n_nodes;
+        op->n_dirichlet = n_dirichlet;
+        op->dirichlet = dirichlet_nodes;
+    };
+    if (is_f32(real_type)) {
+        auto op = std::make_shared<LaplacianOp<float>>();
+        fill(op);
+        h->f = op;
+    } else {
+        auto op = std::make_shared<LaplacianOp<double>>();
+        fill(op);
+        h->d = op;
+    }
+    *out = h;
+    return SFEM_GB300_SUCCESS;
+}
+
+int sfem_gb300_elasticity_op_create(void *context, int real_type, int element_type, ptrdiff_t nelements,
+                                    idx_t **elements, ptrdiff_t jacobian_stride, const float *adjugate,
+                                    const float *determinant, double mu, double lambda, ptrdiff_t n_nodes,
+                                    ptrdiff_t n_dirichlet, const int32_t *dirichlet_nodes, void **out) {
+    auto *c = H(context);
+    auto *h = new Handle();
+    h->kind = "elasticity";
+    h->ctx = c->ctx;
+    h->real_type = is_f32(real_type) ? SFEM_GB300_FLOAT32 : SFEM_GB300_FLOAT64;
+    auto fill = [&](auto op) {
+        op->ctx = c->ctx;
+        op->element_type = element_type;
+        op->nelements = nelements;
+        op->elements = elements;
+        op->jac_stride = jacobian_stride;
+        op->adjugate = adjugate;
+        op->determinant = determinant;
+        op->mu = mu;
+        op->lambda = lambda;
+        op->n_nodes = n_nodes;
+        op->n_dirichlet = n_dirichlet;
+        op->dirichlet = dirichlet_nodes;
+    };
+    if (is_f32(real_type)) {
+        auto op = std::make_shared<ElasticityOp<float>>();
+        fill(op);
+        h->f = op;
+    } else {
+        auto op = std::make_shared<ElasticityOp<double>>();
+        fill(op);
+        h->d = op;
+    }
+    *out = h;
+    return SFEM_GB300_SUCCESS;
+}
+
+int sfem_gb300_prolongation_op_create(void *context, int real_type, ptrdiff_t nelements, int from_level,
+                                      idx_t **from_elements, ptrdiff_t n_from, int to_level, idx_t **to_elements,
+                                      ptrdiff_t n_to, int vec_size, ptrdiff_t n_dirichlet_to,
+                                      const int32_t *dirichlet_to, void **out) {
+    auto *c = H(context);
+    auto *h = new Handle();
+    h->kind = "prolongation";
+    h->ctx = c->ctx;
+    h->real_type = is_f32(real_type) ? SFEM_GB300_FLOAT32 : SFEM_GB300_FLOAT64;
+    auto fill = [&](auto op) {
+        op->ctx = c->ctx;
+        op->nelements = nelements;
+        op->from_level = from_level;
+        op->from_elements = from_elements;
+        op->n_from = n_from;
+        op->to_level = to_level;
+        op->to_elements = to_elements;
+        op->n_to = n_to;
+        op->vec = vec_size;
+        op->n_dirichlet = n_dirichlet_to;
+        op->dirichlet = dirichlet_to;
+    };
+    if (is_f32(real_type)) {
+        auto op = std::make_shared<ProlongationOp<float>>();
+        fill(op);
+        h->f = op;
+    } else {
+        auto op = std::make_shared<ProlongationOp<double>>();
+        fill(op);
+        h->d = op;
+    }
+    *out = h;
+    return SFEM_GB300_SUCCESS;
+}
+
+int sfem_gb300_restriction_op_create(void *context, int real_type, ptrdiff_t nelements, int from_level,
+                                     idx_t **from_elements, const uint16_t *count, ptrdiff_t n_from, int to_level,
+                                     idx_t **to_elements, ptrdiff_t n_to, int vec_size, ptrdiff_t n_dirichlet_to,
+                                     const int32_t *dirichlet_to, void **out) {
+    auto *c = H(context);
+    auto *h = new Handle();
+    h->kind = "restriction";
+    h->ctx = c->ctx;
+    h->real_type = is_f32(real_type) ? SFEM_GB300_FLOAT32 : SFEM_GB300_FLOAT64;
+    auto fill = [&](auto op) {
+        op->ctx = c->ctx;
+        op->nelements = nelements;
+        op->from_level = from_level;
+        op->from_elements = from_elements;
+        op->count = count;
+        op->n_from = n_from;
+        op->to_level = to_level;
+        op->to_elements = to_elements;
+        op->n_to = n_to;
+        op->vec = vec_size;
+        op->n_dirichlet = n_dirichlet_to;
+        op->dirichlet = dirichlet_to;
+    };
+    if (is_f32(real_type)) {
+        auto op = std::make_shared<RestrictionOp<float>>();
+        fill(op);
+        h->f = op;
+    } else {
+        auto op = std::make_shared<RestrictionOp<double>>();
+        fill(op);
+        h->d = op;
+    }
+    *out = h;
+    return SFEM_GB300_SUCCESS;
+}
+
+int sfem_gb300_op_apply(void *op, const void *x, void *y) {
+    auto *h = H(op);
+    if (h->d) return h->d->apply((const double *)x, (double *)y);
+    if (h->f) return h->f->apply((const float *)x, (float *)y);
+    return set_error("sfem_gb300_op_apply: handle of kind '%s' is not an operator", h->kind.c_str());
+}
+
+int sfem_gb300_op_size(void *op, ptrdiff_t *rows, ptrdiff_t *cols) {
+    auto *h = H(op);
+    *rows = h->rows();
+    *cols = h->cols();
+    return SFEM_GB300_SUCCESS;
+}
+
+int sfem_gb300_jacobi_create(void *context, int real_type, ptrdiff_t n, const void *diag, double relaxation,
+                             void **out) {
+    auto *c = H(context);
+    auto *h = new Handle();
+    h->kind = "jacobi";
+    h->ctx = c->ctx;
+    h->real_type = is_f32(real_type) ? SFEM_GB300_FLOAT32 : SFEM_GB300_FLOAT64;
+    int rc;
+    if (is_f32(real_type)) {
+        auto j = std::make_shared<Jacobi<float>>();
+        j->blas = blas_of<float>(c->ctx);
+        j->relaxation = relaxation;
+        rc = j->set_diag((const float *)diag, n);
+        h->f = j;
+    } else {
+        auto j = std::make_shared<Jacobi<double>>();
+        j->blas = blas_of<double>(c->ctx);
+        j->relaxation = relaxation;
+        rc = j->set_diag((const double *)diag, n);
+        h->d = j;
+    }
+    *out = h;
+    return rc;
+}
+
+int sfem_gb300_block_jacobi_create(void *context, int real_type, ptrdiff_t n_nodes, const void *inv_block6,
+                                   void **out) {
+    auto *c = H(context);
+    auto *h = new Handle();
+    h->kind = "block_jacobi";
+    h->ctx = c->ctx;
+    h->real_type = is_f32(real_type) ? SFEM_GB300_FLOAT32 : SFEM_GB300_FLOAT64;
+    if (is_f32(real_type)) {
+        auto j = std::make_shared<BlockJacobi<float>>();
+        j->blas = blas_of<float>(c->ctx);
+        j->inv_block6 = (const float *)inv_block6;
+        j->n_nodes = n_nodes;
+        h->f = j;
+    } else {
+        auto j = std::make_shared<BlockJacobi<double>>();
+        j->blas = blas_of<double>(c->ctx);
+        j->inv_block6 = (const double *)inv_block6;
+        j->n_nodes = n_nodes;
+        h->d = j;
+    }
+    *out = h;
+    return SFEM_GB300_SUCCESS;
+}
+
+int sfem_gb300_stationary_create(void *context, void *op, void *precond, int max_it, void **out) {
+    auto *c = H(context);
+    auto *o = H(op), *p = H(precond);
+    auto *h = new Handle();
+    h->kind = "stationary";
+    h->ctx = c->ctx;
+    h->real_type = o->real_type;
+    if (o->f) {
+        auto s = std::make_shared<Stationary<float>>();
+        s->blas = blas_of<float>(c->ctx);
+        s->op = o->f;
+        s->precond = p->f;
+        s->max_it = max_it;
+        h->f = s;
+    } else {
+        auto s = std::make_shared<Stationary<double>>();
+        s->blas = blas_of<double>(c->ctx);
+        s->op = o->d;
+        s->precond = p->d;
+        s->max_it = max_it;
+        h->d = s;
+    }
+    *out = h;
+    return SFEM_GB300_SUCCESS;
+}
+
+int sfem_gb300_chebyshev3_create(void *context, void *op, int max_it, double scale_eig_max, double scale_eig_min,
+                                 int eigen_max_it, double eigen_tol, void **out) {
+    auto *c = H(context);
+    auto *o = H(op);
+    auto *h = new Handle();
+    h->kind = "chebyshev3";
+    h->ctx = c->ctx;
+    h->real_type = o->real_type;
+    int rc;
+    if (o->f) {
+        auto s = std::make_shared<Chebyshev3<float>>();
+        s->blas = blas_of<float>(c->ctx);
+        s->op = o->f;
+        s->max_it = max_it;
+        s->scale_eig_max = scale_eig_max;
+        s->scale_eig_min = scale_eig_min;
+        s->eigen_max_it = eigen_max_it;
+        s->eigen_tol = eigen_tol;
+        rc = s->init_with_ones();
+        h->f = s;
+        h->impl = s;
+    } else {
+        auto s = std::make_shared<Chebyshev3<double>>();
+        s->blas = blas_of<double>(c->ctx);
+        s->op = o->d;
+        s->max_it = max_it;
+        s->scale_eig_max = scale_eig_max;
+        s->scale_eig_min = scale_eig_min;
+        s->eigen_max_it = eigen_max_it;
+        s->eigen_tol = eigen_tol;
+        rc = s->init_with_ones();
+        h->d = s;
+        h->impl = s;
+    }
+    *out = h;
+    return rc;
+}
+
+int sfem_gb300_chebyshev3_eig_max(void *cheb, double *eig_max) {
+    auto *h = H(cheb);
+    if (h->kind != "chebyshev3") return set_error("not a chebyshev3 handle");
+    if (h->f)
+        *eig_max = std::static_pointer_cast<Chebyshev3<float>>(h->impl)->eig_max;
+    else
+        *eig_max = std::static_pointer_cast<Chebyshev3<double>>(h->impl)->eig_max;
+    return SFEM_GB300_SUCCESS;
+}
+
+int sfem_gb300_chebyshev3_set_eig_max(void *cheb, double eig_max) {
+    auto *h = H(cheb);
+    if (h->kind != "chebyshev3") return set_error("not a chebyshev3 handle");
+    if (h->f)
+        std::static_pointer_cast<Chebyshev3<float>>(h->impl)->eig_max = eig_max;
+    else
+        std::static_pointer_cast<Chebyshev3<double>>(h->impl)->eig_max = eig_max;
+    return SFEM_GB300_SUCCESS;
+}
+
+int sfem_gb300_cg_create(void *context, void *op, void *precond, int max_it, double rtol, double atol, void **out) {
+    auto *c = H(context);
+    auto *o = H(op);
+    auto *p = precond ? H(precond) : nullptr;
+    auto *h = new Handle();
+    h->kind = "cg";
+    h->ctx = c->ctx;
+    h->real_type = o->real_type;
+    if (o->f) {
+        auto s = std::make_shared<ConjugateGradient<float>>();
+        s->blas = blas_of<float>(c->ctx);
+        s->op = o->f;
+        if (p) s->precond = p->f;
+        s->max_it = max_it;
+        s->rtol = rtol;
+        s->atol = atol;
+        h->f = s;
+        h->impl = s;
+    } else {
+        auto s = std::make_shared<ConjugateGradient<double>>();
+        s->blas = blas_of<double>(c->ctx);
+        s->op = o->d;
+        if (p) s->precond = p->d;
+        s->max_it = max_it;
+        s->rtol = rtol;
+        s->atol = atol;
+        h->d = s;
+        h->impl = s;
+    }
+    *out = h;
+    return SFEM_GB300_SUCCESS;
+}
+
+int sfem_gb300_mg_create(void *context, int real_type, int max_it, int cycle_type, void **out) {
+    auto *c = H(context);
+    auto *h = new Handle();
+    h->kind = "mg";
+    h->ctx = c->ctx;
+    h->real_type = is_f32(real_type) ? SFEM_GB300_FLOAT32 : SFEM_GB300_FLOAT64;
+    if (is_f32(real_type)) {
+        auto m = std::make_shared<Multigrid<float>>();
+        m->blas = blas_of<float>(c->ctx);
+        m->max_it = max_it;
+        m->cycle_type = cycle_type;
+        h->f = m;
+        h->impl = m;
+    } else {
+        auto m = std::make_shared<Multigrid<double>>();
+        m->blas = blas_of<double>(c->ctx);
+        m->max_it = max_it;
+        m->cycle_type = cycle_type;
+        h->d = m;
+        h->impl = m;
+    }
+    *out = h;
+    return SFEM_GB300_SUCCESS;
+}
+
+// Levels are added finest first; prolongation maps the next coarser level to this one,
+// restriction maps this level to the next coarser one (both NULL on the coarsest level).
+int sfem_gb300_mg_add_level(void *mg, void *op, void *smoother, void *prolongation, void *restriction) {
+    auto *h = H(mg);
+    if (h->kind != "mg") return set_error("sfem_gb300_mg_add_level: not a multigrid handle");
+    auto *o = H(op), *s = H(smoother);
+    auto *p = prolongation ? H(prolongation) : nullptr, *r = restriction ? H(restriction) : nullptr;
+    if (h->f) {
+        auto m = std::static_pointer_cast<Multigrid<float>>(h->impl);
+        m->add_level(o->f, s->f, p ? p->f : nullptr, r ? r->f : nullptr);
+    } else {
+        auto m = std::static_pointer_cast<Multigrid<double>>(h->impl);
+        m->add_level(o->d, s->d, p ? p->d : nullptr, r ? r->d : nullptr);
+    }
+    return SFEM_GB300_SUCCESS;
+}
+
+int sfem_gb300_ir_create(void *context, void *op64, void *inner32, int max_it, double rtol, void **out) {
+    auto *c = H(context);
+    auto *o = H(op64), *in = H(inner32);
+    if (!o->d || !in->f) return set_error("sfem_gb300_ir_create: needs a double operator and a float inner solver");
+    auto *h = new Handle();
+    h->kind = "ir";
+    h->ctx = c->ctx;
+    h->real_type = SFEM_GB300_FLOAT64;
+    auto s = std::make_shared<IterativeRefinement>();
+    s->ctx = c->ctx;
+    s->op = o->d;
+    s->inner = in->f;
+    s->max_it = max_it;
+    s->rtol = rtol;
+    h->d = s;
+    h->impl = s;
+    *out = h;
+    return SFEM_GB300_SUCCESS;
+}
+
+int sfem_gb300_solver_apply(void *solver, const void *b, void *x) { return sfem_gb300_op_apply(solver, b, x); }
+
+int sfem_gb300_solver_stats(void *solver, int *iterations, double *last_relative) {
+    auto *h = H(solver);
+    *iterations = 0;
+    if (last_relative) *last_relative = 0;
+    if (h->kind == "cg") {
+        if (h->f) {
+            auto s = std::static_pointer_cast<ConjugateGradient<float>>(h->impl);
+            *iterations = s->iterations_;
+            if (last_relative) *last_relative = s->last_rel;
+        } else {
+            auto s = std::static_pointer_cast<ConjugateGradient<double>>(h->impl);
+            *iterations = s->iterations_;
+            if (last_relative) *last_relative = s->last_rel;
+        }
+    } else if (h->kind == "ir") {
+        auto s = std::static_pointer_cast<IterativeRefinement>(h->impl);
+        *iterations = s->iterations_;
+        if (last_relative) *last_relative = s->last_rel;
+    } else if (h->kind == "mg") {
+        if (h->f)
+            *iterations = std::static_pointer_cast<Multigrid<float>>(h->impl)->iterations_;
+        else
+            *iterations = std::static_pointer_cast<Multigrid<double>>(h->impl)->iterations_;
+    }
+    return SFEM_GB300_SUCCESS;
+}
+
+int sfem_gb300_cg_set_verbose(void *solver, int verbose) {
+    auto *h = H(solver);
+    if (h->kind != "cg") return set_error("not a cg handle");
+    if (h->f)
+        std::static_pointer_cast<ConjugateGradient<float>>(h->impl)->verbose = verbose;
+    else
+        std::static_pointer_cast<ConjugateGradient<double>>(h->impl)->verbose = verbose;
+    return SFEM_GB300_SUCCESS;
+}
+
+}  // extern "C"

@@ -56,6 +56,20 @@ struct DeviceBuffer {
     explicit DeviceBuffer(ptrdiff_t size) { resize(size); }
     DeviceBuffer(const DeviceBuffer &) = delete;
     DeviceBuffer &operator=(const DeviceBuffer &) = delete;
+    DeviceBuffer(DeviceBuffer &&o) noexcept : ptr(o.ptr), n(o.n) {
+        o.ptr = nullptr;
+        o.n = 0;
+    }
+    DeviceBuffer &operator=(DeviceBuffer &&o) noexcept {
+        if (this != &o) {
+            release();
+            ptr = o.ptr;
+            n = o.n;
+            o.ptr = nullptr;
+            o.n = 0;
+        }
+        return *this;
+    }
     ~DeviceBuffer() { release(); }
     void release() {
         if (ptr) cudaFree(ptr);
@@ -294,6 +308,21 @@ public:
     int apply(const T *b, T *x) override { return blas.xypaz(inv_diag.n, inv_diag.ptr, b, T(1), x); }
     ptrdiff_t rows() const override { return inv_diag.n; }
     ptrdiff_t cols() const override { return inv_diag.n; }
+};
+
+// ShiftableBlockSymJacobi (algebra/sfem_ShiftableJacobi.hpp:67-155): x += B b with
+// pre-inverted symmetric 3x3 blocks (6 per node).
+template <typename T>
+class BlockJacobi final : public Solver<T> {
+public:
+    Blas<T> blas;
+    const T *inv_block6{nullptr};
+    ptrdiff_t n_nodes{0};
+    int apply(const T *b, T *x) override {
+        return sfem_gb300_block3_apply(real_type_v<T>, n_nodes, inv_block6, b, x, blas.ctx->sp());
+    }
+    ptrdiff_t rows() const override { return 3 * n_nodes; }
+    ptrdiff_t cols() const override { return 3 * n_nodes; }
 };
 
 // StationaryIteration (algebra/sfem_Stationary.hpp:19-133): x += P (b - A x), max_it sweeps.

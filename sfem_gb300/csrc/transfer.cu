@@ -1,0 +1,159 @@
+// Multigrid transfer between nested sshex8 levels (and the sshex8 -> hex8 step).
+//
+// Prolongation (sshex8_prolongate, operators/sshex8/sshex8_interpolate.cpp:259-558;
+// sshex8_hierarchical_prolongation, :129-237): inside each macro element the
+// fine-level values are the trilinear interpolation of the coarse-level values;
+// the output is overwritten (shared nodes receive identical values from every
+// element: the same face corners are summed in the same order).
+//
+// Restriction (sshex8_restrict, :633-760; sshex8_hierarchical_restriction, :12-127):
+// R = P^T, with the fine input divided by the element-node incidence count
+// (sshex8_element_node_incidence_count, :239-257) so that nodes shared by several
+// macro elements are counted once; output accumulated with atomics.
+//
+// One thread per (target node of a macro element, macro element), element index
+// fastest so that the SoA connectivity reads elements[v][e] are coalesced.
+#include "common.cuh"
+
+namespace sfem_gb300 {
+
+// P: to[gid(e, fine lidx)] = sum_c w_c from[gid(e, coarse corner c)]
+template <typename T>
+__global__ void prolongate_kernel(ptrdiff_t nelements, int from_level, const idx_t *const *from_elements, int to_level,
+                                  const idx_t *const *to_elements, int vec_size, const T *__restrict__ from,
+                                  T *__restrict__ to) {
+    const int nf = to_level + 1;
+    const int s = to_level / from_level;
+    const ptrdiff_t total = nelements * (ptrdiff_t)(nf * nf * nf);
+    for (ptrdiff_t t = blockIdx.x * (ptrdiff_t)blockDim.x + threadIdx.x; t < total; t += (ptrdiff_t)gridDim.x * blockDim.x) {
+        const ptrdiff_t e = t % nelements;
+        const int v = (int)(t / nelements);
+        const int xi = v % nf, yi = (v / nf) % nf, zi = v / (nf * nf);
+        const int cx = min(xi / s, from_level - 1), cy = min(yi / s, from_level - 1), cz = min(zi / s, from_level - 1);
+        const T tx = T(xi - cx * s) / T(s), ty = T(yi - cy * s) / T(s), tz = T(zi - cz * s) / T(s);
+        const ptrdiff_t gid = to_elements[v][e];
+        T acc[3] = {0, 0, 0};
+#pragma unroll
+        for (int c = 0; c < 8; c++) {
+            const T w = (c8x(c) ? tx : T(1) - tx) * (c8y(c) ? ty : T(1) - ty) * (c8z(c) ? tz : T(1) - tz);
+            if (w == T(0)) continue;
+            const ptrdiff_t src = from_elements[lidx(from_level, cx + c8x(c), cy + c8y(c), cz + c8z(c))][e];
+            for (int d = 0; d < vec_size; d++) acc[d] += w * from[src * vec_size + d];
+        }
+        for (int d = 0; d < vec_size; d++) to[gid * vec_size + d] = acc[d];
+    }
+}
+
+// R: to[gid(e, coarse node)] += sum over fine nodes f of this element in the coarse node's
+// support of w(f) from[f] / count[f]
+template <typename T>
+__global__ void restrict_kernel(ptrdiff_t nelements, int from_level, const idx_t *const *from_elements,
+                                const uint16_t *__restrict__ count, int to_level, const idx_t *const *to_elements,
+                                int vec_size, const T *__restrict__ from, T *__restrict__ to) {
+    const int nc = to_level + 1;
+    const int s = from_level / to_level;
+    const ptrdiff_t total = nelements * (ptrdiff_t)(nc * nc * nc);
+    for (ptrdiff_t t = blockIdx.x * (ptrdiff_t)blockDim.x + threadIdx.x; t < total; t += (ptrdiff_t)gridDim.x * blockDim.x) {
+        const ptrdiff_t e = t % nelements;
+        const int v = (int)(t / nelements);
+        const int X = v % nc, Y = (v / nc) % nc, Z = v / (nc * nc);
+        T acc[3] = {0, 0, 0};
+        // fine nodes within one coarse cell of (X,Y,Z), inside the macro element
+        const int x0 = max(0, (X - 1) * s + 1), x1 = min(from_level, (X + 1) * s - 1);
+        const int y0 = max(0, (Y - 1) * s + 1), y1 = min(from_level, (Y + 1) * s - 1);
+        const int z0 = max(0, (Z - 1) * s + 1), z1 = min(from_level, (Z + 1) * s - 1);
+        for (int zi = z0; zi <= z1; zi++) {
+            const T wz = T(1) - T(abs(zi - Z * s)) / T(s);
+            for (int yi = y0; yi <= y1; yi++) {
+                const T wy = T(1) - T(abs(yi - Y * s)) / T(s);
+                for (int xi = x0; xi <= x1; xi++) {
+                    const T wx = T(1) - T(abs(xi - X * s)) / T(s);
+                    const ptrdiff_t f = from_elements[lidx(from_level, xi, yi, zi)][e];
+                    const T w = wx * wy * wz / T(count[f]);
+                    for (int d = 0; d < vec_size; d++) acc[d] += w * from[f * vec_size + d];
+                }
+            }
+        }
+        const ptrdiff_t gid = to_elements[v][e];
+        for (int d = 0; d < vec_size; d++) atomicAdd(&to[gid * vec_size + d], acc[d]);
+    }
+}
+
+__global__ void incidence_count_kernel(ptrdiff_t nelements, int level, const idx_t *const *elements, uint16_t *count) {
+    const int n1 = level + 1;
+    const ptrdiff_t total = nelements * (ptrdiff_t)(n1 * n1 * n1);
+    for (ptrdiff_t t = blockIdx.x * (ptrdiff_t)blockDim.x + threadIdx.x; t < total; t += (ptrdiff_t)gridDim.x * blockDim.x) {
+        const ptrdiff_t e = t % nelements;
+        const int v = (int)(t / nelements);
+        // 16-bit counter: lock-free compare-and-swap increment (always progresses)
+        unsigned short *c = (unsigned short *)(count + elements[v][e]);
+        unsigned short old = *c, seen;
+        while ((seen = atomicCAS(c, old, (unsigned short)(old + 1))) != old) old = seen;
+    }
+}
+
+template <typename T>
+static int prolongate_tpl(ptrdiff_t nelements, int from_level, idx_t **from_elements, int to_level,
+                          idx_t **to_elements, int vec_size, const void *from, void *to, cudaStream_t s) {
+    const ptrdiff_t total = nelements * (ptrdiff_t)((to_level + 1) * (to_level + 1) * (to_level + 1));
+    prolongate_kernel<T><<<grid_for(total, 256, kNumSMs * 32), 256, 0, s>>>(
+            nelements, from_level, from_elements, to_level, to_elements, vec_size, (const T *)from, (T *)to);
+    return check_launch("sfem_gb300_sshex8_prolongate");
+}
+
+template <typename T>
+static int restrict_tpl(ptrdiff_t nelements, int from_level, idx_t **from_elements, const uint16_t *count,
+                        int to_level, idx_t **to_elements, int vec_size, const void *from, void *to, cudaStream_t s) {
+    const ptrdiff_t total = nelements * (ptrdiff_t)((to_level + 1) * (to_level + 1) * (to_level + 1));
+    restrict_kernel<T><<<grid_for(total, 256, kNumSMs * 32), 256, 0, s>>>(
+            nelements, from_level, from_elements, count, to_level, to_elements, vec_size, (const T *)from, (T *)to);
+    return check_launch("sfem_gb300_sshex8_restrict");
+}
+
+}  // namespace sfem_gb300
+
+using namespace sfem_gb300;
+
+extern "C" int sfem_gb300_sshex8_prolongate(ptrdiff_t nelements, int from_level, idx_t **from_elements, int to_level,
+                                            idx_t **to_elements, int vec_size, int real_type, const void *from,
+                                            void *to, void *stream) {
+    if (nelements <= 0) return SFEM_GB300_SUCCESS;
+    if (from_level < 1 || to_level < from_level || to_level % from_level)
+        return set_error("sfem_gb300_sshex8_prolongate: nested levels required (to_level %% from_level == 0), got %d -> %d",
+                         from_level, to_level);
+    if (vec_size < 1 || vec_size > 3) return set_error("sfem_gb300_sshex8_prolongate: vec_size must be 1..3");
+    const cudaStream_t s = stream_of(stream);
+    if (real_type == SFEM_GB300_FLOAT32)
+        return prolongate_tpl<float>(nelements, from_level, from_elements, to_level, to_elements, vec_size, from, to, s);
+    if (real_type == SFEM_GB300_FLOAT64 || real_type == SFEM_GB300_REAL_DEFAULT)
+        return prolongate_tpl<double>(nelements, from_level, from_elements, to_level, to_elements, vec_size, from, to, s);
+    return set_error("sfem_gb300_sshex8_prolongate: unsupported real type %d", real_type);
+}
+
+extern "C" int sfem_gb300_sshex8_restrict(ptrdiff_t nelements, int from_level, idx_t **from_elements,
+                                          const uint16_t *from_element_to_node_incidence_count, int to_level,
+                                          idx_t **to_elements, int vec_size, int real_type, const void *from, void *to,
+                                          void *stream) {
+    if (nelements <= 0) return SFEM_GB300_SUCCESS;
+    if (to_level < 1 || from_level < to_level || from_level % to_level)
+        return set_error("sfem_gb300_sshex8_restrict: nested levels required (from_level %% to_level == 0), got %d -> %d",
+                         from_level, to_level);
+    if (vec_size < 1 || vec_size > 3) return set_error("sfem_gb300_sshex8_restrict: vec_size must be 1..3");
+    const cudaStream_t s = stream_of(stream);
+    if (real_type == SFEM_GB300_FLOAT32)
+        return restrict_tpl<float>(nelements, from_level, from_elements, from_element_to_node_incidence_count, to_level,
+                                   to_elements, vec_size, from, to, s);
+    if (real_type == SFEM_GB300_FLOAT64 || real_type == SFEM_GB300_REAL_DEFAULT)
+        return restrict_tpl<double>(nelements, from_level, from_elements, from_element_to_node_incidence_count,
+                                    to_level, to_elements, vec_size, from, to, s);
+    return set_error("sfem_gb300_sshex8_restrict: unsupported real type %d", real_type);
+}
+
+extern "C" int sfem_gb300_sshex8_element_node_incidence_count(int level, ptrdiff_t nelements, idx_t **elements,
+                                                              uint16_t *count, void *stream) {
+    if (nelements <= 0) return SFEM_GB300_SUCCESS;
+    const ptrdiff_t total = nelements * (ptrdiff_t)((level + 1) * (level + 1) * (level + 1));
+    incidence_count_kernel<<<grid_for(total, 256, kNumSMs * 32), 256, 0, stream_of(stream)>>>(nelements, level,
+                                                                                               elements, count);
+    return check_launch("sfem_gb300_sshex8_element_node_incidence_count");
+}
