@@ -70,6 +70,11 @@ def vp(t) -> C.c_void_p:
     return C.c_void_p(t.data_ptr())
 
 
+def c_void(addr: int) -> C.c_void_p:
+    """Raw address as a pointer argument."""
+    return C.c_void_p(int(addr))
+
+
 def i64(v) -> C.c_ssize_t:
     return C.c_ssize_t(int(v))
 

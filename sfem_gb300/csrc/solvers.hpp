@@ -485,7 +485,7 @@ public:
             blas.zeros(nc, C.sol.ptr);
             cycle(l + 1, C.rhs.ptr, C.sol.ptr);
             blas.zeros(n, L.work.ptr);
-            C.prolongation->apply(C.sol.ptr, L.work.ptr);
+            L.prolongation->apply(C.sol.ptr, L.work.ptr);
             blas.axpby(n, T(1), L.work.ptr, T(1), sol);
             L.smoother->apply(rhs, sol);
         }

@@ -1,0 +1,230 @@
+"""Python binding of the device solver object layer (operators, smoothers, CG, multigrid).
+
+Mirrors the reference's frontend composition of a geometric multigrid on a
+semi-structured mesh (``create_gmg_data``, ``algebra/mg/sfem_GeometricMultigrid.cpp:12-167``;
+``drivers/mgsolve.cpp:128-330``): one operator per derefinement level, nested
+prolongation / restriction with Dirichlet zeroing, a smoother per level
+(Chebyshev3 or Jacobi sweeps), a Jacobi-PCG coarse solve, and an outer CG
+preconditioned by one V-cycle.  Every call goes through the C ABI of
+``libsfem_gb300.so``; torch tensors only hold device memory.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import capi
+from .mesh import SSMesh
+from .operators import Laplacian, SSMeshDevice
+
+c_double = C.c_double
+c_int = C.c_int
+
+
+def _lib():
+    return capi.load()
+
+
+class Handle:
+    """Owns one opaque handle of the C ABI (released with sfem_gb300_handle_destroy)."""
+
+    def __init__(self, ptr, keep=()):
+        self.ptr = C.c_void_p(ptr.value if isinstance(ptr, C.c_void_p) else ptr)
+        self.keep = list(keep)
+
+    def __del__(self):
+        try:
+            if self.ptr and self.ptr.value:
+                _lib().sfem_gb300_handle_destroy(self.ptr)
+                self.ptr = C.c_void_p(0)
+        except Exception:
+            pass
+
+
+def _create(fn, *args, keep=()):
+    out = C.c_void_p(0)
+    capi.check(fn(*args, C.byref(out)), fn.__name__)
+    return Handle(out, keep)
+
+
+def context(stream=None) -> Handle:
+    return _create(_lib().sfem_gb300_context_create, stream)
+
+
+def rt_of(dtype) -> int:
+    import torch
+
+    return capi.FLOAT32 if dtype == torch.float32 else capi.FLOAT64
+
+
+def apply(op: Handle, x, y):
+    capi.check(_lib().sfem_gb300_op_apply(op.ptr, capi.vp(x), capi.vp(y)), "sfem_gb300_op_apply")
+    return y
+
+
+def solve(solver: Handle, b, x):
+    rc = _lib().sfem_gb300_solver_apply(solver.ptr, capi.vp(b), capi.vp(x))
+    return rc
+
+
+def stats(solver: Handle):
+    it = c_int(0)
+    rel = c_double(0)
+    _lib().sfem_gb300_solver_stats(solver.ptr, C.byref(it), C.byref(rel))
+    return it.value, rel.value
+
+
+def laplacian_op(ctx, space: SSMeshDevice, fff, dirichlet, dtype) -> Handle:
+    E = space.n_elements
+    return _create(_lib().sfem_gb300_laplacian_op_create, ctx.ptr, c_int(rt_of(dtype)), c_int(space.element_type),
+                   capi.i64(E), space.elements_ptrs.ptr, capi.i64(fff.shape[1]), capi.vp(fff),
+                   capi.i64(space.n_nodes), capi.i64(dirichlet.numel()), capi.vp(dirichlet),
+                   keep=(ctx, space, fff, dirichlet))
+
+
+def elasticity_op(ctx, space: SSMeshDevice, adj, det, mu, lam, dirichlet, dtype) -> Handle:
+    E = space.n_elements
+    return _create(_lib().sfem_gb300_elasticity_op_create, ctx.ptr, c_int(rt_of(dtype)), c_int(space.element_type),
+                   capi.i64(E), space.elements_ptrs.ptr, capi.i64(adj.shape[1]), capi.vp(adj), capi.vp(det),
+                   c_double(mu), c_double(lam), capi.i64(space.n_nodes), capi.i64(dirichlet.numel()),
+                   capi.vp(dirichlet), keep=(ctx, space, adj, det, dirichlet))
+
+
+def prolongation_op(ctx, coarse: SSMeshDevice, fine: SSMeshDevice, vec, dirichlet_fine, dtype) -> Handle:
+    return _create(_lib().sfem_gb300_prolongation_op_create, ctx.ptr, c_int(rt_of(dtype)), capi.i64(fine.n_elements),
+                   c_int(coarse.level), coarse.lidx_ptrs.ptr, capi.i64(coarse.n_nodes), c_int(fine.level),
+                   fine.lidx_ptrs.ptr, capi.i64(fine.n_nodes), c_int(vec), capi.i64(dirichlet_fine.numel()),
+                   capi.vp(dirichlet_fine), keep=(ctx, coarse, fine, dirichlet_fine))
+
+
+def restriction_op(ctx, fine: SSMeshDevice, coarse: SSMeshDevice, vec, dirichlet_coarse, dtype) -> Handle:
+    return _create(_lib().sfem_gb300_restriction_op_create, ctx.ptr, c_int(rt_of(dtype)), capi.i64(fine.n_elements),
+                   c_int(fine.level), fine.lidx_ptrs.ptr, capi.vp(fine.count), capi.i64(fine.n_nodes),
+                   c_int(coarse.level), coarse.lidx_ptrs.ptr, capi.i64(coarse.n_nodes), c_int(vec),
+                   capi.i64(dirichlet_coarse.numel()), capi.vp(dirichlet_coarse), keep=(ctx, coarse, fine, dirichlet_coarse))
+
+
+def jacobi(ctx, diag, relaxation=1.0) -> Handle:
+    return _create(_lib().sfem_gb300_jacobi_create, ctx.ptr, c_int(rt_of(diag.dtype)), capi.i64(diag.numel()),
+                   capi.vp(diag), c_double(relaxation), keep=(ctx,))
+
+
+def block_jacobi(ctx, inv_block6) -> Handle:
+    return _create(_lib().sfem_gb300_block_jacobi_create, ctx.ptr, c_int(rt_of(inv_block6.dtype)),
+                   capi.i64(inv_block6.numel() // 6), capi.vp(inv_block6), keep=(ctx, inv_block6))
+
+
+def stationary(ctx, op, precond, max_it) -> Handle:
+    return _create(_lib().sfem_gb300_stationary_create, ctx.ptr, op.ptr, precond.ptr, c_int(max_it),
+                   keep=(ctx, op, precond))
+
+
+def chebyshev3(ctx, op, max_it=2, scale_eig_max=1.02, scale_eig_min=0.06, eigen_max_it=100, eigen_tol=1e-5,
+               eig_max=None) -> Handle:
+    h = _create(_lib().sfem_gb300_chebyshev3_create, ctx.ptr, op.ptr, c_int(max_it), c_double(scale_eig_max),
+                c_double(scale_eig_min), c_int(eigen_max_it if eig_max is None else 1), c_double(eigen_tol),
+                keep=(ctx, op))
+    if eig_max is not None:
+        capi.check(_lib().sfem_gb300_chebyshev3_set_eig_max(h.ptr, c_double(eig_max)), "set_eig_max")
+    return h
+
+
+def eig_max(cheb: Handle) -> float:
+    v = c_double(0)
+    capi.check(_lib().sfem_gb300_chebyshev3_eig_max(cheb.ptr, C.byref(v)), "eig_max")
+    return v.value
+
+
+def cg(ctx, op, precond=None, max_it=10000, rtol=1e-10, atol=0.0) -> Handle:
+    return _create(_lib().sfem_gb300_cg_create, ctx.ptr, op.ptr, precond.ptr if precond else None, c_int(max_it),
+                   c_double(rtol), c_double(atol), keep=(ctx, op, precond))
+
+
+def multigrid(ctx, dtype, max_it=1, cycle_type=1) -> Handle:
+    return _create(_lib().sfem_gb300_mg_create, ctx.ptr, c_int(rt_of(dtype)), c_int(max_it), c_int(cycle_type),
+                   keep=(ctx,))
+
+
+def mg_add_level(mg, op, smoother, prolongation=None, restriction=None):
+    capi.check(_lib().sfem_gb300_mg_add_level(mg.ptr, op.ptr, smoother.ptr, prolongation.ptr if prolongation else None,
+                                              restriction.ptr if restriction else None), "mg_add_level")
+    mg.keep += [op, smoother, prolongation, restriction]
+
+
+def iterative_refinement(ctx, op64, inner32, max_it=50, rtol=1e-10) -> Handle:
+    return _create(_lib().sfem_gb300_ir_create, ctx.ptr, op64.ptr, inner32.ptr, c_int(max_it), c_double(rtol),
+                   keep=(ctx, op64, inner32))
+
+
+# ---------------------------------------------------------------------------
+# hierarchy builders
+# ---------------------------------------------------------------------------
+class Hierarchy:
+    """Device data of every derefinement level of an :class:`SSMesh` (shared by both precisions)."""
+
+    def __init__(self, mesh: SSMesh, dirichlet_faces=("x0",), device="cuda:0", vec=1, coefficient=None):
+        import torch
+
+        self.mesh = mesh
+        self.vec = vec
+        self.device = torch.device(device)
+        self.spaces = [SSMeshDevice(mesh, l, device=self.device) for l in mesh.levels]
+        for sp in self.spaces:
+            lid = mesh.elements(sp.level)
+            sp.lidx_elements = torch.from_numpy(np.ascontiguousarray(lid)).to(self.device)
+            sp.lidx_ptrs = capi.DevicePtrArray(sp.lidx_elements)
+            cnt = np.bincount(lid.reshape(-1), minlength=mesh.n_nodes(sp.level)).astype(np.uint16)
+            sp.count = torch.from_numpy(cnt.view(np.int16)).to(self.device)
+        self.dirichlet = [sp.dirichlet_nodes(dirichlet_faces) if dirichlet_faces else
+                          torch.zeros(0, dtype=torch.int32, device=self.device) for sp in self.spaces]
+        # geometry shared by all levels (one metric / adjugate per macro element)
+        lap = Laplacian(self.spaces[0], coefficient=coefficient).initialize()
+        self.fff = lap.fff
+        E = mesh.n_elements
+        self.adj = torch.empty((9, E), dtype=torch.float32, device=self.device)
+        self.det = torch.empty(E, dtype=torch.float32, device=self.device)
+        sp = self.spaces[0]
+        capi.check(capi.load().sfem_gb300_hex8_adjugate_fill(capi.i64(E), sp.corners_ptrs.ptr, sp.points_ptrs.ptr,
+                                                            capi.i64(E), capi.vp(self.adj), capi.vp(self.det), None),
+                   "adjugate_fill")
+
+    def n_dofs(self, k=0):
+        return self.vec * self.spaces[k].n_nodes
+
+
+def build_poisson_mg(ctx, H: Hierarchy, dtype, smoother="chebyshev3", sweeps=2, coarse_rtol=1e-6, coarse_max_it=10000,
+                     eig_max=None, jacobi_sweeps=3):
+    """Geometric multigrid for the Laplacian on every level of ``H`` (one V-cycle per apply)."""
+    import torch
+
+    ops, smoothers, Ps, Rs = [], [], [], []
+    nlev = len(H.spaces)
+    eigs = []
+    for k, sp in enumerate(H.spaces):
+        op = laplacian_op(ctx, sp, H.fff, H.dirichlet[k], dtype)
+        ops.append(op)
+        lap = Laplacian(sp).set_fff(H.fff)
+        diag = torch.zeros(sp.n_nodes, dtype=dtype, device=H.device)
+        lap.hessian_diag(diag)
+        diag[H.dirichlet[k].long()] = 1
+        if k == nlev - 1:
+            jac = jacobi(ctx, diag, 1.0)
+            smoothers.append(cg(ctx, op, jac, max_it=coarse_max_it, rtol=coarse_rtol))
+        elif smoother == "chebyshev3":
+            em = None if eig_max is None else eig_max[k]
+            ch = chebyshev3(ctx, op, max_it=sweeps, eig_max=em)
+            eigs.append(globals()["eig_max"](ch))
+            smoothers.append(ch)
+        else:
+            jac = jacobi(ctx, diag, 1.0)
+            smoothers.append(stationary(ctx, op, jac, jacobi_sweeps))
+    mg = multigrid(ctx, dtype)
+    for k in range(nlev):
+        P = prolongation_op(ctx, H.spaces[k + 1], H.spaces[k], 1, H.dirichlet[k], dtype) if k + 1 < nlev else None
+        R = restriction_op(ctx, H.spaces[k], H.spaces[k + 1], 1, H.dirichlet[k + 1], dtype) if k + 1 < nlev else None
+        mg_add_level(mg, ops[k], smoothers[k], P, R)
+    mg.keep += [H]
+    mg.eigs = eigs
+    return mg, ops[0]

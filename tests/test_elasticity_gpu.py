@@ -1,0 +1,102 @@
+"""GPU parity of the matrix-free linear-elasticity operator against the CPU oracle."""
+
+import numpy as np
+import pytest
+
+import oracle as O
+from sfem_gb300 import capi
+from sfem_gb300.mesh import SSMesh
+from sfem_gb300.operators import SSMeshDevice
+
+pytestmark = pytest.mark.gpu
+MU, LAM = 1.0, 10.0
+
+
+def _setup(cuda, L, n=(3, 2, 2), seed=0):
+    import torch
+
+    m = SSMesh(*n, L, box=((0, 4), (0, 1), (0, 1)), perturb=0.1, seed=seed)
+    sp = SSMeshDevice(m, L, device=cuda)
+    el = m.hex8_elements() if L == 1 else m.elements(L)
+    corners = el if L == 1 else el[m.macro_corner_lidx(L)]
+    adj, det = O.adjugate_fill(corners, m.points)
+    adj_d = torch.from_numpy(adj.T.copy()).to(cuda)
+    det_d = torch.from_numpy(det.copy()).to(cuda)
+    return m, sp, el, adj, det, adj_d, det_d
+
+
+def _scale(L, el, adj, det, u):
+    # row scale (|K| |u|) bounded via the oracle on |u| plus the block-diagonal magnitude
+    a = np.abs(O.linear_elasticity_apply(L if L > 1 else 0, el, adj, det, MU, LAM, np.abs(u)))
+    d3, _ = O.linear_elasticity_block_diag(L if L > 1 else 0, el, adj, det, MU, LAM, u.size // 3)
+    return a + 4 * np.abs(d3) * np.abs(u)
+
+
+@pytest.mark.parametrize("L", [1, 2, 3, 4])
+def test_elasticity_apply_fp64(cuda, L):
+    import torch
+
+    m, sp, el, adj, det, adj_d, det_d = _setup(cuda, L)
+    n = m.n_nodes(L)
+    rng = np.random.default_rng(L)
+    u = rng.standard_normal(3 * n)
+    y0 = rng.standard_normal(3 * n)
+    ref = O.linear_elasticity_apply(L if L > 1 else 0, el, adj, det, MU, LAM, u, out=y0.copy())
+    yd = torch.from_numpy(y0).to(cuda)
+    capi.check(capi.load().sfem_gb300_linear_elasticity_apply(sp.element_type, capi.i64(m.n_elements),
+                                                              sp.elements_ptrs.ptr, capi.i64(m.n_elements),
+                                                              capi.vp(adj_d), capi.vp(det_d), ctypes_d(MU),
+                                                              ctypes_d(LAM), capi.FLOAT64,
+                                                              capi.vp(torch.from_numpy(u).to(cuda)), capi.vp(yd), None),
+               "elasticity apply")
+    err = np.abs(yd.cpu().numpy() - ref) / (_scale(L, el, adj, det, u) + np.abs(y0))
+    assert err.max() < 1e-13, err.max()
+
+
+def ctypes_d(v):
+    import ctypes
+
+    return ctypes.c_double(v)
+
+
+def test_elasticity_reference_signature_and_fp32(cuda):
+    import torch
+
+    L = 4
+    m, sp, el, adj, det, adj_d, det_d = _setup(cuda, L, seed=3)
+    n = m.n_nodes(L)
+    u = np.random.default_rng(5).standard_normal(3 * n)
+    ref = O.linear_elasticity_apply(L, el, adj, det, MU, LAM, u)
+    lib = capi.load()
+    for dt, rt, tol in ((torch.float64, capi.FLOAT64, 1e-13), (torch.float32, capi.FLOAT32, 3e-5)):
+        ud = torch.from_numpy(u).to(cuda).to(dt)
+        yd = torch.zeros(3 * n, dtype=dt, device=cuda)
+        es = ud.element_size()
+        capi.check(lib.cu_affine_sshex8_linear_elasticity_apply(
+            L, capi.i64(m.n_elements), sp.elements_ptrs.ptr, capi.i64(m.n_elements), capi.vp(adj_d), capi.vp(det_d),
+            ctypes_d(MU), ctypes_d(LAM), rt, capi.i64(3), capi.vp(ud), capi.c_void(ud.data_ptr() + es),
+            capi.c_void(ud.data_ptr() + 2 * es), capi.i64(3), capi.vp(yd), capi.c_void(yd.data_ptr() + es),
+            capi.c_void(yd.data_ptr() + 2 * es), None), "cu_affine_sshex8_linear_elasticity_apply")
+        err = np.abs(yd.double().cpu().numpy() - ref) / _scale(L, el, adj, det, u)
+        assert err.max() < tol, (dt, err.max())
+    # non-interleaved layouts are rejected with a message
+    assert lib.cu_affine_sshex8_linear_elasticity_apply(
+        L, capi.i64(m.n_elements), sp.elements_ptrs.ptr, capi.i64(m.n_elements), capi.vp(adj_d), capi.vp(det_d),
+        ctypes_d(MU), ctypes_d(LAM), capi.FLOAT64, capi.i64(1), capi.vp(yd), capi.vp(yd), capi.vp(yd), capi.i64(1),
+        capi.vp(yd), capi.vp(yd), capi.vp(yd), None) == 1
+
+
+@pytest.mark.parametrize("L", [1, 2, 4])
+def test_elasticity_block_diag(cuda, L):
+    import torch
+
+    m, sp, el, adj, det, adj_d, det_d = _setup(cuda, L, seed=7)
+    n = m.n_nodes(L)
+    d3_ref, b6_ref = O.linear_elasticity_block_diag(L if L > 1 else 0, el, adj, det, MU, LAM, n)
+    d3 = torch.zeros(3 * n, dtype=torch.float64, device=cuda)
+    b6 = torch.zeros(6 * n, dtype=torch.float64, device=cuda)
+    capi.check(capi.load().sfem_gb300_linear_elasticity_block_diag(
+        sp.element_type, capi.i64(m.n_elements), sp.elements_ptrs.ptr, capi.i64(m.n_elements), capi.vp(adj_d),
+        capi.vp(det_d), ctypes_d(MU), ctypes_d(LAM), capi.FLOAT64, capi.vp(d3), capi.vp(b6), None), "block diag")
+    assert np.abs(d3.cpu().numpy() - d3_ref).max() <= 1e-13 * np.abs(d3_ref).max()
+    assert np.abs(b6.cpu().numpy() - b6_ref).max() <= 1e-13 * np.abs(b6_ref).max()

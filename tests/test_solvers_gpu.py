@@ -1,0 +1,132 @@
+"""Device solver stack (CG, Jacobi, Chebyshev3, multigrid, FP64 iterative refinement)
+against the CPU oracle: every solve is judged by its TRUE FP64 residual
+||b - A x|| / ||b|| computed with the oracle operator, and by its distance to
+a tightly converged oracle solution."""
+
+import numpy as np
+import pytest
+
+import oracle as O
+import oracle.solvers as OS
+from sfem_gb300 import solvers as S
+from sfem_gb300.mesh import SSMesh
+
+pytestmark = pytest.mark.gpu
+
+
+def _oracle_poisson(m, L, fff_aos, dirichlet):
+    el = m.hex8_elements() if L == 1 else m.elements(L)
+
+    def apply(x):
+        y = O.hex8_laplacian_apply(el, fff_aos, x) if L == 1 else O.sshex8_laplacian_apply(L, el, fff_aos, x)
+        y[dirichlet] = x[dirichlet]
+        return y
+
+    d = O.laplacian_diag(L if L > 1 else 0, el, fff_aos, m.n_nodes(L))
+    d[dirichlet] = 1
+    return apply, d
+
+
+def _rhs(m, L, dirichlet, seed=0):
+    b = np.random.default_rng(seed).standard_normal(m.n_nodes(L))
+    b[dirichlet] = 0
+    return b
+
+
+def _check_solution(apply, b, x, x_star, rtol=1e-10, xtol=1e-6):
+    res = np.linalg.norm(b - apply(x)) / np.linalg.norm(b)
+    assert res <= rtol * 1.01, res
+    assert np.linalg.norm(x - x_star) <= xtol * np.linalg.norm(x_star)
+
+
+def test_hex8_poisson_jacobi_pcg(cuda):
+    import torch
+
+    m = SSMesh(12, 12, 12, 1)
+    H = S.Hierarchy(m, dirichlet_faces=("x0", "x1", "y0", "y1", "z0", "z1"), device=cuda)
+    fff = H.fff.cpu().numpy().T.copy()
+    dn = H.dirichlet[0].cpu().numpy()
+    apply, d = _oracle_poisson(m, 1, fff, dn)
+    b = _rhs(m, 1, dn)
+    x_star, _ = OS.cg(apply, b, precond=lambda r: r / d, rtol=1e-14)
+    ctx = S.context()
+    op = S.laplacian_op(ctx, H.spaces[0], H.fff, H.dirichlet[0], torch.float64)
+    jac = S.jacobi(ctx, torch.from_numpy(d).to(cuda), 1.0)
+    solver = S.cg(ctx, op, jac, rtol=1e-12)
+    bd = torch.from_numpy(b).to(cuda)
+    x = torch.zeros_like(bd)
+    assert S.solve(solver, bd, x) == 0
+    it, _ = S.stats(solver)
+    assert 10 < it < 500
+    _check_solution(apply, b, x.cpu().numpy(), x_star, rtol=1e-10, xtol=1e-8)
+
+
+@pytest.mark.parametrize("smoother", ["chebyshev3", "jacobi"])
+def test_sshex8_mg_pcg_fp64(cuda, smoother):
+    import torch
+
+    L = 4
+    m = SSMesh(4, 3, 3, L, perturb=0.1, seed=2)
+    H = S.Hierarchy(m, dirichlet_faces=("x0",), device=cuda)
+    fff = H.fff.cpu().numpy().T.copy()
+    dn = H.dirichlet[0].cpu().numpy()
+    apply, d = _oracle_poisson(m, L, fff, dn)
+    b = _rhs(m, L, dn, seed=4)
+    x_star, _ = OS.cg(apply, b, precond=lambda r: r / d, rtol=1e-14, max_it=20000)
+    ctx = S.context()
+    mg, op = S.build_poisson_mg(ctx, H, torch.float64, smoother=smoother, sweeps=2)
+    solver = S.cg(ctx, op, mg, rtol=1e-11, max_it=200)
+    bd = torch.from_numpy(b).to(cuda)
+    x = torch.zeros_like(bd)
+    assert S.solve(solver, bd, x) == 0
+    it, _ = S.stats(solver)
+    assert it <= 40, it  # multigrid-preconditioned: iteration count independent of h
+    _check_solution(apply, b, x.cpu().numpy(), x_star, rtol=1e-10, xtol=1e-7)
+
+
+def test_mixed_precision_iterative_refinement(cuda):
+    import torch
+
+    L = 4
+    m = SSMesh(4, 4, 3, L, perturb=0.1, seed=3)
+    H = S.Hierarchy(m, dirichlet_faces=("x0",), device=cuda)
+    fff = H.fff.cpu().numpy().T.copy()
+    dn = H.dirichlet[0].cpu().numpy()
+    apply, d = _oracle_poisson(m, L, fff, dn)
+    b = _rhs(m, L, dn, seed=5)
+    x_star, _ = OS.cg(apply, b, precond=lambda r: r / d, rtol=1e-14, max_it=20000)
+    ctx = S.context()
+    mg32, op32 = S.build_poisson_mg(ctx, H, torch.float32, smoother="chebyshev3", sweeps=2)
+    inner = S.cg(ctx, op32, mg32, rtol=1e-4, max_it=30)
+    op64 = S.laplacian_op(ctx, H.spaces[0], H.fff, H.dirichlet[0], torch.float64)
+    ir = S.iterative_refinement(ctx, op64, inner, max_it=30, rtol=1e-10)
+    bd = torch.from_numpy(b).to(cuda)
+    x = torch.zeros_like(bd)
+    assert S.solve(ir, bd, x) == 0
+    it, rel = S.stats(ir)
+    assert rel <= 1e-10 and it <= 6, (it, rel)
+    _check_solution(apply, b, x.cpu().numpy(), x_star, rtol=1e-10, xtol=1e-7)
+
+
+def test_chebyshev_eigenvalue_matches_power_method(cuda):
+    import torch
+
+    L = 2
+    m = SSMesh(3, 3, 3, L, perturb=0.1, seed=1)
+    H = S.Hierarchy(m, dirichlet_faces=("x0",), device=cuda)
+    fff = H.fff.cpu().numpy().T.copy()
+    dn = H.dirichlet[0].cpu().numpy()
+    apply, _ = _oracle_poisson(m, L, fff, dn)
+    ctx = S.context()
+    op = S.laplacian_op(ctx, H.spaces[0], H.fff, H.dirichlet[0], torch.float64)
+    ch = S.chebyshev3(ctx, op, max_it=3, eigen_max_it=100, eigen_tol=1e-5)
+    lam_ref = OS.power_method(apply, m.n_nodes(L), max_it=100, tol=1e-5)
+    assert abs(S.eig_max(ch) - lam_ref) <= 1e-9 * lam_ref
+    # the smoother itself against the oracle restatement
+    b = _rhs(m, L, dn, seed=9)
+    x0 = np.random.default_rng(1).standard_normal(b.size)
+    x0[dn] = 0
+    ref = OS.chebyshev3(apply, b, x0.copy(), lam_ref, 3)
+    xd = torch.from_numpy(x0).to(cuda)
+    S.solve(ch, torch.from_numpy(b).to(cuda), xd)
+    assert np.abs(xd.cpu().numpy() - ref).max() <= 1e-9 * np.abs(ref).max()
