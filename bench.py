@@ -43,6 +43,7 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--nx", type=int, default=NX)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-solve", action="store_true")
     return ap.parse_args()
 
 
@@ -167,6 +168,87 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+
+def time_apply(op, x, y, steps, warmup, flush, stream):
+    """Mean CUDA-event time of op.apply(x, y) with the L2 flushed before every step."""
+    import torch
+
+    for _ in range(max(3, warmup)):
+        y.zero_()
+        op.apply(x, y)
+    torch.cuda.synchronize()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    for k in range(steps):
+        flush.fill_(k & 0xFF)
+        y.zero_()
+        starts[k].record(stream)
+        op.apply(x, y)
+        ends[k].record(stream)
+    torch.cuda.synchronize()
+    return float(np.mean([a.elapsed_time(b) for a, b in zip(starts, ends)])) / 1e3
+
+
+def measure_solves(m, dev, rtol=1e-10):
+    """Time to ||b - A x|| / ||b|| <= rtol (FP64, true residual) on the same problem:
+    plain FP64 MG-PCG (Chebyshev3 V(2,2), Jacobi-PCG coarse) vs FP64 iterative
+    refinement around an FP32 MG-PCG (same hierarchy in float)."""
+    import torch
+
+    from sfem_gb300 import solvers as S
+
+    H = S.Hierarchy(m, dirichlet_faces=("x0",), device=dev)
+    N = m.n_nodes()
+    g = torch.Generator(device=dev).manual_seed(SEED + 7)
+    b = torch.randn(N, dtype=torch.float64, device=dev, generator=g)
+    b[H.dirichlet[0].long()] = 0
+    ctx = S.context()
+    op64 = S.laplacian_op(ctx, H.spaces[0], H.fff, H.dirichlet[0], torch.float64)
+    out = {}
+
+    def true_rel(x):
+        r = torch.zeros_like(b)
+        S.apply(op64, x, r)
+        return float(torch.linalg.vector_norm(b - r) / torch.linalg.vector_norm(b))
+
+    # plain FP64
+    t0 = time.perf_counter()
+    mg64, _ = S.build_poisson_mg(ctx, H, torch.float64, smoother="chebyshev3", sweeps=2)
+    torch.cuda.synchronize()
+    setup64 = time.perf_counter() - t0
+    cg64 = S.cg(ctx, op64, mg64, rtol=rtol * 0.05, max_it=500)
+    x = torch.zeros_like(b)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    rc = S.solve(cg64, b, x)
+    torch.cuda.synchronize()
+    t64 = time.perf_counter() - t0
+    it64, _ = S.stats(cg64)
+    out["plain_fp64_mg_pcg"] = {"seconds": t64, "iterations": it64, "true_rel_residual": true_rel(x), "rc": rc,
+                                "setup_seconds": setup64, "smoother": "Chebyshev3 V(2,2)", "coarse": "Jacobi-PCG 1e-6"}
+    x64 = x.clone()
+    # mixed: FP64 refinement around FP32 MG-PCG (eigenvalues reused from the FP64 setup)
+    t0 = time.perf_counter()
+    mg32, op32 = S.build_poisson_mg(ctx, H, torch.float32, smoother="chebyshev3", sweeps=2, eig_max=mg64.eigs)
+    inner = S.cg(ctx, op32, mg32, rtol=1e-4, max_it=30)
+    ir = S.iterative_refinement(ctx, op64, inner, max_it=30, rtol=rtol)
+    torch.cuda.synchronize()
+    setup32 = time.perf_counter() - t0
+    x = torch.zeros_like(b)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    rc = S.solve(ir, b, x)
+    torch.cuda.synchronize()
+    t32 = time.perf_counter() - t0
+    itir, rel = S.stats(ir)
+    xn = float(torch.linalg.vector_norm(x64))
+    out["mixed_fp32_mg_pcg_fp64_ir"] = {
+        "seconds": t32, "outer_iterations": itir, "true_rel_residual": true_rel(x), "rc": rc, "setup_seconds": setup32,
+        "solution_rel_diff_vs_plain_fp64": float(torch.linalg.vector_norm(x - x64)) / xn}
+    out["speedup_mixed_vs_plain"] = t64 / t32 if t32 > 0 else None
+    return out
+
+
 def run_ours(args):
     import torch
 
@@ -248,8 +330,18 @@ def run_ours(args):
     t_e2e = e0.elapsed_time(e1) / 1e3 / e2e_steps
     e2e_value = world * N / t_e2e / 1e9
 
+    # FP32 apply on the same mesh
+    x32 = x.float()
+    y32 = torch.zeros(N, dtype=torch.float32, device=dev)
+    t32 = time_apply(op, x32, y32, args.steps, args.warmup, flush, stream)
+
+    solve = None
+    if not args.no_solve:
+        solve = measure_solves(m, dev)
+
     peak, peak_kind = measured_peak_hbm()
     alg_bytes = 2 * 8 * N + (4 * (LEVEL + 1) ** 3 + 24) * E
+    alg_bytes32 = 2 * 4 * N + (4 * (LEVEL + 1) ** 3 + 24) * E
     achieved = alg_bytes / t_kernel / 1e9
     fp64_flops = 2 * 64 * (LEVEL ** 3) * E  # element-matrix form, 128 flop per micro element
     line = {
@@ -264,6 +356,9 @@ def run_ours(args):
                      "traffic": None, "peak_kind": peak_kind, "algorithmic_bytes": alg_bytes,
                      "fp64_gflops_achieved": fp64_flops / t_kernel / 1e9},
         "e2e": {"value": e2e_value, "unit": "GDoF/s", "h2d_bytes_per_step": 8 * N, "d2h_bytes_per_step": 8 * N},
+        "fp32_apply": {"gdofs": N / t32 / 1e9, "ms": t32 * 1e3, "achieved_gbs": alg_bytes32 / t32 / 1e9,
+                       "frac_hbm": alg_bytes32 / t32 / 1e9 / peak, "algorithmic_bytes": alg_bytes32},
+        "solve": solve,
         "gpu_launches": args.steps,
         "clocks": clk.summary(),
         "wall_s_timed": wall,
