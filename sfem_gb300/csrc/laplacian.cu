@@ -213,6 +213,95 @@ __global__ void __launch_bounds__(128) sshex8_laplacian_apply_warp_kernel(ptrdif
     }
 }
 
+// v2 (bandwidth path): one THREAD per macro element, everything in registers.
+// Consecutive threads own consecutive macro elements, so every connectivity
+// load elements[v][e] of a warp is one coalesced 128-byte line and the x
+// gathers of a warp fall on a few lines (neighbouring macro elements are
+// neighbours in the mesh).  The thread sweeps the micro-element layers in z
+// with two node planes of x and y in registers; when a layer is done the lower
+// y plane is final and is scattered (plain read-modify-write for nodes strictly
+// inside the macro element, atomicAdd for its surface).  The element matrix is
+// built once per thread from the 6 metric entries (compile-time weights).
+template <typename T, int L>
+__global__ void __launch_bounds__(128) sshex8_laplacian_apply_tpe_kernel(ptrdiff_t nelements,
+                                                                         const idx_t *const *elements,
+                                                                         ptrdiff_t fff_stride, const float *fff,
+                                                                         const T *__restrict__ x, T *__restrict__ y) {
+    constexpr int N1 = L + 1;
+    constexpr int NP = N1 * N1;
+    const ptrdiff_t e = blockIdx.x * (ptrdiff_t)blockDim.x + threadIdx.x;
+    if (e >= nelements) return;
+    const T h = T(1) / T(L);
+    T f[6];
+#pragma unroll
+    for (int m = 0; m < 6; m++) f[m] = (T)__ldg(&fff[m * fff_stride + e]) * h;
+    T A[64];
+#pragma unroll
+    for (int k = 0; k < 64; k++) {
+        T a = 0;
+#pragma unroll
+        for (int m = 0; m < 6; m++) {
+            const double w = LapTable().w[k][m];
+            if (w != 0.0) a += f[m] * T(w);
+        }
+        A[k] = a;
+    }
+    T xa[NP], xb[NP], ya[NP], yb[NP];
+#pragma unroll
+    for (int p = 0; p < NP; p++) {
+        xa[p] = __ldg(&x[__ldg(&elements[p][e])]);
+        ya[p] = 0;
+    }
+#pragma unroll
+    for (int zi = 0; zi < L; zi++) {
+#pragma unroll
+        for (int p = 0; p < NP; p++) {
+            xb[p] = __ldg(&x[__ldg(&elements[(zi + 1) * NP + p][e])]);
+            yb[p] = 0;
+        }
+#pragma unroll
+        for (int yi = 0; yi < L; yi++) {
+#pragma unroll
+            for (int xi = 0; xi < L; xi++) {
+                T u[8];
+#pragma unroll
+                for (int c = 0; c < 8; c++) {
+                    const int p = (yi + c8y(c)) * N1 + xi + c8x(c);
+                    u[c] = c8z(c) ? xb[p] : xa[p];
+                }
+#pragma unroll
+                for (int i = 0; i < 8; i++) {
+                    T acc = 0;
+#pragma unroll
+                    for (int j = 0; j < 8; j++) acc += A[i * 8 + j] * u[j];
+                    const int p = (yi + c8y(i)) * N1 + xi + c8x(i);
+                    if (c8z(i))
+                        yb[p] += acc;
+                    else
+                        ya[p] += acc;
+                }
+            }
+        }
+        // plane zi is final
+#pragma unroll
+        for (int p = 0; p < NP; p++) {
+            const int xi = p % N1, yi = p / N1;
+            const idx_t g = __ldg(&elements[zi * NP + p][e]);
+            if (zi > 0 && xi > 0 && xi < L && yi > 0 && yi < L)
+                y[g] += ya[p];
+            else
+                atomicAdd(&y[g], ya[p]);
+        }
+#pragma unroll
+        for (int p = 0; p < NP; p++) {
+            xa[p] = xb[p];
+            ya[p] = yb[p];
+        }
+    }
+#pragma unroll
+    for (int p = 0; p < NP; p++) atomicAdd(&y[__ldg(&elements[L * NP + p][e])], ya[p]);
+}
+
 // Diagonal: node value = sum over the micro elements of this macro element that
 // contain it of A[a][a] (a = the node's corner in that micro element).
 template <typename T, int L>

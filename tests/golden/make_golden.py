@@ -1,0 +1,66 @@
+"""Generate tests/golden/*.npz from the reference's own CPU kernels.
+
+Run where the reference tree is present (it builds oracle/_ref/libsfem_ref.so
+from the reference sources in place).  The fixtures pin the oracle
+restatement on machines without the reference tree.
+
+    python tests/golden/make_golden.py
+"""
+
+import sys
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT))
+
+import oracle as O  # noqa: E402
+from sfem_gb300.mesh import SSMesh  # noqa: E402
+
+OUT = Path(__file__).resolve().parent
+
+
+def main():
+    assert O.ref() is not None, "reference kernels unavailable"
+    rng = np.random.default_rng(20261203)
+    # sshex8 L=4 on a perturbed 2x2x1 macro mesh of [0,2]x[0,1]x[0,1]
+    L = 4
+    m = SSMesh(2, 2, 1, L, box=((0, 2), (0, 1), (0, 1)), perturb=0.15, seed=11)
+    el = m.elements(L)
+    corners = el[m.macro_corner_lidx(L)]
+    fff = O.fff_fill(corners, m.points, use_ref=True)
+    adj, det = O.adjugate_fill(corners, m.points, use_ref=True)
+    n = m.n_nodes(L)
+    x = rng.standard_normal(n)
+    u = rng.standard_normal(3 * n)
+    lap = O.sshex8_laplacian_apply(L, el, fff, x, use_ref=True)
+    ela = O.linear_elasticity_apply(L, el, adj, det, 1.0, 10.0, u, use_ref=True)
+    e2 = m.elements(2)
+    n2 = m.n_nodes(2)
+    xc = rng.standard_normal(n2)
+    prol = O.prolongate(2, e2, L, el, 1, xc, n, use_ref=True)
+    cnt = O.incidence_count(L, el, n, use_ref=True)
+    rest = O.restrict(L, el, cnt, 2, e2, 1, x, n2, use_ref=True)
+    e1 = m.elements(1)
+    n1 = m.n_nodes(1)
+    x1 = rng.standard_normal(n1)
+    hprol = O.prolongate(1, e1, 2, e2, 1, x1, n2, use_ref=True)
+    cnt2 = O.incidence_count(2, e2, n2, use_ref=True)
+    hrest = O.restrict(2, e2, cnt2, 1, e1, 1, xc, n1, use_ref=True)
+    h8 = m.hex8_elements()
+    hlap = O.hex8_laplacian_apply(h8, fff, x1, use_ref=True)
+    A = O.laplacian_matrix(fff[0].astype(np.float64) / L, use_ref=True)
+    K = O.elasticity_matrix(1.0, 10.0, adj[0].astype(np.float64) / L**2, float(det[0]) / L**3, use_ref=True)
+    np.savez_compressed(
+        OUT / "sshex8_L4_2x2x1.npz",
+        nx=2, ny=2, nz=1, level=L, box=np.array([[0, 2], [0, 1], [0, 1]], float), perturb=0.15, seed=11,
+        elements=el, points=m.points, fff=fff, adjugate=adj, determinant=det, x=x, u=u, laplacian_apply=lap,
+        elasticity_apply=ela, mu=1.0, lam=10.0, x_coarse2=xc, prolongate_2_4=prol, count_4=cnt, restrict_4_2=rest,
+        x_level1=x1, prolongate_1_2=hprol, count_2=cnt2, restrict_2_1=hrest, hex8_elements=h8,
+        hex8_laplacian_apply=hlap, laplacian_matrix_e0=A, elasticity_matrix_e0=K)
+    print("wrote", OUT / "sshex8_L4_2x2x1.npz")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,151 @@
+"""CPU tests: the oracle restatement is pinned against the reference's own CPU
+kernels -- through the committed golden fixtures (always) and directly through
+oracle/_ref when the reference tree is available."""
+
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import oracle as O
+import oracle.solvers as OS
+from sfem_gb300.mesh import SSMesh, derefinement_levels
+
+GOLD = Path(__file__).resolve().parent / "golden" / "sshex8_L4_2x2x1.npz"
+
+
+@pytest.fixture(scope="module")
+def gold():
+    return dict(np.load(GOLD))
+
+
+def _rel(a, b):
+    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
+
+
+def test_mesh_matches_golden(gold):
+    m = SSMesh(2, 2, 1, 4, box=((0, 2), (0, 1), (0, 1)), perturb=0.15, seed=11)
+    assert np.array_equal(m.elements(4), gold["elements"])
+    assert np.array_equal(m.points, gold["points"])
+    assert np.array_equal(m.hex8_elements(), gold["hex8_elements"])
+
+
+def test_oracle_geometry_bitexact(gold):
+    el = gold["elements"]
+    m = SSMesh(2, 2, 1, 4, box=((0, 2), (0, 1), (0, 1)), perturb=0.15, seed=11)
+    corners = el[m.macro_corner_lidx(4)]
+    assert np.array_equal(O.fff_fill(corners, gold["points"]), gold["fff"])
+    adj, det = O.adjugate_fill(corners, gold["points"])
+    assert np.array_equal(adj, gold["adjugate"]) and np.array_equal(det, gold["determinant"])
+
+
+def test_oracle_element_matrices(gold):
+    A = O.laplacian_matrix(gold["fff"][0].astype(np.float64) / 4)
+    assert _rel(A, gold["laplacian_matrix_e0"]) < 1e-14
+    K = O.elasticity_matrix(1.0, 10.0, gold["adjugate"][0].astype(np.float64) / 16, float(gold["determinant"][0]) / 64)
+    assert _rel(K, gold["elasticity_matrix_e0"]) < 1e-14
+    assert np.abs(K - K.T).max() == 0
+
+
+def test_oracle_applies(gold):
+    el, fff = gold["elements"], gold["fff"]
+    assert _rel(O.sshex8_laplacian_apply(4, el, fff, gold["x"]), gold["laplacian_apply"]) < 1e-14
+    assert _rel(O.hex8_laplacian_apply(gold["hex8_elements"], fff, gold["x_level1"]), gold["hex8_laplacian_apply"]) < 1e-14
+    ela = O.linear_elasticity_apply(4, el, gold["adjugate"], gold["determinant"], 1.0, 10.0, gold["u"])
+    assert _rel(ela, gold["elasticity_apply"]) < 1e-14
+
+
+def test_oracle_transfer(gold):
+    m = SSMesh(2, 2, 1, 4, box=((0, 2), (0, 1), (0, 1)), perturb=0.15, seed=11)
+    el, e2, e1 = m.elements(4), m.elements(2), m.elements(1)
+    n, n2, n1 = m.n_nodes(4), m.n_nodes(2), m.n_nodes(1)
+    assert np.array_equal(O.incidence_count(4, el, n), gold["count_4"])
+    assert _rel(O.prolongate(2, e2, 4, el, 1, gold["x_coarse2"], n), gold["prolongate_2_4"]) < 1e-15
+    assert _rel(O.restrict(4, el, gold["count_4"], 2, e2, 1, gold["x"], n2), gold["restrict_4_2"]) < 1e-14
+    assert _rel(O.prolongate(1, e1, 2, e2, 1, gold["x_level1"], n2), gold["prolongate_1_2"]) < 1e-15
+    assert _rel(O.restrict(2, e2, gold["count_2"], 1, e1, 1, gold["x_coarse2"], n1), gold["restrict_2_1"]) < 1e-14
+
+
+def test_stencil_equals_element_matrix_on_skewed_hex():
+    """Known answer (operators/stencil/tests/sfem_StencilTest.cpp:66-140): the reference's
+    27-point stencil + surface pass equals the element-matrix apply on a skewed hex, L=16."""
+    if O.ref() is None:
+        pytest.skip("reference kernels unavailable")
+    m = SSMesh(1, 1, 1, 16, perturb=0.0)
+    # skew the single macro element
+    pts = m.points.astype(np.float64)
+    pts[0] += 0.3 * pts[1] + 0.1 * pts[2]
+    pts[2] += 0.2 * pts[0]
+    el = m.elements(16)
+    fff = O.fff_fill(el[m.macro_corner_lidx(16)], pts.astype(np.float32))
+    x = np.random.default_rng(0).standard_normal(m.n_nodes())
+    a = O.sshex8_laplacian_apply(16, el, fff, x, use_ref=True)
+    b = O.sshex8_laplacian_apply(16, el, fff, x)
+    assert np.abs(a - b).max() < 1e-8
+
+
+def test_operator_properties():
+    """Laplacian rows sum to zero (A 1 = 0 without constraints); Galerkin consistency
+    A_c 1 = P^T A P 1 (algebra/sfem_Multigrid.hpp:112-173) holds trivially for constants."""
+    m = SSMesh(3, 2, 2, 4, perturb=0.1, seed=1)
+    el = m.elements(4)
+    fff = O.fff_fill(el[m.macro_corner_lidx(4)], m.points)
+    ones = np.ones(m.n_nodes())
+    assert np.abs(O.sshex8_laplacian_apply(4, el, fff, ones)).max() < 1e-12
+    # symmetry: (A x, y) = (x, A y)
+    rng = np.random.default_rng(0)
+    x, y = rng.standard_normal(m.n_nodes()), rng.standard_normal(m.n_nodes())
+    Ax, Ay = O.sshex8_laplacian_apply(4, el, fff, x), O.sshex8_laplacian_apply(4, el, fff, y)
+    assert abs(Ax @ y - x @ Ay) < 1e-10 * abs(Ax @ y)
+
+
+def test_reference_direct_pin():
+    """Where the reference tree is present, pin the restatement against it on a fresh mesh."""
+    if O.ref() is None:
+        pytest.skip("reference kernels unavailable")
+    m = SSMesh(3, 2, 2, 3, perturb=0.12, seed=5)
+    el = m.elements(3)
+    corners = el[m.macro_corner_lidx(3)]
+    fff = O.fff_fill(corners, m.points, use_ref=True)
+    x = np.random.default_rng(2).standard_normal(m.n_nodes())
+    assert _rel(O.sshex8_laplacian_apply(3, el, fff, x), O.sshex8_laplacian_apply(3, el, fff, x, use_ref=True)) < 1e-14
+    adj, det = O.adjugate_fill(corners, m.points, use_ref=True)
+    u = np.random.default_rng(3).standard_normal(3 * m.n_nodes())
+    assert _rel(O.linear_elasticity_apply(3, el, adj, det, 2.0, 3.0, u),
+                O.linear_elasticity_apply(3, el, adj, det, 2.0, 3.0, u, use_ref=True)) < 1e-14
+
+
+def test_derefinement_levels():
+    assert derefinement_levels(4) == [4, 2, 1]
+    assert derefinement_levels(3) == [3, 1]
+    assert derefinement_levels(8) == [8, 4, 2, 1]
+    assert derefinement_levels(6) == [6, 3, 1]
+    assert derefinement_levels(1) == [1]
+
+
+def test_nested_numbering_prefix():
+    m = SSMesh(3, 2, 2, 4)
+    for l in m.levels:
+        assert m.elements(l).max() < m.n_nodes(l)
+    # coarse level nodes are the same physical points as in the fine level
+    e2, e4 = m.elements(2), m.elements(4)
+    for lid2 in range(27):
+        z, y, x = lid2 // 9, (lid2 // 3) % 3, lid2 % 3
+        assert np.array_equal(e2[lid2], e4[z * 2 * 25 + y * 2 * 5 + x * 2])
+
+
+def test_oracle_cg_converges():
+    m = SSMesh(4, 4, 4, 1)
+    el = m.hex8_elements()
+    fff = O.fff_fill(el, m.points)
+    dn = m.all_boundary_nodes(1)
+
+    def apply(v):
+        y = O.hex8_laplacian_apply(el, fff, v)
+        y[dn] = v[dn]
+        return y
+
+    b = np.ones(m.n_nodes(1))
+    b[dn] = 0
+    x, it = OS.cg(apply, b, rtol=1e-12)
+    assert np.linalg.norm(b - apply(x)) < 1e-10 * np.linalg.norm(b)
