@@ -180,9 +180,11 @@ int sfem_gb300_cg_update_x_r(int real_type, ptrdiff_t n, const double *alpha_num
 /*   beta = *beta_num / *beta_den;  p = z + beta p. */
 int sfem_gb300_cg_update_p(int real_type, ptrdiff_t n, const double *beta_num, const double *beta_den, const void *z,
                            void *p, void *stream);
-/* Chebyshev3 step p = beta p - rhs + Ax;  x -= alpha p (algebra/sfem_Chebyshev3.hpp:36-52). */
-int sfem_gb300_chebyshev_update(int real_type, ptrdiff_t n, double alpha, double beta, const void *rhs, const void *Ax,
-                                void *p, void *x, void *stream);
+/* Chebyshev3 step p = beta p - rhs + Ax;  x -= alpha p (algebra/sfem_Chebyshev3.hpp:36-52).
+ * With a non-NULL inv_diag the step runs on the Jacobi-scaled operator: p = beta p + D^-1 (Ax - rhs).
+ * beta == 0 ignores the previous p. */
+int sfem_gb300_chebyshev_update(int real_type, ptrdiff_t n, double alpha, double beta, const void *inv_diag,
+                                const void *rhs, const void *Ax, void *p, void *x, void *stream);
 
 /* Dirichlet constraints on interleaved vectors (operators/boundary_conditions/dirichlet.hpp:44-130):
  * dest[node*block+comp] = src[node*block+comp], resp. x[node*block+comp] = value. */
@@ -244,9 +246,12 @@ int sfem_gb300_block_jacobi_create(void *context, int real_type, ptrdiff_t n_nod
 /* Stationary iteration x += P (b - A x), max_it sweeps (algebra/sfem_Stationary.hpp:19-133). */
 int sfem_gb300_stationary_create(void *context, void *op, void *precond, int max_it, void **solver);
 /* Chebyshev3 smoother; runs the power method from a vector of ones at creation
- * (algebra/sfem_Chebyshev3.hpp:56-312, algebra/sfem_PowerMethod.hpp:18-55). */
-int sfem_gb300_chebyshev3_create(void *context, void *op, int max_it, double scale_eig_max, double scale_eig_min,
-                                 int eigen_max_it, double eigen_tol, void **solver);
+ * (algebra/sfem_Chebyshev3.hpp:56-312, algebra/sfem_PowerMethod.hpp:18-55).
+ * inv_diag (n entries, may be NULL) selects the Jacobi-scaled iteration on D^-1 A; the
+ * caller keeps it alive.  Unscaled, the identity rows of Dirichlet nodes (eigenvalue 1)
+ * dominate the spectrum estimate on fine meshes, where the stiffness eigenvalues scale with h. */
+int sfem_gb300_chebyshev3_create(void *context, void *op, const void *inv_diag, int max_it, double scale_eig_max,
+                                 double scale_eig_min, int eigen_max_it, double eigen_tol, void **solver);
 int sfem_gb300_chebyshev3_eig_max(void *solver, double *eig_max);
 int sfem_gb300_chebyshev3_set_eig_max(void *solver, double eig_max);
 /* (Preconditioned) conjugate gradient (algebra/sfem_cg.hpp:79-453); precond may be NULL. */

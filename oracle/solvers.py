@@ -55,18 +55,20 @@ def power_method(apply, n, max_it=100, tol=1e-5, v0=None):
     return lam
 
 
-def chebyshev3(apply, b, x, eig_max, sweeps, scale_max=1.02, scale_min=0.06):
+def chebyshev3(apply, b, x, eig_max, sweeps, scale_max=1.02, scale_min=0.06, inv_diag=None):
+    """Chebyshev3; with inv_diag the iteration runs on D^-1 A (eig_max of D^-1 A)."""
     emax = eig_max * scale_max
     emin = scale_min * emax
     eavg, ediff = (emin + emax) / 2, (emin - emax) / 2
     alpha = 1.0 / eavg
-    p = apply(x) - b
+    s = (lambda v: v) if inv_diag is None else (lambda v: inv_diag * v)
+    p = s(apply(x) - b)
     x = x - alpha * p
     for it in range(1, sweeps):
         dea = ediff * alpha
         beta = (0.5 if it == 1 else 0.25) * dea * dea
         alpha = 1.0 / (eavg - beta / alpha)
-        p = beta * p - b + apply(x)
+        p = beta * p + s(apply(x) - b)
         x = x - alpha * p
     return x
 

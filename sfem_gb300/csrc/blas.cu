@@ -100,12 +100,16 @@ __global__ void cg_update_p_kernel(ptrdiff_t n, const double *__restrict__ num, 
         p[i] = z[i] + beta * p[i];
 }
 
-// Chebyshev3 step (algebra/sfem_Chebyshev3.hpp:36-52): p = beta p - rhs + Ax ; x -= alpha p
+// Chebyshev3 step (algebra/sfem_Chebyshev3.hpp:36-52): p = beta p - rhs + Ax ; x -= alpha p.
+// With inv_diag the step runs on D^-1 A: p = beta p + D^-1 (Ax - rhs).  beta == 0 ignores the old p.
 template <typename T>
-__global__ void cheb_update_kernel(ptrdiff_t n, T alpha, T beta, const T *__restrict__ rhs, const T *__restrict__ Ax,
-                                   T *__restrict__ p, T *__restrict__ x) {
+__global__ void cheb_update_kernel(ptrdiff_t n, T alpha, T beta, const T *__restrict__ inv_diag,
+                                   const T *__restrict__ rhs, const T *__restrict__ Ax, T *__restrict__ p,
+                                   T *__restrict__ x) {
     for (ptrdiff_t i = blockIdx.x * (ptrdiff_t)blockDim.x + threadIdx.x; i < n; i += (ptrdiff_t)gridDim.x * blockDim.x) {
-        const T pi = beta * p[i] - rhs[i] + Ax[i];
+        T g = Ax[i] - rhs[i];
+        if (inv_diag) g *= inv_diag[i];
+        const T pi = (beta != T(0) ? beta * p[i] : T(0)) + g;
         p[i] = pi;
         x[i] -= alpha * pi;
     }
@@ -274,12 +278,14 @@ extern "C" int sfem_gb300_cg_update_p(int real_type, ptrdiff_t n, const double *
     return check_launch("sfem_gb300_cg_update_p");
 }
 
-extern "C" int sfem_gb300_chebyshev_update(int real_type, ptrdiff_t n, double alpha, double beta, const void *rhs,
-                                           const void *Ax, void *p, void *x, void *stream) {
+extern "C" int sfem_gb300_chebyshev_update(int real_type, ptrdiff_t n, double alpha, double beta, const void *inv_diag,
+                                           const void *rhs, const void *Ax, void *p, void *x, void *stream) {
     if (n <= 0) return SFEM_GB300_SUCCESS;
     SFEM_DISPATCH_REAL(real_type, "sfem_gb300_chebyshev_update",
-                       SFEM_EW_LAUNCH(cheb_update_kernel, n, (T)alpha, (T)beta, (const T *)rhs, (const T *)Ax, (T *)p, (T *)x),
-                       SFEM_EW_LAUNCH(cheb_update_kernel, n, (T)alpha, (T)beta, (const T *)rhs, (const T *)Ax, (T *)p, (T *)x));
+                       SFEM_EW_LAUNCH(cheb_update_kernel, n, (T)alpha, (T)beta, (const T *)inv_diag, (const T *)rhs,
+                                      (const T *)Ax, (T *)p, (T *)x),
+                       SFEM_EW_LAUNCH(cheb_update_kernel, n, (T)alpha, (T)beta, (const T *)inv_diag, (const T *)rhs,
+                                      (const T *)Ax, (T *)p, (T *)x));
     return check_launch("sfem_gb300_chebyshev_update");
 }
 

@@ -6,6 +6,7 @@
 // macro element, sub-metric FFF/L for each of the L^3 micro elements, element
 // matrix A = sum_m f_m W_m with the exact Q1 integrals W_m, y += A x.
 #include <cstdio>
+#include <cstdlib>
 
 #include "common.cuh"
 #include "laplacian_kernels.cuh"
@@ -344,6 +345,17 @@ __global__ void __launch_bounds__(128) sshex8_laplacian_diag_kernel(ptrdiff_t ne
 
 // ------------------------------------------------------------------ dispatch
 
+// Kernel variant override for benchmarking: SFEM_GB300_LAPLACIAN_KERNEL=warp forces the
+// warp-per-element kernel (1); default (0) picks thread-per-element for float, L <= 4.
+static int laplacian_variant() {
+    static int v = -1;
+    if (v < 0) {
+        const char *e = getenv("SFEM_GB300_LAPLACIAN_KERNEL");
+        v = (e && e[0] == 'w') ? 1 : 0;
+    }
+    return v;
+}
+
 template <typename T>
 static int laplacian_apply_tpl(int element_type, ptrdiff_t nelements, idx_t **elements, ptrdiff_t fff_stride,
                                const float *fff, const T *x, T *y, cudaStream_t s) {
@@ -354,6 +366,22 @@ static int laplacian_apply_tpl(int element_type, ptrdiff_t nelements, idx_t **el
     }
     const int L = element_type - SFEM_GB300_SSHEX8_BASE;
     const int blocks = grid_for((nelements + 3) / 4, 1, kNumSMs * 64);
+    const bool tpe = sizeof(T) == 4 && L >= 2 && L <= 4 && laplacian_variant() != 1;
+    if (tpe) {
+        const int tb = (int)((nelements + 127) / 128);
+        switch (L) {
+            case 2:
+                sshex8_laplacian_apply_tpe_kernel<T, 2><<<tb, 128, 0, s>>>(nelements, elements, fff_stride, fff, x, y);
+                break;
+            case 3:
+                sshex8_laplacian_apply_tpe_kernel<T, 3><<<tb, 128, 0, s>>>(nelements, elements, fff_stride, fff, x, y);
+                break;
+            default:
+                sshex8_laplacian_apply_tpe_kernel<T, 4><<<tb, 128, 0, s>>>(nelements, elements, fff_stride, fff, x, y);
+                break;
+        }
+        return check_launch("cu_laplacian_apply(SSHEX8, thread per element)");
+    }
 #define SFEM_LAP_CASE(LL)                                                                                     \
     case LL:                                                                                                  \
         sshex8_laplacian_apply_warp_kernel<T, LL><<<blocks, 128, 0, s>>>(nelements, elements, fff_stride, fff, x, y); \

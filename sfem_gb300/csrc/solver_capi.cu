@@ -435,8 +435,8 @@ int sfem_gb300_stationary_create(void *context, void *op, void *precond, int max
     return SFEM_GB300_SUCCESS;
 }
 
-int sfem_gb300_chebyshev3_create(void *context, void *op, int max_it, double scale_eig_max, double scale_eig_min,
-                                 int eigen_max_it, double eigen_tol, void **out) {
+int sfem_gb300_chebyshev3_create(void *context, void *op, const void *inv_diag, int max_it, double scale_eig_max,
+                                 double scale_eig_min, int eigen_max_it, double eigen_tol, void **out) {
     auto *c = H(context);
     auto *o = H(op);
     auto *h = new Handle();
@@ -448,6 +448,7 @@ int sfem_gb300_chebyshev3_create(void *context, void *op, int max_it, double sca
         auto s = std::make_shared<Chebyshev3<float>>();
         s->blas = blas_of<float>(c->ctx);
         s->op = o->f;
+        s->inv_diag = (const float *)inv_diag;
         s->max_it = max_it;
         s->scale_eig_max = scale_eig_max;
         s->scale_eig_min = scale_eig_min;
@@ -460,6 +461,7 @@ int sfem_gb300_chebyshev3_create(void *context, void *op, int max_it, double sca
         auto s = std::make_shared<Chebyshev3<double>>();
         s->blas = blas_of<double>(c->ctx);
         s->op = o->d;
+        s->inv_diag = (const double *)inv_diag;
         s->max_it = max_it;
         s->scale_eig_max = scale_eig_max;
         s->scale_eig_min = scale_eig_min;

@@ -235,12 +235,14 @@ double power_method_max_eigenvalue(const Blas<T> &blas, Operator<T> &op, int max
     return lambda;
 }
 
-// Chebyshev3 (algebra/sfem_Chebyshev3.hpp:183-302).
+// Chebyshev3 (algebra/sfem_Chebyshev3.hpp:183-302).  With inv_diag set, the
+// iteration (and the power method) run on the Jacobi-scaled operator D^-1 A.
 template <typename T>
 class Chebyshev3 final : public Solver<T> {
 public:
     Blas<T> blas;
     std::shared_ptr<Operator<T>> op;
+    const T *inv_diag{nullptr};
     DeviceBuffer<T> p, temp;
     double eig_max{0}, scale_eig_max{1.02}, scale_eig_min{0.06};
     int max_it{3};
@@ -254,8 +256,23 @@ public:
         SFEM_GB300_CHECK(temp.resize(n));
         blas.copy(n, guess, temp.ptr);
         double *slot = blas.ctx->slots(1);
-        eig_max = power_method_max_eigenvalue(blas, *op, eigen_max_it, eigen_tol, n, temp.ptr, p.ptr, slot);
-        return 0;
+        if (!slot) return set_error("Chebyshev3: out of scalar slots");
+        std::shared_ptr<Operator<T>> pm_op = op;
+        DeviceBuffer<T> scratch;
+        if (inv_diag) {
+            SFEM_GB300_CHECK(scratch.resize(n));
+            auto A = op;
+            auto b = blas;
+            const T *d = inv_diag;
+            T *tmp = scratch.ptr;
+            pm_op = make_op<T>(n, n, [A, b, d, tmp, n](const T *x, T *y) {
+                b.zeros(n, tmp);
+                A->apply(x, tmp);
+                return b.xypaz(n, d, tmp, T(1), y);
+            });
+        }
+        eig_max = power_method_max_eigenvalue(blas, *pm_op, eigen_max_it, eigen_tol, n, temp.ptr, p.ptr, slot);
+        return blas.zeros(n, p.ptr);
     }
     int init_with_ones() {
         DeviceBuffer<T> ones(op->rows());
@@ -269,14 +286,10 @@ public:
         const double emin = scale_eig_min * emax;
         const double eavg = (emin + emax) / 2, ediff = (emin - emax) / 2;
         double alpha = 1.0 / eavg, beta = 0, dea = 0;
-        if (initial_guess_zero) {
-            blas.zaxpby(n, T(-1), b, T(0), b, p.ptr);
-        } else {
-            if (!op->overwrites_output()) blas.zeros(n, p.ptr);
-            op->apply(x, p.ptr);
-            blas.axpy(n, T(-1), b, p.ptr);
-        }
-        blas.axpy(n, T(-alpha), p.ptr, x);
+        blas.zeros(n, temp.ptr);
+        if (!initial_guess_zero) op->apply(x, temp.ptr);
+        SFEM_GB300_CHECK(sfem_gb300_chebyshev_update(real_type_v<T>, n, alpha, 0.0, inv_diag, b, temp.ptr, p.ptr, x,
+                                                     blas.ctx->sp()));
         this->iterations_ = 1;
         for (; this->iterations_ < max_it; this->iterations_++) {
             dea = ediff * alpha;
@@ -284,7 +297,7 @@ public:
             alpha = 1.0 / (eavg - beta / alpha);
             if (!op->overwrites_output()) blas.zeros(n, temp.ptr);
             op->apply(x, temp.ptr);
-            SFEM_GB300_CHECK(sfem_gb300_chebyshev_update(real_type_v<T>, n, alpha, beta, b, temp.ptr, p.ptr, x,
+            SFEM_GB300_CHECK(sfem_gb300_chebyshev_update(real_type_v<T>, n, alpha, beta, inv_diag, b, temp.ptr, p.ptr, x,
                                                          blas.ctx->sp()));
         }
         return 0;

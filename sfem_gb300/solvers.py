@@ -122,10 +122,10 @@ def stationary(ctx, op, precond, max_it) -> Handle:
 
 
 def chebyshev3(ctx, op, max_it=2, scale_eig_max=1.02, scale_eig_min=0.06, eigen_max_it=100, eigen_tol=1e-5,
-               eig_max=None) -> Handle:
-    h = _create(_lib().sfem_gb300_chebyshev3_create, ctx.ptr, op.ptr, c_int(max_it), c_double(scale_eig_max),
-                c_double(scale_eig_min), c_int(eigen_max_it if eig_max is None else 1), c_double(eigen_tol),
-                keep=(ctx, op))
+               eig_max=None, inv_diag=None) -> Handle:
+    h = _create(_lib().sfem_gb300_chebyshev3_create, ctx.ptr, op.ptr, capi.vp(inv_diag), c_int(max_it),
+                c_double(scale_eig_max), c_double(scale_eig_min), c_int(eigen_max_it if eig_max is None else 1),
+                c_double(eigen_tol), keep=(ctx, op, inv_diag))
     if eig_max is not None:
         capi.check(_lib().sfem_gb300_chebyshev3_set_eig_max(h.ptr, c_double(eig_max)), "set_eig_max")
     return h
@@ -212,9 +212,12 @@ def build_poisson_mg(ctx, H: Hierarchy, dtype, smoother="chebyshev3", sweeps=2, 
         if k == nlev - 1:
             jac = jacobi(ctx, diag, 1.0)
             smoothers.append(cg(ctx, op, jac, max_it=coarse_max_it, rtol=coarse_rtol))
-        elif smoother == "chebyshev3":
+        elif smoother in ("chebyshev3", "chebyshev3_plain"):
             em = None if eig_max is None else eig_max[k]
-            ch = chebyshev3(ctx, op, max_it=sweeps, eig_max=em)
+            inv = None
+            if smoother == "chebyshev3":  # Jacobi-scaled Chebyshev (iteration on D^-1 A)
+                inv = 1.0 / diag
+            ch = chebyshev3(ctx, op, max_it=sweeps, eig_max=em, inv_diag=inv)
             eigs.append(globals()["eig_max"](ch))
             smoothers.append(ch)
         else:
@@ -224,6 +227,50 @@ def build_poisson_mg(ctx, H: Hierarchy, dtype, smoother="chebyshev3", sweeps=2, 
     for k in range(nlev):
         P = prolongation_op(ctx, H.spaces[k + 1], H.spaces[k], 1, H.dirichlet[k], dtype) if k + 1 < nlev else None
         R = restriction_op(ctx, H.spaces[k], H.spaces[k + 1], 1, H.dirichlet[k + 1], dtype) if k + 1 < nlev else None
+        mg_add_level(mg, ops[k], smoothers[k], P, R)
+    mg.keep += [H]
+    mg.eigs = eigs
+    return mg, ops[0]
+
+
+def _elasticity_diag(H: Hierarchy, k, dtype, mu, lam):
+    import torch
+
+    sp = H.spaces[k]
+    E = sp.n_elements
+    d3 = torch.zeros(3 * sp.n_nodes, dtype=dtype, device=H.device)
+    capi.check(capi.load().sfem_gb300_linear_elasticity_block_diag(
+        sp.element_type, capi.i64(E), sp.elements_ptrs.ptr, capi.i64(E), capi.vp(H.adj), capi.vp(H.det), c_double(mu),
+        c_double(lam), rt_of(dtype), capi.vp(d3), None, None), "elasticity diag")
+    dn = H.dirichlet[k].long()
+    for c in range(3):
+        d3[3 * dn + c] = 1
+    return d3
+
+
+def build_elasticity_mg(ctx, H: Hierarchy, dtype, mu=1.0, lam=10.0, sweeps=2, coarse_rtol=1e-6,
+                        coarse_max_it=10000, eig_max=None):
+    """Geometric multigrid for linear elasticity (3 dofs / node) on every level of ``H``:
+    Jacobi-scaled Chebyshev3 smoothing, nested vector transfer, Jacobi-PCG coarse solve
+    (cf. the vector branch of algebra/mg/sfem_GeometricMultigrid.cpp:89-144)."""
+    ops, smoothers = [], []
+    nlev = len(H.spaces)
+    eigs = []
+    for k, sp in enumerate(H.spaces):
+        op = elasticity_op(ctx, sp, H.adj, H.det, mu, lam, H.dirichlet[k], dtype)
+        ops.append(op)
+        d3 = _elasticity_diag(H, k, dtype, mu, lam)
+        if k == nlev - 1:
+            smoothers.append(cg(ctx, op, jacobi(ctx, d3, 1.0), max_it=coarse_max_it, rtol=coarse_rtol))
+        else:
+            em = None if eig_max is None else eig_max[k]
+            ch = chebyshev3(ctx, op, max_it=sweeps, eig_max=em, inv_diag=1.0 / d3)
+            eigs.append(globals()["eig_max"](ch))
+            smoothers.append(ch)
+    mg = multigrid(ctx, dtype)
+    for k in range(nlev):
+        P = prolongation_op(ctx, H.spaces[k + 1], H.spaces[k], 3, H.dirichlet[k], dtype) if k + 1 < nlev else None
+        R = restriction_op(ctx, H.spaces[k], H.spaces[k + 1], 3, H.dirichlet[k + 1], dtype) if k + 1 < nlev else None
         mg_add_level(mg, ops[k], smoothers[k], P, R)
     mg.keep += [H]
     mg.eigs = eigs

@@ -75,11 +75,20 @@ def test_elementwise(cuda):
     p = y.clone()
     xx = x.clone()
     rhs = z.clone()
-    capi.check(lib.sfem_gb300_chebyshev_update(capi.FLOAT64, capi.i64(n), D(0.7), D(0.2), capi.vp(rhs), capi.vp(y),
-                                               capi.vp(p), capi.vp(xx), None), "")
+    capi.check(lib.sfem_gb300_chebyshev_update(capi.FLOAT64, capi.i64(n), D(0.7), D(0.2), None, capi.vp(rhs),
+                                               capi.vp(y), capi.vp(p), capi.vp(xx), None), "")
     pn = 0.2 * yn - z.cpu().numpy() + yn
     assert np.allclose(p.cpu().numpy(), pn, rtol=1e-14, atol=1e-14)
     assert np.allclose(xx.cpu().numpy(), xn - 0.7 * pn, rtol=1e-14, atol=1e-14)
+    # Jacobi-scaled variant, beta = 0 ignores the old p (even if it holds NaN)
+    inv = torch.rand(n, dtype=torch.float64, device=cuda, generator=g) + 0.5
+    p2 = torch.full_like(y, float("nan"))
+    x2 = x.clone()
+    capi.check(lib.sfem_gb300_chebyshev_update(capi.FLOAT64, capi.i64(n), D(0.7), D(0.0), capi.vp(inv), capi.vp(rhs),
+                                               capi.vp(y), capi.vp(p2), capi.vp(x2), None), "")
+    pn2 = inv.cpu().numpy() * (yn - z.cpu().numpy())
+    assert np.allclose(p2.cpu().numpy(), pn2, rtol=1e-14, atol=1e-14)
+    assert np.allclose(x2.cpu().numpy(), xn - 0.7 * pn2, rtol=1e-14, atol=1e-14)
     # conversions
     f = torch.zeros(n, dtype=torch.float32, device=cuda)
     capi.check(lib.sfem_gb300_convert(capi.i64(n), capi.FLOAT64, capi.vp(x), capi.FLOAT32, capi.vp(f), None), "")

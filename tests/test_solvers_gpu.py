@@ -82,7 +82,7 @@ def test_sshex8_mg_pcg_fp64(cuda, smoother):
     it, _ = S.stats(solver)
     # Chebyshev3 V(2,2) is a strong smoother; the reference's default Jacobi (omega = 1,
     # algebra/mg/sfem_GeometricMultigrid.cpp:113) is a weak one: CG still converges
-    assert it <= (40 if smoother == "chebyshev3" else 200), it
+    assert it <= (20 if smoother == "chebyshev3" else 200), it
     _check_solution(apply, b, x.cpu().numpy(), x_star, rtol=1e-10, xtol=1e-7)
 
 
@@ -132,3 +132,71 @@ def test_chebyshev_eigenvalue_matches_power_method(cuda):
     xd = torch.from_numpy(x0).to(cuda)
     S.solve(ch, torch.from_numpy(b).to(cuda), xd)
     assert np.abs(xd.cpu().numpy() - ref).max() <= 1e-9 * np.abs(ref).max()
+
+
+def test_jacobi_scaled_chebyshev_against_oracle(cuda):
+    import torch
+
+    L = 4
+    m = SSMesh(3, 2, 2, L, perturb=0.1, seed=4)
+    H = S.Hierarchy(m, dirichlet_faces=("x0",), device=cuda)
+    fff = H.fff.cpu().numpy().T.copy()
+    dn = H.dirichlet[0].cpu().numpy()
+    apply, d = _oracle_poisson(m, L, fff, dn)
+    ctx = S.context()
+    op = S.laplacian_op(ctx, H.spaces[0], H.fff, H.dirichlet[0], torch.float64)
+    inv = torch.from_numpy(1.0 / d).to(cuda)
+    ch = S.chebyshev3(ctx, op, max_it=3, eigen_max_it=100, eigen_tol=1e-5, inv_diag=inv)
+    lam_ref = OS.power_method(lambda v: apply(v) / d, m.n_nodes(L), max_it=100, tol=1e-5)
+    assert abs(S.eig_max(ch) - lam_ref) <= 1e-9 * lam_ref
+    assert 1.0 < lam_ref < 2.0  # spectrum of D^-1 A for a Q1 Laplacian
+    b = _rhs(m, L, dn, seed=3)
+    x0 = np.zeros_like(b)
+    ref = OS.chebyshev3(apply, b, x0.copy(), lam_ref, 3, inv_diag=1.0 / d)
+    xd = torch.from_numpy(x0).to(cuda)
+    S.solve(ch, torch.from_numpy(b).to(cuda), xd)
+    assert np.abs(xd.cpu().numpy() - ref).max() <= 1e-9 * np.abs(ref).max()
+
+
+def test_elasticity_mg_pcg_and_mixed(cuda):
+    import torch
+
+    L = 4
+    mu, lam = 1.0, 10.0
+    m = SSMesh(4, 2, 2, L, box=((0, 4), (0, 1), (0, 1)), perturb=0.05, seed=6)
+    H = S.Hierarchy(m, dirichlet_faces=("x0",), device=cuda, vec=3)
+    adj = H.adj.cpu().numpy().T.copy()
+    det = H.det.cpu().numpy().copy()
+    el = m.elements(L)
+    dn = H.dirichlet[0].cpu().numpy()
+    n = m.n_nodes(L)
+
+    def apply(u):
+        y = O.linear_elasticity_apply(L, el, adj, det, mu, lam, u)
+        for c in range(3):
+            y[3 * dn + c] = u[3 * dn + c]
+        return y
+
+    # body force (0, 0, -1) times the nodal volume (1 per node is enough for a test)
+    b = np.zeros(3 * n)
+    b[2::3] = -1.0
+    for c in range(3):
+        b[3 * dn + c] = 0
+    ctx = S.context()
+    mg, op = S.build_elasticity_mg(ctx, H, torch.float64, mu=mu, lam=lam)
+    solver = S.cg(ctx, op, mg, rtol=1e-11, max_it=300)
+    bd = torch.from_numpy(b).to(cuda)
+    x = torch.zeros_like(bd)
+    assert S.solve(solver, bd, x) == 0
+    res = np.linalg.norm(b - apply(x.cpu().numpy())) / np.linalg.norm(b)
+    assert res < 1e-10, res
+    # mixed precision: FP64 refinement around FP32 MG-PCG
+    mg32, op32 = S.build_elasticity_mg(ctx, H, torch.float32, mu=mu, lam=lam, eig_max=mg.eigs)
+    inner = S.cg(ctx, op32, mg32, rtol=1e-4, max_it=40)
+    op64 = S.elasticity_op(ctx, H.spaces[0], H.adj, H.det, mu, lam, H.dirichlet[0], torch.float64)
+    ir = S.iterative_refinement(ctx, op64, inner, max_it=30, rtol=1e-10)
+    x2 = torch.zeros_like(bd)
+    assert S.solve(ir, bd, x2) == 0
+    res2 = np.linalg.norm(b - apply(x2.cpu().numpy())) / np.linalg.norm(b)
+    assert res2 < 1e-10, res2
+    assert np.linalg.norm(x2.cpu().numpy() - x.cpu().numpy()) < 1e-8 * np.linalg.norm(x.cpu().numpy())
