@@ -249,6 +249,74 @@ def measure_solves(m, dev, rtol=1e-10):
     return out
 
 
+def lumped_body_force(m, det):
+    """Lumped-mass load of a unit body force in -z: node i gets sum over micro elements
+    containing it of |micro element| / 8 (affine sub-elements: |e| = det_macro / L^3)."""
+    L = m.L
+    el = m.elements(L)
+    N1 = L + 1
+    lid = np.arange(N1 ** 3)
+    xi, yi, zi = lid % N1, (lid // N1) % N1, lid // (N1 * N1)
+    mult = np.ones(N1 ** 3)
+    for c in (xi, yi, zi):
+        mult *= np.where((c == 0) | (c == L), 1.0, 2.0)  # micro elements of this macro element sharing the node
+    w = (mult[:, None] * (det.astype(np.float64) / (8.0 * L ** 3))[None, :])
+    vol = np.bincount(el.reshape(-1), weights=w.reshape(-1), minlength=m.n_nodes())
+    b = np.zeros(3 * m.n_nodes())
+    b[2::3] = -vol
+    return b
+
+
+def measure_elasticity_solves(dev, nx=64, ny=16, nz=16, rtol=1e-10, mu=1.0, lam=10.0):
+    """Cantilever 4x1x1, macro 64x16x16 at L=4, clamped at x=0, body force (0,0,-1):
+    plain FP64 MG-PCG vs FP64 refinement around FP32 MG-PCG, time to true residual rtol."""
+    import torch
+
+    from sfem_gb300 import solvers as S
+    from sfem_gb300.mesh import SSMesh
+
+    m = SSMesh(nx, ny, nz, LEVEL, box=((0, 4), (0, 1), (0, 1)), perturb=0.0, seed=SEED)
+    H = S.Hierarchy(m, dirichlet_faces=("x0",), device=dev, vec=3)
+    b = torch.from_numpy(lumped_body_force(m, H.det.cpu().numpy())).to(dev)
+    for c in range(3):
+        b[3 * H.dirichlet[0].long() + c] = 0
+    ctx = S.context()
+    op64 = S.elasticity_op(ctx, H.spaces[0], H.adj, H.det, mu, lam, H.dirichlet[0], torch.float64)
+
+    def true_rel(x):
+        r = torch.zeros_like(b)
+        S.apply(op64, x, r)
+        return float(torch.linalg.vector_norm(b - r) / torch.linalg.vector_norm(b))
+
+    out = {"dofs": 3 * m.n_nodes(), "macro_elements": m.n_elements}
+    mg64, _ = S.build_elasticity_mg(ctx, H, torch.float64, mu=mu, lam=lam)
+    cg64 = S.cg(ctx, op64, mg64, rtol=rtol * 0.05, max_it=500)
+    x = torch.zeros_like(b)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    rc = S.solve(cg64, b, x)
+    torch.cuda.synchronize()
+    t64 = time.perf_counter() - t0
+    it64, _ = S.stats(cg64)
+    out["plain_fp64_mg_pcg"] = {"seconds": t64, "iterations": it64, "true_rel_residual": true_rel(x), "rc": rc}
+    x64 = x.clone()
+    mg32, op32 = S.build_elasticity_mg(ctx, H, torch.float32, mu=mu, lam=lam, eig_max=mg64.eigs)
+    inner = S.cg(ctx, op32, mg32, rtol=1e-4, max_it=40)
+    ir = S.iterative_refinement(ctx, op64, inner, max_it=30, rtol=rtol)
+    x = torch.zeros_like(b)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    rc = S.solve(ir, b, x)
+    torch.cuda.synchronize()
+    t32 = time.perf_counter() - t0
+    itir, _ = S.stats(ir)
+    out["mixed_fp32_mg_pcg_fp64_ir"] = {
+        "seconds": t32, "outer_iterations": itir, "true_rel_residual": true_rel(x), "rc": rc,
+        "solution_rel_diff_vs_plain_fp64": float(torch.linalg.vector_norm(x - x64) / torch.linalg.vector_norm(x64))}
+    out["speedup_mixed_vs_plain"] = t64 / t32 if t32 > 0 else None
+    return out
+
+
 def run_ours(args):
     import torch
 
@@ -337,7 +405,8 @@ def run_ours(args):
 
     solve = None
     if not args.no_solve:
-        solve = measure_solves(m, dev)
+        solve = {"poisson_sshex8_L4_48cube": measure_solves(m, dev),
+                 "elasticity_sshex8_L4_64x16x16": measure_elasticity_solves(dev)}
 
     peak, peak_kind = measured_peak_hbm()
     alg_bytes = 2 * 8 * N + (4 * (LEVEL + 1) ** 3 + 24) * E
