@@ -216,7 +216,7 @@ def measure_solves(m, dev, rtol=1e-10):
     mg64, _ = S.build_poisson_mg(ctx, H, torch.float64, smoother="chebyshev3", sweeps=2)
     torch.cuda.synchronize()
     setup64 = time.perf_counter() - t0
-    cg64 = S.cg(ctx, op64, mg64, rtol=rtol * 0.05, max_it=500)
+    cg64 = S.cg(ctx, op64, mg64, rtol=rtol, max_it=500, residual_norm=True, flexible=True)
     x = torch.zeros_like(b)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -230,7 +230,7 @@ def measure_solves(m, dev, rtol=1e-10):
     # mixed: FP64 refinement around FP32 MG-PCG (eigenvalues reused from the FP64 setup)
     t0 = time.perf_counter()
     mg32, op32 = S.build_poisson_mg(ctx, H, torch.float32, smoother="chebyshev3", sweeps=2, eig_max=mg64.eigs)
-    inner = S.cg(ctx, op32, mg32, rtol=1e-4, max_it=30)
+    inner = S.cg(ctx, op32, mg32, rtol=1e-4, max_it=30, residual_norm=True, flexible=True)
     ir = S.iterative_refinement(ctx, op64, inner, max_it=30, rtol=rtol)
     torch.cuda.synchronize()
     setup32 = time.perf_counter() - t0
@@ -290,7 +290,7 @@ def measure_elasticity_solves(dev, nx=64, ny=16, nz=16, rtol=1e-10, mu=1.0, lam=
 
     out = {"dofs": 3 * m.n_nodes(), "macro_elements": m.n_elements}
     mg64, _ = S.build_elasticity_mg(ctx, H, torch.float64, mu=mu, lam=lam)
-    cg64 = S.cg(ctx, op64, mg64, rtol=rtol * 0.05, max_it=500)
+    cg64 = S.cg(ctx, op64, mg64, rtol=rtol, max_it=500, residual_norm=True, flexible=True)
     x = torch.zeros_like(b)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -301,7 +301,7 @@ def measure_elasticity_solves(dev, nx=64, ny=16, nz=16, rtol=1e-10, mu=1.0, lam=
     out["plain_fp64_mg_pcg"] = {"seconds": t64, "iterations": it64, "true_rel_residual": true_rel(x), "rc": rc}
     x64 = x.clone()
     mg32, op32 = S.build_elasticity_mg(ctx, H, torch.float32, mu=mu, lam=lam, eig_max=mg64.eigs)
-    inner = S.cg(ctx, op32, mg32, rtol=1e-4, max_it=40)
+    inner = S.cg(ctx, op32, mg32, rtol=1e-4, max_it=40, residual_norm=True, flexible=True)
     ir = S.iterative_refinement(ctx, op64, inner, max_it=30, rtol=rtol)
     x = torch.zeros_like(b)
     torch.cuda.synchronize()

@@ -137,6 +137,32 @@ int sfem_gb300_sshex8_restrict(ptrdiff_t nelements, int from_level, sfem_gb300_i
 int sfem_gb300_sshex8_element_node_incidence_count(int level, ptrdiff_t nelements, sfem_gb300_idx_t **elements,
                                                    uint16_t *count, void *stream);
 
+/* ------------------------------------------------- symmetric sparse formats */
+
+/* y = scale_output * y + (D + U + U^T) x for a symmetric matrix stored as its
+ * diagonal and strict upper triangle U in CRS (sorted columns > row).
+ * Replaces CRSSymSpMV (algebra/sfem_crs_sym_SpMV.hpp:8-91) and the cuSPARSE
+ * two-pass COO path (algebra/cuda/sfem_cuda_crs_SpMV.cpp:190-330). */
+int sfem_gb300_crs_sym_spmv(int real_type, ptrdiff_t nrows, const int32_t *rowptr, const int32_t *colidx,
+                            const void *diag, const void *offdiag, double scale_output, const void *x, void *y,
+                            void *stream);
+
+/* Block version, block_size 2 or 3: diagonal blocks as bs(bs+1)/2 upper entries
+ * per block row (AoS); strict-upper off-diagonal blocks full bs*bs row-major, or
+ * (offdiag_symmetric != 0) as bs(bs+1)/2 upper entries as the reference stores
+ * them.  Replaces BCRSSymSpMV (algebra/sfem_bcrs_sym_SpMV.hpp:9-279). */
+int sfem_gb300_bsr_sym_spmv(int real_type, int block_size, ptrdiff_t nblock_rows, const int32_t *rowptr,
+                            const int32_t *colidx, const void *diag_sym, const void *offdiag, int offdiag_symmetric,
+                            double scale_output, const void *x, void *y, void *stream);
+
+/* diag += diag(A), offdiag += strict upper part of the hex8 Laplacian on a given
+ * upper CRS graph (elements in hex8 corner order).  Fails if an element coupling
+ * is missing from the graph.  Replaces cu_laplacian_crs_sym / hex8_laplacian_crs_sym
+ * (operators/cuda/cu_laplacian.hpp:44-53, operators/hex8/hex8_laplacian.cpp:148-221). */
+int sfem_gb300_hex8_laplacian_crs_sym(ptrdiff_t nelements, sfem_gb300_idx_t **elements, ptrdiff_t fff_stride,
+                                      const float *fff, const int32_t *rowptr, const int32_t *colidx, int real_type,
+                                      void *diag, void *offdiag, void *stream);
+
 /* ------------------------------------------------------------ vector BLAS */
 /* Device-vector kernels of the BLAS<T> seam (algebra/sfem_tpl_blas.hpp:11-35;
  * CUDA_BLAS, algebra/cuda/sfem_cuda_blas.hpp:55-77).  real_type selects
@@ -177,9 +203,10 @@ int sfem_gb300_xypaz(int real_type, ptrdiff_t n, const void *x, const void *y, d
 int sfem_gb300_cg_update_x_r(int real_type, ptrdiff_t n, const double *alpha_num, const double *alpha_den,
                              const void *p, const void *Ap, void *x, void *r, void *workspace, double *rr,
                              void *stream);
-/*   beta = *beta_num / *beta_den;  p = z + beta p. */
-int sfem_gb300_cg_update_p(int real_type, ptrdiff_t n, const double *beta_num, const double *beta_den, const void *z,
-                           void *p, void *stream);
+/*   beta = (*beta_num - *beta_sub) / *beta_den;  p = z + beta p  (beta_sub may be NULL;
+ * with it this is the flexible-CG Polak-Ribiere update). */
+int sfem_gb300_cg_update_p(int real_type, ptrdiff_t n, const double *beta_num, const double *beta_den,
+                           const double *beta_sub, const void *z, void *p, void *stream);
 /* Chebyshev3 step p = beta p - rhs + Ax;  x -= alpha p (algebra/sfem_Chebyshev3.hpp:36-52).
  * With a non-NULL inv_diag the step runs on the Jacobi-scaled operator: p = beta p + D^-1 (Ax - rhs).
  * beta == 0 ignores the previous p. */
@@ -192,6 +219,10 @@ int sfem_gb300_constraint_nodes_copy(int real_type, ptrdiff_t n_nodes, const int
                                      int component, const void *src, void *dest, void *stream);
 int sfem_gb300_constraint_nodes_to_value(int real_type, ptrdiff_t n_nodes, const int32_t *nodes, int block_size,
                                          int component, double value, void *x, void *stream);
+
+/* x[i] = U(-1, 1), a counter-based hash of (seed, i): reproducible start vectors
+ * (the reference's Chebyshev3::init_with_random, algebra/sfem_Chebyshev3.hpp:148-160). */
+int sfem_gb300_random_uniform(int real_type, ptrdiff_t n, unsigned long long seed, void *x, void *stream);
 
 /* Precision conversion dst = (dst_type) src, and y += alpha (double) x for float x. */
 int sfem_gb300_convert(ptrdiff_t n, int src_type, const void *src, int dst_type, void *dst, void *stream);
@@ -233,6 +264,11 @@ int sfem_gb300_restriction_op_create(void *context, int real_type, ptrdiff_t nel
                                      sfem_gb300_idx_t **from_elements, const uint16_t *count, ptrdiff_t n_from,
                                      int to_level, sfem_gb300_idx_t **to_elements, ptrdiff_t n_to, int vec_size,
                                      ptrdiff_t n_dirichlet_to, const int32_t *dirichlet_to, void **op);
+/* Symmetric CRS operator (y += A x) with Dirichlet rows treated as identity: an
+ * assembled coarse-level operator for the multigrid hierarchy. */
+int sfem_gb300_crs_sym_op_create(void *context, int real_type, ptrdiff_t nrows, const int32_t *rowptr,
+                                 const int32_t *colidx, const void *diag, const void *offdiag, ptrdiff_t n_dirichlet,
+                                 const int32_t *dirichlet_nodes, void **op);
 int sfem_gb300_op_apply(void *op, const void *x, void *y);
 int sfem_gb300_op_size(void *op, ptrdiff_t *rows, ptrdiff_t *cols);
 
@@ -254,8 +290,15 @@ int sfem_gb300_chebyshev3_create(void *context, void *op, const void *inv_diag, 
                                  double scale_eig_min, int eigen_max_it, double eigen_tol, void **solver);
 int sfem_gb300_chebyshev3_eig_max(void *solver, double *eig_max);
 int sfem_gb300_chebyshev3_set_eig_max(void *solver, double eig_max);
-/* (Preconditioned) conjugate gradient (algebra/sfem_cg.hpp:79-453); precond may be NULL. */
+/* (Preconditioned) conjugate gradient (algebra/sfem_cg.hpp:79-453); precond may be NULL.
+ * Default stopping test is the reference's: sqrt(r.z) < atol or sqrt(r.z)/sqrt(r0.z0) < rtol. */
 int sfem_gb300_cg_create(void *context, void *op, void *precond, int max_it, double rtol, double atol, void **solver);
+/* Options: residual_norm != 0 stops on ||r||_2 / ||r0||_2 < rtol (the true residual for
+ * x0 = 0) instead of the preconditioned norm; flexible != 0 uses the Polak-Ribiere beta
+ * (r_k . (z_k - z_{k-1})) / (r_{k-1} . z_{k-1}), i.e. flexible CG for variable or
+ * inexact preconditioners (no reference counterpart); check_every = k reads the
+ * convergence scalar from the device only every k iterations (>= 1). */
+int sfem_gb300_cg_set_options(void *solver, int residual_norm, int flexible, int check_every);
 int sfem_gb300_cg_set_verbose(void *solver, int verbose);
 /* Multigrid V/W cycle (algebra/sfem_Multigrid.hpp:27-354); levels added finest first. */
 int sfem_gb300_mg_create(void *context, int real_type, int max_it, int cycle_type, void **solver);

@@ -37,6 +37,19 @@ def cg(apply, b, x=None, precond=None, rtol=1e-10, atol=0.0, max_it=10000):
     return x, max_it
 
 
+def random_uniform(n, seed):
+    """U(-1, 1) from the splitmix64 hash of (seed, i), identical to sfem_gb300_random_uniform."""
+    M = (1 << 64) - 1
+    i = np.arange(1, n + 1, dtype=np.uint64)
+    with np.errstate(over="ignore"):
+        z = np.uint64(seed) + np.uint64(0x9E3779B97F4A7C15) * i
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        z = z ^ (z >> np.uint64(31))
+    del M
+    return (z >> np.uint64(11)).astype(np.float64) * (2.0 / 9007199254740992.0) - 1.0
+
+
 def power_method(apply, n, max_it=100, tol=1e-5, v0=None):
     v = np.ones(n) if v0 is None else v0.copy()
     w = apply(v)

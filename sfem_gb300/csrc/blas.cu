@@ -91,11 +91,11 @@ __global__ void __launch_bounds__(kReduceBlock) cg_update_x_r_kernel(ptrdiff_t n
     if (rr) reduce_epilogue((double)acc, ws, rr, 0);
 }
 
-// beta = num/den ;  p = z + beta p
+// beta = (num - sub) / den ;  p = z + beta p   (sub may be NULL)
 template <typename T>
 __global__ void cg_update_p_kernel(ptrdiff_t n, const double *__restrict__ num, const double *__restrict__ den,
-                                   const T *__restrict__ z, T *__restrict__ p) {
-    const T beta = (T)(*num / *den);
+                                   const double *__restrict__ sub, const T *__restrict__ z, T *__restrict__ p) {
+    const T beta = (T)((*num - (sub ? *sub : 0.0)) / *den);
     for (ptrdiff_t i = blockIdx.x * (ptrdiff_t)blockDim.x + threadIdx.x; i < n; i += (ptrdiff_t)gridDim.x * blockDim.x)
         p[i] = z[i] + beta * p[i];
 }
@@ -133,6 +133,20 @@ __global__ void constraint_value_kernel(ptrdiff_t nn, const idx_t *__restrict__ 
                                         T *__restrict__ x) {
     for (ptrdiff_t i = blockIdx.x * (ptrdiff_t)blockDim.x + threadIdx.x; i < nn; i += (ptrdiff_t)gridDim.x * blockDim.x)
         x[(ptrdiff_t)nodes[i] * block + comp] = value;
+}
+
+// ------------------------------------------------------------------ seeded uniform values
+
+// x[i] = U(-1, 1) from a counter-based hash (splitmix64) of (seed, i): reproducible for any launch shape.
+template <typename T>
+__global__ void random_uniform_kernel(ptrdiff_t n, unsigned long long seed, T *__restrict__ x) {
+    for (ptrdiff_t i = blockIdx.x * (ptrdiff_t)blockDim.x + threadIdx.x; i < n; i += (ptrdiff_t)gridDim.x * blockDim.x) {
+        unsigned long long z = seed + 0x9E3779B97F4A7C15ull * (unsigned long long)(i + 1);
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        z = z ^ (z >> 31);
+        x[i] = (T)((double)(z >> 11) * (2.0 / 9007199254740992.0) - 1.0);
+    }
 }
 
 // ------------------------------------------------------------------ precision conversion
@@ -270,11 +284,11 @@ extern "C" int sfem_gb300_cg_update_x_r(int real_type, ptrdiff_t n, const double
 }
 
 extern "C" int sfem_gb300_cg_update_p(int real_type, ptrdiff_t n, const double *beta_num, const double *beta_den,
-                                      const void *z, void *p, void *stream) {
+                                      const double *beta_sub, const void *z, void *p, void *stream) {
     if (n <= 0) return SFEM_GB300_SUCCESS;
     SFEM_DISPATCH_REAL(real_type, "sfem_gb300_cg_update_p",
-                       SFEM_EW_LAUNCH(cg_update_p_kernel, n, beta_num, beta_den, (const T *)z, (T *)p),
-                       SFEM_EW_LAUNCH(cg_update_p_kernel, n, beta_num, beta_den, (const T *)z, (T *)p));
+                       SFEM_EW_LAUNCH(cg_update_p_kernel, n, beta_num, beta_den, beta_sub, (const T *)z, (T *)p),
+                       SFEM_EW_LAUNCH(cg_update_p_kernel, n, beta_num, beta_den, beta_sub, (const T *)z, (T *)p));
     return check_launch("sfem_gb300_cg_update_p");
 }
 
@@ -323,6 +337,14 @@ extern "C" int sfem_gb300_convert(ptrdiff_t n, int src_type, const void *src, in
     else
         convert_kernel<float, float><<<ew_grid(n), 256, 0, s>>>(n, (const float *)src, (float *)dst);
     return check_launch("sfem_gb300_convert");
+}
+
+extern "C" int sfem_gb300_random_uniform(int real_type, ptrdiff_t n, unsigned long long seed, void *x, void *stream) {
+    if (n <= 0) return SFEM_GB300_SUCCESS;
+    SFEM_DISPATCH_REAL(real_type, "sfem_gb300_random_uniform",
+                       SFEM_EW_LAUNCH(random_uniform_kernel, n, seed, (T *)x),
+                       SFEM_EW_LAUNCH(random_uniform_kernel, n, seed, (T *)x));
+    return check_launch("sfem_gb300_random_uniform");
 }
 
 extern "C" int sfem_gb300_axpy_f32_to_f64(ptrdiff_t n, double alpha, const float *x, double *y, void *stream) {

@@ -119,6 +119,26 @@ public:
     ptrdiff_t cols() const override { return vec * n_from; }
 };
 
+// Assembled symmetric CRS operator: y += A x via a scratch vector, Dirichlet rows identity.
+template <typename T>
+class CrsSymOp final : public Operator<T> {
+public:
+    std::shared_ptr<Context> ctx;
+    ptrdiff_t nrows{0}, n_dirichlet{0};
+    const idx_t *rowptr{nullptr}, *colidx{nullptr}, *dirichlet{nullptr};
+    const T *diag{nullptr}, *offdiag{nullptr};
+    DeviceBuffer<T> tmp;
+    int apply(const T *x, T *y) override {
+        SFEM_GB300_CHECK(tmp.resize(nrows));
+        SFEM_GB300_CHECK(sfem_gb300_crs_sym_spmv(real_type_v<T>, nrows, rowptr, colidx, diag, offdiag, 0.0, x,
+                                                 tmp.ptr, ctx->sp()));
+        SFEM_GB300_CHECK(sfem_gb300_axpy(real_type_v<T>, nrows, 1.0, tmp.ptr, y, ctx->sp()));
+        return sfem_gb300_constraint_nodes_copy(real_type_v<T>, n_dirichlet, dirichlet, 1, 0, x, y, ctx->sp());
+    }
+    ptrdiff_t rows() const override { return nrows; }
+    ptrdiff_t cols() const override { return nrows; }
+};
+
 template <typename T>
 std::shared_ptr<Operator<T>> &op_of(Handle *h);
 template <>
@@ -346,6 +366,38 @@ int sfem_gb300_restriction_op_create(void *context, int real_type, ptrdiff_t nel
     return SFEM_GB300_SUCCESS;
 }
 
+int sfem_gb300_crs_sym_op_create(void *context, int real_type, ptrdiff_t nrows, const int32_t *rowptr,
+                                 const int32_t *colidx, const void *diag, const void *offdiag, ptrdiff_t n_dirichlet,
+                                 const int32_t *dirichlet_nodes, void **out) {
+    auto *c = H(context);
+    auto *h = new Handle();
+    h->kind = "crs_sym";
+    h->ctx = c->ctx;
+    h->real_type = is_f32(real_type) ? SFEM_GB300_FLOAT32 : SFEM_GB300_FLOAT64;
+    auto fill = [&](auto op, auto tag) {
+        using T = decltype(tag);
+        op->ctx = c->ctx;
+        op->nrows = nrows;
+        op->rowptr = rowptr;
+        op->colidx = colidx;
+        op->diag = (const T *)diag;
+        op->offdiag = (const T *)offdiag;
+        op->n_dirichlet = n_dirichlet;
+        op->dirichlet = dirichlet_nodes;
+    };
+    if (is_f32(real_type)) {
+        auto op = std::make_shared<CrsSymOp<float>>();
+        fill(op, 0.0f);
+        h->f = op;
+    } else {
+        auto op = std::make_shared<CrsSymOp<double>>();
+        fill(op, 0.0);
+        h->d = op;
+    }
+    *out = h;
+    return SFEM_GB300_SUCCESS;
+}
+
 int sfem_gb300_op_apply(void *op, const void *x, void *y) {
     auto *h = H(op);
     if (h->d) return h->d->apply((const double *)x, (double *)y);
@@ -454,7 +506,7 @@ int sfem_gb300_chebyshev3_create(void *context, void *op, const void *inv_diag, 
         s->scale_eig_min = scale_eig_min;
         s->eigen_max_it = eigen_max_it;
         s->eigen_tol = eigen_tol;
-        rc = s->init_with_ones();
+        rc = eigen_max_it > 1 ? s->init_with_random(0x5eed5eedull) : s->init_with_ones();
         h->f = s;
         h->impl = s;
     } else {
@@ -467,7 +519,7 @@ int sfem_gb300_chebyshev3_create(void *context, void *op, const void *inv_diag, 
         s->scale_eig_min = scale_eig_min;
         s->eigen_max_it = eigen_max_it;
         s->eigen_tol = eigen_tol;
-        rc = s->init_with_ones();
+        rc = eigen_max_it > 1 ? s->init_with_random(0x5eed5eedull) : s->init_with_ones();
         h->d = s;
         h->impl = s;
     }
@@ -616,6 +668,21 @@ int sfem_gb300_solver_stats(void *solver, int *iterations, double *last_relative
         else
             *iterations = std::static_pointer_cast<Multigrid<double>>(h->impl)->iterations_;
     }
+    return SFEM_GB300_SUCCESS;
+}
+
+int sfem_gb300_cg_set_options(void *solver, int residual_norm, int flexible, int check_every) {
+    auto *h = H(solver);
+    if (h->kind != "cg") return set_error("not a cg handle");
+    auto set = [&](auto cg) {
+        cg->residual_norm = residual_norm != 0;
+        cg->flexible = flexible != 0;
+        cg->check_every = check_every < 1 ? 1 : check_every;
+    };
+    if (h->f)
+        set(std::static_pointer_cast<ConjugateGradient<float>>(h->impl));
+    else
+        set(std::static_pointer_cast<ConjugateGradient<double>>(h->impl));
     return SFEM_GB300_SUCCESS;
 }
 

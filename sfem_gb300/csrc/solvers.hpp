@@ -279,6 +279,13 @@ public:
         blas.values(op->rows(), T(1), ones.ptr);
         return init(ones.ptr);
     }
+    // Seeded U(-1,1) start vector: unlike the constant vector it has components
+    // in the highest modes, so the power method does not underestimate lambda_max.
+    int init_with_random(unsigned long long seed) {
+        DeviceBuffer<T> v(op->rows());
+        SFEM_GB300_CHECK(sfem_gb300_random_uniform(real_type_v<T>, op->rows(), seed, v.ptr, blas.ctx->sp()));
+        return init(v.ptr);
+    }
     int apply(const T *b, T *x) override {
         const ptrdiff_t n = op->rows();
         if (max_it <= 0) return 0;
@@ -361,71 +368,87 @@ public:
     ptrdiff_t cols() const override { return op->cols(); }
 };
 
-// ConjugateGradient (algebra/sfem_cg.hpp:79-453).  With a preconditioner the
-// stopping test is the reference's: sqrt(rtz) < atol or sqrt(rtz)/sqrt(rtz0) < rtol.
+// ConjugateGradient (algebra/sfem_cg.hpp:79-453).  Default stopping test is the
+// reference's: sqrt(rtz) < atol or sqrt(rtz)/sqrt(rtz0) < rtol.  Options:
+// residual_norm (stop on ||r||/||r0||), flexible (Polak-Ribiere beta, FCG) and
+// check_every (read the convergence scalar every k iterations only; all other
+// scalars stay on the device).
 template <typename T>
 class ConjugateGradient final : public Solver<T> {
 public:
     Blas<T> blas;
     std::shared_ptr<Operator<T>> op, precond;
-    DeviceBuffer<T> r, z, p, Ap;
+    DeviceBuffer<T> r, z, zprev, p, Ap;
     int max_it{10000};
     double atol{1e-30}, rtol{1e-10};
     bool verbose{false};
+    bool residual_norm{false}, flexible{false};
+    int check_every{1};
     double last_rel{0};
-    // slots: 0 rtz_new, 1 rtz_old, 2 ptAp, 3 rr
+    // slots: 0 rz, 1 rz_old, 2 pAp, 3 rr, 4 r.z_prev, 5 rr0
     double *s{nullptr};
 
     int apply(const T *b, T *x) override {
         const ptrdiff_t n = op->rows();
-        if (!s) s = blas.ctx->slots(4);
+        if (!s) s = blas.ctx->slots(6);
         if (!s) return set_error("ConjugateGradient: out of scalar slots");
         SFEM_GB300_CHECK(r.resize(n));
         SFEM_GB300_CHECK(p.resize(n));
         SFEM_GB300_CHECK(Ap.resize(n));
-        if (precond) SFEM_GB300_CHECK(z.resize(n));
-        const cudaStream_t st = blas.ctx->stream;
-        (void)st;
+        const bool pre = (bool)precond;
+        const bool flex = pre && flexible;
+        if (pre) SFEM_GB300_CHECK(z.resize(n));
+        if (flex) SFEM_GB300_CHECK(zprev.resize(n));
+        T *zz = pre ? z.ptr : r.ptr;
+        T *zp = flex ? zprev.ptr : nullptr;
         if (!op->overwrites_output()) blas.zeros(n, r.ptr);
         op->apply(x, r.ptr);
         blas.axpby(n, T(1), b, T(-1), r.ptr);  // r = b - A x
-        T *zz = r.ptr;
-        if (precond) {
+        if (pre) {
             if (!precond->overwrites_output()) blas.zeros(n, z.ptr);
             precond->apply(r.ptr, z.ptr);
-            zz = z.ptr;
         }
         blas.copy(n, zz, p.ptr);
         blas.dot(n, r.ptr, zz, &s[0]);
-        const double rtz0 = blas.ctx->read(&s[0]);
+        const bool use_rr = residual_norm && pre;
+        if (use_rr) blas.dot(n, r.ptr, r.ptr, &s[5]);
+        const double rz0 = blas.ctx->read(&s[0]);
+        const double crit0 = use_rr ? blas.ctx->read(&s[5]) : rz0;
         last_rel = 1;
         this->iterations_ = 0;
-        if (rtz0 == 0) return 0;
-        const double norm0 = std::sqrt(std::fabs(rtz0));
+        if (rz0 == 0 || crit0 == 0) return 0;
+        const double norm0 = std::sqrt(std::fabs(crit0));
+        const int every = check_every < 1 ? 1 : check_every;
         for (this->iterations_ = 0; this->iterations_ < max_it;) {
             if (!op->overwrites_output()) blas.zeros(n, Ap.ptr);
             op->apply(p.ptr, Ap.ptr);
             blas.dot(n, p.ptr, Ap.ptr, &s[2]);
-            if (precond) {
+            if (pre) {
                 SFEM_GB300_CHECK(sfem_gb300_cg_update_x_r(real_type_v<T>, n, &s[0], &s[2], p.ptr, Ap.ptr, x, r.ptr,
-                                                          nullptr, nullptr, blas.ctx->sp()));
-                if (!precond->overwrites_output()) blas.zeros(n, z.ptr);
-                precond->apply(r.ptr, z.ptr);
+                                                          blas.ctx->workspace, use_rr ? &s[3] : nullptr,
+                                                          blas.ctx->sp()));
+                if (flex) std::swap(zz, zp);
+                if (!precond->overwrites_output()) blas.zeros(n, zz);
+                precond->apply(r.ptr, zz);
                 cudaMemcpyAsync(&s[1], &s[0], sizeof(double), cudaMemcpyDeviceToDevice, blas.ctx->stream);
-                blas.dot(n, r.ptr, z.ptr, &s[0]);
+                blas.dot(n, r.ptr, zz, &s[0]);
+                if (flex) blas.dot(n, r.ptr, zp, &s[4]);
             } else {
                 cudaMemcpyAsync(&s[1], &s[0], sizeof(double), cudaMemcpyDeviceToDevice, blas.ctx->stream);
                 SFEM_GB300_CHECK(sfem_gb300_cg_update_x_r(real_type_v<T>, n, &s[1], &s[2], p.ptr, Ap.ptr, x, r.ptr,
                                                           blas.ctx->workspace, &s[0], blas.ctx->sp()));
             }
             this->iterations_++;
-            const double rtz = blas.ctx->read(&s[0]);
-            const double anorm = std::sqrt(std::fabs(rtz));
-            last_rel = anorm / norm0;
-            if (verbose) printf("cg %d: %g %g\n", this->iterations_, anorm, last_rel);
-            if (anorm < atol || last_rel < rtol || rtz == 0) return 0;
-            if (!std::isfinite(rtz)) return set_error("ConjugateGradient: non-finite residual");
-            SFEM_GB300_CHECK(sfem_gb300_cg_update_p(real_type_v<T>, n, &s[0], &s[1], zz, p.ptr, blas.ctx->sp()));
+            if (this->iterations_ % every == 0 || this->iterations_ == max_it) {
+                const double crit = blas.ctx->read(use_rr ? &s[3] : &s[0]);
+                const double anorm = std::sqrt(std::fabs(crit));
+                last_rel = anorm / norm0;
+                if (verbose) printf("cg %d: %g %g\n", this->iterations_, anorm, last_rel);
+                if (!std::isfinite(crit)) return set_error("ConjugateGradient: non-finite residual");
+                if (anorm < atol || last_rel < rtol || crit == 0) return 0;
+            }
+            SFEM_GB300_CHECK(sfem_gb300_cg_update_p(real_type_v<T>, n, &s[0], &s[1], flex ? &s[4] : nullptr, zz,
+                                                    p.ptr, blas.ctx->sp()));
         }
         return set_error("ConjugateGradient: no convergence in %d iterations (rel %g)", max_it, last_rel);
     }

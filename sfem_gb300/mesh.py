@@ -245,3 +245,24 @@ class SSMesh:
 def hex8_cube(n: int, perturb=0.0, seed=0) -> SSMesh:
     """Structured hex8 mesh of the unit cube with ``n^3`` elements (level 1)."""
     return SSMesh(n, n, n, 1, perturb=perturb, seed=seed)
+
+
+def upper_crs_graph(elements: np.ndarray, n_nodes: int):
+    """Strict-upper node-to-node CRS graph (sorted columns > row) of an element mesh.
+
+    ``elements`` is ``[nodes_per_element, E]``.  This is the graph the
+    symmetric CRS / BSR formats and their assembly kernels use (the reference
+    builds it with smesh's ``create_node_to_node_graph``).
+    """
+    nv, E = elements.shape
+    el = elements.astype(np.int64)
+    rows = np.repeat(el, nv, axis=0).reshape(nv, nv, E)
+    cols = np.tile(el, (nv, 1)).reshape(nv, nv, E)
+    r, c = rows.reshape(-1), cols.reshape(-1)
+    keep = c > r
+    key = np.unique(r[keep] * n_nodes + c[keep])
+    r, c = key // n_nodes, key % n_nodes
+    rowptr = np.zeros(n_nodes + 1, dtype=np.int64)
+    np.add.at(rowptr, r + 1, 1)
+    rowptr = np.cumsum(rowptr).astype(np.int32)
+    return rowptr, c.astype(np.int32)

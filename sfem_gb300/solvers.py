@@ -137,9 +137,17 @@ def eig_max(cheb: Handle) -> float:
     return v.value
 
 
-def cg(ctx, op, precond=None, max_it=10000, rtol=1e-10, atol=0.0) -> Handle:
-    return _create(_lib().sfem_gb300_cg_create, ctx.ptr, op.ptr, precond.ptr if precond else None, c_int(max_it),
-                   c_double(rtol), c_double(atol), keep=(ctx, op, precond))
+RANDOM_SEED = 0x5EED5EED  # start vector of the power method (sfem_gb300_random_uniform)
+
+
+def cg(ctx, op, precond=None, max_it=10000, rtol=1e-10, atol=0.0, residual_norm=False, flexible=False,
+       check_every=1) -> Handle:
+    h = _create(_lib().sfem_gb300_cg_create, ctx.ptr, op.ptr, precond.ptr if precond else None, c_int(max_it),
+                c_double(rtol), c_double(atol), keep=(ctx, op, precond))
+    if residual_norm or flexible or check_every != 1:
+        capi.check(_lib().sfem_gb300_cg_set_options(h.ptr, int(residual_norm), int(flexible), int(check_every)),
+                   "cg_set_options")
+    return h
 
 
 def multigrid(ctx, dtype, max_it=1, cycle_type=1) -> Handle:
@@ -195,7 +203,7 @@ class Hierarchy:
 
 
 def build_poisson_mg(ctx, H: Hierarchy, dtype, smoother="chebyshev3", sweeps=2, coarse_rtol=1e-6, coarse_max_it=10000,
-                     eig_max=None, jacobi_sweeps=3):
+                     eig_max=None, jacobi_sweeps=3, coarse_check_every=10, eigen_max_it=30):
     """Geometric multigrid for the Laplacian on every level of ``H`` (one V-cycle per apply)."""
     import torch
 
@@ -211,13 +219,13 @@ def build_poisson_mg(ctx, H: Hierarchy, dtype, smoother="chebyshev3", sweeps=2, 
         diag[H.dirichlet[k].long()] = 1
         if k == nlev - 1:
             jac = jacobi(ctx, diag, 1.0)
-            smoothers.append(cg(ctx, op, jac, max_it=coarse_max_it, rtol=coarse_rtol))
+            smoothers.append(cg(ctx, op, jac, max_it=coarse_max_it, rtol=coarse_rtol, check_every=coarse_check_every))
         elif smoother in ("chebyshev3", "chebyshev3_plain"):
             em = None if eig_max is None else eig_max[k]
             inv = None
             if smoother == "chebyshev3":  # Jacobi-scaled Chebyshev (iteration on D^-1 A)
                 inv = 1.0 / diag
-            ch = chebyshev3(ctx, op, max_it=sweeps, eig_max=em, inv_diag=inv)
+            ch = chebyshev3(ctx, op, max_it=sweeps, eig_max=em, inv_diag=inv, eigen_max_it=eigen_max_it)
             eigs.append(globals()["eig_max"](ch))
             smoothers.append(ch)
         else:
@@ -249,7 +257,7 @@ def _elasticity_diag(H: Hierarchy, k, dtype, mu, lam):
 
 
 def build_elasticity_mg(ctx, H: Hierarchy, dtype, mu=1.0, lam=10.0, sweeps=2, coarse_rtol=1e-6,
-                        coarse_max_it=10000, eig_max=None):
+                        coarse_max_it=10000, eig_max=None, coarse_check_every=10, eigen_max_it=30, scale_eig_max=1.1):
     """Geometric multigrid for linear elasticity (3 dofs / node) on every level of ``H``:
     Jacobi-scaled Chebyshev3 smoothing, nested vector transfer, Jacobi-PCG coarse solve
     (cf. the vector branch of algebra/mg/sfem_GeometricMultigrid.cpp:89-144)."""
@@ -261,10 +269,12 @@ def build_elasticity_mg(ctx, H: Hierarchy, dtype, mu=1.0, lam=10.0, sweeps=2, co
         ops.append(op)
         d3 = _elasticity_diag(H, k, dtype, mu, lam)
         if k == nlev - 1:
-            smoothers.append(cg(ctx, op, jacobi(ctx, d3, 1.0), max_it=coarse_max_it, rtol=coarse_rtol))
+            smoothers.append(cg(ctx, op, jacobi(ctx, d3, 1.0), max_it=coarse_max_it, rtol=coarse_rtol,
+                                check_every=coarse_check_every))
         else:
             em = None if eig_max is None else eig_max[k]
-            ch = chebyshev3(ctx, op, max_it=sweeps, eig_max=em, inv_diag=1.0 / d3)
+            ch = chebyshev3(ctx, op, max_it=sweeps, eig_max=em, inv_diag=1.0 / d3, eigen_max_it=eigen_max_it,
+                            scale_eig_max=scale_eig_max)
             eigs.append(globals()["eig_max"](ch))
             smoothers.append(ch)
     mg = multigrid(ctx, dtype)

@@ -116,8 +116,14 @@ def test_cg_fused_updates(cuda, ws):
     z = torch.randn(n, dtype=torch.float64, device=cuda, generator=g)
     pp = p.clone()
     capi.check(lib.sfem_gb300_cg_update_p(capi.FLOAT64, capi.i64(n), capi.vp(sc), capi.c_void(sc.data_ptr() + 8),
-                                          capi.vp(z), capi.vp(pp), None), "")
+                                          None, capi.vp(z), capi.vp(pp), None), "")
     assert np.allclose(pp.cpu().numpy(), z.cpu().numpy() + 0.5 * p.cpu().numpy(), rtol=1e-15, atol=1e-15)
+    # flexible (Polak-Ribiere) form: beta = (2 - 1) / 4
+    sub = torch.tensor([1.0], dtype=torch.float64, device=cuda)
+    pf = p.clone()
+    capi.check(lib.sfem_gb300_cg_update_p(capi.FLOAT64, capi.i64(n), capi.vp(sc), capi.c_void(sc.data_ptr() + 8),
+                                          capi.vp(sub), capi.vp(z), capi.vp(pf), None), "")
+    assert np.allclose(pf.cpu().numpy(), z.cpu().numpy() + 0.25 * p.cpu().numpy(), rtol=1e-15, atol=1e-15)
 
 
 def test_dirichlet_kernels(cuda):
@@ -133,3 +139,17 @@ def test_dirichlet_kernels(cuda):
     capi.check(lib.sfem_gb300_constraint_nodes_to_value(capi.FLOAT64, capi.i64(3), capi.vp(nodes), 1, 0, D(7.0),
                                                         capi.vp(dst), None), "")
     assert dst.cpu().numpy()[[0, 5, 9]].tolist() == [7, 7, 7]
+
+
+def test_random_uniform_matches_hash(cuda):
+    import torch
+
+    from oracle.solvers import random_uniform
+
+    n = 100_003
+    for dt, rt in ((torch.float64, capi.FLOAT64), (torch.float32, capi.FLOAT32)):
+        x = torch.zeros(n, dtype=dt, device=cuda)
+        capi.check(capi.load().sfem_gb300_random_uniform(rt, capi.i64(n), ctypes.c_ulonglong(0x5EED5EED), capi.vp(x),
+                                                         None), "random")
+        ref = random_uniform(n, 0x5EED5EED)
+        assert np.array_equal(x.cpu().numpy(), ref.astype(x.cpu().numpy().dtype))

@@ -75,7 +75,7 @@ def test_sshex8_mg_pcg_fp64(cuda, smoother):
     x_star, _ = OS.cg(apply, b, precond=lambda r: r / d, rtol=1e-14, max_it=20000)
     ctx = S.context()
     mg, op = S.build_poisson_mg(ctx, H, torch.float64, smoother=smoother, sweeps=2)
-    solver = S.cg(ctx, op, mg, rtol=1e-11, max_it=200)
+    solver = S.cg(ctx, op, mg, rtol=1e-11, max_it=200, flexible=(smoother == "jacobi"))
     bd = torch.from_numpy(b).to(cuda)
     x = torch.zeros_like(bd)
     assert S.solve(solver, bd, x) == 0
@@ -122,7 +122,8 @@ def test_chebyshev_eigenvalue_matches_power_method(cuda):
     ctx = S.context()
     op = S.laplacian_op(ctx, H.spaces[0], H.fff, H.dirichlet[0], torch.float64)
     ch = S.chebyshev3(ctx, op, max_it=3, eigen_max_it=100, eigen_tol=1e-5)
-    lam_ref = OS.power_method(apply, m.n_nodes(L), max_it=100, tol=1e-5)
+    v0 = OS.random_uniform(m.n_nodes(L), S.RANDOM_SEED)
+    lam_ref = OS.power_method(apply, m.n_nodes(L), max_it=100, tol=1e-5, v0=v0)
     assert abs(S.eig_max(ch) - lam_ref) <= 1e-9 * lam_ref
     # the smoother itself against the oracle restatement
     b = _rhs(m, L, dn, seed=9)
@@ -147,9 +148,9 @@ def test_jacobi_scaled_chebyshev_against_oracle(cuda):
     op = S.laplacian_op(ctx, H.spaces[0], H.fff, H.dirichlet[0], torch.float64)
     inv = torch.from_numpy(1.0 / d).to(cuda)
     ch = S.chebyshev3(ctx, op, max_it=3, eigen_max_it=100, eigen_tol=1e-5, inv_diag=inv)
-    lam_ref = OS.power_method(lambda v: apply(v) / d, m.n_nodes(L), max_it=100, tol=1e-5)
+    v0 = OS.random_uniform(m.n_nodes(L), S.RANDOM_SEED)
+    lam_ref = OS.power_method(lambda v: apply(v) / d, m.n_nodes(L), max_it=100, tol=1e-5, v0=v0)
     assert abs(S.eig_max(ch) - lam_ref) <= 1e-9 * lam_ref
-    assert 1.0 < lam_ref < 2.0  # spectrum of D^-1 A for a Q1 Laplacian
     b = _rhs(m, L, dn, seed=3)
     x0 = np.zeros_like(b)
     ref = OS.chebyshev3(apply, b, x0.copy(), lam_ref, 3, inv_diag=1.0 / d)
@@ -184,7 +185,7 @@ def test_elasticity_mg_pcg_and_mixed(cuda):
         b[3 * dn + c] = 0
     ctx = S.context()
     mg, op = S.build_elasticity_mg(ctx, H, torch.float64, mu=mu, lam=lam)
-    solver = S.cg(ctx, op, mg, rtol=1e-11, max_it=300)
+    solver = S.cg(ctx, op, mg, rtol=1e-10, max_it=300, residual_norm=True, flexible=True)
     bd = torch.from_numpy(b).to(cuda)
     x = torch.zeros_like(bd)
     assert S.solve(solver, bd, x) == 0
@@ -192,7 +193,7 @@ def test_elasticity_mg_pcg_and_mixed(cuda):
     assert res < 1e-10, res
     # mixed precision: FP64 refinement around FP32 MG-PCG
     mg32, op32 = S.build_elasticity_mg(ctx, H, torch.float32, mu=mu, lam=lam, eig_max=mg.eigs)
-    inner = S.cg(ctx, op32, mg32, rtol=1e-4, max_it=40)
+    inner = S.cg(ctx, op32, mg32, rtol=1e-4, max_it=40, residual_norm=True, flexible=True)
     op64 = S.elasticity_op(ctx, H.spaces[0], H.adj, H.det, mu, lam, H.dirichlet[0], torch.float64)
     ir = S.iterative_refinement(ctx, op64, inner, max_it=30, rtol=1e-10)
     x2 = torch.zeros_like(bd)
@@ -200,3 +201,27 @@ def test_elasticity_mg_pcg_and_mixed(cuda):
     res2 = np.linalg.norm(b - apply(x2.cpu().numpy())) / np.linalg.norm(b)
     assert res2 < 1e-10, res2
     assert np.linalg.norm(x2.cpu().numpy() - x.cpu().numpy()) < 1e-8 * np.linalg.norm(x.cpu().numpy())
+
+
+def test_cg_options_true_residual_and_check_every(cuda):
+    """residual_norm stops on ||r||/||b||, check_every only changes how often the host looks."""
+    import torch
+
+    m = SSMesh(10, 9, 8, 1)
+    H = S.Hierarchy(m, dirichlet_faces=("x0", "y0"), device=cuda)
+    fff = H.fff.cpu().numpy().T.copy()
+    dn = H.dirichlet[0].cpu().numpy()
+    apply, d = _oracle_poisson(m, 1, fff, dn)
+    b = _rhs(m, 1, dn, seed=2)
+    ctx = S.context()
+    op = S.laplacian_op(ctx, H.spaces[0], H.fff, H.dirichlet[0], torch.float64)
+    jac = S.jacobi(ctx, torch.from_numpy(d).to(cuda), 1.0)
+    its = []
+    for every in (1, 7):
+        solver = S.cg(ctx, op, jac, rtol=1e-10, residual_norm=True, check_every=every)
+        x = torch.zeros(b.size, dtype=torch.float64, device=cuda)
+        assert S.solve(solver, torch.from_numpy(b).to(cuda), x) == 0
+        res = np.linalg.norm(b - apply(x.cpu().numpy())) / np.linalg.norm(b)
+        assert res < 1.5e-10, res
+        its.append(S.stats(solver)[0])
+    assert its[0] <= its[1] < its[0] + 7

@@ -1,0 +1,97 @@
+"""Symmetric CRS / BSR SpMV and the hex8 Laplacian CRS assembly against the oracle."""
+
+import ctypes
+
+import numpy as np
+import pytest
+
+import oracle as O
+from sfem_gb300 import capi
+from sfem_gb300.mesh import SSMesh, upper_crs_graph
+from sfem_gb300.operators import SSMeshDevice
+
+pytestmark = pytest.mark.gpu
+D = ctypes.c_double
+
+
+def _t(a, cuda):
+    import torch
+
+    return torch.from_numpy(np.ascontiguousarray(a)).to(cuda)
+
+
+def test_hex8_laplacian_crs_sym_assembly_and_spmv(cuda):
+    import torch
+
+    m = SSMesh(6, 5, 4, 1, perturb=0.2, seed=3)
+    el = m.hex8_elements()
+    n = m.n_nodes(1)
+    rowptr, colidx = upper_crs_graph(el, n)
+    fff = O.fff_fill(el, m.points)
+    d_ref, o_ref = O.hex8_laplacian_crs_sym(el, fff, rowptr, colidx, n)
+    if O.ref() is not None:  # the oracle assembly is pinned to the reference's
+        d_r, o_r = O.hex8_laplacian_crs_sym(el, fff, rowptr, colidx, n, use_ref=True, points=m.points)
+        assert np.abs(d_r - d_ref).max() <= 1e-6 * np.abs(d_r).max()  # reference uses unrounded geometry
+    sp = SSMeshDevice(m, 1, device=cuda)
+    fff_d = _t(fff.T, cuda)
+    rp, ci = _t(rowptr, cuda), _t(colidx, cuda)
+    diag = torch.zeros(n, dtype=torch.float64, device=cuda)
+    off = torch.zeros(colidx.size, dtype=torch.float64, device=cuda)
+    lib = capi.load()
+    capi.check(lib.sfem_gb300_hex8_laplacian_crs_sym(capi.i64(m.n_elements), sp.elements_ptrs.ptr,
+                                                     capi.i64(m.n_elements), capi.vp(fff_d), capi.vp(rp), capi.vp(ci),
+                                                     capi.FLOAT64, capi.vp(diag), capi.vp(off), None), "assembly")
+    assert np.abs(diag.cpu().numpy() - d_ref).max() <= 1e-13 * np.abs(d_ref).max()
+    assert np.abs(off.cpu().numpy() - o_ref).max() <= 1e-13 * np.abs(o_ref).max()
+    # SpMV == matrix-free apply
+    x = np.random.default_rng(0).standard_normal(n)
+    y_mf = O.hex8_laplacian_apply(el, fff, x)
+    y_or = O.crs_sym_spmv(rowptr, colidx, d_ref, o_ref, x)
+    assert np.abs(y_or - y_mf).max() <= 1e-12 * np.abs(y_mf).max()
+    y = torch.full((n,), 3.0, dtype=torch.float64, device=cuda)
+    capi.check(lib.sfem_gb300_crs_sym_spmv(capi.FLOAT64, capi.i64(n), capi.vp(rp), capi.vp(ci), capi.vp(diag),
+                                           capi.vp(off), D(0.5), capi.vp(_t(x, cuda)), capi.vp(y), None), "spmv")
+    assert np.abs(y.cpu().numpy() - (1.5 + y_or)).max() <= 1e-12 * np.abs(y_or).max()
+
+
+@pytest.mark.parametrize("bs,sym", [(3, 0), (3, 1), (2, 0)])
+def test_bsr_sym_spmv(cuda, bs, sym):
+    import torch
+
+    rng = np.random.default_rng(bs + 10 * sym)
+    nb = 500
+    # random upper block graph
+    rows, cols = [], []
+    for i in range(nb):
+        c = np.unique(rng.integers(i + 1, nb, size=5)) if i + 1 < nb else np.array([], int)
+        rows += [i] * len(c)
+        cols += list(c)
+    rowptr = np.zeros(nb + 1, dtype=np.int32)
+    np.add.at(rowptr, np.array(rows, dtype=np.int64) + 1, 1)
+    rowptr = np.cumsum(rowptr).astype(np.int32)
+    colidx = np.array(cols, dtype=np.int32)
+    ns = bs * (bs + 1) // 2
+    dsym = rng.standard_normal(nb * ns)
+    nnz = colidx.size
+    if sym:
+        off_s = rng.standard_normal(nnz * ns)
+        off_full = np.zeros((nnz, bs, bs))
+        k = 0
+        for a in range(bs):
+            for b in range(a, bs):
+                off_full[:, a, b] = off_s[k::ns]
+                off_full[:, b, a] = off_s[k::ns]
+                k += 1
+        off_in = off_s
+        off_full = off_full.reshape(-1)
+    else:
+        off_full = rng.standard_normal(nnz * bs * bs)
+        off_in = off_full
+    x = rng.standard_normal(nb * bs)
+    ref = O.bsr_sym_spmv(bs, rowptr, colidx, dsym, off_full, x)
+    y = torch.zeros(nb * bs, dtype=torch.float64, device=cuda)
+    capi.check(capi.load().sfem_gb300_bsr_sym_spmv(capi.FLOAT64, bs, capi.i64(nb), capi.vp(_t(rowptr, cuda)),
+                                                   capi.vp(_t(colidx, cuda)), capi.vp(_t(dsym, cuda)),
+                                                   capi.vp(_t(off_in, cuda)), sym, D(0.0), capi.vp(_t(x, cuda)),
+                                                   capi.vp(y), None), "bsr")
+    assert np.abs(y.cpu().numpy() - ref).max() <= 1e-12 * np.abs(ref).max()
