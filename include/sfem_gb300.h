@@ -228,6 +228,34 @@ int sfem_gb300_random_uniform(int real_type, ptrdiff_t n, unsigned long long see
 int sfem_gb300_convert(ptrdiff_t n, int src_type, const void *src, int dst_type, void *dst, void *stream);
 int sfem_gb300_axpy_f32_to_f64(ptrdiff_t n, double alpha, const float *x, double *y, void *stream);
 
+/* ------------------------------------------------------- learned smoother */
+/* No reference counterpart.  A patch is the 5x5x5 node grid of one level-4
+ * sshex8 macro element (lidx order).  Activations are BF16, channels-last
+ * [P][125][C]; weights BF16 [cout][cin][27] (3x3x3 offsets, x fastest); FP32
+ * arithmetic.  Channel pairs (cin, cout) in {1, 16} x {1, 16}. */
+
+/* out = act(conv3x3x3(in, W)) with zero padding; act = ReLU if relu != 0. */
+int sfem_gb300_patchconv_forward(ptrdiff_t P, int cin, int cout, const void *in, const void *W, int relu, void *out,
+                                 void *stream);
+/* gin = conv^T(gout, W), multiplied by ReLU'(in_act) when in_act is not NULL. */
+int sfem_gb300_patchconv_backward_data(ptrdiff_t P, int cin, int cout, const void *gout, const void *W,
+                                       const void *in_act, void *gin, void *stream);
+/* dW (FP32, cout*cin*27) += sum over patches and positions of gout (x) in. */
+int sfem_gb300_patchconv_backward_weights(ptrdiff_t P, int cin, int cout, const void *gout, const void *in, float *dW,
+                                          void *stream);
+/* Patches of (scale .* r) normalised by their RMS (patch_scale[p], 1 for an all-zero patch);
+ * elements = level-4 sshex8 connectivity, scale may be NULL. */
+int sfem_gb300_gather_patches(int real_type, ptrdiff_t P, sfem_gb300_idx_t **elements, const void *r,
+                              const void *scale, void *out_bf16, float *patch_scale, void *stream);
+/* x[g] += alpha * patch_scale[p] * in[p][v] / count[g] (corrections averaged over shared nodes). */
+int sfem_gb300_scatter_patches(int real_type, ptrdiff_t P, sfem_gb300_idx_t **elements, const void *in_bf16,
+                               const float *patch_scale, const uint16_t *count, double alpha, void *x, void *stream);
+/* gy = 2 (y - target) / n (BF16), *loss += mean squared error (FP32, may be NULL). */
+int sfem_gb300_mse_grad(ptrdiff_t n, const void *y, const void *target, void *gy, float *loss, void *stream);
+/* Adam step on FP32 master weights, mirrored into BF16 (t = 1-based step). */
+int sfem_gb300_adam_step(int n, float *w, const float *g, float *m, float *v, void *w_bf16, float lr, float beta1,
+                         float beta2, float eps, int t, void *stream);
+
 /* ------------------------------------------------- operators and solvers */
 /* Opaque handles (void *) over the device solver layer, mirroring the
  * reference's frontend factories (frontend/sfem_API.hpp: create_cg :143,
@@ -303,6 +331,28 @@ int sfem_gb300_cg_set_verbose(void *solver, int verbose);
 /* Multigrid V/W cycle (algebra/sfem_Multigrid.hpp:27-354); levels added finest first. */
 int sfem_gb300_mg_create(void *context, int real_type, int max_it, int cycle_type, void **solver);
 int sfem_gb300_mg_add_level(void *mg, void *op, void *smoother, void *prolongation, void *restriction);
+/* Learned smoother for level-4 sshex8 Laplacians: `sweeps` times
+ *   r = b - A x;  x += omega * scatter(net(gather(D^-1 r)))
+ * with the 3-layer patch network (W1: channels x 1 x 27, W2: channels x channels x 27,
+ * W3: 1 x channels x 27, BF16).  Usable as a multigrid smoother or, with a Chebyshev3
+ * handle as `fallback`, switched to the fallback by sfem_gb300_learned_smoother_use_fallback. */
+int sfem_gb300_learned_smoother_create(void *context, void *op, sfem_gb300_idx_t **elements, ptrdiff_t nelements,
+                                       const uint16_t *count, const void *inv_diag, const void *W1, const void *W2,
+                                       const void *W3, int channels, double omega, int sweeps, void *fallback,
+                                       void **solver);
+int sfem_gb300_learned_smoother_use_fallback(void *solver, int use_fallback);
+/* chain != 0: apply the fallback smoother first, then the learned corrections. */
+int sfem_gb300_learned_smoother_set_chain(void *solver, int chain);
+/* Let a CG (residual not decreasing for 2 checks) or an iterative refinement (FP64
+ * residual not halved by an outer step) switch the learned smoother to its fallback. */
+int sfem_gb300_solver_set_fallback(void *solver, void *learned_smoother);
+int sfem_gb300_solver_fallback_used(void *solver, int *used);
+/* Replace the (pre-)smoother of a level, or set a separate post-smoother (level 0 = finest). */
+int sfem_gb300_mg_set_pre_smoother(void *mg, int level, void *smoother);
+int sfem_gb300_mg_set_post_smoother(void *mg, int level, void *smoother);
+/* Copy of the finest-level iterate after each coarse-grid correction into x_cc (device, n entries). */
+int sfem_gb300_mg_set_harvest(void *mg, void *x_cc);
+
 /* FP64 iterative refinement around a float inner solver (no reference counterpart):
  * r = b - A x in double, d = inner(r/|r|) in float, x += |r| d, until |r| <= rtol |b|. */
 int sfem_gb300_ir_create(void *context, void *op64, void *inner32, int max_it, double rtol, void **solver);

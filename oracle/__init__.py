@@ -296,3 +296,28 @@ def hex8_laplacian_crs_sym(elements, fff_aos, rowptr, colidx, n, use_ref=False, 
         lib().or_hex8_laplacian_crs_sym(c_ptrdiff(E), ea.p, _ptr(_f32(fff_aos)), _ptr(rp), _ptr(ci), _ptr(diag),
                                         _ptr(off))
     return diag, off
+
+
+# ---------------------------------------------------------------------------
+# learned-smoother network (double-precision loop nests)
+# ---------------------------------------------------------------------------
+def patchconv_forward(P, cin, cout, x, W, relu):
+    out = np.zeros(P * 125 * cout)
+    lib().or_patchconv_forward(c_ptrdiff(P), c_int(cin), c_int(cout), _ptr(_f32(x)), _ptr(_f32(W)), c_int(relu),
+                               _ptr(out))
+    return out
+
+
+def patchconv_backward_data(P, cin, cout, gout, W, in_act=None):
+    out = np.zeros(P * 125 * cin)
+    act = _f32(in_act) if in_act is not None else None
+    lib().or_patchconv_backward_data(c_ptrdiff(P), c_int(cin), c_int(cout), _ptr(_f32(gout)), _ptr(_f32(W)),
+                                     _ptr(act) if act is not None else c_void_p(0), _ptr(out))
+    return out
+
+
+def patchconv_backward_weights(P, cin, cout, gout, x):
+    dW = np.zeros(cout * cin * 27)
+    lib().or_patchconv_backward_weights(c_ptrdiff(P), c_int(cin), c_int(cout), _ptr(_f32(gout)), _ptr(_f32(x)),
+                                        _ptr(dW))
+    return dW

@@ -587,3 +587,67 @@ int or_hex8_laplacian_crs_sym(ptrdiff_t nelements, idx_t **elements, const jacob
     }
     return 0;
 }
+
+/* ------------------------------------------------------------------------ */
+/* Learned smoother network (no reference counterpart): 3x3x3 convolutions  */
+/* on 5x5x5 patches, zero padding, channels-last activations [p][v][c],      */
+/* weights [co][ci][27] with offset o = (dz+1)*9 + (dy+1)*3 + (dx+1).        */
+/* Plain loop nests in double for gradient checks of the GPU kernels.        */
+/* ------------------------------------------------------------------------ */
+
+static int pc_neighbor(int v, int o) {
+    const int x = v % 5, y = (v / 5) % 5, z = v / 25;
+    const int X = x + o % 3 - 1, Y = y + (o / 3) % 3 - 1, Z = z + o / 9 - 1;
+    if (X < 0 || X > 4 || Y < 0 || Y > 4 || Z < 0 || Z > 4) return -1;
+    return Z * 25 + Y * 5 + X;
+}
+
+void or_patchconv_forward(ptrdiff_t P, int cin, int cout, const float *in, const float *W, int relu, double *out) {
+#pragma omp parallel for
+    for (ptrdiff_t p = 0; p < P; p++)
+        for (int v = 0; v < 125; v++)
+            for (int co = 0; co < cout; co++) {
+                double acc = 0;
+                for (int o = 0; o < 27; o++) {
+                    const int u = pc_neighbor(v, o);
+                    if (u < 0) continue;
+                    for (int ci = 0; ci < cin; ci++)
+                        acc += (double)W[(co * cin + ci) * 27 + o] * in[(p * 125 + u) * cin + ci];
+                }
+                out[(p * 125 + v) * cout + co] = relu && acc < 0 ? 0 : acc;
+            }
+}
+
+void or_patchconv_backward_data(ptrdiff_t P, int cin, int cout, const float *gout, const float *W, const float *in_act,
+                                double *gin) {
+#pragma omp parallel for
+    for (ptrdiff_t p = 0; p < P; p++)
+        for (int u = 0; u < 125; u++)
+            for (int ci = 0; ci < cin; ci++) {
+                double acc = 0;
+                for (int o = 0; o < 27; o++) {
+                    /* u = v + o  <=>  v = u - o: the neighbour of u at the mirrored offset */
+                    const int v = pc_neighbor(u, 26 - o);
+                    if (v < 0) continue;
+                    for (int co = 0; co < cout; co++) acc += (double)W[(co * cin + ci) * 27 + o] * gout[(p * 125 + v) * cout + co];
+                }
+                if (in_act && in_act[(p * 125 + u) * cin + ci] <= 0) acc = 0;
+                gin[(p * 125 + u) * cin + ci] = acc;
+            }
+}
+
+void or_patchconv_backward_weights(ptrdiff_t P, int cin, int cout, const float *gout, const float *in, double *dW) {
+    for (int co = 0; co < cout; co++)
+        for (int ci = 0; ci < cin; ci++)
+            for (int o = 0; o < 27; o++) {
+                double acc = 0;
+#pragma omp parallel for reduction(+ : acc)
+                for (ptrdiff_t p = 0; p < P; p++)
+                    for (int v = 0; v < 125; v++) {
+                        const int u = pc_neighbor(v, o);
+                        if (u < 0) continue;
+                        acc += (double)gout[(p * 125 + v) * cout + co] * in[(p * 125 + u) * cin + ci];
+                    }
+                dW[(co * cin + ci) * 27 + o] += acc;
+            }
+}

@@ -9,6 +9,10 @@
 // micro element.  K[(i,a),(j,b)] = 1/det sum_pq I_ab^pq (mu adj_pj adj_qi +
 // lambda adj_pi adj_qj + delta_ij mu (adj adj^T)_pq), I_ab^pq the exact Q1
 // integrals of d_p phi_a d_q phi_b on the unit cube.
+#include <cuda_bf16.h>
+
+#include <cstdlib>
+
 #include "common.cuh"
 
 namespace sfem_gb300 {
@@ -60,6 +64,40 @@ __device__ __forceinline__ void load_sub_adjugate(const float *adjugate, const f
         for (int q = 0; q < 3; q++) AA[3 * p + q] = adj[3 * p] * adj[3 * q] + adj[3 * p + 1] * adj[3 * q + 1] + adj[3 * p + 2] * adj[3 * q + 2];
 }
 
+// Cooperative K build by one warp: W[i][j][p][q] = mu adj_pj adj_qi + lambda adj_pi adj_qj
+// + delta_ij mu (adj adj^T)_pq (81 values) then K[(i,a),(j,b)] = inv_det sum_pq I_ab^pq W_ij^pq.
+// I (the unit-cube Q1 gradient integrals) comes from a per-block shared copy: lanes read
+// different entries, which constant memory would serialise.
+template <typename T>
+__device__ __forceinline__ void build_K_warp(const T adj[9], const T AA[9], T inv_det, T mu, T lambda,
+                                             const T *__restrict__ Is, T *__restrict__ Wsm, T *__restrict__ K,
+                                             int ld, int lane) {
+    for (int k = lane; k < 81; k += 32) {
+        const int i = k / 27, j = (k / 9) % 3, p = (k / 3) % 3, q = k % 3;
+        T w = mu * adj[3 * p + j] * adj[3 * q + i] + lambda * adj[3 * p + i] * adj[3 * q + j];
+        if (i == j) w += mu * AA[3 * p + q];
+        Wsm[k] = w;
+    }
+    __syncwarp();
+    for (int k = lane; k < 576; k += 32) {
+        const int row = k / 24, col = k % 24;
+        const int i = row >> 3, a = row & 7, j = col >> 3, b = col & 7;
+        const T *Iab = &Is[(a * 8 + b) * 9];
+        const T *Wij = &Wsm[(i * 3 + j) * 9];
+        T acc = 0;
+#pragma unroll
+        for (int pq = 0; pq < 9; pq++) acc += Iab[pq] * Wij[pq];
+        K[row * ld + col] = acc * inv_det;
+    }
+    __syncwarp();
+}
+
+template <typename T>
+__device__ __forceinline__ void load_grad_table(T *Is) {
+    for (int k = threadIdx.x; k < 576; k += blockDim.x) Is[k] = (T)(&kGrad.I[0][0][0][0])[k];
+    __syncthreads();
+}
+
 // v1: one warp per macro element.  The warp builds K (576 entries) in shared
 // memory, stages the (L+1)^3 x 3 micro-grid values, lanes apply K per micro
 // element with shared-memory accumulation, then scatter (owned interior nodes
@@ -77,14 +115,17 @@ __global__ void __launch_bounds__(64) elasticity_apply_warp_kernel(ptrdiff_t nel
     __shared__ T Ks[WPB][576];
     __shared__ T xs[WPB][3 * NXE];
     __shared__ T ys[WPB][3 * NXE];
+    __shared__ T Is[576];
+    __shared__ T Ws[WPB][81];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     T *K = Ks[warp];
     T *xw = xs[warp];
     T *yw = ys[warp];
+    load_grad_table<T>(Is);
     for (ptrdiff_t e = (ptrdiff_t)blockIdx.x * WPB + warp; e < nelements; e += (ptrdiff_t)gridDim.x * WPB) {
         T adj[9], AA[9], inv_det;
         load_sub_adjugate<T>(adjugate, determinant, stride, e, L, adj, AA, inv_det);
-        for (int k = lane; k < 576; k += 32) K[k] = elasticity_entry<T>(k, adj, AA, inv_det, mu, lambda);
+        build_K_warp<T>(adj, AA, inv_det, mu, lambda, Is, Ws[warp], K, 24, lane);
         idx_t gi[NR];
 #pragma unroll
         for (int r = 0; r < NR; r++) {
@@ -139,6 +180,137 @@ __global__ void __launch_bounds__(64) elasticity_apply_warp_kernel(ptrdiff_t nel
     }
 }
 
+
+// Tensor-core variant (FP32 vectors, BF16 element contraction, FP32 accumulate):
+// per macro element Y(24 x L^3) = K(24 x 24) U(24 x L^3), U[:, m] the 24 dofs of micro
+// element m, with warp-level mma.sync.m16n8k16 (K padded to 32 x 32 in BF16).  One warp
+// per macro element; the micro-grid values are staged in shared memory, outputs are
+// accumulated with shared-memory atomics and scattered like the SIMT kernel.
+__device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
+    const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<const uint32_t *>(&v);
+}
+
+__device__ __forceinline__ void mma_bf16_16816(float d[4], const uint32_t a[4], const uint32_t b[2]) {
+    asm volatile(
+            "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+            "{%0,%1,%2,%3};\n"
+            : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+            : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+template <int L, bool HEX8>
+__global__ void __launch_bounds__(128) elasticity_apply_tc_kernel(ptrdiff_t nelements, const idx_t *const *elements,
+                                                                  ptrdiff_t stride, const float *adjugate,
+                                                                  const float *determinant, float mu, float lambda,
+                                                                  const float *__restrict__ x, float *__restrict__ y) {
+    constexpr int N1 = L + 1;
+    constexpr int NXE = N1 * N1 * N1;
+    constexpr int NM = L * L * L;
+    constexpr int NT = (NM + 7) / 8;  // n-tiles of 8 micro elements
+    constexpr int WPB = 4;
+    constexpr int NR = (NXE + 31) / 32;
+    __shared__ float Ks[WPB][32 * 32];
+    __shared__ float xs[WPB][3 * NXE];
+    __shared__ float ys[WPB][3 * NXE];
+    __shared__ float Is[576];
+    __shared__ float Ws[WPB][81];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int gid = lane >> 2, tig = lane & 3;
+    float *K = Ks[warp];
+    float *xw = xs[warp];
+    float *yw = ys[warp];
+    load_grad_table<float>(Is);
+    for (int k = lane; k < 1024; k += 32) K[k] = 0.f;  // zero padding rows/cols 24..31
+    __syncwarp();
+    for (ptrdiff_t e = (ptrdiff_t)blockIdx.x * WPB + warp; e < nelements; e += (ptrdiff_t)gridDim.x * WPB) {
+        float adj[9], AA[9], inv_det;
+        load_sub_adjugate<float>(adjugate, determinant, stride, e, L, adj, AA, inv_det);
+        build_K_warp<float>(adj, AA, inv_det, mu, lambda, Is, Ws[warp], K, 32, lane);
+        idx_t gi[NR];
+#pragma unroll
+        for (int r = 0; r < NR; r++) {
+            const int l = lane + 32 * r;
+            if (l < NXE) {
+                gi[r] = elements[HEX8 ? hex8_corner_of_lidx1(l) : l][e];
+#pragma unroll
+                for (int d = 0; d < 3; d++) {
+                    xw[d * NXE + l] = x[3 * (ptrdiff_t)gi[r] + d];
+                    yw[d * NXE + l] = 0.f;
+                }
+            }
+        }
+        __syncwarp();
+        // A fragments of K: a[mt][kt]
+        uint32_t a[2][2][4];
+#pragma unroll
+        for (int mt = 0; mt < 2; mt++)
+#pragma unroll
+            for (int kt = 0; kt < 2; kt++) {
+                const int r0 = mt * 16 + gid, c0 = kt * 16 + tig * 2;
+                a[mt][kt][0] = pack_bf16x2(K[r0 * 32 + c0], K[r0 * 32 + c0 + 1]);
+                a[mt][kt][1] = pack_bf16x2(K[(r0 + 8) * 32 + c0], K[(r0 + 8) * 32 + c0 + 1]);
+                a[mt][kt][2] = pack_bf16x2(K[r0 * 32 + c0 + 8], K[r0 * 32 + c0 + 9]);
+                a[mt][kt][3] = pack_bf16x2(K[(r0 + 8) * 32 + c0 + 8], K[(r0 + 8) * 32 + c0 + 9]);
+            }
+#pragma unroll 1
+        for (int nt = 0; nt < NT; nt++) {
+            // B fragment: U[k][m], m = nt*8 + gid (this thread's column)
+            const int m = nt * 8 + gid;
+            const bool mvalid = m < NM;
+            const int xi = m % L, yi = (m / L) % L, zi = m / (L * L);
+            auto U = [&](int k) -> float {
+                if (!mvalid || k >= 24) return 0.f;
+                const int comp = k >> 3, c = k & 7;
+                return xw[comp * NXE + lidx(L, xi + c8x(c), yi + c8y(c), zi + c8z(c))];
+            };
+            uint32_t b[2][2];
+#pragma unroll
+            for (int kt = 0; kt < 2; kt++) {
+                const int k0 = kt * 16 + tig * 2;
+                b[kt][0] = pack_bf16x2(U(k0), U(k0 + 1));
+                b[kt][1] = pack_bf16x2(U(k0 + 8), U(k0 + 9));
+            }
+#pragma unroll
+            for (int mt = 0; mt < 2; mt++) {
+                float d[4] = {0.f, 0.f, 0.f, 0.f};
+                mma_bf16_16816(d, a[mt][0], b[0]);
+                mma_bf16_16816(d, a[mt][1], b[1]);
+                // d[0..1]: row mt*16+gid, cols tig*2+{0,1};  d[2..3]: row +8
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    const int row = mt * 16 + gid + (q >= 2 ? 8 : 0);
+                    const int col = nt * 8 + tig * 2 + (q & 1);
+                    if (row < 24 && col < NM) {
+                        const int cx = col % L, cy = (col / L) % L, cz = col / (L * L);
+                        const int comp = row >> 3, c = row & 7;
+                        atomicAdd(&yw[comp * NXE + lidx(L, cx + c8x(c), cy + c8y(c), cz + c8z(c))], d[q]);
+                    }
+                }
+            }
+        }
+        __syncwarp();
+#pragma unroll
+        for (int r = 0; r < NR; r++) {
+            const int l = lane + 32 * r;
+            if (l < NXE) {
+                const int px = l % N1, py = (l / N1) % N1, pz = l / (N1 * N1);
+                const bool interior = px > 0 && px < L && py > 0 && py < L && pz > 0 && pz < L;
+#pragma unroll
+                for (int d = 0; d < 3; d++) {
+                    const float val = yw[d * NXE + l];
+                    float *dst = &y[3 * (ptrdiff_t)gi[r] + d];
+                    if (interior)
+                        *dst += val;
+                    else
+                        atomicAdd(dst, val);
+                }
+            }
+        }
+        __syncwarp();
+    }
+}
+
 // Diagonal (diag3: 3 per node) and symmetric 3x3 block diagonal (block6: 00,01,02,11,12,22 per node).
 template <typename T, int L, bool HEX8>
 __global__ void __launch_bounds__(64) elasticity_block_diag_kernel(ptrdiff_t nelements, const idx_t *const *elements,
@@ -149,14 +321,19 @@ __global__ void __launch_bounds__(64) elasticity_block_diag_kernel(ptrdiff_t nel
     constexpr int NXE = N1 * N1 * N1;
     constexpr int WPB = 2;
     __shared__ T Bs[WPB][8][6];
+    __shared__ T Ks[WPB][576];
+    __shared__ T Is[576];
+    __shared__ T Ws[WPB][81];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int bi[6] = {0, 0, 0, 1, 1, 2}, bj[6] = {0, 1, 2, 1, 2, 2};
+    load_grad_table<T>(Is);
     for (ptrdiff_t e = (ptrdiff_t)blockIdx.x * WPB + warp; e < nelements; e += (ptrdiff_t)gridDim.x * WPB) {
         T adj[9], AA[9], inv_det;
         load_sub_adjugate<T>(adjugate, determinant, stride, e, L, adj, AA, inv_det);
+        build_K_warp<T>(adj, AA, inv_det, mu, lambda, Is, Ws[warp], Ks[warp], 24, lane);
         for (int k = lane; k < 48; k += 32) {
             const int a = k / 6, c = k % 6;
-            Bs[warp][a][c] = elasticity_entry<T>((bi[c] * 8 + a) * 24 + bj[c] * 8 + a, adj, AA, inv_det, mu, lambda);
+            Bs[warp][a][c] = Ks[warp][(bi[c] * 8 + a) * 24 + bj[c] * 8 + a];
         }
         __syncwarp();
         for (int l = lane; l < NXE; l += 32) {
@@ -240,10 +417,51 @@ __global__ void block_apply_kernel(ptrdiff_t n_nodes, const T *__restrict__ bloc
     }
 }
 
+// FP32 vectors use the tensor-core kernel (BF16 contraction) unless
+// SFEM_GB300_ELASTICITY_KERNEL=simt selects the FP32 SIMT kernel.
+static bool elasticity_use_tc() {
+    static int v = -1;
+    if (v < 0) {
+        const char *e = getenv("SFEM_GB300_ELASTICITY_KERNEL");
+        v = (e && e[0] == 's') ? 0 : 1;
+    }
+    return v == 1;
+}
+
+static int elasticity_apply_tc(int element_type, ptrdiff_t nelements, idx_t **elements, ptrdiff_t stride,
+                               const float *adj, const float *det, float mu, float lambda, const float *x, float *y,
+                               cudaStream_t s) {
+    const int blocks = grid_for((nelements + 3) / 4, 1, kNumSMs * 64);
+    if (element_type == SFEM_GB300_HEX8) {
+        elasticity_apply_tc_kernel<1, true><<<blocks, 128, 0, s>>>(nelements, elements, stride, adj, det, mu, lambda, x, y);
+        return check_launch("sfem_gb300_linear_elasticity_apply(HEX8, tensor cores)");
+    }
+    switch (element_type - SFEM_GB300_SSHEX8_BASE) {
+        case 1:
+            elasticity_apply_tc_kernel<1, false><<<blocks, 128, 0, s>>>(nelements, elements, stride, adj, det, mu, lambda, x, y);
+            break;
+        case 2:
+            elasticity_apply_tc_kernel<2, false><<<blocks, 128, 0, s>>>(nelements, elements, stride, adj, det, mu, lambda, x, y);
+            break;
+        case 3:
+            elasticity_apply_tc_kernel<3, false><<<blocks, 128, 0, s>>>(nelements, elements, stride, adj, det, mu, lambda, x, y);
+            break;
+        case 4:
+            elasticity_apply_tc_kernel<4, false><<<blocks, 128, 0, s>>>(nelements, elements, stride, adj, det, mu, lambda, x, y);
+            break;
+        default:
+            return set_error("sfem_gb300_linear_elasticity_apply: unsupported element type %d", element_type);
+    }
+    return check_launch("sfem_gb300_linear_elasticity_apply(SSHEX8, tensor cores)");
+}
+
 template <typename T>
 static int elasticity_apply_tpl(int element_type, ptrdiff_t nelements, idx_t **elements, ptrdiff_t stride,
                                 const float *adj, const float *det, T mu, T lambda, const T *x, T *y, cudaStream_t s) {
     if (nelements <= 0) return SFEM_GB300_SUCCESS;
+    if (sizeof(T) == 4 && elasticity_use_tc())
+        return elasticity_apply_tc(element_type, nelements, elements, stride, adj, det, (float)mu, (float)lambda,
+                                   (const float *)x, (float *)y, s);
     const int blocks = grid_for((nelements + 1) / 2, 1, kNumSMs * 64);
     if (element_type == SFEM_GB300_HEX8) {
         elasticity_apply_warp_kernel<T, 1, true><<<blocks, 64, 0, s>>>(nelements, elements, stride, adj, det, mu,

@@ -146,11 +146,14 @@ __global__ void __launch_bounds__(128) sshex8_laplacian_apply_warp_kernel(ptrdif
     __shared__ T xs[WPB][NXE];
     __shared__ T ys[WPB][NXE];
     __shared__ T As[WPB][64];
+    __shared__ T Wt[64 * 6];  // element-matrix weights: lanes read different rows
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     T *xw = xs[warp];
     T *yw = ys[warp];
     T *Aw = As[warp];
     const T h = T(1) / T(L);
+    for (int k = threadIdx.x; k < 64 * 6; k += blockDim.x) Wt[k] = lap_w<T>(k / 6, k % 6);
+    __syncthreads();
 
     for (ptrdiff_t e = (ptrdiff_t)blockIdx.x * WPB + warp; e < nelements; e += (ptrdiff_t)gridDim.x * WPB) {
         T f = 0;
@@ -162,7 +165,7 @@ __global__ void __launch_bounds__(128) sshex8_laplacian_apply_warp_kernel(ptrdif
         for (int k = lane; k < 64; k += 32) {
             T a = 0;
 #pragma unroll
-            for (int m = 0; m < 6; m++) a += sub[m] * lap_w<T>(k, m);
+            for (int m = 0; m < 6; m++) a += sub[m] * Wt[k * 6 + m];
             Aw[k] = a;
         }
 

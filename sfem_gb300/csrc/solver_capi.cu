@@ -6,6 +6,7 @@
 // create_hierarchical_restriction :575) and as drivers/mgsolve.cpp:128-330 uses them.
 #include <cstdarg>
 #include <cstring>
+#include <functional>
 #include <memory>
 #include <string>
 
@@ -171,6 +172,8 @@ public:
     double rtol{1e-10}, atol{0};
     double last_rel{0};
     double *s{nullptr};
+    std::function<void()> on_stagnation;  // FP64 residual failed to decrease by half
+    bool stagnated{false};
     int apply(const double *b, double *x) override {
         const ptrdiff_t n = op->rows();
         if (!s) s = ctx->slots(2);
@@ -180,6 +183,9 @@ public:
         Blas<double> bd = blas_of<double>(ctx);
         bd.norm2(n, b, &s[1]);
         const double bnorm = ctx->read(&s[1]);
+        double prev = -1;
+        int flat = 0;
+        stagnated = false;
         for (this->iterations_ = 0;; this->iterations_++) {
             bd.zeros(n, r.ptr);
             SFEM_GB300_CHECK(op->apply(x, r.ptr));
@@ -187,6 +193,19 @@ public:
             bd.norm2(n, r.ptr, &s[0]);
             const double rnorm = ctx->read(&s[0]);
             last_rel = bnorm > 0 ? rnorm / bnorm : rnorm;
+            if (prev >= 0 && rnorm > 0.5 * prev && on_stagnation && !stagnated) {
+                stagnated = true;
+                on_stagnation();
+            }
+            // FP64 attainable accuracy reached: two outer steps without a 10 % reduction
+            if (prev >= 0 && rnorm > 0.9 * prev) {
+                if (++flat >= 2)
+                    return set_error("IterativeRefinement: residual stagnated at %g (rtol %g not attainable)", last_rel,
+                                     rtol);
+            } else {
+                flat = 0;
+            }
+            prev = rnorm;
             if (rnorm <= rtol * bnorm || rnorm <= atol || rnorm == 0) return 0;
             if (!std::isfinite(rnorm)) return set_error("IterativeRefinement: non-finite residual");
             if (this->iterations_ >= max_it) return set_error("IterativeRefinement: no convergence (rel %g)", last_rel);
@@ -619,6 +638,149 @@ int sfem_gb300_mg_add_level(void *mg, void *op, void *smoother, void *prolongati
         auto m = std::static_pointer_cast<Multigrid<double>>(h->impl);
         m->add_level(o->d, s->d, p ? p->d : nullptr, r ? r->d : nullptr);
     }
+    return SFEM_GB300_SUCCESS;
+}
+
+int sfem_gb300_learned_smoother_create(void *context, void *op, idx_t **elements, ptrdiff_t nelements,
+                                       const uint16_t *count, const void *inv_diag, const void *W1, const void *W2,
+                                       const void *W3, int channels, double omega, int sweeps, void *fallback,
+                                       void **out) {
+    auto *c = H(context);
+    auto *o = H(op);
+    auto *fb = fallback ? H(fallback) : nullptr;
+    if (channels != 16) return set_error("sfem_gb300_learned_smoother_create: channels must be 16");
+    auto *h = new Handle();
+    h->kind = "learned";
+    h->ctx = c->ctx;
+    h->real_type = o->real_type;
+    auto fill = [&](auto s, auto tag) {
+        using T = decltype(tag);
+        s->blas = blas_of<T>(c->ctx);
+        s->elements = elements;
+        s->nelements = nelements;
+        s->count = count;
+        s->inv_diag = (const T *)inv_diag;
+        s->W[0] = W1;
+        s->W[1] = W2;
+        s->W[2] = W3;
+        s->channels = channels;
+        s->omega = omega;
+        s->sweeps = sweeps;
+    };
+    if (o->f) {
+        auto s = std::make_shared<LearnedSmoother<float>>();
+        fill(s, 0.0f);
+        s->op = o->f;
+        if (fb) s->fallback = fb->f;
+        h->f = s;
+        h->impl = s;
+    } else {
+        auto s = std::make_shared<LearnedSmoother<double>>();
+        fill(s, 0.0);
+        s->op = o->d;
+        if (fb) s->fallback = fb->d;
+        h->d = s;
+        h->impl = s;
+    }
+    *out = h;
+    return SFEM_GB300_SUCCESS;
+}
+
+int sfem_gb300_solver_set_fallback(void *solver, void *learned) {
+    auto *h = H(solver);
+    auto *l = H(learned);
+    if (l->kind != "learned") return set_error("sfem_gb300_solver_set_fallback: not a learned-smoother handle");
+    std::function<void()> fn;
+    if (l->f) {
+        auto ls = std::static_pointer_cast<LearnedSmoother<float>>(l->impl);
+        fn = [ls]() { ls->use_fallback = true; };
+    } else {
+        auto ls = std::static_pointer_cast<LearnedSmoother<double>>(l->impl);
+        fn = [ls]() { ls->use_fallback = true; };
+    }
+    if (h->kind == "cg") {
+        if (h->f)
+            std::static_pointer_cast<ConjugateGradient<float>>(h->impl)->on_stagnation = fn;
+        else
+            std::static_pointer_cast<ConjugateGradient<double>>(h->impl)->on_stagnation = fn;
+    } else if (h->kind == "ir") {
+        std::static_pointer_cast<IterativeRefinement>(h->impl)->on_stagnation = fn;
+    } else {
+        return set_error("sfem_gb300_solver_set_fallback: handle of kind '%s' has no residual monitor", h->kind.c_str());
+    }
+    return SFEM_GB300_SUCCESS;
+}
+
+int sfem_gb300_solver_fallback_used(void *solver, int *used) {
+    auto *h = H(solver);
+    *used = 0;
+    if (h->kind == "cg")
+        *used = h->f ? std::static_pointer_cast<ConjugateGradient<float>>(h->impl)->stagnated
+                     : std::static_pointer_cast<ConjugateGradient<double>>(h->impl)->stagnated;
+    else if (h->kind == "ir")
+        *used = std::static_pointer_cast<IterativeRefinement>(h->impl)->stagnated;
+    return SFEM_GB300_SUCCESS;
+}
+
+int sfem_gb300_learned_smoother_set_chain(void *solver, int chain) {
+    auto *h = H(solver);
+    if (h->kind != "learned") return set_error("not a learned-smoother handle");
+    if (h->f)
+        std::static_pointer_cast<LearnedSmoother<float>>(h->impl)->chain = chain != 0;
+    else
+        std::static_pointer_cast<LearnedSmoother<double>>(h->impl)->chain = chain != 0;
+    return SFEM_GB300_SUCCESS;
+}
+
+int sfem_gb300_learned_smoother_use_fallback(void *solver, int use_fallback) {
+    auto *h = H(solver);
+    if (h->kind != "learned") return set_error("not a learned-smoother handle");
+    if (h->f)
+        std::static_pointer_cast<LearnedSmoother<float>>(h->impl)->use_fallback = use_fallback != 0;
+    else
+        std::static_pointer_cast<LearnedSmoother<double>>(h->impl)->use_fallback = use_fallback != 0;
+    return SFEM_GB300_SUCCESS;
+}
+
+int sfem_gb300_mg_set_post_smoother(void *mg, int level, void *smoother) {
+    auto *h = H(mg);
+    if (h->kind != "mg") return set_error("not a multigrid handle");
+    auto *s = H(smoother);
+    if (h->f) {
+        auto m = std::static_pointer_cast<Multigrid<float>>(h->impl);
+        if (level < 0 || level >= (int)m->levels.size()) return set_error("mg_set_post_smoother: bad level");
+        m->levels[level].post_smoother = s->f;
+    } else {
+        auto m = std::static_pointer_cast<Multigrid<double>>(h->impl);
+        if (level < 0 || level >= (int)m->levels.size()) return set_error("mg_set_post_smoother: bad level");
+        m->levels[level].post_smoother = s->d;
+    }
+    return SFEM_GB300_SUCCESS;
+}
+
+int sfem_gb300_mg_set_pre_smoother(void *mg, int level, void *smoother) {
+    auto *h = H(mg);
+    if (h->kind != "mg") return set_error("not a multigrid handle");
+    auto *s = H(smoother);
+    if (h->f) {
+        auto m = std::static_pointer_cast<Multigrid<float>>(h->impl);
+        if (level < 0 || level >= (int)m->levels.size()) return set_error("mg_set_pre_smoother: bad level");
+        m->levels[level].smoother = s->f;
+    } else {
+        auto m = std::static_pointer_cast<Multigrid<double>>(h->impl);
+        if (level < 0 || level >= (int)m->levels.size()) return set_error("mg_set_pre_smoother: bad level");
+        m->levels[level].smoother = s->d;
+    }
+    return SFEM_GB300_SUCCESS;
+}
+
+int sfem_gb300_mg_set_harvest(void *mg, void *x_cc) {
+    auto *h = H(mg);
+    if (h->kind != "mg") return set_error("not a multigrid handle");
+    if (h->f)
+        std::static_pointer_cast<Multigrid<float>>(h->impl)->harvest = (float *)x_cc;
+    else
+        std::static_pointer_cast<Multigrid<double>>(h->impl)->harvest = (double *)x_cc;
     return SFEM_GB300_SUCCESS;
 }
 

@@ -345,6 +345,54 @@ public:
     ptrdiff_t cols() const override { return 3 * n_nodes; }
 };
 
+// Learned patch smoother (no reference counterpart), see sfem_gb300_learned_smoother_create.
+template <typename T>
+class LearnedSmoother final : public Solver<T> {
+public:
+    Blas<T> blas;
+    std::shared_ptr<Operator<T>> op, fallback;
+    idx_t **elements{nullptr};
+    ptrdiff_t nelements{0};
+    const uint16_t *count{nullptr};
+    const T *inv_diag{nullptr};
+    const void *W[3]{nullptr, nullptr, nullptr};
+    int channels{16}, sweeps{1};
+    double omega{1.0};
+    bool use_fallback{false};
+    bool chain{false};  // apply the fallback first, then the learned corrections
+    DeviceBuffer<T> r;
+    DeviceBuffer<uint16_t> a0, a1, a2, a3;  // BF16 activations
+    DeviceBuffer<float> pscale;
+    int apply(const T *b, T *x) override {
+        if (fallback && (chain || use_fallback)) SFEM_GB300_CHECK(fallback->apply(b, x));
+        if (use_fallback) return 0;
+        const ptrdiff_t n = op->rows();
+        const ptrdiff_t P = nelements;
+        SFEM_GB300_CHECK(r.resize(n));
+        SFEM_GB300_CHECK(a0.resize(P * 125));
+        SFEM_GB300_CHECK(a1.resize(P * 125 * channels));
+        SFEM_GB300_CHECK(a2.resize(P * 125 * channels));
+        SFEM_GB300_CHECK(a3.resize(P * 125));
+        SFEM_GB300_CHECK(pscale.resize(P));
+        void *sp = blas.ctx->sp();
+        for (this->iterations_ = 0; this->iterations_ < sweeps; this->iterations_++) {
+            blas.zeros(n, r.ptr);
+            SFEM_GB300_CHECK(op->apply(x, r.ptr));
+            blas.axpby(n, T(1), b, T(-1), r.ptr);
+            SFEM_GB300_CHECK(sfem_gb300_gather_patches(real_type_v<T>, P, elements, r.ptr, inv_diag, a0.ptr,
+                                                       pscale.ptr, sp));
+            SFEM_GB300_CHECK(sfem_gb300_patchconv_forward(P, 1, channels, a0.ptr, W[0], 1, a1.ptr, sp));
+            SFEM_GB300_CHECK(sfem_gb300_patchconv_forward(P, channels, channels, a1.ptr, W[1], 1, a2.ptr, sp));
+            SFEM_GB300_CHECK(sfem_gb300_patchconv_forward(P, channels, 1, a2.ptr, W[2], 0, a3.ptr, sp));
+            SFEM_GB300_CHECK(sfem_gb300_scatter_patches(real_type_v<T>, P, elements, a3.ptr, pscale.ptr, count, omega,
+                                                        x, sp));
+        }
+        return 0;
+    }
+    ptrdiff_t rows() const override { return op->rows(); }
+    ptrdiff_t cols() const override { return op->cols(); }
+};
+
 // StationaryIteration (algebra/sfem_Stationary.hpp:19-133): x += P (b - A x), max_it sweeps.
 template <typename T>
 class Stationary final : public Solver<T> {
@@ -385,6 +433,11 @@ public:
     bool residual_norm{false}, flexible{false};
     int check_every{1};
     double last_rel{0};
+    // called once when the monitored residual has not decreased for `patience`
+    // consecutive checks (e.g. to switch a learned smoother to its fallback)
+    std::function<void()> on_stagnation;
+    int patience{2};
+    bool stagnated{false};
     // slots: 0 rz, 1 rz_old, 2 pAp, 3 rr, 4 r.z_prev, 5 rr0
     double *s{nullptr};
 
@@ -419,6 +472,9 @@ public:
         if (rz0 == 0 || crit0 == 0) return 0;
         const double norm0 = std::sqrt(std::fabs(crit0));
         const int every = check_every < 1 ? 1 : check_every;
+        double best = 1.0;
+        int bad = 0;
+        stagnated = false;
         for (this->iterations_ = 0; this->iterations_ < max_it;) {
             if (!op->overwrites_output()) blas.zeros(n, Ap.ptr);
             op->apply(p.ptr, Ap.ptr);
@@ -446,6 +502,13 @@ public:
                 if (verbose) printf("cg %d: %g %g\n", this->iterations_, anorm, last_rel);
                 if (!std::isfinite(crit)) return set_error("ConjugateGradient: non-finite residual");
                 if (anorm < atol || last_rel < rtol || crit == 0) return 0;
+                if (last_rel < best) {
+                    best = last_rel;
+                    bad = 0;
+                } else if (on_stagnation && !stagnated && ++bad >= patience) {
+                    stagnated = true;
+                    on_stagnation();
+                }
             }
             SFEM_GB300_CHECK(sfem_gb300_cg_update_p(real_type_v<T>, n, &s[0], &s[1], flex ? &s[4] : nullptr, zz,
                                                     p.ptr, blas.ctx->sp()));
@@ -462,6 +525,7 @@ class Multigrid final : public Solver<T> {
 public:
     struct Level {
         std::shared_ptr<Operator<T>> op, smoother, prolongation /* from next coarser */, restriction /* to coarser */;
+        std::shared_ptr<Operator<T>> post_smoother;  // optional, defaults to smoother
         DeviceBuffer<T> rhs, sol, work;
     };
     Blas<T> blas;
@@ -472,6 +536,9 @@ public:
     double *s{nullptr};
     bool wrap_input{true};
     double norm_residual0{0}, norm_residual{0};
+    // optional copy of the finest-level iterate after the coarse-grid correction
+    // (before post-smoothing): the residual / error pairs a learned smoother trains on
+    T *harvest{nullptr};
 
     void add_level(std::shared_ptr<Operator<T>> op, std::shared_ptr<Operator<T>> smoother,
                    std::shared_ptr<Operator<T>> prolongation, std::shared_ptr<Operator<T>> restriction) {
@@ -523,7 +590,8 @@ public:
             blas.zeros(n, L.work.ptr);
             L.prolongation->apply(C.sol.ptr, L.work.ptr);
             blas.axpby(n, T(1), L.work.ptr, T(1), sol);
-            L.smoother->apply(rhs, sol);
+            if (l == 0 && harvest) blas.copy(n, sol, harvest);
+            (L.post_smoother ? L.post_smoother : L.smoother)->apply(rhs, sol);
         }
         return 0;
     }

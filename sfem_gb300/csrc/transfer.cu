@@ -18,10 +18,29 @@
 namespace sfem_gb300 {
 
 // P: to[gid(e, fine lidx)] = sum_c w_c from[gid(e, coarse corner c)]
+// No floating-point division inside the kernels (FP64 division is a long
+// instruction sequence on GB300): the 1/s factor comes from the host and the
+// incidence counts of nested hex meshes (1, 2, 4, 8) are inverted exactly.
+template <typename T>
+__device__ __forceinline__ T inv_count(unsigned c) {
+    switch (c) {
+        case 1:
+            return T(1);
+        case 2:
+            return T(0.5);
+        case 4:
+            return T(0.25);
+        case 8:
+            return T(0.125);
+        default:
+            return T(1) / T(c);
+    }
+}
+
 template <typename T>
 __global__ void prolongate_kernel(ptrdiff_t nelements, int from_level, const idx_t *const *from_elements, int to_level,
                                   const idx_t *const *to_elements, int vec_size, const T *__restrict__ from,
-                                  T *__restrict__ to) {
+                                  T *__restrict__ to, T inv_s) {
     const int nf = to_level + 1;
     const int s = to_level / from_level;
     const ptrdiff_t total = nelements * (ptrdiff_t)(nf * nf * nf);
@@ -30,7 +49,7 @@ __global__ void prolongate_kernel(ptrdiff_t nelements, int from_level, const idx
         const int v = (int)(t / nelements);
         const int xi = v % nf, yi = (v / nf) % nf, zi = v / (nf * nf);
         const int cx = min(xi / s, from_level - 1), cy = min(yi / s, from_level - 1), cz = min(zi / s, from_level - 1);
-        const T tx = T(xi - cx * s) / T(s), ty = T(yi - cy * s) / T(s), tz = T(zi - cz * s) / T(s);
+        const T tx = T(xi - cx * s) * inv_s, ty = T(yi - cy * s) * inv_s, tz = T(zi - cz * s) * inv_s;
         const ptrdiff_t gid = to_elements[v][e];
         T acc[3] = {0, 0, 0};
 #pragma unroll
@@ -49,7 +68,7 @@ __global__ void prolongate_kernel(ptrdiff_t nelements, int from_level, const idx
 template <typename T>
 __global__ void restrict_kernel(ptrdiff_t nelements, int from_level, const idx_t *const *from_elements,
                                 const uint16_t *__restrict__ count, int to_level, const idx_t *const *to_elements,
-                                int vec_size, const T *__restrict__ from, T *__restrict__ to) {
+                                int vec_size, const T *__restrict__ from, T *__restrict__ to, T inv_s) {
     const int nc = to_level + 1;
     const int s = from_level / to_level;
     const ptrdiff_t total = nelements * (ptrdiff_t)(nc * nc * nc);
@@ -63,13 +82,13 @@ __global__ void restrict_kernel(ptrdiff_t nelements, int from_level, const idx_t
         const int y0 = max(0, (Y - 1) * s + 1), y1 = min(from_level, (Y + 1) * s - 1);
         const int z0 = max(0, (Z - 1) * s + 1), z1 = min(from_level, (Z + 1) * s - 1);
         for (int zi = z0; zi <= z1; zi++) {
-            const T wz = T(1) - T(abs(zi - Z * s)) / T(s);
+            const T wz = T(1) - T(abs(zi - Z * s)) * inv_s;
             for (int yi = y0; yi <= y1; yi++) {
-                const T wy = T(1) - T(abs(yi - Y * s)) / T(s);
+                const T wy = T(1) - T(abs(yi - Y * s)) * inv_s;
                 for (int xi = x0; xi <= x1; xi++) {
-                    const T wx = T(1) - T(abs(xi - X * s)) / T(s);
+                    const T wx = T(1) - T(abs(xi - X * s)) * inv_s;
                     const ptrdiff_t f = from_elements[lidx(from_level, xi, yi, zi)][e];
-                    const T w = wx * wy * wz / T(count[f]);
+                    const T w = wx * wy * wz * inv_count<T>(count[f]);
                     for (int d = 0; d < vec_size; d++) acc[d] += w * from[f * vec_size + d];
                 }
             }
@@ -97,7 +116,8 @@ static int prolongate_tpl(ptrdiff_t nelements, int from_level, idx_t **from_elem
                           idx_t **to_elements, int vec_size, const void *from, void *to, cudaStream_t s) {
     const ptrdiff_t total = nelements * (ptrdiff_t)((to_level + 1) * (to_level + 1) * (to_level + 1));
     prolongate_kernel<T><<<grid_for(total, 256, kNumSMs * 32), 256, 0, s>>>(
-            nelements, from_level, from_elements, to_level, to_elements, vec_size, (const T *)from, (T *)to);
+            nelements, from_level, from_elements, to_level, to_elements, vec_size, (const T *)from, (T *)to,
+            (T)(1.0 / (double)(to_level / from_level)));
     return check_launch("sfem_gb300_sshex8_prolongate");
 }
 
@@ -106,7 +126,8 @@ static int restrict_tpl(ptrdiff_t nelements, int from_level, idx_t **from_elemen
                         int to_level, idx_t **to_elements, int vec_size, const void *from, void *to, cudaStream_t s) {
     const ptrdiff_t total = nelements * (ptrdiff_t)((to_level + 1) * (to_level + 1) * (to_level + 1));
     restrict_kernel<T><<<grid_for(total, 256, kNumSMs * 32), 256, 0, s>>>(
-            nelements, from_level, from_elements, count, to_level, to_elements, vec_size, (const T *)from, (T *)to);
+            nelements, from_level, from_elements, count, to_level, to_elements, vec_size, (const T *)from, (T *)to,
+            (T)(1.0 / (double)(from_level / to_level)));
     return check_launch("sfem_gb300_sshex8_restrict");
 }
 

@@ -238,6 +238,7 @@ def build_poisson_mg(ctx, H: Hierarchy, dtype, smoother="chebyshev3", sweeps=2, 
         mg_add_level(mg, ops[k], smoothers[k], P, R)
     mg.keep += [H]
     mg.eigs = eigs
+    mg.smoothers = smoothers
     return mg, ops[0]
 
 

@@ -43,11 +43,12 @@ def test_elasticity_apply_fp64(cuda, L):
     y0 = rng.standard_normal(3 * n)
     ref = O.linear_elasticity_apply(L if L > 1 else 0, el, adj, det, MU, LAM, u, out=y0.copy())
     yd = torch.from_numpy(y0).to(cuda)
+    ud = torch.from_numpy(u).to(cuda)
     capi.check(capi.load().sfem_gb300_linear_elasticity_apply(sp.element_type, capi.i64(m.n_elements),
                                                               sp.elements_ptrs.ptr, capi.i64(m.n_elements),
                                                               capi.vp(adj_d), capi.vp(det_d), ctypes_d(MU),
                                                               ctypes_d(LAM), capi.FLOAT64,
-                                                              capi.vp(torch.from_numpy(u).to(cuda)), capi.vp(yd), None),
+                                                              capi.vp(ud), capi.vp(yd), None),
                "elasticity apply")
     err = np.abs(yd.cpu().numpy() - ref) / (_scale(L, el, adj, det, u) + np.abs(y0))
     assert err.max() < 1e-13, err.max()
@@ -68,7 +69,8 @@ def test_elasticity_reference_signature_and_fp32(cuda):
     u = np.random.default_rng(5).standard_normal(3 * n)
     ref = O.linear_elasticity_apply(L, el, adj, det, MU, LAM, u)
     lib = capi.load()
-    for dt, rt, tol in ((torch.float64, capi.FLOAT64, 1e-13), (torch.float32, capi.FLOAT32, 3e-5)):
+    # FP32 vectors run the tensor-core kernel: BF16 element contraction (8-bit mantissa), FP32 accumulate
+    for dt, rt, tol in ((torch.float64, capi.FLOAT64, 1e-13), (torch.float32, capi.FLOAT32, 2e-2)):
         ud = torch.from_numpy(u).to(cuda).to(dt)
         yd = torch.zeros(3 * n, dtype=dt, device=cuda)
         es = ud.element_size()

@@ -149,3 +149,25 @@ def test_oracle_cg_converges():
     b[dn] = 0
     x, it = OS.cg(apply, b, rtol=1e-12)
     assert np.linalg.norm(b - apply(x)) < 1e-10 * np.linalg.norm(b)
+
+
+def test_patchconv_oracle_matches_torch_autograd():
+    """The oracle loop nests of the learned-smoother network agree with an independent
+    torch CPU conv3d + autograd (forward, input gradient, weight gradient)."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(0)
+    for cin, cout in ((1, 16), (16, 16), (16, 1)):
+        P = 3
+        x = rng.standard_normal((P, 125, cin)).astype(np.float32)
+        W = rng.standard_normal((cout, cin, 27)).astype(np.float32)
+        xt = torch.from_numpy(x).double().reshape(P, 5, 5, 5, cin).permute(0, 4, 1, 2, 3).requires_grad_(True)
+        Wt = torch.from_numpy(W).double().reshape(cout, cin, 3, 3, 3).requires_grad_(True)
+        yt = torch.nn.functional.conv3d(xt, Wt, padding=1).permute(0, 2, 3, 4, 1).reshape(P, 125, cout)
+        y = O.patchconv_forward(P, cin, cout, x, W, 0).reshape(P, 125, cout)
+        assert np.abs(yt.detach().numpy() - y).max() < 1e-11
+        g = rng.standard_normal((P, 125, cout)).astype(np.float32)
+        yt.backward(torch.from_numpy(g).double())
+        gin = O.patchconv_backward_data(P, cin, cout, g, W).reshape(P, 125, cin)
+        assert np.abs(xt.grad.permute(0, 2, 3, 4, 1).reshape(P, 125, cin).numpy() - gin).max() < 1e-11
+        dW = O.patchconv_backward_weights(P, cin, cout, g, x)
+        assert np.abs(Wt.grad.reshape(-1).numpy() - dW).max() < 1e-11

@@ -49,8 +49,9 @@ def test_hex8_laplacian_crs_sym_assembly_and_spmv(cuda):
     y_or = O.crs_sym_spmv(rowptr, colidx, d_ref, o_ref, x)
     assert np.abs(y_or - y_mf).max() <= 1e-12 * np.abs(y_mf).max()
     y = torch.full((n,), 3.0, dtype=torch.float64, device=cuda)
+    x_d = _t(x, cuda)
     capi.check(lib.sfem_gb300_crs_sym_spmv(capi.FLOAT64, capi.i64(n), capi.vp(rp), capi.vp(ci), capi.vp(diag),
-                                           capi.vp(off), D(0.5), capi.vp(_t(x, cuda)), capi.vp(y), None), "spmv")
+                                           capi.vp(off), D(0.5), capi.vp(x_d), capi.vp(y), None), "spmv")
     assert np.abs(y.cpu().numpy() - (1.5 + y_or)).max() <= 1e-12 * np.abs(y_or).max()
 
 
@@ -90,8 +91,11 @@ def test_bsr_sym_spmv(cuda, bs, sym):
     x = rng.standard_normal(nb * bs)
     ref = O.bsr_sym_spmv(bs, rowptr, colidx, dsym, off_full, x)
     y = torch.zeros(nb * bs, dtype=torch.float64, device=cuda)
-    capi.check(capi.load().sfem_gb300_bsr_sym_spmv(capi.FLOAT64, bs, capi.i64(nb), capi.vp(_t(rowptr, cuda)),
-                                                   capi.vp(_t(colidx, cuda)), capi.vp(_t(dsym, cuda)),
-                                                   capi.vp(_t(off_in, cuda)), sym, D(0.0), capi.vp(_t(x, cuda)),
-                                                   capi.vp(y), None), "bsr")
+    # keep every device array referenced until the kernel has run (no temporaries whose
+    # memory the caching allocator could hand to the next argument)
+    rp_d, ci_d, d_d, o_d, x_d = (_t(a, cuda) for a in (rowptr, colidx, dsym, off_in, x))
+    capi.check(capi.load().sfem_gb300_bsr_sym_spmv(capi.FLOAT64, bs, capi.i64(nb), capi.vp(rp_d), capi.vp(ci_d),
+                                                   capi.vp(d_d), capi.vp(o_d), sym, D(0.0), capi.vp(x_d), capi.vp(y),
+                                                   None), "bsr")
+    torch.cuda.synchronize()
     assert np.abs(y.cpu().numpy() - ref).max() <= 1e-12 * np.abs(ref).max()

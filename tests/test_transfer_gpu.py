@@ -30,8 +30,9 @@ def test_prolongate_restrict(cuda, L, lc, vec):
     xc = rng.standard_normal(nc * vec)
     ref = O.prolongate(lc, ec, L, ef, vec, xc, nf)
     out = torch.zeros(nf * vec, dtype=torch.float64, device=cuda)
+    xc_d = _dev(xc, cuda)
     capi.check(lib.sfem_gb300_sshex8_prolongate(capi.i64(m.n_elements), lc, pc.ptr, L, pf.ptr, vec, capi.FLOAT64,
-                                                capi.vp(_dev(xc, cuda)), capi.vp(out), None), "prolongate")
+                                                capi.vp(xc_d), capi.vp(out), None), "prolongate")
     assert np.abs(out.cpu().numpy() - ref).max() <= 1e-14 * np.abs(ref).max()
 
     cnt = O.incidence_count(L, ef, nf)
@@ -42,8 +43,9 @@ def test_prolongate_restrict(cuda, L, lc, vec):
     xf = rng.standard_normal(nf * vec)
     ref_r = O.restrict(L, ef, cnt, lc, ec, vec, xf, nc)
     out_r = torch.zeros(nc * vec, dtype=torch.float64, device=cuda)
+    xf_d = _dev(xf, cuda)
     capi.check(lib.sfem_gb300_sshex8_restrict(capi.i64(m.n_elements), L, pf.ptr, capi.vp(cnt_d), lc, pc.ptr, vec,
-                                              capi.FLOAT64, capi.vp(_dev(xf, cuda)), capi.vp(out_r), None), "restrict")
+                                              capi.FLOAT64, capi.vp(xf_d), capi.vp(out_r), None), "restrict")
     assert np.abs(out_r.cpu().numpy() - ref_r).max() <= 1e-13 * np.abs(ref_r).max()
     # R = P^T: (R xf, xc) == (xf, P xc)
     lhs = float(out_r.cpu().numpy() @ xc)
