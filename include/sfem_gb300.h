@@ -197,6 +197,21 @@ int sfem_gb300_reciprocal(int real_type, ptrdiff_t n, double alpha, void *x, voi
 /* z = x * y + alpha z  (BLAS<T>::xypaz; the Jacobi smoother step) */
 int sfem_gb300_xypaz(int real_type, ptrdiff_t n, const void *x, const void *y, double alpha, void *z, void *stream);
 
+/* Allocation-free dot product for callers that cannot allocate device memory:
+ * code running while someone else's stream capture is building a CUDA graph,
+ * code inside a memory arena or pool that forbids cudaMalloc, plugins whose host
+ * application owns every allocation.  No reference counterpart.  Same result as
+ * sfem_gb300_dot (deterministic order), but the scratch is a fixed array inside
+ * the library (1024 block partial sums + a ticket word, 8.25 KiB per GPU, held
+ * until the process exits) instead of a caller workspace.  n above
+ * SFEM_GB300_NOALLOC_MAX_N is rejected.  All calls on a GPU share that scratch:
+ * calls that may overlap on the GPU (different streams, unordered threads) race
+ * and must be serialised by the caller.  The first call on each device looks up
+ * the scratch address and clears it; make that first call before any stream
+ * capture.  *result is a device pointer. */
+#define SFEM_GB300_NOALLOC_MAX_N 2147483647LL
+int sfem_gb300_dot_noalloc(int real_type, ptrdiff_t n, const void *x, const void *y, double *result, void *stream);
+
 /* Fused CG updates with device-resident scalars (no host round trip), cf. the
  * host fusion in algebra/sfem_cg.hpp:26-72:
  *   alpha = *alpha_num / *alpha_den;  x += alpha p;  r -= alpha Ap;  if rr: *rr = (r, r). */
