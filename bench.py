@@ -206,19 +206,20 @@ def time_apply(op, x, y, steps, warmup, flush, stream):
 def measure_solves(m, dev, rtol=1e-10):
     """Time to ||b - A x|| / ||b|| <= rtol (FP64, true residual) on the same problem:
     plain FP64 MG-PCG (Chebyshev3 V(2,2), Jacobi-PCG coarse) vs FP64 iterative
-    refinement around an FP32 MG-PCG (same hierarchy in float)."""
+    refinement around an FP32 MG-PCG (same hierarchy in float).  The hierarchy is
+    the sshex8 levels followed by hex8 levels coarsening the macro grid."""
     import torch
 
     from sfem_gb300 import solvers as S
 
-    H = S.Hierarchy(m, dirichlet_faces=("x0",), device=dev)
+    H = S.Hierarchy(m, dirichlet_faces=("x0",), device=dev, coarsen_macro=True)
     N = m.n_nodes()
     g = torch.Generator(device=dev).manual_seed(SEED + 7)
     b = torch.randn(N, dtype=torch.float64, device=dev, generator=g)
     b[H.dirichlet[0].long()] = 0
     ctx = S.context()
     op64 = S.laplacian_op(ctx, H.spaces[0], H.fff, H.dirichlet[0], torch.float64)
-    out = {}
+    out = {"levels_nodes": [sp.n_nodes for sp in H.spaces]}
 
     def true_rel(x):
         r = torch.zeros_like(b)
@@ -239,7 +240,8 @@ def measure_solves(m, dev, rtol=1e-10):
     t64 = time.perf_counter() - t0
     it64, _ = S.stats(cg64)
     out["plain_fp64_mg_pcg"] = {"seconds": t64, "iterations": it64, "true_rel_residual": true_rel(x), "rc": rc,
-                                "setup_seconds": setup64, "smoother": "Chebyshev3 V(2,2)", "coarse": "Jacobi-PCG 1e-6"}
+                                "setup_seconds": setup64, "smoother": "Chebyshev3 V(2,2)",
+                                "coarse": "Jacobi-PCG 1e-6 on the coarsest hex8 level"}
     x64 = x.clone()
     # mixed: FP64 refinement around FP32 MG-PCG (eigenvalues reused from the FP64 setup)
     t0 = time.perf_counter()
@@ -293,7 +295,7 @@ def measure_elasticity_solves(dev, nx=64, ny=16, nz=16, rtol=1e-9, mu=1.0, lam=1
     from sfem_gb300.mesh import SSMesh
 
     m = SSMesh(nx, ny, nz, LEVEL, box=((0, 4), (0, 1), (0, 1)), perturb=0.0, seed=SEED)
-    H = S.Hierarchy(m, dirichlet_faces=("x0",), device=dev, vec=3)
+    H = S.Hierarchy(m, dirichlet_faces=("x0",), device=dev, vec=3, coarsen_macro=True)
     b = torch.from_numpy(lumped_body_force(m, H.det.cpu().numpy())).to(dev)
     for c in range(3):
         b[3 * H.dirichlet[0].long() + c] = 0
@@ -305,7 +307,7 @@ def measure_elasticity_solves(dev, nx=64, ny=16, nz=16, rtol=1e-9, mu=1.0, lam=1
         S.apply(op64, x, r)
         return float(torch.linalg.vector_norm(b - r) / torch.linalg.vector_norm(b))
 
-    out = {"dofs": 3 * m.n_nodes(), "macro_elements": m.n_elements}
+    out = {"dofs": 3 * m.n_nodes(), "macro_elements": m.n_elements, "levels_nodes": [sp.n_nodes for sp in H.spaces]}
     mg64, _ = S.build_elasticity_mg(ctx, H, torch.float64, mu=mu, lam=lam, coarse_max_it=300)
     cg64 = S.cg(ctx, op64, mg64, rtol=rtol, max_it=500, residual_norm=True, flexible=True)
     x = torch.zeros_like(b)
@@ -318,7 +320,8 @@ def measure_elasticity_solves(dev, nx=64, ny=16, nz=16, rtol=1e-9, mu=1.0, lam=1
     out["plain_fp64_mg_pcg"] = {"seconds": t64, "iterations": it64, "true_rel_residual": true_rel(x), "rc": rc,
                                 "rtol": rtol}
     x64 = x.clone()
-    mg32, op32 = S.build_elasticity_mg(ctx, H, torch.float32, mu=mu, lam=lam, eig_max=mg64.eigs, coarse_max_it=300)
+    mg32, op32 = S.build_elasticity_mg(ctx, H, torch.float32, mu=mu, lam=lam, eig_max=mg64.eigs, coarse_max_it=300,
+                                       tensor_cores=True)
     inner = S.cg(ctx, op32, mg32, rtol=1e-4, max_it=40, residual_norm=True, flexible=True)
     ir = S.iterative_refinement(ctx, op64, inner, max_it=30, rtol=rtol)
     x = torch.zeros_like(b)

@@ -39,6 +39,11 @@ extern "C" {
 #define SFEM_GB300_REAL_DEFAULT 0
 #define SFEM_GB300_FLOAT32 1
 #define SFEM_GB300_FLOAT64 2
+/* float vectors with the element contraction on the tensor cores in BF16
+ * (FP32 accumulate); accepted by the linear-elasticity apply only.  Entry
+ * error is about 1e-2 of |K||u|: for smoothers inside a multigrid
+ * preconditioner, not for the operator of a Krylov method. */
+#define SFEM_GB300_FLOAT32_BF16TC 3
 
 typedef int32_t sfem_gb300_idx_t;
 
@@ -373,6 +378,47 @@ int sfem_gb300_mg_set_harvest(void *mg, void *x_cc);
 int sfem_gb300_ir_create(void *context, void *op64, void *inner32, int max_it, double rtol, void **solver);
 int sfem_gb300_solver_apply(void *solver, const void *b, void *x);
 int sfem_gb300_solver_stats(void *solver, int *iterations, double *last_relative);
+
+/* ------------------------------------------------------------ batched solves
+ * No reference counterpart (the reference runs one solve per process).  The
+ * vectors of P independent problems are concatenated, problem p owning the
+ * dof range [offsets[p], offsets[p+1]).  Element operators need no batched
+ * form: connectivity of several problems concatenated with node offsets is a
+ * larger mesh.  The calls below add the per-problem Krylov algebra. */
+
+/* Work list of (problem, dof range) chunks of at most `chunk` dofs (host offsets, P + 1). */
+int sfem_gb300_batch_layout_create(void *context, int n_problems, const int64_t *offsets, int chunk, void **layout);
+/* Launch shape of the batched vector kernels: chunk, threads per CTA (multiple of 32,
+ * <= 1024), CTAs per SM of the persistent grid.  Graphs captured before are rebuilt. */
+int sfem_gb300_batch_layout_set_launch(void *layout, int chunk, int threads, int ctas_per_sm);
+/* d_out[p] = (x_p, y_p) for every problem (device array of P doubles), deterministic. */
+int sfem_gb300_batch_dot(void *layout, int real_type, const void *x, const void *y, double *d_out);
+/* Block-diagonal operator: ops[g] acts on [offsets[g], offsets[g+1]) (host offsets). */
+int sfem_gb300_batch_grouped_op_create(void *context, int real_type, int n_ops, void **ops, const int64_t *offsets,
+                                       void **op);
+/* Chebyshev3 on D^-1 A with one eigenvalue estimate per problem (batched power method,
+ * eigen_max_it normalised iterations from a seeded U(-1,1) vector). */
+int sfem_gb300_batch_chebyshev3_create(void *context, void *layout, void *op, const void *inv_diag, int max_it,
+                                       double scale_eig_max, double scale_eig_min, int eigen_max_it,
+                                       unsigned long long seed, void **solver);
+int sfem_gb300_batch_chebyshev3_eig_max(void *solver, double *eig_max_out /* host, P */);
+/* (Flexible) preconditioned CG over the batch: exactly `iterations` iterations per
+ * apply, per-problem scalars on the device, problem p stops updating once
+ * ||r_p|| <= rtol ||r0_p||.  Never synchronises with the host. */
+int sfem_gb300_batch_cg_create(void *context, void *layout, void *op, void *precond, int iterations, double rtol,
+                               int flexible, void **solver);
+/* FP64 iterative refinement over the batch around a float batched inner solver; with
+ * use_graph one outer step is captured into a CUDA graph and replayed. */
+int sfem_gb300_batch_ir_create(void *context, void *layout, void *op64, void *inner32, int max_outer, double rtol,
+                               int use_graph, void **solver);
+/* Solves to ||b_p - A x_p|| <= rtol ||b_p|| for every p.  Host outputs (each may be
+ * NULL): seconds from start until problem p was seen converged, the outer step at
+ * which it converged, its last relative residual; total seconds. */
+int sfem_gb300_batch_ir_solve(void *solver, const double *b, double *x, double *latency_s,
+                              int *outer_steps_per_problem, double *final_rel, double *seconds);
+/* Mean milliseconds of `reps` replays of the captured outer step, starting from x
+ * (x is modified): the autotuner's measurement. */
+int sfem_gb300_batch_ir_time_step(void *solver, const double *b, double *x, int reps, double *ms);
 
 #ifdef __cplusplus
 }

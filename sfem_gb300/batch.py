@@ -1,0 +1,340 @@
+"""Batched serving: many independent sshex8 Poisson / elasticity solves at once.
+
+No reference counterpart (the reference runs one solve per process,
+``drivers/mgsolve.cpp``).  Problems are grouped by (kind, level L); within a
+group the meshes of all problems are concatenated with node offsets, so every
+element operator and transfer of the group is ONE launch of the single-problem
+kernels over all its problems.  Vectors of all groups are concatenated again
+into one batch vector (problem p owns a contiguous dof range), on which the
+batched kernels of ``csrc/batched.cu`` run the per-problem Krylov algebra:
+
+    FP64 iterative refinement (per-problem residual check, rtol on ||r_p|| / ||b_p||)
+      -> FP32 flexible CG, fixed iterations, per-problem scalars and masks
+         -> block-diagonal preconditioner: one multigrid V(s, s) per group with
+            per-problem Chebyshev3 bounds and a batched Jacobi-PCG coarse solve.
+
+One outer step is captured into a CUDA graph and replayed; the autotuner picks
+the work-list chunk and CTA shape of the batched vector kernels by timing the
+captured step.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import capi
+from . import solvers as S
+from .mesh import SSMesh, derefinement_levels, perturbed_macro_points
+from .operators import Laplacian
+
+c_double = C.c_double
+c_int = C.c_int
+
+
+@dataclass(frozen=True)
+class ProblemSpec:
+    kind: str  # "poisson" | "elasticity"
+    n: int  # macro elements per cube edge
+    level: int  # micro level L
+    seed: int
+
+    @property
+    def vec(self) -> int:
+        return 3 if self.kind == "elasticity" else 1
+
+
+def draw_problems(count=256, n_range=(8, 32), levels=(2, 3, 4), seed=0, kinds=("poisson", "elasticity")):
+    """Seeded problem mix: kind uniform over ``kinds``, edge n uniform in n_range
+    (inclusive), level uniform over ``levels``."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(count):
+        kind = kinds[int(rng.integers(len(kinds)))]
+        n = int(rng.integers(n_range[0], n_range[1] + 1))
+        L = int(levels[int(rng.integers(len(levels)))])
+        out.append(ProblemSpec(kind, n, L, int(seed * 100003 + i)))
+    return out
+
+
+_MESHES: dict = {}
+
+
+def _mesh(n, L) -> SSMesh:
+    """Numbering / connectivity of an n^3 cube at level L (geometry is per problem)."""
+    key = (n, L)
+    if key not in _MESHES:
+        _MESHES[key] = SSMesh(n, n, n, L)
+    return _MESHES[key]
+
+
+class _LevelSpace:
+    """One level of a group: concatenated connectivity of its problems on the device."""
+
+    def __init__(self, device, level, element_type, elements, lidx, count, n_nodes, n_elements):
+        import torch
+
+        t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(device)
+        self.level = level
+        self.element_type = element_type
+        self.n_nodes = n_nodes
+        self.n_elements = n_elements
+        self.device = device
+        self.elements = t(elements)
+        self.elements_ptrs = capi.DevicePtrArray(self.elements)
+        self.corners_ptrs = None
+        self.lidx_elements = t(lidx)
+        self.lidx_ptrs = capi.DevicePtrArray(self.lidx_elements)
+        self.count = t(count.view(np.int16))
+
+
+class BatchGroup:
+    """All problems of one (kind, level): concatenated hierarchy, geometry, rhs."""
+
+    def __init__(self, kind, level, problems, device, perturb=0.1, dirichlet_face="x0"):
+        import torch
+
+        self.kind, self.L, self.problems = kind, level, list(problems)
+        self.vec = 3 if kind == "elasticity" else 1
+        self.device = torch.device(device)
+        self.levels = derefinement_levels(level)
+        meshes = [_mesh(p.n, level) for p in self.problems]
+        self.spaces, self.dirichlet, self.node_offsets = [], [], []
+        for l in self.levels:
+            offs = np.cumsum([0] + [m.n_nodes(l) for m in meshes])
+            self.node_offsets.append(offs)
+            els, lids, cnts, dns = [], [], [], []
+            for m, o in zip(meshes, offs[:-1]):
+                lid = m.elements(l)
+                lids.append(lid + o)
+                els.append((m.hex8_elements() if l == 1 else lid) + o)
+                cnts.append(np.bincount(lid.reshape(-1), minlength=m.n_nodes(l)).astype(np.uint16))
+                dns.append(m.boundary_nodes(dirichlet_face, l) + o)
+            E = sum(m.n_elements for m in meshes)
+            et = capi.HEX8 if l == 1 else capi.SSHEX8(l)
+            self.spaces.append(_LevelSpace(self.device, l, et, np.concatenate(els, axis=1).astype(np.int32),
+                                           np.concatenate(lids, axis=1).astype(np.int32), np.concatenate(cnts),
+                                           int(offs[-1]), E))
+            self.dirichlet.append(torch.from_numpy(np.concatenate(dns).astype(np.int32)).to(self.device))
+        self.n_nodes = int(self.node_offsets[0][-1])
+        self.n_dofs = self.vec * self.n_nodes
+        self._geometry(meshes, perturb)
+
+    def _geometry(self, meshes, perturb):
+        """Per-problem perturbed macro grids -> FFF (Laplacian) or adjugate (elasticity)."""
+        import torch
+
+        pts, corners = [], []
+        off = 0
+        for p, m in zip(self.problems, meshes):
+            macro = perturbed_macro_points(p.n, p.n, p.n, perturb=perturb, seed=p.seed).astype(np.float32)
+            K, J, I = np.meshgrid(np.arange(p.n + 1), np.arange(p.n + 1), np.arange(p.n + 1), indexing="ij")
+            ids = m.node_id(I * m.L, J * m.L, K * m.L).reshape(-1)  # level-1 ids
+            P1 = np.empty((3, m.n_nodes(1)), dtype=np.float32)
+            P1[:, ids] = macro.reshape(3, -1)
+            pts.append(P1)
+            corners.append(m.hex8_elements() + off)
+            off += m.n_nodes(1)
+        dev = self.device
+        self._points = torch.from_numpy(np.ascontiguousarray(np.concatenate(pts, axis=1))).to(dev)
+        self._corners = torch.from_numpy(np.ascontiguousarray(np.concatenate(corners, axis=1))).to(dev)
+        pp, cp = capi.DevicePtrArray(self._points), capi.DevicePtrArray(self._corners)
+        E = self._corners.shape[1]
+        lib = capi.load()
+        self.fff = torch.empty((6, E), dtype=torch.float32, device=dev)
+        capi.check(lib.sfem_gb300_hex8_fff_fill(capi.i64(E), cp.ptr, pp.ptr, capi.i64(E), capi.vp(self.fff), None),
+                   "fff_fill")
+        self.adj = torch.empty((9, E), dtype=torch.float32, device=dev)
+        self.det = torch.empty(E, dtype=torch.float32, device=dev)
+        capi.check(lib.sfem_gb300_hex8_adjugate_fill(capi.i64(E), cp.ptr, pp.ptr, capi.i64(E), capi.vp(self.adj),
+                                                     capi.vp(self.det), None), "adjugate_fill")
+
+    def problem_dof_offsets(self, k=0):
+        return self.vec * self.node_offsets[k]
+
+    def rhs(self):
+        """N(0,1) per dof (seeded per problem), zero on Dirichlet dofs."""
+        parts = []
+        for p, o0, o1 in zip(self.problems, self.node_offsets[0][:-1], self.node_offsets[0][1:]):
+            parts.append(np.random.default_rng(p.seed + 7).standard_normal(self.vec * int(o1 - o0)))
+        b = np.concatenate(parts)
+        dn = self.dirichlet[0].cpu().numpy().astype(np.int64)
+        for c in range(self.vec):
+            b[self.vec * dn + c] = 0
+        return b
+
+    # ------------------------------------------------------------------ operators
+    def op(self, ctx, k, dtype, tensor_cores=False):
+        sp = self.spaces[k]
+        if self.kind == "poisson":
+            return S.laplacian_op(ctx, sp, self.fff, self.dirichlet[k], dtype)
+        return S.elasticity_op(ctx, sp, self.adj, self.det, 1.0, 10.0, self.dirichlet[k], dtype,
+                               tensor_cores=tensor_cores)
+
+    def diag(self, k, dtype):
+        import torch
+
+        sp = self.spaces[k]
+        d = torch.zeros(self.vec * sp.n_nodes, dtype=dtype, device=self.device)
+        if self.kind == "poisson":
+            Laplacian(sp).set_fff(self.fff).hessian_diag(d)
+        else:
+            E = sp.n_elements
+            capi.check(capi.load().sfem_gb300_linear_elasticity_block_diag(
+                sp.element_type, capi.i64(E), sp.elements_ptrs.ptr, capi.i64(E), capi.vp(self.adj),
+                capi.vp(self.det), c_double(1.0), c_double(10.0), S.rt_of(dtype), capi.vp(d), None, None), "diag")
+        dn = self.dirichlet[k].long()
+        for c in range(self.vec):
+            d[self.vec * dn + c] = 1
+        return d
+
+    def transfer(self, ctx, k, dtype):
+        C_, F = self.spaces[k + 1], self.spaces[k]
+        P = S.prolongation_op(ctx, C_, F, self.vec, self.dirichlet[k], dtype)
+        R = S.restriction_op(ctx, F, C_, self.vec, self.dirichlet[k + 1], dtype)
+        return P, R
+
+
+def _layout(ctx, dof_offsets, chunk=4096) -> S.Handle:
+    offs = np.ascontiguousarray(np.asarray(dof_offsets, dtype=np.int64))
+    return S._create(capi.load().sfem_gb300_batch_layout_create, ctx.ptr, c_int(len(offs) - 1),
+                     offs.ctypes.data_as(C.c_void_p), c_int(chunk), keep=(ctx,))
+
+
+class BatchSolver:
+    """Mixed-precision batched solver over a list of :class:`ProblemSpec`."""
+
+    def __init__(self, problems, device="cuda:0", sweeps=2, coarse_iterations=30, inner_iterations=8,
+                 inner_rtol=1e-4, rtol=1e-10, max_outer=30, tensor_cores=True, use_graph=True, eigen_max_it=20,
+                 perturb=0.1):
+        import torch
+
+        self.device = torch.device(device)
+        self.ctx = S.context()
+        ctx = self.ctx
+        lib = capi.load()
+        keys = sorted({(p.kind, p.level) for p in problems})
+        self.groups = [BatchGroup(kd, L, [p for p in problems if (p.kind, p.level) == (kd, L)], self.device,
+                                  perturb=perturb) for kd, L in keys]
+        self.problems = [p for g in self.groups for p in g.problems]  # batch order
+        self.layouts = []
+        ops64, ops32, mgs, goffs = [], [], [], [0]
+        self.keep = []
+        for g in self.groups:
+            nlev = len(g.levels)
+            mg = S.multigrid(ctx, torch.float32)
+            lev_ops, smoothers = [], []
+            for k in range(nlev):
+                lay = _layout(ctx, g.problem_dof_offsets(k))
+                self.layouts.append(lay)
+                op = g.op(ctx, k, torch.float32)
+                d = g.diag(k, torch.float32)
+                if k == nlev - 1:
+                    jac = S.jacobi(ctx, d, 1.0)
+                    sm = S._create(lib.sfem_gb300_batch_cg_create, ctx.ptr, lay.ptr, op.ptr, jac.ptr,
+                                   c_int(coarse_iterations), c_double(1e-6), c_int(0), keep=(ctx, lay, op, jac))
+                else:
+                    sop = g.op(ctx, k, torch.float32, tensor_cores=tensor_cores and g.kind == "elasticity")
+                    inv = (1.0 / d).contiguous()
+                    sm = S._create(lib.sfem_gb300_batch_chebyshev3_create, ctx.ptr, lay.ptr, sop.ptr, capi.vp(inv),
+                                   c_int(sweeps), c_double(1.1 if g.kind == "elasticity" else 1.02), c_double(0.06),
+                                   c_int(eigen_max_it), C.c_ulonglong(S.RANDOM_SEED), keep=(ctx, lay, sop, inv))
+                P, R = g.transfer(ctx, k, torch.float32) if k + 1 < nlev else (None, None)
+                S.mg_add_level(mg, op, sm, P, R)
+                lev_ops.append(op)
+            mgs.append(mg)
+            ops32.append(lev_ops[0])
+            ops64.append(g.op(ctx, 0, torch.float64))
+            goffs.append(goffs[-1] + g.n_dofs)
+        self.group_offsets = np.asarray(goffs, dtype=np.int64)
+        self.n = int(goffs[-1])
+        dof_offs = [0]
+        for g in self.groups:
+            o = g.problem_dof_offsets(0)
+            dof_offs += list(dof_offs[-1] + o[1:])
+        self.dof_offsets = np.asarray(dof_offs, dtype=np.int64)
+        self.layout = _layout(ctx, self.dof_offsets)
+        self.layouts.append(self.layout)
+        self.op64 = self._grouped(torch.float64, ops64)
+        self.op32 = self._grouped(torch.float32, ops32)
+        self.precond = self._grouped(torch.float32, mgs)
+        self.inner = S._create(lib.sfem_gb300_batch_cg_create, ctx.ptr, self.layout.ptr, self.op32.ptr,
+                               self.precond.ptr, c_int(inner_iterations), c_double(inner_rtol), c_int(1),
+                               keep=(ctx, self.layout, self.op32, self.precond))
+        self.ir = S._create(lib.sfem_gb300_batch_ir_create, ctx.ptr, self.layout.ptr, self.op64.ptr, self.inner.ptr,
+                            c_int(max_outer), c_double(rtol), c_int(int(use_graph)),
+                            keep=(ctx, self.layout, self.op64, self.inner))
+        self.tuned = None
+
+    def _grouped(self, dtype, ops):
+        arr = (C.c_void_p * len(ops))(*[o.ptr.value for o in ops])
+        offs = np.ascontiguousarray(self.group_offsets)
+        return S._create(capi.load().sfem_gb300_batch_grouped_op_create, self.ctx.ptr, c_int(S.rt_of(dtype)),
+                         c_int(len(ops)), arr, offs.ctypes.data_as(C.c_void_p), keep=(self.ctx, *ops))
+
+    @property
+    def n_problems(self):
+        return len(self.problems)
+
+    def rhs(self):
+        import torch
+
+        return torch.from_numpy(np.concatenate([g.rhs() for g in self.groups])).to(self.device)
+
+    def set_launch(self, chunk, threads, ctas_per_sm):
+        for lay in self.layouts:
+            capi.check(capi.load().sfem_gb300_batch_layout_set_launch(lay.ptr, c_int(chunk), c_int(threads),
+                                                                       c_int(ctas_per_sm)), "set_launch")
+
+    def time_step(self, b, x, reps=2) -> float:
+        ms = c_double(0)
+        capi.check(capi.load().sfem_gb300_batch_ir_time_step(self.ir.ptr, capi.vp(b), capi.vp(x), c_int(reps),
+                                                             C.byref(ms)), "batch_ir_time_step")
+        return ms.value
+
+    def autotune(self, b, candidates=None, reps=2):
+        """Pick (chunk, threads, CTAs per SM) of the batched vector kernels by timing
+        the captured outer step on a scratch iterate; returns the timing table."""
+        import torch
+
+        if candidates is None:
+            candidates = [(2048, 256, 8), (4096, 256, 8), (8192, 256, 8), (8192, 512, 4), (16384, 512, 4),
+                          (4096, 128, 16)]
+        table = []
+        for cand in candidates:
+            self.set_launch(*cand)
+            xs = torch.zeros_like(b)
+            table.append((cand, self.time_step(b, xs, reps)))
+        best = min(table, key=lambda t: t[1])[0]
+        self.set_launch(*best)
+        self.tuned = best
+        return table
+
+    def solve(self, b, x):
+        """Solve every problem to ||b_p - A_p x_p|| <= rtol ||b_p|| (FP64).  Returns
+        (rc, per-problem latency s, per-problem outer steps, per-problem final rel, seconds)."""
+        P = self.n_problems
+        lat = np.zeros(P)
+        steps = np.zeros(P, dtype=np.int32)
+        rel = np.zeros(P)
+        sec = c_double(0)
+        rc = capi.load().sfem_gb300_batch_ir_solve(self.ir.ptr, capi.vp(b), capi.vp(x),
+                                                   lat.ctypes.data_as(C.c_void_p), steps.ctypes.data_as(C.c_void_p),
+                                                   rel.ctypes.data_as(C.c_void_p), C.byref(sec))
+        return rc, lat, steps, rel, sec.value
+
+    def true_residuals(self, b, x):
+        """||b_p - A_p x_p|| / ||b_p|| per problem with the FP64 operators (device)."""
+        import torch
+
+        r = torch.zeros_like(b)
+        S.apply(self.op64, x, r)
+        r = b - r
+        rr = torch.zeros(self.n_problems, dtype=torch.float64, device=self.device)
+        bb = torch.zeros_like(rr)
+        lib = capi.load()
+        capi.check(lib.sfem_gb300_batch_dot(self.layout.ptr, capi.FLOAT64, capi.vp(r), capi.vp(r), capi.vp(rr)), "dot")
+        capi.check(lib.sfem_gb300_batch_dot(self.layout.ptr, capi.FLOAT64, capi.vp(b), capi.vp(b), capi.vp(bb)), "dot")
+        return (rr.sqrt() / bb.sqrt()).cpu().numpy()

@@ -19,6 +19,7 @@ SUCCESS = 0
 HEX8 = 8
 SSHEX8_BASE = 1000
 REAL_DEFAULT, FLOAT32, FLOAT64 = 0, 1, 2
+FLOAT32_BF16TC = 3  # float vectors, BF16 tensor-core element contraction (elasticity)
 
 
 def SSHEX8(L: int) -> int:

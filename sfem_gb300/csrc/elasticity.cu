@@ -417,17 +417,6 @@ __global__ void block_apply_kernel(ptrdiff_t n_nodes, const T *__restrict__ bloc
     }
 }
 
-// FP32 vectors use the tensor-core kernel (BF16 contraction) unless
-// SFEM_GB300_ELASTICITY_KERNEL=simt selects the FP32 SIMT kernel.
-static bool elasticity_use_tc() {
-    static int v = -1;
-    if (v < 0) {
-        const char *e = getenv("SFEM_GB300_ELASTICITY_KERNEL");
-        v = (e && e[0] == 's') ? 0 : 1;
-    }
-    return v == 1;
-}
-
 static int elasticity_apply_tc(int element_type, ptrdiff_t nelements, idx_t **elements, ptrdiff_t stride,
                                const float *adj, const float *det, float mu, float lambda, const float *x, float *y,
                                cudaStream_t s) {
@@ -459,9 +448,6 @@ template <typename T>
 static int elasticity_apply_tpl(int element_type, ptrdiff_t nelements, idx_t **elements, ptrdiff_t stride,
                                 const float *adj, const float *det, T mu, T lambda, const T *x, T *y, cudaStream_t s) {
     if (nelements <= 0) return SFEM_GB300_SUCCESS;
-    if (sizeof(T) == 4 && elasticity_use_tc())
-        return elasticity_apply_tc(element_type, nelements, elements, stride, adj, det, (float)mu, (float)lambda,
-                                   (const float *)x, (float *)y, s);
     const int blocks = grid_for((nelements + 1) / 2, 1, kNumSMs * 64);
     if (element_type == SFEM_GB300_HEX8) {
         elasticity_apply_warp_kernel<T, 1, true><<<blocks, 64, 0, s>>>(nelements, elements, stride, adj, det, mu,
@@ -524,6 +510,11 @@ extern "C" int sfem_gb300_linear_elasticity_apply(int element_type, ptrdiff_t ne
     if (real_type == SFEM_GB300_FLOAT32)
         return elasticity_apply_tpl<float>(element_type, nelements, elements, jacobian_stride, adjugate, determinant,
                                            (float)mu, (float)lambda, (const float *)u, (float *)out, s);
+    if (real_type == SFEM_GB300_FLOAT32_BF16TC) {
+        if (nelements <= 0) return SFEM_GB300_SUCCESS;
+        return elasticity_apply_tc(element_type, nelements, elements, jacobian_stride, adjugate, determinant,
+                                   (float)mu, (float)lambda, (const float *)u, (float *)out, s);
+    }
     if (real_type == SFEM_GB300_FLOAT64 || real_type == SFEM_GB300_REAL_DEFAULT)
         return elasticity_apply_tpl<double>(element_type, nelements, elements, jacobian_stride, adjugate, determinant,
                                             mu, lambda, (const double *)u, (double *)out, s);
@@ -537,7 +528,7 @@ extern "C" int cu_affine_sshex8_linear_elasticity_apply(int level, ptrdiff_t nel
                                                         const void *uy, const void *uz, ptrdiff_t out_stride,
                                                         void *outx, void *outy, void *outz, void *stream) {
     // Interleaved xyz vectors only: ux = u, uy = u + 1, uz = u + 2 with stride 3.
-    const size_t es = real_type == SFEM_GB300_FLOAT32 ? 4 : 8;
+    const size_t es = (real_type == SFEM_GB300_FLOAT32 || real_type == SFEM_GB300_FLOAT32_BF16TC) ? 4 : 8;
     if (u_stride != 3 || out_stride != 3 || (const char *)uy != (const char *)ux + es ||
         (const char *)uz != (const char *)ux + 2 * es || (char *)outy != (char *)outx + es ||
         (char *)outz != (char *)outx + 2 * es)

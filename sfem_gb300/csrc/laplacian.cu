@@ -306,6 +306,110 @@ __global__ void __launch_bounds__(128) sshex8_laplacian_apply_tpe_kernel(ptrdiff
     for (int p = 0; p < NP; p++) atomicAdd(&y[__ldg(&elements[L * NP + p][e])], ya[p]);
 }
 
+// v3 (bandwidth path, staged): a CTA owns a tile of TILE consecutive macro
+// elements, one thread per element.  Phase 1 gathers the tile's micro grids into
+// shared memory plane by plane (one coalesced connectivity line per warp and
+// plane node, then the x gathers, many loads in flight per thread); phase 2
+// applies the element matrix from shared memory with the two active y planes in
+// registers, writing each finished y plane over the x plane it no longer needs;
+// phase 3 scatters (plain read-modify-write inside the macro element, atomics
+// on its surface).  Shared layout [node][TILE] keeps every warp access
+// conflict-free.
+template <typename T, int L, int TILE>
+__global__ void __launch_bounds__(TILE) sshex8_laplacian_apply_staged_kernel(ptrdiff_t nelements,
+                                                                             const idx_t *const *elements,
+                                                                             ptrdiff_t fff_stride, const float *fff,
+                                                                             const T *__restrict__ x,
+                                                                             T *__restrict__ y) {
+    constexpr int N1 = L + 1;
+    constexpr int NP = N1 * N1;
+    constexpr int NXE = NP * N1;
+    extern __shared__ unsigned char smem_raw[];
+    T *xs = reinterpret_cast<T *>(smem_raw);  // [NXE][TILE]
+    const int t = threadIdx.x;
+    const ptrdiff_t e = (ptrdiff_t)blockIdx.x * TILE + t;
+    const bool active = e < nelements;
+    // phase 1: gather
+#pragma unroll 1
+    for (int z = 0; z < N1; z++) {
+        idx_t g[NP];
+#pragma unroll
+        for (int p = 0; p < NP; p++) g[p] = active ? __ldg(&elements[z * NP + p][e]) : 0;
+#pragma unroll
+        for (int p = 0; p < NP; p++) xs[(z * NP + p) * TILE + t] = active ? __ldg(&x[g[p]]) : T(0);
+    }
+    if (!active) return;  // no block-wide synchronisation below: each thread owns its column
+    const T h = T(1) / T(L);
+    T f[6];
+#pragma unroll
+    for (int m = 0; m < 6; m++) f[m] = (T)__ldg(&fff[m * fff_stride + e]) * h;
+    T A[64];
+#pragma unroll
+    for (int k = 0; k < 64; k++) {
+        T a = 0;
+#pragma unroll
+        for (int m = 0; m < 6; m++) {
+            const double w = LapTable().w[k][m];
+            if (w != 0.0) a += f[m] * T(w);
+        }
+        A[k] = a;
+    }
+    // phase 2: apply, planes of y in registers
+    T ya[NP], yb[NP];
+#pragma unroll
+    for (int p = 0; p < NP; p++) ya[p] = 0;
+#pragma unroll
+    for (int zi = 0; zi < L; zi++) {
+#pragma unroll
+        for (int p = 0; p < NP; p++) yb[p] = 0;
+#pragma unroll
+        for (int yi = 0; yi < L; yi++) {
+#pragma unroll
+            for (int xi = 0; xi < L; xi++) {
+                T u[8];
+#pragma unroll
+                for (int c = 0; c < 8; c++)
+                    u[c] = xs[((zi + c8z(c)) * NP + (yi + c8y(c)) * N1 + xi + c8x(c)) * TILE + t];
+#pragma unroll
+                for (int i = 0; i < 8; i++) {
+                    T acc = 0;
+#pragma unroll
+                    for (int j = 0; j < 8; j++) acc += A[i * 8 + j] * u[j];
+                    const int p = (yi + c8y(i)) * N1 + xi + c8x(i);
+                    if (c8z(i))
+                        yb[p] += acc;
+                    else
+                        ya[p] += acc;
+                }
+            }
+        }
+        // x plane zi is no longer needed: it receives the finished y plane zi
+#pragma unroll
+        for (int p = 0; p < NP; p++) {
+            xs[(zi * NP + p) * TILE + t] = ya[p];
+            ya[p] = yb[p];
+        }
+    }
+#pragma unroll
+    for (int p = 0; p < NP; p++) xs[(L * NP + p) * TILE + t] = ya[p];
+    // phase 3: scatter
+#pragma unroll 1
+    for (int z = 0; z < N1; z++) {
+        idx_t g[NP];
+#pragma unroll
+        for (int p = 0; p < NP; p++) g[p] = __ldg(&elements[z * NP + p][e]);
+#pragma unroll
+        for (int p = 0; p < NP; p++) {
+            const int xi = p % N1, yi = p / N1;
+            const T v = xs[(z * NP + p) * TILE + t];
+            if (z > 0 && z < L && xi > 0 && xi < L && yi > 0 && yi < L)
+                y[g[p]] += v;
+            else
+                atomicAdd(&y[g[p]], v);
+        }
+    }
+}
+
 // Diagonal: node value = sum over the micro elements of this macro element that
 // contain it of A[a][a] (a = the node's corner in that micro element).
 template <typename T, int L>
@@ -348,13 +452,14 @@ __global__ void __launch_bounds__(128) sshex8_laplacian_diag_kernel(ptrdiff_t ne
 
 // ------------------------------------------------------------------ dispatch
 
-// Kernel variant override for benchmarking: SFEM_GB300_LAPLACIAN_KERNEL=warp forces the
-// warp-per-element kernel (1); default (0) picks thread-per-element for float, L <= 4.
+// Kernel variant override for benchmarking (SFEM_GB300_LAPLACIAN_KERNEL):
+// default / "staged" (0) = shared-memory staged tile kernel for float, L <= 4;
+// "warp" (1) = warp per element; "thread" (2) = registers-only thread per element.
 static int laplacian_variant() {
     static int v = -1;
     if (v < 0) {
         const char *e = getenv("SFEM_GB300_LAPLACIAN_KERNEL");
-        v = (e && e[0] == 'w') ? 1 : 0;
+        v = (e && e[0] == 'w') ? 1 : (e && e[0] == 't') ? 2 : 0;
     }
     return v;
 }
@@ -369,7 +474,29 @@ static int laplacian_apply_tpl(int element_type, ptrdiff_t nelements, idx_t **el
     }
     const int L = element_type - SFEM_GB300_SSHEX8_BASE;
     const int blocks = grid_for((nelements + 3) / 4, 1, kNumSMs * 64);
-    const bool tpe = sizeof(T) == 4 && L >= 2 && L <= 4 && laplacian_variant() != 1;
+    const int variant = laplacian_variant();
+    if (sizeof(T) == 4 && L >= 2 && L <= 4 && variant == 0) {
+        constexpr int TILE = 64;
+        const int tb = (int)((nelements + TILE - 1) / TILE);
+        auto launch = [&](auto kernel, int nxe) {
+            const size_t smem = (size_t)nxe * TILE * sizeof(T);
+            if (smem > 48 * 1024) cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            kernel<<<tb, TILE, smem, s>>>(nelements, elements, fff_stride, fff, x, y);
+        };
+        switch (L) {
+            case 2:
+                launch(sshex8_laplacian_apply_staged_kernel<T, 2, TILE>, 27);
+                break;
+            case 3:
+                launch(sshex8_laplacian_apply_staged_kernel<T, 3, TILE>, 64);
+                break;
+            default:
+                launch(sshex8_laplacian_apply_staged_kernel<T, 4, TILE>, 125);
+                break;
+        }
+        return check_launch("cu_laplacian_apply(SSHEX8, staged tile)");
+    }
+    const bool tpe = sizeof(T) == 4 && L >= 2 && L <= 4 && variant == 2;
     if (tpe) {
         const int tb = (int)((nelements + 127) / 128);
         switch (L) {

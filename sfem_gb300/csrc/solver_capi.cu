@@ -11,23 +11,10 @@
 #include <string>
 
 #include "common.cuh"
+#include "capi_handle.hpp"
 #include "solvers.hpp"
 
 namespace sfem_gb300 {
-
-struct Handle {
-    int real_type{SFEM_GB300_FLOAT64};
-    std::string kind;
-    std::shared_ptr<Context> ctx;
-    std::shared_ptr<Operator<double>> d;
-    std::shared_ptr<Operator<float>> f;
-    // typed views for kind-specific calls
-    std::shared_ptr<void> impl;
-    ptrdiff_t rows() const { return d ? d->rows() : (f ? f->rows() : 0); }
-    ptrdiff_t cols() const { return d ? d->cols() : (f ? f->cols() : 0); }
-};
-
-static bool is_f32(int rt) { return rt == SFEM_GB300_FLOAT32; }
 
 // ---------------------------------------------------------------- operators
 
@@ -62,9 +49,10 @@ public:
     const float *adjugate{nullptr}, *determinant{nullptr};
     double mu{1}, lambda{1};
     const idx_t *dirichlet{nullptr};
+    int contraction{real_type_v<T>};  // FLOAT32_BF16TC: tensor-core BF16 element contraction
     int apply(const T *x, T *y) override {
         SFEM_GB300_CHECK(sfem_gb300_linear_elasticity_apply(element_type, nelements, elements, jac_stride, adjugate,
-                                                            determinant, mu, lambda, real_type_v<T>, x, y, ctx->sp()));
+                                                            determinant, mu, lambda, contraction, x, y, ctx->sp()));
         for (int c = 0; c < 3; c++)
             SFEM_GB300_CHECK(
                     sfem_gb300_constraint_nodes_copy(real_type_v<T>, n_dirichlet, dirichlet, 3, c, x, y, ctx->sp()));
@@ -140,24 +128,6 @@ public:
     ptrdiff_t cols() const override { return nrows; }
 };
 
-template <typename T>
-std::shared_ptr<Operator<T>> &op_of(Handle *h);
-template <>
-std::shared_ptr<Operator<double>> &op_of<double>(Handle *h) {
-    return h->d;
-}
-template <>
-std::shared_ptr<Operator<float>> &op_of<float>(Handle *h) {
-    return h->f;
-}
-
-template <typename T>
-Blas<T> blas_of(const std::shared_ptr<Context> &ctx) {
-    Blas<T> b;
-    b.ctx = ctx;
-    return b;
-}
-
 // Iterative refinement (no reference counterpart): outer loop in double with the
 // double operator, inner solve in float on the normalised residual.
 //   r = b - A x ; d = inner(r / |r|) ; x += |r| d ; until |r| <= rtol |b|.
@@ -226,7 +196,6 @@ using namespace sfem_gb300;
 
 typedef Handle sfem_gb300_handle;
 
-#define H(p) reinterpret_cast<Handle *>(p)
 
 extern "C" {
 
@@ -304,6 +273,7 @@ int sfem_gb300_elasticity_op_create(void *context, int real_type, int element_ty
     if (is_f32(real_type)) {
         auto op = std::make_shared<ElasticityOp<float>>();
         fill(op);
+        if (real_type == SFEM_GB300_FLOAT32_BF16TC) op->contraction = SFEM_GB300_FLOAT32_BF16TC;
         h->f = op;
     } else {
         auto op = std::make_shared<ElasticityOp<double>>();
@@ -667,10 +637,19 @@ int sfem_gb300_learned_smoother_create(void *context, void *op, idx_t **elements
         s->omega = omega;
         s->sweeps = sweeps;
     };
+    // the correction is zeroed on the operator's Dirichlet nodes
+    auto constraints = [](auto s, auto op) {
+        using T = typename std::remove_reference_t<decltype(*op)>::value_type;
+        if (auto lop = std::dynamic_pointer_cast<LaplacianOp<T>>(op)) {
+            s->dirichlet = lop->dirichlet;
+            s->n_dirichlet = lop->n_dirichlet;
+        }
+    };
     if (o->f) {
         auto s = std::make_shared<LearnedSmoother<float>>();
         fill(s, 0.0f);
         s->op = o->f;
+        constraints(s, o->f);
         if (fb) s->fallback = fb->f;
         h->f = s;
         h->impl = s;
@@ -678,6 +657,7 @@ int sfem_gb300_learned_smoother_create(void *context, void *op, idx_t **elements
         auto s = std::make_shared<LearnedSmoother<double>>();
         fill(s, 0.0);
         s->op = o->d;
+        constraints(s, o->d);
         if (fb) s->fallback = fb->d;
         h->d = s;
         h->impl = s;

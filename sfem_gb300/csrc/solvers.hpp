@@ -169,6 +169,7 @@ struct Blas {
 template <typename T>
 class Operator {
 public:
+    using value_type = T;
     virtual ~Operator() = default;
     virtual int apply(const T *x, T *y) = 0;
     virtual ptrdiff_t rows() const = 0;
@@ -355,25 +356,37 @@ public:
     ptrdiff_t nelements{0};
     const uint16_t *count{nullptr};
     const T *inv_diag{nullptr};
+    const idx_t *dirichlet{nullptr};  // the correction is zero on these nodes
+    ptrdiff_t n_dirichlet{0};
     const void *W[3]{nullptr, nullptr, nullptr};
     int channels{16}, sweeps{1};
     double omega{1.0};
     bool use_fallback{false};
-    bool chain{false};  // apply the fallback first, then the learned corrections
-    DeviceBuffer<T> r;
+    bool chain{false};        // apply the fallback first, then the learned corrections
+    bool line_search{true};   // step length minimising the energy norm of the error along the correction
+    DeviceBuffer<T> r, d, Ad;
     DeviceBuffer<uint16_t> a0, a1, a2, a3;  // BF16 activations
     DeviceBuffer<float> pscale;
+    double *s{nullptr};  // device scalars: (d, r), (d, A d)
+    // One sweep: r = b - A x; d = net(D^-1 r patches) scattered and zeroed on
+    // Dirichlet nodes; x += alpha d with alpha = (d, r) / (d, A d) computed on the
+    // device.  For SPD A that alpha minimises ||x* - x - alpha d||_A, so a poor
+    // correction can only be scaled down, never increase the error energy.
     int apply(const T *b, T *x) override {
         if (fallback && (chain || use_fallback)) SFEM_GB300_CHECK(fallback->apply(b, x));
         if (use_fallback) return 0;
         const ptrdiff_t n = op->rows();
         const ptrdiff_t P = nelements;
         SFEM_GB300_CHECK(r.resize(n));
+        SFEM_GB300_CHECK(d.resize(n));
+        SFEM_GB300_CHECK(Ad.resize(n));
         SFEM_GB300_CHECK(a0.resize(P * 125));
         SFEM_GB300_CHECK(a1.resize(P * 125 * channels));
         SFEM_GB300_CHECK(a2.resize(P * 125 * channels));
         SFEM_GB300_CHECK(a3.resize(P * 125));
         SFEM_GB300_CHECK(pscale.resize(P));
+        if (!s) s = blas.ctx->slots(2);
+        if (!s) return set_error("LearnedSmoother: out of scalar slots");
         void *sp = blas.ctx->sp();
         for (this->iterations_ = 0; this->iterations_ < sweeps; this->iterations_++) {
             blas.zeros(n, r.ptr);
@@ -384,8 +397,21 @@ public:
             SFEM_GB300_CHECK(sfem_gb300_patchconv_forward(P, 1, channels, a0.ptr, W[0], 1, a1.ptr, sp));
             SFEM_GB300_CHECK(sfem_gb300_patchconv_forward(P, channels, channels, a1.ptr, W[1], 1, a2.ptr, sp));
             SFEM_GB300_CHECK(sfem_gb300_patchconv_forward(P, channels, 1, a2.ptr, W[2], 0, a3.ptr, sp));
+            T *target = line_search ? d.ptr : x;
+            if (line_search) blas.zeros(n, d.ptr);
             SFEM_GB300_CHECK(sfem_gb300_scatter_patches(real_type_v<T>, P, elements, a3.ptr, pscale.ptr, count, omega,
-                                                        x, sp));
+                                                        target, sp));
+            if (!line_search) continue;
+            if (n_dirichlet > 0)
+                SFEM_GB300_CHECK(sfem_gb300_constraint_nodes_to_value(real_type_v<T>, n_dirichlet, dirichlet, 1, 0, 0.0,
+                                                                      d.ptr, sp));
+            blas.zeros(n, Ad.ptr);
+            SFEM_GB300_CHECK(op->apply(d.ptr, Ad.ptr));
+            SFEM_GB300_CHECK(blas.dot(n, d.ptr, r.ptr, &s[0]));
+            SFEM_GB300_CHECK(blas.dot(n, d.ptr, Ad.ptr, &s[1]));
+            // x += alpha d (r is scratch from here on)
+            SFEM_GB300_CHECK(sfem_gb300_cg_update_x_r(real_type_v<T>, n, &s[0], &s[1], d.ptr, Ad.ptr, x, r.ptr,
+                                                      blas.ctx->workspace, nullptr, sp));
         }
         return 0;
     }
@@ -532,7 +558,11 @@ public:
     std::vector<Level> levels;
     int max_it{1};
     int cycle_type{1};
-    double atol{1e-30};
+    // atol > 0 checks ||b - A x|| on the finest level after every pre-smoothing
+    // (one host read per cycle, as algebra/sfem_Multigrid.hpp does); the default 0
+    // skips the check, which is what a preconditioner (one cycle) wants and what
+    // keeps a cycle free of host synchronisation (graph capture)
+    double atol{0};
     double *s{nullptr};
     bool wrap_input{true};
     double norm_residual0{0}, norm_residual{0};

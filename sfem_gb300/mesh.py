@@ -62,6 +62,28 @@ HEX8_CORNERS = np.array(
 )
 
 
+def perturbed_macro_points(nx, ny, nz, box=((0.0, 1.0), (0.0, 1.0), (0.0, 1.0)), perturb=0.0, seed=0) -> np.ndarray:
+    """Macro node coordinates ``[3, nz+1, ny+1, nx+1]`` (float64) of a box: a uniform
+    grid whose interior nodes move by U(-perturb, perturb)*h per coordinate (seeded)."""
+    (x0, x1), (y0, y1), (z0, z1) = box
+    hx, hy, hz = (x1 - x0) / nx, (y1 - y0) / ny, (z1 - z0) / nz
+    X = x0 + hx * np.arange(nx + 1, dtype=np.float64)
+    Y = y0 + hy * np.arange(ny + 1, dtype=np.float64)
+    Z = z0 + hz * np.arange(nz + 1, dtype=np.float64)
+    MZ, MY, MX = np.meshgrid(Z, Y, X, indexing="ij")
+    macro = np.stack([MX, MY, MZ])
+    if perturb > 0:
+        rng = np.random.default_rng(seed)
+        noise = rng.uniform(-perturb, perturb, size=macro.shape)
+        noise[0] *= hx
+        noise[1] *= hy
+        noise[2] *= hz
+        interior = np.zeros(macro.shape[1:], dtype=bool)
+        interior[1:-1, 1:-1, 1:-1] = True
+        macro = macro + noise * interior[None]
+    return macro
+
+
 class SSMesh:
     """A box meshed by ``nx*ny*nz`` macro hex8 elements refined at level ``L``.
 
@@ -168,23 +190,7 @@ class SSMesh:
     # ------------------------------------------------------------------ geometry
     def _build_points(self):
         nx, ny, nz, L = self.nx, self.ny, self.nz, self.L
-        (x0, x1), (y0, y1), (z0, z1) = self.box
-        hx, hy, hz = (x1 - x0) / nx, (y1 - y0) / ny, (z1 - z0) / nz
-        # macro node coordinates (float64 while building)
-        X = x0 + hx * np.arange(nx + 1, dtype=np.float64)
-        Y = y0 + hy * np.arange(ny + 1, dtype=np.float64)
-        Z = z0 + hz * np.arange(nz + 1, dtype=np.float64)
-        MZ, MY, MX = np.meshgrid(Z, Y, X, indexing="ij")
-        macro = np.stack([MX, MY, MZ])  # [3, nz+1, ny+1, nx+1]
-        if self.perturb > 0:
-            rng = np.random.default_rng(self.seed)
-            noise = rng.uniform(-self.perturb, self.perturb, size=macro.shape)
-            noise[0] *= hx
-            noise[1] *= hy
-            noise[2] *= hz
-            interior = np.zeros(macro.shape[1:], dtype=bool)
-            interior[1:-1, 1:-1, 1:-1] = True
-            macro = macro + noise * interior[None]
+        macro = perturbed_macro_points(nx, ny, nz, self.box, self.perturb, self.seed)
         self.macro_points = macro.astype(np.float32)
         # fine nodes: trilinear interpolation inside the owning macro cell
         gx, gy, gz = self.grid_shape()
@@ -266,3 +272,81 @@ def upper_crs_graph(elements: np.ndarray, n_nodes: int):
     np.add.at(rowptr, r + 1, 1)
     rowptr = np.cumsum(rowptr).astype(np.int32)
     return rowptr, c.astype(np.int32)
+
+
+class CoarseHex8Level:
+    """A plain hex8 level made by coarsening a structured hex8 grid 2x in every direction.
+
+    The reference's sshex8 hierarchy ends at the hex8 macro mesh, whose solve it
+    hands to a coarse solver (``algebra/mg/sfem_GeometricMultigrid.cpp``).  On box
+    meshes the macro grid is itself structured, so geometric multigrid can go on
+    below it: the finer grid's nodes at even positions form the coarse grid and
+    every coarse element is a 2x2x2 block of finer elements.  Seen from the coarse
+    element, the finer nodes inside it are the micro grid of a level-2 sshex8
+    element, so the level-1 -> level-2 sshex8 transfer kernels serve unchanged.
+
+    ``fine_points``: float32 ``[3, gz, gy, gx]`` coordinates of the finer grid
+    nodes; ``fine_ids``: int ``[gz, gy, gx]`` their ids in the finer vector.
+    Coarse nodes are numbered lexicographically (x fastest), coarse elements
+    ``e = a + cx*(b + cy*c)``.
+    """
+
+    def __init__(self, fine_points: np.ndarray, fine_ids: np.ndarray):
+        gz, gy, gx = fine_ids.shape
+        if (gx - 1) % 2 or (gy - 1) % 2 or (gz - 1) % 2:
+            raise ValueError("a coarse hex8 level needs an even number of finer elements per direction")
+        cx, cy, cz = (gx - 1) // 2, (gy - 1) // 2, (gz - 1) // 2
+        self.shape = (cx, cy, cz)
+        self.n_elements = cx * cy * cz
+        self.n_nodes = (cx + 1) * (cy + 1) * (cz + 1)
+        self.ids = np.arange(self.n_nodes, dtype=np.int64).reshape(cz + 1, cy + 1, cx + 1)
+        self.points_grid = np.ascontiguousarray(fine_points[:, ::2, ::2, ::2]).astype(np.float32)
+        self.points = np.ascontiguousarray(self.points_grid.reshape(3, -1))
+        e = np.arange(self.n_elements, dtype=np.int64)
+        a, b, c = e % cx, (e // cx) % cy, e // (cx * cy)
+        self.hex8 = np.ascontiguousarray(np.stack(
+            [self.ids[c + dz, b + dy, a + dx] for dx, dy, dz in HEX8_CORNERS]).astype(np.int32))
+        # transfer view: coarse element = level-2 sshex8 element over the finer nodes
+        self.from_lidx = np.ascontiguousarray(np.stack(
+            [self.ids[c + zi, b + yi, a + xi] for zi in range(2) for yi in range(2) for xi in range(2)]).astype(np.int32))
+        self.to_lidx = np.ascontiguousarray(np.stack(
+            [fine_ids[2 * c + zi, 2 * b + yi, 2 * a + xi] for zi in range(3) for yi in range(3) for xi in range(3)]
+        ).astype(np.int32))
+        self.n_fine_nodes = int(fine_ids.size)
+        self.fine_count = np.bincount(self.to_lidx.reshape(-1), minlength=self.n_fine_nodes).astype(np.uint16)
+
+    def can_coarsen(self) -> bool:
+        return all(n % 2 == 0 and n >= 2 for n in self.shape)
+
+    def coarser(self) -> "CoarseHex8Level":
+        return CoarseHex8Level(self.points_grid, self.ids)
+
+    def boundary_nodes(self, face: str) -> np.ndarray:
+        axis, side = face[0], face[1]
+        idx = 0 if side == "0" else -1
+        sl = {"x": (slice(None), slice(None), idx), "y": (slice(None), idx, slice(None)),
+              "z": (idx, slice(None), slice(None))}[axis]
+        return np.unique(self.ids[sl].reshape(-1)).astype(np.int32)
+
+
+def macro_level_grid(mesh: SSMesh):
+    """(points ``[3, nz+1, ny+1, nx+1]``, ids ``[nz+1, ny+1, nx+1]``) of the level-1 (macro) grid of ``mesh``."""
+    L = mesh.L
+    K, J, I = np.meshgrid(np.arange(mesh.nz + 1), np.arange(mesh.ny + 1), np.arange(mesh.nx + 1), indexing="ij")
+    ids = mesh.node_id(I * L, J * L, K * L)
+    return mesh.macro_points, ids
+
+
+def macro_coarse_levels(mesh: SSMesh, min_nodes: int = 64) -> list:
+    """Coarse hex8 levels below the macro mesh, finest first, while every direction
+    halves evenly and the next level keeps at least ``min_nodes`` nodes."""
+    pts, ids = macro_level_grid(mesh)
+    out = []
+    shape = (mesh.nx, mesh.ny, mesh.nz)
+    while all(n % 2 == 0 and n >= 2 for n in shape):
+        nxt = CoarseHex8Level(pts, ids) if not out else out[-1].coarser()
+        if nxt.n_nodes < min_nodes:
+            break
+        out.append(nxt)
+        shape = nxt.shape
+    return out

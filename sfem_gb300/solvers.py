@@ -16,7 +16,7 @@ import ctypes as C
 import numpy as np
 
 from . import capi
-from .mesh import SSMesh
+from .mesh import CoarseHex8Level, SSMesh, macro_coarse_levels
 from .operators import Laplacian, SSMeshDevice
 
 c_double = C.c_double
@@ -84,9 +84,18 @@ def laplacian_op(ctx, space: SSMeshDevice, fff, dirichlet, dtype) -> Handle:
                    keep=(ctx, space, fff, dirichlet))
 
 
-def elasticity_op(ctx, space: SSMeshDevice, adj, det, mu, lam, dirichlet, dtype) -> Handle:
+def elasticity_op(ctx, space: SSMeshDevice, adj, det, mu, lam, dirichlet, dtype, tensor_cores=False) -> Handle:
+    """Linear-elasticity operator.  ``tensor_cores`` (float32 only) runs the element
+    contraction in BF16 on the tensor cores: fast but accurate to about 1e-2 of
+    |K||u| per entry, so it is meant for multigrid smoothers, not for a Krylov
+    operator."""
     E = space.n_elements
-    return _create(_lib().sfem_gb300_elasticity_op_create, ctx.ptr, c_int(rt_of(dtype)), c_int(space.element_type),
+    rt = rt_of(dtype)
+    if tensor_cores:
+        if rt != capi.FLOAT32:
+            raise ValueError("tensor-core elasticity contraction needs float32 vectors")
+        rt = capi.FLOAT32_BF16TC
+    return _create(_lib().sfem_gb300_elasticity_op_create, ctx.ptr, c_int(rt), c_int(space.element_type),
                    capi.i64(E), space.elements_ptrs.ptr, capi.i64(adj.shape[1]), capi.vp(adj), capi.vp(det),
                    c_double(mu), c_double(lam), capi.i64(space.n_nodes), capi.i64(dirichlet.numel()),
                    capi.vp(dirichlet), keep=(ctx, space, adj, det, dirichlet))
@@ -169,10 +178,52 @@ def iterative_refinement(ctx, op64, inner32, max_it=50, rtol=1e-10) -> Handle:
 # ---------------------------------------------------------------------------
 # hierarchy builders
 # ---------------------------------------------------------------------------
-class Hierarchy:
-    """Device data of every derefinement level of an :class:`SSMesh` (shared by both precisions)."""
+class CoarseSpaceDevice:
+    """A :class:`CoarseHex8Level` resident on the GPU: its hex8 operator data and the
+    transfer arrays to the next finer level (coarse element = level-2 sshex8 element)."""
 
-    def __init__(self, mesh: SSMesh, dirichlet_faces=("x0",), device="cuda:0", vec=1, coefficient=None):
+    is_macro_coarse = True
+
+    def __init__(self, lvl: CoarseHex8Level, device):
+        import torch
+
+        self.lvl = lvl
+        self.level = 1
+        self.element_type = capi.HEX8
+        self.n_elements = lvl.n_elements
+        self.n_nodes = lvl.n_nodes
+        self.device = torch.device(device)
+        t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(self.device)
+        self.elements = t(lvl.hex8)
+        self.elements_ptrs = capi.DevicePtrArray(self.elements)
+        self.corners_ptrs = self.elements_ptrs
+        self.points = t(lvl.points)
+        self.points_ptrs = capi.DevicePtrArray(self.points)
+        self.from_elements = t(lvl.from_lidx)
+        self.from_ptrs = capi.DevicePtrArray(self.from_elements)
+        self.to_elements = t(lvl.to_lidx)
+        self.to_ptrs = capi.DevicePtrArray(self.to_elements)
+        self.count = t(lvl.fine_count.view(np.int16))
+
+    def dirichlet_nodes(self, faces=("x0",)):
+        import torch
+
+        ids = np.unique(np.concatenate([self.lvl.boundary_nodes(f) for f in faces])).astype(np.int32)
+        return torch.from_numpy(ids).to(self.device)
+
+
+class Hierarchy:
+    """Device data of every level of a multigrid hierarchy on an :class:`SSMesh`
+    (shared by both precisions): the sshex8 derefinement levels and, with
+    ``coarsen_macro``, plain hex8 levels below the macro mesh
+    (:func:`sfem_gb300.mesh.macro_coarse_levels`).
+
+    Every space carries its own geometry (``fff``, ``adj``, ``det``); the sshex8
+    levels share the macro element metric.  A per-macro-element ``coefficient``
+    scales the metric; coarse hex8 levels take the mean over their 2x2x2 children."""
+
+    def __init__(self, mesh: SSMesh, dirichlet_faces=("x0",), device="cuda:0", vec=1, coefficient=None,
+                 coarsen_macro=False, min_coarse_nodes=64):
         import torch
 
         self.mesh = mesh
@@ -185,21 +236,55 @@ class Hierarchy:
             sp.lidx_ptrs = capi.DevicePtrArray(sp.lidx_elements)
             cnt = np.bincount(lid.reshape(-1), minlength=mesh.n_nodes(sp.level)).astype(np.uint16)
             sp.count = torch.from_numpy(cnt.view(np.int16)).to(self.device)
+        self.n_sshex8_levels = len(self.spaces)
+        self.coarse_levels = macro_coarse_levels(mesh, min_coarse_nodes) if coarsen_macro else []
+        self.spaces += [CoarseSpaceDevice(lvl, self.device) for lvl in self.coarse_levels]
         self.dirichlet = [sp.dirichlet_nodes(dirichlet_faces) if dirichlet_faces else
                           torch.zeros(0, dtype=torch.int32, device=self.device) for sp in self.spaces]
-        # geometry shared by all levels (one metric / adjugate per macro element)
+        # geometry: one metric / adjugate per macro element for all sshex8 levels
         lap = Laplacian(self.spaces[0], coefficient=coefficient).initialize()
         self.fff = lap.fff
-        E = mesh.n_elements
-        self.adj = torch.empty((9, E), dtype=torch.float32, device=self.device)
-        self.det = torch.empty(E, dtype=torch.float32, device=self.device)
-        sp = self.spaces[0]
+        self.adj, self.det = self._adjugate(self.spaces[0])
+        for sp in self.spaces[:self.n_sshex8_levels]:
+            sp.fff, sp.adj, sp.det = self.fff, self.adj, self.det
+        k = None if coefficient is None else np.asarray(coefficient, dtype=np.float64).reshape(mesh.nz, mesh.ny, mesh.nx)
+        for sp in self.spaces[self.n_sshex8_levels:]:
+            if k is not None:
+                cx, cy, cz = sp.lvl.shape
+                k = k.reshape(cz, 2, cy, 2, cx, 2).mean(axis=(1, 3, 5))
+            sp.fff = Laplacian(sp, coefficient=None if k is None else k.reshape(-1)).initialize().fff
+            sp.adj, sp.det = self._adjugate(sp)
+
+    def _adjugate(self, sp):
+        import torch
+
+        E = sp.n_elements
+        adj = torch.empty((9, E), dtype=torch.float32, device=self.device)
+        det = torch.empty(E, dtype=torch.float32, device=self.device)
         capi.check(capi.load().sfem_gb300_hex8_adjugate_fill(capi.i64(E), sp.corners_ptrs.ptr, sp.points_ptrs.ptr,
-                                                            capi.i64(E), capi.vp(self.adj), capi.vp(self.det), None),
+                                                            capi.i64(E), capi.vp(adj), capi.vp(det), None),
                    "adjugate_fill")
+        return adj, det
 
     def n_dofs(self, k=0):
         return self.vec * self.spaces[k].n_nodes
+
+
+def transfer_ops(ctx, H: Hierarchy, k: int, vec: int, dtype):
+    """(P, R) between level k+1 (coarse) and level k (fine) of ``H``."""
+    C, F = H.spaces[k + 1], H.spaces[k]
+    if getattr(C, "is_macro_coarse", False):
+        rt = c_int(rt_of(dtype))
+        dF, dC = H.dirichlet[k], H.dirichlet[k + 1]
+        P = _create(_lib().sfem_gb300_prolongation_op_create, ctx.ptr, rt, capi.i64(C.n_elements), c_int(1),
+                    C.from_ptrs.ptr, capi.i64(C.n_nodes), c_int(2), C.to_ptrs.ptr, capi.i64(F.n_nodes), c_int(vec),
+                    capi.i64(dF.numel()), capi.vp(dF), keep=(ctx, C, F, dF))
+        R = _create(_lib().sfem_gb300_restriction_op_create, ctx.ptr, rt, capi.i64(C.n_elements), c_int(2),
+                    C.to_ptrs.ptr, capi.vp(C.count), capi.i64(F.n_nodes), c_int(1), C.from_ptrs.ptr,
+                    capi.i64(C.n_nodes), c_int(vec), capi.i64(dC.numel()), capi.vp(dC), keep=(ctx, C, F, dC))
+        return P, R
+    return (prolongation_op(ctx, C, F, vec, H.dirichlet[k], dtype),
+            restriction_op(ctx, F, C, vec, H.dirichlet[k + 1], dtype))
 
 
 def build_poisson_mg(ctx, H: Hierarchy, dtype, smoother="chebyshev3", sweeps=2, coarse_rtol=1e-6, coarse_max_it=10000,
@@ -211,9 +296,9 @@ def build_poisson_mg(ctx, H: Hierarchy, dtype, smoother="chebyshev3", sweeps=2, 
     nlev = len(H.spaces)
     eigs = []
     for k, sp in enumerate(H.spaces):
-        op = laplacian_op(ctx, sp, H.fff, H.dirichlet[k], dtype)
+        op = laplacian_op(ctx, sp, sp.fff, H.dirichlet[k], dtype)
         ops.append(op)
-        lap = Laplacian(sp).set_fff(H.fff)
+        lap = Laplacian(sp).set_fff(sp.fff)
         diag = torch.zeros(sp.n_nodes, dtype=dtype, device=H.device)
         lap.hessian_diag(diag)
         diag[H.dirichlet[k].long()] = 1
@@ -233,8 +318,7 @@ def build_poisson_mg(ctx, H: Hierarchy, dtype, smoother="chebyshev3", sweeps=2, 
             smoothers.append(stationary(ctx, op, jac, jacobi_sweeps))
     mg = multigrid(ctx, dtype)
     for k in range(nlev):
-        P = prolongation_op(ctx, H.spaces[k + 1], H.spaces[k], 1, H.dirichlet[k], dtype) if k + 1 < nlev else None
-        R = restriction_op(ctx, H.spaces[k], H.spaces[k + 1], 1, H.dirichlet[k + 1], dtype) if k + 1 < nlev else None
+        P, R = transfer_ops(ctx, H, k, 1, dtype) if k + 1 < nlev else (None, None)
         mg_add_level(mg, ops[k], smoothers[k], P, R)
     mg.keep += [H]
     mg.eigs = eigs
@@ -249,7 +333,7 @@ def _elasticity_diag(H: Hierarchy, k, dtype, mu, lam):
     E = sp.n_elements
     d3 = torch.zeros(3 * sp.n_nodes, dtype=dtype, device=H.device)
     capi.check(capi.load().sfem_gb300_linear_elasticity_block_diag(
-        sp.element_type, capi.i64(E), sp.elements_ptrs.ptr, capi.i64(E), capi.vp(H.adj), capi.vp(H.det), c_double(mu),
+        sp.element_type, capi.i64(E), sp.elements_ptrs.ptr, capi.i64(E), capi.vp(sp.adj), capi.vp(sp.det), c_double(mu),
         c_double(lam), rt_of(dtype), capi.vp(d3), None, None), "elasticity diag")
     dn = H.dirichlet[k].long()
     for c in range(3):
@@ -258,15 +342,26 @@ def _elasticity_diag(H: Hierarchy, k, dtype, mu, lam):
 
 
 def build_elasticity_mg(ctx, H: Hierarchy, dtype, mu=1.0, lam=10.0, sweeps=2, coarse_rtol=1e-6,
-                        coarse_max_it=10000, eig_max=None, coarse_check_every=10, eigen_max_it=30, scale_eig_max=1.1):
+                        coarse_max_it=10000, eig_max=None, coarse_check_every=10, eigen_max_it=30, scale_eig_max=1.1,
+                        tensor_cores=False):
     """Geometric multigrid for linear elasticity (3 dofs / node) on every level of ``H``:
     Jacobi-scaled Chebyshev3 smoothing, nested vector transfer, Jacobi-PCG coarse solve
-    (cf. the vector branch of algebra/mg/sfem_GeometricMultigrid.cpp:89-144)."""
+    (cf. the vector branch of algebra/mg/sfem_GeometricMultigrid.cpp:89-144).
+
+    With ``tensor_cores`` (float32) the smoothers and the multigrid residuals of
+    the non-coarsest levels use the BF16 tensor-core contraction; the coarse
+    solve and the returned fine operator (for the outer Krylov method) stay
+    FP32 SIMT."""
     ops, smoothers = [], []
     nlev = len(H.spaces)
     eigs = []
+    fine_op = None
     for k, sp in enumerate(H.spaces):
-        op = elasticity_op(ctx, sp, H.adj, H.det, mu, lam, H.dirichlet[k], dtype)
+        op = elasticity_op(ctx, sp, sp.adj, sp.det, mu, lam, H.dirichlet[k], dtype)
+        if k == 0:
+            fine_op = op
+        if tensor_cores and k < nlev - 1:
+            op = elasticity_op(ctx, sp, sp.adj, sp.det, mu, lam, H.dirichlet[k], dtype, tensor_cores=True)
         ops.append(op)
         d3 = _elasticity_diag(H, k, dtype, mu, lam)
         if k == nlev - 1:
@@ -280,9 +375,8 @@ def build_elasticity_mg(ctx, H: Hierarchy, dtype, mu=1.0, lam=10.0, sweeps=2, co
             smoothers.append(ch)
     mg = multigrid(ctx, dtype)
     for k in range(nlev):
-        P = prolongation_op(ctx, H.spaces[k + 1], H.spaces[k], 3, H.dirichlet[k], dtype) if k + 1 < nlev else None
-        R = restriction_op(ctx, H.spaces[k], H.spaces[k + 1], 3, H.dirichlet[k + 1], dtype) if k + 1 < nlev else None
+        P, R = transfer_ops(ctx, H, k, 3, dtype) if k + 1 < nlev else (None, None)
         mg_add_level(mg, ops[k], smoothers[k], P, R)
-    mg.keep += [H]
+    mg.keep += [H, fine_op]
     mg.eigs = eigs
-    return mg, ops[0]
+    return mg, fine_op

@@ -69,8 +69,11 @@ def test_elasticity_reference_signature_and_fp32(cuda):
     u = np.random.default_rng(5).standard_normal(3 * n)
     ref = O.linear_elasticity_apply(L, el, adj, det, MU, LAM, u)
     lib = capi.load()
-    # FP32 vectors run the tensor-core kernel: BF16 element contraction (8-bit mantissa), FP32 accumulate
-    for dt, rt, tol in ((torch.float64, capi.FLOAT64, 1e-13), (torch.float32, capi.FLOAT32, 2e-2)):
+    # FLOAT32: FP32 SIMT contraction.  FLOAT32_BF16TC: tensor-core BF16 contraction with FP32
+    # accumulate; K and u rounded to 8-bit mantissas (2^-8 per product) against a row scale that
+    # underestimates sum |K_ij||u_j| several-fold: 2.8e-2 observed, bounded here by 6e-2.
+    for dt, rt, tol in ((torch.float64, capi.FLOAT64, 1e-13), (torch.float32, capi.FLOAT32, 2e-5),
+                        (torch.float32, capi.FLOAT32_BF16TC, 6e-2)):
         ud = torch.from_numpy(u).to(cuda).to(dt)
         yd = torch.zeros(3 * n, dtype=dt, device=cuda)
         es = ud.element_size()
@@ -80,7 +83,7 @@ def test_elasticity_reference_signature_and_fp32(cuda):
             capi.c_void(ud.data_ptr() + 2 * es), capi.i64(3), capi.vp(yd), capi.c_void(yd.data_ptr() + es),
             capi.c_void(yd.data_ptr() + 2 * es), None), "cu_affine_sshex8_linear_elasticity_apply")
         err = np.abs(yd.double().cpu().numpy() - ref) / _scale(L, el, adj, det, u)
-        assert err.max() < tol, (dt, err.max())
+        assert err.max() < tol, (dt, rt, err.max())
     # non-interleaved layouts are rejected with a message
     assert lib.cu_affine_sshex8_linear_elasticity_apply(
         L, capi.i64(m.n_elements), sp.elements_ptrs.ptr, capi.i64(m.n_elements), capi.vp(adj_d), capi.vp(det_d),

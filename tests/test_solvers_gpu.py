@@ -86,6 +86,41 @@ def test_sshex8_mg_pcg_fp64(cuda, smoother):
     _check_solution(apply, b, x.cpu().numpy(), x_star, rtol=1e-10, xtol=1e-7)
 
 
+@pytest.mark.parametrize("mixed", [False, True])
+def test_mg_with_macro_coarse_levels(cuda, mixed):
+    """Poisson MG-PCG whose hierarchy continues below the macro mesh with plain hex8
+    levels (2x coarsening of the macro grid): same solution, few iterations."""
+    import torch
+
+    L = 4
+    m = SSMesh(8, 8, 4, L, perturb=0.1, seed=6)
+    H = S.Hierarchy(m, dirichlet_faces=("x0",), device=cuda, coarsen_macro=True, min_coarse_nodes=8)
+    assert len(H.spaces) == 5 and H.spaces[-1].n_nodes == 18
+    fff = H.fff.cpu().numpy().T.copy()
+    dn = H.dirichlet[0].cpu().numpy()
+    apply, d = _oracle_poisson(m, L, fff, dn)
+    b = _rhs(m, L, dn, seed=8)
+    x_star, _ = OS.cg(apply, b, precond=lambda r: r / d, rtol=1e-14, max_it=20000)
+    ctx = S.context()
+    bd = torch.from_numpy(b).to(cuda)
+    x = torch.zeros_like(bd)
+    if not mixed:
+        mg, op = S.build_poisson_mg(ctx, H, torch.float64, sweeps=2)
+        solver = S.cg(ctx, op, mg, rtol=1e-11, max_it=100)
+        assert S.solve(solver, bd, x) == 0
+        it, _ = S.stats(solver)
+        assert it <= 20, it
+    else:
+        mg32, op32 = S.build_poisson_mg(ctx, H, torch.float32, sweeps=2)
+        inner = S.cg(ctx, op32, mg32, rtol=1e-4, max_it=30)
+        op64 = S.laplacian_op(ctx, H.spaces[0], H.fff, H.dirichlet[0], torch.float64)
+        solver = S.iterative_refinement(ctx, op64, inner, max_it=30, rtol=1e-11)
+        assert S.solve(solver, bd, x) == 0
+        it, _ = S.stats(solver)
+        assert it <= 6, it
+    _check_solution(apply, b, x.cpu().numpy(), x_star, rtol=1e-10, xtol=1e-7)
+
+
 def test_mixed_precision_iterative_refinement(cuda):
     import torch
 
@@ -159,13 +194,15 @@ def test_jacobi_scaled_chebyshev_against_oracle(cuda):
     assert np.abs(xd.cpu().numpy() - ref).max() <= 1e-9 * np.abs(ref).max()
 
 
-def test_elasticity_mg_pcg_and_mixed(cuda):
+@pytest.mark.parametrize("coarsen", [False, True])
+def test_elasticity_mg_pcg_and_mixed(cuda, coarsen):
     import torch
 
     L = 4
     mu, lam = 1.0, 10.0
     m = SSMesh(4, 2, 2, L, box=((0, 4), (0, 1), (0, 1)), perturb=0.05, seed=6)
-    H = S.Hierarchy(m, dirichlet_faces=("x0",), device=cuda, vec=3)
+    H = S.Hierarchy(m, dirichlet_faces=("x0",), device=cuda, vec=3, coarsen_macro=coarsen, min_coarse_nodes=8)
+    assert len(H.spaces) == (4 if coarsen else 3)
     adj = H.adj.cpu().numpy().T.copy()
     det = H.det.cpu().numpy().copy()
     el = m.elements(L)
@@ -192,15 +229,17 @@ def test_elasticity_mg_pcg_and_mixed(cuda):
     res = np.linalg.norm(b - apply(x.cpu().numpy())) / np.linalg.norm(b)
     assert res < 1e-10, res
     # mixed precision: FP64 refinement around FP32 MG-PCG
-    mg32, op32 = S.build_elasticity_mg(ctx, H, torch.float32, mu=mu, lam=lam, eig_max=mg.eigs)
-    inner = S.cg(ctx, op32, mg32, rtol=1e-4, max_it=40, residual_norm=True, flexible=True)
+    # (tensor_cores: BF16 tensor-core contraction in the smoothers, FP32 SIMT outer operator)
     op64 = S.elasticity_op(ctx, H.spaces[0], H.adj, H.det, mu, lam, H.dirichlet[0], torch.float64)
-    ir = S.iterative_refinement(ctx, op64, inner, max_it=30, rtol=1e-10)
-    x2 = torch.zeros_like(bd)
-    assert S.solve(ir, bd, x2) == 0
-    res2 = np.linalg.norm(b - apply(x2.cpu().numpy())) / np.linalg.norm(b)
-    assert res2 < 1e-10, res2
-    assert np.linalg.norm(x2.cpu().numpy() - x.cpu().numpy()) < 1e-8 * np.linalg.norm(x.cpu().numpy())
+    for tc in (False, True):
+        mg32, op32 = S.build_elasticity_mg(ctx, H, torch.float32, mu=mu, lam=lam, eig_max=mg.eigs, tensor_cores=tc)
+        inner = S.cg(ctx, op32, mg32, rtol=1e-4, max_it=40, residual_norm=True, flexible=True)
+        ir = S.iterative_refinement(ctx, op64, inner, max_it=30, rtol=1e-10)
+        x2 = torch.zeros_like(bd)
+        assert S.solve(ir, bd, x2) == 0, tc
+        res2 = np.linalg.norm(b - apply(x2.cpu().numpy())) / np.linalg.norm(b)
+        assert res2 < 1e-10, (tc, res2)
+        assert np.linalg.norm(x2.cpu().numpy() - x.cpu().numpy()) < 1e-8 * np.linalg.norm(x.cpu().numpy()), tc
 
 
 def test_cg_options_true_residual_and_check_every(cuda):
