@@ -1,16 +1,21 @@
-"""Benchmark: sshex8 Laplacian matrix-free apply at L=4 on a 48^3 macro mesh.
+"""Benchmark: sshex8 Laplacian matrix-free apply at L=4 on a 48^3 macro mesh, and solves.
 
-Workload (one "step"): one FP64 apply y = A x of the affine sshex8 Laplacian
+Workload (one "step"): one FP32 apply y += A x of the affine sshex8 Laplacian
 (level 4, 48x48x48 macro hex8 elements of the unit cube, interior macro nodes
 perturbed by U(-0.1,0.1) h, seed 0): 110,592 macro elements, 7,189,057 nodes.
+FP32 is the precision the mixed-precision solvers apply the operator in.
 ``value`` = GDoF/s with x, y and the mesh resident in HBM; the L2 cache is
 flushed (a 512 MiB write) before every timed step and kernels are timed with
 CUDA events on the launching stream.  ``e2e`` = the same apply through the C
 ABI with host buffers: pinned host x -> device, zero y, apply, y -> pinned host.
+``fp64_apply`` = the FP64 apply (the precision of the oracle parity, 1e-13).
+``solve`` = time to a true FP64 relative residual, plain FP64 multigrid-CG
+against the mixed-precision solvers (Poisson 48^3 L=4, elasticity cantilever
+64x16x16 L=4), and the batched serving run (256 uneven problems).
 
 ``--impl reference`` times the reference CPU implementation of the same apply
-(the oracle port of affine_sshex8_laplacian_stencil_apply_fff, OpenMP, all host
-threads) on the same mesh.
+in the same precision (the oracle port of affine_sshex8_laplacian_stencil_apply_fff
+in the reference's float32 number configuration, OpenMP, all host threads).
 """
 
 from __future__ import annotations
@@ -31,6 +36,11 @@ sys.path.insert(0, str(ROOT))
 
 NX = 48
 LEVEL = 4
+METRIC = "sshex8 Laplacian apply GDoF/s (FP32, L=4, 48^3 macro); solve times to FP64 residual in 'solve'"
+NOMINAL_FP64_TFLOPS = 1.25  # GB300 nominal FP64 (no measured figure in the peaks file)
+# dram__bytes_read.sum + dram__bytes_write.sum of one launch of the default float
+# kernel on this workload (ncu, cold cache); see the profile summary of that kernel
+TRAFFIC_BYTES_PER_LAUNCH = None
 SEED = 0
 PERTURB = 0.1
 
@@ -44,6 +54,8 @@ def parse():
     ap.add_argument("--nx", type=int, default=NX)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-solve", action="store_true")
+    ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--batch-problems", type=int, default=256)
     return ap.parse_args()
 
 
@@ -132,23 +144,34 @@ def measured_peak_hbm():
     return 6800.0, "fallback"
 
 
-def cpu_baseline(m, reps=3):
-    """Time the CPU oracle apply (port of the reference CPU kernel) on the host cores."""
+def cpu_apply_time(m, dtype, reps=3):
+    """Seconds per apply of the CPU oracle port (OpenMP, all host threads) on the full mesh."""
     import oracle as O
 
     el = m.elements(LEVEL)
     fff = O.fff_fill(el[m.macro_corner_lidx(LEVEL)], m.points)
     x = np.random.default_rng(1).standard_normal(m.n_nodes())
+    if dtype == "f32":
+        x = x.astype(np.float32)
+        fn = lambda out: O.sshex8_laplacian_apply_f32(LEVEL, el, fff, x, out=out)
+    else:
+        fn = lambda out: O.sshex8_laplacian_apply(LEVEL, el, fff, x, out=out)
     y = np.zeros_like(x)
-    O.sshex8_laplacian_apply(LEVEL, el, fff, x, out=y)  # warm-up
+    fn(y)  # warm-up
     t = time.perf_counter()
     for _ in range(reps):
         y[:] = 0
-        O.sshex8_laplacian_apply(LEVEL, el, fff, x, out=y)
-    dt = (time.perf_counter() - t) / reps
+        fn(y)
+    return (time.perf_counter() - t) / reps
+
+
+def cpu_baseline(m, reps=3):
+    """The CPU oracle apply (port of the reference CPU kernel, float32 configuration) on the host cores."""
+    dt = cpu_apply_time(m, "f32", reps)
     return {"value": m.n_nodes() / dt / 1e9, "unit": "GDoF/s", "cores": os.cpu_count(), "kind": "port",
-            "sample": f"{reps} FP64 applies of the full 48^3 L=4 mesh (oracle port of "
-                      f"affine_sshex8_laplacian_stencil_apply_fff, OpenMP)", "seconds_per_apply": dt}
+            "sample": f"{reps} FP32 applies of the full 48^3 L=4 mesh (oracle port of "
+                      f"affine_sshex8_laplacian_stencil_apply_fff, float32 number configuration, OpenMP)",
+            "seconds_per_apply": dt}
 
 
 def run_reference(args):
@@ -160,27 +183,28 @@ def run_reference(args):
 
     el = m.elements(LEVEL)
     fff = O.fff_fill(el[m.macro_corner_lidx(LEVEL)], m.points)
-    x = np.random.default_rng(1).standard_normal(m.n_nodes())
+    x = np.random.default_rng(1).standard_normal(m.n_nodes()).astype(np.float32)
     y = np.zeros_like(x)
     for _ in range(max(1, args.warmup)):
-        O.sshex8_laplacian_apply(LEVEL, el, fff, x, out=y)
+        O.sshex8_laplacian_apply_f32(LEVEL, el, fff, x, out=y)
+    steps = max(1, min(args.steps, 20))  # bounded CPU sample
     t = time.perf_counter()
-    for _ in range(args.steps):
+    for _ in range(steps):
         y[:] = 0
-        O.sshex8_laplacian_apply(LEVEL, el, fff, x, out=y)
-    dt = (time.perf_counter() - t) / args.steps
+        O.sshex8_laplacian_apply_f32(LEVEL, el, fff, x, out=y)
+    dt = (time.perf_counter() - t) / steps
     v = m.n_nodes() / dt / 1e9
     line = {
-        "impl": "reference", "metric": "sshex8 Laplacian apply GDoF/s (FP64, L=4, 48^3 macro)", "value": v,
-        "unit": "GDoF/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "impl": "reference", "metric": METRIC, "value": v,
+        "unit": "GDoF/s", "n_gpus": world, "steps": steps, "warmup": args.warmup, "ms_per_step": dt * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": "sshex8_laplacian_apply_L4_48cube", "nodes": m.n_nodes(), "macro_elements": m.n_elements},
         "cpu_baseline": {"value": v, "unit": "GDoF/s", "cores": os.cpu_count(), "kind": "port",
-                         "sample": f"{args.steps} timed FP64 applies of the full mesh (oracle port, OpenMP)"},
+                         "sample": f"{steps} timed FP32 applies of the full mesh (oracle port of the reference "
+                                   f"CPU kernel in its float32 configuration, OpenMP)"},
         "e2e": {"value": v, "unit": "GDoF/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
-
 
 
 def time_apply(op, x, y, steps, warmup, flush, stream):
@@ -203,11 +227,24 @@ def time_apply(op, x, y, steps, warmup, flush, stream):
     return float(np.mean([a.elapsed_time(b) for a, b in zip(starts, ends)])) / 1e3
 
 
+def _timed_solve(S, solver, b, x):
+    import torch
+
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    rc = S.solve(solver, b, x)
+    torch.cuda.synchronize()
+    return rc, time.perf_counter() - t0
+
+
 def measure_solves(m, dev, rtol=1e-10):
-    """Time to ||b - A x|| / ||b|| <= rtol (FP64, true residual) on the same problem:
-    plain FP64 MG-PCG (Chebyshev3 V(2,2), Jacobi-PCG coarse) vs FP64 iterative
-    refinement around an FP32 MG-PCG (same hierarchy in float).  The hierarchy is
-    the sshex8 levels followed by hex8 levels coarsening the macro grid."""
+    """Time to ||b - A x|| / ||b|| <= rtol (FP64, true residual) on the same problem and
+    hierarchy (sshex8 levels 4, 2, 1, then hex8 levels coarsening the macro grid;
+    Chebyshev3 V(2,2); Jacobi-PCG 1e-6 on the coarsest level):
+      plain: FP64 flexible CG + FP64 multigrid;
+      mixed_ir: FP64 iterative refinement around FP32 CG + FP32 multigrid;
+      mixed_precond: FP64 flexible CG preconditioned by the FP32 multigrid
+      (FP64 only for the residual, dot products and solution update)."""
     import torch
 
     from sfem_gb300 import solvers as S
@@ -219,49 +256,44 @@ def measure_solves(m, dev, rtol=1e-10):
     b[H.dirichlet[0].long()] = 0
     ctx = S.context()
     op64 = S.laplacian_op(ctx, H.spaces[0], H.fff, H.dirichlet[0], torch.float64)
-    out = {"levels_nodes": [sp.n_nodes for sp in H.spaces]}
+    out = {"levels_nodes": [sp.n_nodes for sp in H.spaces], "rtol": rtol,
+           "smoother": "Jacobi-scaled Chebyshev3 V(2,2)", "coarse": "Jacobi-PCG 1e-6 on the coarsest hex8 level"}
 
     def true_rel(x):
         r = torch.zeros_like(b)
         S.apply(op64, x, r)
         return float(torch.linalg.vector_norm(b - r) / torch.linalg.vector_norm(b))
 
-    # plain FP64
     t0 = time.perf_counter()
     mg64, _ = S.build_poisson_mg(ctx, H, torch.float64, smoother="chebyshev3", sweeps=2)
     torch.cuda.synchronize()
     setup64 = time.perf_counter() - t0
     cg64 = S.cg(ctx, op64, mg64, rtol=rtol, max_it=500, residual_norm=True, flexible=True)
     x = torch.zeros_like(b)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    rc = S.solve(cg64, b, x)
-    torch.cuda.synchronize()
-    t64 = time.perf_counter() - t0
-    it64, _ = S.stats(cg64)
-    out["plain_fp64_mg_pcg"] = {"seconds": t64, "iterations": it64, "true_rel_residual": true_rel(x), "rc": rc,
-                                "setup_seconds": setup64, "smoother": "Chebyshev3 V(2,2)",
-                                "coarse": "Jacobi-PCG 1e-6 on the coarsest hex8 level"}
+    rc, t64 = _timed_solve(S, cg64, b, x)
+    out["plain_fp64_mg_pcg"] = {"seconds": t64, "iterations": S.stats(cg64)[0], "true_rel_residual": true_rel(x),
+                                "rc": rc, "setup_seconds": setup64}
     x64 = x.clone()
-    # mixed: FP64 refinement around FP32 MG-PCG (eigenvalues reused from the FP64 setup)
+    xn = float(torch.linalg.vector_norm(x64))
     t0 = time.perf_counter()
     mg32, op32 = S.build_poisson_mg(ctx, H, torch.float32, smoother="chebyshev3", sweeps=2, eig_max=mg64.eigs)
-    inner = S.cg(ctx, op32, mg32, rtol=1e-4, max_it=30, residual_norm=True, flexible=True)
-    ir = S.iterative_refinement(ctx, op64, inner, max_it=30, rtol=rtol)
     torch.cuda.synchronize()
     setup32 = time.perf_counter() - t0
+    inner = S.cg(ctx, op32, mg32, rtol=1e-4, max_it=30, residual_norm=True, flexible=True)
+    ir = S.iterative_refinement(ctx, op64, inner, max_it=30, rtol=rtol)
     x = torch.zeros_like(b)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    rc = S.solve(ir, b, x)
-    torch.cuda.synchronize()
-    t32 = time.perf_counter() - t0
-    itir, rel = S.stats(ir)
-    xn = float(torch.linalg.vector_norm(x64))
-    out["mixed_fp32_mg_pcg_fp64_ir"] = {
-        "seconds": t32, "outer_iterations": itir, "true_rel_residual": true_rel(x), "rc": rc, "setup_seconds": setup32,
-        "solution_rel_diff_vs_plain_fp64": float(torch.linalg.vector_norm(x - x64)) / xn}
-    out["speedup_mixed_vs_plain"] = t64 / t32 if t32 > 0 else None
+    rc, tir = _timed_solve(S, ir, b, x)
+    out["mixed_ir"] = {"seconds": tir, "outer_iterations": S.stats(ir)[0], "true_rel_residual": true_rel(x),
+                       "rc": rc, "setup_seconds": setup32,
+                       "solution_rel_diff_vs_plain_fp64": float(torch.linalg.vector_norm(x - x64)) / xn}
+    pc = S.mixed_precond(ctx, mg32)
+    cgm = S.cg(ctx, op64, pc, rtol=rtol, max_it=500, residual_norm=True, flexible=True)
+    x = torch.zeros_like(b)
+    rc, tpc = _timed_solve(S, cgm, b, x)
+    out["mixed_precond"] = {"seconds": tpc, "iterations": S.stats(cgm)[0], "true_rel_residual": true_rel(x),
+                            "rc": rc, "solution_rel_diff_vs_plain_fp64": float(torch.linalg.vector_norm(x - x64)) / xn}
+    out["speedup_mixed_ir_vs_plain"] = t64 / tir
+    out["speedup_mixed_precond_vs_plain"] = t64 / tpc
     return out
 
 
@@ -283,12 +315,13 @@ def lumped_body_force(m, det):
     return b
 
 
-def measure_elasticity_solves(dev, nx=64, ny=16, nz=16, rtol=1e-9, mu=1.0, lam=10.0):
-    """Cantilever 4x1x1, macro 64x16x16 at L=4, clamped at x=0, body force (0,0,-1):
-    plain FP64 MG-PCG vs FP64 refinement around FP32 (tensor-core BF16 element
-    contraction) MG-PCG, time to a true FP64 residual of rtol.  rtol is 1e-9 here:
-    the conditioning of the clamped 4:1 cantilever puts the attainable FP64 true
-    residual of either method near 5e-10."""
+def measure_elasticity_solves(dev, nx=64, ny=16, nz=16, rtol=1e-9, mu=1.0, lam=10.0, coarse_max_it=50):
+    """Cantilever 4x1x1, macro 64x16x16 at L=4, clamped at x=0, lumped body force (0,0,-1):
+    plain FP64 flexible CG + FP64 multigrid against the same CG preconditioned by the
+    FP32 multigrid, time to a true FP64 residual of rtol.  Same hierarchy and coarse
+    solve (Jacobi-PCG, at most coarse_max_it iterations) for both.  rtol is 1e-9:
+    |A||x| / |b| of the clamped 4:1 cantilever puts the FP64 evaluation floor of the
+    residual itself near 5e-10, which both methods reach and neither can go below."""
     import torch
 
     from sfem_gb300 import solvers as S
@@ -307,35 +340,63 @@ def measure_elasticity_solves(dev, nx=64, ny=16, nz=16, rtol=1e-9, mu=1.0, lam=1
         S.apply(op64, x, r)
         return float(torch.linalg.vector_norm(b - r) / torch.linalg.vector_norm(b))
 
-    out = {"dofs": 3 * m.n_nodes(), "macro_elements": m.n_elements, "levels_nodes": [sp.n_nodes for sp in H.spaces]}
-    mg64, _ = S.build_elasticity_mg(ctx, H, torch.float64, mu=mu, lam=lam, coarse_max_it=300)
+    out = {"dofs": 3 * m.n_nodes(), "macro_elements": m.n_elements, "levels_nodes": [sp.n_nodes for sp in H.spaces],
+           "rtol": rtol, "coarse": f"Jacobi-PCG 1e-6, <= {coarse_max_it} iterations"}
+    mg64, _ = S.build_elasticity_mg(ctx, H, torch.float64, mu=mu, lam=lam, coarse_max_it=coarse_max_it)
     cg64 = S.cg(ctx, op64, mg64, rtol=rtol, max_it=500, residual_norm=True, flexible=True)
     x = torch.zeros_like(b)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    rc = S.solve(cg64, b, x)
-    torch.cuda.synchronize()
-    t64 = time.perf_counter() - t0
-    it64, _ = S.stats(cg64)
-    out["plain_fp64_mg_pcg"] = {"seconds": t64, "iterations": it64, "true_rel_residual": true_rel(x), "rc": rc,
-                                "rtol": rtol}
+    rc, t64 = _timed_solve(S, cg64, b, x)
+    out["plain_fp64_mg_pcg"] = {"seconds": t64, "iterations": S.stats(cg64)[0], "true_rel_residual": true_rel(x),
+                                "rc": rc}
     x64 = x.clone()
-    mg32, op32 = S.build_elasticity_mg(ctx, H, torch.float32, mu=mu, lam=lam, eig_max=mg64.eigs, coarse_max_it=300,
-                                       tensor_cores=True)
-    inner = S.cg(ctx, op32, mg32, rtol=1e-4, max_it=40, residual_norm=True, flexible=True)
-    ir = S.iterative_refinement(ctx, op64, inner, max_it=30, rtol=rtol)
+    mg32, _ = S.build_elasticity_mg(ctx, H, torch.float32, mu=mu, lam=lam, eig_max=mg64.eigs,
+                                    coarse_max_it=coarse_max_it)
+    pc = S.mixed_precond(ctx, mg32)
+    cgm = S.cg(ctx, op64, pc, rtol=rtol, max_it=500, residual_norm=True, flexible=True)
     x = torch.zeros_like(b)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    rc = S.solve(ir, b, x)
-    torch.cuda.synchronize()
-    t32 = time.perf_counter() - t0
-    itir, _ = S.stats(ir)
-    out["mixed_fp32_mg_pcg_fp64_ir"] = {
-        "seconds": t32, "outer_iterations": itir, "true_rel_residual": true_rel(x), "rc": rc,
+    rc, tpc = _timed_solve(S, cgm, b, x)
+    out["mixed_precond"] = {
+        "seconds": tpc, "iterations": S.stats(cgm)[0], "true_rel_residual": true_rel(x), "rc": rc,
         "solution_rel_diff_vs_plain_fp64": float(torch.linalg.vector_norm(x - x64) / torch.linalg.vector_norm(x64))}
-    out["speedup_mixed_vs_plain"] = t64 / t32 if t32 > 0 else None
+    out["speedup_mixed_precond_vs_plain"] = t64 / tpc
     return out
+
+
+def measure_batch(dev, count=256, seed=0):
+    """Batched serving: ``count`` uneven Poisson / elasticity problems (cube edge 8..32
+    macro elements, L in {2, 3, 4}, perturbation 0.1 h, N(0,1) rhs, seeded) solved
+    together to FP64 relative residual 1e-10 (batched FP64 flexible CG, FP32 multigrid
+    per group, chunks of 5 iterations replayed as one CUDA graph); launch shape from
+    the autotuner.  Latency of a problem = time from the start of the batch solve
+    until the host saw it converged."""
+    import torch
+
+    from sfem_gb300.batch import BatchSolver, draw_problems
+
+    t0 = time.perf_counter()
+    probs = draw_problems(count, seed=seed)
+    bs = BatchSolver(probs, device=dev)
+    b = bs.rhs()
+    torch.cuda.synchronize()
+    setup = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    table = bs.autotune(b)
+    tune = time.perf_counter() - t0
+    x = torch.zeros_like(b)
+    rc, lat, its, sec = bs.solve(b, x)
+    tr = bs.true_residuals(b, x)
+    kinds = [p.kind for p in bs.problems]
+    return {
+        "problems": count, "dofs": int(bs.n), "groups": len(bs.groups), "rc": int(rc), "seconds": sec,
+        "solves_per_s": count / sec,
+        "latency_p50_s": float(np.percentile(lat, 50)), "latency_p99_s": float(np.percentile(lat, 99)),
+        "iterations_max": int(its.max()), "max_true_rel_residual": float(tr.max()),
+        "all_converged": bool(rc == 0 and (tr <= 1.5e-10).all()),
+        "poisson": kinds.count("poisson"), "elasticity": kinds.count("elasticity"),
+        "setup_seconds": setup, "autotune_seconds": tune,
+        "autotune": [{"chunk": c[0], "threads": c[1], "ctas_per_sm": c[2], "ms_per_chunk": t} for c, t in table],
+        "tuned": list(bs.tuned),
+    }
 
 
 def run_ours(args):
@@ -357,17 +418,15 @@ def run_ours(args):
     sp = SSMeshDevice(m, LEVEL, device=dev)
     op = Laplacian(sp).initialize()
     N, E = m.n_nodes(), m.n_elements
-    x = torch.randn(N, dtype=torch.float64, device=dev, generator=torch.Generator(device=dev).manual_seed(1))
-    y = torch.zeros(N, dtype=torch.float64, device=dev)
+    x64 = torch.randn(N, dtype=torch.float64, device=dev, generator=torch.Generator(device=dev).manual_seed(1))
+    x = x64.float()
+    y = torch.zeros(N, dtype=torch.float32, device=dev)
     flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device=dev)
     stream = torch.cuda.current_stream(dev)
 
-    def step():
+    for _ in range(max(3, args.warmup)):
         y.zero_()
         op.apply(x, y)
-
-    for _ in range(max(3, args.warmup)):
-        step()
     torch.cuda.synchronize()
     # device-timed region: events around each apply (the y.zero_ is the
     # accumulate-interface's caller-side reset and is excluded), L2 flushed before each step
@@ -386,14 +445,14 @@ def run_ours(args):
             ends[k].record(stream)
         torch.cuda.synchronize()
         wall = time.perf_counter() - wall0
-    times = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    times = [s_.elapsed_time(e_) for s_, e_ in zip(starts, ends)]
     value, t_kernel = replica_aggregate(float(np.mean(times)) / 1e3, N, world, dev)
     value /= 1e9
 
     # end-to-end through the C ABI with host buffers
-    xh = torch.empty(N, dtype=torch.float64, pin_memory=True)
+    xh = torch.empty(N, dtype=torch.float32, pin_memory=True)
     xh.copy_(x.cpu())
-    yh = torch.empty(N, dtype=torch.float64, pin_memory=True)
+    yh = torch.empty(N, dtype=torch.float32, pin_memory=True)
     xd = torch.empty_like(x)
     e2e_steps = max(3, args.steps // 5)
     for _ in range(2):
@@ -415,35 +474,38 @@ def run_ours(args):
     t_e2e = e0.elapsed_time(e1) / 1e3 / e2e_steps
     e2e_value = world * N / t_e2e / 1e9
 
-    # FP32 apply on the same mesh
-    x32 = x.float()
-    y32 = torch.zeros(N, dtype=torch.float32, device=dev)
-    t32 = time_apply(op, x32, y32, args.steps, args.warmup, flush, stream)
+    # FP64 apply on the same mesh (oracle-parity precision)
+    y64 = torch.zeros(N, dtype=torch.float64, device=dev)
+    t64 = time_apply(op, x64, y64, args.steps, args.warmup, flush, stream)
+    del flush
 
     solve = None
     if not args.no_solve:
         solve = {"poisson_sshex8_L4_48cube": measure_solves(m, dev),
                  "elasticity_sshex8_L4_64x16x16": measure_elasticity_solves(dev)}
+        if not args.no_batch:
+            solve["batched_serving"] = measure_batch(dev, args.batch_problems)
 
     peak, peak_kind = measured_peak_hbm()
-    alg_bytes = 2 * 8 * N + (4 * (LEVEL + 1) ** 3 + 24) * E
-    alg_bytes32 = 2 * 4 * N + (4 * (LEVEL + 1) ** 3 + 24) * E
+    alg_bytes = 2 * 4 * N + (4 * (LEVEL + 1) ** 3 + 24) * E
+    alg_bytes64 = 2 * 8 * N + (4 * (LEVEL + 1) ** 3 + 24) * E
     achieved = alg_bytes / t_kernel / 1e9
     fp64_flops = 2 * 64 * (LEVEL ** 3) * E  # element-matrix form, 128 flop per micro element
     line = {
-        "metric": "sshex8 Laplacian apply GDoF/s (FP64, L=4, 48^3 macro); time-to-1e-10 solve in 'solve'",
+        "metric": METRIC,
         "value": value, "unit": "GDoF/s", "n_gpus": world, "steps": args.steps, "warmup": max(3, args.warmup),
-        "ms_per_step": t_kernel * 1e3, "higher_is_better": True, "scaling": "weak" if world > 1 else "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "ms_per_step": t_kernel * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": "sshex8_laplacian_apply_L4_48cube", "nodes": N, "macro_elements": E, "level": LEVEL,
                    "perturb": PERTURB, "seed": SEED, "l2": "flushed (512 MiB write) before every timed step",
                    "parallelism": f"replicas{world}" if world > 1 else "single"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": None, "peak_kind": peak_kind, "algorithmic_bytes": alg_bytes,
-                     "fp64_gflops_achieved": fp64_flops / t_kernel / 1e9},
-        "e2e": {"value": e2e_value, "unit": "GDoF/s", "h2d_bytes_per_step": 8 * N, "d2h_bytes_per_step": 8 * N},
-        "fp32_apply": {"gdofs": N / t32 / 1e9, "ms": t32 * 1e3, "achieved_gbs": alg_bytes32 / t32 / 1e9,
-                       "frac_hbm": alg_bytes32 / t32 / 1e9 / peak, "algorithmic_bytes": alg_bytes32},
+                     "traffic": TRAFFIC_BYTES_PER_LAUNCH, "peak_kind": peak_kind, "algorithmic_bytes": alg_bytes},
+        "e2e": {"value": e2e_value, "unit": "GDoF/s", "h2d_bytes_per_step": 4 * N, "d2h_bytes_per_step": 4 * N},
+        "fp64_apply": {"gdofs": N / t64 / 1e9, "ms": t64 * 1e3, "achieved_gbs": alg_bytes64 / t64 / 1e9,
+                       "fp64_tflops": fp64_flops / t64 / 1e12,
+                       "fp64_frac_of_nominal": fp64_flops / t64 / 1e12 / NOMINAL_FP64_TFLOPS,
+                       "bound": "fp64 pipe (FMA)"},
         "solve": solve,
         "gpu_launches": args.steps,
         "clocks": clk.summary(),
@@ -452,6 +514,7 @@ def run_ours(args):
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         try:
             line["cpu_baseline"] = cpu_baseline(m)
+            line["fp64_apply"]["cpu_port_gdofs"] = N / cpu_apply_time(m, "f64") / 1e9
         except Exception as exc:
             line["cpu_baseline"] = {"value": None, "error": str(exc)}
     if rank == 0:

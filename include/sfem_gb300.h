@@ -80,6 +80,12 @@ int cu_laplacian_apply(int element_type, ptrdiff_t nelements, sfem_gb300_idx_t *
 int cu_laplacian_diag(int element_type, ptrdiff_t nelements, sfem_gb300_idx_t **elements, ptrdiff_t fff_stride,
                       const void *fff, int real_type_diag, void *diag, void *stream);
 
+/* Kernel used for float sshex8 applies (process-wide tuning knob, no reference
+ * counterpart): 0 shared-memory staged tile (default), 1 warp per element,
+ * 2 thread per element in registers, 3 cp.async staged tile with two threads per
+ * element (even L; other levels use the default).  Returns the previous value. */
+int sfem_gb300_set_laplacian_kernel(int variant);
+
 /* ------------------------------------------------------- linear elasticity */
 
 /* out += K u for the affine hex8 / sshex8 linear-elasticity operator with
@@ -136,6 +142,13 @@ int sfem_gb300_sshex8_restrict(ptrdiff_t nelements, int from_level, sfem_gb300_i
                                const uint16_t *from_element_to_node_incidence_count, int to_level,
                                sfem_gb300_idx_t **to_elements, int vec_size, int real_type, const void *from, void *to,
                                void *stream);
+
+/* y[vec*i + c] = sum_k weights[k] x[vec*colidx[k] + c] over the CSR row i (overwrites y):
+ * nested interpolation between plain hex8 grids below the macro mesh, or its transpose.
+ * No reference counterpart (the reference's hierarchy ends at the macro mesh). */
+int sfem_gb300_crs_transfer(int real_type, ptrdiff_t nrows, int vec_size, const sfem_gb300_idx_t *rowptr,
+                            const sfem_gb300_idx_t *colidx, const double *weights, const void *x, void *y,
+                            void *stream);
 
 /* count[node] += number of macro elements containing the node (count zeroed by the caller).
  * Replaces sshex8_element_node_incidence_count (operators/sshex8/sshex8_interpolate.cpp:239). */
@@ -247,6 +260,10 @@ int sfem_gb300_random_uniform(int real_type, ptrdiff_t n, unsigned long long see
 /* Precision conversion dst = (dst_type) src, and y += alpha (double) x for float x. */
 int sfem_gb300_convert(ptrdiff_t n, int src_type, const void *src, int dst_type, void *dst, void *stream);
 int sfem_gb300_axpy_f32_to_f64(ptrdiff_t n, double alpha, const float *x, double *y, void *stream);
+/* Precision bridge with a device-resident scale (no host round trip):
+ * dst = (float)(src / *nrm) (0 if *nrm == 0);  y += *nrm * (double) x. */
+int sfem_gb300_scaled_to_f32(ptrdiff_t n, const double *nrm, const double *src, float *dst, void *stream);
+int sfem_gb300_scaled_axpy_f32_to_f64(ptrdiff_t n, const double *nrm, const float *x, double *y, void *stream);
 
 /* ------------------------------------------------------- learned smoother */
 /* No reference counterpart.  A patch is the 5x5x5 node grid of one level-4
@@ -372,10 +389,27 @@ int sfem_gb300_mg_set_pre_smoother(void *mg, int level, void *smoother);
 int sfem_gb300_mg_set_post_smoother(void *mg, int level, void *smoother);
 /* Copy of the finest-level iterate after each coarse-grid correction into x_cc (device, n entries). */
 int sfem_gb300_mg_set_harvest(void *mg, void *x_cc);
+/* Graph mode (no reference counterpart): the V-cycles of each (b, x) pair are
+ * captured once into a CUDA graph and replayed.  Requires host-synchronisation-free
+ * levels (Chebyshev3 / Jacobi smoothers, a dense coarse solver). */
+int sfem_gb300_mg_set_graph(void *mg, int enable);
+/* Dense direct solver for a small (<= 1536 unknowns) SPD coarsest level: the matrix is
+ * built from the operator, inverted once by Cholesky, applied as x += A^-1 b. */
+int sfem_gb300_dense_solver_create(void *context, void *op, void **solver);
+/* Operator y = P x (CSR, see sfem_gb300_crs_transfer), output Dirichlet dofs zeroed. */
+int sfem_gb300_crs_transfer_op_create(void *context, int real_type, ptrdiff_t nrows, ptrdiff_t ncols,
+                                      const sfem_gb300_idx_t *rowptr, const sfem_gb300_idx_t *colidx,
+                                      const double *weights, int vec_size, ptrdiff_t n_dirichlet,
+                                      const sfem_gb300_idx_t *dirichlet, void **op);
 
 /* FP64 iterative refinement around a float inner solver (no reference counterpart):
  * r = b - A x in double, d = inner(r/|r|) in float, x += |r| d, until |r| <= rtol |b|. */
 int sfem_gb300_ir_create(void *context, void *op64, void *inner32, int max_it, double rtol, void **solver);
+/* Float preconditioner for a double Krylov method (no reference counterpart):
+ * z = |r| inner(r / |r|) with the norm kept on the device, so FP64 carries the
+ * Krylov recurrence, true residual and solution while the preconditioner (e.g. a
+ * float multigrid V-cycle) runs in FP32. */
+int sfem_gb300_mixed_precond_create(void *context, void *inner32, void **op64);
 int sfem_gb300_solver_apply(void *solver, const void *b, void *x);
 int sfem_gb300_solver_stats(void *solver, int *iterations, double *last_relative);
 
@@ -407,18 +441,22 @@ int sfem_gb300_batch_chebyshev3_eig_max(void *solver, double *eig_max_out /* hos
  * ||r_p|| <= rtol ||r0_p||.  Never synchronises with the host. */
 int sfem_gb300_batch_cg_create(void *context, void *layout, void *op, void *precond, int iterations, double rtol,
                                int flexible, void **solver);
-/* FP64 iterative refinement over the batch around a float batched inner solver; with
- * use_graph one outer step is captured into a CUDA graph and replayed. */
-int sfem_gb300_batch_ir_create(void *context, void *layout, void *op64, void *inner32, int max_outer, double rtol,
-                               int use_graph, void **solver);
-/* Solves to ||b_p - A x_p|| <= rtol ||b_p|| for every p.  Host outputs (each may be
- * NULL): seconds from start until problem p was seen converged, the outer step at
- * which it converged, its last relative residual; total seconds. */
-int sfem_gb300_batch_ir_solve(void *solver, const double *b, double *x, double *latency_s,
-                              int *outer_steps_per_problem, double *final_rel, double *seconds);
-/* Mean milliseconds of `reps` replays of the captured outer step, starting from x
- * (x is modified): the autotuner's measurement. */
-int sfem_gb300_batch_ir_time_step(void *solver, const double *b, double *x, int reps, double *ms);
+/* z += ||r_p|| M32(r_p / ||r_p||): a float preconditioner (the grouped float
+ * multigrid) under a double batched Krylov method, norms kept on the device. */
+int sfem_gb300_batch_bridge_create(void *context, void *layout, void *inner32, void **op64);
+/* Host driver of a double batched CG: start, then chunks of check_every iterations
+ * captured into one CUDA graph (use_graph) and replayed until every problem has
+ * ||r_p|| <= rtol ||b_p|| (the CG's rtol; zero initial guess). */
+int sfem_gb300_batch_solve_create(void *context, void *layout, void *cg64, int check_every, int max_it,
+                                  int use_graph, void **solver);
+int sfem_gb300_batch_solve_set_launch(void *solver, int check_every);
+/* Host outputs (each may be NULL): seconds from start until problem p was seen
+ * converged, the iteration count at that check, total seconds. */
+int sfem_gb300_batch_solve_run(void *solver, const double *b, double *x, double *latency_s,
+                               int *iterations_per_problem, double *seconds);
+/* Mean milliseconds of `reps` replays of the captured chunk starting from x (x is
+ * modified): the autotuner's measurement. */
+int sfem_gb300_batch_solve_time_chunk(void *solver, const double *b, double *x, int reps, double *ms);
 
 #ifdef __cplusplus
 }

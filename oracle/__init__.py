@@ -134,6 +134,18 @@ def sshex8_laplacian_apply(L, elements, fff_aos, u, out=None, use_ref=False):
     return out
 
 
+def sshex8_laplacian_apply_f32(L, elements, fff_aos, u, out=None):
+    """values += A u in float32 arithmetic (the reference's float32 number configuration)."""
+    E = elements.shape[1]
+    u = np.ascontiguousarray(u, dtype=np.float32)
+    out = np.zeros_like(u) if out is None else out
+    assert out.dtype == np.float32
+    ea = PtrArray(elements.astype(np.int32))
+    f = _f32(fff_aos)
+    lib().or_sshex8_laplacian_apply_f32(c_int(L), c_ptrdiff(E), ea.p, _ptr(f), _ptr(u), _ptr(out))
+    return out
+
+
 def hex8_laplacian_apply(elements, fff_aos, u, out=None, use_ref=False):
     E = elements.shape[1]
     u = _f64(u)

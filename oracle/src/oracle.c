@@ -239,6 +239,55 @@ int or_sshex8_laplacian_apply(int L, ptrdiff_t nelements, idx_t **elements, cons
     return 0;
 }
 
+static inline void atomic_add_f(float *p, float v) {
+#pragma omp atomic update
+    *p += v;
+}
+
+/* The same apply in the reference's float32 number configuration
+ * (SFEM_REAL_TYPE=float32, cmake/SFEMNumbers.cmake:5-10: real, scalar and
+ * accumulator all float): element matrix, gathers, products and sums in float. */
+int or_sshex8_laplacian_apply_f32(int L, ptrdiff_t nelements, idx_t **elements, const jacobian_t *fff, const float *u,
+                                  float *values) {
+    const int nxe = (L + 1) * (L + 1) * (L + 1);
+#pragma omp parallel
+    {
+        float *eu = (float *)malloc(nxe * sizeof(float));
+        float *ev = (float *)malloc(nxe * sizeof(float));
+        idx_t *idx = (idx_t *)malloc(nxe * sizeof(idx_t));
+#pragma omp for
+        for (ptrdiff_t e = 0; e < nelements; e++) {
+            double sub[6], Ad[64];
+            float A[64];
+            const float h = 1.0f / (float)L;
+            for (int d = 0; d < 6; d++) sub[d] = (double)(fff[e * 6 + d] * h);
+            or_hex8_laplacian_matrix(sub, Ad);
+            for (int k = 0; k < 64; k++) A[k] = (float)Ad[k];
+            for (int v = 0; v < nxe; v++) {
+                idx[v] = elements[v][e];
+                eu[v] = u[idx[v]];
+                ev[v] = 0;
+            }
+            for (int zi = 0; zi < L; zi++)
+                for (int yi = 0; yi < L; yi++)
+                    for (int xi = 0; xi < L; xi++) {
+                        int lev[8];
+                        sshex8_micro_nodes(L, xi, yi, zi, lev);
+                        for (int i = 0; i < 8; i++) {
+                            float acc = 0;
+                            for (int j = 0; j < 8; j++) acc += A[i * 8 + j] * eu[lev[j]];
+                            ev[lev[i]] += acc;
+                        }
+                    }
+            for (int v = 0; v < nxe; v++) atomic_add_f(&values[idx[v]], ev[v]);
+        }
+        free(eu);
+        free(ev);
+        free(idx);
+    }
+    return 0;
+}
+
 /* hex8_laplacian_apply_opt (operators/hex8/hex8_laplacian.cpp:309-345);
  * elements in hex8 corner order. */
 int or_hex8_laplacian_apply(ptrdiff_t nelements, idx_t **elements, const jacobian_t *fff, const double *u,

@@ -8,14 +8,15 @@ kernels over all its problems.  Vectors of all groups are concatenated again
 into one batch vector (problem p owns a contiguous dof range), on which the
 batched kernels of ``csrc/batched.cu`` run the per-problem Krylov algebra:
 
-    FP64 iterative refinement (per-problem residual check, rtol on ||r_p|| / ||b_p||)
-      -> FP32 flexible CG, fixed iterations, per-problem scalars and masks
-         -> block-diagonal preconditioner: one multigrid V(s, s) per group with
-            per-problem Chebyshev3 bounds and a batched Jacobi-PCG coarse solve.
+    FP64 flexible CG over the batch (per-problem scalars and masks, stop on
+    ||r_p|| <= rtol ||b_p||), preconditioned through a per-problem precision bridge
+      -> block-diagonal FP32 preconditioner: one multigrid V(s, s) per group
+         (sshex8 levels, then hex8 levels coarsening each macro grid) with
+         per-problem Chebyshev3 bounds and a batched Jacobi-PCG coarse solve.
 
-One outer step is captured into a CUDA graph and replayed; the autotuner picks
-the work-list chunk and CTA shape of the batched vector kernels by timing the
-captured step.
+Chunks of CG iterations are captured into a CUDA graph and replayed; the
+autotuner picks the work-list chunk and CTA shape of the batched vector kernels
+by timing the captured chunk.
 """
 
 from __future__ import annotations
@@ -27,7 +28,7 @@ import numpy as np
 
 from . import capi
 from . import solvers as S
-from .mesh import SSMesh, derefinement_levels, perturbed_macro_points
+from .mesh import CoarseHex8Level, SSMesh, derefinement_levels, perturbed_macro_points
 from .operators import Laplacian
 
 c_double = C.c_double
@@ -70,10 +71,21 @@ def _mesh(n, L) -> SSMesh:
     return _MESHES[key]
 
 
+def coarse_depth(n: int, min_nodes: int = 27) -> int:
+    """Number of 2x coarsenings of an n^3 macro grid (odd edges keep a thin last
+    element) while an edge has >= 2 elements and the next grid >= min_nodes nodes."""
+    d = 0
+    while n >= 2 and ((n + 1) // 2 + 1) ** 3 >= min_nodes:
+        n = (n + 1) // 2
+        d += 1
+    return d
+
+
 class _LevelSpace:
     """One level of a group: concatenated connectivity of its problems on the device."""
 
-    def __init__(self, device, level, element_type, elements, lidx, count, n_nodes, n_elements):
+    def __init__(self, device, level, element_type, elements, n_nodes, n_elements, lidx=None, count=None, P=None,
+                 R=None):
         import torch
 
         t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(device)
@@ -84,16 +96,34 @@ class _LevelSpace:
         self.device = device
         self.elements = t(elements)
         self.elements_ptrs = capi.DevicePtrArray(self.elements)
-        self.corners_ptrs = None
-        self.lidx_elements = t(lidx)
-        self.lidx_ptrs = capi.DevicePtrArray(self.lidx_elements)
-        self.count = t(count.view(np.int16))
+        self.is_macro_coarse = P is not None
+        if lidx is not None:
+            self.lidx_elements = t(lidx)
+            self.lidx_ptrs = capi.DevicePtrArray(self.lidx_elements)
+            self.count = t(count.view(np.int16))
+        if self.is_macro_coarse:
+            self.P = tuple(t(a) for a in P)
+            self.R = tuple(t(a) for a in R)
+
+
+def _block_diag_csr(blocks, row_offs, col_offs):
+    """Concatenate per-problem CSR triples block-diagonally."""
+    ptr, idx, val = [np.zeros(1, dtype=np.int64)], [], []
+    nnz = 0
+    for (rp, ci, w), co in zip(blocks, col_offs):
+        ptr.append(rp[1:].astype(np.int64) + nnz)
+        idx.append(ci.astype(np.int64) + co)
+        val.append(w)
+        nnz += int(rp[-1])
+    return (np.concatenate(ptr).astype(np.int32), np.concatenate(idx).astype(np.int32), np.concatenate(val))
 
 
 class BatchGroup:
-    """All problems of one (kind, level): concatenated hierarchy, geometry, rhs."""
+    """All problems of one (kind, level, coarse depth): concatenated hierarchy, geometry, rhs.
+    Transfers of the hex8 levels below the macro grids are block-diagonal CSR
+    interpolations (one block per problem)."""
 
-    def __init__(self, kind, level, problems, device, perturb=0.1, dirichlet_face="x0"):
+    def __init__(self, kind, level, problems, device, perturb=0.1, dirichlet_face="x0", depth=0):
         import torch
 
         self.kind, self.L, self.problems = kind, level, list(problems)
@@ -115,41 +145,74 @@ class BatchGroup:
             E = sum(m.n_elements for m in meshes)
             et = capi.HEX8 if l == 1 else capi.SSHEX8(l)
             self.spaces.append(_LevelSpace(self.device, l, et, np.concatenate(els, axis=1).astype(np.int32),
-                                           np.concatenate(lids, axis=1).astype(np.int32), np.concatenate(cnts),
-                                           int(offs[-1]), E))
+                                           int(offs[-1]), E, lidx=np.concatenate(lids, axis=1).astype(np.int32),
+                                           count=np.concatenate(cnts)))
             self.dirichlet.append(torch.from_numpy(np.concatenate(dns).astype(np.int32)).to(self.device))
-        self.n_nodes = int(self.node_offsets[0][-1])
-        self.n_dofs = self.vec * self.n_nodes
-        self._geometry(meshes, perturb)
-
-    def _geometry(self, meshes, perturb):
-        """Per-problem perturbed macro grids -> FFF (Laplacian) or adjugate (elasticity)."""
-        import torch
-
-        pts, corners = [], []
-        off = 0
+        self.n_sshex8 = len(self.spaces)
+        # per-problem macro grids and their coarse hex8 chains
+        grids = []
         for p, m in zip(self.problems, meshes):
             macro = perturbed_macro_points(p.n, p.n, p.n, perturb=perturb, seed=p.seed).astype(np.float32)
             K, J, I = np.meshgrid(np.arange(p.n + 1), np.arange(p.n + 1), np.arange(p.n + 1), indexing="ij")
-            ids = m.node_id(I * m.L, J * m.L, K * m.L).reshape(-1)  # level-1 ids
+            grids.append((macro, m.node_id(I * m.L, J * m.L, K * m.L)))
+        chains = []
+        for macro, ids in grids:
+            chain = []
+            for _ in range(depth):
+                chain.append(CoarseHex8Level(macro, ids) if not chain else chain[-1].coarser())
+            chains.append(chain)
+        for c in range(depth):
+            lv = [ch[c] for ch in chains]
+            offs = np.cumsum([0] + [x.n_nodes for x in lv])
+            fine_offs = self.node_offsets[-1]
+            els = np.concatenate([x.hex8 + o for x, o in zip(lv, offs[:-1])], axis=1).astype(np.int32)
+            P = _block_diag_csr([x.P for x in lv], fine_offs[:-1], offs[:-1])
+            R = _block_diag_csr([x.R for x in lv], offs[:-1], fine_offs[:-1])
+            sp = _LevelSpace(self.device, 1, capi.HEX8, els, int(offs[-1]), els.shape[1], P=P, R=R)
+            sp.points_host = np.concatenate([x.points for x in lv], axis=1)
+            self.spaces.append(sp)
+            self.dirichlet.append(torch.from_numpy(np.concatenate(
+                [x.boundary_nodes(dirichlet_face) + o for x, o in zip(lv, offs[:-1])]).astype(np.int32)).to(self.device))
+            self.node_offsets.append(offs)
+        self.n_nodes = int(self.node_offsets[0][-1])
+        self.n_dofs = self.vec * self.n_nodes
+        self._geometry(meshes, grids)
+
+    def _fill(self, corners, points):
+        import torch
+
+        dev = self.device
+        pts = torch.from_numpy(np.ascontiguousarray(points)).to(dev)
+        cor = torch.from_numpy(np.ascontiguousarray(corners)).to(dev)
+        pp, cp = capi.DevicePtrArray(pts), capi.DevicePtrArray(cor)
+        E = cor.shape[1]
+        lib = capi.load()
+        fff = torch.empty((6, E), dtype=torch.float32, device=dev)
+        capi.check(lib.sfem_gb300_hex8_fff_fill(capi.i64(E), cp.ptr, pp.ptr, capi.i64(E), capi.vp(fff), None),
+                   "fff_fill")
+        adj = torch.empty((9, E), dtype=torch.float32, device=dev)
+        det = torch.empty(E, dtype=torch.float32, device=dev)
+        capi.check(lib.sfem_gb300_hex8_adjugate_fill(capi.i64(E), cp.ptr, pp.ptr, capi.i64(E), capi.vp(adj),
+                                                     capi.vp(det), None), "adjugate_fill")
+        torch.cuda.synchronize(dev)
+        return fff, adj, det
+
+    def _geometry(self, meshes, grids):
+        """Per-problem perturbed macro grids -> FFF / adjugate of every level."""
+        pts, corners = [], []
+        off = 0
+        for (macro, ids), m in zip(grids, meshes):
             P1 = np.empty((3, m.n_nodes(1)), dtype=np.float32)
-            P1[:, ids] = macro.reshape(3, -1)
+            P1[:, ids.reshape(-1)] = macro.reshape(3, -1)
             pts.append(P1)
             corners.append(m.hex8_elements() + off)
             off += m.n_nodes(1)
-        dev = self.device
-        self._points = torch.from_numpy(np.ascontiguousarray(np.concatenate(pts, axis=1))).to(dev)
-        self._corners = torch.from_numpy(np.ascontiguousarray(np.concatenate(corners, axis=1))).to(dev)
-        pp, cp = capi.DevicePtrArray(self._points), capi.DevicePtrArray(self._corners)
-        E = self._corners.shape[1]
-        lib = capi.load()
-        self.fff = torch.empty((6, E), dtype=torch.float32, device=dev)
-        capi.check(lib.sfem_gb300_hex8_fff_fill(capi.i64(E), cp.ptr, pp.ptr, capi.i64(E), capi.vp(self.fff), None),
-                   "fff_fill")
-        self.adj = torch.empty((9, E), dtype=torch.float32, device=dev)
-        self.det = torch.empty(E, dtype=torch.float32, device=dev)
-        capi.check(lib.sfem_gb300_hex8_adjugate_fill(capi.i64(E), cp.ptr, pp.ptr, capi.i64(E), capi.vp(self.adj),
-                                                     capi.vp(self.det), None), "adjugate_fill")
+        fff, adj, det = self._fill(np.concatenate(corners, axis=1), np.concatenate(pts, axis=1))
+        self.fff, self.adj, self.det = fff, adj, det
+        for sp in self.spaces[:self.n_sshex8]:
+            sp.fff, sp.adj, sp.det = fff, adj, det
+        for sp in self.spaces[self.n_sshex8:]:
+            sp.fff, sp.adj, sp.det = self._fill(sp.elements.cpu().numpy(), sp.points_host)
 
     def problem_dof_offsets(self, k=0):
         return self.vec * self.node_offsets[k]
@@ -169,8 +232,8 @@ class BatchGroup:
     def op(self, ctx, k, dtype, tensor_cores=False):
         sp = self.spaces[k]
         if self.kind == "poisson":
-            return S.laplacian_op(ctx, sp, self.fff, self.dirichlet[k], dtype)
-        return S.elasticity_op(ctx, sp, self.adj, self.det, 1.0, 10.0, self.dirichlet[k], dtype,
+            return S.laplacian_op(ctx, sp, sp.fff, self.dirichlet[k], dtype)
+        return S.elasticity_op(ctx, sp, sp.adj, sp.det, 1.0, 10.0, self.dirichlet[k], dtype,
                                tensor_cores=tensor_cores)
 
     def diag(self, k, dtype):
@@ -179,12 +242,12 @@ class BatchGroup:
         sp = self.spaces[k]
         d = torch.zeros(self.vec * sp.n_nodes, dtype=dtype, device=self.device)
         if self.kind == "poisson":
-            Laplacian(sp).set_fff(self.fff).hessian_diag(d)
+            Laplacian(sp).set_fff(sp.fff).hessian_diag(d)
         else:
             E = sp.n_elements
             capi.check(capi.load().sfem_gb300_linear_elasticity_block_diag(
-                sp.element_type, capi.i64(E), sp.elements_ptrs.ptr, capi.i64(E), capi.vp(self.adj),
-                capi.vp(self.det), c_double(1.0), c_double(10.0), S.rt_of(dtype), capi.vp(d), None, None), "diag")
+                sp.element_type, capi.i64(E), sp.elements_ptrs.ptr, capi.i64(E), capi.vp(sp.adj),
+                capi.vp(sp.det), c_double(1.0), c_double(10.0), S.rt_of(dtype), capi.vp(d), None, None), "diag")
         dn = self.dirichlet[k].long()
         for c in range(self.vec):
             d[self.vec * dn + c] = 1
@@ -192,6 +255,10 @@ class BatchGroup:
 
     def transfer(self, ctx, k, dtype):
         C_, F = self.spaces[k + 1], self.spaces[k]
+        if C_.is_macro_coarse:
+            P = S.crs_transfer_op(ctx, C_.P, F.n_nodes, C_.n_nodes, self.vec, self.dirichlet[k], dtype)
+            R = S.crs_transfer_op(ctx, C_.R, C_.n_nodes, F.n_nodes, self.vec, self.dirichlet[k + 1], dtype)
+            return P, R
         P = S.prolongation_op(ctx, C_, F, self.vec, self.dirichlet[k], dtype)
         R = S.restriction_op(ctx, F, C_, self.vec, self.dirichlet[k + 1], dtype)
         return P, R
@@ -206,26 +273,25 @@ def _layout(ctx, dof_offsets, chunk=4096) -> S.Handle:
 class BatchSolver:
     """Mixed-precision batched solver over a list of :class:`ProblemSpec`."""
 
-    def __init__(self, problems, device="cuda:0", sweeps=2, coarse_iterations=30, inner_iterations=8,
-                 inner_rtol=1e-4, rtol=1e-10, max_outer=30, tensor_cores=True, use_graph=True, eigen_max_it=20,
-                 perturb=0.1):
+    def __init__(self, problems, device="cuda:0", sweeps=2, coarse_iterations=20, rtol=1e-10, max_it=300,
+                 check_every=5, tensor_cores=False, use_graph=True, eigen_max_it=20, perturb=0.1,
+                 coarse_min_nodes=27):
         import torch
 
         self.device = torch.device(device)
         self.ctx = S.context()
         ctx = self.ctx
         lib = capi.load()
-        keys = sorted({(p.kind, p.level) for p in problems})
-        self.groups = [BatchGroup(kd, L, [p for p in problems if (p.kind, p.level) == (kd, L)], self.device,
-                                  perturb=perturb) for kd, L in keys]
+        keyf = lambda p: (p.kind, p.level, coarse_depth(p.n, coarse_min_nodes))
+        keys = sorted({keyf(p) for p in problems})
+        self.groups = [BatchGroup(kd, L, [p for p in problems if keyf(p) == (kd, L, dp)], self.device,
+                                  perturb=perturb, depth=dp) for kd, L, dp in keys]
         self.problems = [p for g in self.groups for p in g.problems]  # batch order
         self.layouts = []
         ops64, ops32, mgs, goffs = [], [], [], [0]
-        self.keep = []
         for g in self.groups:
-            nlev = len(g.levels)
+            nlev = len(g.spaces)
             mg = S.multigrid(ctx, torch.float32)
-            lev_ops, smoothers = [], []
             for k in range(nlev):
                 lay = _layout(ctx, g.problem_dof_offsets(k))
                 self.layouts.append(lay)
@@ -243,9 +309,8 @@ class BatchSolver:
                                    c_int(eigen_max_it), C.c_ulonglong(S.RANDOM_SEED), keep=(ctx, lay, sop, inv))
                 P, R = g.transfer(ctx, k, torch.float32) if k + 1 < nlev else (None, None)
                 S.mg_add_level(mg, op, sm, P, R)
-                lev_ops.append(op)
             mgs.append(mg)
-            ops32.append(lev_ops[0])
+            ops32.append(g.op(ctx, 0, torch.float32))
             ops64.append(g.op(ctx, 0, torch.float64))
             goffs.append(goffs[-1] + g.n_dofs)
         self.group_offsets = np.asarray(goffs, dtype=np.int64)
@@ -258,14 +323,14 @@ class BatchSolver:
         self.layout = _layout(ctx, self.dof_offsets)
         self.layouts.append(self.layout)
         self.op64 = self._grouped(torch.float64, ops64)
-        self.op32 = self._grouped(torch.float32, ops32)
-        self.precond = self._grouped(torch.float32, mgs)
-        self.inner = S._create(lib.sfem_gb300_batch_cg_create, ctx.ptr, self.layout.ptr, self.op32.ptr,
-                               self.precond.ptr, c_int(inner_iterations), c_double(inner_rtol), c_int(1),
-                               keep=(ctx, self.layout, self.op32, self.precond))
-        self.ir = S._create(lib.sfem_gb300_batch_ir_create, ctx.ptr, self.layout.ptr, self.op64.ptr, self.inner.ptr,
-                            c_int(max_outer), c_double(rtol), c_int(int(use_graph)),
-                            keep=(ctx, self.layout, self.op64, self.inner))
+        self.precond32 = self._grouped(torch.float32, mgs)
+        self.bridge = S._create(lib.sfem_gb300_batch_bridge_create, ctx.ptr, self.layout.ptr, self.precond32.ptr,
+                                keep=(ctx, self.layout, self.precond32))
+        self.cg = S._create(lib.sfem_gb300_batch_cg_create, ctx.ptr, self.layout.ptr, self.op64.ptr, self.bridge.ptr,
+                            c_int(1), c_double(rtol), c_int(1), keep=(ctx, self.layout, self.op64, self.bridge))
+        self.solver = S._create(lib.sfem_gb300_batch_solve_create, ctx.ptr, self.layout.ptr, self.cg.ptr,
+                                c_int(check_every), c_int(max_it), c_int(int(use_graph)), keep=(ctx, self.layout, self.cg))
+        self.check_every = check_every
         self.tuned = None
 
     def _grouped(self, dtype, ops):
@@ -287,43 +352,43 @@ class BatchSolver:
         for lay in self.layouts:
             capi.check(capi.load().sfem_gb300_batch_layout_set_launch(lay.ptr, c_int(chunk), c_int(threads),
                                                                        c_int(ctas_per_sm)), "set_launch")
+        capi.check(capi.load().sfem_gb300_batch_solve_set_launch(self.solver.ptr, c_int(self.check_every)),
+                   "solve_set_launch")
 
-    def time_step(self, b, x, reps=2) -> float:
+    def time_chunk(self, b, x, reps=1) -> float:
         ms = c_double(0)
-        capi.check(capi.load().sfem_gb300_batch_ir_time_step(self.ir.ptr, capi.vp(b), capi.vp(x), c_int(reps),
-                                                             C.byref(ms)), "batch_ir_time_step")
+        capi.check(capi.load().sfem_gb300_batch_solve_time_chunk(self.solver.ptr, capi.vp(b), capi.vp(x), c_int(reps),
+                                                                 C.byref(ms)), "batch_solve_time_chunk")
         return ms.value
 
-    def autotune(self, b, candidates=None, reps=2):
-        """Pick (chunk, threads, CTAs per SM) of the batched vector kernels by timing
-        the captured outer step on a scratch iterate; returns the timing table."""
+    def autotune(self, b, candidates=None, reps=1):
+        """Pick (chunk, threads, CTAs per SM) of the batched vector kernels by timing a
+        captured chunk of CG iterations on a scratch iterate; returns the timing table."""
         import torch
 
         if candidates is None:
-            candidates = [(2048, 256, 8), (4096, 256, 8), (8192, 256, 8), (8192, 512, 4), (16384, 512, 4),
-                          (4096, 128, 16)]
+            candidates = [(2048, 256, 8), (4096, 256, 8), (8192, 512, 4), (4096, 128, 16)]
         table = []
         for cand in candidates:
             self.set_launch(*cand)
             xs = torch.zeros_like(b)
-            table.append((cand, self.time_step(b, xs, reps)))
+            table.append((cand, self.time_chunk(b, xs, reps)))
         best = min(table, key=lambda t: t[1])[0]
         self.set_launch(*best)
         self.tuned = best
         return table
 
     def solve(self, b, x):
-        """Solve every problem to ||b_p - A_p x_p|| <= rtol ||b_p|| (FP64).  Returns
-        (rc, per-problem latency s, per-problem outer steps, per-problem final rel, seconds)."""
+        """Solve every problem to ||b_p - A_p x_p|| <= rtol ||b_p|| (FP64, zero start).
+        Returns (rc, per-problem latency s, per-problem iterations, seconds)."""
         P = self.n_problems
         lat = np.zeros(P)
-        steps = np.zeros(P, dtype=np.int32)
-        rel = np.zeros(P)
+        its = np.zeros(P, dtype=np.int32)
         sec = c_double(0)
-        rc = capi.load().sfem_gb300_batch_ir_solve(self.ir.ptr, capi.vp(b), capi.vp(x),
-                                                   lat.ctypes.data_as(C.c_void_p), steps.ctypes.data_as(C.c_void_p),
-                                                   rel.ctypes.data_as(C.c_void_p), C.byref(sec))
-        return rc, lat, steps, rel, sec.value
+        rc = capi.load().sfem_gb300_batch_solve_run(self.solver.ptr, capi.vp(b), capi.vp(x),
+                                                    lat.ctypes.data_as(C.c_void_p), its.ctypes.data_as(C.c_void_p),
+                                                    C.byref(sec))
+        return rc, lat, its, sec.value
 
     def true_residuals(self, b, x):
         """||b_p - A_p x_p|| / ||b_p|| per problem with the FP64 operators (device)."""

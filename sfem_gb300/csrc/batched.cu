@@ -13,14 +13,17 @@
 //    its partials in list order: results are deterministic;
 //  * Krylov scalars (alpha, beta, residual norms, convergence masks) live in
 //    device arrays of length P, so no iteration reads anything on the host;
-//  * an outer FP64 refinement step (residual, inner FP32 batched flexible CG
-//    preconditioned by per-group multigrid, update) is captured once into a CUDA
-//    graph and replayed; the host reads the active mask once per step;
-//  * the work-list chunk and the CTA shape of the vector kernels are picked by
-//    an autotuner that times the captured step for each candidate.
+//  * the outer solver is a batched FP64 flexible CG whose preconditioner runs the
+//    per-group FP32 multigrid on per-problem normalised residuals (FP64 only for
+//    the residual recurrence, dot products and solution update); chunks of
+//    iterations are captured once into a CUDA graph and replayed, the host reads
+//    the per-problem active mask once per chunk;
+//  * the work-list chunk, the CTA shape of the vector kernels and the chunk length
+//    are picked by an autotuner that times the captured chunk for each candidate.
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <functional>
 #include <memory>
 #include <vector>
 
@@ -189,31 +192,6 @@ __global__ void bcg_check_kernel(int P, const double *__restrict__ rr, const dou
     if (!(rr[p] > tol2 * rr0[p])) active[p] = 0;
 }
 
-// Outer refinement check on the FP64 residual: a problem stays active while
-// ||r_p|| > rtol ||b_p||; then inv_p = 1 / ||r_p|| and scale_p = ||r_p||,
-// both 0 for inactive problems.  Counts the active problems.
-__global__ void bir_check_kernel(int P, const double *__restrict__ rr, const double *__restrict__ bb, double rtol,
-                                 const int *__restrict__ step, int *__restrict__ active, int *__restrict__ done_step,
-                                 double *__restrict__ rel, double *__restrict__ inv, double *__restrict__ scale,
-                                 int *__restrict__ n_active) {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= P) return;
-    const double rn = sqrt(rr[p]), bn = sqrt(bb[p]);
-    if (active[p]) {
-        rel[p] = bn > 0 ? rn / bn : 0.0;
-        if (!(rn > rtol * bn) || !(rn == rn)) {
-            active[p] = 0;
-            done_step[p] = *step;
-        }
-    }
-    const bool on = active[p] != 0;
-    inv[p] = on ? 1.0 / rn : 0.0;
-    scale[p] = on ? rn : 0.0;
-    if (on) atomicAdd(n_active, 1);
-}
-
-__global__ void bstep_kernel(int *step) { *step += 1; }
-
 // ---------------------------------------------------------------- layout
 
 // Dof layout of one batch of concatenated vectors and its work list.
@@ -362,9 +340,10 @@ public:
     ptrdiff_t cols() const override { return op->cols(); }
 };
 
-// Preconditioned (flexible, Polak-Ribiere) CG over a batch: a fixed number of
-// iterations per apply, per-problem scalars on the device, a problem stops
-// updating once ||r_p|| <= rtol ||r0_p||.  No host synchronisation.
+// Preconditioned (flexible, Polak-Ribiere) CG over a batch: per-problem scalars on
+// the device, a problem stops updating once ||r_p|| <= rtol ||r0_p||.  No host
+// synchronisation: apply() runs exactly max_it iterations; start() / iterate()
+// let an outer driver run (and graph-capture) the iterations in chunks.
 template <typename T>
 class BatchCG final : public Solver<T> {
 public:
@@ -376,6 +355,7 @@ public:
     int max_it{10};
     double rtol{1e-4};
     bool flexible{true};
+    T *zz{nullptr}, *zp{nullptr};  // current / previous preconditioned residual
 
     int prepare() {
         const ptrdiff_t n = op->rows();
@@ -388,144 +368,156 @@ public:
         SFEM_GB300_CHECK(active.resize(lay->P));
         return 0;
     }
-    int apply(const T *b, T *x) override {
+    double *scal(int k) { return sc.ptr + (ptrdiff_t)k * lay->P; }
+    int start(const T *b, const T *x) {
         const ptrdiff_t n = op->rows();
         const int P = lay->P;
         if (!active.ptr) SFEM_GB300_CHECK(prepare());
         const cudaStream_t s = lay->ctx->stream;
-        void *sp = lay->ctx->sp();
-        const int rt = real_type_v<T>;
-        double *rz = sc.ptr, *rz_old = sc.ptr + P, *pAp = sc.ptr + 2 * P, *rr = sc.ptr + 3 * P,
-               *rzp = sc.ptr + 4 * P, *rr0 = sc.ptr + 5 * P;
         const bool pre = (bool)precond;
-        const bool flex = pre && flexible;
-        T *zz = pre ? z.ptr : r.ptr;
-        T *zp = flex ? zprev.ptr : nullptr;
+        zz = pre ? z.ptr : r.ptr;
+        zp = pre && flexible ? zprev.ptr : nullptr;
         if (!op->overwrites_output()) SFEM_GB300_CUDA(cudaMemsetAsync(r.ptr, 0, n * sizeof(T), s));
         SFEM_GB300_CHECK(op->apply(x, r.ptr));
-        SFEM_GB300_CHECK(sfem_gb300_axpby(rt, n, 1.0, b, -1.0, r.ptr, sp));  // r = b - A x
+        SFEM_GB300_CHECK(sfem_gb300_axpby(real_type_v<T>, n, 1.0, b, -1.0, r.ptr, lay->ctx->sp()));  // r = b - A x
         if (pre) {
             if (!precond->overwrites_output()) SFEM_GB300_CUDA(cudaMemsetAsync(z.ptr, 0, n * sizeof(T), s));
             SFEM_GB300_CHECK(precond->apply(r.ptr, z.ptr));
         }
         SFEM_GB300_CUDA(cudaMemcpyAsync(p.ptr, zz, n * sizeof(T), cudaMemcpyDeviceToDevice, s));
-        SFEM_GB300_CHECK(lay->dot(r.ptr, zz, rz));
-        SFEM_GB300_CHECK(lay->dot(r.ptr, r.ptr, rr0));
-        bcg_start_kernel<<<lay->pgrid(), 128, 0, s>>>(P, rr0, active.ptr);
+        SFEM_GB300_CHECK(lay->dot(r.ptr, zz, scal(0)));
+        SFEM_GB300_CHECK(lay->dot(r.ptr, r.ptr, scal(5)));
+        bcg_start_kernel<<<lay->pgrid(), 128, 0, s>>>(P, scal(5), active.ptr);
+        return check_launch("BatchCG start");
+    }
+    // k iterations from the current state; rr0 (scal(5)) is the reference of the test
+    int iterate(int k, T *x) {
+        const ptrdiff_t n = op->rows();
+        const int P = lay->P;
+        const cudaStream_t s = lay->ctx->stream;
+        const bool pre = (bool)precond;
+        const bool flex = zp != nullptr;
         const double tol2 = rtol * rtol;
-        for (int it = 0; it < max_it; it++) {
+        for (int it = 0; it < k; it++) {
             if (!op->overwrites_output()) SFEM_GB300_CUDA(cudaMemsetAsync(Ap.ptr, 0, n * sizeof(T), s));
             SFEM_GB300_CHECK(op->apply(p.ptr, Ap.ptr));
-            SFEM_GB300_CHECK(lay->dot(p.ptr, Ap.ptr, pAp));
-            bcg_update_x_r_kernel<T><<<lay->grid(), lay->threads, 0, s>>>(lay->n_items, lay->work.ptr, rz, pAp,
-                                                                           active.ptr, p.ptr, Ap.ptr, x, r.ptr,
-                                                                           lay->partials.ptr);
-            bsum_kernel<<<lay->pgrid(), 128, 0, s>>>(P, lay->first_item.ptr, lay->partials.ptr, rr);
-            bcg_check_kernel<<<lay->pgrid(), 128, 0, s>>>(P, rr, rr0, tol2, active.ptr);
-            if (it + 1 == max_it) break;
-            SFEM_GB300_CUDA(cudaMemcpyAsync(rz_old, rz, P * sizeof(double), cudaMemcpyDeviceToDevice, s));
+            SFEM_GB300_CHECK(lay->dot(p.ptr, Ap.ptr, scal(2)));
+            bcg_update_x_r_kernel<T><<<lay->grid(), lay->threads, 0, s>>>(lay->n_items, lay->work.ptr, scal(0),
+                                                                           scal(2), active.ptr, p.ptr, Ap.ptr, x,
+                                                                           r.ptr, lay->partials.ptr);
+            bsum_kernel<<<lay->pgrid(), 128, 0, s>>>(P, lay->first_item.ptr, lay->partials.ptr, scal(3));
+            bcg_check_kernel<<<lay->pgrid(), 128, 0, s>>>(P, scal(3), scal(5), tol2, active.ptr);
+            SFEM_GB300_CUDA(cudaMemcpyAsync(scal(1), scal(0), P * sizeof(double), cudaMemcpyDeviceToDevice, s));
             if (pre) {
                 if (flex) std::swap(zz, zp);
                 if (!precond->overwrites_output()) SFEM_GB300_CUDA(cudaMemsetAsync(zz, 0, n * sizeof(T), s));
                 SFEM_GB300_CHECK(precond->apply(r.ptr, zz));
-                SFEM_GB300_CHECK(lay->dot(r.ptr, zz, rz));
-                if (flex) SFEM_GB300_CHECK(lay->dot(r.ptr, zp, rzp));
+                SFEM_GB300_CHECK(lay->dot(r.ptr, zz, scal(0)));
+                if (flex) SFEM_GB300_CHECK(lay->dot(r.ptr, zp, scal(4)));
             } else {
-                SFEM_GB300_CUDA(cudaMemcpyAsync(rz, rr, P * sizeof(double), cudaMemcpyDeviceToDevice, s));
+                SFEM_GB300_CUDA(cudaMemcpyAsync(scal(0), scal(3), P * sizeof(double), cudaMemcpyDeviceToDevice, s));
             }
-            bcg_update_p_kernel<T><<<lay->grid(), lay->threads, 0, s>>>(lay->n_items, lay->work.ptr, rz, rz_old,
-                                                                         flex ? rzp : nullptr, active.ptr, zz, p.ptr);
+            bcg_update_p_kernel<T><<<lay->grid(), lay->threads, 0, s>>>(lay->n_items, lay->work.ptr, scal(0), scal(1),
+                                                                         flex ? scal(4) : nullptr, active.ptr, zz,
+                                                                         p.ptr);
         }
+        return check_launch("BatchCG iterate");
+    }
+    int apply(const T *b, T *x) override {
+        SFEM_GB300_CHECK(start(b, x));
+        SFEM_GB300_CHECK(iterate(max_it, x));
         this->iterations_ = max_it;
-        return check_launch("BatchCG");
+        return 0;
     }
     ptrdiff_t rows() const override { return op->rows(); }
     ptrdiff_t cols() const override { return op->cols(); }
 };
 
-// FP64 iterative refinement over a batch around an FP32 batched inner solver.
-// One outer step (residual, per-problem check, normalised FP32 residual, inner
-// solve, update) is captured into a CUDA graph and replayed.
-class BatchIR {
+// Per-problem precision bridge: z += ||r_p|| M32(r_p / ||r_p||) for a float
+// preconditioner M32 (e.g. the grouped float multigrid) under a double Krylov method.
+__global__ void bbridge_scale_kernel(int P, const double *__restrict__ rr, double *__restrict__ inv,
+                                     double *__restrict__ scale) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= P) return;
+    const double n = sqrt(rr[p]);
+    inv[p] = n > 0 ? 1.0 / n : 0.0;
+    scale[p] = n;
+}
+
+class BatchBridge final : public Operator<double> {
+public:
+    std::shared_ptr<BatchLayout> lay;
+    std::shared_ptr<Operator<float>> inner;
+    DeviceBuffer<float> r32, z32;
+    DeviceBuffer<double> rr, inv, scale;
+    int apply(const double *r, double *z) override {
+        const ptrdiff_t n = inner->rows();
+        const int P = lay->P;
+        const cudaStream_t s = lay->ctx->stream;
+        if (!r32.ptr) {
+            SFEM_GB300_CHECK(r32.resize(n));
+            SFEM_GB300_CHECK(z32.resize(n));
+            SFEM_GB300_CHECK(rr.resize(P));
+            SFEM_GB300_CHECK(inv.resize(P));
+            SFEM_GB300_CHECK(scale.resize(P));
+        }
+        SFEM_GB300_CHECK(lay->dot(r, r, rr.ptr));
+        bbridge_scale_kernel<<<lay->pgrid(), 128, 0, s>>>(P, rr.ptr, inv.ptr, scale.ptr);
+        bconvert_scaled_kernel<<<lay->grid(), lay->threads, 0, s>>>(lay->n_items, lay->work.ptr, inv.ptr, r, r32.ptr);
+        SFEM_GB300_CUDA(cudaMemsetAsync(z32.ptr, 0, n * sizeof(float), s));
+        SFEM_GB300_CHECK(inner->apply(r32.ptr, z32.ptr));
+        baxpy_f32_to_f64_kernel<<<lay->grid(), lay->threads, 0, s>>>(lay->n_items, lay->work.ptr, scale.ptr, z32.ptr,
+                                                                     z);
+        return check_launch("BatchBridge");
+    }
+    ptrdiff_t rows() const override { return inner->rows(); }
+    ptrdiff_t cols() const override { return inner->cols(); }
+};
+
+// Host driver of a batched double CG (typically flexible, preconditioned by a
+// BatchBridge over the grouped float multigrid): chunks of `check_every`
+// iterations are captured into one CUDA graph on a private stream and replayed;
+// after each chunk the host reads the per-problem active mask (one small copy)
+// to time every problem's convergence and to stop when all have converged.
+class BatchSolve {
 public:
     std::shared_ptr<Context> ctx;
     std::shared_ptr<BatchLayout> lay;
-    std::shared_ptr<Operator<double>> op;
-    std::shared_ptr<Operator<float>> inner;
-    int max_outer{30};
-    double rtol{1e-10};
+    std::shared_ptr<BatchCG<double>> cg;
+    int check_every{5};
+    int max_it{300};
     bool use_graph{true};
-    DeviceBuffer<double> r64, bb, rr, inv, scale, rel;
-    DeviceBuffer<float> r32, e32;
-    DeviceBuffer<int> active, done_step, counters;  // counters: [0] active problems, [1] step
-    int *h_counters{nullptr};
     cudaStream_t stream{nullptr};
     cudaGraphExec_t exec{nullptr};
-    const double *g_b{nullptr};
     double *g_x{nullptr};
-    // results of the last solve (host)
-    std::vector<int> h_done;
-    std::vector<double> h_rel, h_latency;
-    int outer_steps{0};
+    std::vector<double> h_latency;
+    std::vector<int> h_iters;
+    int iterations{0};
     double seconds{0};
 
-    ~BatchIR() {
-        if (exec) cudaGraphExecDestroy(exec);
+    ~BatchSolve() {
+        exec_reset();
         if (stream) cudaStreamDestroy(stream);
-        if (h_counters) cudaFreeHost(h_counters);
-    }
-    int prepare() {
-        const ptrdiff_t n = op->rows();
-        const int P = lay->P;
-        SFEM_GB300_CHECK(r64.resize(n));
-        SFEM_GB300_CHECK(r32.resize(n));
-        SFEM_GB300_CHECK(e32.resize(n));
-        for (auto *b : {&bb, &rr, &inv, &scale, &rel}) SFEM_GB300_CHECK(b->resize(P));
-        SFEM_GB300_CHECK(active.resize(P));
-        SFEM_GB300_CHECK(done_step.resize(P));
-        SFEM_GB300_CHECK(counters.resize(2));
-        if (!h_counters) SFEM_GB300_CUDA(cudaMallocHost((void **)&h_counters, 2 * sizeof(int)));
-        if (!stream) SFEM_GB300_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
-        return 0;
-    }
-    // one outer step on the context stream
-    int step(const double *b, double *x) {
-        const ptrdiff_t n = op->rows();
-        const int P = lay->P;
-        const cudaStream_t s = ctx->stream;
-        void *sp = ctx->sp();
-        SFEM_GB300_CUDA(cudaMemsetAsync(counters.ptr, 0, sizeof(int), s));
-        if (!op->overwrites_output()) SFEM_GB300_CUDA(cudaMemsetAsync(r64.ptr, 0, n * sizeof(double), s));
-        SFEM_GB300_CHECK(op->apply(x, r64.ptr));
-        SFEM_GB300_CHECK(sfem_gb300_axpby(SFEM_GB300_FLOAT64, n, 1.0, b, -1.0, r64.ptr, sp));
-        SFEM_GB300_CHECK(lay->dot(r64.ptr, r64.ptr, rr.ptr));
-        bir_check_kernel<<<lay->pgrid(), 128, 0, s>>>(P, rr.ptr, bb.ptr, rtol, counters.ptr + 1, active.ptr,
-                                                      done_step.ptr, rel.ptr, inv.ptr, scale.ptr, counters.ptr);
-        bconvert_scaled_kernel<<<lay->grid(), lay->threads, 0, s>>>(lay->n_items, lay->work.ptr, inv.ptr, r64.ptr,
-                                                                    r32.ptr);
-        SFEM_GB300_CUDA(cudaMemsetAsync(e32.ptr, 0, n * sizeof(float), s));
-        SFEM_GB300_CHECK(inner->apply(r32.ptr, e32.ptr));
-        baxpy_f32_to_f64_kernel<<<lay->grid(), lay->threads, 0, s>>>(lay->n_items, lay->work.ptr, scale.ptr, e32.ptr,
-                                                                     x);
-        bstep_kernel<<<1, 1, 0, s>>>(counters.ptr + 1);
-        SFEM_GB300_CUDA(cudaMemcpyAsync(h_counters, counters.ptr, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
-        return check_launch("BatchIR step");
     }
     void exec_reset() {
         if (exec) cudaGraphExecDestroy(exec);
         exec = nullptr;
-        g_b = nullptr;
         g_x = nullptr;
     }
-    int capture(const double *b, double *x) {
-        exec_reset();
+    int on_stream(const std::function<int()> &fn) {
         const cudaStream_t saved = ctx->stream;
         ctx->stream = stream;
+        const int rc = fn();
+        ctx->stream = saved;
+        return rc;
+    }
+    int capture(double *x) {
+        exec_reset();
         cudaGraph_t graph = nullptr;
         cudaError_t e = cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal);
-        int rc = e == cudaSuccess ? step(b, x) : set_error("cudaStreamBeginCapture: %s", cudaGetErrorString(e));
+        int rc = e == cudaSuccess ? on_stream([&] { return cg->iterate(check_every, x); })
+                                  : set_error("cudaStreamBeginCapture: %s", cudaGetErrorString(e));
         cudaError_t e2 = e == cudaSuccess ? cudaStreamEndCapture(stream, &graph) : cudaSuccess;
-        ctx->stream = saved;
         if (rc) {
             if (graph) cudaGraphDestroy(graph);
             return rc;
@@ -534,75 +526,54 @@ public:
         e = cudaGraphInstantiate(&exec, graph, 0);
         cudaGraphDestroy(graph);
         if (e != cudaSuccess) return set_error("cudaGraphInstantiate: %s", cudaGetErrorString(e));
-        g_b = b;
         g_x = x;
         return 0;
     }
-    // Per-problem state for right-hand side b, on the solver stream (synchronises it).
-    int reset(const double *b) {
-        const int P = lay->P;
-        const cudaStream_t saved = ctx->stream;
-        ctx->stream = stream;
-        const int rc = lay->dot(b, b, bb.ptr);
-        ctx->stream = saved;
-        if (rc) return rc;
-        std::vector<int> ones(P, 1), minus(P, -1);
-        SFEM_GB300_CUDA(cudaMemcpyAsync(active.ptr, ones.data(), P * sizeof(int), cudaMemcpyHostToDevice, stream));
-        SFEM_GB300_CUDA(cudaMemcpyAsync(done_step.ptr, minus.data(), P * sizeof(int), cudaMemcpyHostToDevice, stream));
-        SFEM_GB300_CUDA(cudaMemsetAsync(counters.ptr, 0, 2 * sizeof(int), stream));
-        SFEM_GB300_CUDA(cudaStreamSynchronize(stream));  // the host vectors above are temporaries
-        return 0;
-    }
-    int eager_step(const double *b, double *x) {
-        const cudaStream_t saved = ctx->stream;
-        ctx->stream = stream;
-        const int rc = step(b, x);
-        ctx->stream = saved;
-        return rc;
-    }
-    // Makes sure a graph of the step for (b, x) exists; a warm-up step on a
-    // scratch copy of x first sizes every lazily allocated buffer.
-    int ensure_graph(const double *b, double *x) {
-        if (exec && g_b == b && g_x == x) return 0;
-        DeviceBuffer<double> xs(op->rows());
-        SFEM_GB300_CUDA(cudaMemcpyAsync(xs.ptr, x, op->rows() * sizeof(double), cudaMemcpyDeviceToDevice, stream));
-        SFEM_GB300_CHECK(eager_step(b, xs.ptr));
-        SFEM_GB300_CUDA(cudaStreamSynchronize(stream));
-        return capture(b, x);
+    int chunk(double *x) {
+        if (use_graph) {
+            SFEM_GB300_CUDA(cudaGraphLaunch(exec, stream));
+            return 0;
+        }
+        return on_stream([&] { return cg->iterate(check_every, x); });
     }
     int solve(const double *b, double *x) {
         const int P = lay->P;
-        SFEM_GB300_CHECK(prepare());
-        // the solver stream runs after all work the caller queued on the context stream
-        SFEM_GB300_CUDA(cudaStreamSynchronize(ctx->stream));
-        if (use_graph) SFEM_GB300_CHECK(ensure_graph(b, x));
-        SFEM_GB300_CHECK(reset(b));
-        h_latency.assign(P, -1.0);
+        if (!stream) SFEM_GB300_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+        SFEM_GB300_CUDA(cudaStreamSynchronize(ctx->stream));  // caller's work on b, x is done
+        if (use_graph && (!exec || g_x != x)) {
+            // eager warm-up on a scratch iterate sizes every lazily allocated buffer
+            DeviceBuffer<double> xs(cg->rows());
+            SFEM_GB300_CUDA(cudaMemcpyAsync(xs.ptr, x, cg->rows() * sizeof(double), cudaMemcpyDeviceToDevice, stream));
+            SFEM_GB300_CHECK(on_stream([&] { return cg->start(b, xs.ptr); }));
+            SFEM_GB300_CHECK(on_stream([&] { return cg->iterate(1, xs.ptr); }));
+            SFEM_GB300_CUDA(cudaStreamSynchronize(stream));
+            SFEM_GB300_CHECK(capture(x));
+        }
         std::vector<int> h_active(P, 1), prev(P, 1);
+        h_latency.assign(P, -1.0);
+        h_iters.assign(P, -1);
         const auto t0 = std::chrono::steady_clock::now();
-        outer_steps = 0;
-        for (int k = 0; k <= max_outer; k++) {
-            if (use_graph)
-                SFEM_GB300_CUDA(cudaGraphLaunch(exec, stream));
-            else
-                SFEM_GB300_CHECK(eager_step(b, x));
-            SFEM_GB300_CUDA(cudaMemcpyAsync(h_active.data(), active.ptr, P * sizeof(int), cudaMemcpyDeviceToHost,
+        SFEM_GB300_CHECK(on_stream([&] { return cg->start(b, x); }));
+        int n_active = P;
+        for (iterations = 0; iterations < max_it && n_active > 0;) {
+            SFEM_GB300_CHECK(chunk(x));
+            iterations += check_every;
+            SFEM_GB300_CUDA(cudaMemcpyAsync(h_active.data(), cg->active.ptr, P * sizeof(int), cudaMemcpyDeviceToHost,
                                             stream));
             SFEM_GB300_CUDA(cudaStreamSynchronize(stream));
             const double now = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-            outer_steps = k + 1;
-            for (int q = 0; q < P; q++)
-                if (prev[q] && !h_active[q]) h_latency[q] = now;
+            n_active = 0;
+            for (int q = 0; q < P; q++) {
+                if (prev[q] && !h_active[q]) {
+                    h_latency[q] = now;
+                    h_iters[q] = iterations;
+                }
+                n_active += h_active[q] != 0;
+            }
             prev = h_active;
-            if (h_counters[0] == 0) break;
         }
         seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-        h_done.resize(P);
-        h_rel.resize(P);
-        SFEM_GB300_CUDA(cudaMemcpy(h_done.data(), done_step.ptr, P * sizeof(int), cudaMemcpyDeviceToHost));
-        SFEM_GB300_CUDA(cudaMemcpy(h_rel.data(), rel.ptr, P * sizeof(double), cudaMemcpyDeviceToHost));
-        if (h_counters[0] != 0)
-            return set_error("BatchIR: %d problems not converged in %d outer steps", h_counters[0], max_outer);
+        if (n_active) return set_error("BatchSolve: %d problems not converged in %d iterations", n_active, max_it);
         return 0;
     }
 };
@@ -766,63 +737,87 @@ extern "C" int sfem_gb300_batch_cg_create(void *context, void *layout, void *op,
     return SFEM_GB300_SUCCESS;
 }
 
-extern "C" int sfem_gb300_batch_ir_create(void *context, void *layout, void *op64, void *inner32, int max_outer,
-                                          double rtol, int use_graph, void **out) {
+extern "C" int sfem_gb300_batch_bridge_create(void *context, void *layout, void *inner32, void **out) {
     auto *c = H(context);
     auto lay = layout_of(H(layout));
-    if (!H(op64)->d || !H(inner32)->f)
-        return set_error("sfem_gb300_batch_ir_create: needs a double operator and a float inner solver");
-    if (H(op64)->rows() != lay->n() || H(inner32)->rows() != lay->n())
-        return set_error("sfem_gb300_batch_ir_create: operator / layout size mismatch");
-    auto ir = std::make_shared<BatchIR>();
-    ir->ctx = c->ctx;
-    ir->lay = lay;
-    ir->op = H(op64)->d;
-    ir->inner = H(inner32)->f;
-    ir->max_outer = max_outer;
-    ir->rtol = rtol;
-    ir->use_graph = use_graph != 0;
+    if (!H(inner32)->f) return set_error("sfem_gb300_batch_bridge_create: inner operator must be float");
+    if (H(inner32)->rows() != lay->n()) return set_error("sfem_gb300_batch_bridge_create: size mismatch");
+    auto b = std::make_shared<BatchBridge>();
+    b->lay = lay;
+    b->inner = H(inner32)->f;
     auto *h = new Handle();
-    h->kind = "batch_ir";
+    h->kind = "batch_bridge";
     h->ctx = c->ctx;
-    h->impl = ir;
+    h->real_type = SFEM_GB300_FLOAT64;
+    h->d = b;
     *out = h;
     return SFEM_GB300_SUCCESS;
 }
 
-extern "C" int sfem_gb300_batch_ir_solve(void *solver, const double *b, double *x, double *latency_s,
-                                         int *outer_steps_per_problem, double *final_rel, double *seconds) {
-    auto ir = std::static_pointer_cast<BatchIR>(H(solver)->impl);
-    const int rc = ir->solve(b, x);
-    const int P = ir->lay->P;
-    if (latency_s && (int)ir->h_latency.size() == P) std::memcpy(latency_s, ir->h_latency.data(), P * sizeof(double));
-    if (outer_steps_per_problem && (int)ir->h_done.size() == P)
-        std::memcpy(outer_steps_per_problem, ir->h_done.data(), P * sizeof(int));
-    if (final_rel && (int)ir->h_rel.size() == P) std::memcpy(final_rel, ir->h_rel.data(), P * sizeof(double));
-    if (seconds) *seconds = ir->seconds;
+extern "C" int sfem_gb300_batch_solve_create(void *context, void *layout, void *cg64, int check_every, int max_it,
+                                             int use_graph, void **out) {
+    auto *c = H(context);
+    auto lay = layout_of(H(layout));
+    auto *h_cg = H(cg64);
+    if (h_cg->kind != "batch_cg" || !h_cg->d) return set_error("sfem_gb300_batch_solve_create: needs a double batch CG");
+    if (check_every < 1) return set_error("sfem_gb300_batch_solve_create: check_every must be >= 1");
+    auto bs = std::make_shared<BatchSolve>();
+    bs->ctx = c->ctx;
+    bs->lay = lay;
+    bs->cg = std::static_pointer_cast<BatchCG<double>>(h_cg->impl);
+    bs->check_every = check_every;
+    bs->max_it = max_it;
+    bs->use_graph = use_graph != 0;
+    auto *h = new Handle();
+    h->kind = "batch_solve";
+    h->ctx = c->ctx;
+    h->impl = bs;
+    *out = h;
+    return SFEM_GB300_SUCCESS;
+}
+
+extern "C" int sfem_gb300_batch_solve_set_launch(void *solver, int check_every) {
+    auto bs = std::static_pointer_cast<BatchSolve>(H(solver)->impl);
+    if (check_every < 1) return set_error("sfem_gb300_batch_solve_set_launch: check_every must be >= 1");
+    bs->check_every = check_every;
+    bs->exec_reset();
+    return SFEM_GB300_SUCCESS;
+}
+
+extern "C" int sfem_gb300_batch_solve_run(void *solver, const double *b, double *x, double *latency_s,
+                                          int *iterations_per_problem, double *seconds) {
+    auto bs = std::static_pointer_cast<BatchSolve>(H(solver)->impl);
+    const int rc = bs->solve(b, x);
+    const int P = bs->lay->P;
+    if (latency_s && (int)bs->h_latency.size() == P) std::memcpy(latency_s, bs->h_latency.data(), P * sizeof(double));
+    if (iterations_per_problem && (int)bs->h_iters.size() == P)
+        std::memcpy(iterations_per_problem, bs->h_iters.data(), P * sizeof(int));
+    if (seconds) *seconds = bs->seconds;
     return rc;
 }
 
-extern "C" int sfem_gb300_batch_ir_time_step(void *solver, const double *b, double *x, int reps, double *ms) {
-    auto ir = std::static_pointer_cast<BatchIR>(H(solver)->impl);
-    SFEM_GB300_CHECK(ir->prepare());
-    SFEM_GB300_CUDA(cudaStreamSynchronize(ir->ctx->stream));
-    ir->exec_reset();
-    SFEM_GB300_CHECK(ir->ensure_graph(b, x));
-    SFEM_GB300_CHECK(ir->reset(b));
+extern "C" int sfem_gb300_batch_solve_time_chunk(void *solver, const double *b, double *x, int reps, double *ms) {
+    auto bs = std::static_pointer_cast<BatchSolve>(H(solver)->impl);
+    if (!bs->stream) SFEM_GB300_CUDA(cudaStreamCreateWithFlags(&bs->stream, cudaStreamNonBlocking));
+    SFEM_GB300_CUDA(cudaStreamSynchronize(bs->ctx->stream));
+    bs->use_graph = true;
+    SFEM_GB300_CHECK(bs->on_stream([&] { return bs->cg->start(b, x); }));
+    SFEM_GB300_CHECK(bs->on_stream([&] { return bs->cg->iterate(1, x); }));  // eager warm-up
+    SFEM_GB300_CUDA(cudaStreamSynchronize(bs->stream));
+    SFEM_GB300_CHECK(bs->capture(x));
     cudaEvent_t e0, e1;
     SFEM_GB300_CUDA(cudaEventCreate(&e0));
     SFEM_GB300_CUDA(cudaEventCreate(&e1));
-    cudaGraphLaunch(ir->exec, ir->stream);
-    cudaEventRecord(e0, ir->stream);
-    for (int k = 0; k < reps; k++) cudaGraphLaunch(ir->exec, ir->stream);
-    cudaEventRecord(e1, ir->stream);
+    cudaEventRecord(e0, bs->stream);
+    for (int k = 0; k < reps; k++) cudaGraphLaunch(bs->exec, bs->stream);
+    cudaEventRecord(e1, bs->stream);
     const cudaError_t e = cudaEventSynchronize(e1);
     float t = 0;
     cudaEventElapsedTime(&t, e0, e1);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    if (e != cudaSuccess) return set_error("sfem_gb300_batch_ir_time_step: %s", cudaGetErrorString(e));
+    bs->exec_reset();
+    if (e != cudaSuccess) return set_error("sfem_gb300_batch_solve_time_chunk: %s", cudaGetErrorString(e));
     *ms = t / (reps > 0 ? reps : 1);
     return SFEM_GB300_SUCCESS;
 }

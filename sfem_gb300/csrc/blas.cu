@@ -163,6 +163,34 @@ __global__ void axpy_f32_to_f64_kernel(ptrdiff_t n, double alpha, const float *_
         y[i] += alpha * (double)x[i];
 }
 
+// dst = (float)(src / *nrm)  (device-resident scale; 0 if *nrm == 0)
+__global__ void scaled_to_f32_kernel(ptrdiff_t n, const double *__restrict__ nrm, const double *__restrict__ src,
+                                     float *__restrict__ dst) {
+    const double s = *nrm > 0 ? 1.0 / *nrm : 0.0;
+    for (ptrdiff_t i = blockIdx.x * (ptrdiff_t)blockDim.x + threadIdx.x; i < n; i += (ptrdiff_t)gridDim.x * blockDim.x)
+        dst[i] = (float)(src[i] * s);
+}
+
+// y += *nrm * (double) x
+__global__ void scaled_axpy_f32_to_f64_kernel(ptrdiff_t n, const double *__restrict__ nrm, const float *__restrict__ x,
+                                              double *__restrict__ y) {
+    const double s = *nrm;
+    for (ptrdiff_t i = blockIdx.x * (ptrdiff_t)blockDim.x + threadIdx.x; i < n; i += (ptrdiff_t)gridDim.x * blockDim.x)
+        y[i] += s * (double)x[i];
+}
+
+// x += M b, M dense row-major n x n: one warp per row
+template <typename T>
+__global__ void dense_mv_add_kernel(ptrdiff_t n, const T *__restrict__ M, const T *__restrict__ b, T *__restrict__ x) {
+    const ptrdiff_t row = (ptrdiff_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (row >= n) return;
+    T acc = 0;
+    for (ptrdiff_t j = lane; j < n; j += 32) acc += M[row * n + j] * b[j];
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if (lane == 0) x[row] += acc;
+}
+
 // ------------------------------------------------------------------ host helpers
 
 static inline int ew_grid(ptrdiff_t n) { return grid_for(n, 256, kNumSMs * 16); }
@@ -352,3 +380,30 @@ extern "C" int sfem_gb300_axpy_f32_to_f64(ptrdiff_t n, double alpha, const float
     axpy_f32_to_f64_kernel<<<ew_grid(n), 256, 0, stream_of(stream)>>>(n, alpha, x, y);
     return check_launch("sfem_gb300_axpy_f32_to_f64");
 }
+
+extern "C" int sfem_gb300_scaled_to_f32(ptrdiff_t n, const double *nrm, const double *src, float *dst, void *stream) {
+    if (n <= 0) return SFEM_GB300_SUCCESS;
+    scaled_to_f32_kernel<<<ew_grid(n), 256, 0, stream_of(stream)>>>(n, nrm, src, dst);
+    return check_launch("sfem_gb300_scaled_to_f32");
+}
+
+extern "C" int sfem_gb300_scaled_axpy_f32_to_f64(ptrdiff_t n, const double *nrm, const float *x, double *y,
+                                                 void *stream) {
+    if (n <= 0) return SFEM_GB300_SUCCESS;
+    scaled_axpy_f32_to_f64_kernel<<<ew_grid(n), 256, 0, stream_of(stream)>>>(n, nrm, x, y);
+    return check_launch("sfem_gb300_scaled_axpy_f32_to_f64");
+}
+
+namespace sfem_gb300 {
+int dense_symv_add(int real_type, ptrdiff_t n, const void *M, const void *b, void *x, void *stream) {
+    if (n <= 0) return SFEM_GB300_SUCCESS;
+    const int blocks = (int)((n + 7) / 8);
+    if (real_type == SFEM_GB300_FLOAT32)
+        dense_mv_add_kernel<float><<<blocks, 256, 0, stream_of(stream)>>>(n, (const float *)M, (const float *)b,
+                                                                           (float *)x);
+    else
+        dense_mv_add_kernel<double><<<blocks, 256, 0, stream_of(stream)>>>(n, (const double *)M, (const double *)b,
+                                                                            (double *)x);
+    return check_launch("dense_symv_add");
+}
+}  // namespace sfem_gb300

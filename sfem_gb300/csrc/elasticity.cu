@@ -140,22 +140,39 @@ __global__ void __launch_bounds__(64) elasticity_apply_warp_kernel(ptrdiff_t nel
             }
         }
         __syncwarp();
-        for (int m = lane; m < NM; m += 32) {
-            const int xi = m % L, yi = (m / L) % L, zi = m / (L * L);
-            int v[8];
-            T u[24];
+        if constexpr (NM >= 32) {
+            // one micro element per lane: u read once, reused by the 24 rows
+            for (int m = lane; m < NM; m += 32) {
+                const int xi = m % L, yi = (m / L) % L, zi = m / (L * L);
+                int v[8];
+                T u[24];
 #pragma unroll
-            for (int c = 0; c < 8; c++) {
-                v[c] = lidx(L, xi + c8x(c), yi + c8y(c), zi + c8z(c));
+                for (int c = 0; c < 8; c++) {
+                    v[c] = lidx(L, xi + c8x(c), yi + c8y(c), zi + c8z(c));
 #pragma unroll
-                for (int d = 0; d < 3; d++) u[d * 8 + c] = xw[d * NXE + v[c]];
-            }
+                    for (int d = 0; d < 3; d++) u[d * 8 + c] = xw[d * NXE + v[c]];
+                }
 #pragma unroll 4
-            for (int i = 0; i < 24; i++) {
+                for (int i = 0; i < 24; i++) {
+                    T acc = 0;
+#pragma unroll
+                    for (int j = 0; j < 24; j++) acc += K[i * 24 + j] * u[j];
+                    atomicAdd(&yw[(i / 8) * NXE + v[i % 8]], acc);
+                }
+            }
+        } else {
+            // few micro elements (hex8, L = 2, 3 with L^3 < 32): one (micro element, row) pair per lane
+            for (int t = lane; t < NM * 24; t += 32) {
+                const int m = t / 24, i = t % 24;
+                const int xi = m % L, yi = (m / L) % L, zi = m / (L * L);
                 T acc = 0;
 #pragma unroll
-                for (int j = 0; j < 24; j++) acc += K[i * 24 + j] * u[j];
-                atomicAdd(&yw[(i / 8) * NXE + v[i % 8]], acc);
+                for (int j = 0; j < 24; j++) {
+                    const int c = j % 8;
+                    acc += K[i * 24 + j] * xw[(j / 8) * NXE + lidx(L, xi + c8x(c), yi + c8y(c), zi + c8z(c))];
+                }
+                const int ci = i % 8;
+                atomicAdd(&yw[(i / 8) * NXE + lidx(L, xi + c8x(ci), yi + c8y(ci), zi + c8z(ci))], acc);
             }
         }
         __syncwarp();

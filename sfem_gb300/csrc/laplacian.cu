@@ -410,6 +410,177 @@ __global__ void __launch_bounds__(TILE) sshex8_laplacian_apply_staged_kernel(ptr
     }
 }
 
+// v4 (float bandwidth path, asynchronous staging): a CTA of 2*TILE threads owns
+// TILE consecutive macro elements.
+//  1. the tile's connectivity rows elements[v][e0 .. e0+TILE) are copied to shared
+//     memory with cp.async (16-byte copies where the row is 16-byte aligned), one
+//     coalesced line per row and no register round trip;
+//  2. x[idx] is gathered into shared memory with 4-byte cp.async copies (the
+//     dependent load chain costs no registers and every thread keeps dozens of
+//     copies in flight);
+//  3. two threads per element apply the element matrix, warp 0 the micro layers
+//     0 .. L/2-1 bottom-up, warp 1 the layers L/2 .. L-1 top-down, two node planes
+//     of y in registers, FP32x2 packed FMAs (A as 32 float2: rows 2k, 2k+1 of a
+//     column); each finished y plane overwrites its x plane, the shared middle
+//     plane is summed after a barrier;
+//  4. the y values of the tile are scattered with atomics, one coalesced pass.
+// Shared layout [node][TILE] keeps every access conflict-free.
+__device__ __forceinline__ void cp_async4(void *smem, const void *gmem) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// Inversion symmetry of the affine element matrix: the point reflection
+// xi -> 1 - xi maps hex8 corner c to pi(c) = (0 6)(1 7)(2 4)(3 5) and leaves
+// grad(phi_i) . G grad(phi_j) unchanged, so A[pi(i)][pi(j)] = A[i][j].  Rows 6, 7
+// and 4, 5 are therefore rows 0, 1 and 2, 3 read at permuted columns: the packed
+// FP32x2 form needs only A2[j][k] = (A[2k][j], A[2k+1][j]) for k = 0, 1.
+__host__ __device__ constexpr int hex8_inv(int c) { return c == 0 ? 6 : c == 1 ? 7 : c == 2 ? 4 : c == 3 ? 5 : c == 4 ? 2 : c == 5 ? 3 : c == 6 ? 0 : 1; }
+
+// one micro layer (base = x column of plane zi): lo (plane zi) and up (plane zi+1) accumulate A u
+template <int L, int TILE>
+__device__ __forceinline__ void lap_layer_f32x2(const float *__restrict__ xbase, const float2 (&A2)[8][2],
+                                                float (&lo)[(L + 1) * (L + 1)], float (&up)[(L + 1) * (L + 1)]) {
+    constexpr int N1 = L + 1;
+    constexpr int NP = N1 * N1;
+#pragma unroll
+    for (int yi = 0; yi < L; yi++) {
+#pragma unroll
+        for (int xi = 0; xi < L; xi++) {
+            float u[8];
+#pragma unroll
+            for (int c = 0; c < 8; c++) u[c] = xbase[(c8z(c) * NP + (yi + c8y(c)) * N1 + xi + c8x(c)) * TILE];
+            float2 acc[4];
+#pragma unroll
+            for (int k = 0; k < 4; k++) acc[k] = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+                const float2 uu = make_float2(u[j], u[j]);
+                acc[0] = __ffma2_rn(A2[j][0], uu, acc[0]);                 // rows 0, 1
+                acc[1] = __ffma2_rn(A2[j][1], uu, acc[1]);                 // rows 2, 3
+                acc[2] = __ffma2_rn(A2[hex8_inv(j)][1], uu, acc[2]);       // rows 4, 5
+                acc[3] = __ffma2_rn(A2[hex8_inv(j)][0], uu, acc[3]);       // rows 6, 7
+            }
+#pragma unroll
+            for (int i = 0; i < 8; i++) {
+                const float v = (i & 1) ? acc[i >> 1].y : acc[i >> 1].x;
+                const int p = (yi + c8y(i)) * N1 + xi + c8x(i);
+                if (c8z(i))
+                    up[p] += v;
+                else
+                    lo[p] += v;
+            }
+        }
+    }
+}
+
+template <int L, int TILE>
+__global__ void __launch_bounds__(2 * TILE, 6) sshex8_laplacian_apply_async_kernel(ptrdiff_t nelements,
+                                                                                const idx_t *const *elements,
+                                                                                ptrdiff_t fff_stride,
+                                                                                const float *fff,
+                                                                                const float *__restrict__ x,
+                                                                                float *__restrict__ y) {
+    static_assert(L % 2 == 0, "two threads per element split the micro layers in halves");
+    constexpr int N1 = L + 1;
+    constexpr int NP = N1 * N1;
+    constexpr int NXE = NP * N1;
+    constexpr int H = L / 2;  // layers per half; the shared plane is H
+    __shared__ __align__(16) idx_t sidx[NXE * TILE];
+    __shared__ __align__(16) float sx[NXE * TILE];
+    __shared__ float spart[NP * TILE];  // upper half's partial sum of the shared plane
+    const int tid = threadIdx.x;
+    const ptrdiff_t e0 = (ptrdiff_t)blockIdx.x * TILE;
+    const int nvalid = (int)((nelements - e0) < TILE ? (nelements - e0) : TILE);
+    // 1. connectivity rows
+    for (int v = tid / (TILE / 4); v < NXE; v += (2 * TILE) / (TILE / 4)) {
+        const int q = tid % (TILE / 4);  // 16-byte quarter of the row segment
+        const idx_t *row = elements[v] + e0;
+        if (nvalid == TILE && ((reinterpret_cast<uintptr_t>(row) & 15) == 0)) {
+            cp_async16(&sidx[v * TILE + 4 * q], row + 4 * q);
+        } else {
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+                if (4 * q + k < nvalid) cp_async4(&sidx[v * TILE + 4 * q + k], row + 4 * q + k);
+        }
+    }
+    cp_async_wait_all();
+    __syncthreads();
+    // 2. gather x
+    for (int t = tid; t < NXE * TILE; t += 2 * TILE) {
+        const int el = t % TILE;
+        if (el < nvalid) cp_async4(&sx[t], x + sidx[t]);
+    }
+    const int el = tid % TILE;
+    const int half = tid / TILE;  // warp-uniform for TILE = 32
+    const bool valid = el < nvalid;
+    // element matrix, rows 0..3 packed by pairs (overlaps the gathers in flight)
+    float2 A2[8][2];
+    {
+        float f[6];
+        const float h = 1.f / (float)L;
+#pragma unroll
+        for (int m = 0; m < 6; m++) f[m] = valid ? __ldg(&fff[m * fff_stride + e0 + el]) * h : 0.f;
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+#pragma unroll
+            for (int k = 0; k < 2; k++) {
+                float a0 = 0.f, a1 = 0.f;
+#pragma unroll
+                for (int m = 0; m < 6; m++) {
+                    const double w0 = LapTable().w[(2 * k) * 8 + j][m];
+                    const double w1 = LapTable().w[(2 * k + 1) * 8 + j][m];
+                    if (w0 != 0.0) a0 += f[m] * (float)w0;
+                    if (w1 != 0.0) a1 += f[m] * (float)w1;
+                }
+                A2[j][k] = make_float2(a0, a1);
+            }
+        }
+    }
+    cp_async_wait_all();
+    __syncthreads();
+    // 3. apply: half h runs layers h*H .. h*H + H - 1 upwards (same code for both halves)
+    float *col = sx + el;
+    const int z0 = half * H;
+    float lo[NP], up[NP];
+#pragma unroll
+    for (int p = 0; p < NP; p++) lo[p] = 0.f;
+#pragma unroll 1
+    for (int zi = z0; zi < z0 + H; zi++) {
+#pragma unroll
+        for (int p = 0; p < NP; p++) up[p] = 0.f;
+        lap_layer_f32x2<L, TILE>(col + zi * NP * TILE, A2, lo, up);
+        // plane zi is complete for this half; its x is not read again by this half.
+        // The upper half's bottom plane is the shared one: keep it aside.
+        float *dst = (zi == H && half == 1) ? (spart + el) : (col + zi * NP * TILE);
+#pragma unroll
+        for (int p = 0; p < NP; p++) {
+            dst[p * TILE] = lo[p];
+            lo[p] = up[p];
+        }
+    }
+    // lo = plane z0 + H: the lower half's partial of the shared plane, the upper half's top plane
+    if (half == 1) {
+#pragma unroll
+        for (int p = 0; p < NP; p++) col[(L * NP + p) * TILE] = lo[p];
+    }
+    __syncthreads();  // every x read of the shared plane is done
+    if (half == 0) {
+#pragma unroll
+        for (int p = 0; p < NP; p++) col[(H * NP + p) * TILE] = lo[p] + spart[p * TILE + el];
+    }
+    __syncthreads();
+    // 4. scatter
+    for (int t = tid; t < NXE * TILE; t += 2 * TILE) {
+        if (t % TILE < nvalid) atomicAdd(&y[sidx[t]], sx[t]);
+    }
+}
+
 // Diagonal: node value = sum over the micro elements of this macro element that
 // contain it of A[a][a] (a = the node's corner in that micro element).
 template <typename T, int L>
@@ -454,12 +625,15 @@ __global__ void __launch_bounds__(128) sshex8_laplacian_diag_kernel(ptrdiff_t ne
 
 // Kernel variant override for benchmarking (SFEM_GB300_LAPLACIAN_KERNEL):
 // default / "staged" (0) = shared-memory staged tile kernel for float, L <= 4;
-// "warp" (1) = warp per element; "thread" (2) = registers-only thread per element.
+// "warp" (1) = warp per element; "thread" (2) = registers-only thread per element;
+// "async" (3) = cp.async staged tile, two threads per element, packed FP32x2 FMAs (even L).
+static int g_laplacian_variant = -1;
 static int laplacian_variant() {
-    static int v = -1;
+    int v = __atomic_load_n(&g_laplacian_variant, __ATOMIC_RELAXED);
     if (v < 0) {
         const char *e = getenv("SFEM_GB300_LAPLACIAN_KERNEL");
-        v = (e && e[0] == 'w') ? 1 : (e && e[0] == 't') ? 2 : 0;
+        v = (e && e[0] == 'w') ? 1 : (e && e[0] == 't') ? 2 : (e && e[0] == 'a') ? 3 : 0;
+        __atomic_store_n(&g_laplacian_variant, v, __ATOMIC_RELAXED);
     }
     return v;
 }
@@ -495,6 +669,17 @@ static int laplacian_apply_tpl(int element_type, ptrdiff_t nelements, idx_t **el
                 break;
         }
         return check_launch("cu_laplacian_apply(SSHEX8, staged tile)");
+    }
+    if (sizeof(T) == 4 && (L == 2 || L == 4) && variant == 3) {
+        constexpr int TILE = 32;
+        const int tb = (int)((nelements + TILE - 1) / TILE);
+        if (L == 2)
+            sshex8_laplacian_apply_async_kernel<2, TILE><<<tb, 2 * TILE, 0, s>>>(
+                    nelements, elements, fff_stride, fff, (const float *)x, (float *)y);
+        else
+            sshex8_laplacian_apply_async_kernel<4, TILE><<<tb, 2 * TILE, 0, s>>>(
+                    nelements, elements, fff_stride, fff, (const float *)x, (float *)y);
+        return check_launch("cu_laplacian_apply(SSHEX8, async tile)");
     }
     const bool tpe = sizeof(T) == 4 && L >= 2 && L <= 4 && variant == 2;
     if (tpe) {
@@ -607,4 +792,11 @@ extern "C" int cu_laplacian_diag(int element_type, ptrdiff_t nelements, idx_t **
         default:
             return set_error("cu_laplacian_diag: unsupported real type %d", real_type_diag);
     }
+}
+
+extern "C" int sfem_gb300_set_laplacian_kernel(int variant) {
+    if (variant < 0 || variant > 3) return set_error("sfem_gb300_set_laplacian_kernel: variant must be 0..3");
+    const int prev = laplacian_variant();
+    __atomic_store_n(&g_laplacian_variant, variant, __ATOMIC_RELAXED);
+    return prev;
 }

@@ -85,6 +85,29 @@ public:
     bool overwrites_output() const override { return true; }
 };
 
+// Nested interpolation (or its transpose) stored as CSR: overwrites y, then zeroes
+// the output Dirichlet dofs (used for the hex8 levels below the macro mesh).
+template <typename T>
+class CrsTransferOp final : public Operator<T> {
+public:
+    std::shared_ptr<Context> ctx;
+    ptrdiff_t nrows{0}, ncols{0}, n_dirichlet{0};
+    int vec{1};
+    const idx_t *rowptr{nullptr}, *colidx{nullptr};
+    const double *weights{nullptr};
+    const idx_t *dirichlet{nullptr};
+    int apply(const T *x, T *y) override {
+        SFEM_GB300_CHECK(sfem_gb300_crs_transfer(real_type_v<T>, nrows, vec, rowptr, colidx, weights, x, y, ctx->sp()));
+        for (int c = 0; c < vec; c++)
+            SFEM_GB300_CHECK(
+                    sfem_gb300_constraint_nodes_to_value(real_type_v<T>, n_dirichlet, dirichlet, vec, c, 0.0, y, ctx->sp()));
+        return 0;
+    }
+    ptrdiff_t rows() const override { return vec * nrows; }
+    ptrdiff_t cols() const override { return vec * ncols; }
+    bool overwrites_output() const override { return true; }
+};
+
 // Restriction (accumulates into y) followed by zeroing the coarse Dirichlet dofs
 // (algebra/mg/sfem_GeometricMultigrid.cpp:38-52).
 template <typename T>
@@ -730,10 +753,12 @@ int sfem_gb300_mg_set_post_smoother(void *mg, int level, void *smoother) {
         auto m = std::static_pointer_cast<Multigrid<float>>(h->impl);
         if (level < 0 || level >= (int)m->levels.size()) return set_error("mg_set_post_smoother: bad level");
         m->levels[level].post_smoother = s->f;
+        m->release_graphs();
     } else {
         auto m = std::static_pointer_cast<Multigrid<double>>(h->impl);
         if (level < 0 || level >= (int)m->levels.size()) return set_error("mg_set_post_smoother: bad level");
         m->levels[level].post_smoother = s->d;
+        m->release_graphs();
     }
     return SFEM_GB300_SUCCESS;
 }
@@ -746,10 +771,84 @@ int sfem_gb300_mg_set_pre_smoother(void *mg, int level, void *smoother) {
         auto m = std::static_pointer_cast<Multigrid<float>>(h->impl);
         if (level < 0 || level >= (int)m->levels.size()) return set_error("mg_set_pre_smoother: bad level");
         m->levels[level].smoother = s->f;
+        m->release_graphs();
     } else {
         auto m = std::static_pointer_cast<Multigrid<double>>(h->impl);
         if (level < 0 || level >= (int)m->levels.size()) return set_error("mg_set_pre_smoother: bad level");
         m->levels[level].smoother = s->d;
+        m->release_graphs();
+    }
+    return SFEM_GB300_SUCCESS;
+}
+
+int sfem_gb300_crs_transfer_op_create(void *context, int real_type, ptrdiff_t nrows, ptrdiff_t ncols,
+                                      const idx_t *rowptr, const idx_t *colidx, const double *weights, int vec_size,
+                                      ptrdiff_t n_dirichlet, const idx_t *dirichlet, void **out) {
+    auto *c = H(context);
+    auto *h = new Handle();
+    h->kind = "crs_transfer";
+    h->ctx = c->ctx;
+    h->real_type = is_f32(real_type) ? SFEM_GB300_FLOAT32 : SFEM_GB300_FLOAT64;
+    auto fill = [&](auto op) {
+        op->ctx = c->ctx;
+        op->nrows = nrows;
+        op->ncols = ncols;
+        op->rowptr = rowptr;
+        op->colidx = colidx;
+        op->weights = weights;
+        op->vec = vec_size;
+        op->n_dirichlet = n_dirichlet;
+        op->dirichlet = dirichlet;
+    };
+    if (is_f32(real_type)) {
+        auto op = std::make_shared<CrsTransferOp<float>>();
+        fill(op);
+        h->f = op;
+    } else {
+        auto op = std::make_shared<CrsTransferOp<double>>();
+        fill(op);
+        h->d = op;
+    }
+    *out = h;
+    return SFEM_GB300_SUCCESS;
+}
+
+int sfem_gb300_dense_solver_create(void *context, void *op, void **out) {
+    auto *c = H(context);
+    auto *o = H(op);
+    auto *h = new Handle();
+    h->kind = "dense";
+    h->ctx = c->ctx;
+    h->real_type = o->real_type;
+    auto make = [&](auto tag) -> int {
+        using T = decltype(tag);
+        auto s = std::make_shared<DenseCoarseSolver<T>>();
+        s->blas = blas_of<T>(c->ctx);
+        s->op = op_of<T>(o);
+        op_of<T>(h) = s;
+        h->impl = s;
+        return s->setup();
+    };
+    const int rc = o->f ? make(0.0f) : make(0.0);
+    if (rc) {
+        delete h;
+        return rc;
+    }
+    *out = h;
+    return SFEM_GB300_SUCCESS;
+}
+
+int sfem_gb300_mg_set_graph(void *mg, int enable) {
+    auto *h = H(mg);
+    if (h->kind != "mg") return set_error("not a multigrid handle");
+    if (h->f) {
+        auto m = std::static_pointer_cast<Multigrid<float>>(h->impl);
+        m->release_graphs();
+        m->use_graph = enable != 0;
+    } else {
+        auto m = std::static_pointer_cast<Multigrid<double>>(h->impl);
+        m->release_graphs();
+        m->use_graph = enable != 0;
     }
     return SFEM_GB300_SUCCESS;
 }
@@ -758,9 +857,15 @@ int sfem_gb300_mg_set_harvest(void *mg, void *x_cc) {
     auto *h = H(mg);
     if (h->kind != "mg") return set_error("not a multigrid handle");
     if (h->f)
-        std::static_pointer_cast<Multigrid<float>>(h->impl)->harvest = (float *)x_cc;
-    else
-        std::static_pointer_cast<Multigrid<double>>(h->impl)->harvest = (double *)x_cc;
+    {
+        auto m = std::static_pointer_cast<Multigrid<float>>(h->impl);
+        m->harvest = (float *)x_cc;
+        m->release_graphs();
+    } else {
+        auto m = std::static_pointer_cast<Multigrid<double>>(h->impl);
+        m->harvest = (double *)x_cc;
+        m->release_graphs();
+    }
     return SFEM_GB300_SUCCESS;
 }
 
@@ -785,6 +890,35 @@ int sfem_gb300_ir_create(void *context, void *op64, void *inner32, int max_it, d
 }
 
 int sfem_gb300_solver_apply(void *solver, const void *b, void *x) { return sfem_gb300_op_apply(solver, b, x); }
+int sfem_gb300_mixed_precond_create(void *context, void *inner32, void **out) {
+    auto *c = H(context);
+    auto *in = H(inner32);
+    if (!in->f) return set_error("sfem_gb300_mixed_precond_create: inner operator must be float");
+    auto inner = in->f;
+    auto ctx = c->ctx;
+    double *slot = ctx->slots(1);
+    if (!slot) return set_error("sfem_gb300_mixed_precond_create: out of scalar slots");
+    const ptrdiff_t n = inner->rows();
+    auto r32 = std::make_shared<DeviceBuffer<float>>(n);
+    auto z32 = std::make_shared<DeviceBuffer<float>>(n);
+    if (n > 0 && (!r32->ptr || !z32->ptr)) return set_error("sfem_gb300_mixed_precond_create: allocation failed");
+    auto op = make_op<double>(n, n, [ctx, inner, slot, r32, z32, n](const double *r, double *z) {
+        void *sp = ctx->sp();
+        SFEM_GB300_CHECK(sfem_gb300_norm2(SFEM_GB300_FLOAT64, n, r, ctx->workspace, slot, sp));
+        SFEM_GB300_CHECK(sfem_gb300_scaled_to_f32(n, slot, r, r32->ptr, sp));
+        SFEM_GB300_CUDA(cudaMemsetAsync(z32->ptr, 0, n * sizeof(float), ctx->stream));
+        SFEM_GB300_CHECK(inner->apply(r32->ptr, z32->ptr));
+        return sfem_gb300_scaled_axpy_f32_to_f64(n, slot, z32->ptr, z, sp);
+    });
+    auto *h = new Handle();
+    h->kind = "mixed_precond";
+    h->ctx = ctx;
+    h->real_type = SFEM_GB300_FLOAT64;
+    h->d = op;
+    *out = h;
+    return SFEM_GB300_SUCCESS;
+}
+
 
 int sfem_gb300_solver_stats(void *solver, int *iterations, double *last_relative) {
     auto *h = H(solver);

@@ -545,6 +545,96 @@ public:
     ptrdiff_t cols() const override { return op->cols(); }
 };
 
+// Dense direct solve for a small coarsest level (no reference counterpart; the
+// reference runs an iterative coarse solver).  The operator's n x n matrix is
+// built by n applies to unit vectors, inverted once on the host by Cholesky,
+// and applied as x += A^-1 b with one dense matrix-vector kernel: no iteration
+// count, no host synchronisation.  Right-hand sides must vanish on the
+// Dirichlet dofs (as restricted residuals do).
+int dense_symv_add(int real_type, ptrdiff_t n, const void *M, const void *b, void *x, void *stream);
+
+template <typename T>
+class DenseCoarseSolver final : public Solver<T> {
+public:
+    Blas<T> blas;
+    std::shared_ptr<Operator<T>> op;
+    DeviceBuffer<T> inv;  // row-major n x n
+    static constexpr ptrdiff_t kMaxN = 1536;
+    int setup() {
+        const ptrdiff_t n = op->rows();
+        if (n > kMaxN) return set_error("DenseCoarseSolver: %td unknowns exceed the dense limit %td", n, kMaxN);
+        DeviceBuffer<T> e(n), col(n);
+        std::vector<T> hcol(n);
+        std::vector<double> A((size_t)n * n), Linv((size_t)n * n, 0.0);
+        for (ptrdiff_t j = 0; j < n; j++) {
+            blas.zeros(n, e.ptr);
+            const T one = 1;
+            SFEM_GB300_CUDA(cudaMemcpyAsync(e.ptr + j, &one, sizeof(T), cudaMemcpyHostToDevice, blas.ctx->stream));
+            blas.zeros(n, col.ptr);
+            SFEM_GB300_CHECK(op->apply(e.ptr, col.ptr));
+            SFEM_GB300_CUDA(cudaMemcpyAsync(hcol.data(), col.ptr, n * sizeof(T), cudaMemcpyDeviceToHost,
+                                            blas.ctx->stream));
+            SFEM_GB300_CUDA(cudaStreamSynchronize(blas.ctx->stream));
+            for (ptrdiff_t i = 0; i < n; i++) A[(size_t)i * n + j] = (double)hcol[i];
+        }
+        // Dirichlet dofs appear as identity rows (the operator copies constrained
+        // entries); their columns still hold couplings.  With a zero right-hand side
+        // on those dofs (restriction zeroes them) the solution is that of the matrix
+        // with the constrained columns zeroed too, which is SPD.
+        for (ptrdiff_t i = 0; i < n; i++) {
+            bool identity = A[(size_t)i * n + i] == 1.0;
+            for (ptrdiff_t j = 0; j < n && identity; j++)
+                if (j != i && A[(size_t)i * n + j] != 0.0) identity = false;
+            if (identity)
+                for (ptrdiff_t k = 0; k < n; k++)
+                    if (k != i) A[(size_t)k * n + i] = 0.0;
+        }
+        // symmetrise (the assembled operator is symmetric up to rounding), Cholesky A = L L^T
+        for (ptrdiff_t i = 0; i < n; i++)
+            for (ptrdiff_t j = 0; j < i; j++) {
+                const double v = 0.5 * (A[(size_t)i * n + j] + A[(size_t)j * n + i]);
+                A[(size_t)i * n + j] = A[(size_t)j * n + i] = v;
+            }
+        for (ptrdiff_t j = 0; j < n; j++) {
+            double d = A[(size_t)j * n + j];
+            for (ptrdiff_t k = 0; k < j; k++) d -= A[(size_t)j * n + k] * A[(size_t)j * n + k];
+            if (!(d > 0)) return set_error("DenseCoarseSolver: matrix not positive definite (pivot %td)", j);
+            d = std::sqrt(d);
+            A[(size_t)j * n + j] = d;
+            for (ptrdiff_t i = j + 1; i < n; i++) {
+                double v = A[(size_t)i * n + j];
+                for (ptrdiff_t k = 0; k < j; k++) v -= A[(size_t)i * n + k] * A[(size_t)j * n + k];
+                A[(size_t)i * n + j] = v / d;
+            }
+        }
+        // L^-1 (lower triangular), then A^-1 = L^-T L^-1
+        for (ptrdiff_t j = 0; j < n; j++) {
+            Linv[(size_t)j * n + j] = 1.0 / A[(size_t)j * n + j];
+            for (ptrdiff_t i = j + 1; i < n; i++) {
+                double v = 0;
+                for (ptrdiff_t k = j; k < i; k++) v -= A[(size_t)i * n + k] * Linv[(size_t)k * n + j];
+                Linv[(size_t)i * n + j] = v / A[(size_t)i * n + i];
+            }
+        }
+        std::vector<T> Ainv((size_t)n * n);
+        for (ptrdiff_t i = 0; i < n; i++)
+            for (ptrdiff_t j = 0; j <= i; j++) {
+                double v = 0;
+                for (ptrdiff_t k = i; k < n; k++) v += Linv[(size_t)k * n + i] * Linv[(size_t)k * n + j];
+                Ainv[(size_t)i * n + j] = Ainv[(size_t)j * n + i] = (T)v;
+            }
+        SFEM_GB300_CHECK(inv.resize(n * n));
+        SFEM_GB300_CUDA(cudaMemcpy(inv.ptr, Ainv.data(), (size_t)n * n * sizeof(T), cudaMemcpyHostToDevice));
+        return 0;
+    }
+    int apply(const T *b, T *x) override {
+        this->iterations_ = 1;
+        return dense_symv_add(real_type_v<T>, op->rows(), inv.ptr, b, x, blas.ctx->sp());
+    }
+    ptrdiff_t rows() const override { return op->rows(); }
+    ptrdiff_t cols() const override { return op->cols(); }
+};
+
 // Multigrid (algebra/sfem_Multigrid.hpp:27-354).  Level 0 is the finest.
 template <typename T>
 class Multigrid final : public Solver<T> {
@@ -625,11 +715,76 @@ public:
         }
         return 0;
     }
-    int apply(const T *b, T *x) override {
-        SFEM_GB300_CHECK(ensure_init());
+    // Graph mode: each (b, x) pair's cycles are captured once into a CUDA graph on
+    // a private stream and replayed, ordered after / before the context stream
+    // with events.  Every level operator and smoother must then be free of host
+    // synchronisation (no iterative coarse solver with convergence checks).
+    bool use_graph{false};
+    struct GraphEntry {
+        const T *b;
+        T *x;
+        cudaGraphExec_t exec;
+    };
+    std::vector<GraphEntry> graphs;
+    cudaStream_t gstream{nullptr};
+    cudaEvent_t ev_in{nullptr}, ev_out{nullptr};
+    int warm{0};
+    ~Multigrid() {
+        release_graphs();
+        if (ev_in) cudaEventDestroy(ev_in);
+        if (ev_out) cudaEventDestroy(ev_out);
+        if (gstream) cudaStreamDestroy(gstream);
+    }
+    void release_graphs() {
+        for (auto &g : graphs) cudaGraphExecDestroy(g.exec);
+        graphs.clear();
+        warm = 0;
+    }
+    int run_cycles(const T *b, T *x) {
         for (this->iterations_ = 0; this->iterations_ < max_it; this->iterations_++) {
             if (cycle(0, b, x)) break;
         }
+        return 0;
+    }
+    int apply(const T *b, T *x) override {
+        SFEM_GB300_CHECK(ensure_init());
+        if (!use_graph || atol > 0 || warm < 1) {
+            if (use_graph) warm++;  // first call eager: sizes every lazily allocated buffer
+            return run_cycles(b, x);
+        }
+        Context &c = *blas.ctx;
+        if (!gstream) {
+            SFEM_GB300_CUDA(cudaStreamCreateWithFlags(&gstream, cudaStreamNonBlocking));
+            SFEM_GB300_CUDA(cudaEventCreateWithFlags(&ev_in, cudaEventDisableTiming));
+            SFEM_GB300_CUDA(cudaEventCreateWithFlags(&ev_out, cudaEventDisableTiming));
+        }
+        cudaGraphExec_t exec = nullptr;
+        for (auto &g : graphs)
+            if (g.b == b && g.x == x) exec = g.exec;
+        SFEM_GB300_CUDA(cudaEventRecord(ev_in, c.stream));
+        SFEM_GB300_CUDA(cudaStreamWaitEvent(gstream, ev_in, 0));
+        if (!exec) {
+            if (graphs.size() >= 8) release_graphs();
+            const cudaStream_t saved = c.stream;
+            c.stream = gstream;
+            cudaGraph_t graph = nullptr;
+            cudaError_t e = cudaStreamBeginCapture(gstream, cudaStreamCaptureModeThreadLocal);
+            int rc = e == cudaSuccess ? run_cycles(b, x) : set_error("Multigrid capture: %s", cudaGetErrorString(e));
+            cudaError_t e2 = e == cudaSuccess ? cudaStreamEndCapture(gstream, &graph) : cudaSuccess;
+            c.stream = saved;
+            if (rc) {
+                if (graph) cudaGraphDestroy(graph);
+                return rc;
+            }
+            if (e2 != cudaSuccess) return set_error("Multigrid capture: %s", cudaGetErrorString(e2));
+            e = cudaGraphInstantiate(&exec, graph, 0);
+            cudaGraphDestroy(graph);
+            if (e != cudaSuccess) return set_error("Multigrid graph instantiate: %s", cudaGetErrorString(e));
+            graphs.push_back({b, x, exec});
+        }
+        SFEM_GB300_CUDA(cudaGraphLaunch(exec, gstream));
+        SFEM_GB300_CUDA(cudaEventRecord(ev_out, gstream));
+        SFEM_GB300_CUDA(cudaStreamWaitEvent(c.stream, ev_out, 0));
         return 0;
     }
     ptrdiff_t rows() const override { return levels[0].op->rows(); }

@@ -131,6 +131,26 @@ static int restrict_tpl(ptrdiff_t nelements, int from_level, idx_t **from_elemen
     return check_launch("sfem_gb300_sshex8_restrict");
 }
 
+// y[vec*i + c] = sum_k w[k] x[vec*col[k] + c]: a nested interpolation (or its
+// transpose) stored as CSR with double weights; one thread per (row, component).
+template <typename T>
+__global__ void crs_transfer_kernel(ptrdiff_t nrows, int vec, const idx_t *__restrict__ rowptr,
+                                    const idx_t *__restrict__ colidx, const double *__restrict__ w,
+                                    const T *__restrict__ x, T *__restrict__ y) {
+    const ptrdiff_t total = nrows * vec;
+    for (ptrdiff_t t = blockIdx.x * (ptrdiff_t)blockDim.x + threadIdx.x; t < total;
+         t += (ptrdiff_t)gridDim.x * blockDim.x) {
+        const ptrdiff_t i = t / vec;
+        const int c = (int)(t - i * vec);
+        double acc = 0;
+        for (idx_t k = rowptr[i]; k < rowptr[i + 1]; k++) acc += w[k] * (double)x[(ptrdiff_t)colidx[k] * vec + c];
+        y[t] = (T)acc;
+    }
+}
+
+}  // namespace sfem_gb300
+
+namespace sfem_gb300 {
 }  // namespace sfem_gb300
 
 using namespace sfem_gb300;
@@ -177,4 +197,20 @@ extern "C" int sfem_gb300_sshex8_element_node_incidence_count(int level, ptrdiff
     incidence_count_kernel<<<grid_for(total, 256, kNumSMs * 32), 256, 0, stream_of(stream)>>>(nelements, level,
                                                                                                elements, count);
     return check_launch("sfem_gb300_sshex8_element_node_incidence_count");
+}
+
+extern "C" int sfem_gb300_crs_transfer(int real_type, ptrdiff_t nrows, int vec_size, const idx_t *rowptr,
+                                       const idx_t *colidx, const double *weights, const void *x, void *y,
+                                       void *stream) {
+    if (nrows <= 0) return SFEM_GB300_SUCCESS;
+    if (vec_size < 1) return set_error("sfem_gb300_crs_transfer: vec_size must be >= 1");
+    const cudaStream_t s = stream_of(stream);
+    const int blocks = grid_for(nrows * vec_size, 256, kNumSMs * 16);
+    if (real_type == SFEM_GB300_FLOAT32)
+        crs_transfer_kernel<float><<<blocks, 256, 0, s>>>(nrows, vec_size, rowptr, colidx, weights, (const float *)x,
+                                                          (float *)y);
+    else
+        crs_transfer_kernel<double><<<blocks, 256, 0, s>>>(nrows, vec_size, rowptr, colidx, weights,
+                                                           (const double *)x, (double *)y);
+    return check_launch("sfem_gb300_crs_transfer");
 }

@@ -274,16 +274,41 @@ def upper_crs_graph(elements: np.ndarray, n_nodes: int):
     return rowptr, c.astype(np.int32)
 
 
+def _coarse_axis(n: int) -> np.ndarray:
+    """Finer-grid indices kept on a 2x coarser axis of n elements: the even ones,
+    plus the last index when n is odd (the last coarse element then spans one
+    finer element)."""
+    idx = list(range(0, n + 1, 2))
+    if n % 2:
+        idx.append(n)
+    return np.asarray(idx, dtype=np.int64)
+
+
+def _interp_1d(n: int, kept: np.ndarray) -> np.ndarray:
+    """Dense (n+1) x len(kept) linear interpolation from the kept nodes to all nodes."""
+    P = np.zeros((n + 1, kept.size))
+    for i in range(n + 1):
+        b = int(np.searchsorted(kept, i))
+        if kept[b] == i:
+            P[i, b] = 1.0
+        else:
+            a = b - 1
+            t = (i - kept[a]) / (kept[b] - kept[a])
+            P[i, a] = 1.0 - t
+            P[i, b] = t
+    return P
+
+
 class CoarseHex8Level:
     """A plain hex8 level made by coarsening a structured hex8 grid 2x in every direction.
 
     The reference's sshex8 hierarchy ends at the hex8 macro mesh, whose solve it
     hands to a coarse solver (``algebra/mg/sfem_GeometricMultigrid.cpp``).  On box
     meshes the macro grid is itself structured, so geometric multigrid can go on
-    below it: the finer grid's nodes at even positions form the coarse grid and
-    every coarse element is a 2x2x2 block of finer elements.  Seen from the coarse
-    element, the finer nodes inside it are the micro grid of a level-2 sshex8
-    element, so the level-1 -> level-2 sshex8 transfer kernels serve unchanged.
+    below it: the finer grid's nodes at even positions (and the last one of an odd
+    axis) form the coarse grid, which is nested in the finer one and keeps its
+    geometry.  The transfer is the trilinear nested interpolation P (CSR, finer
+    rows) and its transpose R.
 
     ``fine_points``: float32 ``[3, gz, gy, gx]`` coordinates of the finer grid
     nodes; ``fine_ids``: int ``[gz, gy, gx]`` their ids in the finer vector.
@@ -292,31 +317,38 @@ class CoarseHex8Level:
     """
 
     def __init__(self, fine_points: np.ndarray, fine_ids: np.ndarray):
+        from scipy import sparse
+
         gz, gy, gx = fine_ids.shape
-        if (gx - 1) % 2 or (gy - 1) % 2 or (gz - 1) % 2:
-            raise ValueError("a coarse hex8 level needs an even number of finer elements per direction")
-        cx, cy, cz = (gx - 1) // 2, (gy - 1) // 2, (gz - 1) // 2
+        kx, ky, kz = _coarse_axis(gx - 1), _coarse_axis(gy - 1), _coarse_axis(gz - 1)
+        cx, cy, cz = kx.size - 1, ky.size - 1, kz.size - 1
         self.shape = (cx, cy, cz)
         self.n_elements = cx * cy * cz
         self.n_nodes = (cx + 1) * (cy + 1) * (cz + 1)
         self.ids = np.arange(self.n_nodes, dtype=np.int64).reshape(cz + 1, cy + 1, cx + 1)
-        self.points_grid = np.ascontiguousarray(fine_points[:, ::2, ::2, ::2]).astype(np.float32)
+        self.points_grid = np.ascontiguousarray(fine_points[:, kz][:, :, ky][:, :, :, kx]).astype(np.float32)
         self.points = np.ascontiguousarray(self.points_grid.reshape(3, -1))
         e = np.arange(self.n_elements, dtype=np.int64)
         a, b, c = e % cx, (e // cx) % cy, e // (cx * cy)
         self.hex8 = np.ascontiguousarray(np.stack(
             [self.ids[c + dz, b + dy, a + dx] for dx, dy, dz in HEX8_CORNERS]).astype(np.int32))
-        # transfer view: coarse element = level-2 sshex8 element over the finer nodes
-        self.from_lidx = np.ascontiguousarray(np.stack(
-            [self.ids[c + zi, b + yi, a + xi] for zi in range(2) for yi in range(2) for xi in range(2)]).astype(np.int32))
-        self.to_lidx = np.ascontiguousarray(np.stack(
-            [fine_ids[2 * c + zi, 2 * b + yi, 2 * a + xi] for zi in range(3) for yi in range(3) for xi in range(3)]
-        ).astype(np.int32))
+        # P: finer (lexicographic, then renumbered by fine_ids) x coarse (lexicographic)
+        Px = sparse.csr_matrix(_interp_1d(gx - 1, kx))
+        Py = sparse.csr_matrix(_interp_1d(gy - 1, ky))
+        Pz = sparse.csr_matrix(_interp_1d(gz - 1, kz))
+        P = sparse.kron(Pz, sparse.kron(Py, Px)).tocsr()
+        perm = np.empty(fine_ids.size, dtype=np.int64)
+        perm[fine_ids.reshape(-1)] = np.arange(fine_ids.size)  # fine id -> lexicographic row
+        P = P[perm].tocsr()
+        P.sort_indices()
         self.n_fine_nodes = int(fine_ids.size)
-        self.fine_count = np.bincount(self.to_lidx.reshape(-1), minlength=self.n_fine_nodes).astype(np.uint16)
+        self.P = (P.indptr.astype(np.int32), P.indices.astype(np.int32), P.data.astype(np.float64))
+        R = P.T.tocsr()
+        R.sort_indices()
+        self.R = (R.indptr.astype(np.int32), R.indices.astype(np.int32), R.data.astype(np.float64))
 
     def can_coarsen(self) -> bool:
-        return all(n % 2 == 0 and n >= 2 for n in self.shape)
+        return all(n >= 2 for n in self.shape)
 
     def coarser(self) -> "CoarseHex8Level":
         return CoarseHex8Level(self.points_grid, self.ids)
@@ -337,16 +369,22 @@ def macro_level_grid(mesh: SSMesh):
     return mesh.macro_points, ids
 
 
+def coarse_shape(shape):
+    return tuple((n + 1) // 2 for n in shape)
+
+
 def macro_coarse_levels(mesh: SSMesh, min_nodes: int = 64) -> list:
-    """Coarse hex8 levels below the macro mesh, finest first, while every direction
-    halves evenly and the next level keeps at least ``min_nodes`` nodes."""
+    """Coarse hex8 levels below the macro mesh, finest first: 2x coarsening (odd axes
+    keep a thin last element) while every axis has at least 2 elements and the
+    next level keeps at least ``min_nodes`` nodes."""
     pts, ids = macro_level_grid(mesh)
     out = []
     shape = (mesh.nx, mesh.ny, mesh.nz)
-    while all(n % 2 == 0 and n >= 2 for n in shape):
-        nxt = CoarseHex8Level(pts, ids) if not out else out[-1].coarser()
-        if nxt.n_nodes < min_nodes:
+    while all(n >= 2 for n in shape):
+        cs = coarse_shape(shape)
+        if int(np.prod([n + 1 for n in cs])) < min_nodes:
             break
+        nxt = CoarseHex8Level(pts, ids) if not out else out[-1].coarser()
         out.append(nxt)
         shape = nxt.shape
     return out

@@ -170,6 +170,24 @@ def mg_add_level(mg, op, smoother, prolongation=None, restriction=None):
     mg.keep += [op, smoother, prolongation, restriction]
 
 
+def dense_solver(ctx, op) -> Handle:
+    """Dense Cholesky-inverse solve of a small SPD operator (<= 1536 unknowns)."""
+    return _create(_lib().sfem_gb300_dense_solver_create, ctx.ptr, op.ptr, keep=(ctx, op))
+
+
+def mg_set_graph(mg, enable=True):
+    capi.check(_lib().sfem_gb300_mg_set_graph(mg.ptr, int(enable)), "mg_set_graph")
+
+
+DENSE_MAX = 1536
+
+
+def mixed_precond(ctx, inner32) -> Handle:
+    """Double-precision preconditioner z = |r| inner32(r / |r|) (e.g. a float multigrid
+    V-cycle under a double flexible CG)."""
+    return _create(_lib().sfem_gb300_mixed_precond_create, ctx.ptr, inner32.ptr, keep=(ctx, inner32))
+
+
 def iterative_refinement(ctx, op64, inner32, max_it=50, rtol=1e-10) -> Handle:
     return _create(_lib().sfem_gb300_ir_create, ctx.ptr, op64.ptr, inner32.ptr, c_int(max_it), c_double(rtol),
                    keep=(ctx, op64, inner32))
@@ -180,7 +198,7 @@ def iterative_refinement(ctx, op64, inner32, max_it=50, rtol=1e-10) -> Handle:
 # ---------------------------------------------------------------------------
 class CoarseSpaceDevice:
     """A :class:`CoarseHex8Level` resident on the GPU: its hex8 operator data and the
-    transfer arrays to the next finer level (coarse element = level-2 sshex8 element)."""
+    CSR transfers to / from the next finer level."""
 
     is_macro_coarse = True
 
@@ -192,6 +210,7 @@ class CoarseSpaceDevice:
         self.element_type = capi.HEX8
         self.n_elements = lvl.n_elements
         self.n_nodes = lvl.n_nodes
+        self.n_fine_nodes = lvl.n_fine_nodes
         self.device = torch.device(device)
         t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(self.device)
         self.elements = t(lvl.hex8)
@@ -199,17 +218,22 @@ class CoarseSpaceDevice:
         self.corners_ptrs = self.elements_ptrs
         self.points = t(lvl.points)
         self.points_ptrs = capi.DevicePtrArray(self.points)
-        self.from_elements = t(lvl.from_lidx)
-        self.from_ptrs = capi.DevicePtrArray(self.from_elements)
-        self.to_elements = t(lvl.to_lidx)
-        self.to_ptrs = capi.DevicePtrArray(self.to_elements)
-        self.count = t(lvl.fine_count.view(np.int16))
+        self.P = tuple(t(a) for a in lvl.P)  # finer rows x coarse cols
+        self.R = tuple(t(a) for a in lvl.R)  # coarse rows x finer cols
 
     def dirichlet_nodes(self, faces=("x0",)):
         import torch
 
         ids = np.unique(np.concatenate([self.lvl.boundary_nodes(f) for f in faces])).astype(np.int32)
         return torch.from_numpy(ids).to(self.device)
+
+
+def crs_transfer_op(ctx, csr, nrows, ncols, vec, dirichlet_out, dtype) -> Handle:
+    """y = M x for a CSR (rowptr, colidx, weights) device triple; output Dirichlet dofs zeroed."""
+    rp, ci, w = csr
+    return _create(_lib().sfem_gb300_crs_transfer_op_create, ctx.ptr, c_int(rt_of(dtype)), capi.i64(nrows),
+                   capi.i64(ncols), capi.vp(rp), capi.vp(ci), capi.vp(w), c_int(vec), capi.i64(dirichlet_out.numel()),
+                   capi.vp(dirichlet_out), keep=(ctx, rp, ci, w, dirichlet_out))
 
 
 class Hierarchy:
@@ -272,24 +296,22 @@ class Hierarchy:
 
 def transfer_ops(ctx, H: Hierarchy, k: int, vec: int, dtype):
     """(P, R) between level k+1 (coarse) and level k (fine) of ``H``."""
-    C, F = H.spaces[k + 1], H.spaces[k]
-    if getattr(C, "is_macro_coarse", False):
-        rt = c_int(rt_of(dtype))
-        dF, dC = H.dirichlet[k], H.dirichlet[k + 1]
-        P = _create(_lib().sfem_gb300_prolongation_op_create, ctx.ptr, rt, capi.i64(C.n_elements), c_int(1),
-                    C.from_ptrs.ptr, capi.i64(C.n_nodes), c_int(2), C.to_ptrs.ptr, capi.i64(F.n_nodes), c_int(vec),
-                    capi.i64(dF.numel()), capi.vp(dF), keep=(ctx, C, F, dF))
-        R = _create(_lib().sfem_gb300_restriction_op_create, ctx.ptr, rt, capi.i64(C.n_elements), c_int(2),
-                    C.to_ptrs.ptr, capi.vp(C.count), capi.i64(F.n_nodes), c_int(1), C.from_ptrs.ptr,
-                    capi.i64(C.n_nodes), c_int(vec), capi.i64(dC.numel()), capi.vp(dC), keep=(ctx, C, F, dC))
+    C_, F = H.spaces[k + 1], H.spaces[k]
+    if getattr(C_, "is_macro_coarse", False):
+        P = crs_transfer_op(ctx, C_.P, F.n_nodes, C_.n_nodes, vec, H.dirichlet[k], dtype)
+        R = crs_transfer_op(ctx, C_.R, C_.n_nodes, F.n_nodes, vec, H.dirichlet[k + 1], dtype)
         return P, R
-    return (prolongation_op(ctx, C, F, vec, H.dirichlet[k], dtype),
-            restriction_op(ctx, F, C, vec, H.dirichlet[k + 1], dtype))
+    return (prolongation_op(ctx, C_, F, vec, H.dirichlet[k], dtype),
+            restriction_op(ctx, F, C_, vec, H.dirichlet[k + 1], dtype))
 
 
 def build_poisson_mg(ctx, H: Hierarchy, dtype, smoother="chebyshev3", sweeps=2, coarse_rtol=1e-6, coarse_max_it=10000,
-                     eig_max=None, jacobi_sweeps=3, coarse_check_every=10, eigen_max_it=30):
-    """Geometric multigrid for the Laplacian on every level of ``H`` (one V-cycle per apply)."""
+                     eig_max=None, jacobi_sweeps=3, coarse_check_every=10, eigen_max_it=30, coarse="cg", graph=False):
+    """Geometric multigrid for the Laplacian on every level of ``H`` (one V-cycle per apply).
+
+    coarse="cg": Jacobi-PCG to coarse_rtol on the coarsest level; coarse="dense": dense
+    Cholesky-inverse solve (coarsest level <= 1536 unknowns).  graph=True replays the
+    V-cycle as a CUDA graph (needs coarse="dense")."""
     import torch
 
     ops, smoothers, Ps, Rs = [], [], [], []
@@ -303,8 +325,12 @@ def build_poisson_mg(ctx, H: Hierarchy, dtype, smoother="chebyshev3", sweeps=2, 
         lap.hessian_diag(diag)
         diag[H.dirichlet[k].long()] = 1
         if k == nlev - 1:
-            jac = jacobi(ctx, diag, 1.0)
-            smoothers.append(cg(ctx, op, jac, max_it=coarse_max_it, rtol=coarse_rtol, check_every=coarse_check_every))
+            if coarse == "dense":
+                smoothers.append(dense_solver(ctx, op))
+            else:
+                jac = jacobi(ctx, diag, 1.0)
+                smoothers.append(cg(ctx, op, jac, max_it=coarse_max_it, rtol=coarse_rtol,
+                                    check_every=coarse_check_every))
         elif smoother in ("chebyshev3", "chebyshev3_plain"):
             em = None if eig_max is None else eig_max[k]
             inv = None
@@ -323,6 +349,8 @@ def build_poisson_mg(ctx, H: Hierarchy, dtype, smoother="chebyshev3", sweeps=2, 
     mg.keep += [H]
     mg.eigs = eigs
     mg.smoothers = smoothers
+    if graph:
+        mg_set_graph(mg, True)
     return mg, ops[0]
 
 
@@ -343,7 +371,7 @@ def _elasticity_diag(H: Hierarchy, k, dtype, mu, lam):
 
 def build_elasticity_mg(ctx, H: Hierarchy, dtype, mu=1.0, lam=10.0, sweeps=2, coarse_rtol=1e-6,
                         coarse_max_it=10000, eig_max=None, coarse_check_every=10, eigen_max_it=30, scale_eig_max=1.1,
-                        tensor_cores=False):
+                        tensor_cores=False, coarse="cg", graph=False):
     """Geometric multigrid for linear elasticity (3 dofs / node) on every level of ``H``:
     Jacobi-scaled Chebyshev3 smoothing, nested vector transfer, Jacobi-PCG coarse solve
     (cf. the vector branch of algebra/mg/sfem_GeometricMultigrid.cpp:89-144).
@@ -365,8 +393,11 @@ def build_elasticity_mg(ctx, H: Hierarchy, dtype, mu=1.0, lam=10.0, sweeps=2, co
         ops.append(op)
         d3 = _elasticity_diag(H, k, dtype, mu, lam)
         if k == nlev - 1:
-            smoothers.append(cg(ctx, op, jacobi(ctx, d3, 1.0), max_it=coarse_max_it, rtol=coarse_rtol,
-                                check_every=coarse_check_every))
+            if coarse == "dense":
+                smoothers.append(dense_solver(ctx, op))
+            else:
+                smoothers.append(cg(ctx, op, jacobi(ctx, d3, 1.0), max_it=coarse_max_it, rtol=coarse_rtol,
+                                    check_every=coarse_check_every))
         else:
             em = None if eig_max is None else eig_max[k]
             ch = chebyshev3(ctx, op, max_it=sweeps, eig_max=em, inv_diag=1.0 / d3, eigen_max_it=eigen_max_it,
@@ -379,4 +410,6 @@ def build_elasticity_mg(ctx, H: Hierarchy, dtype, mu=1.0, lam=10.0, sweeps=2, co
         mg_add_level(mg, ops[k], smoothers[k], P, R)
     mg.keep += [H, fine_op]
     mg.eigs = eigs
+    if graph:
+        mg_set_graph(mg, True)
     return mg, fine_op

@@ -12,9 +12,11 @@ from sfem_gb300.mesh import SSMesh
 
 pytestmark = pytest.mark.gpu
 
+# uneven sizes and levels; even edges also get hex8 levels below their macro grid
 PROBLEMS = [ProblemSpec("poisson", 4, 2, 11), ProblemSpec("poisson", 6, 2, 12), ProblemSpec("poisson", 3, 4, 13),
             ProblemSpec("poisson", 5, 3, 14), ProblemSpec("elasticity", 4, 2, 21), ProblemSpec("elasticity", 3, 3, 22),
-            ProblemSpec("elasticity", 2, 4, 23), ProblemSpec("poisson", 2, 4, 15)]
+            ProblemSpec("elasticity", 2, 4, 23), ProblemSpec("poisson", 2, 4, 15), ProblemSpec("poisson", 8, 2, 16),
+            ProblemSpec("elasticity", 4, 4, 24)]
 
 
 def _oracle_residual(p, b, x, perturb=0.1):
@@ -37,7 +39,7 @@ def _oracle_residual(p, b, x, perturb=0.1):
 
 @pytest.fixture(scope="module")
 def batch(cuda):
-    return BatchSolver(PROBLEMS, device=cuda, coarse_iterations=20, inner_iterations=8)
+    return BatchSolver(PROBLEMS, device=cuda, coarse_iterations=20)
 
 
 def test_batch_solve_matches_oracle(cuda, batch):
@@ -45,12 +47,11 @@ def test_batch_solve_matches_oracle(cuda, batch):
 
     b = batch.rhs()
     x = torch.zeros_like(b)
-    rc, lat, steps, rel, sec = batch.solve(b, x)
+    rc, lat, its, sec = batch.solve(b, x)
     assert rc == 0, capi.last_error()
-    assert (rel <= 1e-10).all(), rel
-    assert (steps >= 1).all() and (lat > 0).all() and lat.max() <= sec + 1e-9
+    assert (its >= 1).all() and (lat > 0).all() and lat.max() <= sec + 1e-9
     tr = batch.true_residuals(b, x)
-    assert (tr <= 1.01e-10).all(), tr
+    assert (tr <= 1.5e-10).all(), tr
     bh, xh = b.cpu().numpy(), x.cpu().numpy()
     for i, p in enumerate(batch.problems):
         s = slice(batch.dof_offsets[i], batch.dof_offsets[i + 1])
@@ -64,14 +65,15 @@ def test_batch_graph_matches_eager(cuda):
     probs = PROBLEMS[:3] + PROBLEMS[4:6]
     xs = []
     for g in (False, True):
-        bs = BatchSolver(probs, device=cuda, coarse_iterations=20, inner_iterations=8, use_graph=g)
+        bs = BatchSolver(probs, device=cuda, coarse_iterations=20, use_graph=g)
         b = bs.rhs()
         x = torch.zeros_like(b)
         rc, *_ = bs.solve(b, x)
         assert rc == 0, capi.last_error()
         xs.append(x)
-    # same kernels in the same order: bitwise identical
-    assert torch.equal(xs[0], xs[1])
+    # same kernels in the same order; the element scatters use float atomics, so the
+    # two runs agree to rounding, far inside the solve tolerance
+    assert float(torch.linalg.vector_norm(xs[0] - xs[1])) <= 1e-8 * float(torch.linalg.vector_norm(xs[0]))
 
 
 def test_batch_autotune_and_dot(cuda, batch):
@@ -79,12 +81,13 @@ def test_batch_autotune_and_dot(cuda, batch):
 
     b = batch.rhs()
     table = batch.autotune(b, candidates=[(1024, 128, 8), (4096, 256, 8)], reps=1)
+    assert any(g.spaces[-1].is_macro_coarse for g in batch.groups)
     assert len(table) == 2 and all(t > 0 for _, t in table)
     assert batch.tuned in [c for c, _ in table]
     x = torch.zeros_like(b)
-    rc, lat, steps, rel, sec = batch.solve(b, x)
+    rc, lat, its, sec = batch.solve(b, x)
     assert rc == 0, capi.last_error()
-    assert (batch.true_residuals(b, x) <= 1.01e-10).all()
+    assert (batch.true_residuals(b, x) <= 1.5e-10).all()
     # segmented dot against per-problem torch dots
     y = torch.randn_like(b)
     out = torch.zeros(batch.n_problems, dtype=torch.float64, device=cuda)

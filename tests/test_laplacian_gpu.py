@@ -69,6 +69,41 @@ def test_sshex8_laplacian_apply_fp32(cuda, L):
     assert err.max() < RTOL32, err.max()
 
 
+@pytest.mark.parametrize("variant", [0, 1, 2, 3])
+@pytest.mark.parametrize("L", [2, 3, 4])
+@pytest.mark.parametrize("aligned", [True, False])
+def test_sshex8_laplacian_fp32_kernels(cuda, variant, L, aligned):
+    """Every float kernel on a mesh whose element count is not a tile multiple (60 =
+    32 + 28), with connectivity rows 16-byte aligned or not (row stride E + 1)."""
+    import torch
+
+    m = SSMesh(5, 4, 3, L, perturb=0.1, seed=2)
+    el = m.elements(L)
+    E = m.n_elements
+    fff_aos = O.fff_fill(el[m.macro_corner_lidx(L)], m.points)
+    fff = torch.from_numpy(fff_aos.T.copy()).to(cuda)
+    stride = E if aligned else E + 1
+    buf = torch.zeros((el.shape[0], stride), dtype=torch.int32, device=cuda)
+    buf[:, :E] = torch.from_numpy(el).to(cuda)
+    rows = capi.DevicePtrArray(buf)
+    x = np.random.default_rng(4).standard_normal(m.n_nodes(L))
+    y0 = np.random.default_rng(5).standard_normal(m.n_nodes(L))
+    ref = O.sshex8_laplacian_apply(L, el, fff_aos, x, out=y0.copy())
+    xd = torch.from_numpy(x).float().to(cuda)
+    yd = torch.from_numpy(y0).float().to(cuda)
+    lib = capi.load()
+    prev = lib.sfem_gb300_set_laplacian_kernel(variant)
+    try:
+        capi.check(lib.cu_laplacian_apply(capi.SSHEX8(L), capi.i64(E), rows.ptr, capi.i64(E), capi.vp(fff),
+                                          capi.FLOAT32, capi.vp(xd), capi.vp(yd), None), "apply")
+        torch.cuda.synchronize()
+    finally:
+        lib.sfem_gb300_set_laplacian_kernel(prev)
+    scale = _row_scale_lap(L, el, fff_aos, x) + np.abs(y0)
+    err = np.abs(yd.double().cpu().numpy() - ref) / scale
+    assert err.max() < RTOL32, (variant, L, aligned, err.max())
+
+
 def test_hex8_laplacian_apply_and_diag(cuda):
     import torch
 

@@ -171,3 +171,22 @@ def test_patchconv_oracle_matches_torch_autograd():
         assert np.abs(xt.grad.permute(0, 2, 3, 4, 1).reshape(P, 125, cin).numpy() - gin).max() < 1e-11
         dW = O.patchconv_backward_weights(P, cin, cout, g, x)
         assert np.abs(Wt.grad.reshape(-1).numpy() - dW).max() < 1e-11
+
+
+def test_float32_configuration_apply():
+    """The float32 restatement (reference number configuration SFEM_REAL_TYPE=float32)
+    agrees with the FP64 apply to float rounding and keeps its symmetry."""
+    from sfem_gb300.mesh import SSMesh
+
+    L = 4
+    m = SSMesh(3, 3, 2, L, perturb=0.1, seed=4)
+    el = m.elements(L)
+    fff = O.fff_fill(el[m.macro_corner_lidx(L)], m.points)
+    rng = np.random.default_rng(2)
+    x, z = rng.standard_normal(m.n_nodes()), rng.standard_normal(m.n_nodes())
+    a = O.sshex8_laplacian_apply(L, el, fff, x)
+    b = O.sshex8_laplacian_apply_f32(L, el, fff, x)
+    assert b.dtype == np.float32
+    assert np.abs(a - b).max() <= 1e-5 * np.abs(a).max()
+    zb = O.sshex8_laplacian_apply_f32(L, el, fff, z)
+    assert abs(float(z.astype(np.float32) @ b) - float(x.astype(np.float32) @ zb)) <= 1e-4 * abs(float(z @ a))

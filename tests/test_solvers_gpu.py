@@ -222,7 +222,7 @@ def test_elasticity_mg_pcg_and_mixed(cuda, coarsen):
         b[3 * dn + c] = 0
     ctx = S.context()
     mg, op = S.build_elasticity_mg(ctx, H, torch.float64, mu=mu, lam=lam)
-    solver = S.cg(ctx, op, mg, rtol=1e-10, max_it=300, residual_norm=True, flexible=True)
+    solver = S.cg(ctx, op, mg, rtol=5e-11, max_it=300, residual_norm=True, flexible=True)
     bd = torch.from_numpy(b).to(cuda)
     x = torch.zeros_like(bd)
     assert S.solve(solver, bd, x) == 0
@@ -234,12 +234,19 @@ def test_elasticity_mg_pcg_and_mixed(cuda, coarsen):
     for tc in (False, True):
         mg32, op32 = S.build_elasticity_mg(ctx, H, torch.float32, mu=mu, lam=lam, eig_max=mg.eigs, tensor_cores=tc)
         inner = S.cg(ctx, op32, mg32, rtol=1e-4, max_it=40, residual_norm=True, flexible=True)
-        ir = S.iterative_refinement(ctx, op64, inner, max_it=30, rtol=1e-10)
+        ir = S.iterative_refinement(ctx, op64, inner, max_it=30, rtol=5e-11)
         x2 = torch.zeros_like(bd)
         assert S.solve(ir, bd, x2) == 0, tc
         res2 = np.linalg.norm(b - apply(x2.cpu().numpy())) / np.linalg.norm(b)
         assert res2 < 1e-10, (tc, res2)
         assert np.linalg.norm(x2.cpu().numpy() - x.cpu().numpy()) < 1e-8 * np.linalg.norm(x.cpu().numpy()), tc
+    # FP64 flexible CG preconditioned by the FP32 multigrid (float only inside the V-cycle)
+    mg32, _ = S.build_elasticity_mg(ctx, H, torch.float32, mu=mu, lam=lam, eig_max=mg.eigs)
+    solver = S.cg(ctx, op64, S.mixed_precond(ctx, mg32), rtol=5e-11, max_it=300, residual_norm=True, flexible=True)
+    x3 = torch.zeros_like(bd)
+    assert S.solve(solver, bd, x3) == 0
+    res3 = np.linalg.norm(b - apply(x3.cpu().numpy())) / np.linalg.norm(b)
+    assert res3 < 1e-10, res3
 
 
 def test_cg_options_true_residual_and_check_every(cuda):
@@ -264,3 +271,48 @@ def test_cg_options_true_residual_and_check_every(cuda):
         assert res < 1.5e-10, res
         its.append(S.stats(solver)[0])
     assert its[0] <= its[1] < its[0] + 7
+
+
+@pytest.mark.parametrize("kind", ["poisson", "elasticity"])
+def test_dense_coarse_and_graph_vcycle(cuda, kind):
+    """Dense Cholesky coarse solve + CUDA-graph V-cycle: the coarse solve is exact, the
+    graph replay reproduces the eager V-cycle, and FCG converges to the oracle residual."""
+    import torch
+
+    L = 4
+    vec = 3 if kind == "elasticity" else 1
+    m = SSMesh(4, 4, 4, L, perturb=0.05, seed=9)
+    H = S.Hierarchy(m, dirichlet_faces=("x0",), device=cuda, vec=vec, coarsen_macro=True, min_coarse_nodes=8)
+    ctx = S.context()
+    build = S.build_elasticity_mg if kind == "elasticity" else S.build_poisson_mg
+    # coarse exactness: A (A^-1 b) = b on the coarsest level
+    cs = H.spaces[-1]
+    if kind == "elasticity":
+        cop = S.elasticity_op(ctx, cs, cs.adj, cs.det, 1.0, 10.0, H.dirichlet[-1], torch.float64)
+    else:
+        cop = S.laplacian_op(ctx, cs, cs.fff, H.dirichlet[-1], torch.float64)
+    ds = S.dense_solver(ctx, cop)
+    bc = torch.randn(vec * cs.n_nodes, dtype=torch.float64, device=cuda)
+    xc = torch.zeros_like(bc)
+    S.solve(ds, bc, xc)
+    r = torch.zeros_like(bc)
+    S.apply(cop, xc, r)
+    assert float(torch.linalg.vector_norm(r - bc) / torch.linalg.vector_norm(bc)) < 1e-10
+    # eager vs graph V-cycle on the fine level
+    mg_e, op = build(ctx, H, torch.float64, coarse="dense")
+    mg_g, _ = build(ctx, H, torch.float64, coarse="dense", graph=True, eig_max=mg_e.eigs)
+    b = torch.randn(vec * H.spaces[0].n_nodes, dtype=torch.float64, device=cuda)
+    b[(vec * H.dirichlet[0].long()[:, None] + torch.arange(vec, device=cuda)).reshape(-1)] = 0
+    outs = []
+    for mg in (mg_e, mg_g, mg_g, mg_g):  # graph: eager warm-up, capture, replay
+        x = torch.zeros_like(b)
+        S.solve(mg, b, x)
+        outs.append(x)
+    for o in outs[1:]:
+        assert float(torch.linalg.vector_norm(o - outs[0])) <= 1e-12 * float(torch.linalg.vector_norm(outs[0]))
+    solver = S.cg(ctx, op, mg_g, rtol=1e-10, max_it=100, residual_norm=True, flexible=True)
+    x = torch.zeros_like(b)
+    assert S.solve(solver, b, x) == 0
+    r = torch.zeros_like(b)
+    S.apply(op, x, r)
+    assert float(torch.linalg.vector_norm(b - r) / torch.linalg.vector_norm(b)) < 2e-10
