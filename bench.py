@@ -240,7 +240,7 @@ def _timed_solve(S, solver, b, x):
 def measure_solves(m, dev, rtol=1e-10):
     """Time to ||b - A x|| / ||b|| <= rtol (FP64, true residual) on the same problem and
     hierarchy (sshex8 levels 4, 2, 1, then hex8 levels coarsening the macro grid;
-    Chebyshev3 V(2,2); Jacobi-PCG 1e-6 on the coarsest level):
+    Chebyshev3 V(2,2); dense coarsest solve; V-cycles replayed as CUDA graphs):
       plain: FP64 flexible CG + FP64 multigrid;
       mixed_ir: FP64 iterative refinement around FP32 CG + FP32 multigrid;
       mixed_precond: FP64 flexible CG preconditioned by the FP32 multigrid
@@ -257,7 +257,8 @@ def measure_solves(m, dev, rtol=1e-10):
     ctx = S.context()
     op64 = S.laplacian_op(ctx, H.spaces[0], H.fff, H.dirichlet[0], torch.float64)
     out = {"levels_nodes": [sp.n_nodes for sp in H.spaces], "rtol": rtol,
-           "smoother": "Jacobi-scaled Chebyshev3 V(2,2)", "coarse": "Jacobi-PCG 1e-6 on the coarsest hex8 level"}
+           "smoother": "Jacobi-scaled Chebyshev3 V(2,2)", "coarse": "dense Cholesky inverse on the coarsest hex8 level",
+           "vcycle": "CUDA graph replay"}
 
     def true_rel(x):
         r = torch.zeros_like(b)
@@ -265,7 +266,7 @@ def measure_solves(m, dev, rtol=1e-10):
         return float(torch.linalg.vector_norm(b - r) / torch.linalg.vector_norm(b))
 
     t0 = time.perf_counter()
-    mg64, _ = S.build_poisson_mg(ctx, H, torch.float64, smoother="chebyshev3", sweeps=2)
+    mg64, _ = S.build_poisson_mg(ctx, H, torch.float64, smoother="chebyshev3", sweeps=2, coarse="dense", graph=True)
     torch.cuda.synchronize()
     setup64 = time.perf_counter() - t0
     cg64 = S.cg(ctx, op64, mg64, rtol=rtol, max_it=500, residual_norm=True, flexible=True)
@@ -276,7 +277,8 @@ def measure_solves(m, dev, rtol=1e-10):
     x64 = x.clone()
     xn = float(torch.linalg.vector_norm(x64))
     t0 = time.perf_counter()
-    mg32, op32 = S.build_poisson_mg(ctx, H, torch.float32, smoother="chebyshev3", sweeps=2, eig_max=mg64.eigs)
+    mg32, op32 = S.build_poisson_mg(ctx, H, torch.float32, smoother="chebyshev3", sweeps=2, eig_max=mg64.eigs,
+                                    coarse="dense", graph=True)
     torch.cuda.synchronize()
     setup32 = time.perf_counter() - t0
     inner = S.cg(ctx, op32, mg32, rtol=1e-4, max_it=30, residual_norm=True, flexible=True)
@@ -315,11 +317,11 @@ def lumped_body_force(m, det):
     return b
 
 
-def measure_elasticity_solves(dev, nx=64, ny=16, nz=16, rtol=1e-9, mu=1.0, lam=10.0, coarse_max_it=50):
+def measure_elasticity_solves(dev, nx=64, ny=16, nz=16, rtol=1e-9, mu=1.0, lam=10.0):
     """Cantilever 4x1x1, macro 64x16x16 at L=4, clamped at x=0, lumped body force (0,0,-1):
     plain FP64 flexible CG + FP64 multigrid against the same CG preconditioned by the
-    FP32 multigrid, time to a true FP64 residual of rtol.  Same hierarchy and coarse
-    solve (Jacobi-PCG, at most coarse_max_it iterations) for both.  rtol is 1e-9:
+    FP32 multigrid, time to a true FP64 residual of rtol.  Same hierarchy, smoother,
+    dense coarsest solve and graph-replayed V-cycles for both.  rtol is 1e-9:
     |A||x| / |b| of the clamped 4:1 cantilever puts the FP64 evaluation floor of the
     residual itself near 5e-10, which both methods reach and neither can go below."""
     import torch
@@ -341,16 +343,17 @@ def measure_elasticity_solves(dev, nx=64, ny=16, nz=16, rtol=1e-9, mu=1.0, lam=1
         return float(torch.linalg.vector_norm(b - r) / torch.linalg.vector_norm(b))
 
     out = {"dofs": 3 * m.n_nodes(), "macro_elements": m.n_elements, "levels_nodes": [sp.n_nodes for sp in H.spaces],
-           "rtol": rtol, "coarse": f"Jacobi-PCG 1e-6, <= {coarse_max_it} iterations"}
-    mg64, _ = S.build_elasticity_mg(ctx, H, torch.float64, mu=mu, lam=lam, coarse_max_it=coarse_max_it)
+           "rtol": rtol, "smoother": "Jacobi-scaled Chebyshev3 V(2,2)",
+           "coarse": "dense Cholesky inverse on the coarsest hex8 level", "vcycle": "CUDA graph replay"}
+    mg64, _ = S.build_elasticity_mg(ctx, H, torch.float64, mu=mu, lam=lam, coarse="dense", graph=True)
     cg64 = S.cg(ctx, op64, mg64, rtol=rtol, max_it=500, residual_norm=True, flexible=True)
     x = torch.zeros_like(b)
     rc, t64 = _timed_solve(S, cg64, b, x)
     out["plain_fp64_mg_pcg"] = {"seconds": t64, "iterations": S.stats(cg64)[0], "true_rel_residual": true_rel(x),
                                 "rc": rc}
     x64 = x.clone()
-    mg32, _ = S.build_elasticity_mg(ctx, H, torch.float32, mu=mu, lam=lam, eig_max=mg64.eigs,
-                                    coarse_max_it=coarse_max_it)
+    mg32, _ = S.build_elasticity_mg(ctx, H, torch.float32, mu=mu, lam=lam, eig_max=mg64.eigs, coarse="dense",
+                                    graph=True)
     pc = S.mixed_precond(ctx, mg32)
     cgm = S.cg(ctx, op64, pc, rtol=rtol, max_it=500, residual_norm=True, flexible=True)
     x = torch.zeros_like(b)

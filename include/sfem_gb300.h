@@ -81,9 +81,11 @@ int cu_laplacian_diag(int element_type, ptrdiff_t nelements, sfem_gb300_idx_t **
                       const void *fff, int real_type_diag, void *diag, void *stream);
 
 /* Kernel used for float sshex8 applies (process-wide tuning knob, no reference
- * counterpart): 0 shared-memory staged tile (default), 1 warp per element,
- * 2 thread per element in registers, 3 cp.async staged tile with two threads per
- * element (even L; other levels use the default).  Returns the previous value. */
+ * counterpart): -1 per-level default, 0 shared-memory staged tile, 1 warp per
+ * element, 2 thread per element in registers, 3 cp.async staged tile with two
+ * threads per element, 4 persistent cp.async pipeline with one warp per micro
+ * layer (3 and 4: even L; other levels use the staged tile).  Returns the previous
+ * setting (-1 if none was forced). */
 int sfem_gb300_set_laplacian_kernel(int variant);
 
 /* ------------------------------------------------------- linear elasticity */
@@ -378,7 +380,8 @@ int sfem_gb300_learned_smoother_create(void *context, void *op, sfem_gb300_idx_t
                                        const void *W3, int channels, double omega, int sweeps, void *fallback,
                                        void **solver);
 int sfem_gb300_learned_smoother_use_fallback(void *solver, int use_fallback);
-/* chain != 0: apply the fallback smoother first, then the learned corrections. */
+/* chain 1: the fallback smoother first, then the learned corrections; chain 2: the
+ * learned corrections first (on the coarse-grid-corrected iterate), then the fallback. */
 int sfem_gb300_learned_smoother_set_chain(void *solver, int chain);
 /* Let a CG (residual not decreasing for 2 checks) or an iterative refinement (FP64
  * residual not halved by an outer step) switch the learned smoother to its fallback. */

@@ -274,7 +274,7 @@ class BatchSolver:
     """Mixed-precision batched solver over a list of :class:`ProblemSpec`."""
 
     def __init__(self, problems, device="cuda:0", sweeps=2, coarse_iterations=20, rtol=1e-10, max_it=300,
-                 check_every=5, tensor_cores=False, use_graph=True, eigen_max_it=20, perturb=0.1,
+                 check_every=5, tensor_cores=False, use_graph=True, eigen_max_it=40, perturb=0.1,
                  coarse_min_nodes=27):
         import torch
 
@@ -305,7 +305,7 @@ class BatchSolver:
                     sop = g.op(ctx, k, torch.float32, tensor_cores=tensor_cores and g.kind == "elasticity")
                     inv = (1.0 / d).contiguous()
                     sm = S._create(lib.sfem_gb300_batch_chebyshev3_create, ctx.ptr, lay.ptr, sop.ptr, capi.vp(inv),
-                                   c_int(sweeps), c_double(1.1 if g.kind == "elasticity" else 1.02), c_double(0.06),
+                                   c_int(sweeps), c_double(1.1 if g.kind == "elasticity" else 1.05), c_double(0.06),
                                    c_int(eigen_max_it), C.c_ulonglong(S.RANDOM_SEED), keep=(ctx, lay, sop, inv))
                 P, R = g.transfer(ctx, k, torch.float32) if k + 1 < nlev else (None, None)
                 S.mg_add_level(mg, op, sm, P, R)

@@ -581,6 +581,149 @@ __global__ void __launch_bounds__(2 * TILE, 6) sshex8_laplacian_apply_async_kern
     }
 }
 
+// v5 (float bandwidth path, persistent and pipelined): each CTA of L warps loops
+// over tiles of TILE = 32 consecutive macro elements.  While tile t is applied,
+// the x gathers of tile t+G (G = grid size) and the connectivity + metric rows of
+// tile t+2G are in flight (cp.async into three index stages and two x stages),
+// so HBM streams continuously instead of stopping at every tile's barriers.
+// Warp q applies micro layer q of all 32 elements (lane = element); the two
+// partial sums of each inner plane are combined in shared memory after the
+// layer pass.  Same packed FP32x2 / inversion-symmetry arithmetic as v4.
+template <int L, int TILE>
+__device__ __forceinline__ void pipe_load_rows(const idx_t *const *elements, const float *fff, ptrdiff_t fff_stride,
+                                               ptrdiff_t e0, int nvalid, idx_t *sidx, float *sfff) {
+    constexpr int N1 = L + 1;
+    constexpr int NXE = N1 * N1 * N1;
+    constexpr int NT = 32 * L;
+    constexpr int Q = TILE / 4;  // 16-byte chunks per row segment
+    for (int t = threadIdx.x; t < NXE * Q; t += NT) {
+        const int v = t / Q, q = t % Q;
+        const idx_t *row = elements[v] + e0;
+        if (nvalid == TILE && ((reinterpret_cast<uintptr_t>(row) & 15) == 0)) {
+            cp_async16(&sidx[v * TILE + 4 * q], row + 4 * q);
+        } else {
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+                if (4 * q + k < nvalid) cp_async4(&sidx[v * TILE + 4 * q + k], row + 4 * q + k);
+        }
+    }
+    for (int t = threadIdx.x; t < 6 * TILE; t += NT) {
+        const int m = t / TILE, el = t % TILE;
+        if (el < nvalid) cp_async4(&sfff[t], fff + m * fff_stride + e0 + el);
+    }
+}
+
+template <int L, int TILE>
+__device__ __forceinline__ void pipe_gather(const float *__restrict__ x, const idx_t *sidx, int nvalid, float *sx) {
+    constexpr int N1 = L + 1;
+    constexpr int NXE = N1 * N1 * N1;
+    constexpr int NT = 32 * L;
+    for (int t = threadIdx.x; t < NXE * TILE; t += NT)
+        if (t % TILE < nvalid) cp_async4(&sx[t], x + sidx[t]);
+}
+
+template <int L, int TILE>
+__global__ void __launch_bounds__(32 * L, 2) sshex8_laplacian_apply_pipe_kernel(ptrdiff_t nelements,
+                                                                              const idx_t *const *elements,
+                                                                              ptrdiff_t fff_stride,
+                                                                              const float *fff,
+                                                                              const float *__restrict__ x,
+                                                                              float *__restrict__ y) {
+    constexpr int N1 = L + 1;
+    constexpr int NP = N1 * N1;
+    constexpr int NXE = NP * N1;
+    constexpr int NT = 32 * L;
+    constexpr int SI = NXE * TILE;  // one stage of indices or values
+    extern __shared__ __align__(16) unsigned char smem_pipe[];
+    idx_t *sidx = reinterpret_cast<idx_t *>(smem_pipe);              // [3][SI]
+    float *sx = reinterpret_cast<float *>(sidx + 3 * SI);            // [2][SI]
+    float *sfff = sx + 2 * SI;                                       // [3][6 * TILE]
+    const ptrdiff_t ntiles = (nelements + TILE - 1) / TILE;
+    const ptrdiff_t G = gridDim.x;
+    auto nvalid_of = [&](ptrdiff_t t) {
+        const ptrdiff_t r = nelements - t * TILE;
+        return (int)(r < TILE ? r : TILE);
+    };
+    const int q = threadIdx.x >> 5;  // micro layer of this warp
+    const int el = threadIdx.x & 31;
+    ptrdiff_t t = blockIdx.x;
+    if (t >= ntiles) return;
+    // prologue: rows of t and t+G, gather of t
+    pipe_load_rows<L, TILE>(elements, fff, fff_stride, t * TILE, nvalid_of(t), sidx, sfff);
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+    if (t + G < ntiles)
+        pipe_load_rows<L, TILE>(elements, fff, fff_stride, (t + G) * TILE, nvalid_of(t + G), sidx + SI,
+                                sfff + 6 * TILE);
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+    asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+    __syncthreads();
+    pipe_gather<L, TILE>(x, sidx, nvalid_of(t), sx);
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+    for (int k = 0; t < ntiles; k++, t += G) {
+        const int si = k % 3, sxs = k & 1;
+        const int nvalid = nvalid_of(t);
+        cp_async_wait_all();  // x(t) and the rows of t+G
+        __syncthreads();
+        if (t + G < ntiles) pipe_gather<L, TILE>(x, sidx + ((k + 1) % 3) * SI, nvalid_of(t + G), sx + (sxs ^ 1) * SI);
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
+        if (t + 2 * G < ntiles)
+            pipe_load_rows<L, TILE>(elements, fff, fff_stride, (t + 2 * G) * TILE, nvalid_of(t + 2 * G),
+                                    sidx + ((k + 2) % 3) * SI, sfff + ((k + 2) % 3) * 6 * TILE);
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
+        // element matrix of this lane's element
+        float2 A2[8][2];
+        {
+            const float *ff = sfff + si * 6 * TILE + el;
+            const float h = 1.f / (float)L;
+            float f[6];
+#pragma unroll
+            for (int m = 0; m < 6; m++) f[m] = el < nvalid ? ff[m * TILE] * h : 0.f;
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+#pragma unroll
+                for (int kk = 0; kk < 2; kk++) {
+                    float a0 = 0.f, a1 = 0.f;
+#pragma unroll
+                    for (int m = 0; m < 6; m++) {
+                        const double w0 = LapTable().w[(2 * kk) * 8 + j][m];
+                        const double w1 = LapTable().w[(2 * kk + 1) * 8 + j][m];
+                        if (w0 != 0.0) a0 += f[m] * (float)w0;
+                        if (w1 != 0.0) a1 += f[m] * (float)w1;
+                    }
+                    A2[j][kk] = make_float2(a0, a1);
+                }
+            }
+        }
+        float *col = sx + sxs * SI + el;
+        float lo[NP], up[NP];
+#pragma unroll
+        for (int p = 0; p < NP; p++) {
+            lo[p] = 0.f;
+            up[p] = 0.f;
+        }
+        lap_layer_f32x2<L, TILE>(col + q * NP * TILE, A2, lo, up);
+        __syncthreads();  // every x read of this tile is done
+#pragma unroll
+        for (int p = 0; p < NP; p++) col[((q + 1) * NP + p) * TILE] = up[p];
+        if (q == 0) {
+#pragma unroll
+            for (int p = 0; p < NP; p++) col[p * TILE] = lo[p];
+        }
+        __syncthreads();
+        if (q > 0) {
+#pragma unroll
+            for (int p = 0; p < NP; p++) col[(q * NP + p) * TILE] += lo[p];
+        }
+        __syncthreads();
+        const idx_t *ri = sidx + si * SI;
+        const float *rv = sx + sxs * SI;
+        for (int i = threadIdx.x; i < SI; i += NT)
+            if (i % TILE < nvalid) atomicAdd(&y[ri[i]], rv[i]);
+        __syncthreads();  // stage buffers of t are free
+    }
+    cp_async_wait_all();
+}
+
 // Diagonal: node value = sum over the micro elements of this macro element that
 // contain it of A[a][a] (a = the node's corner in that micro element).
 template <typename T, int L>
@@ -623,16 +766,21 @@ __global__ void __launch_bounds__(128) sshex8_laplacian_diag_kernel(ptrdiff_t ne
 
 // ------------------------------------------------------------------ dispatch
 
-// Kernel variant override for benchmarking (SFEM_GB300_LAPLACIAN_KERNEL):
-// default / "staged" (0) = shared-memory staged tile kernel for float, L <= 4;
+// Kernel variant override for benchmarking (SFEM_GB300_LAPLACIAN_KERNEL or
+// sfem_gb300_set_laplacian_kernel); without one, float applies pick per level
+// (L=4 async tile, L=2 thread per element, L=3 staged tile).
+// "staged" (0) = shared-memory staged tile kernel for float, L <= 4;
 // "warp" (1) = warp per element; "thread" (2) = registers-only thread per element;
-// "async" (3) = cp.async staged tile, two threads per element, packed FP32x2 FMAs (even L).
+// "async" (3) = cp.async staged tile, two threads per element, packed FP32x2 FMAs (even L);
+// "pipe" (4) = persistent CTAs, cp.async pipeline across tiles, one warp per micro layer (even L).
 static int g_laplacian_variant = -1;
+static int g_laplacian_variant_forced = 0;  // set by sfem_gb300_set_laplacian_kernel
 static int laplacian_variant() {
     int v = __atomic_load_n(&g_laplacian_variant, __ATOMIC_RELAXED);
     if (v < 0) {
         const char *e = getenv("SFEM_GB300_LAPLACIAN_KERNEL");
-        v = (e && e[0] == 'w') ? 1 : (e && e[0] == 't') ? 2 : (e && e[0] == 'a') ? 3 : 0;
+        v = (e && e[0] == 'w') ? 1 : (e && e[0] == 't') ? 2 : (e && e[0] == 'a') ? 3 : (e && e[0] == 'p') ? 4 : 0;
+        if (e && e[0]) __atomic_store_n(&g_laplacian_variant_forced, 1, __ATOMIC_RELAXED);
         __atomic_store_n(&g_laplacian_variant, v, __ATOMIC_RELAXED);
     }
     return v;
@@ -648,7 +796,9 @@ static int laplacian_apply_tpl(int element_type, ptrdiff_t nelements, idx_t **el
     }
     const int L = element_type - SFEM_GB300_SSHEX8_BASE;
     const int blocks = grid_for((nelements + 3) / 4, 1, kNumSMs * 64);
-    const int variant = laplacian_variant();
+    // default per level (measured at 7.2M nodes): L=4 async tile, L=2 thread per element, else staged tile
+    int variant = laplacian_variant();
+    if (__atomic_load_n(&g_laplacian_variant_forced, __ATOMIC_RELAXED) == 0) variant = (L == 4) ? 3 : (L == 2) ? 2 : 0;
     if (sizeof(T) == 4 && L >= 2 && L <= 4 && variant == 0) {
         constexpr int TILE = 64;
         const int tb = (int)((nelements + TILE - 1) / TILE);
@@ -669,6 +819,29 @@ static int laplacian_apply_tpl(int element_type, ptrdiff_t nelements, idx_t **el
                 break;
         }
         return check_launch("cu_laplacian_apply(SSHEX8, staged tile)");
+    }
+    if (sizeof(T) == 4 && (L == 2 || L == 4) && variant == 4) {
+        constexpr int TILE = 32;
+        const ptrdiff_t ntiles = (nelements + TILE - 1) / TILE;
+        auto launch = [&](auto kernel, int LL) {
+            const int nxe = (LL + 1) * (LL + 1) * (LL + 1);
+            const size_t smem = (size_t)5 * nxe * TILE * sizeof(float) + 3 * 6 * TILE * sizeof(float);
+            static int per_sm_cache[8] = {0};  // CTAs per SM, set on first use of each level
+            int per_sm = per_sm_cache[LL];
+            if (per_sm == 0) {
+                cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 32 * LL, smem);
+                if (per_sm < 1) per_sm = 1;
+                per_sm_cache[LL] = per_sm;
+            }
+            const ptrdiff_t grid = std::min<ptrdiff_t>(ntiles, (ptrdiff_t)kNumSMs * per_sm);
+            kernel<<<(int)grid, 32 * LL, smem, s>>>(nelements, elements, fff_stride, fff, (const float *)x, (float *)y);
+        };
+        if (L == 2)
+            launch(sshex8_laplacian_apply_pipe_kernel<2, TILE>, 2);
+        else
+            launch(sshex8_laplacian_apply_pipe_kernel<4, TILE>, 4);
+        return check_launch("cu_laplacian_apply(SSHEX8, pipelined tile)");
     }
     if (sizeof(T) == 4 && (L == 2 || L == 4) && variant == 3) {
         constexpr int TILE = 32;
@@ -795,8 +968,10 @@ extern "C" int cu_laplacian_diag(int element_type, ptrdiff_t nelements, idx_t **
 }
 
 extern "C" int sfem_gb300_set_laplacian_kernel(int variant) {
-    if (variant < 0 || variant > 3) return set_error("sfem_gb300_set_laplacian_kernel: variant must be 0..3");
-    const int prev = laplacian_variant();
-    __atomic_store_n(&g_laplacian_variant, variant, __ATOMIC_RELAXED);
+    if (variant < -1 || variant > 4) return set_error("sfem_gb300_set_laplacian_kernel: variant must be -1..4");
+    const int cur = laplacian_variant();
+    const int prev = __atomic_load_n(&g_laplacian_variant_forced, __ATOMIC_RELAXED) ? cur : -1;
+    __atomic_store_n(&g_laplacian_variant, variant < 0 ? 0 : variant, __ATOMIC_RELAXED);
+    __atomic_store_n(&g_laplacian_variant_forced, variant < 0 ? 0 : 1, __ATOMIC_RELAXED);
     return prev;
 }

@@ -728,10 +728,11 @@ int sfem_gb300_solver_fallback_used(void *solver, int *used) {
 int sfem_gb300_learned_smoother_set_chain(void *solver, int chain) {
     auto *h = H(solver);
     if (h->kind != "learned") return set_error("not a learned-smoother handle");
+    if (chain < 0 || chain > 2) return set_error("sfem_gb300_learned_smoother_set_chain: chain must be 0, 1 or 2");
     if (h->f)
-        std::static_pointer_cast<LearnedSmoother<float>>(h->impl)->chain = chain != 0;
+        std::static_pointer_cast<LearnedSmoother<float>>(h->impl)->chain = chain;
     else
-        std::static_pointer_cast<LearnedSmoother<double>>(h->impl)->chain = chain != 0;
+        std::static_pointer_cast<LearnedSmoother<double>>(h->impl)->chain = chain;
     return SFEM_GB300_SUCCESS;
 }
 

@@ -362,7 +362,7 @@ public:
     int channels{16}, sweeps{1};
     double omega{1.0};
     bool use_fallback{false};
-    bool chain{false};        // apply the fallback first, then the learned corrections
+    int chain{0};  // 1: the fallback smoother first, then the learned corrections; 2: learned first, then fallback
     bool line_search{true};   // step length minimising the energy norm of the error along the correction
     DeviceBuffer<T> r, d, Ad;
     DeviceBuffer<uint16_t> a0, a1, a2, a3;  // BF16 activations
@@ -373,8 +373,13 @@ public:
     // device.  For SPD A that alpha minimises ||x* - x - alpha d||_A, so a poor
     // correction can only be scaled down, never increase the error energy.
     int apply(const T *b, T *x) override {
-        if (fallback && (chain || use_fallback)) SFEM_GB300_CHECK(fallback->apply(b, x));
+        if (fallback && (chain == 1 || use_fallback)) SFEM_GB300_CHECK(fallback->apply(b, x));
         if (use_fallback) return 0;
+        SFEM_GB300_CHECK(learned_sweeps(b, x));
+        if (fallback && chain == 2) SFEM_GB300_CHECK(fallback->apply(b, x));
+        return 0;
+    }
+    int learned_sweeps(const T *b, T *x) {
         const ptrdiff_t n = op->rows();
         const ptrdiff_t P = nelements;
         SFEM_GB300_CHECK(r.resize(n));
@@ -549,8 +554,7 @@ public:
 // reference runs an iterative coarse solver).  The operator's n x n matrix is
 // built by n applies to unit vectors, inverted once on the host by Cholesky,
 // and applied as x += A^-1 b with one dense matrix-vector kernel: no iteration
-// count, no host synchronisation.  Right-hand sides must vanish on the
-// Dirichlet dofs (as restricted residuals do).
+// count, no host synchronisation.
 int dense_symv_add(int real_type, ptrdiff_t n, const void *M, const void *b, void *x, void *stream);
 
 template <typename T>
@@ -578,16 +582,21 @@ public:
             for (ptrdiff_t i = 0; i < n; i++) A[(size_t)i * n + j] = (double)hcol[i];
         }
         // Dirichlet dofs appear as identity rows (the operator copies constrained
-        // entries); their columns still hold couplings.  With a zero right-hand side
-        // on those dofs (restriction zeroes them) the solution is that of the matrix
-        // with the constrained columns zeroed too, which is SPD.
+        // entries) while their columns keep the couplings: M = [[A_II, A_ID], [0, I]].
+        // Factor the SPD part (constrained columns zeroed) and fold the couplings
+        // back in afterwards: M^-1 = S^-1 (I - N), N = the zeroed couplings.
+        std::vector<ptrdiff_t> constrained;
+        std::vector<double> coupling;  // column d's couplings, per constrained dof
         for (ptrdiff_t i = 0; i < n; i++) {
             bool identity = A[(size_t)i * n + i] == 1.0;
             for (ptrdiff_t j = 0; j < n && identity; j++)
                 if (j != i && A[(size_t)i * n + j] != 0.0) identity = false;
-            if (identity)
-                for (ptrdiff_t k = 0; k < n; k++)
-                    if (k != i) A[(size_t)k * n + i] = 0.0;
+            if (!identity) continue;
+            constrained.push_back(i);
+            for (ptrdiff_t k = 0; k < n; k++) {
+                coupling.push_back(k != i ? A[(size_t)k * n + i] : 0.0);
+                if (k != i) A[(size_t)k * n + i] = 0.0;
+            }
         }
         // symmetrise (the assembled operator is symmetric up to rounding), Cholesky A = L L^T
         for (ptrdiff_t i = 0; i < n; i++)
@@ -616,13 +625,24 @@ public:
                 Linv[(size_t)i * n + j] = v / A[(size_t)i * n + i];
             }
         }
-        std::vector<T> Ainv((size_t)n * n);
+        std::vector<double> Sinv((size_t)n * n);
         for (ptrdiff_t i = 0; i < n; i++)
             for (ptrdiff_t j = 0; j <= i; j++) {
                 double v = 0;
                 for (ptrdiff_t k = i; k < n; k++) v += Linv[(size_t)k * n + i] * Linv[(size_t)k * n + j];
-                Ainv[(size_t)i * n + j] = Ainv[(size_t)j * n + i] = (T)v;
+                Sinv[(size_t)i * n + j] = Sinv[(size_t)j * n + i] = v;
             }
+        std::vector<T> Ainv((size_t)n * n);
+        for (size_t k = 0; k < Sinv.size(); k++) Ainv[k] = (T)Sinv[k];
+        for (size_t c = 0; c < constrained.size(); c++) {
+            const ptrdiff_t d = constrained[c];
+            const double *cp = &coupling[c * (size_t)n];
+            for (ptrdiff_t r = 0; r < n; r++) {
+                double v = Sinv[(size_t)r * n + d];
+                for (ptrdiff_t k = 0; k < n; k++) v -= Sinv[(size_t)r * n + k] * cp[k];
+                Ainv[(size_t)r * n + d] = (T)v;
+            }
+        }
         SFEM_GB300_CHECK(inv.resize(n * n));
         SFEM_GB300_CUDA(cudaMemcpy(inv.ptr, Ainv.data(), (size_t)n * n * sizeof(T), cudaMemcpyHostToDevice));
         return 0;

@@ -25,6 +25,7 @@ import numpy as np
 
 from . import capi
 from . import solvers as S
+from .mesh import coarsen_coefficient
 
 CH = 16
 
@@ -124,13 +125,17 @@ def _gather(space_lidx_ptrs, P, v, scale, out, pscale, dtype):
                                                 capi.vp(scale), capi.vp(out), capi.vp(pscale), None), "gather")
 
 
-def harvest(H, dtype, cycles=4, n_patches=None, seed=0, rhs=None, mg=None, ctx=None, point="cycle"):
+def harvest(H, dtype, cycles=4, n_patches=None, seed=0, rhs=None, mg=None, ctx=None, point="cycle", target="local"):
     """(input, target) BF16 patch pairs from plain V-cycles on the hierarchy ``H``.
 
     point="cycle": pairs (D^-1 r_k, e_k) after every complete V-cycle of the stationary
     iteration x_{k+1} = x_k + MG(b - A x_k) (what a correction applied after the cycle's
     post-smoothing sees); point="coarse": after each coarse-grid correction of the finest
-    level, before post-smoothing."""
+    level, before post-smoothing.
+
+    target="local": the error patch minus its trilinear interpolant from the 8 macro
+    corners, i.e. the part of the error the coarse levels cannot represent and the
+    patch residual can predict; target="full": the error patch itself."""
     import torch
 
     ctx = ctx or S.context()
@@ -171,7 +176,11 @@ def harvest(H, dtype, cycles=4, n_patches=None, seed=0, rhs=None, mg=None, ctx=N
         # target: e patches scaled by the input patch's RMS
         _gather(fine.lidx_ptrs, P, e, None, tmp, torch.empty_like(ps), dtype)
         tscale = _patch_rms(e, fine, P, dtype)
-        tgt = (tmp.float() * (tscale / ps)[:, None]).to(torch.bfloat16)
+        tgt = tmp.float() * (tscale / ps)[:, None]
+        if target == "local":
+            W, corners = _corner_interp(dev)
+            tgt = tgt - tgt[:, corners] @ W.T
+        tgt = tgt.to(torch.bfloat16)
         ins.append(pin.clone())
         tgts.append(tgt)
     if point == "coarse":
@@ -183,6 +192,26 @@ def harvest(H, dtype, cycles=4, n_patches=None, seed=0, rhs=None, mg=None, ctx=N
         idx = idx[:n_patches]
         xin, xt = xin[idx], xt[idx]
     return xin, xt
+
+
+def _corner_interp(device, L=4):
+    """([125, 8] trilinear weights, the 8 corner positions) of an (L+1)^3 micro grid, lidx order."""
+    import torch
+
+    n1 = L + 1
+    corners = [(cz * n1 + cy) * n1 + cx for cz in (0, L) for cy in (0, L) for cx in (0, L)]
+    t = np.arange(n1) / L
+    W = np.zeros((n1 ** 3, 8))
+    for z in range(n1):
+        for y in range(n1):
+            for x in range(n1):
+                k = 0
+                for wz in (1 - t[z], t[z]):
+                    for wy in (1 - t[y], t[y]):
+                        for wx in (1 - t[x], t[x]):
+                            W[(z * n1 + y) * n1 + x, k] = wz * wy * wx
+                            k += 1
+    return torch.from_numpy(W).float().to(device), torch.tensor(corners, device=device)
 
 
 def _patch_rms(v, space, P, dtype):
@@ -226,13 +255,16 @@ def train(net: PatchNet, xin, xt, epochs=20, batch=4096, lr=2e-3, seed=0, log=No
     return history
 
 
-def learned_mg(ctx, H, net: PatchNet, dtype, omega=1.0, sweeps=1, eig_max=None, post_only=False, chain=True):
+def learned_mg(ctx, H, net: PatchNet, dtype, omega=1.0, sweeps=1, eig_max=None, post_only=False, chain=True,
+               **mg_kwargs):
     """Multigrid with the learned smoother on the finest level.
 
-    chain=True (default): the finest-level post-smoother is Chebyshev3 followed by the
-    learned correction (pre-smoothing unchanged), matching point="cycle" training data.
-    chain=False: the learned smoother replaces Chebyshev3 (pre and post unless post_only)."""
-    mg, op = S.build_poisson_mg(ctx, H, dtype, smoother="chebyshev3", sweeps=2, eig_max=eig_max)
+    chain="before" : the finest-level post-smoothing is the learned correction of the
+    coarse-grid-corrected iterate followed by Chebyshev3 (matches point="coarse" data);
+    chain=True (or "after"): Chebyshev3 followed by the learned correction (matches
+    point="cycle" data); chain=False: the learned smoother replaces Chebyshev3 (pre and
+    post unless post_only)."""
+    mg, op = S.build_poisson_mg(ctx, H, dtype, smoother="chebyshev3", sweeps=2, eig_max=eig_max, **mg_kwargs)
     fine = H.spaces[0]
     inv_diag = fine_inv_diag(H, dtype)
     lib = _lib()
@@ -244,7 +276,7 @@ def learned_mg(ctx, H, net: PatchNet, dtype, omega=1.0, sweeps=1, eig_max=None, 
         C.byref(out)), "learned smoother")
     ls = S.Handle(out, keep=(ctx, op, inv_diag, net, ch))
     if chain:
-        capi.check(lib.sfem_gb300_learned_smoother_set_chain(ls.ptr, 1), "chain")
+        capi.check(lib.sfem_gb300_learned_smoother_set_chain(ls.ptr, 2 if chain == "before" else 1), "chain")
         capi.check(lib.sfem_gb300_mg_set_post_smoother(mg.ptr, 0, ls.ptr), "post smoother")
     elif post_only:
         capi.check(lib.sfem_gb300_mg_set_post_smoother(mg.ptr, 0, ls.ptr), "post smoother")
@@ -271,28 +303,44 @@ def fallback_used(solver) -> bool:
     return bool(v.value)
 
 
-def hierarchy_with_coefficient(mesh, k, device, base=None):
-    """Hierarchy of ``mesh`` whose metric is scaled per macro element by ``k`` (reuses ``base``'s device mesh)."""
+def hierarchy_with_coefficient(mesh, k, device, base=None, coarsen_macro=True):
+    """Hierarchy of ``mesh`` whose metric is scaled per macro element by ``k`` (reuses
+    ``base``'s device mesh).  The metrics are rescaled in place, so every level and
+    every operator built on them sees the coefficient; hex8 levels below the macro
+    mesh take the mean of their children's coefficients."""
     import torch
 
     if base is None:
-        base = S.Hierarchy(mesh, dirichlet_faces=("x0",), device=device)
-        base.fff_unscaled = base.fff.clone()
-    kt = torch.as_tensor(k, dtype=torch.float32, device=base.device)
-    base.fff = (base.fff_unscaled * kt[None, :]).contiguous()
+        base = S.Hierarchy(mesh, dirichlet_faces=("x0",), device=device, coarsen_macro=coarsen_macro)
+        base.fff_unscaled = [sp.fff.clone() for sp in base.spaces]
+    kk = np.asarray(k, dtype=np.float64).reshape(mesh.nz, mesh.ny, mesh.nx)
+    for i, sp in enumerate(base.spaces):
+        if getattr(sp, "is_macro_coarse", False):
+            cx, cy, cz = sp.lvl.shape
+            kk = coarsen_coefficient(kk, (cz, cy, cx))
+            kt = torch.as_tensor(kk.reshape(-1), dtype=torch.float32, device=base.device)
+        else:
+            kt = torch.as_tensor(np.asarray(k, dtype=np.float64), dtype=torch.float32, device=base.device)
+        sp.fff.copy_(base.fff_unscaled[i] * kt[None, :])
     return base
 
 
 def run_experiment(nx=32, draws=64, n_pairs=100_000, epochs=30, eval_draws=2, device="cuda:0", seed=0, log=None,
-                   rtol=1e-10, dtype_name="float64"):
-    """Train on ``draws`` coefficient fields, then A/B FCG(MG + learned correction) against FCG(MG)."""
+                   rtol=1e-10, placement="before", arms=("chebyshev3", "learned", "mixed", "mixed_learned")):
+    """Train on ``draws`` coefficient fields, then A/B on fresh draws: FP64 flexible CG
+    preconditioned by the FP64 multigrid (chebyshev3), the same plus the learned correction
+    (learned), the FP32 multigrid through the precision bridge (mixed), and that plus the
+    learned correction (mixed_learned).
+
+    placement="before": pairs harvested after each coarse-grid correction of the finest
+    level and the correction applied there, before the Chebyshev3 post-smoothing;
+    "after": pairs after complete V-cycles, correction after the post-smoothing."""
     import torch
 
     from .coefficients import lognormal_coefficient
     from .mesh import SSMesh
 
     dev = torch.device(device)
-    dtype = torch.float64 if dtype_name == "float64" else torch.float32
     mesh = SSMesh(nx, nx, nx, 4)
     H = None
     per_draw = max(1, n_pairs // draws)
@@ -302,7 +350,8 @@ def run_experiment(nx=32, draws=64, n_pairs=100_000, epochs=30, eval_draws=2, de
     for d in range(draws):
         k = lognormal_coefficient(nx, nx, nx, ell=8.0 * nx / 32.0, sigma=1.0, seed=seed + 1000 + d)
         H = hierarchy_with_coefficient(mesh, k, dev, H)
-        xin, xt = harvest(H, torch.float32, cycles=3, n_patches=per_draw, seed=seed + d, ctx=ctx)
+        xin, xt = harvest(H, torch.float32, cycles=3, n_patches=per_draw, seed=seed + d, ctx=ctx,
+                          point="coarse" if placement == "before" else "cycle")
         xs.append(xin)
         ts.append(xt)
     xin, xt = torch.cat(xs), torch.cat(ts)
@@ -313,21 +362,30 @@ def run_experiment(nx=32, draws=64, n_pairs=100_000, epochs=30, eval_draws=2, de
     torch.cuda.synchronize()
     t_train = time.perf_counter() - t0
     results = []
+    chain = "before" if placement == "before" else True
     for d in range(eval_draws):
         k = lognormal_coefficient(nx, nx, nx, ell=8.0 * nx / 32.0, sigma=1.0, seed=seed + 5000 + d)
         H = hierarchy_with_coefficient(mesh, k, dev, H)
         g = torch.Generator(device=dev).manual_seed(seed + 77 + d)
-        b = torch.randn(H.spaces[0].n_nodes, dtype=dtype, device=dev, generator=g)
+        b = torch.randn(H.spaces[0].n_nodes, dtype=torch.float64, device=dev, generator=g)
         b[H.dirichlet[0].long()] = 0
         row = {}
-        for name in ("chebyshev3", "learned"):
+        # FP64 flexible CG in every arm; the preconditioner differs: FP64 multigrid with or
+        # without the learned correction, FP32 multigrid (bridged) with or without it
+        for name in arms:
             ctx = S.context()
-            if name == "learned":
-                mg, op = learned_mg(ctx, H, net, dtype)
+            learned_arm = name.endswith("learned")
+            if name in ("chebyshev3", "learned"):
+                mg, op = (learned_mg(ctx, H, net, torch.float64, chain=chain, coarse="dense") if learned_arm else
+                          S.build_poisson_mg(ctx, H, torch.float64, smoother="chebyshev3", sweeps=2, coarse="dense"))
+                pc, op64 = mg, op
             else:
-                mg, op = S.build_poisson_mg(ctx, H, dtype, smoother="chebyshev3", sweeps=2)
-            solver = S.cg(ctx, op, mg, rtol=rtol, max_it=500, residual_norm=True, flexible=True)
-            if name == "learned":
+                mg, _ = (learned_mg(ctx, H, net, torch.float32, chain=chain, coarse="dense") if learned_arm else
+                         S.build_poisson_mg(ctx, H, torch.float32, smoother="chebyshev3", sweeps=2, coarse="dense"))
+                op64 = S.laplacian_op(ctx, H.spaces[0], H.spaces[0].fff, H.dirichlet[0], torch.float64)
+                pc = S.mixed_precond(ctx, mg)
+            solver = S.cg(ctx, op64, pc, rtol=rtol, max_it=500, residual_norm=True, flexible=True)
+            if learned_arm:
                 set_fallback(solver, mg)
             x = torch.zeros_like(b)
             torch.cuda.synchronize()
@@ -336,12 +394,13 @@ def run_experiment(nx=32, draws=64, n_pairs=100_000, epochs=30, eval_draws=2, de
             torch.cuda.synchronize()
             dt = time.perf_counter() - t1
             r = torch.zeros_like(b)
-            S.apply(op, x, r)
+            S.apply(op64, x, r)
             true_rel = float(torch.linalg.vector_norm(b - r) / torch.linalg.vector_norm(b))
             it, _ = S.stats(solver)
             row[name] = {"iterations": it, "seconds": dt, "true_rel_residual": true_rel, "rc": rc,
-                         "fallback_used": fallback_used(solver) if name == "learned" else False}
+                         "fallback_used": fallback_used(solver) if learned_arm else False}
         results.append(row)
-    return {"nx": nx, "draws": draws, "pairs": int(xin.shape[0]), "epochs": epochs, "loss_first": hist[0],
+    return {"nx": nx, "draws": draws, "pairs": int(xin.shape[0]), "epochs": epochs, "placement": placement,
+            "loss_first": hist[0],
             "loss_last": hist[-1], "harvest_seconds": t_harvest, "train_seconds": t_train, "eval": results,
             "net": net}

@@ -388,3 +388,16 @@ def macro_coarse_levels(mesh: SSMesh, min_nodes: int = 64) -> list:
         out.append(nxt)
         shape = nxt.shape
     return out
+
+
+def coarsen_coefficient(k: np.ndarray, shape) -> np.ndarray:
+    """Per-element coefficient ``k[z, y, x]`` of a grid, averaged onto its 2x coarser grid
+    of ``shape`` (z, y, x): the mean of the (up to 2x2x2) children of each coarse element
+    (an odd axis ends in a thin element with one child layer)."""
+    out = np.asarray(k, dtype=np.float64)
+    for axis, n in enumerate(shape):
+        m = out.shape[axis]
+        parts = [np.take(out, list(range(2 * i, min(2 * i + 2, m))), axis=axis).mean(axis=axis, keepdims=True)
+                 for i in range(n)]
+        out = np.concatenate(parts, axis=axis)
+    return out

@@ -16,7 +16,7 @@ import ctypes as C
 import numpy as np
 
 from . import capi
-from .mesh import CoarseHex8Level, SSMesh, macro_coarse_levels
+from .mesh import CoarseHex8Level, SSMesh, coarsen_coefficient, macro_coarse_levels
 from .operators import Laplacian, SSMeshDevice
 
 c_double = C.c_double
@@ -275,7 +275,7 @@ class Hierarchy:
         for sp in self.spaces[self.n_sshex8_levels:]:
             if k is not None:
                 cx, cy, cz = sp.lvl.shape
-                k = k.reshape(cz, 2, cy, 2, cx, 2).mean(axis=(1, 3, 5))
+                k = coarsen_coefficient(k, (cz, cy, cx))
             sp.fff = Laplacian(sp, coefficient=None if k is None else k.reshape(-1)).initialize().fff
             sp.adj, sp.det = self._adjugate(sp)
 

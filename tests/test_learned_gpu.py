@@ -84,7 +84,8 @@ def test_learned_smoother_pipeline_small(cuda):
     trained correction does not cost iterations against the same MG without it."""
     from sfem_gb300 import learned
 
-    res = learned.run_experiment(nx=8, draws=4, n_pairs=8000, epochs=8, eval_draws=1, device=str(cuda))
+    res = learned.run_experiment(nx=8, draws=4, n_pairs=8000, epochs=8, eval_draws=1, device=str(cuda),
+                                 placement="before")
     assert res["loss_last"] < res["loss_first"]
     row = res["eval"][0]
     for name in ("chebyshev3", "learned"):

@@ -292,7 +292,7 @@ def test_dense_coarse_and_graph_vcycle(cuda, kind):
     else:
         cop = S.laplacian_op(ctx, cs, cs.fff, H.dirichlet[-1], torch.float64)
     ds = S.dense_solver(ctx, cop)
-    bc = torch.randn(vec * cs.n_nodes, dtype=torch.float64, device=cuda)
+    bc = torch.randn(vec * cs.n_nodes, dtype=torch.float64, device=cuda)  # nonzero on Dirichlet dofs too
     xc = torch.zeros_like(bc)
     S.solve(ds, bc, xc)
     r = torch.zeros_like(bc)
