@@ -55,6 +55,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-solve", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--no-learned", action="store_true")
     ap.add_argument("--batch-problems", type=int, default=256)
     return ap.parse_args()
 
@@ -365,6 +366,33 @@ def measure_elasticity_solves(dev, nx=64, ny=16, nz=16, rtol=1e-9, mu=1.0, lam=1
     return out
 
 
+def measure_learned(dev, nx=32, draws=64, n_pairs=100_000, epochs=20, eval_draws=2):
+    """Config 4: sshex8 L=4 on a 32^3 macro mesh, k = exp(g) per macro element (GRF,
+    sigma 1, correlation length 8 macro elements), N(0,1) rhs.  The 3-layer BF16 conv
+    smoother is trained by the project's kernels on 10^5 residual/error pairs from plain
+    V-cycles on 64 coefficient draws, then every arm solves fresh draws to FP64 1e-10
+    with flexible CG: FP64 multigrid (plain), + learned correction, FP32 multigrid
+    through the precision bridge (mixed), + learned correction (mixed_learned)."""
+    from sfem_gb300 import learned
+
+    res = learned.run_experiment(nx=nx, draws=draws, n_pairs=n_pairs, epochs=epochs, eval_draws=eval_draws,
+                                 device=str(dev), placement="before")
+    arms = list(res["eval"][0].keys())
+    out = {"nx": nx, "draws": draws, "pairs": res["pairs"], "epochs": epochs, "placement": res["placement"],
+           "loss_first": res["loss_first"], "loss_last": res["loss_last"], "harvest_seconds": res["harvest_seconds"],
+           "train_seconds": res["train_seconds"]}
+    for a in arms:
+        rows = [r[a] for r in res["eval"]]
+        out[a] = {"seconds": float(np.mean([r["seconds"] for r in rows])),
+                  "iterations": [r["iterations"] for r in rows],
+                  "true_rel_residual_max": max(r["true_rel_residual"] for r in rows),
+                  "rc": max(r["rc"] for r in rows), "fallback_used": any(r["fallback_used"] for r in rows)}
+    base = out["chebyshev3"]["seconds"]
+    for a in arms:
+        out[f"speedup_{a}_vs_plain_fp64"] = base / out[a]["seconds"]
+    return out
+
+
 def measure_batch(dev, count=256, seed=0):
     """Batched serving: ``count`` uneven Poisson / elasticity problems (cube edge 8..32
     macro elements, L in {2, 3, 4}, perturbation 0.1 h, N(0,1) rhs, seeded) solved
@@ -486,6 +514,8 @@ def run_ours(args):
     if not args.no_solve:
         solve = {"poisson_sshex8_L4_48cube": measure_solves(m, dev),
                  "elasticity_sshex8_L4_64x16x16": measure_elasticity_solves(dev)}
+        if not args.no_learned:
+            solve["learned_smoother_32cube"] = measure_learned(dev)
         if not args.no_batch:
             solve["batched_serving"] = measure_batch(dev, args.batch_problems)
 

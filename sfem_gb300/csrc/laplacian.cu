@@ -233,6 +233,13 @@ __global__ void __launch_bounds__(128) sshex8_laplacian_apply_tpe_kernel(ptrdiff
                                                                          const T *__restrict__ x, T *__restrict__ y) {
     constexpr int N1 = L + 1;
     constexpr int NP = N1 * N1;
+    constexpr int NXE = NP * N1;
+    // the row pointers in shared memory: one global load each per block instead of
+    // one per thread and row ahead of every dependent index load
+    __shared__ const idx_t *srow_tpe[NXE];
+    for (int v = threadIdx.x; v < NXE; v += blockDim.x) srow_tpe[v] = elements[v];
+    __syncthreads();
+    const idx_t *const *rows = srow_tpe;
     const ptrdiff_t e = blockIdx.x * (ptrdiff_t)blockDim.x + threadIdx.x;
     if (e >= nelements) return;
     const T h = T(1) / T(L);
@@ -253,14 +260,14 @@ __global__ void __launch_bounds__(128) sshex8_laplacian_apply_tpe_kernel(ptrdiff
     T xa[NP], xb[NP], ya[NP], yb[NP];
 #pragma unroll
     for (int p = 0; p < NP; p++) {
-        xa[p] = __ldg(&x[__ldg(&elements[p][e])]);
+        xa[p] = __ldg(&x[__ldg(&rows[p][e])]);
         ya[p] = 0;
     }
 #pragma unroll
     for (int zi = 0; zi < L; zi++) {
 #pragma unroll
         for (int p = 0; p < NP; p++) {
-            xb[p] = __ldg(&x[__ldg(&elements[(zi + 1) * NP + p][e])]);
+            xb[p] = __ldg(&x[__ldg(&rows[(zi + 1) * NP + p][e])]);
             yb[p] = 0;
         }
 #pragma unroll
@@ -290,7 +297,7 @@ __global__ void __launch_bounds__(128) sshex8_laplacian_apply_tpe_kernel(ptrdiff
 #pragma unroll
         for (int p = 0; p < NP; p++) {
             const int xi = p % N1, yi = p / N1;
-            const idx_t g = __ldg(&elements[zi * NP + p][e]);
+            const idx_t g = __ldg(&rows[zi * NP + p][e]);
             if (zi > 0 && xi > 0 && xi < L && yi > 0 && yi < L)
                 y[g] += ya[p];
             else
@@ -303,7 +310,7 @@ __global__ void __launch_bounds__(128) sshex8_laplacian_apply_tpe_kernel(ptrdiff
         }
     }
 #pragma unroll
-    for (int p = 0; p < NP; p++) atomicAdd(&y[__ldg(&elements[L * NP + p][e])], ya[p]);
+    for (int p = 0; p < NP; p++) atomicAdd(&y[__ldg(&rows[L * NP + p][e])], ya[p]);
 }
 
 // v3 (bandwidth path, staged): a CTA owns a tile of TILE consecutive macro
@@ -494,13 +501,16 @@ __global__ void __launch_bounds__(2 * TILE, 6) sshex8_laplacian_apply_async_kern
     __shared__ __align__(16) idx_t sidx[NXE * TILE];
     __shared__ __align__(16) float sx[NXE * TILE];
     __shared__ float spart[NP * TILE];  // upper half's partial sum of the shared plane
+    __shared__ const idx_t *srow[NXE];  // the row pointers: one global load each, then shared
     const int tid = threadIdx.x;
     const ptrdiff_t e0 = (ptrdiff_t)blockIdx.x * TILE;
     const int nvalid = (int)((nelements - e0) < TILE ? (nelements - e0) : TILE);
+    for (int v = tid; v < NXE; v += 2 * TILE) srow[v] = elements[v];
+    __syncthreads();
     // 1. connectivity rows
     for (int v = tid / (TILE / 4); v < NXE; v += (2 * TILE) / (TILE / 4)) {
         const int q = tid % (TILE / 4);  // 16-byte quarter of the row segment
-        const idx_t *row = elements[v] + e0;
+        const idx_t *row = srow[v] + e0;
         if (nvalid == TILE && ((reinterpret_cast<uintptr_t>(row) & 15) == 0)) {
             cp_async16(&sidx[v * TILE + 4 * q], row + 4 * q);
         } else {
@@ -590,7 +600,7 @@ __global__ void __launch_bounds__(2 * TILE, 6) sshex8_laplacian_apply_async_kern
 // partial sums of each inner plane are combined in shared memory after the
 // layer pass.  Same packed FP32x2 / inversion-symmetry arithmetic as v4.
 template <int L, int TILE>
-__device__ __forceinline__ void pipe_load_rows(const idx_t *const *elements, const float *fff, ptrdiff_t fff_stride,
+__device__ __forceinline__ void pipe_load_rows(const idx_t *const *srow, const float *fff, ptrdiff_t fff_stride,
                                                ptrdiff_t e0, int nvalid, idx_t *sidx, float *sfff) {
     constexpr int N1 = L + 1;
     constexpr int NXE = N1 * N1 * N1;
@@ -598,7 +608,7 @@ __device__ __forceinline__ void pipe_load_rows(const idx_t *const *elements, con
     constexpr int Q = TILE / 4;  // 16-byte chunks per row segment
     for (int t = threadIdx.x; t < NXE * Q; t += NT) {
         const int v = t / Q, q = t % Q;
-        const idx_t *row = elements[v] + e0;
+        const idx_t *row = srow[v] + e0;
         if (nvalid == TILE && ((reinterpret_cast<uintptr_t>(row) & 15) == 0)) {
             cp_async16(&sidx[v * TILE + 4 * q], row + 4 * q);
         } else {
@@ -638,6 +648,9 @@ __global__ void __launch_bounds__(32 * L, 2) sshex8_laplacian_apply_pipe_kernel(
     idx_t *sidx = reinterpret_cast<idx_t *>(smem_pipe);              // [3][SI]
     float *sx = reinterpret_cast<float *>(sidx + 3 * SI);            // [2][SI]
     float *sfff = sx + 2 * SI;                                       // [3][6 * TILE]
+    __shared__ const idx_t *srow[NXE];                               // row pointers, loaded once
+    for (int v = threadIdx.x; v < NXE; v += NT) srow[v] = elements[v];
+    __syncthreads();
     const ptrdiff_t ntiles = (nelements + TILE - 1) / TILE;
     const ptrdiff_t G = gridDim.x;
     auto nvalid_of = [&](ptrdiff_t t) {
@@ -649,10 +662,10 @@ __global__ void __launch_bounds__(32 * L, 2) sshex8_laplacian_apply_pipe_kernel(
     ptrdiff_t t = blockIdx.x;
     if (t >= ntiles) return;
     // prologue: rows of t and t+G, gather of t
-    pipe_load_rows<L, TILE>(elements, fff, fff_stride, t * TILE, nvalid_of(t), sidx, sfff);
+    pipe_load_rows<L, TILE>(srow, fff, fff_stride, t * TILE, nvalid_of(t), sidx, sfff);
     asm volatile("cp.async.commit_group;\n" ::: "memory");
     if (t + G < ntiles)
-        pipe_load_rows<L, TILE>(elements, fff, fff_stride, (t + G) * TILE, nvalid_of(t + G), sidx + SI,
+        pipe_load_rows<L, TILE>(srow, fff, fff_stride, (t + G) * TILE, nvalid_of(t + G), sidx + SI,
                                 sfff + 6 * TILE);
     asm volatile("cp.async.commit_group;\n" ::: "memory");
     asm volatile("cp.async.wait_group 1;\n" ::: "memory");
@@ -667,7 +680,7 @@ __global__ void __launch_bounds__(32 * L, 2) sshex8_laplacian_apply_pipe_kernel(
         if (t + G < ntiles) pipe_gather<L, TILE>(x, sidx + ((k + 1) % 3) * SI, nvalid_of(t + G), sx + (sxs ^ 1) * SI);
         asm volatile("cp.async.commit_group;\n" ::: "memory");
         if (t + 2 * G < ntiles)
-            pipe_load_rows<L, TILE>(elements, fff, fff_stride, (t + 2 * G) * TILE, nvalid_of(t + 2 * G),
+            pipe_load_rows<L, TILE>(srow, fff, fff_stride, (t + 2 * G) * TILE, nvalid_of(t + 2 * G),
                                     sidx + ((k + 2) % 3) * SI, sfff + ((k + 2) % 3) * 6 * TILE);
         asm volatile("cp.async.commit_group;\n" ::: "memory");
         // element matrix of this lane's element

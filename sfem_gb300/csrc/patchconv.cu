@@ -13,6 +13,8 @@
 // weights in shared memory.
 #include <cuda_bf16.h>
 
+#include <algorithm>
+
 #include "common.cuh"
 
 namespace sfem_gb300 {
@@ -233,6 +235,224 @@ __global__ void adam_kernel(int n, float *w, const float *g, float *m, float *v,
     }
 }
 
+// ---------------------------------------------------------------------------- fused inference
+// The learned correction of the smoother in one kernel: gather + RMS normalise,
+// the three convolutions on the tensor cores (mma.sync m16n8k16, BF16 operands,
+// FP32 accumulate, BF16 activations between layers exactly as the layer kernels
+// above store them), and the averaged scatter.  One warp per patch; a patch is a
+// GEMM with M = 128 positions (125 used), N = 16 channels, K = 27 taps x C_in:
+// conv1 K = 32 (27 taps padded), conv2 and conv3 one k-tile of 16 input channels
+// per tap.  Activations live in shared memory as [padded position][channel]
+// rows of 32 bytes, so a k-tile of A is one ldmatrix.x4 from 16 row addresses.
+constexpr int LC_WARPS = 4;
+constexpr int LC_ROWS = PPV + 1;  // padded positions + one zero row for unused GEMM rows
+constexpr int LC_BF1 = 2 * 2 * 32;   // uint2 fragments: [k-tile][n-tile][lane]
+constexpr int LC_BF2 = 27 * 2 * 32;  // [tap][n-tile][lane]
+constexpr int LC_BF3 = 27 * 32;      // [tap][lane] (n-tile 0, column 0 only)
+
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
+    const __nv_bfloat16 a = __float2bfloat16(lo), b = __float2bfloat16(hi);
+    return (uint32_t)__bfloat16_as_ushort(a) | ((uint32_t)__bfloat16_as_ushort(b) << 16);
+}
+__device__ __forceinline__ uint32_t pack_bf16_raw(__nv_bfloat16 a, __nv_bfloat16 b) {
+    return (uint32_t)__bfloat16_as_ushort(a) | ((uint32_t)__bfloat16_as_ushort(b) << 16);
+}
+
+__device__ __forceinline__ void mma_bf16_16816(float (&c)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+    asm volatile(
+            "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+            "{%0,%1,%2,%3};\n"
+            : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+            : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+__device__ __forceinline__ void ldmatrix_x4(uint32_t (&a)[4], const void *smem_row) {
+    const unsigned addr = (unsigned)__cvta_generic_to_shared(smem_row);
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(a[0]), "=r"(a[1]), "=r"(a[2]), "=r"(a[3])
+                 : "r"(addr));
+}
+
+// B fragments of the three layers from the [co][ci][27] BF16 weights.  Fragment of
+// lane (g = lane/4, q = lane%4): b0 = (B[2q][g], B[2q+1][g]), b1 = (B[2q+8][g], B[2q+9][g]).
+__global__ void learned_fragments_kernel(const __nv_bfloat16 *__restrict__ W1, const __nv_bfloat16 *__restrict__ W2,
+                                         const __nv_bfloat16 *__restrict__ W3, uint2 *__restrict__ frag) {
+    const __nv_bfloat16 zero = __float2bfloat16(0.f);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < LC_BF1 + LC_BF2 + LC_BF3; i += gridDim.x * blockDim.x) {
+        const int lane = i % 32, g = lane >> 2, q = lane & 3;
+        uint2 f;
+        if (i < LC_BF1) {  // conv1: B[k = tap][n = co] = W1[co][0][tap]
+            const int j = (i / 32) % 2, kt = i / 64;
+            auto w = [&](int k) { const int tap = 16 * kt + k; return tap < 27 ? W1[(8 * j + g) * 27 + tap] : zero; };
+            f.x = pack_bf16_raw(w(2 * q), w(2 * q + 1));
+            f.y = pack_bf16_raw(w(2 * q + 8), w(2 * q + 9));
+        } else if (i < LC_BF1 + LC_BF2) {  // conv2 tap t: B[ci][co] = W2[co][ci][t]
+            const int k = i - LC_BF1, j = (k / 32) % 2, t = k / 64;
+            auto w = [&](int ci) { return W2[((8 * j + g) * KMAX_C + ci) * 27 + t]; };
+            f.x = pack_bf16_raw(w(2 * q), w(2 * q + 1));
+            f.y = pack_bf16_raw(w(2 * q + 8), w(2 * q + 9));
+        } else {  // conv3 tap t: column 0 = W3[0][ci][t], columns 1..7 zero
+            const int t = (i - LC_BF1 - LC_BF2) / 32;
+            auto w = [&](int ci) { return g == 0 ? W3[ci * 27 + t] : zero; };
+            f.x = pack_bf16_raw(w(2 * q), w(2 * q + 1));
+            f.y = pack_bf16_raw(w(2 * q + 8), w(2 * q + 9));
+        }
+        frag[i] = f;
+    }
+}
+
+// d[g] += omega * s_p * net(patch_p)[v] / count[g] for every patch p (g = elements[v][p])
+template <typename T>
+__global__ void __launch_bounds__(32 * LC_WARPS, 2) learned_correction_kernel(
+        ptrdiff_t P, const idx_t *const *elements, const T *__restrict__ r, const T *__restrict__ inv_diag,
+        const uint2 *__restrict__ frag_g, const uint16_t *__restrict__ count, float omega, T *__restrict__ d) {
+    extern __shared__ __align__(16) unsigned char lc_smem[];
+    uint2 *frag = reinterpret_cast<uint2 *>(lc_smem);
+    __nv_bfloat16 *act = reinterpret_cast<__nv_bfloat16 *>(frag + LC_BF1 + LC_BF2 + LC_BF3);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int g = lane >> 2, q = lane & 3;
+    __nv_bfloat16 *a1 = act + (size_t)warp * 2 * LC_ROWS * KMAX_C;  // [LC_ROWS][16]
+    __nv_bfloat16 *a2 = a1 + LC_ROWS * KMAX_C;                      // [LC_ROWS][16]
+    __nv_bfloat16 *a0 = act + (size_t)LC_WARPS * 2 * LC_ROWS * KMAX_C + warp * (PPV + 1);  // [PPV]
+    float *outp = reinterpret_cast<float *>(act + (size_t)LC_WARPS * 2 * LC_ROWS * KMAX_C + LC_WARPS * (PPV + 1)) +
+                  warp * 128;
+    for (int i = threadIdx.x; i < LC_BF1 + LC_BF2 + LC_BF3; i += blockDim.x) frag[i] = frag_g[i];
+    // zero every activation buffer once: the padding rows are never written again
+    const __nv_bfloat16 zero = __float2bfloat16(0.f);
+    for (int i = lane; i < 2 * LC_ROWS * KMAX_C; i += 32) a1[i] = zero;
+    for (int i = lane; i < PPV; i += 32) a0[i] = zero;
+    __syncthreads();
+    const uint2 *bf1 = frag, *bf2 = frag + LC_BF1, *bf3 = frag + LC_BF1 + LC_BF2;
+    const ptrdiff_t nwarps = (ptrdiff_t)gridDim.x * LC_WARPS;
+    for (ptrdiff_t p = (ptrdiff_t)blockIdx.x * LC_WARPS + warp; p < P; p += nwarps) {
+        // gather D^-1 r, normalise by the patch RMS
+        idx_t gv[4];
+        float val[4];
+        float ss = 0.f;
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const int v = lane + 32 * k;
+            gv[k] = 0;
+            val[k] = 0.f;
+            if (v < PV) {
+                gv[k] = elements[v][p];
+                float x = (float)r[gv[k]];
+                if (inv_diag) x *= (float)inv_diag[gv[k]];
+                val[k] = x;
+                ss += x * x;
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o);
+        float sc = sqrtf(ss / PV);
+        if (!(sc > 0.f)) sc = 1.f;
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const int v = lane + 32 * k;
+            if (v < PV) a0[pad_index(v)] = __float2bfloat16(val[k] / sc);
+        }
+        __syncwarp();
+        // conv1 (1 -> 16), ReLU: A[pos][tap] = a0[pad(pos) + delta(tap)]
+#pragma unroll 1
+        for (int mt = 0; mt < 8; mt++) {
+            float acc[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
+            const int r0 = 16 * mt + g, r1 = r0 + 8;
+            const int b0 = r0 < PV ? pad_index(r0) : -1, b1 = r1 < PV ? pad_index(r1) : -1;
+#pragma unroll
+            for (int kt = 0; kt < 2; kt++) {
+                auto av = [&](int base, int k) {
+                    const int tap = 16 * kt + k;
+                    return (base >= 0 && tap < 27) ? a0[base + off_delta(tap)] : zero;
+                };
+                uint32_t a[4];
+                a[0] = pack_bf16_raw(av(b0, 2 * q), av(b0, 2 * q + 1));
+                a[1] = pack_bf16_raw(av(b1, 2 * q), av(b1, 2 * q + 1));
+                a[2] = pack_bf16_raw(av(b0, 2 * q + 8), av(b0, 2 * q + 9));
+                a[3] = pack_bf16_raw(av(b1, 2 * q + 8), av(b1, 2 * q + 9));
+#pragma unroll
+                for (int j = 0; j < 2; j++) {
+                    const uint2 bb = bf1[(kt * 2 + j) * 32 + lane];
+                    mma_bf16_16816(acc[j], a, bb.x, bb.y);
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < 2; j++) {
+                const int co = 8 * j + 2 * q;
+                if (b0 >= 0)
+                    *reinterpret_cast<uint32_t *>(&a1[b0 * KMAX_C + co]) =
+                            pack_bf16(fmaxf(acc[j][0], 0.f), fmaxf(acc[j][1], 0.f));
+                if (b1 >= 0)
+                    *reinterpret_cast<uint32_t *>(&a1[b1 * KMAX_C + co]) =
+                            pack_bf16(fmaxf(acc[j][2], 0.f), fmaxf(acc[j][3], 0.f));
+            }
+        }
+        __syncwarp();
+        // conv2 (16 -> 16), ReLU; conv3 (16 -> 1): one k-tile of 16 channels per tap
+        const int mrow = (lane >> 3 & 1) * 8 + (lane & 7);  // row of this lane's ldmatrix address
+        const int mcol = (lane >> 4) * 8;                    // column half
+#pragma unroll 1
+        for (int layer = 2; layer <= 3; layer++) {
+            const __nv_bfloat16 *src = layer == 2 ? a1 : a2;
+#pragma unroll 1
+            for (int mt = 0; mt < 8; mt++) {
+                float acc[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
+                const int pos = 16 * mt + mrow;
+                const int base = pos < PV ? pad_index(pos) : -1;
+#pragma unroll 3
+                for (int t = 0; t < 27; t++) {
+                    const int row = base >= 0 ? base + off_delta(t) : PPV;  // PPV = the zero row
+                    uint32_t a[4];
+                    ldmatrix_x4(a, src + row * KMAX_C + mcol);
+                    if (layer == 2) {
+#pragma unroll
+                        for (int j = 0; j < 2; j++) {
+                            const uint2 bb = bf2[(t * 2 + j) * 32 + lane];
+                            mma_bf16_16816(acc[j], a, bb.x, bb.y);
+                        }
+                    } else {
+                        const uint2 bb = bf3[t * 32 + lane];
+                        mma_bf16_16816(acc[0], a, bb.x, bb.y);
+                    }
+                }
+                const int r0 = 16 * mt + g, r1 = r0 + 8;
+                if (layer == 2) {
+#pragma unroll
+                    for (int j = 0; j < 2; j++) {
+                        const int co = 8 * j + 2 * q;
+                        if (r0 < PV)
+                            *reinterpret_cast<uint32_t *>(&a2[pad_index(r0) * KMAX_C + co]) =
+                                    pack_bf16(fmaxf(acc[j][0], 0.f), fmaxf(acc[j][1], 0.f));
+                        if (r1 < PV)
+                            *reinterpret_cast<uint32_t *>(&a2[pad_index(r1) * KMAX_C + co]) =
+                                    pack_bf16(fmaxf(acc[j][2], 0.f), fmaxf(acc[j][3], 0.f));
+                    }
+                } else if (q == 0) {  // column 0 of the 16 x 8 tile, rounded like the stored activations
+                    outp[r0] = __bfloat162float(__float2bfloat16(acc[0][0]));
+                    outp[r1] = __bfloat162float(__float2bfloat16(acc[0][2]));
+                }
+            }
+            __syncwarp();
+        }
+        // scatter, averaged over the macro elements sharing a node
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const int v = lane + 32 * k;
+            if (v < PV) {
+                const idx_t gg = gv[k];
+                const T inc = (T)omega * (T)(sc * outp[v]) / (T)count[gg];
+                atomicAdd(&d[gg], inc);
+            }
+        }
+        __syncwarp();
+    }
+}
+
+static size_t lc_smem_bytes() {
+    return sizeof(uint2) * (LC_BF1 + LC_BF2 + LC_BF3) +
+           sizeof(__nv_bfloat16) * ((size_t)LC_WARPS * 2 * LC_ROWS * KMAX_C + LC_WARPS * (PPV + 1)) +
+           sizeof(float) * LC_WARPS * 128;
+}
+
 static int conv_grid(ptrdiff_t P) { return grid_for(P, 1, kNumSMs * 8); }
 
 }  // namespace sfem_gb300
@@ -340,4 +560,42 @@ extern "C" int sfem_gb300_adam_step(int n, float *w, const float *g, float *m, f
     adam_kernel<<<grid_for(n, 256, 64), 256, 0, stream_of(stream)>>>(n, w, g, m, v, (__nv_bfloat16 *)w_bf16, lr, beta1,
                                                                       beta2, eps, t);
     return check_launch("sfem_gb300_adam_step");
+}
+
+extern "C" size_t sfem_gb300_learned_fragments_size(void) { return sizeof(uint2) * (LC_BF1 + LC_BF2 + LC_BF3); }
+
+extern "C" int sfem_gb300_learned_fragments(const void *W1, const void *W2, const void *W3, void *frag, void *stream) {
+    learned_fragments_kernel<<<(LC_BF1 + LC_BF2 + LC_BF3 + 255) / 256, 256, 0, stream_of(stream)>>>(
+            (const __nv_bfloat16 *)W1, (const __nv_bfloat16 *)W2, (const __nv_bfloat16 *)W3, (uint2 *)frag);
+    return check_launch("sfem_gb300_learned_fragments");
+}
+
+extern "C" int sfem_gb300_learned_correction(int real_type, ptrdiff_t P, idx_t **elements, const void *r,
+                                             const void *inv_diag, const void *frag, const uint16_t *count,
+                                             double omega, void *d, void *stream) {
+    if (P <= 0) return SFEM_GB300_SUCCESS;
+    const cudaStream_t s = stream_of(stream);
+    const size_t smem = lc_smem_bytes();
+    static bool attr[2] = {false, false};
+    const int grid = (int)std::min<ptrdiff_t>((P + LC_WARPS - 1) / LC_WARPS, (ptrdiff_t)kNumSMs * 2);
+    if (real_type == SFEM_GB300_FLOAT32) {
+        if (!attr[0]) {
+            cudaFuncSetAttribute(learned_correction_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem);
+            attr[0] = true;
+        }
+        learned_correction_kernel<float><<<grid, 32 * LC_WARPS, smem, s>>>(
+                P, elements, (const float *)r, (const float *)inv_diag, (const uint2 *)frag, count, (float)omega,
+                (float *)d);
+    } else {
+        if (!attr[1]) {
+            cudaFuncSetAttribute(learned_correction_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem);
+            attr[1] = true;
+        }
+        learned_correction_kernel<double><<<grid, 32 * LC_WARPS, smem, s>>>(
+                P, elements, (const double *)r, (const double *)inv_diag, (const uint2 *)frag, count, (float)omega,
+                (double *)d);
+    }
+    return check_launch("sfem_gb300_learned_correction");
 }

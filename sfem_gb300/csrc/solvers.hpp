@@ -90,45 +90,51 @@ struct DeviceBuffer {
     T *data() const { return ptr; }
 };
 
-// Stream + reduction workspace + device/pinned scalar slots shared by the solvers of one hierarchy.
+// Stream + reduction workspace + device scalar slots shared by the solvers of one
+// hierarchy.  Slots are handed out from blocks of kSlotBlock doubles; a full block
+// is kept (its slots stay valid) and a new one is allocated, so a context can
+// serve any number of solver objects.
 struct Context {
+    static constexpr int kSlotBlock = 1024;
     cudaStream_t stream{0};
     void *workspace{nullptr};
-    double *d_scalars{nullptr};
-    double *h_scalars{nullptr};
-    int n_slots{0};
-    int next_slot{0};
+    std::vector<double *> blocks;
+    int next_slot{kSlotBlock};
+    double *h_scalar{nullptr};  // pinned staging for host reads
 
-    static std::shared_ptr<Context> create(cudaStream_t s, int n_slots = 256) {
+    static std::shared_ptr<Context> create(cudaStream_t s, int = 0) {
         auto c = std::make_shared<Context>();
         c->stream = s;
-        c->n_slots = n_slots;
         if (cudaMalloc(&c->workspace, sfem_gb300_reduce_workspace_size()) != cudaSuccess) return nullptr;
         if (cudaMemset(c->workspace, 0, sfem_gb300_reduce_workspace_size()) != cudaSuccess) return nullptr;
-        if (cudaMalloc((void **)&c->d_scalars, n_slots * sizeof(double)) != cudaSuccess) return nullptr;
-        if (cudaMemset(c->d_scalars, 0, n_slots * sizeof(double)) != cudaSuccess) return nullptr;
-        if (cudaMallocHost((void **)&c->h_scalars, n_slots * sizeof(double)) != cudaSuccess) return nullptr;
+        if (cudaMallocHost((void **)&c->h_scalar, sizeof(double)) != cudaSuccess) return nullptr;
         return c;
     }
     ~Context() {
         if (workspace) cudaFree(workspace);
-        if (d_scalars) cudaFree(d_scalars);
-        if (h_scalars) cudaFreeHost(h_scalars);
+        for (double *b : blocks) cudaFree(b);
+        if (h_scalar) cudaFreeHost(h_scalar);
     }
-    // Reserve k consecutive device scalar slots.
+    // Reserve k consecutive device scalar slots (zero-initialised).
     double *slots(int k) {
-        if (next_slot + k > n_slots) return nullptr;
-        double *p = d_scalars + next_slot;
+        if (k > kSlotBlock) return nullptr;
+        if (next_slot + k > kSlotBlock) {
+            double *b = nullptr;
+            if (cudaMalloc((void **)&b, kSlotBlock * sizeof(double)) != cudaSuccess) return nullptr;
+            if (cudaMemset(b, 0, kSlotBlock * sizeof(double)) != cudaSuccess) return nullptr;
+            blocks.push_back(b);
+            next_slot = 0;
+        }
+        double *p = blocks.back() + next_slot;
         next_slot += k;
         return p;
     }
     void *sp() { return stream ? (void *)&stream : nullptr; }
     // Copy one device scalar to the host (synchronizes the stream).
     double read(const double *d) {
-        const int k = (int)(d - d_scalars);
-        cudaMemcpyAsync(h_scalars + k, d, sizeof(double), cudaMemcpyDeviceToHost, stream);
+        cudaMemcpyAsync(h_scalar, d, sizeof(double), cudaMemcpyDeviceToHost, stream);
         cudaStreamSynchronize(stream);
-        return h_scalars[k];
+        return *h_scalar;
     }
 };
 
@@ -364,9 +370,11 @@ public:
     bool use_fallback{false};
     int chain{0};  // 1: the fallback smoother first, then the learned corrections; 2: learned first, then fallback
     bool line_search{true};   // step length minimising the energy norm of the error along the correction
+    bool fused{true};  // one tensor-core kernel for gather + network + scatter
     DeviceBuffer<T> r, d, Ad;
-    DeviceBuffer<uint16_t> a0, a1, a2, a3;  // BF16 activations
+    DeviceBuffer<uint16_t> a0, a1, a2, a3;  // BF16 activations (unfused path)
     DeviceBuffer<float> pscale;
+    DeviceBuffer<unsigned char> frag;  // B fragments of the three layers (fused path)
     double *s{nullptr};  // device scalars: (d, r), (d, A d)
     // One sweep: r = b - A x; d = net(D^-1 r patches) scattered and zeroed on
     // Dirichlet nodes; x += alpha d with alpha = (d, r) / (d, A d) computed on the
@@ -385,27 +393,37 @@ public:
         SFEM_GB300_CHECK(r.resize(n));
         SFEM_GB300_CHECK(d.resize(n));
         SFEM_GB300_CHECK(Ad.resize(n));
-        SFEM_GB300_CHECK(a0.resize(P * 125));
-        SFEM_GB300_CHECK(a1.resize(P * 125 * channels));
-        SFEM_GB300_CHECK(a2.resize(P * 125 * channels));
-        SFEM_GB300_CHECK(a3.resize(P * 125));
-        SFEM_GB300_CHECK(pscale.resize(P));
+        if (fused) {
+            SFEM_GB300_CHECK(frag.resize((ptrdiff_t)sfem_gb300_learned_fragments_size()));
+        } else {
+            SFEM_GB300_CHECK(a0.resize(P * 125));
+            SFEM_GB300_CHECK(a1.resize(P * 125 * channels));
+            SFEM_GB300_CHECK(a2.resize(P * 125 * channels));
+            SFEM_GB300_CHECK(a3.resize(P * 125));
+            SFEM_GB300_CHECK(pscale.resize(P));
+        }
         if (!s) s = blas.ctx->slots(2);
         if (!s) return set_error("LearnedSmoother: out of scalar slots");
         void *sp = blas.ctx->sp();
+        if (fused) SFEM_GB300_CHECK(sfem_gb300_learned_fragments(W[0], W[1], W[2], frag.ptr, sp));
         for (this->iterations_ = 0; this->iterations_ < sweeps; this->iterations_++) {
             blas.zeros(n, r.ptr);
             SFEM_GB300_CHECK(op->apply(x, r.ptr));
             blas.axpby(n, T(1), b, T(-1), r.ptr);
-            SFEM_GB300_CHECK(sfem_gb300_gather_patches(real_type_v<T>, P, elements, r.ptr, inv_diag, a0.ptr,
-                                                       pscale.ptr, sp));
-            SFEM_GB300_CHECK(sfem_gb300_patchconv_forward(P, 1, channels, a0.ptr, W[0], 1, a1.ptr, sp));
-            SFEM_GB300_CHECK(sfem_gb300_patchconv_forward(P, channels, channels, a1.ptr, W[1], 1, a2.ptr, sp));
-            SFEM_GB300_CHECK(sfem_gb300_patchconv_forward(P, channels, 1, a2.ptr, W[2], 0, a3.ptr, sp));
             T *target = line_search ? d.ptr : x;
             if (line_search) blas.zeros(n, d.ptr);
-            SFEM_GB300_CHECK(sfem_gb300_scatter_patches(real_type_v<T>, P, elements, a3.ptr, pscale.ptr, count, omega,
-                                                        target, sp));
+            if (fused) {
+                SFEM_GB300_CHECK(sfem_gb300_learned_correction(real_type_v<T>, P, elements, r.ptr, inv_diag, frag.ptr,
+                                                               count, omega, target, sp));
+            } else {
+                SFEM_GB300_CHECK(sfem_gb300_gather_patches(real_type_v<T>, P, elements, r.ptr, inv_diag, a0.ptr,
+                                                           pscale.ptr, sp));
+                SFEM_GB300_CHECK(sfem_gb300_patchconv_forward(P, 1, channels, a0.ptr, W[0], 1, a1.ptr, sp));
+                SFEM_GB300_CHECK(sfem_gb300_patchconv_forward(P, channels, channels, a1.ptr, W[1], 1, a2.ptr, sp));
+                SFEM_GB300_CHECK(sfem_gb300_patchconv_forward(P, channels, 1, a2.ptr, W[2], 0, a3.ptr, sp));
+                SFEM_GB300_CHECK(sfem_gb300_scatter_patches(real_type_v<T>, P, elements, a3.ptr, pscale.ptr, count,
+                                                            omega, target, sp));
+            }
             if (!line_search) continue;
             if (n_dirichlet > 0)
                 SFEM_GB300_CHECK(sfem_gb300_constraint_nodes_to_value(real_type_v<T>, n_dirichlet, dirichlet, 1, 0, 0.0,

@@ -78,6 +78,55 @@ def test_adam_and_mse(cuda):
     assert torch.allclose(wb.float(), w, rtol=1e-2, atol=1e-2)
 
 
+@pytest.mark.parametrize("dtype_name", ["float32", "float64"])
+def test_fused_tensor_core_correction_matches_layer_kernels(cuda, dtype_name):
+    """The fused tensor-core inference kernel against gather + three layer kernels + scatter
+    (which the oracle pins): same network, same BF16 rounding points, FP32 accumulation in a
+    different order, so agreement to BF16 resolution."""
+    import torch
+
+    from sfem_gb300.learned import PatchNet
+    from sfem_gb300.mesh import SSMesh
+    from sfem_gb300.solvers import Hierarchy
+
+    dt = getattr(torch, dtype_name)
+    m = SSMesh(5, 4, 3, 4, perturb=0.1, seed=1)
+    H = Hierarchy(m, dirichlet_faces=("x0",), device=cuda)
+    fine = H.spaces[0]
+    P, N = m.n_elements, m.n_nodes()
+    net = PatchNet(cuda, seed=3)
+    for w in net.w32:  # larger output weights than the training init so the output is not tiny
+        w.mul_(3.0)
+    net.wbf = [w.to(torch.bfloat16) for w in net.w32]
+    g = torch.Generator(device=cuda).manual_seed(5)
+    r = torch.randn(N, dtype=dt, device=cuda, generator=g)
+    inv = torch.rand(N, dtype=dt, device=cuda, generator=g) + 0.5
+    lib = capi.load()
+    frag = torch.empty(lib.sfem_gb300_learned_fragments_size(), dtype=torch.uint8, device=cuda)
+    capi.check(lib.sfem_gb300_learned_fragments(capi.vp(net.wbf[0]), capi.vp(net.wbf[1]), capi.vp(net.wbf[2]),
+                                                capi.vp(frag), None), "fragments")
+    rt = capi.FLOAT32 if dt == torch.float32 else capi.FLOAT64
+    d_fused = torch.zeros(N, dtype=dt, device=cuda)
+    capi.check(lib.sfem_gb300_learned_correction(rt, capi.i64(P), fine.lidx_ptrs.ptr, capi.vp(r), capi.vp(inv),
+                                                 capi.vp(frag), capi.vp(fine.count), ctypes.c_double(0.7),
+                                                 capi.vp(d_fused), None), "fused")
+    a0 = torch.empty((P, 125), dtype=torch.bfloat16, device=cuda)
+    ps = torch.empty(P, dtype=torch.float32, device=cuda)
+    capi.check(lib.sfem_gb300_gather_patches(rt, capi.i64(P), fine.lidx_ptrs.ptr, capi.vp(r), capi.vp(inv),
+                                             capi.vp(a0), capi.vp(ps), None), "gather")
+    a1, a2, y = net.forward(a0)
+    d_ref = torch.zeros(N, dtype=dt, device=cuda)
+    capi.check(lib.sfem_gb300_scatter_patches(rt, capi.i64(P), fine.lidx_ptrs.ptr, capi.vp(y), capi.vp(ps),
+                                              capi.vp(fine.count), ctypes.c_double(0.7), capi.vp(d_ref), None),
+               "scatter")
+    torch.cuda.synchronize()
+    ref, got = d_ref.double(), d_fused.double()
+    assert float(ref.abs().max()) > 0
+    rel = float(torch.linalg.vector_norm(got - ref) / torch.linalg.vector_norm(ref))
+    assert rel < 2e-2, rel
+    assert float((got - ref).abs().max()) < 0.1 * float(ref.abs().max())
+
+
 def test_learned_smoother_pipeline_small(cuda):
     """Harvest -> train (own BF16 kernels) -> FCG with the learned correction on a fresh
     coefficient draw: the loss drops, the solve reaches 1e-10 true residual, and the
