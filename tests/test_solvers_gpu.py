@@ -61,6 +61,34 @@ def test_hex8_poisson_jacobi_pcg(cuda):
     _check_solution(apply, b, x.cpu().numpy(), x_star, rtol=1e-10, xtol=1e-8)
 
 
+def test_hex8_cube32_jacobi_pcg_config1(cuda):
+    """The reference's CPU-runnable case: hex8 32^3 unit cube, Dirichlet on all six faces,
+    lumped-mass load of f = 1, Jacobi-PCG (omega = 1) to 1e-10 in FP64, against the
+    oracle CG solution on the same system."""
+    import torch
+
+    m = SSMesh(32, 32, 32, 1)
+    faces = ("x0", "x1", "y0", "y1", "z0", "z1")
+    H = S.Hierarchy(m, dirichlet_faces=faces, device=cuda)
+    fff = H.fff.cpu().numpy().T.copy()
+    dn = H.dirichlet[0].cpu().numpy()
+    apply, d = _oracle_poisson(m, 1, fff, dn)
+    el = m.hex8_elements()
+    h3 = (1.0 / 32) ** 3
+    b = np.bincount(el.reshape(-1), weights=np.full(el.size, h3 / 8), minlength=m.n_nodes(1))
+    b[dn] = 0
+    assert m.n_nodes(1) == 35937 and dn.size == 35937 - 31 ** 3
+    x_star, _ = OS.cg(apply, b, precond=lambda r: r / d, rtol=1e-13, max_it=5000)
+    ctx = S.context()
+    op = S.laplacian_op(ctx, H.spaces[0], H.fff, H.dirichlet[0], torch.float64)
+    solver = S.cg(ctx, op, S.jacobi(ctx, torch.from_numpy(d).to(cuda), 1.0), rtol=1e-10, max_it=5000,
+                  residual_norm=True)
+    bd = torch.from_numpy(b).to(cuda)
+    x = torch.zeros_like(bd)
+    assert S.solve(solver, bd, x) == 0
+    _check_solution(apply, b, x.cpu().numpy(), x_star, rtol=1.5e-10, xtol=1e-8)
+
+
 @pytest.mark.parametrize("smoother", ["chebyshev3", "jacobi"])
 def test_sshex8_mg_pcg_fp64(cuda, smoother):
     import torch
