@@ -39,8 +39,9 @@ LEVEL = 4
 METRIC = "sshex8 Laplacian apply GDoF/s (FP32, L=4, 48^3 macro); solve times to FP64 residual in 'solve'"
 NOMINAL_FP64_TFLOPS = 1.25  # GB300 nominal FP64 (no measured figure in the peaks file)
 # dram__bytes_read.sum + dram__bytes_write.sum of one launch of the default float
-# kernel on this workload (ncu, cold cache); see the profile summary of that kernel
-TRAFFIC_BYTES_PER_LAUNCH = None
+# kernel on this workload (ncu --set full, cold cache: 115.5 MB read + 5.3 MB
+# written), from profiles/sshex8_laplacian_apply_async_fp32_L4_48cube.md
+TRAFFIC_BYTES_PER_LAUNCH = 120.8e6
 SEED = 0
 PERTURB = 0.1
 
@@ -56,6 +57,8 @@ def parse():
     ap.add_argument("--no-solve", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-learned", action="store_true")
+    ap.add_argument("--profile-kernels", action="store_true",
+                    help="launch each main kernel twice on the bench workloads and exit (an ncu target)")
     ap.add_argument("--batch-problems", type=int, default=256)
     return ap.parse_args()
 
@@ -556,8 +559,72 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
+def profile_kernels():
+    """Two launches of each main kernel on the bench workloads (48^3 L=4 Laplacian FP32 /
+    FP64 apply, level 2 <-> 4 transfers, the fused learned correction on the 48^3
+    patches, 64x16x16 L=4 elasticity FP32 / FP64): the target of the ncu captures
+    summarised in profiles/."""
+    import ctypes
+
+    import torch
+
+    from sfem_gb300 import capi
+    from sfem_gb300 import solvers as S
+    from sfem_gb300.learned import PatchNet
+    from sfem_gb300.mesh import SSMesh
+    from sfem_gb300.operators import Laplacian
+
+    dev = torch.device("cuda:0")
+    lib = capi.load()
+    m = workload_config(NX)
+    H = S.Hierarchy(m, dirichlet_faces=("x0",), device=dev)
+    sp = H.spaces[0]
+    op = Laplacian(sp).set_fff(H.fff)
+    N = m.n_nodes()
+    for dt in (torch.float32, torch.float64):
+        x = torch.randn(N, dtype=dt, device=dev)
+        y = torch.zeros_like(x)
+        for _ in range(2):
+            y.zero_()
+            op.apply(x, y)
+    ctx = S.context()
+    P = S.prolongation_op(ctx, H.spaces[1], H.spaces[0], 1, H.dirichlet[0], torch.float32)
+    R = S.restriction_op(ctx, H.spaces[0], H.spaces[1], 1, H.dirichlet[1], torch.float32)
+    xc = torch.randn(H.spaces[1].n_nodes, dtype=torch.float32, device=dev)
+    xf = torch.randn(N, dtype=torch.float32, device=dev)
+    for _ in range(2):
+        S.apply(P, xc, xf)
+        S.apply(R, xf, xc)
+    net = PatchNet(dev, seed=0)
+    frag = torch.empty(lib.sfem_gb300_learned_fragments_size(), dtype=torch.uint8, device=dev)
+    capi.check(lib.sfem_gb300_learned_fragments(capi.vp(net.wbf[0]), capi.vp(net.wbf[1]), capi.vp(net.wbf[2]),
+                                                capi.vp(frag), None), "fragments")
+    r = torch.randn(N, dtype=torch.float32, device=dev)
+    inv = torch.ones_like(r)
+    d = torch.zeros_like(r)
+    for _ in range(2):
+        capi.check(lib.sfem_gb300_learned_correction(capi.FLOAT32, capi.i64(m.n_elements), sp.lidx_ptrs.ptr,
+                                                     capi.vp(r), capi.vp(inv), capi.vp(frag), capi.vp(sp.count),
+                                                     ctypes.c_double(1.0), capi.vp(d), None), "learned")
+    del H, op
+    me = SSMesh(64, 16, 16, LEVEL, box=((0, 4), (0, 1), (0, 1)))
+    He = S.Hierarchy(me, dirichlet_faces=("x0",), device=dev, vec=3)
+    for dt in (torch.float32, torch.float64):
+        ope = S.elasticity_op(ctx, He.spaces[0], He.adj, He.det, 1.0, 10.0, He.dirichlet[0], dt)
+        u = torch.randn(3 * me.n_nodes(), dtype=dt, device=dev)
+        v = torch.zeros_like(u)
+        for _ in range(2):
+            v.zero_()
+            S.apply(ope, u, v)
+    torch.cuda.synchronize()
+    print("profile kernels: done")
+
+
 def main():
     args = parse()
+    if args.profile_kernels:
+        profile_kernels()
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -812,7 +812,10 @@ static int laplacian_apply_tpl(int element_type, ptrdiff_t nelements, idx_t **el
     // default per level (measured at 7.2M nodes): L=4 async tile, L=2 thread per element, else staged tile
     int variant = laplacian_variant();
     if (__atomic_load_n(&g_laplacian_variant_forced, __ATOMIC_RELAXED) == 0) variant = (L == 4) ? 3 : (L == 2) ? 2 : 0;
-    if (sizeof(T) == 4 && L >= 2 && L <= 4 && variant == 0) {
+    // FP64 at L = 2, 3: few micro elements per macro element leave most lanes of the warp
+    // kernel idle; the staged tile (one thread per element) keeps them busy
+    if (sizeof(T) == 8 && (L == 2 || L == 3) && variant != 1) variant = 5;
+    if ((sizeof(T) == 4 && L >= 2 && L <= 4 && variant == 0) || variant == 5) {
         constexpr int TILE = 64;
         const int tb = (int)((nelements + TILE - 1) / TILE);
         auto launch = [&](auto kernel, int nxe) {

@@ -324,6 +324,12 @@ __global__ void __launch_bounds__(32 * LC_WARPS, 2) learned_correction_kernel(
     __syncthreads();
     const uint2 *bf1 = frag, *bf2 = frag + LC_BF1, *bf3 = frag + LC_BF1 + LC_BF2;
     const ptrdiff_t nwarps = (ptrdiff_t)gridDim.x * LC_WARPS;
+    // ldmatrix row of this lane in each m-tile (-1: a GEMM row past the 125 positions)
+    const int mrow = (lane >> 3 & 1) * 8 + (lane & 7);
+    const int mcol = (lane >> 4) * 8;
+    int rowbase[8];
+#pragma unroll
+    for (int mt = 0; mt < 8; mt++) rowbase[mt] = 16 * mt + mrow < PV ? pad_index(16 * mt + mrow) : -1;
     for (ptrdiff_t p = (ptrdiff_t)blockIdx.x * LC_WARPS + warp; p < P; p += nwarps) {
         // gather D^-1 r, normalise by the patch RMS
         idx_t gv[4];
@@ -387,52 +393,73 @@ __global__ void __launch_bounds__(32 * LC_WARPS, 2) learned_correction_kernel(
             }
         }
         __syncwarp();
-        // conv2 (16 -> 16), ReLU; conv3 (16 -> 1): one k-tile of 16 channels per tap
-        const int mrow = (lane >> 3 & 1) * 8 + (lane & 7);  // row of this lane's ldmatrix address
-        const int mcol = (lane >> 4) * 8;                    // column half
-#pragma unroll 1
-        for (int layer = 2; layer <= 3; layer++) {
-            const __nv_bfloat16 *src = layer == 2 ? a1 : a2;
-#pragma unroll 1
-            for (int mt = 0; mt < 8; mt++) {
-                float acc[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
-                const int pos = 16 * mt + mrow;
-                const int base = pos < PV ? pad_index(pos) : -1;
-#pragma unroll 3
-                for (int t = 0; t < 27; t++) {
-                    const int row = base >= 0 ? base + off_delta(t) : PPV;  // PPV = the zero row
+        // conv2 (16 -> 16), ReLU: one k-tile of 16 input channels per tap, taps outer so the
+        // B fragments of a tap are loaded once for the 8 m-tiles; all 16 accumulators stay
+        // in registers.  Row addresses: this lane's ldmatrix row of m-tile mt is the padded
+        // position rowbase[mt] (patch independent) shifted by the tap's compile-time offset.
+        {
+            float acc[8][2][4];
+#pragma unroll
+            for (int mt = 0; mt < 8; mt++)
+#pragma unroll
+                for (int j = 0; j < 2; j++)
+#pragma unroll
+                    for (int c = 0; c < 4; c++) acc[mt][j][c] = 0.f;
+#pragma unroll
+            for (int t = 0; t < 27; t++) {
+                const uint2 bb0 = bf2[(t * 2 + 0) * 32 + lane], bb1 = bf2[(t * 2 + 1) * 32 + lane];
+#pragma unroll
+                for (int mt = 0; mt < 8; mt++) {
+                    const int row = rowbase[mt] >= 0 ? rowbase[mt] + off_delta(t) : PPV;
                     uint32_t a[4];
-                    ldmatrix_x4(a, src + row * KMAX_C + mcol);
-                    if (layer == 2) {
-#pragma unroll
-                        for (int j = 0; j < 2; j++) {
-                            const uint2 bb = bf2[(t * 2 + j) * 32 + lane];
-                            mma_bf16_16816(acc[j], a, bb.x, bb.y);
-                        }
-                    } else {
-                        const uint2 bb = bf3[t * 32 + lane];
-                        mma_bf16_16816(acc[0], a, bb.x, bb.y);
-                    }
-                }
-                const int r0 = 16 * mt + g, r1 = r0 + 8;
-                if (layer == 2) {
-#pragma unroll
-                    for (int j = 0; j < 2; j++) {
-                        const int co = 8 * j + 2 * q;
-                        if (r0 < PV)
-                            *reinterpret_cast<uint32_t *>(&a2[pad_index(r0) * KMAX_C + co]) =
-                                    pack_bf16(fmaxf(acc[j][0], 0.f), fmaxf(acc[j][1], 0.f));
-                        if (r1 < PV)
-                            *reinterpret_cast<uint32_t *>(&a2[pad_index(r1) * KMAX_C + co]) =
-                                    pack_bf16(fmaxf(acc[j][2], 0.f), fmaxf(acc[j][3], 0.f));
-                    }
-                } else if (q == 0) {  // column 0 of the 16 x 8 tile, rounded like the stored activations
-                    outp[r0] = __bfloat162float(__float2bfloat16(acc[0][0]));
-                    outp[r1] = __bfloat162float(__float2bfloat16(acc[0][2]));
+                    ldmatrix_x4(a, a1 + row * KMAX_C + mcol);
+                    mma_bf16_16816(acc[mt][0], a, bb0.x, bb0.y);
+                    mma_bf16_16816(acc[mt][1], a, bb1.x, bb1.y);
                 }
             }
-            __syncwarp();
+#pragma unroll
+            for (int mt = 0; mt < 8; mt++) {
+                const int r0 = 16 * mt + g, r1 = r0 + 8;
+#pragma unroll
+                for (int j = 0; j < 2; j++) {
+                    const int co = 8 * j + 2 * q;
+                    if (r0 < PV)
+                        *reinterpret_cast<uint32_t *>(&a2[pad_index(r0) * KMAX_C + co]) =
+                                pack_bf16(fmaxf(acc[mt][j][0], 0.f), fmaxf(acc[mt][j][1], 0.f));
+                    if (r1 < PV)
+                        *reinterpret_cast<uint32_t *>(&a2[pad_index(r1) * KMAX_C + co]) =
+                                pack_bf16(fmaxf(acc[mt][j][2], 0.f), fmaxf(acc[mt][j][3], 0.f));
+                }
+            }
         }
+        __syncwarp();
+        // conv3 (16 -> 1): output column 0 of an 8-wide n-tile
+        {
+            float acc[8][4];
+#pragma unroll
+            for (int mt = 0; mt < 8; mt++)
+#pragma unroll
+                for (int c = 0; c < 4; c++) acc[mt][c] = 0.f;
+#pragma unroll
+            for (int t = 0; t < 27; t++) {
+                const uint2 bb = bf3[t * 32 + lane];
+#pragma unroll
+                for (int mt = 0; mt < 8; mt++) {
+                    const int row = rowbase[mt] >= 0 ? rowbase[mt] + off_delta(t) : PPV;
+                    uint32_t a[4];
+                    ldmatrix_x4(a, a2 + row * KMAX_C + mcol);
+                    mma_bf16_16816(acc[mt], a, bb.x, bb.y);
+                }
+            }
+            if (q == 0) {  // rounded like the stored activations of the layer kernels
+#pragma unroll
+                for (int mt = 0; mt < 8; mt++) {
+                    outp[16 * mt + g] = __bfloat162float(__float2bfloat16(acc[mt][0]));
+                    outp[16 * mt + g + 8] = __bfloat162float(__float2bfloat16(acc[mt][2]));
+                }
+            }
+        }
+        __syncwarp();
         // scatter, averaged over the macro elements sharing a node
 #pragma unroll
         for (int k = 0; k < 4; k++) {

@@ -77,24 +77,91 @@ __global__ void restrict_kernel(ptrdiff_t nelements, int from_level, const idx_t
         const int v = (int)(t / nelements);
         const int X = v % nc, Y = (v / nc) % nc, Z = v / (nc * nc);
         T acc[3] = {0, 0, 0};
-        // fine nodes within one coarse cell of (X,Y,Z), inside the macro element
+        // fine nodes within one coarse cell of (X,Y,Z), inside the macro element.  For a
+        // power-of-two ratio the weights (products of k/s and 1/count) are dyadic and exact
+        // in float: they are formed in float and only the weighted sum runs in T.
         const int x0 = max(0, (X - 1) * s + 1), x1 = min(from_level, (X + 1) * s - 1);
         const int y0 = max(0, (Y - 1) * s + 1), y1 = min(from_level, (Y + 1) * s - 1);
         const int z0 = max(0, (Z - 1) * s + 1), z1 = min(from_level, (Z + 1) * s - 1);
+        const bool dyadic = (s & (s - 1)) == 0;
+        const float inv_sf = 1.0f / (float)s;
         for (int zi = z0; zi <= z1; zi++) {
             const T wz = T(1) - T(abs(zi - Z * s)) * inv_s;
+            const float wzf = 1.0f - (float)abs(zi - Z * s) * inv_sf;
             for (int yi = y0; yi <= y1; yi++) {
                 const T wy = T(1) - T(abs(yi - Y * s)) * inv_s;
+                const float wyf = 1.0f - (float)abs(yi - Y * s) * inv_sf;
                 for (int xi = x0; xi <= x1; xi++) {
-                    const T wx = T(1) - T(abs(xi - X * s)) * inv_s;
                     const ptrdiff_t f = from_elements[lidx(from_level, xi, yi, zi)][e];
-                    const T w = wx * wy * wz * inv_count<T>(count[f]);
+                    T w;
+                    if (dyadic) {
+                        const float wxf = 1.0f - (float)abs(xi - X * s) * inv_sf;
+                        w = (T)(wxf * wyf * wzf * inv_count<float>(count[f]));
+                    } else {
+                        const T wx = T(1) - T(abs(xi - X * s)) * inv_s;
+                        w = wx * wy * wz * inv_count<T>(count[f]);
+                    }
                     for (int d = 0; d < vec_size; d++) acc[d] += w * from[f * vec_size + d];
                 }
             }
         }
         const ptrdiff_t gid = to_elements[v][e];
         for (int d = 0; d < vec_size; d++) atomicAdd(&to[gid * vec_size + d], acc[d]);
+    }
+}
+
+// Factor-2 prolongation (coarse level LC -> fine level 2 LC, the 1 -> 2 and 2 -> 4
+// steps) with one thread per macro element: the (LC+1)^3 coarse values of the
+// element are loaded once into registers and the (2LC+1)^3 fine values follow from
+// compile-time weights (1, 1/2, 1/4, 1/8: each fine node is a coarse node, an edge
+// midpoint, a face centre or a cell centre).  Consecutive threads own consecutive
+// elements, so every connectivity row read is coalesced.  Same values and
+// summation order as the per-(node, element) kernel above.  (The same structure for
+// the restriction, 125 fine loads and 27 accumulators per thread, ran slower than
+// the per-(coarse node, element) kernel, which keeps the restriction.)
+template <int LC>
+__host__ __device__ constexpr int fine_lidx2(int x, int y, int z) {
+    return (z * (2 * LC + 1) + y) * (2 * LC + 1) + x;
+}
+
+template <typename T, int LC>
+__global__ void __launch_bounds__(128, LC == 1 ? 4 : 2) prolongate2_kernel(ptrdiff_t nelements, const idx_t *const *from_elements,
+                                                          const idx_t *const *to_elements, int vec_size,
+                                                          const T *__restrict__ from, T *__restrict__ to) {
+    constexpr int NC = LC + 1, NCV = NC * NC * NC;
+    constexpr int NF = 2 * LC + 1, NFV = NF * NF * NF;
+    __shared__ const idx_t *srow_c[NCV], *srow_f[NFV];
+    for (int v = threadIdx.x; v < NCV; v += blockDim.x) srow_c[v] = from_elements[v];
+    for (int v = threadIdx.x; v < NFV; v += blockDim.x) srow_f[v] = to_elements[v];
+    __syncthreads();
+    const ptrdiff_t e = blockIdx.x * (ptrdiff_t)blockDim.x + threadIdx.x;
+    if (e >= nelements) return;
+    idx_t cid[NCV];
+#pragma unroll
+    for (int v = 0; v < NCV; v++) cid[v] = __ldg(&srow_c[v][e]);
+    for (int d = 0; d < vec_size; d++) {
+        T cv[NCV];
+#pragma unroll
+        for (int v = 0; v < NCV; v++) cv[v] = __ldg(&from[(ptrdiff_t)cid[v] * vec_size + d]);
+#pragma unroll
+        for (int zi = 0; zi < NF; zi++)
+#pragma unroll
+            for (int yi = 0; yi < NF; yi++)
+#pragma unroll
+                for (int xi = 0; xi < NF; xi++) {
+                    // the same corner order and weights as the general kernel: w_c = prod of (t or 1-t)
+                    const int cx = min(xi / 2, LC - 1), cy = min(yi / 2, LC - 1), cz = min(zi / 2, LC - 1);
+                    const T tx = T(xi - 2 * cx) * T(0.5), ty = T(yi - 2 * cy) * T(0.5), tz = T(zi - 2 * cz) * T(0.5);
+                    T acc = 0;
+#pragma unroll
+                    for (int c = 0; c < 8; c++) {
+                        const T w = (c8x(c) ? tx : T(1) - tx) * (c8y(c) ? ty : T(1) - ty) * (c8z(c) ? tz : T(1) - tz);
+                        if (w == T(0)) continue;
+                        acc += w * cv[((cz + c8z(c)) * NC + cy + c8y(c)) * NC + cx + c8x(c)];
+                    }
+                    const ptrdiff_t gid = __ldg(&srow_f[fine_lidx2<LC>(xi, yi, zi)][e]);
+                    to[gid * vec_size + d] = acc;
+                }
     }
 }
 
@@ -114,6 +181,16 @@ __global__ void incidence_count_kernel(ptrdiff_t nelements, int level, const idx
 template <typename T>
 static int prolongate_tpl(ptrdiff_t nelements, int from_level, idx_t **from_elements, int to_level,
                           idx_t **to_elements, int vec_size, const void *from, void *to, cudaStream_t s) {
+    if (to_level == 2 * from_level && (from_level == 1 || from_level == 2)) {
+        const int blocks = (int)((nelements + 127) / 128);
+        if (from_level == 1)
+            prolongate2_kernel<T, 1><<<blocks, 128, 0, s>>>(nelements, from_elements, to_elements, vec_size,
+                                                              (const T *)from, (T *)to);
+        else
+            prolongate2_kernel<T, 2><<<blocks, 128, 0, s>>>(nelements, from_elements, to_elements, vec_size,
+                                                              (const T *)from, (T *)to);
+        return check_launch("sfem_gb300_sshex8_prolongate (factor 2)");
+    }
     const ptrdiff_t total = nelements * (ptrdiff_t)((to_level + 1) * (to_level + 1) * (to_level + 1));
     prolongate_kernel<T><<<grid_for(total, 256, kNumSMs * 32), 256, 0, s>>>(
             nelements, from_level, from_elements, to_level, to_elements, vec_size, (const T *)from, (T *)to,
