@@ -83,7 +83,7 @@ __global__ void restrict_kernel(ptrdiff_t nelements, int from_level, const idx_t
         const int x0 = max(0, (X - 1) * s + 1), x1 = min(from_level, (X + 1) * s - 1);
         const int y0 = max(0, (Y - 1) * s + 1), y1 = min(from_level, (Y + 1) * s - 1);
         const int z0 = max(0, (Z - 1) * s + 1), z1 = min(from_level, (Z + 1) * s - 1);
-        const bool dyadic = (s & (s - 1)) == 0;
+        const bool dyadic = sizeof(T) == 8 && (s & (s - 1)) == 0;  // float vectors: plain path
         const float inv_sf = 1.0f / (float)s;
         for (int zi = z0; zi <= z1; zi++) {
             const T wz = T(1) - T(abs(zi - Z * s)) * inv_s;
