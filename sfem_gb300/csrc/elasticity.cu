@@ -140,7 +140,42 @@ __global__ void __launch_bounds__(64) elasticity_apply_warp_kernel(ptrdiff_t nel
             }
         }
         __syncwarp();
-        if constexpr (NM >= 32) {
+        if constexpr (sizeof(T) == 4 && NM == 64) {
+            // two micro elements per lane (m and m + 32) in one pass: each element-matrix
+            // entry read from shared memory feeds one packed FP32x2 FMA for both
+            int va[8], vb[8];
+            float2 uu[24];
+            {
+                const int ma = lane, mb = lane + 32;
+                const int xa = ma % L, ya = (ma / L) % L, za = ma / (L * L);
+                const int xb = mb % L, yb = (mb / L) % L, zb = mb / (L * L);
+#pragma unroll
+                for (int c = 0; c < 8; c++) {
+                    va[c] = lidx(L, xa + c8x(c), ya + c8y(c), za + c8z(c));
+                    vb[c] = lidx(L, xb + c8x(c), yb + c8y(c), zb + c8z(c));
+                }
+#pragma unroll
+                for (int d = 0; d < 3; d++)
+#pragma unroll
+                    for (int c = 0; c < 8; c++)
+                        uu[d * 8 + c] = make_float2((float)xw[d * NXE + va[c]], (float)xw[d * NXE + vb[c]]);
+            }
+#pragma unroll 1
+            for (int d = 0; d < 3; d++) {
+#pragma unroll
+                for (int c = 0; c < 8; c++) {
+                    const int i = d * 8 + c;
+                    float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+                    for (int j = 0; j < 24; j++) {
+                        const float k = (float)K[i * 24 + j];
+                        acc = __ffma2_rn(make_float2(k, k), uu[j], acc);
+                    }
+                    atomicAdd(&yw[d * NXE + va[c]], (T)acc.x);
+                    atomicAdd(&yw[d * NXE + vb[c]], (T)acc.y);
+                }
+            }
+        } else if constexpr (NM >= 32) {
             // one micro element per lane: u read once, reused by the 24 rows
             for (int m = lane; m < NM; m += 32) {
                 const int xi = m % L, yi = (m / L) % L, zi = m / (L * L);
