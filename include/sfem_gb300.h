@@ -293,15 +293,21 @@ int sfem_gb300_scatter_patches(int real_type, ptrdiff_t P, sfem_gb300_idx_t **el
 /* Fused learned correction (inference): for every patch p, gather s^-1 (inv_diag . r)
  * (s = patch RMS), run the three BF16 convolutions on the tensor cores (FP32
  * accumulate), and d[g] += omega * s * out[v] / count[g].  `frag` holds the
- * weights as tensor-core B fragments (sfem_gb300_learned_fragments_size() bytes,
- * built by sfem_gb300_learned_fragments from the [co][ci][27] BF16 weights of
- * the 1 -> 16 -> 16 -> 1 network).  Same result as gather_patches +
- * patchconv_forward x3 + scatter_patches up to accumulation order. */
+ * weights as tensor-core operands (sfem_gb300_learned_fragments_size() bytes,
+ * 16-byte aligned, built by sfem_gb300_learned_fragments from the [co][ci][27]
+ * BF16 weights of the 1 -> 16 -> 16 -> 1 network).  Same result as
+ * gather_patches + patchconv_forward x3 + scatter_patches up to accumulation order.
+ * Kernel variant (sfem_gb300_set_learned_kernel): 0 = tcgen05.mma with the
+ * accumulators in tensor memory (default), 1 = warp-level mma.sync.
+ * sfem_gb300_learned_status returns (and clears) 1 if a tcgen05 kernel gave up
+ * waiting for its tensor-core work (its corrections are then incomplete), 0 if not. */
 size_t sfem_gb300_learned_fragments_size(void);
 int sfem_gb300_learned_fragments(const void *W1, const void *W2, const void *W3, void *frag, void *stream);
 int sfem_gb300_learned_correction(int real_type, ptrdiff_t P, sfem_gb300_idx_t **elements, const void *r,
                                   const void *inv_diag, const void *frag, const uint16_t *count, double omega,
                                   void *d, void *stream);
+int sfem_gb300_set_learned_kernel(int variant);
+int sfem_gb300_learned_status(void);
 /* gy = 2 (y - target) / n (BF16), *loss += mean squared error (FP32, may be NULL). */
 int sfem_gb300_mse_grad(ptrdiff_t n, const void *y, const void *target, void *gy, float *loss, void *stream);
 /* Adam step on FP32 master weights, mirrored into BF16 (t = 1-based step). */

@@ -16,6 +16,7 @@
 #include <algorithm>
 
 #include "common.cuh"
+#include "tcgen05.cuh"
 
 namespace sfem_gb300 {
 
@@ -474,6 +475,244 @@ __global__ void __launch_bounds__(32 * LC_WARPS, 2) learned_correction_kernel(
     }
 }
 
+// ---------------------------------------------------------------------------- tcgen05 inference
+// The same fused correction on the 5th-generation tensor cores.  One CTA of four
+// warps owns one patch at a time; one thread issues tcgen05.mma (M = 128 positions,
+// N = 16 channels, K = 16, BF16 in, FP32 accumulate in tensor memory) and the four
+// warps read the accumulators back with tcgen05.ld (warp w owns TMEM lanes 32w..32w+31).
+//
+// Every layer's GEMM rows are padded positions q = TC_Q0 + i, i < 256 (two M tiles),
+// which cover the 125 interior positions (57..285 of the 7^3 padded grid); rows that
+// are halo positions are computed and discarded.  The activations of conv1 / conv2
+// are stored as [channel chunk][padded position][8 BF16] rows of 16 bytes with a zero
+// halo, so the A operand of tap t is the activation buffer started off_delta(t) rows
+// later (a descriptor start-address shift, no im2col copy).  conv1 has one input
+// channel: its A operand is an im2col of the padded input with K = 27 taps (+5 zero).
+// conv3 (16 -> 1) uses output column 0 of an N = 16 GEMM.
+constexpr int TC_Q0 = PP * PP + PP + 1;  // 57: padded index of patch node 0
+constexpr int TC_ROWS = 384;             // activation rows: max q + off_delta = 312 + 57 = 369
+constexpr int TC_ACT_CHUNK = TC_ROWS * 16;
+constexpr int TC_COL_CHUNK = 256 * 16;
+constexpr int TC_B1_BYTES = 2 * 2 * 16 * 16;   // [kstep][chunk][n][8] BF16
+constexpr int TC_B2_BYTES = 27 * 2 * 16 * 16;  // [tap][chunk][n][8]
+constexpr int TC_OPERAND_BYTES = TC_B1_BYTES + 2 * TC_B2_BYTES;  // B1, B2, B3
+constexpr int TC_OFF_B1 = 0, TC_OFF_B2 = TC_B1_BYTES, TC_OFF_B3 = TC_B1_BYTES + TC_B2_BYTES;
+constexpr int TC_OFF_ACT1 = TC_OPERAND_BYTES;
+constexpr int TC_OFF_ACT2 = TC_OFF_ACT1 + 2 * TC_ACT_CHUNK;
+constexpr int TC_OFF_COL = TC_OFF_ACT2 + 2 * TC_ACT_CHUNK;
+constexpr int TC_OFF_A0 = TC_OFF_COL + 4 * TC_COL_CHUNK;
+constexpr int TC_OFF_OUT = TC_OFF_A0 + TC_ROWS * 2;
+constexpr int TC_OFF_RED = TC_OFF_OUT + 128 * 4;
+constexpr int TC_SMEM = TC_OFF_RED + 16;
+constexpr int TC_CTAS_PER_SM = 3;
+constexpr uint32_t TC_TMEM_COLS = 128;  // D1 cols 0..31, D2 32..63, D3 64..95
+constexpr int TC_WAIT_POLLS = 1 << 20;
+static_assert(TC_SMEM * TC_CTAS_PER_SM <= 227 * 1024, "shared memory of the resident CTAs");
+static_assert(TC_TMEM_COLS * TC_CTAS_PER_SM <= 512, "tensor memory of the resident CTAs");
+static_assert(TC_Q0 + 255 + TC_Q0 < TC_ROWS, "shifted operand rows stay inside the activation buffer");
+
+__device__ int g_lc_status;  // nonzero: a tensor-core wait gave up (kernel returned early)
+
+// B operands in the no-swizzle K-major layout from the [co][ci][27] BF16 weights
+__global__ void learned_tc_operands_kernel(const __nv_bfloat16 *__restrict__ W1, const __nv_bfloat16 *__restrict__ W2,
+                                           const __nv_bfloat16 *__restrict__ W3, __nv_bfloat16 *__restrict__ out) {
+    const __nv_bfloat16 zero = __float2bfloat16(0.f);
+    constexpr int n1 = TC_B1_BYTES / 2, n2 = TC_B2_BYTES / 2;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n1 + 2 * n2; i += gridDim.x * blockDim.x) {
+        if (i < n1) {  // conv1: k = tap = 16 s + 8 c + e, n = co
+            const int e = i % 8, n = (i / 8) % 16, c = (i / 128) % 2, st = i / 256;
+            const int k = 16 * st + 8 * c + e;
+            out[i] = k < 27 ? W1[n * 27 + k] : zero;
+        } else {
+            const int j = (i - n1) % n2, layer = (i - n1) / n2;
+            const int e = j % 8, n = (j / 8) % 16, c = (j / 128) % 2, t = j / 256;
+            const int ci = 8 * c + e;
+            if (layer == 0)
+                out[i] = W2[(n * KMAX_C + ci) * 27 + t];
+            else
+                out[i] = n == 0 ? W3[ci * 27 + t] : zero;
+        }
+    }
+}
+
+__device__ __forceinline__ bool tc_interior(int q) {
+    const int x = q % PP, y = (q / PP) % PP, z = q / (PP * PP);
+    return q < PPV && x >= 1 && x <= PN && y >= 1 && y <= PN && z >= 1 && z <= PN;
+}
+
+// epilogue of conv1 / conv2: ReLU, BF16, rows of interior positions into the activation buffer
+__device__ __forceinline__ void tc_store_act(uint32_t tmem_d, unsigned char *act, int warp, int lane) {
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        float v[16];
+        tc::tmem_ld16(tmem_d + ((uint32_t)(32 * warp) << 16) + 16 * h, v);
+        const int q = TC_Q0 + 128 * h + 32 * warp + lane;
+        if (tc_interior(q)) {
+#pragma unroll
+            for (int c = 0; c < 2; c++) {
+                uint4 w;
+                w.x = pack_bf16(fmaxf(v[8 * c + 0], 0.f), fmaxf(v[8 * c + 1], 0.f));
+                w.y = pack_bf16(fmaxf(v[8 * c + 2], 0.f), fmaxf(v[8 * c + 3], 0.f));
+                w.z = pack_bf16(fmaxf(v[8 * c + 4], 0.f), fmaxf(v[8 * c + 5], 0.f));
+                w.w = pack_bf16(fmaxf(v[8 * c + 6], 0.f), fmaxf(v[8 * c + 7], 0.f));
+                *reinterpret_cast<uint4 *>(act + c * TC_ACT_CHUNK + q * 16) = w;
+            }
+        }
+    }
+}
+
+// one tap-shifted layer: 27 taps x 2 M tiles into D columns [dcol, dcol + 32)
+__device__ __forceinline__ void tc_issue_shift_layer(uint32_t act, uint32_t bops, uint32_t tmem_d) {
+    constexpr uint32_t id = tc::idesc_bf16_f32(128, 16);
+#pragma unroll 1
+    for (int t = 0; t < 27; t++) {
+        const int dz = t / 9 - 1, dy = (t / 3) % 3 - 1, dx = t % 3 - 1;
+        const int off = dz * PP * PP + dy * PP + dx;
+        const uint64_t bd = tc::sdesc(bops + 512 * t, 256, 128);
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const uint64_t ad = tc::sdesc(act + 16 * (TC_Q0 + 128 * h + off), TC_ACT_CHUNK, 128);
+            tc::mma_bf16(tmem_d + 16 * h, ad, bd, id, t > 0);
+        }
+    }
+}
+
+// d[g] += omega * s_p * net(patch_p)[v] / count[g] for every patch p (g = elements[v][p])
+template <typename T>
+__global__ void __launch_bounds__(128, TC_CTAS_PER_SM) learned_correction_tc_kernel(
+        ptrdiff_t P, const idx_t *const *elements, const T *__restrict__ r, const T *__restrict__ inv_diag,
+        const uint4 *__restrict__ operands, const uint16_t *__restrict__ count, float omega, T *__restrict__ d) {
+    extern __shared__ __align__(16) unsigned char tcs[];
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t tmem_holder;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    __nv_bfloat16 *a0 = reinterpret_cast<__nv_bfloat16 *>(tcs + TC_OFF_A0);
+    float *outp = reinterpret_cast<float *>(tcs + TC_OFF_OUT);
+    float *red = reinterpret_cast<float *>(tcs + TC_OFF_RED);
+    // operands in, activation / im2col / input buffers zeroed (their halo rows stay zero)
+    for (int i = tid; i < TC_OPERAND_BYTES / 16; i += 128) reinterpret_cast<uint4 *>(tcs)[i] = operands[i];
+    for (int i = TC_OPERAND_BYTES / 16 + tid; i < TC_OFF_OUT / 16; i += 128)
+        reinterpret_cast<uint4 *>(tcs)[i] = make_uint4(0, 0, 0, 0);
+    if (warp == 0) tc::tmem_alloc(&tmem_holder, TC_TMEM_COLS);
+    if (tid == 0) tc::mbar_init(&mbar, 1);
+    tc::fence_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = tmem_holder;
+    const uint32_t s_b1 = tc::smem_u32(tcs + TC_OFF_B1), s_b2 = tc::smem_u32(tcs + TC_OFF_B2),
+                   s_b3 = tc::smem_u32(tcs + TC_OFF_B3), s_act1 = tc::smem_u32(tcs + TC_OFF_ACT1),
+                   s_act2 = tc::smem_u32(tcs + TC_OFF_ACT2), s_col = tc::smem_u32(tcs + TC_OFF_COL);
+    uint32_t phase = 0;
+    bool ok = true;
+    for (ptrdiff_t p = blockIdx.x; p < P && ok; p += gridDim.x) {
+        // gather D^-1 r, normalise by the patch RMS (thread v owns patch node v)
+        const int v = tid;
+        idx_t gv = 0;
+        float val = 0.f;
+        if (v < PV) {
+            gv = elements[v][p];
+            float x = (float)r[gv];
+            if (inv_diag) x *= (float)inv_diag[gv];
+            val = x;
+        }
+        float ss = val * val;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o);
+        if (lane == 0) red[warp] = ss;
+        __syncthreads();
+        float sc = sqrtf((red[0] + red[1] + red[2] + red[3]) / PV);
+        if (!(sc > 0.f)) sc = 1.f;
+        if (v < PV) a0[pad_index(v)] = __float2bfloat16(val / sc);
+        __syncthreads();
+        // conv1 im2col: col[i][k] = a0[TC_Q0 + i + off_delta(k)], k < 27
+#pragma unroll 1
+        for (int i = tid; i < 256; i += 128) {
+            const int q = TC_Q0 + i;
+#pragma unroll
+            for (int c = 0; c < 4; c++) {
+                uint32_t w[4];
+#pragma unroll
+                for (int e2 = 0; e2 < 4; e2++) {
+                    const int k0 = 8 * c + 2 * e2, k1 = k0 + 1;
+                    const __nv_bfloat16 lo = k0 < 27 ? a0[q + off_delta(k0)] : __float2bfloat16(0.f);
+                    const __nv_bfloat16 hi = k1 < 27 ? a0[q + off_delta(k1)] : __float2bfloat16(0.f);
+                    w[e2] = pack_bf16_raw(lo, hi);
+                }
+                *reinterpret_cast<uint4 *>(tcs + TC_OFF_COL + c * TC_COL_CHUNK + i * 16) =
+                        make_uint4(w[0], w[1], w[2], w[3]);
+            }
+        }
+        tc::fence_async_smem();
+        tc::fence_before_sync();
+        __syncthreads();
+        tc::fence_after_sync();
+        if (tid == 0) {
+            constexpr uint32_t id = tc::idesc_bf16_f32(128, 16);
+#pragma unroll
+            for (int h = 0; h < 2; h++)
+#pragma unroll
+                for (int st = 0; st < 2; st++)
+                    tc::mma_bf16(tmem + 16 * h, tc::sdesc(s_col + 2 * st * TC_COL_CHUNK + h * 128 * 16, TC_COL_CHUNK, 128),
+                                 tc::sdesc(s_b1 + 512 * st, 256, 128), id, st > 0);
+            tc::commit(&mbar);
+        }
+        ok = __syncthreads_and(tc::mbar_wait(&mbar, phase, TC_WAIT_POLLS));
+        phase ^= 1;
+        tc::fence_after_sync();
+        if (!ok) break;
+        tc_store_act(tmem + 0, tcs + TC_OFF_ACT1, warp, lane);
+        tc::fence_async_smem();
+        tc::fence_before_sync();
+        __syncthreads();
+        tc::fence_after_sync();
+        if (tid == 0) {
+            tc_issue_shift_layer(s_act1, s_b2, tmem + 32);
+            tc::commit(&mbar);
+        }
+        ok = __syncthreads_and(tc::mbar_wait(&mbar, phase, TC_WAIT_POLLS));
+        phase ^= 1;
+        tc::fence_after_sync();
+        if (!ok) break;
+        tc_store_act(tmem + 32, tcs + TC_OFF_ACT2, warp, lane);
+        tc::fence_async_smem();
+        tc::fence_before_sync();
+        __syncthreads();
+        tc::fence_after_sync();
+        if (tid == 0) {
+            tc_issue_shift_layer(s_act2, s_b3, tmem + 64);
+            tc::commit(&mbar);
+        }
+        ok = __syncthreads_and(tc::mbar_wait(&mbar, phase, TC_WAIT_POLLS));
+        phase ^= 1;
+        tc::fence_after_sync();
+        if (!ok) break;
+        // conv3 output (column 0), rounded like the stored activations of the layer kernels
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const float o = tc::tmem_ld1(tmem + ((uint32_t)(32 * warp) << 16) + 64 + 16 * h);
+            const int q = TC_Q0 + 128 * h + 32 * warp + lane;
+            if (tc_interior(q)) {
+                const int x = q % PP - 1, y = (q / PP) % PP - 1, z = q / (PP * PP) - 1;
+                outp[(z * PN + y) * PN + x] = __bfloat162float(__float2bfloat16(o));
+            }
+        }
+        tc::fence_before_sync();
+        __syncthreads();
+        tc::fence_after_sync();
+        if (v < PV) atomicAdd(&d[gv], (T)omega * (T)(sc * outp[v]) / (T)count[gv]);
+    }
+    if (!ok) {
+        if (tid == 0) atomicExch(&g_lc_status, 1);
+        // let the MMAs still in flight finish (bounded) before the tensor memory is released
+        tc::mbar_wait(&mbar, phase ^ 1, TC_WAIT_POLLS);
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    if (warp == 0) tc::tmem_dealloc(tmem, TC_TMEM_COLS);
+}
+
 static size_t lc_smem_bytes() {
     return sizeof(uint2) * (LC_BF1 + LC_BF2 + LC_BF3) +
            sizeof(__nv_bfloat16) * ((size_t)LC_WARPS * 2 * LC_ROWS * KMAX_C + LC_WARPS * (PPV + 1)) +
@@ -589,12 +828,39 @@ extern "C" int sfem_gb300_adam_step(int n, float *w, const float *g, float *m, f
     return check_launch("sfem_gb300_adam_step");
 }
 
-extern "C" size_t sfem_gb300_learned_fragments_size(void) { return sizeof(uint2) * (LC_BF1 + LC_BF2 + LC_BF3); }
+// operand buffer: [mma.sync B fragments][tcgen05 B operands]
+static constexpr size_t kLcFragBytes = sizeof(uint2) * (LC_BF1 + LC_BF2 + LC_BF3);
+static_assert(kLcFragBytes % 16 == 0, "tensor-core operands start 16-byte aligned");
+static int g_learned_kernel = 0;  // 0: tcgen05 (default), 1: mma.sync
+
+extern "C" size_t sfem_gb300_learned_fragments_size(void) { return kLcFragBytes + TC_OPERAND_BYTES; }
 
 extern "C" int sfem_gb300_learned_fragments(const void *W1, const void *W2, const void *W3, void *frag, void *stream) {
-    learned_fragments_kernel<<<(LC_BF1 + LC_BF2 + LC_BF3 + 255) / 256, 256, 0, stream_of(stream)>>>(
+    if ((reinterpret_cast<uintptr_t>(frag) & 15) != 0)
+        return set_error("sfem_gb300_learned_fragments: operand buffer must be 16-byte aligned");
+    const cudaStream_t s = stream_of(stream);
+    learned_fragments_kernel<<<(LC_BF1 + LC_BF2 + LC_BF3 + 255) / 256, 256, 0, s>>>(
             (const __nv_bfloat16 *)W1, (const __nv_bfloat16 *)W2, (const __nv_bfloat16 *)W3, (uint2 *)frag);
+    learned_tc_operands_kernel<<<(TC_OPERAND_BYTES / 2 + 255) / 256, 256, 0, s>>>(
+            (const __nv_bfloat16 *)W1, (const __nv_bfloat16 *)W2, (const __nv_bfloat16 *)W3,
+            reinterpret_cast<__nv_bfloat16 *>(static_cast<unsigned char *>(frag) + kLcFragBytes));
     return check_launch("sfem_gb300_learned_fragments");
+}
+
+extern "C" int sfem_gb300_set_learned_kernel(int variant) {
+    if (variant < 0 || variant > 1) return set_error("sfem_gb300_set_learned_kernel: variant %d (0 or 1)", variant);
+    g_learned_kernel = variant;
+    return SFEM_GB300_SUCCESS;
+}
+
+extern "C" int sfem_gb300_learned_status(void) {
+    int st = 0;
+    if (cudaMemcpyFromSymbol(&st, g_lc_status, sizeof(int)) != cudaSuccess) return -1;
+    if (st) {
+        const int zero = 0;
+        cudaMemcpyToSymbol(g_lc_status, &zero, sizeof(int));
+    }
+    return st;
 }
 
 extern "C" int sfem_gb300_learned_correction(int real_type, ptrdiff_t P, idx_t **elements, const void *r,
@@ -602,6 +868,31 @@ extern "C" int sfem_gb300_learned_correction(int real_type, ptrdiff_t P, idx_t *
                                              double omega, void *d, void *stream) {
     if (P <= 0) return SFEM_GB300_SUCCESS;
     const cudaStream_t s = stream_of(stream);
+    if (g_learned_kernel == 0) {
+        static bool tc_attr[2] = {false, false};
+        const int grid = (int)std::min<ptrdiff_t>(P, (ptrdiff_t)kNumSMs * TC_CTAS_PER_SM);
+        const uint4 *ops = reinterpret_cast<const uint4 *>(static_cast<const unsigned char *>(frag) + kLcFragBytes);
+        if (real_type == SFEM_GB300_FLOAT32) {
+            if (!tc_attr[0]) {
+                cudaFuncSetAttribute(learned_correction_tc_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     TC_SMEM);
+                tc_attr[0] = true;
+            }
+            learned_correction_tc_kernel<float><<<grid, 128, TC_SMEM, s>>>(P, elements, (const float *)r,
+                                                                           (const float *)inv_diag, ops, count,
+                                                                           (float)omega, (float *)d);
+        } else {
+            if (!tc_attr[1]) {
+                cudaFuncSetAttribute(learned_correction_tc_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     TC_SMEM);
+                tc_attr[1] = true;
+            }
+            learned_correction_tc_kernel<double><<<grid, 128, TC_SMEM, s>>>(P, elements, (const double *)r,
+                                                                            (const double *)inv_diag, ops, count,
+                                                                            (float)omega, (double *)d);
+        }
+        return check_launch("sfem_gb300_learned_correction");
+    }
     const size_t smem = lc_smem_bytes();
     static bool attr[2] = {false, false};
     const int grid = (int)std::min<ptrdiff_t>((P + LC_WARPS - 1) / LC_WARPS, (ptrdiff_t)kNumSMs * 2);

@@ -78,11 +78,13 @@ def test_adam_and_mse(cuda):
     assert torch.allclose(wb.float(), w, rtol=1e-2, atol=1e-2)
 
 
+@pytest.mark.parametrize("variant", [0, 1], ids=["tcgen05", "mma_sync"])
 @pytest.mark.parametrize("dtype_name", ["float32", "float64"])
-def test_fused_tensor_core_correction_matches_layer_kernels(cuda, dtype_name):
-    """The fused tensor-core inference kernel against gather + three layer kernels + scatter
-    (which the oracle pins): same network, same BF16 rounding points, FP32 accumulation in a
-    different order, so agreement to BF16 resolution."""
+def test_fused_tensor_core_correction_matches_layer_kernels(cuda, dtype_name, variant):
+    """The fused tensor-core inference kernels (tcgen05 with tensor-memory accumulators, and
+    warp-level mma.sync) against gather + three layer kernels + scatter (which the oracle
+    pins): same network, same BF16 rounding points, FP32 accumulation in a different order,
+    so agreement to BF16 resolution."""
     import torch
 
     from sfem_gb300.learned import PatchNet
@@ -107,9 +109,15 @@ def test_fused_tensor_core_correction_matches_layer_kernels(cuda, dtype_name):
                                                 capi.vp(frag), None), "fragments")
     rt = capi.FLOAT32 if dt == torch.float32 else capi.FLOAT64
     d_fused = torch.zeros(N, dtype=dt, device=cuda)
-    capi.check(lib.sfem_gb300_learned_correction(rt, capi.i64(P), fine.lidx_ptrs.ptr, capi.vp(r), capi.vp(inv),
-                                                 capi.vp(frag), capi.vp(fine.count), ctypes.c_double(0.7),
-                                                 capi.vp(d_fused), None), "fused")
+    capi.check(lib.sfem_gb300_set_learned_kernel(variant), "variant")
+    try:
+        capi.check(lib.sfem_gb300_learned_correction(rt, capi.i64(P), fine.lidx_ptrs.ptr, capi.vp(r), capi.vp(inv),
+                                                     capi.vp(frag), capi.vp(fine.count), ctypes.c_double(0.7),
+                                                     capi.vp(d_fused), None), "fused")
+        torch.cuda.synchronize()
+    finally:
+        capi.check(lib.sfem_gb300_set_learned_kernel(0), "variant")
+    assert lib.sfem_gb300_learned_status() == 0
     a0 = torch.empty((P, 125), dtype=torch.bfloat16, device=cuda)
     ps = torch.empty(P, dtype=torch.float32, device=cuda)
     capi.check(lib.sfem_gb300_gather_patches(rt, capi.i64(P), fine.lidx_ptrs.ptr, capi.vp(r), capi.vp(inv),
