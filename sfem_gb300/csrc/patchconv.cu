@@ -477,39 +477,45 @@ __global__ void __launch_bounds__(32 * LC_WARPS, 2) learned_correction_kernel(
 
 // ---------------------------------------------------------------------------- tcgen05 inference
 // The same fused correction on the 5th-generation tensor cores.  One CTA of four
-// warps owns one patch at a time; one thread issues tcgen05.mma (M = 128 positions,
-// N = 16 channels, K = 16, BF16 in, FP32 accumulate in tensor memory) and the four
+// warps owns one patch at a time (four CTAs per SM); tcgen05.mma (M = 128, K = 16,
+// BF16 in, FP32 accumulate in tensor memory) is issued by lane 0 of each warp, so up
+// to four independent accumulation chains are in flight (one thread issues one MMA
+// every ~56 cycles, far below the tensor pipe's rate at these small N), and the four
 // warps read the accumulators back with tcgen05.ld (warp w owns TMEM lanes 32w..32w+31).
 //
-// Every layer's GEMM rows are padded positions q = TC_Q0 + i, i < 256 (two M tiles),
+// conv1 / conv2 rows are padded positions q = TC_Q0 + i, i < 256 (two M tiles),
 // which cover the 125 interior positions (57..285 of the 7^3 padded grid); rows that
-// are halo positions are computed and discarded.  The activations of conv1 / conv2
-// are stored as [channel chunk][padded position][8 BF16] rows of 16 bytes with a zero
-// halo, so the A operand of tap t is the activation buffer started off_delta(t) rows
-// later (a descriptor start-address shift, no im2col copy).  conv1 has one input
-// channel: its A operand is an im2col of the padded input with K = 27 taps (+5 zero).
-// conv3 (16 -> 1) uses output column 0 of an N = 16 GEMM.
+// are halo positions are computed and discarded.  Activations are stored as
+// [channel chunk][padded position][8 BF16] rows of 16 bytes with a zero halo, so the
+// A operand of tap t is the activation buffer started off_delta(t) rows later (a
+// descriptor start-address shift, no im2col copy).
+//   conv1 (1 -> 16): A = im2col of the padded input, K = 27 taps (+5 zero), 2 K steps.
+//   conv2 (16 -> 16): 27 taps x 2 tiles, each tile's taps split in two halves
+//                     accumulated separately (four chains), summed in the epilogue.
+//   conv3 (16 -> 1):  taps as GEMM columns: D3[r][t] = sum_ci act2[r][ci] W3[ci][t]
+//                     for all rows r < 384 (3 tiles, N = 32), then out[q] =
+//                     sum_t D3[q + off_delta(t)][t] through shared memory.
 constexpr int TC_Q0 = PP * PP + PP + 1;  // 57: padded index of patch node 0
 constexpr int TC_ROWS = 384;             // activation rows: max q + off_delta = 312 + 57 = 369
 constexpr int TC_ACT_CHUNK = TC_ROWS * 16;
 constexpr int TC_COL_CHUNK = 256 * 16;
-constexpr int TC_B1_BYTES = 2 * 2 * 16 * 16;   // [kstep][chunk][n][8] BF16
-constexpr int TC_B2_BYTES = 27 * 2 * 16 * 16;  // [tap][chunk][n][8]
-constexpr int TC_OPERAND_BYTES = TC_B1_BYTES + 2 * TC_B2_BYTES;  // B1, B2, B3
+constexpr int TC_B1_BYTES = 2 * 2 * 16 * 16;   // [kstep][chunk][n 16][8] BF16
+constexpr int TC_B2_BYTES = 27 * 2 * 16 * 16;  // [tap][chunk][n 16][8]
+constexpr int TC_B3_BYTES = 2 * 32 * 16;       // [chunk][n = tap 32][8]
+constexpr int TC_OPERAND_BYTES = TC_B1_BYTES + TC_B2_BYTES + TC_B3_BYTES;
 constexpr int TC_OFF_B1 = 0, TC_OFF_B2 = TC_B1_BYTES, TC_OFF_B3 = TC_B1_BYTES + TC_B2_BYTES;
 constexpr int TC_OFF_ACT1 = TC_OPERAND_BYTES;
-constexpr int TC_OFF_ACT2 = TC_OFF_ACT1 + 2 * TC_ACT_CHUNK;
-constexpr int TC_OFF_COL = TC_OFF_ACT2 + 2 * TC_ACT_CHUNK;
+constexpr int TC_OFF_COL = TC_OFF_ACT1 + 2 * TC_ACT_CHUNK;  // im2col, then act2, then the conv3 dump
 constexpr int TC_OFF_A0 = TC_OFF_COL + 4 * TC_COL_CHUNK;
-constexpr int TC_OFF_OUT = TC_OFF_A0 + TC_ROWS * 2;
-constexpr int TC_OFF_RED = TC_OFF_OUT + 128 * 4;
+constexpr int TC_OFF_RED = TC_OFF_A0 + TC_ROWS * 2;
 constexpr int TC_SMEM = TC_OFF_RED + 16;
-constexpr int TC_CTAS_PER_SM = 3;
-constexpr uint32_t TC_TMEM_COLS = 128;  // D1 cols 0..31, D2 32..63, D3 64..95
+constexpr int TC_CTAS_PER_SM = 4;
+constexpr uint32_t TC_TMEM_COLS = 128;  // D1 cols 0..31, D2 32..95, then D3 0..95
 constexpr int TC_WAIT_POLLS = 1 << 20;
-static_assert(TC_SMEM * TC_CTAS_PER_SM <= 227 * 1024, "shared memory of the resident CTAs");
+static_assert((TC_SMEM + 1024 + 1024) * TC_CTAS_PER_SM <= 228 * 1024, "shared memory of the resident CTAs");
 static_assert(TC_TMEM_COLS * TC_CTAS_PER_SM <= 512, "tensor memory of the resident CTAs");
 static_assert(TC_Q0 + 255 + TC_Q0 < TC_ROWS, "shifted operand rows stay inside the activation buffer");
+static_assert(2 * TC_ACT_CHUNK <= 4 * TC_COL_CHUNK && 27 * PV * 4 <= 4 * TC_COL_CHUNK, "aliases of the col region");
 
 __device__ int g_lc_status;  // nonzero: a tensor-core wait gave up (kernel returned early)
 
@@ -517,64 +523,47 @@ __device__ int g_lc_status;  // nonzero: a tensor-core wait gave up (kernel retu
 __global__ void learned_tc_operands_kernel(const __nv_bfloat16 *__restrict__ W1, const __nv_bfloat16 *__restrict__ W2,
                                            const __nv_bfloat16 *__restrict__ W3, __nv_bfloat16 *__restrict__ out) {
     const __nv_bfloat16 zero = __float2bfloat16(0.f);
-    constexpr int n1 = TC_B1_BYTES / 2, n2 = TC_B2_BYTES / 2;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n1 + 2 * n2; i += gridDim.x * blockDim.x) {
+    constexpr int n1 = TC_B1_BYTES / 2, n2 = TC_B2_BYTES / 2, n3 = TC_B3_BYTES / 2;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n1 + n2 + n3; i += gridDim.x * blockDim.x) {
         if (i < n1) {  // conv1: k = tap = 16 s + 8 c + e, n = co
             const int e = i % 8, n = (i / 8) % 16, c = (i / 128) % 2, st = i / 256;
             const int k = 16 * st + 8 * c + e;
             out[i] = k < 27 ? W1[n * 27 + k] : zero;
-        } else {
-            const int j = (i - n1) % n2, layer = (i - n1) / n2;
+        } else if (i < n1 + n2) {  // conv2 tap t: n = co, k = ci
+            const int j = i - n1;
             const int e = j % 8, n = (j / 8) % 16, c = (j / 128) % 2, t = j / 256;
-            const int ci = 8 * c + e;
-            if (layer == 0)
-                out[i] = W2[(n * KMAX_C + ci) * 27 + t];
-            else
-                out[i] = n == 0 ? W3[ci * 27 + t] : zero;
+            out[i] = W2[(n * KMAX_C + 8 * c + e) * 27 + t];
+        } else {  // conv3: n = tap, k = ci
+            const int j = i - n1 - n2;
+            const int e = j % 8, t = (j / 8) % 32, c = j / 256;
+            out[i] = t < 27 ? W3[(8 * c + e) * 27 + t] : zero;
         }
     }
 }
 
 __device__ __forceinline__ bool tc_interior(int q) {
     const int x = q % PP, y = (q / PP) % PP, z = q / (PP * PP);
-    return q < PPV && x >= 1 && x <= PN && y >= 1 && y <= PN && z >= 1 && z <= PN;
+    return q >= 0 && q < PPV && x >= 1 && x <= PN && y >= 1 && y <= PN && z >= 1 && z <= PN;
 }
 
-// epilogue of conv1 / conv2: ReLU, BF16, rows of interior positions into the activation buffer
-__device__ __forceinline__ void tc_store_act(uint32_t tmem_d, unsigned char *act, int warp, int lane) {
+__device__ __forceinline__ void tc_store_row(unsigned char *act, int q, const float (&v)[16], bool keep) {
 #pragma unroll
-    for (int h = 0; h < 2; h++) {
-        float v[16];
-        tc::tmem_ld16(tmem_d + ((uint32_t)(32 * warp) << 16) + 16 * h, v);
-        const int q = TC_Q0 + 128 * h + 32 * warp + lane;
-        if (tc_interior(q)) {
-#pragma unroll
-            for (int c = 0; c < 2; c++) {
-                uint4 w;
-                w.x = pack_bf16(fmaxf(v[8 * c + 0], 0.f), fmaxf(v[8 * c + 1], 0.f));
-                w.y = pack_bf16(fmaxf(v[8 * c + 2], 0.f), fmaxf(v[8 * c + 3], 0.f));
-                w.z = pack_bf16(fmaxf(v[8 * c + 4], 0.f), fmaxf(v[8 * c + 5], 0.f));
-                w.w = pack_bf16(fmaxf(v[8 * c + 6], 0.f), fmaxf(v[8 * c + 7], 0.f));
-                *reinterpret_cast<uint4 *>(act + c * TC_ACT_CHUNK + q * 16) = w;
-            }
+    for (int c = 0; c < 2; c++) {
+        uint4 w = make_uint4(0, 0, 0, 0);
+        if (keep) {
+            w.x = pack_bf16(fmaxf(v[8 * c + 0], 0.f), fmaxf(v[8 * c + 1], 0.f));
+            w.y = pack_bf16(fmaxf(v[8 * c + 2], 0.f), fmaxf(v[8 * c + 3], 0.f));
+            w.z = pack_bf16(fmaxf(v[8 * c + 4], 0.f), fmaxf(v[8 * c + 5], 0.f));
+            w.w = pack_bf16(fmaxf(v[8 * c + 6], 0.f), fmaxf(v[8 * c + 7], 0.f));
         }
+        *reinterpret_cast<uint4 *>(act + c * TC_ACT_CHUNK + q * 16) = w;
     }
 }
 
-// one tap-shifted layer: 27 taps x 2 M tiles into D columns [dcol, dcol + 32)
-__device__ __forceinline__ void tc_issue_shift_layer(uint32_t act, uint32_t bops, uint32_t tmem_d) {
-    constexpr uint32_t id = tc::idesc_bf16_f32(128, 16);
-#pragma unroll 1
-    for (int t = 0; t < 27; t++) {
-        const int dz = t / 9 - 1, dy = (t / 3) % 3 - 1, dx = t % 3 - 1;
-        const int off = dz * PP * PP + dy * PP + dx;
-        const uint64_t bd = tc::sdesc(bops + 512 * t, 256, 128);
-#pragma unroll
-        for (int h = 0; h < 2; h++) {
-            const uint64_t ad = tc::sdesc(act + 16 * (TC_Q0 + 128 * h + off), TC_ACT_CHUNK, 128);
-            tc::mma_bf16(tmem_d + 16 * h, ad, bd, id, t > 0);
-        }
-    }
+__device__ __forceinline__ void tc_sync() {
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
 }
 
 // d[g] += omega * s_p * net(patch_p)[v] / count[g] for every patch p (g = elements[v][p])
@@ -585,37 +574,57 @@ __global__ void __launch_bounds__(128, TC_CTAS_PER_SM) learned_correction_tc_ker
     extern __shared__ __align__(16) unsigned char tcs[];
     __shared__ __align__(8) uint64_t mbar;
     __shared__ uint32_t tmem_holder;
+    __shared__ const idx_t *srow[PV];  // connectivity row pointers, loaded once
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     __nv_bfloat16 *a0 = reinterpret_cast<__nv_bfloat16 *>(tcs + TC_OFF_A0);
-    float *outp = reinterpret_cast<float *>(tcs + TC_OFF_OUT);
     float *red = reinterpret_cast<float *>(tcs + TC_OFF_RED);
-    // operands in, activation / im2col / input buffers zeroed (their halo rows stay zero)
+    float *dump = reinterpret_cast<float *>(tcs + TC_OFF_COL);  // [tap][patch node]
+    unsigned char *act1 = tcs + TC_OFF_ACT1, *act2 = tcs + TC_OFF_COL;
+    // operands in; activation / im2col / input buffers zeroed (halo rows of act1 and a0 stay zero)
     for (int i = tid; i < TC_OPERAND_BYTES / 16; i += 128) reinterpret_cast<uint4 *>(tcs)[i] = operands[i];
-    for (int i = TC_OPERAND_BYTES / 16 + tid; i < TC_OFF_OUT / 16; i += 128)
+    for (int i = TC_OPERAND_BYTES / 16 + tid; i < TC_OFF_RED / 16; i += 128)
         reinterpret_cast<uint4 *>(tcs)[i] = make_uint4(0, 0, 0, 0);
+    if (tid < PV) srow[tid] = elements[tid];
     if (warp == 0) tc::tmem_alloc(&tmem_holder, TC_TMEM_COLS);
-    if (tid == 0) tc::mbar_init(&mbar, 1);
+    if (tid == 0) tc::mbar_init(&mbar, 4);  // one arrival per issuing warp and layer
     tc::fence_async_smem();
-    tc::fence_before_sync();
-    __syncthreads();
-    tc::fence_after_sync();
+    tc_sync();
     const uint32_t tmem = tmem_holder;
-    const uint32_t s_b1 = tc::smem_u32(tcs + TC_OFF_B1), s_b2 = tc::smem_u32(tcs + TC_OFF_B2),
-                   s_b3 = tc::smem_u32(tcs + TC_OFF_B3), s_act1 = tc::smem_u32(tcs + TC_OFF_ACT1),
-                   s_act2 = tc::smem_u32(tcs + TC_OFF_ACT2), s_col = tc::smem_u32(tcs + TC_OFF_COL);
+    const uint32_t lane_base = (uint32_t)(32 * warp) << 16;
+    const bool issuer = lane == 0;
+    constexpr uint32_t id16 = tc::idesc_bf16_f32(128, 16), id32 = tc::idesc_bf16_f32(128, 32);
+    const uint64_t d_col = tc::sdesc(tc::smem_u32(tcs + TC_OFF_COL), TC_COL_CHUNK, 128);
+    const uint64_t d_act1 = tc::sdesc(tc::smem_u32(act1), TC_ACT_CHUNK, 128);
+    const uint64_t d_act2 = tc::sdesc(tc::smem_u32(act2), TC_ACT_CHUNK, 128);
+    const uint64_t d_b1 = tc::sdesc(tc::smem_u32(tcs + TC_OFF_B1), 256, 128);
+    const uint64_t d_b2 = tc::sdesc(tc::smem_u32(tcs + TC_OFF_B2), 256, 128);
+    const uint64_t d_b3 = tc::sdesc(tc::smem_u32(tcs + TC_OFF_B3), 512, 128);
     uint32_t phase = 0;
     bool ok = true;
+    // thread v owns patch node v; the next patch's node index is loaded one patch ahead and
+    // its residual value after the current patch's first tensor-core wait
+    const int v = tid;
+    auto load_val = [&](idx_t g) {
+        float x = (float)r[g];
+        if (inv_diag) x *= (float)inv_diag[g];
+        return x;
+    };
+    idx_t gv_next = 0;
+    float val_next = 0.f;
+    if ((ptrdiff_t)blockIdx.x < P && v < PV) {
+        gv_next = srow[v][blockIdx.x];
+        val_next = load_val(gv_next);
+    }
+    // the interior position of each of this thread's conv1 / conv2 rows
+    const int q0 = TC_Q0 + 32 * warp + lane, q1 = q0 + 128;
+    const bool in0 = tc_interior(q0), in1 = tc_interior(q1);
     for (ptrdiff_t p = blockIdx.x; p < P && ok; p += gridDim.x) {
-        // gather D^-1 r, normalise by the patch RMS (thread v owns patch node v)
-        const int v = tid;
-        idx_t gv = 0;
-        float val = 0.f;
-        if (v < PV) {
-            gv = elements[v][p];
-            float x = (float)r[gv];
-            if (inv_diag) x *= (float)inv_diag[gv];
-            val = x;
-        }
+        // D^-1 r of this patch, normalised by the patch RMS
+        const idx_t gv = gv_next;
+        const float val = val_next;
+        const ptrdiff_t pn = p + gridDim.x;
+        const bool has_next = pn < P && v < PV;
+        if (has_next) gv_next = srow[v][pn];
         float ss = val * val;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o);
@@ -644,72 +653,114 @@ __global__ void __launch_bounds__(128, TC_CTAS_PER_SM) learned_correction_tc_ker
             }
         }
         tc::fence_async_smem();
-        tc::fence_before_sync();
-        __syncthreads();
-        tc::fence_after_sync();
-        if (tid == 0) {
-            constexpr uint32_t id = tc::idesc_bf16_f32(128, 16);
-#pragma unroll
-            for (int h = 0; h < 2; h++)
+        tc_sync();
+        // conv1: warp h < 2 issues tile h (two K steps into cols 16h)
+        if (issuer) {
+            if (warp < 2) {
 #pragma unroll
                 for (int st = 0; st < 2; st++)
-                    tc::mma_bf16(tmem + 16 * h, tc::sdesc(s_col + 2 * st * TC_COL_CHUNK + h * 128 * 16, TC_COL_CHUNK, 128),
-                                 tc::sdesc(s_b1 + 512 * st, 256, 128), id, st > 0);
+                    tc::mma_bf16(tmem + 16 * warp, d_col + (uint64_t)(2 * st * TC_COL_CHUNK / 16 + warp * 128),
+                                 d_b1 + (uint64_t)(32 * st), id16, st > 0);
+            }
             tc::commit(&mbar);
         }
         ok = __syncthreads_and(tc::mbar_wait(&mbar, phase, TC_WAIT_POLLS));
         phase ^= 1;
         tc::fence_after_sync();
         if (!ok) break;
-        tc_store_act(tmem + 0, tcs + TC_OFF_ACT1, warp, lane);
+        if (has_next) val_next = load_val(gv_next);
+        {
+            float a[16], b[16];
+            tc::tmem_ld16(tmem + lane_base + 0, a);
+            tc::tmem_ld16(tmem + lane_base + 16, b);
+            if (in0) tc_store_row(act1, q0, a, true);
+            if (in1) tc_store_row(act1, q1, b, true);
+        }
         tc::fence_async_smem();
-        tc::fence_before_sync();
-        __syncthreads();
-        tc::fence_after_sync();
-        if (tid == 0) {
-            tc_issue_shift_layer(s_act1, s_b2, tmem + 32);
-            tc::commit(&mbar);
-        }
-        ok = __syncthreads_and(tc::mbar_wait(&mbar, phase, TC_WAIT_POLLS));
-        phase ^= 1;
-        tc::fence_after_sync();
-        if (!ok) break;
-        tc_store_act(tmem + 32, tcs + TC_OFF_ACT2, warp, lane);
-        tc::fence_async_smem();
-        tc::fence_before_sync();
-        __syncthreads();
-        tc::fence_after_sync();
-        if (tid == 0) {
-            tc_issue_shift_layer(s_act2, s_b3, tmem + 64);
-            tc::commit(&mbar);
-        }
-        ok = __syncthreads_and(tc::mbar_wait(&mbar, phase, TC_WAIT_POLLS));
-        phase ^= 1;
-        tc::fence_after_sync();
-        if (!ok) break;
-        // conv3 output (column 0), rounded like the stored activations of the layer kernels
+        tc_sync();
+        // conv2: warp w = 2 h + s issues tile h, taps [14 s, 14 s + 14) into cols 32 + 32 h + 16 s
+        if (issuer) {
+            const int h = warp >> 1, sh = warp & 1;
+            const uint32_t dcol = tmem + 32 + 32 * h + 16 * sh;
+            const uint64_t arow = d_act1 + (uint64_t)(TC_Q0 + 128 * h);
+            if (sh == 0) {
 #pragma unroll
-        for (int h = 0; h < 2; h++) {
-            const float o = tc::tmem_ld1(tmem + ((uint32_t)(32 * warp) << 16) + 64 + 16 * h);
-            const int q = TC_Q0 + 128 * h + 32 * warp + lane;
-            if (tc_interior(q)) {
-                const int x = q % PP - 1, y = (q / PP) % PP - 1, z = q / (PP * PP) - 1;
-                outp[(z * PN + y) * PN + x] = __bfloat162float(__float2bfloat16(o));
+                for (int t = 0; t < 14; t++)
+                    tc::mma_bf16(dcol, arow + (uint64_t)(int64_t)off_delta(t), d_b2 + (uint64_t)(32 * t), id16, t > 0);
+            } else {
+#pragma unroll
+                for (int t = 14; t < 27; t++)
+                    tc::mma_bf16(dcol, arow + (uint64_t)(int64_t)off_delta(t), d_b2 + (uint64_t)(32 * t), id16,
+                                 t > 14);
+            }
+            tc::commit(&mbar);
+        }
+        ok = __syncthreads_and(tc::mbar_wait(&mbar, phase, TC_WAIT_POLLS));
+        phase ^= 1;
+        tc::fence_after_sync();
+        if (!ok) break;
+        {
+            // act2 = ReLU(D2 halves summed); every one of its 384 rows is rewritten (the
+            // region is shared with the im2col buffer and the conv3 dump)
+            float a[16], b[16];
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                tc::tmem_ld16(tmem + lane_base + 32 + 32 * h, a);
+                tc::tmem_ld16(tmem + lane_base + 48 + 32 * h, b);
+#pragma unroll
+                for (int j = 0; j < 16; j++) a[j] += b[j];
+                tc_store_row(act2, h ? q1 : q0, a, h ? in1 : in0);
+            }
+            const int zrow = tid < TC_Q0 ? tid : TC_Q0 + 256 + (tid - TC_Q0);  // rows 0..56, 313..383
+            tc_store_row(act2, zrow, a, false);
+        }
+        tc::fence_async_smem();
+        tc_sync();
+        // conv3: warp h < 3 issues tile h (rows 128 h ..), N = 32 taps, into cols 32 h
+        if (issuer) {
+            if (warp < 3) tc::mma_bf16(tmem + 32 * warp, d_act2 + (uint64_t)(128 * warp), d_b3, id32, 0);
+            tc::commit(&mbar);
+        }
+        ok = __syncthreads_and(tc::mbar_wait(&mbar, phase, TC_WAIT_POLLS));
+        phase ^= 1;
+        tc::fence_after_sync();
+        if (!ok) break;
+        // dump D3[row][t] to dump[t][v] for the patch node v = row - off_delta(t)
+#pragma unroll 1
+        for (int h = 0; h < 3; h++) {
+            const int row = 128 * h + 32 * warp + lane;
+            const int rx = row % PP, ry = (row / PP) % PP, rz = row / (PP * PP);
+#pragma unroll
+            for (int part = 0; part < 2; part++) {
+                float a[16];
+                tc::tmem_ld16(tmem + lane_base + 32 * h + 16 * part, a);
+#pragma unroll
+                for (int j = 0; j < 16; j++) {
+                    const int t = 16 * part + j;
+                    if (t < 27) {
+                        // patch node (rx - dx - 1, ry - dy - 1, rz - dz - 1) when inside the patch
+                        const int x = rx - (t % 3 - 1) - 1, y = ry - ((t / 3) % 3 - 1) - 1, z = rz - (t / 9 - 1) - 1;
+                        if ((unsigned)x < PN && (unsigned)y < PN && (unsigned)z < PN && row < PPV)
+                            dump[t * PV + (z * PN + y) * PN + x] = a[j];
+                    }
+                }
             }
         }
-        tc::fence_before_sync();
-        __syncthreads();
-        tc::fence_after_sync();
-        if (v < PV) atomicAdd(&d[gv], (T)omega * (T)(sc * outp[v]) / (T)count[gv]);
+        tc_sync();
+        if (v < PV) {
+            float o = 0.f;
+#pragma unroll
+            for (int t = 0; t < 27; t++) o += dump[t * PV + v];
+            o = __bfloat162float(__float2bfloat16(o));  // rounded like the stored activations of the layer kernels
+            atomicAdd(&d[gv], (T)omega * (T)(sc * o) / (T)count[gv]);
+        }
     }
     if (!ok) {
         if (tid == 0) atomicExch(&g_lc_status, 1);
         // let the MMAs still in flight finish (bounded) before the tensor memory is released
         tc::mbar_wait(&mbar, phase ^ 1, TC_WAIT_POLLS);
     }
-    tc::fence_before_sync();
-    __syncthreads();
-    tc::fence_after_sync();
+    tc_sync();
     if (warp == 0) tc::tmem_dealloc(tmem, TC_TMEM_COLS);
 }
 
