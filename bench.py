@@ -222,8 +222,8 @@ def time_apply(op, x, y, steps, warmup, flush, stream):
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
     for k in range(steps):
-        flush.fill_(k & 0xFF)
         y.zero_()
+        flush.fill_(k & 0xFF)  # after the reset, so y too comes from HBM
         starts[k].record(stream)
         op.apply(x, y)
         ends[k].record(stream)
@@ -463,7 +463,8 @@ def run_ours(args):
         op.apply(x, y)
     torch.cuda.synchronize()
     # device-timed region: events around each apply (the y.zero_ is the
-    # accumulate-interface's caller-side reset and is excluded), L2 flushed before each step
+    # accumulate-interface's caller-side reset and is excluded), L2 flushed after the reset
+    # and before each step, so x, y, connectivity and metric all come from HBM
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     if world > 1:
@@ -472,8 +473,8 @@ def run_ours(args):
     with ClockSampler(local) as clk:
         wall0 = time.perf_counter()
         for k in range(args.steps):
-            flush.fill_(k & 0xFF)
             y.zero_()
+            flush.fill_(k & 0xFF)  # after the reset, so y too comes from HBM
             starts[k].record(stream)
             op.apply(x, y)
             ends[k].record(stream)
@@ -523,8 +524,10 @@ def run_ours(args):
             solve["batched_serving"] = measure_batch(dev, args.batch_problems)
 
     peak, peak_kind = measured_peak_hbm()
-    alg_bytes = 2 * 4 * N + (4 * (LEVEL + 1) ** 3 + 24) * E
-    alg_bytes64 = 2 * 8 * N + (4 * (LEVEL + 1) ** 3 + 24) * E
+    # compulsory bytes of y += A x through the accumulate interface: x read, y read and
+    # written (the caller's reset is a separate pass), connectivity and FFF read once
+    alg_bytes = 3 * 4 * N + (4 * (LEVEL + 1) ** 3 + 24) * E
+    alg_bytes64 = 3 * 8 * N + (4 * (LEVEL + 1) ** 3 + 24) * E
     achieved = alg_bytes / t_kernel / 1e9
     fp64_flops = 2 * 64 * (LEVEL ** 3) * E  # element-matrix form, 128 flop per micro element
     line = {
@@ -533,7 +536,7 @@ def run_ours(args):
         "ms_per_step": t_kernel * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": "sshex8_laplacian_apply_L4_48cube", "nodes": N, "macro_elements": E, "level": LEVEL,
-                   "perturb": PERTURB, "seed": SEED, "l2": "flushed (512 MiB write) before every timed step",
+                   "perturb": PERTURB, "seed": SEED, "l2": "flushed (512 MiB write) after the y reset, before every timed step",
                    "parallelism": f"replicas{world}" if world > 1 else "single"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": TRAFFIC_BYTES_PER_LAUNCH, "peak_kind": peak_kind, "algorithmic_bytes": alg_bytes},

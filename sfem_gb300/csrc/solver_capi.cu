@@ -696,10 +696,16 @@ int sfem_gb300_solver_set_fallback(void *solver, void *learned) {
     std::function<void()> fn;
     if (l->f) {
         auto ls = std::static_pointer_cast<LearnedSmoother<float>>(l->impl);
-        fn = [ls]() { ls->use_fallback = true; };
+        fn = [ls]() {
+            ls->use_fallback = true;
+            ls->blas.ctx->epoch++;
+        };
     } else {
         auto ls = std::static_pointer_cast<LearnedSmoother<double>>(l->impl);
-        fn = [ls]() { ls->use_fallback = true; };
+        fn = [ls]() {
+            ls->use_fallback = true;
+            ls->blas.ctx->epoch++;
+        };
     }
     if (h->kind == "cg") {
         if (h->f)
@@ -729,20 +735,30 @@ int sfem_gb300_learned_smoother_set_chain(void *solver, int chain) {
     auto *h = H(solver);
     if (h->kind != "learned") return set_error("not a learned-smoother handle");
     if (chain < 0 || chain > 2) return set_error("sfem_gb300_learned_smoother_set_chain: chain must be 0, 1 or 2");
-    if (h->f)
-        std::static_pointer_cast<LearnedSmoother<float>>(h->impl)->chain = chain;
-    else
-        std::static_pointer_cast<LearnedSmoother<double>>(h->impl)->chain = chain;
+    if (h->f) {
+        auto ls = std::static_pointer_cast<LearnedSmoother<float>>(h->impl);
+        ls->chain = chain;
+        ls->blas.ctx->epoch++;
+    } else {
+        auto ls = std::static_pointer_cast<LearnedSmoother<double>>(h->impl);
+        ls->chain = chain;
+        ls->blas.ctx->epoch++;
+    }
     return SFEM_GB300_SUCCESS;
 }
 
 int sfem_gb300_learned_smoother_use_fallback(void *solver, int use_fallback) {
     auto *h = H(solver);
     if (h->kind != "learned") return set_error("not a learned-smoother handle");
-    if (h->f)
-        std::static_pointer_cast<LearnedSmoother<float>>(h->impl)->use_fallback = use_fallback != 0;
-    else
-        std::static_pointer_cast<LearnedSmoother<double>>(h->impl)->use_fallback = use_fallback != 0;
+    if (h->f) {
+        auto ls = std::static_pointer_cast<LearnedSmoother<float>>(h->impl);
+        ls->use_fallback = use_fallback != 0;
+        ls->blas.ctx->epoch++;
+    } else {
+        auto ls = std::static_pointer_cast<LearnedSmoother<double>>(h->impl);
+        ls->use_fallback = use_fallback != 0;
+        ls->blas.ctx->epoch++;
+    }
     return SFEM_GB300_SUCCESS;
 }
 

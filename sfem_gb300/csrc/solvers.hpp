@@ -101,6 +101,9 @@ struct Context {
     std::vector<double *> blocks;
     int next_slot{kSlotBlock};
     double *h_scalar{nullptr};  // pinned staging for host reads
+    // bumped whenever a solver changes which kernels it launches (e.g. a learned
+    // smoother switching to its fallback): captured CUDA graphs of older epochs are stale
+    uint64_t epoch{0};
 
     static std::shared_ptr<Context> create(cudaStream_t s, int = 0) {
         auto c = std::make_shared<Context>();
@@ -764,6 +767,7 @@ public:
         cudaGraphExec_t exec;
     };
     std::vector<GraphEntry> graphs;
+    uint64_t graph_epoch{0};
     cudaStream_t gstream{nullptr};
     cudaEvent_t ev_in{nullptr}, ev_out{nullptr};
     int warm{0};
@@ -786,6 +790,10 @@ public:
     }
     int apply(const T *b, T *x) override {
         SFEM_GB300_CHECK(ensure_init());
+        if (use_graph && graph_epoch != blas.ctx->epoch) {
+            release_graphs();
+            graph_epoch = blas.ctx->epoch;
+        }
         if (!use_graph || atol > 0 || warm < 1) {
             if (use_graph) warm++;  // first call eager: sizes every lazily allocated buffer
             return run_cycles(b, x);

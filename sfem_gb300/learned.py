@@ -326,7 +326,8 @@ def hierarchy_with_coefficient(mesh, k, device, base=None, coarsen_macro=True):
 
 
 def run_experiment(nx=32, draws=64, n_pairs=100_000, epochs=30, eval_draws=2, device="cuda:0", seed=0, log=None,
-                   rtol=1e-10, placement="before", arms=("chebyshev3", "learned", "mixed", "mixed_learned")):
+                   rtol=1e-10, placement="before", arms=("chebyshev3", "learned", "mixed", "mixed_learned"),
+                   graph=True):
     """Train on ``draws`` coefficient fields, then A/B on fresh draws: FP64 flexible CG
     preconditioned by the FP64 multigrid (chebyshev3), the same plus the learned correction
     (learned), the FP32 multigrid through the precision bridge (mixed), and that plus the
@@ -334,7 +335,9 @@ def run_experiment(nx=32, draws=64, n_pairs=100_000, epochs=30, eval_draws=2, de
 
     placement="before": pairs harvested after each coarse-grid correction of the finest
     level and the correction applied there, before the Chebyshev3 post-smoothing;
-    "after": pairs after complete V-cycles, correction after the post-smoothing."""
+    "after": pairs after complete V-cycles, correction after the post-smoothing.
+    graph=True replays every arm's V-cycle as a captured CUDA graph (the learned
+    correction has no host synchronisation; a switch to the fallback re-captures)."""
     import torch
 
     from .coefficients import lognormal_coefficient
@@ -376,12 +379,16 @@ def run_experiment(nx=32, draws=64, n_pairs=100_000, epochs=30, eval_draws=2, de
             ctx = S.context()
             learned_arm = name.endswith("learned")
             if name in ("chebyshev3", "learned"):
-                mg, op = (learned_mg(ctx, H, net, torch.float64, chain=chain, coarse="dense") if learned_arm else
-                          S.build_poisson_mg(ctx, H, torch.float64, smoother="chebyshev3", sweeps=2, coarse="dense"))
+                mg, op = (learned_mg(ctx, H, net, torch.float64, chain=chain, coarse="dense", graph=graph)
+                          if learned_arm else
+                          S.build_poisson_mg(ctx, H, torch.float64, smoother="chebyshev3", sweeps=2, coarse="dense",
+                                             graph=graph))
                 pc, op64 = mg, op
             else:
-                mg, _ = (learned_mg(ctx, H, net, torch.float32, chain=chain, coarse="dense") if learned_arm else
-                         S.build_poisson_mg(ctx, H, torch.float32, smoother="chebyshev3", sweeps=2, coarse="dense"))
+                mg, _ = (learned_mg(ctx, H, net, torch.float32, chain=chain, coarse="dense", graph=graph)
+                         if learned_arm else
+                         S.build_poisson_mg(ctx, H, torch.float32, smoother="chebyshev3", sweeps=2, coarse="dense",
+                                            graph=graph))
                 op64 = S.laplacian_op(ctx, H.spaces[0], H.spaces[0].fff, H.dirichlet[0], torch.float64)
                 pc = S.mixed_precond(ctx, mg)
             solver = S.cg(ctx, op64, pc, rtol=rtol, max_it=500, residual_norm=True, flexible=True)
