@@ -476,45 +476,52 @@ __global__ void __launch_bounds__(32 * LC_WARPS, 2) learned_correction_kernel(
 }
 
 // ---------------------------------------------------------------------------- tcgen05 inference
-// The same fused correction on the 5th-generation tensor cores.  One CTA of four
-// warps owns one patch at a time (four CTAs per SM); tcgen05.mma (M = 128, K = 16,
-// BF16 in, FP32 accumulate in tensor memory) is issued by lane 0 of each warp, so up
-// to four independent accumulation chains are in flight (one thread issues one MMA
-// every ~56 cycles, far below the tensor pipe's rate at these small N), and the four
-// warps read the accumulators back with tcgen05.ld (warp w owns TMEM lanes 32w..32w+31).
+// The same fused correction on the 5th-generation tensor cores.  One CTA of eight
+// warps owns one patch at a time (four CTAs per SM).  tcgen05.mma (M = 128, K = 16,
+// BF16 in, FP32 accumulate in tensor memory) is issued by lane 0 of warps 0..2, and
+// the accumulators are read back with tcgen05.ld: warps w and w + 4 share TMEM lanes
+// 32 (w % 4) .. + 31 and split the work between them by tile or by column.
 //
-// conv1 / conv2 rows are padded positions q = TC_Q0 + i, i < 256 (two M tiles),
-// which cover the 125 interior positions (57..285 of the 7^3 padded grid); rows that
-// are halo positions are computed and discarded.  Activations are stored as
-// [channel chunk][padded position][8 BF16] rows of 16 bytes with a zero halo, so the
-// A operand of tap t is the activation buffer started off_delta(t) rows later (a
-// descriptor start-address shift, no im2col copy).
-//   conv1 (1 -> 16): A = im2col of the padded input, K = 27 taps (+5 zero), 2 K steps.
-//   conv2 (16 -> 16): 27 taps x 2 tiles, each tile's taps split in two halves
-//                     accumulated separately (four chains), summed in the epilogue.
+// The tensor pipe takes about 40 cycles per M = 128, K = 16 MMA whatever N is up to
+// N = 32 (measured on GB300), so the layers are arranged for few, wide MMAs:
+//   conv1 (1 -> 16):  A = im2col of the padded input (K = 27 taps + 5 zero, two K
+//                     steps) for rows q = 57 + i, i < 256 (two M tiles), N = 16.
+//   conv2 (16 -> 16): taps grouped by dx: D[r][(dx, co)] = sum_{dy,dz,ci}
+//                     act1[r + 7 dy + 49 dz][ci] W2[co][ci][(dx, dy, dz)], N = 48,
+//                     nine MMAs per tile (rows r = 56 + i); the A operand of (dy, dz) is
+//                     the activation buffer started 7 dy + 49 dz rows later (a descriptor
+//                     start-address shift).  out[r] = sum_dx D[r + dx][dx] with warp
+//                     shuffles (rows r +- 1 are the neighbouring lanes; the rows at warp
+//                     boundaries go through shared memory).
 //   conv3 (16 -> 1):  taps as GEMM columns: D3[r][t] = sum_ci act2[r][ci] W3[ci][t]
 //                     for all rows r < 384 (3 tiles, N = 32), then out[q] =
 //                     sum_t D3[q + off_delta(t)][t] through shared memory.
+// Activations are [channel chunk][padded position][8 BF16] rows of 16 bytes (7^3
+// padded grid, zero halo); rows that are halo positions are computed and discarded.
 constexpr int TC_Q0 = PP * PP + PP + 1;  // 57: padded index of patch node 0
-constexpr int TC_ROWS = 384;             // activation rows: max q + off_delta = 312 + 57 = 369
+constexpr int TC_R2 = TC_Q0 - 1;         // first conv2 row (rows r - 1 .. r + 1 of every output)
+constexpr int TC_ROWS = 384;             // activation rows: max shifted row 56 + 255 + 56 = 367
 constexpr int TC_ACT_CHUNK = TC_ROWS * 16;
 constexpr int TC_COL_CHUNK = 256 * 16;
-constexpr int TC_B1_BYTES = 2 * 2 * 16 * 16;   // [kstep][chunk][n 16][8] BF16
-constexpr int TC_B2_BYTES = 27 * 2 * 16 * 16;  // [tap][chunk][n 16][8]
-constexpr int TC_B3_BYTES = 2 * 32 * 16;       // [chunk][n = tap 32][8]
+constexpr int TC_B1_BYTES = 2 * 2 * 16 * 16;  // [kstep][chunk][n 16][8] BF16
+constexpr int TC_B2_BLOCK = 2 * 48 * 16;      // one (dy, dz): [chunk][n = (dx, co) 48][8]
+constexpr int TC_B2_BYTES = 9 * TC_B2_BLOCK;
+constexpr int TC_B3_BYTES = 2 * 32 * 16;  // [chunk][n = tap 32][8]
 constexpr int TC_OPERAND_BYTES = TC_B1_BYTES + TC_B2_BYTES + TC_B3_BYTES;
 constexpr int TC_OFF_B1 = 0, TC_OFF_B2 = TC_B1_BYTES, TC_OFF_B3 = TC_B1_BYTES + TC_B2_BYTES;
 constexpr int TC_OFF_ACT1 = TC_OPERAND_BYTES;
 constexpr int TC_OFF_COL = TC_OFF_ACT1 + 2 * TC_ACT_CHUNK;  // im2col, then act2, then the conv3 dump
 constexpr int TC_OFF_A0 = TC_OFF_COL + 4 * TC_COL_CHUNK;
-constexpr int TC_OFF_RED = TC_OFF_A0 + TC_ROWS * 2;
-constexpr int TC_SMEM = TC_OFF_RED + 16;
+constexpr int TC_OFF_XB = TC_OFF_A0 + TC_ROWS * 2;  // conv2 rows at warp boundaries: [chunk 8][2][16] float
+constexpr int TC_OFF_RED = TC_OFF_XB + 8 * 2 * 16 * 4;
+constexpr int TC_SMEM = TC_OFF_RED + 8 * 4;
+constexpr int TC_THREADS = 256;
 constexpr int TC_CTAS_PER_SM = 4;
-constexpr uint32_t TC_TMEM_COLS = 128;  // D1 cols 0..31, D2 32..95, then D3 0..95
+constexpr uint32_t TC_TMEM_COLS = 128;  // D1 cols 0..31, D2 32..127, then D3 0..95
 constexpr int TC_WAIT_POLLS = 1 << 20;
 static_assert((TC_SMEM + 1024 + 1024) * TC_CTAS_PER_SM <= 228 * 1024, "shared memory of the resident CTAs");
 static_assert(TC_TMEM_COLS * TC_CTAS_PER_SM <= 512, "tensor memory of the resident CTAs");
-static_assert(TC_Q0 + 255 + TC_Q0 < TC_ROWS, "shifted operand rows stay inside the activation buffer");
+static_assert(TC_R2 + 255 + 7 + 49 < TC_ROWS && TC_Q0 + 255 + TC_Q0 < TC_ROWS, "shifted rows stay in the buffers");
 static_assert(2 * TC_ACT_CHUNK <= 4 * TC_COL_CHUNK && 27 * PV * 4 <= 4 * TC_COL_CHUNK, "aliases of the col region");
 
 __device__ int g_lc_status;  // nonzero: a tensor-core wait gave up (kernel returned early)
@@ -529,10 +536,12 @@ __global__ void learned_tc_operands_kernel(const __nv_bfloat16 *__restrict__ W1,
             const int e = i % 8, n = (i / 8) % 16, c = (i / 128) % 2, st = i / 256;
             const int k = 16 * st + 8 * c + e;
             out[i] = k < 27 ? W1[n * 27 + k] : zero;
-        } else if (i < n1 + n2) {  // conv2 tap t: n = co, k = ci
+        } else if (i < n1 + n2) {  // conv2 (dy, dz) block g: n = 16 (dx + 1) + co, k = ci
             const int j = i - n1;
-            const int e = j % 8, n = (j / 8) % 16, c = (j / 128) % 2, t = j / 256;
-            out[i] = W2[(n * KMAX_C + 8 * c + e) * 27 + t];
+            const int e = j % 8, n = (j / 8) % 48, c = (j / 384) % 2, g = j / 768;
+            const int dxi = n / 16, co = n % 16, dyi = g % 3, dzi = g / 3;
+            const int t = dzi * 9 + dyi * 3 + dxi;
+            out[i] = W2[(co * KMAX_C + 8 * c + e) * 27 + t];
         } else {  // conv3: n = tap, k = ci
             const int j = i - n1 - n2;
             const int e = j % 8, t = (j / 8) % 32, c = j / 256;
@@ -560,6 +569,24 @@ __device__ __forceinline__ void tc_store_row(unsigned char *act, int q, const fl
     }
 }
 
+// dump[t][v] = D3[row][t] for the taps t = 16 G + j of this thread's row, v = the patch
+// node at row - off_delta(t) when that is inside the patch
+template <int G>
+__device__ __forceinline__ void tc_dump_taps(float *dump, int row, const float (&a)[16]) {
+    const int rx = row % PP - 1, ry = (row / PP) % PP - 1, rz = row / (PP * PP) - 1;
+    const int vbase = (rz * PN + ry) * PN + rx;
+#pragma unroll
+    for (int j = 0; j < 16; j++) {
+        constexpr int kLimit = 27 - 16 * G;
+        if (j < kLimit) {
+            const int t = 16 * G + j;
+            const int dx = t % 3 - 1, dy = (t / 3) % 3 - 1, dz = t / 9 - 1;
+            if ((unsigned)(rx - dx) < PN && (unsigned)(ry - dy) < PN && (unsigned)(rz - dz) < PN && row < PPV)
+                dump[t * PV + vbase - (dz * PN + dy) * PN - dx] = a[j];
+        }
+    }
+}
+
 __device__ __forceinline__ void tc_sync() {
     tc::fence_before_sync();
     __syncthreads();
@@ -568,7 +595,7 @@ __device__ __forceinline__ void tc_sync() {
 
 // d[g] += omega * s_p * net(patch_p)[v] / count[g] for every patch p (g = elements[v][p])
 template <typename T>
-__global__ void __launch_bounds__(128, TC_CTAS_PER_SM) learned_correction_tc_kernel(
+__global__ void __launch_bounds__(TC_THREADS, TC_CTAS_PER_SM) learned_correction_tc_kernel(
         ptrdiff_t P, const idx_t *const *elements, const T *__restrict__ r, const T *__restrict__ inv_diag,
         const uint4 *__restrict__ operands, const uint16_t *__restrict__ count, float omega, T *__restrict__ d) {
     extern __shared__ __align__(16) unsigned char tcs[];
@@ -576,29 +603,33 @@ __global__ void __launch_bounds__(128, TC_CTAS_PER_SM) learned_correction_tc_ker
     __shared__ uint32_t tmem_holder;
     __shared__ const idx_t *srow[PV];  // connectivity row pointers, loaded once
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int wq = warp & 3, grp = warp >> 2;  // TMEM lane quarter, warp group
     __nv_bfloat16 *a0 = reinterpret_cast<__nv_bfloat16 *>(tcs + TC_OFF_A0);
     float *red = reinterpret_cast<float *>(tcs + TC_OFF_RED);
+    float *xb = reinterpret_cast<float *>(tcs + TC_OFF_XB);
     float *dump = reinterpret_cast<float *>(tcs + TC_OFF_COL);  // [tap][patch node]
     unsigned char *act1 = tcs + TC_OFF_ACT1, *act2 = tcs + TC_OFF_COL;
     // operands in; activation / im2col / input buffers zeroed (halo rows of act1 and a0 stay zero)
-    for (int i = tid; i < TC_OPERAND_BYTES / 16; i += 128) reinterpret_cast<uint4 *>(tcs)[i] = operands[i];
-    for (int i = TC_OPERAND_BYTES / 16 + tid; i < TC_OFF_RED / 16; i += 128)
+    for (int i = tid; i < TC_OPERAND_BYTES / 16; i += TC_THREADS) reinterpret_cast<uint4 *>(tcs)[i] = operands[i];
+    for (int i = TC_OPERAND_BYTES / 16 + tid; i < TC_OFF_XB / 16; i += TC_THREADS)
         reinterpret_cast<uint4 *>(tcs)[i] = make_uint4(0, 0, 0, 0);
     if (tid < PV) srow[tid] = elements[tid];
     if (warp == 0) tc::tmem_alloc(&tmem_holder, TC_TMEM_COLS);
-    if (tid == 0) tc::mbar_init(&mbar, 4);  // one arrival per issuing warp and layer
+    if (tid == 0) tc::mbar_init(&mbar, 4);  // one arrival from lane 0 of warps 0..3 per layer
     tc::fence_async_smem();
     tc_sync();
     const uint32_t tmem = tmem_holder;
-    const uint32_t lane_base = (uint32_t)(32 * warp) << 16;
-    const bool issuer = lane == 0;
-    constexpr uint32_t id16 = tc::idesc_bf16_f32(128, 16), id32 = tc::idesc_bf16_f32(128, 32);
-    const uint64_t d_col = tc::sdesc(tc::smem_u32(tcs + TC_OFF_COL), TC_COL_CHUNK, 128);
-    const uint64_t d_act1 = tc::sdesc(tc::smem_u32(act1), TC_ACT_CHUNK, 128);
-    const uint64_t d_act2 = tc::sdesc(tc::smem_u32(act2), TC_ACT_CHUNK, 128);
-    const uint64_t d_b1 = tc::sdesc(tc::smem_u32(tcs + TC_OFF_B1), 256, 128);
-    const uint64_t d_b2 = tc::sdesc(tc::smem_u32(tcs + TC_OFF_B2), 256, 128);
-    const uint64_t d_b3 = tc::sdesc(tc::smem_u32(tcs + TC_OFF_B3), 512, 128);
+    const uint32_t lane_base = (uint32_t)(32 * wq) << 16;
+    const bool committer = lane == 0 && warp < 4;
+    constexpr uint32_t id16 = tc::idesc_bf16_f32(128, 16), id32 = tc::idesc_bf16_f32(128, 32),
+                       id48 = tc::idesc_bf16_f32(128, 48);
+    // operand descriptors (built where they are issued, to keep registers free)
+    auto d_col = [&]() { return tc::sdesc(tc::smem_u32(tcs + TC_OFF_COL), TC_COL_CHUNK, 128); };
+    auto d_act1 = [&]() { return tc::sdesc(tc::smem_u32(act1), TC_ACT_CHUNK, 128); };
+    auto d_act2 = [&]() { return tc::sdesc(tc::smem_u32(act2), TC_ACT_CHUNK, 128); };
+    auto d_b1 = [&]() { return tc::sdesc(tc::smem_u32(tcs + TC_OFF_B1), 256, 128); };
+    auto d_b2 = [&]() { return tc::sdesc(tc::smem_u32(tcs + TC_OFF_B2), 48 * 16, 128); };
+    auto d_b3 = [&]() { return tc::sdesc(tc::smem_u32(tcs + TC_OFF_B3), 512, 128); };
     uint32_t phase = 0;
     bool ok = true;
     // thread v owns patch node v; the next patch's node index is loaded one patch ahead and
@@ -615,9 +646,11 @@ __global__ void __launch_bounds__(128, TC_CTAS_PER_SM) learned_correction_tc_ker
         gv_next = srow[v][blockIdx.x];
         val_next = load_val(gv_next);
     }
-    // the interior position of each of this thread's conv1 / conv2 rows
-    const int q0 = TC_Q0 + 32 * warp + lane, q1 = q0 + 128;
-    const bool in0 = tc_interior(q0), in1 = tc_interior(q1);
+    // this thread's rows: conv1 row q1 (tile grp), conv2 row r2 (tile grp, chunk c2 = 4 grp + wq)
+    const int q1 = TC_Q0 + 128 * grp + 32 * wq + lane;
+    const int c2 = 4 * grp + wq;
+    const int r2 = TC_R2 + 32 * c2 + lane;
+    const bool in_q1 = tc_interior(q1), in_r2 = tc_interior(r2);
     for (ptrdiff_t p = blockIdx.x; p < P && ok; p += gridDim.x) {
         // D^-1 r of this patch, normalised by the patch RMS
         const idx_t gv = gv_next;
@@ -630,14 +663,16 @@ __global__ void __launch_bounds__(128, TC_CTAS_PER_SM) learned_correction_tc_ker
         for (int o = 16; o > 0; o >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o);
         if (lane == 0) red[warp] = ss;
         __syncthreads();
-        float sc = sqrtf((red[0] + red[1] + red[2] + red[3]) / PV);
+        float sc = 0.f;
+#pragma unroll
+        for (int k = 0; k < 8; k++) sc += red[k];
+        sc = sqrtf(sc / PV);
         if (!(sc > 0.f)) sc = 1.f;
         if (v < PV) a0[pad_index(v)] = __float2bfloat16(val / sc);
         __syncthreads();
-        // conv1 im2col: col[i][k] = a0[TC_Q0 + i + off_delta(k)], k < 27
-#pragma unroll 1
-        for (int i = tid; i < 256; i += 128) {
-            const int q = TC_Q0 + i;
+        // conv1 im2col: col[i][k] = a0[TC_Q0 + i + off_delta(k)], k < 27 (row i = tid)
+        {
+            const int i = tid, q = TC_Q0 + i;
 #pragma unroll
             for (int c = 0; c < 4; c++) {
                 uint32_t w[4];
@@ -654,13 +689,13 @@ __global__ void __launch_bounds__(128, TC_CTAS_PER_SM) learned_correction_tc_ker
         }
         tc::fence_async_smem();
         tc_sync();
-        // conv1: warp h < 2 issues tile h (two K steps into cols 16h)
-        if (issuer) {
+        // conv1: warp h < 2 issues tile h (two K steps into cols 16 h)
+        if (committer) {
             if (warp < 2) {
 #pragma unroll
                 for (int st = 0; st < 2; st++)
-                    tc::mma_bf16(tmem + 16 * warp, d_col + (uint64_t)(2 * st * TC_COL_CHUNK / 16 + warp * 128),
-                                 d_b1 + (uint64_t)(32 * st), id16, st > 0);
+                    tc::mma_bf16(tmem + 16 * warp, d_col() + (uint64_t)(2 * st * TC_COL_CHUNK / 16 + warp * 128),
+                                 d_b1() + (uint64_t)(32 * st), id16, st > 0);
             }
             tc::commit(&mbar);
         }
@@ -670,28 +705,22 @@ __global__ void __launch_bounds__(128, TC_CTAS_PER_SM) learned_correction_tc_ker
         if (!ok) break;
         if (has_next) val_next = load_val(gv_next);
         {
-            float a[16], b[16];
-            tc::tmem_ld16(tmem + lane_base + 0, a);
-            tc::tmem_ld16(tmem + lane_base + 16, b);
-            if (in0) tc_store_row(act1, q0, a, true);
-            if (in1) tc_store_row(act1, q1, b, true);
+            float a[16];
+            tc::tmem_ld16(tmem + lane_base + 16 * grp, a);
+            if (in_q1) tc_store_row(act1, q1, a, true);
         }
         tc::fence_async_smem();
         tc_sync();
-        // conv2: warp w = 2 h + s issues tile h, taps [14 s, 14 s + 14) into cols 32 + 32 h + 16 s
-        if (issuer) {
-            const int h = warp >> 1, sh = warp & 1;
-            const uint32_t dcol = tmem + 32 + 32 * h + 16 * sh;
-            const uint64_t arow = d_act1 + (uint64_t)(TC_Q0 + 128 * h);
-            if (sh == 0) {
+        // conv2: warp h < 2 issues tile h: nine (dy, dz) MMAs of N = 48 into cols 32 + 48 h
+        if (committer) {
+            if (warp < 2) {
+                const uint64_t arow = d_act1() + (uint64_t)(TC_R2 + 128 * warp), b2 = d_b2();
 #pragma unroll
-                for (int t = 0; t < 14; t++)
-                    tc::mma_bf16(dcol, arow + (uint64_t)(int64_t)off_delta(t), d_b2 + (uint64_t)(32 * t), id16, t > 0);
-            } else {
-#pragma unroll
-                for (int t = 14; t < 27; t++)
-                    tc::mma_bf16(dcol, arow + (uint64_t)(int64_t)off_delta(t), d_b2 + (uint64_t)(32 * t), id16,
-                                 t > 14);
+                for (int g = 0; g < 9; g++) {
+                    const int shift = 7 * (g % 3 - 1) + 49 * (g / 3 - 1);
+                    tc::mma_bf16(tmem + 32 + 48 * warp, arow + (uint64_t)(int64_t)shift,
+                                 b2 + (uint64_t)(TC_B2_BLOCK / 16 * g), id48, g > 0);
+                }
             }
             tc::commit(&mbar);
         }
@@ -700,51 +729,64 @@ __global__ void __launch_bounds__(128, TC_CTAS_PER_SM) learned_correction_tc_ker
         tc::fence_after_sync();
         if (!ok) break;
         {
-            // act2 = ReLU(D2 halves summed); every one of its 384 rows is rewritten (the
-            // region is shared with the im2col buffer and the conv3 dump)
-            float a[16], b[16];
+            // out[r] = D[r - 1][dx = -1] + D[r][dx = 0] + D[r + 1][dx = +1] (16 channels)
+            const uint32_t dcol = tmem + lane_base + 32 + 48 * grp;
+            float acc[16], t[16];
+            tc::tmem_ld16(dcol + 0, t);  // dx = -1 slice of row r2: needed by row r2 + 1
+            if (lane == 31)
 #pragma unroll
-            for (int h = 0; h < 2; h++) {
-                tc::tmem_ld16(tmem + lane_base + 32 + 32 * h, a);
-                tc::tmem_ld16(tmem + lane_base + 48 + 32 * h, b);
+                for (int j = 0; j < 16; j++) xb[(c2 * 2 + 0) * 16 + j] = t[j];
 #pragma unroll
-                for (int j = 0; j < 16; j++) a[j] += b[j];
-                tc_store_row(act2, h ? q1 : q0, a, h ? in1 : in0);
+            for (int j = 0; j < 16; j++) {
+                const float u = __shfl_up_sync(0xffffffffu, t[j], 1);
+                acc[j] = lane == 0 ? 0.f : u;
             }
-            const int zrow = tid < TC_Q0 ? tid : TC_Q0 + 256 + (tid - TC_Q0);  // rows 0..56, 313..383
-            tc_store_row(act2, zrow, a, false);
+            tc::tmem_ld16(dcol + 32, t);  // dx = +1 slice of row r2: needed by row r2 - 1
+            if (lane == 0)
+#pragma unroll
+                for (int j = 0; j < 16; j++) xb[(c2 * 2 + 1) * 16 + j] = t[j];
+#pragma unroll
+            for (int j = 0; j < 16; j++) {
+                const float u = __shfl_down_sync(0xffffffffu, t[j], 1);
+                acc[j] += lane == 31 ? 0.f : u;
+            }
+            tc::tmem_ld16(dcol + 16, t);  // dx = 0 slice
+#pragma unroll
+            for (int j = 0; j < 16; j++) acc[j] += t[j];
+            __syncthreads();
+            if (lane == 0 && c2 > 0)
+#pragma unroll
+                for (int j = 0; j < 16; j++) acc[j] += xb[((c2 - 1) * 2 + 0) * 16 + j];
+            if (lane == 31 && c2 < 7)
+#pragma unroll
+                for (int j = 0; j < 16; j++) acc[j] += xb[((c2 + 1) * 2 + 1) * 16 + j];
+            // act2: every one of its 384 rows is rewritten (the region is shared with the
+            // im2col buffer and the conv3 dump): rows 56..311 here, the rest zeroed
+            tc_store_row(act2, r2, acc, in_r2);
+            if (tid < 128) tc_store_row(act2, tid < TC_R2 ? tid : TC_R2 + 256 + (tid - TC_R2), acc, false);
         }
         tc::fence_async_smem();
         tc_sync();
         // conv3: warp h < 3 issues tile h (rows 128 h ..), N = 32 taps, into cols 32 h
-        if (issuer) {
-            if (warp < 3) tc::mma_bf16(tmem + 32 * warp, d_act2 + (uint64_t)(128 * warp), d_b3, id32, 0);
+        if (committer) {
+            if (warp < 3) tc::mma_bf16(tmem + 32 * warp, d_act2() + (uint64_t)(128 * warp), d_b3(), id32, 0);
             tc::commit(&mbar);
         }
         ok = __syncthreads_and(tc::mbar_wait(&mbar, phase, TC_WAIT_POLLS));
         phase ^= 1;
         tc::fence_after_sync();
         if (!ok) break;
-        // dump D3[row][t] to dump[t][v] for the patch node v = row - off_delta(t)
+        // dump D3[row][t] to dump[t][v] for the patch node v = row - off_delta(t); warp
+        // group g takes the taps 16 g .. 16 g + 15
 #pragma unroll 1
         for (int h = 0; h < 3; h++) {
-            const int row = 128 * h + 32 * warp + lane;
-            const int rx = row % PP, ry = (row / PP) % PP, rz = row / (PP * PP);
-#pragma unroll
-            for (int part = 0; part < 2; part++) {
-                float a[16];
-                tc::tmem_ld16(tmem + lane_base + 32 * h + 16 * part, a);
-#pragma unroll
-                for (int j = 0; j < 16; j++) {
-                    const int t = 16 * part + j;
-                    if (t < 27) {
-                        // patch node (rx - dx - 1, ry - dy - 1, rz - dz - 1) when inside the patch
-                        const int x = rx - (t % 3 - 1) - 1, y = ry - ((t / 3) % 3 - 1) - 1, z = rz - (t / 9 - 1) - 1;
-                        if ((unsigned)x < PN && (unsigned)y < PN && (unsigned)z < PN && row < PPV)
-                            dump[t * PV + (z * PN + y) * PN + x] = a[j];
-                    }
-                }
-            }
+            const int row = 128 * h + 32 * wq + lane;
+            float a[16];
+            tc::tmem_ld16(tmem + lane_base + 32 * h + 16 * grp, a);
+            if (grp == 0)
+                tc_dump_taps<0>(dump, row, a);
+            else
+                tc_dump_taps<1>(dump, row, a);
         }
         tc_sync();
         if (v < PV) {
@@ -929,7 +971,7 @@ extern "C" int sfem_gb300_learned_correction(int real_type, ptrdiff_t P, idx_t *
                                      TC_SMEM);
                 tc_attr[0] = true;
             }
-            learned_correction_tc_kernel<float><<<grid, 128, TC_SMEM, s>>>(P, elements, (const float *)r,
+            learned_correction_tc_kernel<float><<<grid, TC_THREADS, TC_SMEM, s>>>(P, elements, (const float *)r,
                                                                            (const float *)inv_diag, ops, count,
                                                                            (float)omega, (float *)d);
         } else {
@@ -938,7 +980,7 @@ extern "C" int sfem_gb300_learned_correction(int real_type, ptrdiff_t P, idx_t *
                                      TC_SMEM);
                 tc_attr[1] = true;
             }
-            learned_correction_tc_kernel<double><<<grid, 128, TC_SMEM, s>>>(P, elements, (const double *)r,
+            learned_correction_tc_kernel<double><<<grid, TC_THREADS, TC_SMEM, s>>>(P, elements, (const double *)r,
                                                                             (const double *)inv_diag, ops, count,
                                                                             (float)omega, (double *)d);
         }
