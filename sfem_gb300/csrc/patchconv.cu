@@ -493,9 +493,8 @@ __global__ void __launch_bounds__(32 * LC_WARPS, 2) learned_correction_kernel(
 //                     start-address shift).  out[r] = sum_dx D[r + dx][dx] with warp
 //                     shuffles (rows r +- 1 are the neighbouring lanes; the rows at warp
 //                     boundaries go through shared memory).
-//   conv3 (16 -> 1):  taps as GEMM columns: D3[r][t] = sum_ci act2[r][ci] W3[ci][t]
-//                     for all rows r < 384 (3 tiles, N = 32), then out[q] =
-//                     sum_t D3[q + off_delta(t)][t] through shared memory.
+//   conv3 (16 -> 1):  the same grouping with N = 16 (columns dx + 1 = 0, 1, 2 used):
+//                     out[r] = D3[r - 1][0] + D3[r][1] + D3[r + 1][2].
 // Activations are [channel chunk][padded position][8 BF16] rows of 16 bytes (7^3
 // padded grid, zero halo); rows that are halo positions are computed and discarded.
 constexpr int TC_Q0 = PP * PP + PP + 1;  // 57: padded index of patch node 0
@@ -506,23 +505,25 @@ constexpr int TC_COL_CHUNK = 256 * 16;
 constexpr int TC_B1_BYTES = 2 * 2 * 16 * 16;  // [kstep][chunk][n 16][8] BF16
 constexpr int TC_B2_BLOCK = 2 * 48 * 16;      // one (dy, dz): [chunk][n = (dx, co) 48][8]
 constexpr int TC_B2_BYTES = 9 * TC_B2_BLOCK;
-constexpr int TC_B3_BYTES = 2 * 32 * 16;  // [chunk][n = tap 32][8]
+constexpr int TC_B3_BLOCK = 2 * 16 * 16;       // one (dy, dz): [chunk][n = dx + 1 (3 of 16)][8]
+constexpr int TC_B3_BYTES = 9 * TC_B3_BLOCK;
 constexpr int TC_OPERAND_BYTES = TC_B1_BYTES + TC_B2_BYTES + TC_B3_BYTES;
 constexpr int TC_OFF_B1 = 0, TC_OFF_B2 = TC_B1_BYTES, TC_OFF_B3 = TC_B1_BYTES + TC_B2_BYTES;
 constexpr int TC_OFF_ACT1 = TC_OPERAND_BYTES;
-constexpr int TC_OFF_COL = TC_OFF_ACT1 + 2 * TC_ACT_CHUNK;  // im2col, then act2, then the conv3 dump
+constexpr int TC_OFF_COL = TC_OFF_ACT1 + 2 * TC_ACT_CHUNK;  // im2col, then act2
 constexpr int TC_OFF_A0 = TC_OFF_COL + 4 * TC_COL_CHUNK;
-constexpr int TC_OFF_XB = TC_OFF_A0 + TC_ROWS * 2;  // conv2 rows at warp boundaries: [chunk 8][2][16] float
-constexpr int TC_OFF_RED = TC_OFF_XB + 8 * 2 * 16 * 4;
+constexpr int TC_OFF_XB = TC_OFF_A0 + TC_ROWS * 2;  // rows at warp boundaries: [chunk 8][2][16] float
+constexpr int TC_OFF_OUT = TC_OFF_XB + 8 * 2 * 16 * 4;  // network output per patch node
+constexpr int TC_OFF_RED = TC_OFF_OUT + 128 * 4;
 constexpr int TC_SMEM = TC_OFF_RED + 8 * 4;
 constexpr int TC_THREADS = 256;
 constexpr int TC_CTAS_PER_SM = 4;
-constexpr uint32_t TC_TMEM_COLS = 128;  // D1 cols 0..31, D2 32..127, then D3 0..95
+constexpr uint32_t TC_TMEM_COLS = 128;  // D1 cols 0..31, D2 32..127, then D3 0..31
 constexpr int TC_WAIT_POLLS = 1 << 20;
 static_assert((TC_SMEM + 1024 + 1024) * TC_CTAS_PER_SM <= 228 * 1024, "shared memory of the resident CTAs");
 static_assert(TC_TMEM_COLS * TC_CTAS_PER_SM <= 512, "tensor memory of the resident CTAs");
 static_assert(TC_R2 + 255 + 7 + 49 < TC_ROWS && TC_Q0 + 255 + TC_Q0 < TC_ROWS, "shifted rows stay in the buffers");
-static_assert(2 * TC_ACT_CHUNK <= 4 * TC_COL_CHUNK && 27 * PV * 4 <= 4 * TC_COL_CHUNK, "aliases of the col region");
+static_assert(2 * TC_ACT_CHUNK <= 4 * TC_COL_CHUNK, "act2 aliases the im2col region");
 
 __device__ int g_lc_status;  // nonzero: a tensor-core wait gave up (kernel returned early)
 
@@ -542,10 +543,11 @@ __global__ void learned_tc_operands_kernel(const __nv_bfloat16 *__restrict__ W1,
             const int dxi = n / 16, co = n % 16, dyi = g % 3, dzi = g / 3;
             const int t = dzi * 9 + dyi * 3 + dxi;
             out[i] = W2[(co * KMAX_C + 8 * c + e) * 27 + t];
-        } else {  // conv3: n = tap, k = ci
+        } else {  // conv3 (dy, dz) block g: n = dx + 1 (n < 3), k = ci
             const int j = i - n1 - n2;
-            const int e = j % 8, t = (j / 8) % 32, c = j / 256;
-            out[i] = t < 27 ? W3[(8 * c + e) * 27 + t] : zero;
+            const int e = j % 8, n = (j / 8) % 16, c = (j / 128) % 2, g = j / 256;
+            const int t = (g / 3) * 9 + (g % 3) * 3 + n;
+            out[i] = n < 3 ? W3[(8 * c + e) * 27 + t] : zero;
         }
     }
 }
@@ -569,24 +571,6 @@ __device__ __forceinline__ void tc_store_row(unsigned char *act, int q, const fl
     }
 }
 
-// dump[t][v] = D3[row][t] for the taps t = 16 G + j of this thread's row, v = the patch
-// node at row - off_delta(t) when that is inside the patch
-template <int G>
-__device__ __forceinline__ void tc_dump_taps(float *dump, int row, const float (&a)[16]) {
-    const int rx = row % PP - 1, ry = (row / PP) % PP - 1, rz = row / (PP * PP) - 1;
-    const int vbase = (rz * PN + ry) * PN + rx;
-#pragma unroll
-    for (int j = 0; j < 16; j++) {
-        constexpr int kLimit = 27 - 16 * G;
-        if (j < kLimit) {
-            const int t = 16 * G + j;
-            const int dx = t % 3 - 1, dy = (t / 3) % 3 - 1, dz = t / 9 - 1;
-            if ((unsigned)(rx - dx) < PN && (unsigned)(ry - dy) < PN && (unsigned)(rz - dz) < PN && row < PPV)
-                dump[t * PV + vbase - (dz * PN + dy) * PN - dx] = a[j];
-        }
-    }
-}
-
 __device__ __forceinline__ void tc_sync() {
     tc::fence_before_sync();
     __syncthreads();
@@ -607,7 +591,7 @@ __global__ void __launch_bounds__(TC_THREADS, TC_CTAS_PER_SM) learned_correction
     __nv_bfloat16 *a0 = reinterpret_cast<__nv_bfloat16 *>(tcs + TC_OFF_A0);
     float *red = reinterpret_cast<float *>(tcs + TC_OFF_RED);
     float *xb = reinterpret_cast<float *>(tcs + TC_OFF_XB);
-    float *dump = reinterpret_cast<float *>(tcs + TC_OFF_COL);  // [tap][patch node]
+    float *outp = reinterpret_cast<float *>(tcs + TC_OFF_OUT);
     unsigned char *act1 = tcs + TC_OFF_ACT1, *act2 = tcs + TC_OFF_COL;
     // operands in; activation / im2col / input buffers zeroed (halo rows of act1 and a0 stay zero)
     for (int i = tid; i < TC_OPERAND_BYTES / 16; i += TC_THREADS) reinterpret_cast<uint4 *>(tcs)[i] = operands[i];
@@ -621,17 +605,25 @@ __global__ void __launch_bounds__(TC_THREADS, TC_CTAS_PER_SM) learned_correction
     const uint32_t tmem = tmem_holder;
     const uint32_t lane_base = (uint32_t)(32 * wq) << 16;
     const bool committer = lane == 0 && warp < 4;
-    constexpr uint32_t id16 = tc::idesc_bf16_f32(128, 16), id32 = tc::idesc_bf16_f32(128, 32),
-                       id48 = tc::idesc_bf16_f32(128, 48);
+    constexpr uint32_t id16 = tc::idesc_bf16_f32(128, 16), id48 = tc::idesc_bf16_f32(128, 48);
     // operand descriptors (built where they are issued, to keep registers free)
     auto d_col = [&]() { return tc::sdesc(tc::smem_u32(tcs + TC_OFF_COL), TC_COL_CHUNK, 128); };
     auto d_act1 = [&]() { return tc::sdesc(tc::smem_u32(act1), TC_ACT_CHUNK, 128); };
     auto d_act2 = [&]() { return tc::sdesc(tc::smem_u32(act2), TC_ACT_CHUNK, 128); };
     auto d_b1 = [&]() { return tc::sdesc(tc::smem_u32(tcs + TC_OFF_B1), 256, 128); };
     auto d_b2 = [&]() { return tc::sdesc(tc::smem_u32(tcs + TC_OFF_B2), 48 * 16, 128); };
-    auto d_b3 = [&]() { return tc::sdesc(tc::smem_u32(tcs + TC_OFF_B3), 512, 128); };
+    auto d_b3 = [&]() { return tc::sdesc(tc::smem_u32(tcs + TC_OFF_B3), 256, 128); };
     uint32_t phase = 0;
     bool ok = true;
+    // one thread polls the mbarrier; the others wait at the CTA barrier (no issue slots)
+    auto wait_mma = [&]() {
+        bool w = true;
+        if (warp == 0) w = tc::mbar_wait(&mbar, phase, TC_WAIT_POLLS);
+        const bool all = __syncthreads_and(w);
+        phase ^= 1;
+        tc::fence_after_sync();
+        return all;
+    };
     // thread v owns patch node v; the next patch's node index is loaded one patch ahead and
     // its residual value after the current patch's first tensor-core wait
     const int v = tid;
@@ -699,9 +691,7 @@ __global__ void __launch_bounds__(TC_THREADS, TC_CTAS_PER_SM) learned_correction
             }
             tc::commit(&mbar);
         }
-        ok = __syncthreads_and(tc::mbar_wait(&mbar, phase, TC_WAIT_POLLS));
-        phase ^= 1;
-        tc::fence_after_sync();
+        ok = wait_mma();
         if (!ok) break;
         if (has_next) val_next = load_val(gv_next);
         {
@@ -724,9 +714,7 @@ __global__ void __launch_bounds__(TC_THREADS, TC_CTAS_PER_SM) learned_correction
             }
             tc::commit(&mbar);
         }
-        ok = __syncthreads_and(tc::mbar_wait(&mbar, phase, TC_WAIT_POLLS));
-        phase ^= 1;
-        tc::fence_after_sync();
+        ok = wait_mma();
         if (!ok) break;
         {
             // out[r] = D[r - 1][dx = -1] + D[r][dx = 0] + D[r + 1][dx = +1] (16 channels)
@@ -767,35 +755,40 @@ __global__ void __launch_bounds__(TC_THREADS, TC_CTAS_PER_SM) learned_correction
         }
         tc::fence_async_smem();
         tc_sync();
-        // conv3: warp h < 3 issues tile h (rows 128 h ..), N = 32 taps, into cols 32 h
+        // conv3: warp h < 2 issues tile h: nine (dy, dz) MMAs of N = 16 into cols 16 h
         if (committer) {
-            if (warp < 3) tc::mma_bf16(tmem + 32 * warp, d_act2() + (uint64_t)(128 * warp), d_b3(), id32, 0);
+            if (warp < 2) {
+                const uint64_t arow = d_act2() + (uint64_t)(TC_R2 + 128 * warp), b3 = d_b3();
+#pragma unroll
+                for (int g = 0; g < 9; g++) {
+                    const int shift = 7 * (g % 3 - 1) + 49 * (g / 3 - 1);
+                    tc::mma_bf16(tmem + 16 * warp, arow + (uint64_t)(int64_t)shift,
+                                 b3 + (uint64_t)(TC_B3_BLOCK / 16 * g), id16, g > 0);
+                }
+            }
             tc::commit(&mbar);
         }
-        ok = __syncthreads_and(tc::mbar_wait(&mbar, phase, TC_WAIT_POLLS));
-        phase ^= 1;
-        tc::fence_after_sync();
+        ok = wait_mma();
         if (!ok) break;
-        // dump D3[row][t] to dump[t][v] for the patch node v = row - off_delta(t); warp
-        // group g takes the taps 16 g .. 16 g + 15
-#pragma unroll 1
-        for (int h = 0; h < 3; h++) {
-            const int row = 128 * h + 32 * wq + lane;
-            float a[16];
-            tc::tmem_ld16(tmem + lane_base + 32 * h + 16 * grp, a);
-            if (grp == 0)
-                tc_dump_taps<0>(dump, row, a);
-            else
-                tc_dump_taps<1>(dump, row, a);
+        {
+            // out[r] = D3[r - 1][0] + D3[r][1] + D3[r + 1][2]
+            float a[4];
+            tc::tmem_ld4(tmem + lane_base + 16 * grp, a);
+            if (lane == 31) xb[(c2 * 2 + 0) * 16] = a[0];
+            if (lane == 0) xb[(c2 * 2 + 1) * 16] = a[2];
+            const float um = __shfl_up_sync(0xffffffffu, a[0], 1), up = __shfl_down_sync(0xffffffffu, a[2], 1);
+            float o = a[1] + (lane == 0 ? 0.f : um) + (lane == 31 ? 0.f : up);
+            __syncthreads();
+            if (lane == 0 && c2 > 0) o += xb[((c2 - 1) * 2 + 0) * 16];
+            if (lane == 31 && c2 < 7) o += xb[((c2 + 1) * 2 + 1) * 16];
+            if (in_r2) {
+                const int x = r2 % PP - 1, y = (r2 / PP) % PP - 1, z = r2 / (PP * PP) - 1;
+                outp[(z * PN + y) * PN + x] = __bfloat162float(__float2bfloat16(o));  // rounded like the layer kernels
+            }
         }
         tc_sync();
-        if (v < PV) {
-            float o = 0.f;
-#pragma unroll
-            for (int t = 0; t < 27; t++) o += dump[t * PV + v];
-            o = __bfloat162float(__float2bfloat16(o));  // rounded like the stored activations of the layer kernels
-            atomicAdd(&d[gv], (T)omega * (T)(sc * o) / (T)count[gv]);
-        }
+        if (v < PV) atomicAdd(&d[gv], (T)omega * (T)(sc * outp[v]) / (T)count[gv]);
+        __syncthreads();  // outp and xb are rewritten by the next patch
     }
     if (!ok) {
         if (tid == 0) atomicExch(&g_lc_status, 1);
