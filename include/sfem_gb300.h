@@ -100,6 +100,13 @@ int sfem_gb300_linear_elasticity_apply(int element_type, ptrdiff_t nelements, sf
                                        double mu, double lambda, int real_type, const void *u, void *out,
                                        void *stream);
 
+/* FP32 sshex8 kernel choice (no reference counterpart): -1 default, 0 the SIMT warp
+ * kernel, 1 the tcgen05 kernel (L = 4: element-matrix contraction on the tensor cores in
+ * 3xTF32, FP32-level accuracy; the default at L = 4).  sfem_gb300_elasticity_status
+ * returns (and clears) 1 if a tcgen05 kernel gave up waiting for its MMAs, else 0. */
+int sfem_gb300_set_elasticity_kernel(int variant);
+int sfem_gb300_elasticity_status(void);
+
 /* The reference's exact sshex8 entry point (operators/sshex8/cuda/cu_sshex8_linear_elasticity.cu:1730-1748);
  * only the interleaved layout (u_stride = out_stride = 3, uy = ux + 1, uz = ux + 2) is accepted. */
 int cu_affine_sshex8_linear_elasticity_apply(int level, ptrdiff_t nelements, sfem_gb300_idx_t **elements,

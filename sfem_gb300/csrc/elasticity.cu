@@ -11,9 +11,11 @@
 // integrals of d_p phi_a d_q phi_b on the unit cube.
 #include <cuda_bf16.h>
 
+#include <algorithm>
 #include <cstdlib>
 
 #include "common.cuh"
+#include "tcgen05.cuh"
 
 namespace sfem_gb300 {
 
@@ -496,6 +498,212 @@ static int elasticity_apply_tc(int element_type, ptrdiff_t nelements, idx_t **el
     return check_launch("sfem_gb300_linear_elasticity_apply(SSHEX8, tensor cores)");
 }
 
+// ---------------------------------------------------------------------------- tcgen05, 3xTF32
+// FP32 sshex8 apply at L = 4 with the element-matrix contraction on the 5th-generation
+// tensor cores.  A CTA of four warps takes macro elements in pairs (e0, e1): one M = 128
+// tile holds the 64 micro elements of each (rows 0..63: e0, 64..127: e1) by their 24
+// dofs, A[m][(j, b)] = u_j(corner b of micro element m); B_e = K_e (24 x 24, N padded
+// to 32, K-major); D_e = A K_e^T in tensor memory (the rows of e are kept).  Operands
+// are split into TF32 hi = tf32(x) and lo = x - hi and multiplied as hi.hi + hi.lo +
+// lo.hi (kind::tf32, K = 8 per MMA, FP32 accumulate): 18 MMAs per pair, FP32-level
+// accuracy (the dropped lo.lo term is ~2^-22 relative).  Epilogue: warp w reads TMEM
+// lanes 32w.. (w < 2: e0, else e1), adds the 24 values of each micro element into the
+// element's node accumulator in shared memory, then the nodes are scattered like the
+// SIMT kernel (plain read-modify-write on interior nodes, atomics on the surface).
+constexpr int ETC_L = 4, ETC_N1 = ETC_L + 1, ETC_NXE = ETC_N1 * ETC_N1 * ETC_N1;  // 125 nodes
+constexpr int ETC_A_CHUNK = 128 * 16;   // [chunk of 4 dofs][row 128][16 B]
+constexpr int ETC_A_BYTES = 6 * ETC_A_CHUNK;
+constexpr int ETC_B_CHUNK = 32 * 16;    // [chunk][n 32][16 B]
+constexpr int ETC_B_BYTES = 6 * ETC_B_CHUNK;  // one element
+constexpr int ETC_OFF_AHI = 0, ETC_OFF_ALO = ETC_A_BYTES;
+constexpr int ETC_OFF_BHI = 2 * ETC_A_BYTES, ETC_OFF_BLO = ETC_OFF_BHI + 2 * ETC_B_BYTES;
+constexpr int ETC_OFF_I = ETC_OFF_BLO + 2 * ETC_B_BYTES;   // 576 floats
+constexpr int ETC_OFF_W = ETC_OFF_I + 576 * 4;             // [2][81] floats (+ pad)
+constexpr int ETC_OFF_X = ETC_OFF_W + 2 * 84 * 4;          // [2][3][125] floats
+constexpr int ETC_OFF_Y = ETC_OFF_X + 2 * 3 * ETC_NXE * 4;  // [2][3][125] floats
+constexpr int ETC_SMEM = ETC_OFF_Y + 2 * 3 * ETC_NXE * 4;
+constexpr int ETC_CTAS_PER_SM = 4;
+constexpr uint32_t ETC_TMEM_COLS = 64;  // D_e at cols 32 e
+constexpr int ETC_WAIT_POLLS = 1 << 20;
+static_assert((ETC_SMEM + 2048) * ETC_CTAS_PER_SM <= 228 * 1024, "shared memory of the resident CTAs");
+__device__ int g_etc_status;  // nonzero: a tensor-core wait gave up
+
+__global__ void __launch_bounds__(128, ETC_CTAS_PER_SM) elasticity_apply_tf32x3_kernel(
+        ptrdiff_t nelements, const idx_t *const *elements, ptrdiff_t stride, const float *adjugate,
+        const float *determinant, float mu, float lambda, const float *__restrict__ x, float *__restrict__ y) {
+    extern __shared__ __align__(16) unsigned char es[];
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t tmem_holder;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int e_loc = tid >> 6, u = tid & 63;  // element of the pair this thread serves in phases 1-2, 5
+    float *Is = reinterpret_cast<float *>(es + ETC_OFF_I);
+    float *W = reinterpret_cast<float *>(es + ETC_OFF_W) + 84 * e_loc;
+    float *xs = reinterpret_cast<float *>(es + ETC_OFF_X);
+    float *ys = reinterpret_cast<float *>(es + ETC_OFF_Y);
+    for (int i = tid; i < ETC_OFF_I / 16; i += 128) reinterpret_cast<uint4 *>(es)[i] = make_uint4(0, 0, 0, 0);
+    for (int k = tid; k < 576; k += 128) Is[k] = (float)(&kGrad.I[0][0][0][0])[k];
+    for (int i = tid; i < 2 * 3 * ETC_NXE; i += 128) ys[i] = 0.f;
+    if (warp == 0) tc::tmem_alloc(&tmem_holder, ETC_TMEM_COLS);
+    if (tid == 0) tc::mbar_init(&mbar, 1);
+    tc::fence_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = tmem_holder;
+    uint32_t phase = 0;
+    bool ok = true;
+    // micro element of this thread's A row (row tid: element tid / 64, micro element tid % 64)
+    const int mx = u % ETC_L, my = (u / ETC_L) % ETC_L, mz = u / (ETC_L * ETC_L);
+    for (ptrdiff_t pr = blockIdx.x; 2 * pr < nelements && ok; pr += gridDim.x) {
+        const ptrdiff_t e = 2 * pr + e_loc;
+        const bool valid = e < nelements;
+        const bool pair = 2 * pr + 1 < nelements;
+        // 1. sub-adjugate, W, gather of the element's 125 x 3 values
+        float adj[9], AA[9], inv_det = 0.f;
+        if (valid) {
+            load_sub_adjugate<float>(adjugate, determinant, stride, e, ETC_L, adj, AA, inv_det);
+            for (int k = u; k < 81; k += 64) {
+                const int i = k / 27, j = (k / 9) % 3, p = (k / 3) % 3, q = k % 3;
+                float w = mu * adj[3 * p + j] * adj[3 * q + i] + lambda * adj[3 * p + i] * adj[3 * q + j];
+                if (i == j) w += mu * AA[3 * p + q];
+                W[k] = w;
+            }
+            for (int v = u; v < ETC_NXE; v += 64) {
+                const idx_t g = elements[v][e];
+#pragma unroll
+                for (int d = 0; d < 3; d++) xs[(e_loc * 3 + d) * ETC_NXE + v] = x[3 * (ptrdiff_t)g + d];
+            }
+        }
+        __syncthreads();
+        // 2. B_e = K_e (hi / lo) and this thread's A row
+        if (valid) {
+            for (int k = u; k < 576; k += 64) {
+                const int row = k / 24, col = k % 24;
+                const int i = row >> 3, a = row & 7, j = col >> 3, b = col & 7;
+                const float *Iab = &Is[(a * 8 + b) * 9];
+                const float *Wij = &W[(i * 3 + j) * 9];
+                float acc = 0.f;
+#pragma unroll
+                for (int pq = 0; pq < 9; pq++) acc += Iab[pq] * Wij[pq];
+                acc *= inv_det;
+                const float hi = tc::tf32_round(acc);
+                const int off = e_loc * ETC_B_BYTES + (col >> 2) * ETC_B_CHUNK + row * 16 + (col & 3) * 4;
+                *reinterpret_cast<float *>(es + ETC_OFF_BHI + off) = hi;
+                *reinterpret_cast<float *>(es + ETC_OFF_BLO + off) = acc - hi;
+            }
+            const float *xe = xs + e_loc * 3 * ETC_NXE;
+#pragma unroll
+            for (int c4 = 0; c4 < 6; c4++) {
+                float h[4], l[4];
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    const int col = 4 * c4 + k, j = col >> 3, b = col & 7;
+                    const float val =
+                            xe[j * ETC_NXE + lidx(ETC_L, mx + c8x(b), my + c8y(b), mz + c8z(b))];
+                    h[k] = tc::tf32_round(val);
+                    l[k] = val - h[k];
+                }
+                *reinterpret_cast<float4 *>(es + ETC_OFF_AHI + c4 * ETC_A_CHUNK + tid * 16) = make_float4(h[0], h[1], h[2], h[3]);
+                *reinterpret_cast<float4 *>(es + ETC_OFF_ALO + c4 * ETC_A_CHUNK + tid * 16) = make_float4(l[0], l[1], l[2], l[3]);
+            }
+        }
+        tc::fence_async_smem();
+        tc::fence_before_sync();
+        __syncthreads();
+        tc::fence_after_sync();
+        // 3. MMAs: D_e (+)= A_hi B_hi + A_hi B_lo + A_lo B_hi over 3 K steps
+        if (tid == 0) {
+            constexpr uint32_t id = tc::idesc_tf32_f32(128, 32);
+            const uint64_t ahi = tc::sdesc(tc::smem_u32(es + ETC_OFF_AHI), ETC_A_CHUNK, 128);
+            const uint64_t alo = tc::sdesc(tc::smem_u32(es + ETC_OFF_ALO), ETC_A_CHUNK, 128);
+            const uint64_t bhi = tc::sdesc(tc::smem_u32(es + ETC_OFF_BHI), ETC_B_CHUNK, 128);
+            const uint64_t blo = tc::sdesc(tc::smem_u32(es + ETC_OFF_BLO), ETC_B_CHUNK, 128);
+            for (int el = 0; el < (pair ? 2 : 1); el++) {
+#pragma unroll
+                for (int st = 0; st < 3; st++) {
+                    const uint64_t ao = (uint64_t)(2 * st * ETC_A_CHUNK / 16);
+                    const uint64_t bo = (uint64_t)((el * ETC_B_BYTES + 2 * st * ETC_B_CHUNK) / 16);
+                    tc::mma_tf32(tmem + 32 * el, ahi + ao, bhi + bo, id, st > 0);
+                    tc::mma_tf32(tmem + 32 * el, ahi + ao, blo + bo, id, 1);
+                    tc::mma_tf32(tmem + 32 * el, alo + ao, bhi + bo, id, 1);
+                }
+            }
+            tc::commit(&mbar);
+        }
+        {
+            bool w = true;
+            if (warp == 0) w = tc::mbar_wait(&mbar, phase, ETC_WAIT_POLLS);
+            ok = __syncthreads_and(w);
+            phase ^= 1;
+            tc::fence_after_sync();
+        }
+        if (!ok) break;
+        // 4. epilogue: row m of warp w's lanes -> the element's node accumulator
+        {
+            const int el = warp >> 1;
+            float a[16], b[16];
+            tc::tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + 32 * el, a);
+            tc::tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + 32 * el + 16, b);
+            if (2 * pr + el < nelements) {
+                const int m = (32 * warp + lane) & 63;
+                const int px = m % ETC_L, py = (m / ETC_L) % ETC_L, pz = m / (ETC_L * ETC_L);
+                float *ye = ys + el * 3 * ETC_NXE;
+#pragma unroll
+                for (int r = 0; r < 24; r++) {
+                    const int i = r >> 3, c = r & 7;
+                    atomicAdd(&ye[i * ETC_NXE + lidx(ETC_L, px + c8x(c), py + c8y(c), pz + c8z(c))],
+                              r < 16 ? a[r] : b[r - 16]);
+                }
+            }
+        }
+        tc::fence_before_sync();
+        __syncthreads();
+        tc::fence_after_sync();
+        // 5. scatter and reset the accumulator
+        if (valid) {
+            for (int v = u; v < ETC_NXE; v += 64) {
+                const idx_t g = elements[v][e];
+                const int vx = v % ETC_N1, vy = (v / ETC_N1) % ETC_N1, vz = v / (ETC_N1 * ETC_N1);
+                const bool interior = vx > 0 && vx < ETC_L && vy > 0 && vy < ETC_L && vz > 0 && vz < ETC_L;
+#pragma unroll
+                for (int d = 0; d < 3; d++) {
+                    float *yv = &ys[(e_loc * 3 + d) * ETC_NXE + v];
+                    float *dst = &y[3 * (ptrdiff_t)g + d];
+                    if (interior)
+                        *dst += *yv;
+                    else
+                        atomicAdd(dst, *yv);
+                    *yv = 0.f;
+                }
+            }
+        }
+        __syncthreads();
+    }
+    if (!ok) {
+        if (tid == 0) atomicExch(&g_etc_status, 1);
+        tc::mbar_wait(&mbar, phase ^ 1, ETC_WAIT_POLLS);
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    if (warp == 0) tc::tmem_dealloc(tmem, ETC_TMEM_COLS);
+}
+
+static int g_elasticity_kernel = -1;  // -1 default, 0 SIMT warp kernel, 1 tcgen05 3xTF32 (FP32, L = 4)
+
+static int elasticity_apply_tf32x3(ptrdiff_t nelements, idx_t **elements, ptrdiff_t stride, const float *adj,
+                                   const float *det, float mu, float lambda, const float *x, float *y, cudaStream_t s) {
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(elasticity_apply_tf32x3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, ETC_SMEM);
+        attr = true;
+    }
+    const ptrdiff_t pairs = (nelements + 1) / 2;
+    const int grid = (int)std::min<ptrdiff_t>(pairs, (ptrdiff_t)kNumSMs * ETC_CTAS_PER_SM);
+    elasticity_apply_tf32x3_kernel<<<grid, 128, ETC_SMEM, s>>>(nelements, elements, stride, adj, det, mu, lambda, x, y);
+    return check_launch("sfem_gb300_linear_elasticity_apply(SSHEX8 L=4, tcgen05 3xTF32)");
+}
+
 template <typename T>
 static int elasticity_apply_tpl(int element_type, ptrdiff_t nelements, idx_t **elements, ptrdiff_t stride,
                                 const float *adj, const float *det, T mu, T lambda, const T *x, T *y, cudaStream_t s) {
@@ -507,6 +715,10 @@ static int elasticity_apply_tpl(int element_type, ptrdiff_t nelements, idx_t **e
         return check_launch("sfem_gb300_linear_elasticity_apply(HEX8)");
     }
     const int L = element_type - SFEM_GB300_SSHEX8_BASE;
+    if constexpr (sizeof(T) == 4) {
+        if (L == 4 && g_elasticity_kernel != 0)
+            return elasticity_apply_tf32x3(nelements, elements, stride, adj, det, mu, lambda, x, y, s);
+    }
 #define SFEM_EL_CASE(LL)                                                                                             \
     case LL:                                                                                                         \
         elasticity_apply_warp_kernel<T, LL, false><<<blocks, 64, 0, s>>>(nelements, elements, stride, adj, det, mu, \
@@ -571,6 +783,22 @@ extern "C" int sfem_gb300_linear_elasticity_apply(int element_type, ptrdiff_t ne
         return elasticity_apply_tpl<double>(element_type, nelements, elements, jacobian_stride, adjugate, determinant,
                                             mu, lambda, (const double *)u, (double *)out, s);
     return set_error("sfem_gb300_linear_elasticity_apply: unsupported real type %d", real_type);
+}
+
+extern "C" int sfem_gb300_set_elasticity_kernel(int variant) {
+    if (variant < -1 || variant > 1) return set_error("sfem_gb300_set_elasticity_kernel: variant %d (-1, 0 or 1)", variant);
+    g_elasticity_kernel = variant;
+    return SFEM_GB300_SUCCESS;
+}
+
+extern "C" int sfem_gb300_elasticity_status(void) {
+    int st = 0;
+    if (cudaMemcpyFromSymbol(&st, g_etc_status, sizeof(int)) != cudaSuccess) return -1;
+    if (st) {
+        const int zero = 0;
+        cudaMemcpyToSymbol(g_etc_status, &zero, sizeof(int));
+    }
+    return st;
 }
 
 extern "C" int cu_affine_sshex8_linear_elasticity_apply(int level, ptrdiff_t nelements, idx_t **elements,

@@ -60,15 +60,20 @@ def ctypes_d(v):
     return ctypes.c_double(v)
 
 
-def test_elasticity_reference_signature_and_fp32(cuda):
+@pytest.mark.parametrize("shape", [(3, 2, 2), (3, 3, 1)], ids=["12elements", "9elements"])
+@pytest.mark.parametrize("fp32_kernel", [0, 1], ids=["simt", "tcgen05_3xtf32"])
+def test_elasticity_reference_signature_and_fp32(cuda, fp32_kernel, shape):
+    """FP64 = oracle to 1e-13; FP32 through the SIMT kernel or the tcgen05 3xTF32
+    contraction (K and u split into TF32 hi + lo, hi.hi + hi.lo + lo.hi: FP32-level error)."""
     import torch
 
     L = 4
-    m, sp, el, adj, det, adj_d, det_d = _setup(cuda, L, seed=3)
+    m, sp, el, adj, det, adj_d, det_d = _setup(cuda, L, n=shape, seed=3)
     n = m.n_nodes(L)
     u = np.random.default_rng(5).standard_normal(3 * n)
     ref = O.linear_elasticity_apply(L, el, adj, det, MU, LAM, u)
     lib = capi.load()
+    capi.check(lib.sfem_gb300_set_elasticity_kernel(fp32_kernel), "variant")
     # FLOAT32: FP32 SIMT contraction.  FLOAT32_BF16TC: tensor-core BF16 contraction with FP32
     # accumulate; K and u rounded to 8-bit mantissas (2^-8 per product) against a row scale that
     # underestimates sum |K_ij||u_j| several-fold: 2.8e-2 observed, bounded here by 6e-2.
@@ -84,6 +89,8 @@ def test_elasticity_reference_signature_and_fp32(cuda):
             capi.c_void(yd.data_ptr() + 2 * es), None), "cu_affine_sshex8_linear_elasticity_apply")
         err = np.abs(yd.double().cpu().numpy() - ref) / _scale(L, el, adj, det, u)
         assert err.max() < tol, (dt, rt, err.max())
+    capi.check(lib.sfem_gb300_set_elasticity_kernel(-1), "variant")
+    assert lib.sfem_gb300_elasticity_status() == 0
     # non-interleaved layouts are rejected with a message
     assert lib.cu_affine_sshex8_linear_elasticity_apply(
         L, capi.i64(m.n_elements), sp.elements_ptrs.ptr, capi.i64(m.n_elements), capi.vp(adj_d), capi.vp(det_d),
