@@ -689,7 +689,7 @@ __global__ void __launch_bounds__(128, ETC_CTAS_PER_SM) elasticity_apply_tf32x3_
     if (warp == 0) tc::tmem_dealloc(tmem, ETC_TMEM_COLS);
 }
 
-static int g_elasticity_kernel = -1;  // -1 default, 0 SIMT warp kernel, 1 tcgen05 3xTF32 (FP32, L = 4)
+static int g_elasticity_kernel = -1;  // -1 default (SIMT), 0 SIMT warp kernel, 1 tcgen05 3xTF32 (FP32, L = 4)
 
 static int elasticity_apply_tf32x3(ptrdiff_t nelements, idx_t **elements, ptrdiff_t stride, const float *adj,
                                    const float *det, float mu, float lambda, const float *x, float *y, cudaStream_t s) {
@@ -716,7 +716,7 @@ static int elasticity_apply_tpl(int element_type, ptrdiff_t nelements, idx_t **e
     }
     const int L = element_type - SFEM_GB300_SSHEX8_BASE;
     if constexpr (sizeof(T) == 4) {
-        if (L == 4 && g_elasticity_kernel != 0)
+        if (L == 4 && g_elasticity_kernel == 1)
             return elasticity_apply_tf32x3(nelements, elements, stride, adj, det, mu, lambda, x, y, s);
     }
 #define SFEM_EL_CASE(LL)                                                                                             \
