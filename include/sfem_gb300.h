@@ -102,7 +102,7 @@ int sfem_gb300_linear_elasticity_apply(int element_type, ptrdiff_t nelements, sf
 
 /* FP32 sshex8 kernel choice (no reference counterpart): -1 default, 0 the SIMT warp
  * kernel, 1 the tcgen05 kernel (L = 4: element-matrix contraction on the tensor cores in
- * 3xTF32, FP32-level accuracy).  sfem_gb300_elasticity_status
+ * 3xTF32, FP32-level accuracy; the default at L = 4).  sfem_gb300_elasticity_status
  * returns (and clears) 1 if a tcgen05 kernel gave up waiting for its MMAs, else 0. */
 int sfem_gb300_set_elasticity_kernel(int variant);
 int sfem_gb300_elasticity_status(void);

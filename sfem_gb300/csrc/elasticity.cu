@@ -505,27 +505,29 @@ static int elasticity_apply_tc(int element_type, ptrdiff_t nelements, idx_t **el
 // dofs, A[m][(j, b)] = u_j(corner b of micro element m); B_e = K_e (24 x 24, N padded
 // to 32, K-major); D_e = A K_e^T in tensor memory (the rows of e are kept).  Operands
 // are split into TF32 hi = tf32(x) and lo = x - hi and multiplied as hi.hi + hi.lo +
-// lo.hi (kind::tf32, K = 8 per MMA, FP32 accumulate): 18 MMAs per pair, FP32-level
-// accuracy (the dropped lo.lo term is ~2^-22 relative).  Epilogue: warp w reads TMEM
-// lanes 32w.. (w < 2: e0, else e1), adds the 24 values of each micro element into the
-// element's node accumulator in shared memory, then the nodes are scattered like the
-// SIMT kernel (plain read-modify-write on interior nodes, atomics on the surface).
+// lo.hi (kind::tf32, K = 8 per MMA, FP32 accumulate): 9 MMAs per element, issued by
+// lane 0 of warp e, FP32-level accuracy (the dropped lo.lo term is ~2^-22 relative).
+// K is built from its six distinct 8x8 blocks (K_ji = K_ij^T).  The next pair's
+// metric, node indices and values are loaded while the current pair is processed.
+// Epilogue: the D rows go to shared memory; each thread then sums the (up to 8)
+// micro-element contributions of its nodes and adds them to y with atomics.
 constexpr int ETC_L = 4, ETC_N1 = ETC_L + 1, ETC_NXE = ETC_N1 * ETC_N1 * ETC_N1;  // 125 nodes
 constexpr int ETC_A_CHUNK = 128 * 16;   // [chunk of 4 dofs][row 128][16 B]
 constexpr int ETC_A_BYTES = 6 * ETC_A_CHUNK;
 constexpr int ETC_B_CHUNK = 32 * 16;    // [chunk][n 32][16 B]
 constexpr int ETC_B_BYTES = 6 * ETC_B_CHUNK;  // one element
-constexpr int ETC_OFF_AHI = 0, ETC_OFF_ALO = ETC_A_BYTES;
+constexpr int ETC_YLD = 25;             // row stride (floats) of the D rows in shared memory
+constexpr int ETC_OFF_AHI = 0, ETC_OFF_ALO = ETC_A_BYTES;  // D rows alias both after the MMAs
 constexpr int ETC_OFF_BHI = 2 * ETC_A_BYTES, ETC_OFF_BLO = ETC_OFF_BHI + 2 * ETC_B_BYTES;
 constexpr int ETC_OFF_I = ETC_OFF_BLO + 2 * ETC_B_BYTES;   // 576 floats
 constexpr int ETC_OFF_W = ETC_OFF_I + 576 * 4;             // [2][81] floats (+ pad)
 constexpr int ETC_OFF_X = ETC_OFF_W + 2 * 84 * 4;          // [2][3][125] floats
-constexpr int ETC_OFF_Y = ETC_OFF_X + 2 * 3 * ETC_NXE * 4;  // [2][3][125] floats
-constexpr int ETC_SMEM = ETC_OFF_Y + 2 * 3 * ETC_NXE * 4;
+constexpr int ETC_SMEM = ETC_OFF_X + 2 * 3 * ETC_NXE * 4;
 constexpr int ETC_CTAS_PER_SM = 4;
 constexpr uint32_t ETC_TMEM_COLS = 64;  // D_e at cols 32 e
 constexpr int ETC_WAIT_POLLS = 1 << 20;
 static_assert((ETC_SMEM + 2048) * ETC_CTAS_PER_SM <= 228 * 1024, "shared memory of the resident CTAs");
+static_assert(128 * ETC_YLD * 4 <= 2 * ETC_A_BYTES, "D rows fit in the A region");
 __device__ int g_etc_status;  // nonzero: a tensor-core wait gave up
 
 __global__ void __launch_bounds__(128, ETC_CTAS_PER_SM) elasticity_apply_tf32x3_kernel(
@@ -534,17 +536,19 @@ __global__ void __launch_bounds__(128, ETC_CTAS_PER_SM) elasticity_apply_tf32x3_
     extern __shared__ __align__(16) unsigned char es[];
     __shared__ __align__(8) uint64_t mbar;
     __shared__ uint32_t tmem_holder;
+    __shared__ const idx_t *srow[ETC_NXE];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int e_loc = tid >> 6, u = tid & 63;  // element of the pair this thread serves in phases 1-2, 5
+    const int e_loc = tid >> 6, u = tid & 63;  // element of the pair this thread serves
     float *Is = reinterpret_cast<float *>(es + ETC_OFF_I);
     float *W = reinterpret_cast<float *>(es + ETC_OFF_W) + 84 * e_loc;
     float *xs = reinterpret_cast<float *>(es + ETC_OFF_X);
-    float *ys = reinterpret_cast<float *>(es + ETC_OFF_Y);
+    float *Yd = reinterpret_cast<float *>(es + ETC_OFF_AHI);  // D rows after the MMAs
     for (int i = tid; i < ETC_OFF_I / 16; i += 128) reinterpret_cast<uint4 *>(es)[i] = make_uint4(0, 0, 0, 0);
     for (int k = tid; k < 576; k += 128) Is[k] = (float)(&kGrad.I[0][0][0][0])[k];
-    for (int i = tid; i < 2 * 3 * ETC_NXE; i += 128) ys[i] = 0.f;
+    if (tid < ETC_NXE) srow[tid] = elements[tid];
+    if (tid + 128 < ETC_NXE) srow[tid + 128] = elements[tid + 128];
     if (warp == 0) tc::tmem_alloc(&tmem_holder, ETC_TMEM_COLS);
-    if (tid == 0) tc::mbar_init(&mbar, 1);
+    if (tid == 0) tc::mbar_init(&mbar, 2);  // one arrival per issuing warp (0, 1)
     tc::fence_async_smem();
     tc::fence_before_sync();
     __syncthreads();
@@ -552,73 +556,120 @@ __global__ void __launch_bounds__(128, ETC_CTAS_PER_SM) elasticity_apply_tf32x3_
     const uint32_t tmem = tmem_holder;
     uint32_t phase = 0;
     bool ok = true;
-    // micro element of this thread's A row (row tid: element tid / 64, micro element tid % 64)
-    const int mx = u % ETC_L, my = (u / ETC_L) % ETC_L, mz = u / (ETC_L * ETC_L);
+    // this thread's A row: micro element u of element e_loc; its nodes' lidx base
+    const int mbase = lidx(ETC_L, u % ETC_L, (u / ETC_L) % ETC_L, u / (ETC_L * ETC_L));
+    // this thread's nodes (v = u and u + 64 < 125) of element e_loc: prefetched metric,
+    // indices and values of the next pair
+    float pad_[10];
+    idx_t pg[2] = {0, 0};
+    float px[2][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
+    auto fetch_meta = [&](ptrdiff_t e) {
+#pragma unroll
+        for (int d = 0; d < 9; d++) pad_[d] = adjugate[d * stride + e];
+        pad_[9] = determinant[e];
+#pragma unroll
+        for (int k = 0; k < 2; k++) pg[k] = (u + 64 * k < ETC_NXE) ? srow[u + 64 * k][e] : 0;
+    };
+    auto fetch_x = [&]() {
+#pragma unroll
+        for (int k = 0; k < 2; k++)
+            if (u + 64 * k < ETC_NXE)
+#pragma unroll
+                for (int d = 0; d < 3; d++) px[k][d] = x[3 * (ptrdiff_t)pg[k] + d];
+    };
+    {
+        const ptrdiff_t e = 2 * (ptrdiff_t)blockIdx.x + e_loc;
+        if (e < nelements) {
+            fetch_meta(e);
+            fetch_x();
+        }
+    }
     for (ptrdiff_t pr = blockIdx.x; 2 * pr < nelements && ok; pr += gridDim.x) {
         const ptrdiff_t e = 2 * pr + e_loc;
         const bool valid = e < nelements;
         const bool pair = 2 * pr + 1 < nelements;
-        // 1. sub-adjugate, W, gather of the element's 125 x 3 values
-        float adj[9], AA[9], inv_det = 0.f;
+        // 1. W from the prefetched metric, the element's values into shared memory
+        idx_t gcur[2] = {pg[0], pg[1]};
+        float inv_det = 0.f;
         if (valid) {
-            load_sub_adjugate<float>(adjugate, determinant, stride, e, ETC_L, adj, AA, inv_det);
+            const float h = 1.f / (float)ETC_L;
+            float adj[9], AA[9];
+#pragma unroll
+            for (int d = 0; d < 9; d++) adj[d] = pad_[d] * (h * h);
+            inv_det = 1.f / (pad_[9] * (h * h * h));
+#pragma unroll
+            for (int p = 0; p < 3; p++)
+#pragma unroll
+                for (int q = 0; q < 3; q++)
+                    AA[3 * p + q] = adj[3 * p] * adj[3 * q] + adj[3 * p + 1] * adj[3 * q + 1] + adj[3 * p + 2] * adj[3 * q + 2];
             for (int k = u; k < 81; k += 64) {
                 const int i = k / 27, j = (k / 9) % 3, p = (k / 3) % 3, q = k % 3;
                 float w = mu * adj[3 * p + j] * adj[3 * q + i] + lambda * adj[3 * p + i] * adj[3 * q + j];
                 if (i == j) w += mu * AA[3 * p + q];
                 W[k] = w;
             }
-            for (int v = u; v < ETC_NXE; v += 64) {
-                const idx_t g = elements[v][e];
 #pragma unroll
-                for (int d = 0; d < 3; d++) xs[(e_loc * 3 + d) * ETC_NXE + v] = x[3 * (ptrdiff_t)g + d];
-            }
+            for (int k = 0; k < 2; k++)
+                if (u + 64 * k < ETC_NXE)
+#pragma unroll
+                    for (int d = 0; d < 3; d++) xs[(e_loc * 3 + d) * ETC_NXE + u + 64 * k] = px[k][d];
         }
+        // next pair's metric and node indices (consumed next iteration)
+        const ptrdiff_t en = 2 * (pr + gridDim.x) + e_loc;
+        const bool has_next = en < nelements;
+        if (has_next) fetch_meta(en);
         __syncthreads();
-        // 2. B_e = K_e (hi / lo) and this thread's A row
+        // 2. B_e = K_e (hi / lo) from its six distinct 8x8 blocks, and this thread's A row
         if (valid) {
-            for (int k = u; k < 576; k += 64) {
-                const int row = k / 24, col = k % 24;
-                const int i = row >> 3, a = row & 7, j = col >> 3, b = col & 7;
+            for (int k = u; k < 6 * 64; k += 64) {
+                const int blk = k >> 6, a = (k >> 3) & 7, b = k & 7;
+                const int i = blk < 3 ? 0 : (blk < 5 ? 1 : 2);
+                const int j = blk < 3 ? blk : (blk < 5 ? blk - 2 : 2);  // (0,0) (0,1) (0,2) (1,1) (1,2) (2,2)
                 const float *Iab = &Is[(a * 8 + b) * 9];
                 const float *Wij = &W[(i * 3 + j) * 9];
                 float acc = 0.f;
 #pragma unroll
                 for (int pq = 0; pq < 9; pq++) acc += Iab[pq] * Wij[pq];
                 acc *= inv_det;
-                const float hi = tc::tf32_round(acc);
-                const int off = e_loc * ETC_B_BYTES + (col >> 2) * ETC_B_CHUNK + row * 16 + (col & 3) * 4;
-                *reinterpret_cast<float *>(es + ETC_OFF_BHI + off) = hi;
-                *reinterpret_cast<float *>(es + ETC_OFF_BLO + off) = acc - hi;
+                const float hi = tc::tf32_round(acc), lo = acc - hi;
+                const int r1 = i * 8 + a, c1 = j * 8 + b;
+                const int o1 = e_loc * ETC_B_BYTES + (c1 >> 2) * ETC_B_CHUNK + r1 * 16 + (c1 & 3) * 4;
+                const int o2 = e_loc * ETC_B_BYTES + (r1 >> 2) * ETC_B_CHUNK + c1 * 16 + (r1 & 3) * 4;
+                *reinterpret_cast<float *>(es + ETC_OFF_BHI + o1) = hi;
+                *reinterpret_cast<float *>(es + ETC_OFF_BLO + o1) = lo;
+                *reinterpret_cast<float *>(es + ETC_OFF_BHI + o2) = hi;  // K symmetric
+                *reinterpret_cast<float *>(es + ETC_OFF_BLO + o2) = lo;
             }
-            const float *xe = xs + e_loc * 3 * ETC_NXE;
+            const float *xe = xs + e_loc * 3 * ETC_NXE + mbase;
 #pragma unroll
             for (int c4 = 0; c4 < 6; c4++) {
-                float h[4], l[4];
+                float hv[4], lv[4];
 #pragma unroll
                 for (int k = 0; k < 4; k++) {
                     const int col = 4 * c4 + k, j = col >> 3, b = col & 7;
-                    const float val =
-                            xe[j * ETC_NXE + lidx(ETC_L, mx + c8x(b), my + c8y(b), mz + c8z(b))];
-                    h[k] = tc::tf32_round(val);
-                    l[k] = val - h[k];
+                    const float val = xe[j * ETC_NXE + lidx(ETC_L, c8x(b), c8y(b), c8z(b))];
+                    hv[k] = tc::tf32_round(val);
+                    lv[k] = val - hv[k];
                 }
-                *reinterpret_cast<float4 *>(es + ETC_OFF_AHI + c4 * ETC_A_CHUNK + tid * 16) = make_float4(h[0], h[1], h[2], h[3]);
-                *reinterpret_cast<float4 *>(es + ETC_OFF_ALO + c4 * ETC_A_CHUNK + tid * 16) = make_float4(l[0], l[1], l[2], l[3]);
+                *reinterpret_cast<float4 *>(es + ETC_OFF_AHI + c4 * ETC_A_CHUNK + tid * 16) =
+                        make_float4(hv[0], hv[1], hv[2], hv[3]);
+                *reinterpret_cast<float4 *>(es + ETC_OFF_ALO + c4 * ETC_A_CHUNK + tid * 16) =
+                        make_float4(lv[0], lv[1], lv[2], lv[3]);
             }
         }
         tc::fence_async_smem();
         tc::fence_before_sync();
         __syncthreads();
         tc::fence_after_sync();
-        // 3. MMAs: D_e (+)= A_hi B_hi + A_hi B_lo + A_lo B_hi over 3 K steps
-        if (tid == 0) {
-            constexpr uint32_t id = tc::idesc_tf32_f32(128, 32);
-            const uint64_t ahi = tc::sdesc(tc::smem_u32(es + ETC_OFF_AHI), ETC_A_CHUNK, 128);
-            const uint64_t alo = tc::sdesc(tc::smem_u32(es + ETC_OFF_ALO), ETC_A_CHUNK, 128);
-            const uint64_t bhi = tc::sdesc(tc::smem_u32(es + ETC_OFF_BHI), ETC_B_CHUNK, 128);
-            const uint64_t blo = tc::sdesc(tc::smem_u32(es + ETC_OFF_BLO), ETC_B_CHUNK, 128);
-            for (int el = 0; el < (pair ? 2 : 1); el++) {
+        // 3. MMAs: lane 0 of warp el issues D_el (+)= A_hi B_hi + A_hi B_lo + A_lo B_hi, 3 K steps
+        if (lane == 0 && warp < 2) {
+            const int el = warp;
+            if (el == 0 || pair) {
+                constexpr uint32_t id = tc::idesc_tf32_f32(128, 32);
+                const uint64_t ahi = tc::sdesc(tc::smem_u32(es + ETC_OFF_AHI), ETC_A_CHUNK, 128);
+                const uint64_t alo = tc::sdesc(tc::smem_u32(es + ETC_OFF_ALO), ETC_A_CHUNK, 128);
+                const uint64_t bhi = tc::sdesc(tc::smem_u32(es + ETC_OFF_BHI), ETC_B_CHUNK, 128);
+                const uint64_t blo = tc::sdesc(tc::smem_u32(es + ETC_OFF_BLO), ETC_B_CHUNK, 128);
 #pragma unroll
                 for (int st = 0; st < 3; st++) {
                     const uint64_t ao = (uint64_t)(2 * st * ETC_A_CHUNK / 16);
@@ -630,6 +681,7 @@ __global__ void __launch_bounds__(128, ETC_CTAS_PER_SM) elasticity_apply_tf32x3_
             }
             tc::commit(&mbar);
         }
+        if (has_next) fetch_x();  // the values of the next pair's nodes (indices loaded above)
         {
             bool w = true;
             if (warp == 0) w = tc::mbar_wait(&mbar, phase, ETC_WAIT_POLLS);
@@ -638,42 +690,43 @@ __global__ void __launch_bounds__(128, ETC_CTAS_PER_SM) elasticity_apply_tf32x3_
             tc::fence_after_sync();
         }
         if (!ok) break;
-        // 4. epilogue: row m of warp w's lanes -> the element's node accumulator
+        // 4. D rows to shared memory (row 32 w + lane of element w / 2)
         {
             const int el = warp >> 1;
             float a[16], b[16];
             tc::tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + 32 * el, a);
             tc::tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + 32 * el + 16, b);
-            if (2 * pr + el < nelements) {
-                const int m = (32 * warp + lane) & 63;
-                const int px = m % ETC_L, py = (m / ETC_L) % ETC_L, pz = m / (ETC_L * ETC_L);
-                float *ye = ys + el * 3 * ETC_NXE;
+            float *yr = Yd + tid * ETC_YLD;
 #pragma unroll
-                for (int r = 0; r < 24; r++) {
-                    const int i = r >> 3, c = r & 7;
-                    atomicAdd(&ye[i * ETC_NXE + lidx(ETC_L, px + c8x(c), py + c8y(c), pz + c8z(c))],
-                              r < 16 ? a[r] : b[r - 16]);
-                }
-            }
+            for (int r = 0; r < 16; r++) yr[r] = a[r];
+#pragma unroll
+            for (int r = 0; r < 8; r++) yr[16 + r] = b[r];
         }
         tc::fence_before_sync();
         __syncthreads();
         tc::fence_after_sync();
-        // 5. scatter and reset the accumulator
+        // 5. node sums over the (up to 8) micro elements around each node, added to y
         if (valid) {
-            for (int v = u; v < ETC_NXE; v += 64) {
-                const idx_t g = elements[v][e];
-                const int vx = v % ETC_N1, vy = (v / ETC_N1) % ETC_N1, vz = v / (ETC_N1 * ETC_N1);
-                const bool interior = vx > 0 && vx < ETC_L && vy > 0 && vy < ETC_L && vz > 0 && vz < ETC_L;
 #pragma unroll
-                for (int d = 0; d < 3; d++) {
-                    float *yv = &ys[(e_loc * 3 + d) * ETC_NXE + v];
-                    float *dst = &y[3 * (ptrdiff_t)g + d];
-                    if (interior)
-                        *dst += *yv;
-                    else
-                        atomicAdd(dst, *yv);
-                    *yv = 0.f;
+            for (int k = 0; k < 2; k++) {
+                const int v = u + 64 * k;
+                if (v < ETC_NXE) {
+                    const int vx = v % ETC_N1, vy = (v / ETC_N1) % ETC_N1, vz = v / (ETC_N1 * ETC_N1);
+                    float s0 = 0.f, s1 = 0.f, s2 = 0.f;
+#pragma unroll
+                    for (int c = 0; c < 8; c++) {
+                        const int mx = vx - c8x(c), my = vy - c8y(c), mz = vz - c8z(c);
+                        if ((unsigned)mx < ETC_L && (unsigned)my < ETC_L && (unsigned)mz < ETC_L) {
+                            const float *yr = Yd + (e_loc * 64 + (mz * ETC_L + my) * ETC_L + mx) * ETC_YLD;
+                            s0 += yr[c];
+                            s1 += yr[8 + c];
+                            s2 += yr[16 + c];
+                        }
+                    }
+                    float *dst = &y[3 * (ptrdiff_t)gcur[k]];
+                    atomicAdd(dst, s0);
+                    atomicAdd(dst + 1, s1);
+                    atomicAdd(dst + 2, s2);
                 }
             }
         }
@@ -689,7 +742,7 @@ __global__ void __launch_bounds__(128, ETC_CTAS_PER_SM) elasticity_apply_tf32x3_
     if (warp == 0) tc::tmem_dealloc(tmem, ETC_TMEM_COLS);
 }
 
-static int g_elasticity_kernel = -1;  // -1 default (SIMT), 0 SIMT warp kernel, 1 tcgen05 3xTF32 (FP32, L = 4)
+static int g_elasticity_kernel = -1;  // -1 default (tcgen05 at L = 4), 0 SIMT warp kernel, 1 tcgen05 3xTF32
 
 static int elasticity_apply_tf32x3(ptrdiff_t nelements, idx_t **elements, ptrdiff_t stride, const float *adj,
                                    const float *det, float mu, float lambda, const float *x, float *y, cudaStream_t s) {
@@ -716,7 +769,7 @@ static int elasticity_apply_tpl(int element_type, ptrdiff_t nelements, idx_t **e
     }
     const int L = element_type - SFEM_GB300_SSHEX8_BASE;
     if constexpr (sizeof(T) == 4) {
-        if (L == 4 && g_elasticity_kernel == 1)
+        if (L == 4 && g_elasticity_kernel != 0)
             return elasticity_apply_tf32x3(nelements, elements, stride, adj, det, mu, lambda, x, y, s);
     }
 #define SFEM_EL_CASE(LL)                                                                                             \
