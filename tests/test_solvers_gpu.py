@@ -103,7 +103,10 @@ def test_sshex8_mg_pcg_fp64(cuda, smoother):
     x_star, _ = OS.cg(apply, b, precond=lambda r: r / d, rtol=1e-14, max_it=20000)
     ctx = S.context()
     mg, op = S.build_poisson_mg(ctx, H, torch.float64, smoother=smoother, sweeps=2)
-    solver = S.cg(ctx, op, mg, rtol=1e-11, max_it=200, flexible=(smoother == "jacobi"))
+    # stop on the residual norm: with the weak Jacobi-smoothed V-cycle the reference's
+    # preconditioned criterion sqrt(r.z) / sqrt(r0.z0) can pass while ||r|| / ||r0|| is
+    # still above the 1e-10 the test checks
+    solver = S.cg(ctx, op, mg, rtol=1e-11, max_it=200, flexible=(smoother == "jacobi"), residual_norm=True)
     bd = torch.from_numpy(b).to(cuda)
     x = torch.zeros_like(bd)
     assert S.solve(solver, bd, x) == 0
