@@ -427,13 +427,18 @@ def measure_learned(dev, nx=32, draws=64, n_pairs=100_000, epochs=20, eval_draws
     smoother is trained by the project's kernels on 10^5 residual/error pairs from plain
     V-cycles on 64 coefficient draws, then every arm solves fresh draws to FP64 1e-10
     with flexible CG: FP64 multigrid (plain), + learned correction, FP32 multigrid
-    through the precision bridge (mixed), + learned correction (mixed_learned)."""
+    through the precision bridge (mixed), + learned correction (mixed_learned).  Plain
+    and mixed smooth with Chebyshev3 V(2,2); in the learned arms the post-smoothing is
+    the learned correction followed by one Chebyshev3 sweep (the correction takes the
+    place of the second sweep)."""
     from sfem_gb300 import learned
 
     res = learned.run_experiment(nx=nx, draws=draws, n_pairs=n_pairs, epochs=epochs, eval_draws=eval_draws,
-                                 device=str(dev), placement="before")
+                                 device=str(dev), placement="before", fallback_sweeps=1)
     arms = list(res["eval"][0].keys())
     out = {"nx": nx, "draws": draws, "pairs": res["pairs"], "epochs": epochs, "placement": res["placement"],
+           "smoothing": {"plain_and_mixed": "Chebyshev3 V(2,2)",
+                         "learned_arms": "pre: 2 Chebyshev3 sweeps; post: learned correction + 1 Chebyshev3 sweep"},
            "loss_first": res["loss_first"], "loss_last": res["loss_last"], "harvest_seconds": res["harvest_seconds"],
            "train_seconds": res["train_seconds"]}
     for a in arms:

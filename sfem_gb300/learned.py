@@ -256,19 +256,23 @@ def train(net: PatchNet, xin, xt, epochs=20, batch=4096, lr=2e-3, seed=0, log=No
 
 
 def learned_mg(ctx, H, net: PatchNet, dtype, omega=1.0, sweeps=1, eig_max=None, post_only=False, chain=True,
-               **mg_kwargs):
+               fallback_sweeps=None, **mg_kwargs):
     """Multigrid with the learned smoother on the finest level.
 
     chain="before" : the finest-level post-smoothing is the learned correction of the
     coarse-grid-corrected iterate followed by Chebyshev3 (matches point="coarse" data);
     chain=True (or "after"): Chebyshev3 followed by the learned correction (matches
     point="cycle" data); chain=False: the learned smoother replaces Chebyshev3 (pre and
-    post unless post_only)."""
+    post unless post_only).  fallback_sweeps: Chebyshev3 sweeps of the post-smoother that
+    follows (or precedes) the learned correction (default: the pre-smoother's 2)."""
     mg, op = S.build_poisson_mg(ctx, H, dtype, smoother="chebyshev3", sweeps=2, eig_max=eig_max, **mg_kwargs)
     fine = H.spaces[0]
     inv_diag = fine_inv_diag(H, dtype)
     lib = _lib()
     ch = mg.smoothers[0]  # finest-level Chebyshev3: the fallback
+    if fallback_sweeps is not None and fallback_sweeps != 2:
+        ch = S.chebyshev3(ctx, op, max_it=fallback_sweeps, eig_max=mg.eigs[0], inv_diag=inv_diag)
+        mg.keep.append(ch)
     out = C.c_void_p(0)
     capi.check(lib.sfem_gb300_learned_smoother_create(
         ctx.ptr, op.ptr, fine.lidx_ptrs.ptr, capi.i64(H.mesh.n_elements), capi.vp(fine.count), capi.vp(inv_diag),
@@ -327,7 +331,7 @@ def hierarchy_with_coefficient(mesh, k, device, base=None, coarsen_macro=True):
 
 def run_experiment(nx=32, draws=64, n_pairs=100_000, epochs=30, eval_draws=2, device="cuda:0", seed=0, log=None,
                    rtol=1e-10, placement="before", arms=("chebyshev3", "learned", "mixed", "mixed_learned"),
-                   graph=True):
+                   graph=True, fallback_sweeps=None):
     """Train on ``draws`` coefficient fields, then A/B on fresh draws: FP64 flexible CG
     preconditioned by the FP64 multigrid (chebyshev3), the same plus the learned correction
     (learned), the FP32 multigrid through the precision bridge (mixed), and that plus the
@@ -379,13 +383,15 @@ def run_experiment(nx=32, draws=64, n_pairs=100_000, epochs=30, eval_draws=2, de
             ctx = S.context()
             learned_arm = name.endswith("learned")
             if name in ("chebyshev3", "learned"):
-                mg, op = (learned_mg(ctx, H, net, torch.float64, chain=chain, coarse="dense", graph=graph)
+                mg, op = (learned_mg(ctx, H, net, torch.float64, chain=chain, coarse="dense", graph=graph,
+                                     fallback_sweeps=fallback_sweeps)
                           if learned_arm else
                           S.build_poisson_mg(ctx, H, torch.float64, smoother="chebyshev3", sweeps=2, coarse="dense",
                                              graph=graph))
                 pc, op64 = mg, op
             else:
-                mg, _ = (learned_mg(ctx, H, net, torch.float32, chain=chain, coarse="dense", graph=graph)
+                mg, _ = (learned_mg(ctx, H, net, torch.float32, chain=chain, coarse="dense", graph=graph,
+                                    fallback_sweeps=fallback_sweeps)
                          if learned_arm else
                          S.build_poisson_mg(ctx, H, torch.float32, smoother="chebyshev3", sweeps=2, coarse="dense",
                                             graph=graph))
