@@ -486,29 +486,26 @@ __device__ __forceinline__ void lap_layer_f32x2(const float *__restrict__ xbase,
     }
 }
 
-template <int L, int TILE>
-__global__ void __launch_bounds__(2 * TILE, 6) sshex8_laplacian_apply_async_kernel(ptrdiff_t nelements,
-                                                                                const idx_t *const *elements,
-                                                                                ptrdiff_t fff_stride,
-                                                                                const float *fff,
-                                                                                const float *__restrict__ x,
-                                                                                float *__restrict__ y) {
-    static_assert(L % 2 == 0, "two threads per element split the micro layers in halves");
+template <int L, int TILE, int NQ = 2>
+__global__ void __launch_bounds__(NQ * TILE, NQ == 2 ? 6 : 4) sshex8_laplacian_apply_async_kernel(
+        ptrdiff_t nelements, const idx_t *const *elements, ptrdiff_t fff_stride, const float *fff,
+        const float *__restrict__ x, float *__restrict__ y) {
+    static_assert(L % NQ == 0, "NQ threads per element split the micro layers evenly");
     constexpr int N1 = L + 1;
     constexpr int NP = N1 * N1;
     constexpr int NXE = NP * N1;
-    constexpr int H = L / 2;  // layers per half; the shared plane is H
+    constexpr int H = L / NQ;  // layers per thread; thread q's bottom plane q H is shared with thread q - 1
     __shared__ __align__(16) idx_t sidx[NXE * TILE];
     __shared__ __align__(16) float sx[NXE * TILE];
-    __shared__ float spart[NP * TILE];  // upper half's partial sum of the shared plane
+    __shared__ float spart[(NQ - 1) * NP * TILE];  // partial sums of the shared planes (from the upper thread)
     __shared__ const idx_t *srow[NXE];  // the row pointers: one global load each, then shared
     const int tid = threadIdx.x;
     const ptrdiff_t e0 = (ptrdiff_t)blockIdx.x * TILE;
     const int nvalid = (int)((nelements - e0) < TILE ? (nelements - e0) : TILE);
-    for (int v = tid; v < NXE; v += 2 * TILE) srow[v] = elements[v];
+    for (int v = tid; v < NXE; v += NQ * TILE) srow[v] = elements[v];
     __syncthreads();
     // 1. connectivity rows
-    for (int v = tid / (TILE / 4); v < NXE; v += (2 * TILE) / (TILE / 4)) {
+    for (int v = tid / (TILE / 4); v < NXE; v += (NQ * TILE) / (TILE / 4)) {
         const int q = tid % (TILE / 4);  // 16-byte quarter of the row segment
         const idx_t *row = srow[v] + e0;
         if (nvalid == TILE && ((reinterpret_cast<uintptr_t>(row) & 15) == 0)) {
@@ -522,12 +519,12 @@ __global__ void __launch_bounds__(2 * TILE, 6) sshex8_laplacian_apply_async_kern
     cp_async_wait_all();
     __syncthreads();
     // 2. gather x
-    for (int t = tid; t < NXE * TILE; t += 2 * TILE) {
+    for (int t = tid; t < NXE * TILE; t += NQ * TILE) {
         const int el = t % TILE;
         if (el < nvalid) cp_async4(&sx[t], x + sidx[t]);
     }
     const int el = tid % TILE;
-    const int half = tid / TILE;  // warp-uniform for TILE = 32
+    const int half = tid / TILE;  // the thread's layer group q; warp-uniform for TILE = 32
     const bool valid = el < nvalid;
     // element matrix, rows 0..3 packed by pairs (overlaps the gathers in flight)
     float2 A2[8][2];
@@ -554,7 +551,7 @@ __global__ void __launch_bounds__(2 * TILE, 6) sshex8_laplacian_apply_async_kern
     }
     cp_async_wait_all();
     __syncthreads();
-    // 3. apply: half h runs layers h*H .. h*H + H - 1 upwards (same code for both halves)
+    // 3. apply: thread group q runs layers q*H .. q*H + H - 1 upwards (same code for every q)
     float *col = sx + el;
     const int z0 = half * H;
     float lo[NP], up[NP];
@@ -565,28 +562,29 @@ __global__ void __launch_bounds__(2 * TILE, 6) sshex8_laplacian_apply_async_kern
 #pragma unroll
         for (int p = 0; p < NP; p++) up[p] = 0.f;
         lap_layer_f32x2<L, TILE>(col + zi * NP * TILE, A2, lo, up);
-        // plane zi is complete for this half; its x is not read again by this half.
-        // The upper half's bottom plane is the shared one: keep it aside.
-        float *dst = (zi == H && half == 1) ? (spart + el) : (col + zi * NP * TILE);
+        // plane zi is complete for this thread; its x is not read again by it.  A bottom
+        // plane shared with the group below (zi == z0 > 0) is kept aside.
+        float *dst = (zi == z0 && half > 0) ? (spart + (half - 1) * NP * TILE + el) : (col + zi * NP * TILE);
 #pragma unroll
         for (int p = 0; p < NP; p++) {
             dst[p * TILE] = lo[p];
             lo[p] = up[p];
         }
     }
-    // lo = plane z0 + H: the lower half's partial of the shared plane, the upper half's top plane
-    if (half == 1) {
+    // lo = plane z0 + H: the top group's last plane, the others' partial of a shared plane
+    if (half == NQ - 1) {
 #pragma unroll
         for (int p = 0; p < NP; p++) col[(L * NP + p) * TILE] = lo[p];
     }
-    __syncthreads();  // every x read of the shared plane is done
-    if (half == 0) {
+    __syncthreads();  // every x read of the shared planes is done
+    if (half < NQ - 1) {
+        const float *sp = spart + half * NP * TILE + el;
 #pragma unroll
-        for (int p = 0; p < NP; p++) col[(H * NP + p) * TILE] = lo[p] + spart[p * TILE + el];
+        for (int p = 0; p < NP; p++) col[((z0 + H) * NP + p) * TILE] = lo[p] + sp[p * TILE];
     }
     __syncthreads();
     // 4. scatter
-    for (int t = tid; t < NXE * TILE; t += 2 * TILE) {
+    for (int t = tid; t < NXE * TILE; t += NQ * TILE) {
         if (t % TILE < nvalid) atomicAdd(&y[sidx[t]], sx[t]);
     }
 }
@@ -785,7 +783,8 @@ __global__ void __launch_bounds__(128) sshex8_laplacian_diag_kernel(ptrdiff_t ne
 // "staged" (0) = shared-memory staged tile kernel for float, L <= 4;
 // "warp" (1) = warp per element; "thread" (2) = registers-only thread per element;
 // "async" (3) = cp.async staged tile, two threads per element, packed FP32x2 FMAs (even L);
-// "pipe" (4) = persistent CTAs, cp.async pipeline across tiles, one warp per micro layer (even L).
+// "pipe" (4) = persistent CTAs, cp.async pipeline across tiles, one warp per micro layer (even L);
+// 6 = the async tile with four threads per element (one micro layer each, L = 4).
 static int g_laplacian_variant = -1;
 static int g_laplacian_variant_forced = 0;  // set by sfem_gb300_set_laplacian_kernel
 static int laplacian_variant() {
@@ -858,6 +857,13 @@ static int laplacian_apply_tpl(int element_type, ptrdiff_t nelements, idx_t **el
         else
             launch(sshex8_laplacian_apply_pipe_kernel<4, TILE>, 4);
         return check_launch("cu_laplacian_apply(SSHEX8, pipelined tile)");
+    }
+    if (sizeof(T) == 4 && L == 4 && variant == 6) {
+        constexpr int TILE = 32;
+        const int tb = (int)((nelements + TILE - 1) / TILE);
+        sshex8_laplacian_apply_async_kernel<4, TILE, 4><<<tb, 4 * TILE, 0, s>>>(nelements, elements, fff_stride, fff,
+                                                                                (const float *)x, (float *)y);
+        return check_launch("cu_laplacian_apply(SSHEX8, async tile, four threads per element)");
     }
     if (sizeof(T) == 4 && (L == 2 || L == 4) && variant == 3) {
         constexpr int TILE = 32;
@@ -984,7 +990,8 @@ extern "C" int cu_laplacian_diag(int element_type, ptrdiff_t nelements, idx_t **
 }
 
 extern "C" int sfem_gb300_set_laplacian_kernel(int variant) {
-    if (variant < -1 || variant > 4) return set_error("sfem_gb300_set_laplacian_kernel: variant must be -1..4");
+    if (variant < -1 || variant > 6 || variant == 5)
+        return set_error("sfem_gb300_set_laplacian_kernel: variant must be -1..4 or 6");
     const int cur = laplacian_variant();
     const int prev = __atomic_load_n(&g_laplacian_variant_forced, __ATOMIC_RELAXED) ? cur : -1;
     __atomic_store_n(&g_laplacian_variant, variant < 0 ? 0 : variant, __ATOMIC_RELAXED);
