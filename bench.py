@@ -62,6 +62,9 @@ def parse():
     ap.add_argument("--profile-kernels", action="store_true",
                     help="launch each main kernel twice on the bench workloads and exit (an ncu target)")
     ap.add_argument("--batch-problems", type=int, default=256)
+    ap.add_argument("--profile-solves", action="store_true",
+                    help="run one mixed + learned Poisson solve (32^3 L=4, k = exp(g)) and one mixed elasticity "
+                         "solve (64x16x16 L=4): the target of the solver launch-list captures in profiles/")
     return ap.parse_args()
 
 
@@ -661,10 +664,56 @@ def profile_kernels():
     print("profile kernels: done")
 
 
+def profile_solves():
+    """One FP64 flexible-CG solve preconditioned by the FP32 multigrid with the learned
+    correction (32^3 L=4, k = exp(g), untrained network, 12 iterations) and one
+    mixed-precision elasticity solve (64x16x16 L=4, to 1e-9); V-cycles graph-replayed."""
+    import torch
+
+    from sfem_gb300 import learned
+    from sfem_gb300 import solvers as S
+    from sfem_gb300.coefficients import lognormal_coefficient
+    from sfem_gb300.mesh import SSMesh
+
+    dev = torch.device("cuda:0")
+    nx = 32
+    mesh = SSMesh(nx, nx, nx, LEVEL)
+    H = learned.hierarchy_with_coefficient(mesh, lognormal_coefficient(nx, nx, nx, ell=8.0, sigma=1.0, seed=5000), dev)
+    net = learned.PatchNet(dev, seed=0)
+    g = torch.Generator(device=dev).manual_seed(0)
+    b = torch.randn(H.spaces[0].n_nodes, dtype=torch.float64, device=dev, generator=g)
+    b[H.dirichlet[0].long()] = 0
+    ctx = S.context()
+    mg, _ = learned.learned_mg(ctx, H, net, torch.float32, chain="before", coarse="dense", graph=True, fallback_sweeps=1)
+    op64 = S.laplacian_op(ctx, H.spaces[0], H.spaces[0].fff, H.dirichlet[0], torch.float64)
+    solver = S.cg(ctx, op64, S.mixed_precond(ctx, mg), rtol=1e-10, max_it=12, residual_norm=True, flexible=True)
+    for _ in range(2):
+        x = torch.zeros_like(b)
+        S.solve(solver, b, x)
+    torch.cuda.synchronize()
+    del mg, solver, H
+    me = SSMesh(64, 16, 16, LEVEL, box=((0, 4), (0, 1), (0, 1)), perturb=0.0, seed=SEED)
+    He = S.Hierarchy(me, dirichlet_faces=("x0",), device=dev, vec=3, coarsen_macro=True)
+    mge, _ = S.build_elasticity_mg(ctx, He, torch.float32, coarse="dense", graph=True)
+    ope = S.elasticity_op(ctx, He.spaces[0], He.adj, He.det, 1.0, 10.0, He.dirichlet[0], torch.float64)
+    fe = torch.from_numpy(lumped_body_force(me, He.det.cpu().numpy())).to(dev)
+    for c in range(3):
+        fe[3 * He.dirichlet[0].long() + c] = 0
+    solver = S.cg(ctx, ope, S.mixed_precond(ctx, mge), rtol=1e-9, max_it=60, residual_norm=True, flexible=True)
+    for _ in range(2):
+        u = torch.zeros_like(fe)
+        S.solve(solver, fe, u)
+    torch.cuda.synchronize()
+    print("profile solves: done")
+
+
 def main():
     args = parse()
     if args.profile_kernels:
         profile_kernels()
+        return
+    if args.profile_solves:
+        profile_solves()
         return
     if args.impl == "reference":
         run_reference(args)
