@@ -519,9 +519,7 @@ constexpr int ETC_B_BYTES = 6 * ETC_B_CHUNK;  // one element
 constexpr int ETC_YLD = 25;             // row stride (floats) of the D rows in shared memory
 constexpr int ETC_OFF_AHI = 0, ETC_OFF_ALO = ETC_A_BYTES;  // D rows alias both after the MMAs
 constexpr int ETC_OFF_BHI = 2 * ETC_A_BYTES, ETC_OFF_BLO = ETC_OFF_BHI + 2 * ETC_B_BYTES;
-constexpr int ETC_OFF_I = ETC_OFF_BLO + 2 * ETC_B_BYTES;   // 576 floats
-constexpr int ETC_OFF_W = ETC_OFF_I + 576 * 4;             // [2][81] floats (+ pad)
-constexpr int ETC_OFF_X = ETC_OFF_W + 2 * 84 * 4;          // [2][3][125] floats
+constexpr int ETC_OFF_X = ETC_OFF_BLO + 2 * ETC_B_BYTES;   // [2][3][125] floats
 constexpr int ETC_SMEM = ETC_OFF_X + 2 * 3 * ETC_NXE * 4;
 constexpr int ETC_CTAS_PER_SM = 4;
 constexpr uint32_t ETC_TMEM_COLS = 64;  // D_e at cols 32 e
@@ -539,12 +537,14 @@ __global__ void __launch_bounds__(128, ETC_CTAS_PER_SM) elasticity_apply_tf32x3_
     __shared__ const idx_t *srow[ETC_NXE];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int e_loc = tid >> 6, u = tid & 63;  // element of the pair this thread serves
-    float *Is = reinterpret_cast<float *>(es + ETC_OFF_I);
-    float *W = reinterpret_cast<float *>(es + ETC_OFF_W) + 84 * e_loc;
     float *xs = reinterpret_cast<float *>(es + ETC_OFF_X);
     float *Yd = reinterpret_cast<float *>(es + ETC_OFF_AHI);  // D rows after the MMAs
-    for (int i = tid; i < ETC_OFF_I / 16; i += 128) reinterpret_cast<uint4 *>(es)[i] = make_uint4(0, 0, 0, 0);
-    for (int k = tid; k < 576; k += 128) Is[k] = (float)(&kGrad.I[0][0][0][0])[k];
+    for (int i = tid; i < ETC_OFF_X / 16; i += 128) reinterpret_cast<uint4 *>(es)[i] = make_uint4(0, 0, 0, 0);
+    // this thread builds the entries (a, b) = (u / 8, u % 8) of the six distinct 8x8 blocks
+    // of K: its nine gradient integrals I_ab^pq stay in registers
+    float Ir[9];
+#pragma unroll
+    for (int pq = 0; pq < 9; pq++) Ir[pq] = (float)kGrad.I[u >> 3][u & 7][pq / 3][pq % 3];
     if (tid < ETC_NXE) srow[tid] = elements[tid];
     if (tid + 128 < ETC_NXE) srow[tid + 128] = elements[tid + 128];
     if (warp == 0) tc::tmem_alloc(&tmem_holder, ETC_TMEM_COLS);
@@ -588,26 +588,23 @@ __global__ void __launch_bounds__(128, ETC_CTAS_PER_SM) elasticity_apply_tf32x3_
         const ptrdiff_t e = 2 * pr + e_loc;
         const bool valid = e < nelements;
         const bool pair = 2 * pr + 1 < nelements;
-        // 1. W from the prefetched metric, the element's values into shared memory
+        // 1. sub-adjugate from the prefetched metric (registers), the element's values into
+        // shared memory
         idx_t gcur[2] = {pg[0], pg[1]};
         float inv_det = 0.f;
-        if (valid) {
+        float adj[9], AA[9];
+        {
             const float h = 1.f / (float)ETC_L;
-            float adj[9], AA[9];
 #pragma unroll
             for (int d = 0; d < 9; d++) adj[d] = pad_[d] * (h * h);
-            inv_det = 1.f / (pad_[9] * (h * h * h));
+            inv_det = valid ? 1.f / (pad_[9] * (h * h * h)) : 0.f;
 #pragma unroll
             for (int p = 0; p < 3; p++)
 #pragma unroll
                 for (int q = 0; q < 3; q++)
                     AA[3 * p + q] = adj[3 * p] * adj[3 * q] + adj[3 * p + 1] * adj[3 * q + 1] + adj[3 * p + 2] * adj[3 * q + 2];
-            for (int k = u; k < 81; k += 64) {
-                const int i = k / 27, j = (k / 9) % 3, p = (k / 3) % 3, q = k % 3;
-                float w = mu * adj[3 * p + j] * adj[3 * q + i] + lambda * adj[3 * p + i] * adj[3 * q + j];
-                if (i == j) w += mu * AA[3 * p + q];
-                W[k] = w;
-            }
+        }
+        if (valid) {
 #pragma unroll
             for (int k = 0; k < 2; k++)
                 if (u + 64 * k < ETC_NXE)
@@ -619,17 +616,24 @@ __global__ void __launch_bounds__(128, ETC_CTAS_PER_SM) elasticity_apply_tf32x3_
         const bool has_next = en < nelements;
         if (has_next) fetch_meta(en);
         __syncthreads();
-        // 2. B_e = K_e (hi / lo) from its six distinct 8x8 blocks, and this thread's A row
+        // 2. B_e = K_e (hi / lo) from its six distinct 8x8 blocks (entry (a, b) of each by this
+        // thread, W_ij^pq = mu adj_pj adj_qi + lambda adj_pi adj_qj + delta_ij mu (adj adj^T)_pq
+        // in registers), and this thread's A row
         if (valid) {
-            for (int k = u; k < 6 * 64; k += 64) {
-                const int blk = k >> 6, a = (k >> 3) & 7, b = k & 7;
+            const int a = u >> 3, b = u & 7;
+#pragma unroll
+            for (int blk = 0; blk < 6; blk++) {
                 const int i = blk < 3 ? 0 : (blk < 5 ? 1 : 2);
                 const int j = blk < 3 ? blk : (blk < 5 ? blk - 2 : 2);  // (0,0) (0,1) (0,2) (1,1) (1,2) (2,2)
-                const float *Iab = &Is[(a * 8 + b) * 9];
-                const float *Wij = &W[(i * 3 + j) * 9];
                 float acc = 0.f;
 #pragma unroll
-                for (int pq = 0; pq < 9; pq++) acc += Iab[pq] * Wij[pq];
+                for (int p = 0; p < 3; p++)
+#pragma unroll
+                    for (int q = 0; q < 3; q++) {
+                        float w = mu * adj[3 * p + j] * adj[3 * q + i] + lambda * adj[3 * p + i] * adj[3 * q + j];
+                        if (i == j) w += mu * AA[3 * p + q];
+                        acc += Ir[3 * p + q] * w;
+                    }
                 acc *= inv_det;
                 const float hi = tc::tf32_round(acc), lo = acc - hi;
                 const int r1 = i * 8 + a, c1 = j * 8 + b;
