@@ -148,3 +148,38 @@ def test_learned_smoother_pipeline_small(cuda):
     for name in ("chebyshev3", "learned"):
         assert row[name]["rc"] == 0 and row[name]["true_rel_residual"] < 1e-10, row
     assert row["learned"]["iterations"] <= row["chebyshev3"]["iterations"] + 1, row
+
+
+def test_fallback_switch_recaptures_graph(cuda):
+    """Graph-replayed V-cycles with the learned smoother: switching it to its Chebyshev3
+    fallback must change what the replay runs (the graph is re-captured), so the switched
+    solver takes exactly the plain V(2,2) multigrid's iterations and reaches its solution."""
+    import torch
+
+    from sfem_gb300 import learned
+    from sfem_gb300 import solvers as S
+    from sfem_gb300.mesh import SSMesh
+
+    m = SSMesh(8, 8, 8, 4, perturb=0.1, seed=3)
+    H = S.Hierarchy(m, dirichlet_faces=("x0",), device=cuda)
+    g = torch.Generator(device=cuda).manual_seed(2)
+    b = torch.randn(H.spaces[0].n_nodes, dtype=torch.float64, device=cuda, generator=g)
+    b[H.dirichlet[0].long()] = 0
+    net = learned.PatchNet(cuda, seed=1)
+
+    def run(mg, op):
+        solver = S.cg(S.context(), op, mg, rtol=1e-10, max_it=200, residual_norm=True, flexible=True)
+        x = torch.zeros_like(b)
+        assert S.solve(solver, b, x) == 0
+        return S.stats(solver)[0], x
+
+    ctx = S.context()
+    mg_plain, op = S.build_poisson_mg(ctx, H, torch.float64, smoother="chebyshev3", sweeps=2, coarse="dense",
+                                      graph=True)
+    it_plain, x_plain = run(mg_plain, op)
+    mg, op2 = learned.learned_mg(ctx, H, net, torch.float64, chain="before", coarse="dense", graph=True)
+    it_learned, _ = run(mg, op2)  # captures the learned V-cycle
+    learned.use_fallback(mg, True)
+    it_fb, x_fb = run(mg, op2)
+    assert it_fb == it_plain, (it_plain, it_learned, it_fb)
+    assert float(torch.linalg.vector_norm(x_fb - x_plain) / torch.linalg.vector_norm(x_plain)) < 1e-8
