@@ -78,9 +78,10 @@ def test_adam_and_mse(cuda):
     assert torch.allclose(wb.float(), w, rtol=1e-2, atol=1e-2)
 
 
+@pytest.mark.parametrize("shape", [(5, 4, 3), (1, 1, 1), (3, 3, 3)], ids=["60patches", "1patch", "27patches"])
 @pytest.mark.parametrize("variant", [0, 1], ids=["tcgen05", "mma_sync"])
 @pytest.mark.parametrize("dtype_name", ["float32", "float64"])
-def test_fused_tensor_core_correction_matches_layer_kernels(cuda, dtype_name, variant):
+def test_fused_tensor_core_correction_matches_layer_kernels(cuda, dtype_name, variant, shape):
     """The fused tensor-core inference kernels (tcgen05 with tensor-memory accumulators, and
     warp-level mma.sync) against gather + three layer kernels + scatter (which the oracle
     pins): same network, same BF16 rounding points, FP32 accumulation in a different order,
@@ -92,7 +93,7 @@ def test_fused_tensor_core_correction_matches_layer_kernels(cuda, dtype_name, va
     from sfem_gb300.solvers import Hierarchy
 
     dt = getattr(torch, dtype_name)
-    m = SSMesh(5, 4, 3, 4, perturb=0.1, seed=1)
+    m = SSMesh(*shape, 4, perturb=0.1, seed=1)
     H = Hierarchy(m, dirichlet_faces=("x0",), device=cuda)
     fine = H.spaces[0]
     P, N = m.n_elements, m.n_nodes()
