@@ -28,7 +28,8 @@ struct GradTable {
                     for (int q = 0; q < 3; q++) I[a][b][p][q] = q1_grad_integral(a, b, p, q);
     }
 };
-static __constant__ GradTable kGrad = GradTable();
+// global (not __constant__): lanes read different entries, which the constant cache would serialise
+static __device__ GradTable kGrad = GradTable();
 
 // sshex8 lidx of the hex8 corner c at level 1 (used when a hex8 mesh is given in hex8 order)
 __host__ __device__ constexpr int hex8_corner_of_lidx1(int l) {
@@ -94,6 +95,50 @@ __device__ __forceinline__ void build_K_warp(const T adj[9], const T AA[9], T in
     __syncwarp();
 }
 
+// Same K from its six distinct 8x8 blocks (K_ji = K_ij^T): lane l owns the entries
+// (a, b) = (l / 8, l % 8) and (l / 8 + 4, l % 8) of every block, with their Q1
+// gradient integrals I_ab^pq held in registers (Ir, loaded once per kernel) and the 81
+// W values read from shared memory as warp-wide broadcasts.
+template <typename T>
+__device__ __forceinline__ void load_grad_regs(int lane, T (&Ir)[2][9]) {
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        const int l = lane + 32 * h;
+#pragma unroll
+        for (int pq = 0; pq < 9; pq++) Ir[h][pq] = (T)kGrad.I[l >> 3][l & 7][pq / 3][pq % 3];
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ void build_K_warp_sym(const T adj[9], const T AA[9], T inv_det, T mu, T lambda,
+                                                 const T (&Ir)[2][9], T *__restrict__ Wsm, T *__restrict__ K,
+                                                 int ld, int lane) {
+    for (int k = lane; k < 81; k += 32) {
+        const int i = k / 27, j = (k / 9) % 3, p = (k / 3) % 3, q = k % 3;
+        T w = mu * adj[3 * p + j] * adj[3 * q + i] + lambda * adj[3 * p + i] * adj[3 * q + j];
+        if (i == j) w += mu * AA[3 * p + q];
+        Wsm[k] = w;
+    }
+    __syncwarp();
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        const int l = lane + 32 * h, a = l >> 3, b = l & 7;
+#pragma unroll
+        for (int blk = 0; blk < 6; blk++) {
+            const int i = blk < 3 ? 0 : (blk < 5 ? 1 : 2);
+            const int j = blk < 3 ? blk : (blk < 5 ? blk - 2 : 2);  // (0,0) (0,1) (0,2) (1,1) (1,2) (2,2)
+            const T *Wij = &Wsm[(i * 3 + j) * 9];
+            T acc = 0;
+#pragma unroll
+            for (int pq = 0; pq < 9; pq++) acc += Ir[h][pq] * Wij[pq];
+            acc *= inv_det;
+            K[(i * 8 + a) * ld + j * 8 + b] = acc;
+            if (i != j) K[(j * 8 + b) * ld + i * 8 + a] = acc;
+        }
+    }
+    __syncwarp();
+}
+
 template <typename T>
 __device__ __forceinline__ void load_grad_table(T *Is) {
     for (int k = threadIdx.x; k < 576; k += blockDim.x) Is[k] = (T)(&kGrad.I[0][0][0][0])[k];
@@ -117,17 +162,17 @@ __global__ void __launch_bounds__(64) elasticity_apply_warp_kernel(ptrdiff_t nel
     __shared__ T Ks[WPB][576];
     __shared__ T xs[WPB][3 * NXE];
     __shared__ T ys[WPB][3 * NXE];
-    __shared__ T Is[576];
     __shared__ T Ws[WPB][81];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     T *K = Ks[warp];
     T *xw = xs[warp];
     T *yw = ys[warp];
-    load_grad_table<T>(Is);
+    T Ir[2][9];
+    load_grad_regs<T>(lane, Ir);
     for (ptrdiff_t e = (ptrdiff_t)blockIdx.x * WPB + warp; e < nelements; e += (ptrdiff_t)gridDim.x * WPB) {
         T adj[9], AA[9], inv_det;
         load_sub_adjugate<T>(adjugate, determinant, stride, e, L, adj, AA, inv_det);
-        build_K_warp<T>(adj, AA, inv_det, mu, lambda, Is, Ws[warp], K, 24, lane);
+        build_K_warp_sym<T>(adj, AA, inv_det, mu, lambda, Ir, Ws[warp], K, 24, lane);
         idx_t gi[NR];
 #pragma unroll
         for (int r = 0; r < NR; r++) {
