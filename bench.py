@@ -62,6 +62,9 @@ def parse():
     ap.add_argument("--profile-kernels", action="store_true",
                     help="launch each main kernel twice on the bench workloads and exit (an ncu target)")
     ap.add_argument("--batch-problems", type=int, default=256)
+    ap.add_argument("--profile-zoo", action="store_true",
+                    help="launch every vector, SpMV and coarse-level kernel twice on inputs larger than L2: "
+                         "the target of the per-kernel roofline table in profiles/")
     ap.add_argument("--profile-solves", action="store_true",
                     help="run one mixed + learned Poisson solve (32^3 L=4, k = exp(g)) and one mixed elasticity "
                          "solve (64x16x16 L=4): the target of the solver launch-list captures in profiles/")
@@ -664,6 +667,109 @@ def profile_kernels():
     print("profile kernels: done")
 
 
+def profile_zoo():
+    """Two launches of each remaining kernel family on inputs larger than the 126 MB L2:
+    the BLAS / CG / Chebyshev / precision-bridge vector kernels on 40M-entry vectors,
+    the Dirichlet copy, the symmetric CRS and 3x3 BSR SpMV and the matrix-free hex8
+    Laplacian on a 96^3 hex8 mesh (912,673 nodes), the L=2 thread-per-element and
+    L=3 staged float sshex8 kernels on 96^3 / 64^3 macro meshes, and the dense
+    coarse-level mat-vec (1536 unknowns)."""
+    import ctypes
+
+    import torch
+
+    from sfem_gb300 import capi
+    from sfem_gb300 import solvers as S
+    from sfem_gb300.mesh import SSMesh, upper_crs_graph
+    from sfem_gb300.operators import Laplacian, SSMeshDevice
+
+    dev = torch.device("cuda:0")
+    lib = capi.load()
+    D = ctypes.c_double
+    ws = torch.zeros(lib.sfem_gb300_reduce_workspace_size(), dtype=torch.uint8, device=dev)
+    sc = torch.ones(8, dtype=torch.float64, device=dev)
+    n = 40_000_000
+    for dt, rt in ((torch.float64, capi.FLOAT64), (torch.float32, capi.FLOAT32)):
+        x, y, z, w = (torch.rand(n, dtype=dt, device=dev) + 0.5 for _ in range(4))
+        for _ in range(2):
+            capi.check(lib.sfem_gb300_dot(rt, capi.i64(n), capi.vp(x), capi.vp(y), capi.vp(ws), capi.vp(sc), None), "dot")
+            capi.check(lib.sfem_gb300_axpby(rt, capi.i64(n), D(0.5), capi.vp(x), D(0.5), capi.vp(y), None), "axpby")
+            capi.check(lib.sfem_gb300_zaxpby(rt, capi.i64(n), D(0.5), capi.vp(x), D(0.5), capi.vp(y), capi.vp(z), None),
+                       "zaxpby")
+            capi.check(lib.sfem_gb300_xypaz(rt, capi.i64(n), capi.vp(x), capi.vp(y), D(0.5), capi.vp(z), None), "xypaz")
+            capi.check(lib.sfem_gb300_cg_update_x_r(rt, capi.i64(n), capi.vp(sc), capi.c_void(sc.data_ptr() + 8),
+                                                     capi.vp(x), capi.vp(y), capi.vp(z), capi.vp(w), capi.vp(ws),
+                                                     capi.c_void(sc.data_ptr() + 16), None), "cg_update_x_r")
+            capi.check(lib.sfem_gb300_cg_update_p(rt, capi.i64(n), capi.vp(sc), capi.c_void(sc.data_ptr() + 8), None,
+                                                   capi.vp(x), capi.vp(y), None), "cg_update_p")
+            capi.check(lib.sfem_gb300_chebyshev_update(rt, capi.i64(n), D(0.1), D(0.5), capi.vp(w), capi.vp(x),
+                                                        capi.vp(y), capi.vp(z), capi.vp(w), None), "chebyshev_update")
+        del x, y, z, w
+    x64 = torch.rand(n, dtype=torch.float64, device=dev)
+    y32 = torch.rand(n, dtype=torch.float32, device=dev)
+    nodes = torch.randperm(n // 4, device=dev)[: n // 40].to(torch.int32).sort().values
+    for _ in range(2):
+        capi.check(lib.sfem_gb300_scaled_to_f32(capi.i64(n), capi.vp(sc), capi.vp(x64), capi.vp(y32), None), "to_f32")
+        capi.check(lib.sfem_gb300_scaled_axpy_f32_to_f64(capi.i64(n), capi.vp(sc), capi.vp(y32), capi.vp(x64), None),
+                   "axpy_f32_to_f64")
+        capi.check(lib.sfem_gb300_constraint_nodes_copy(capi.FLOAT64, capi.i64(nodes.numel()), capi.vp(nodes), 4, 0,
+                                                         capi.vp(x64), capi.c_void(x64.data_ptr()), None),
+                   "constraint copy")
+    del x64, y32
+    # hex8 Laplacian on 96^3 elements: matrix-free apply, CRS assembly, symmetric CRS and BSR SpMV
+    m = SSMesh(96, 96, 96, 1, perturb=0.1)
+    sp = SSMeshDevice(m, 1, device=dev)
+    lap = Laplacian(sp).initialize()
+    N = m.n_nodes(1)
+    rowptr, colidx = upper_crs_graph(m.hex8_elements(), N)
+    rp = torch.from_numpy(rowptr).to(dev)
+    ci = torch.from_numpy(colidx).to(dev)
+    nnz = int(colidx.size)
+    for dt, rt in ((torch.float64, capi.FLOAT64), (torch.float32, capi.FLOAT32)):
+        xv = torch.rand(N, dtype=dt, device=dev)
+        yv = torch.zeros_like(xv)
+        diag = torch.zeros(N, dtype=dt, device=dev)
+        off = torch.zeros(nnz, dtype=dt, device=dev)
+        capi.check(lib.sfem_gb300_hex8_laplacian_crs_sym(capi.i64(m.n_elements), sp.elements_ptrs.ptr, capi.i64(m.n_elements),
+                                                          capi.vp(lap.fff), capi.vp(rp), capi.vp(ci), rt, capi.vp(diag),
+                                                          capi.vp(off), None), "crs assembly")
+        for _ in range(2):
+            lap.apply(xv, yv)
+            capi.check(lib.sfem_gb300_crs_sym_spmv(rt, capi.i64(N), capi.vp(rp), capi.vp(ci), capi.vp(diag), capi.vp(off),
+                                                    D(0.0), capi.vp(xv), capi.vp(yv), None), "crs spmv")
+        del xv, yv, diag, off
+    bx = torch.rand(3 * N, dtype=torch.float64, device=dev)
+    by = torch.zeros_like(bx)
+    bd = torch.rand(6 * N, dtype=torch.float64, device=dev)
+    bo = torch.rand(9 * nnz, dtype=torch.float64, device=dev) * 1e-3
+    for _ in range(2):
+        capi.check(lib.sfem_gb300_bsr_sym_spmv(capi.FLOAT64, 3, capi.i64(N), capi.vp(rp), capi.vp(ci), capi.vp(bd),
+                                                capi.vp(bo), 0, D(0.0), capi.vp(bx), capi.vp(by), None), "bsr spmv")
+    del bx, by, bd, bo, lap, sp
+    # float sshex8 kernels of the coarser levels: L=2 (thread per element) and L=3 (staged tile)
+    for L, nx in ((2, 96), (3, 64)):
+        ms = SSMesh(nx, nx, nx, L, perturb=0.1)
+        sps = SSMeshDevice(ms, L, device=dev)
+        ops = Laplacian(sps).initialize()
+        xs = torch.rand(ms.n_nodes(L), dtype=torch.float32, device=dev)
+        ys = torch.zeros_like(xs)
+        for _ in range(2):
+            ops.apply(xs, ys)
+        del ops, sps, xs, ys
+    # dense coarse-level solve (1536 unknowns): a hex8 Poisson level of 15 x 15 x 5 elements
+    mc = SSMesh(15, 15, 5, 1)
+    Hc = S.Hierarchy(mc, dirichlet_faces=("x0",), device=dev, coarsen_macro=False)
+    ctx = S.context()
+    opc = S.laplacian_op(ctx, Hc.spaces[0], Hc.fff, Hc.dirichlet[0], torch.float32)
+    dsol = S.dense_solver(ctx, opc)
+    bc = torch.rand(Hc.spaces[0].n_nodes, dtype=torch.float32, device=dev)
+    xc = torch.zeros_like(bc)
+    for _ in range(2):
+        S.apply(dsol, bc, xc)
+    torch.cuda.synchronize()
+    print("profile zoo: done")
+
+
 def profile_solves():
     """One FP64 flexible-CG solve preconditioned by the FP32 multigrid with the learned
     correction (32^3 L=4, k = exp(g), untrained network, 12 iterations) and one
@@ -714,6 +820,9 @@ def main():
         return
     if args.profile_solves:
         profile_solves()
+        return
+    if args.profile_zoo:
+        profile_zoo()
         return
     if args.impl == "reference":
         run_reference(args)
