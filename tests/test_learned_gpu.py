@@ -78,10 +78,11 @@ def test_adam_and_mse(cuda):
     assert torch.allclose(wb.float(), w, rtol=1e-2, atol=1e-2)
 
 
+@pytest.mark.parametrize("scaled", [True, False], ids=["inv_diag", "no_inv_diag"])
 @pytest.mark.parametrize("shape", [(5, 4, 3), (1, 1, 1), (3, 3, 3)], ids=["60patches", "1patch", "27patches"])
 @pytest.mark.parametrize("variant", [0, 1], ids=["tcgen05", "mma_sync"])
 @pytest.mark.parametrize("dtype_name", ["float32", "float64"])
-def test_fused_tensor_core_correction_matches_layer_kernels(cuda, dtype_name, variant, shape):
+def test_fused_tensor_core_correction_matches_layer_kernels(cuda, dtype_name, variant, shape, scaled):
     """The fused tensor-core inference kernels (tcgen05 with tensor-memory accumulators, and
     warp-level mma.sync) against gather + three layer kernels + scatter (which the oracle
     pins): same network, same BF16 rounding points, FP32 accumulation in a different order,
@@ -103,7 +104,7 @@ def test_fused_tensor_core_correction_matches_layer_kernels(cuda, dtype_name, va
     net.wbf = [w.to(torch.bfloat16) for w in net.w32]
     g = torch.Generator(device=cuda).manual_seed(5)
     r = torch.randn(N, dtype=dt, device=cuda, generator=g)
-    inv = torch.rand(N, dtype=dt, device=cuda, generator=g) + 0.5
+    inv = (torch.rand(N, dtype=dt, device=cuda, generator=g) + 0.5) if scaled else None
     lib = capi.load()
     frag = torch.empty(lib.sfem_gb300_learned_fragments_size(), dtype=torch.uint8, device=cuda)
     capi.check(lib.sfem_gb300_learned_fragments(capi.vp(net.wbf[0]), capi.vp(net.wbf[1]), capi.vp(net.wbf[2]),
