@@ -487,7 +487,7 @@ __device__ __forceinline__ void lap_layer_f32x2(const float *__restrict__ xbase,
 }
 
 template <int L, int TILE, int NQ = 2>
-__global__ void __launch_bounds__(NQ * TILE, NQ == 2 ? 6 : 4) sshex8_laplacian_apply_async_kernel(
+__global__ void __launch_bounds__(NQ * TILE, NQ == 2 ? (TILE == 32 ? 6 : 3) : 4) sshex8_laplacian_apply_async_kernel(
         ptrdiff_t nelements, const idx_t *const *elements, ptrdiff_t fff_stride, const float *fff,
         const float *__restrict__ x, float *__restrict__ y) {
     static_assert(L % NQ == 0, "NQ threads per element split the micro layers evenly");
@@ -784,7 +784,8 @@ __global__ void __launch_bounds__(128) sshex8_laplacian_diag_kernel(ptrdiff_t ne
 // "warp" (1) = warp per element; "thread" (2) = registers-only thread per element;
 // "async" (3) = cp.async staged tile, two threads per element, packed FP32x2 FMAs (even L);
 // "pipe" (4) = persistent CTAs, cp.async pipeline across tiles, one warp per micro layer (even L);
-// 6 = the async tile with four threads per element (one micro layer each, L = 4).
+// 6 = the async tile with four threads per element (one micro layer each, L = 4);
+// 7 = the async tile of 64 elements (128 threads per CTA, L = 4).
 static int g_laplacian_variant = -1;
 static int g_laplacian_variant_forced = 0;  // set by sfem_gb300_set_laplacian_kernel
 static int laplacian_variant() {
@@ -857,6 +858,13 @@ static int laplacian_apply_tpl(int element_type, ptrdiff_t nelements, idx_t **el
         else
             launch(sshex8_laplacian_apply_pipe_kernel<4, TILE>, 4);
         return check_launch("cu_laplacian_apply(SSHEX8, pipelined tile)");
+    }
+    if (sizeof(T) == 4 && L == 4 && variant == 7) {
+        constexpr int TILE = 64;
+        const int tb = (int)((nelements + TILE - 1) / TILE);
+        sshex8_laplacian_apply_async_kernel<4, TILE, 2><<<tb, 2 * TILE, 0, s>>>(nelements, elements, fff_stride, fff,
+                                                                                (const float *)x, (float *)y);
+        return check_launch("cu_laplacian_apply(SSHEX8, async tile of 64 elements)");
     }
     if (sizeof(T) == 4 && L == 4 && variant == 6) {
         constexpr int TILE = 32;
@@ -990,8 +998,8 @@ extern "C" int cu_laplacian_diag(int element_type, ptrdiff_t nelements, idx_t **
 }
 
 extern "C" int sfem_gb300_set_laplacian_kernel(int variant) {
-    if (variant < -1 || variant > 6 || variant == 5)
-        return set_error("sfem_gb300_set_laplacian_kernel: variant must be -1..4 or 6");
+    if (variant < -1 || variant > 7 || variant == 5)
+        return set_error("sfem_gb300_set_laplacian_kernel: variant must be -1..4, 6 or 7");
     const int cur = laplacian_variant();
     const int prev = __atomic_load_n(&g_laplacian_variant_forced, __ATOMIC_RELAXED) ? cur : -1;
     __atomic_store_n(&g_laplacian_variant, variant < 0 ? 0 : variant, __ATOMIC_RELAXED);

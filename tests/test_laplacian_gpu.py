@@ -69,7 +69,7 @@ def test_sshex8_laplacian_apply_fp32(cuda, L):
     assert err.max() < RTOL32, err.max()
 
 
-@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 6])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 6, 7])
 @pytest.mark.parametrize("L", [2, 3, 4])
 @pytest.mark.parametrize("aligned", [True, False])
 def test_sshex8_laplacian_fp32_kernels(cuda, variant, L, aligned):
