@@ -54,6 +54,28 @@ def test_elasticity_apply_fp64(cuda, L):
     assert err.max() < 1e-13, err.max()
 
 
+@pytest.mark.parametrize("L", [1, 2, 3])
+def test_elasticity_apply_fp32_coarse_levels(cuda, L):
+    """The float apply of the hex8 and L = 2, 3 levels (SIMT kernel) against the oracle."""
+    import torch
+
+    m, sp, el, adj, det, adj_d, det_d = _setup(cuda, L)
+    n = m.n_nodes(L)
+    rng = np.random.default_rng(10 + L)
+    u = rng.standard_normal(3 * n)
+    ref = O.linear_elasticity_apply(L if L > 1 else 0, el, adj, det, MU, LAM, u)
+    yd = torch.zeros(3 * n, dtype=torch.float32, device=cuda)
+    ud = torch.from_numpy(u).float().to(cuda)
+    capi.check(capi.load().sfem_gb300_linear_elasticity_apply(sp.element_type, capi.i64(m.n_elements),
+                                                              sp.elements_ptrs.ptr, capi.i64(m.n_elements),
+                                                              capi.vp(adj_d), capi.vp(det_d), ctypes_d(MU),
+                                                              ctypes_d(LAM), capi.FLOAT32,
+                                                              capi.vp(ud), capi.vp(yd), None),
+               "elasticity apply")
+    err = np.abs(yd.double().cpu().numpy() - ref) / _scale(L, el, adj, det, u)
+    assert err.max() < 2e-5, err.max()
+
+
 def ctypes_d(v):
     import ctypes
 

@@ -51,11 +51,12 @@ def test_sshex8_laplacian_apply_fp64(cuda, L, n):
     assert err.max() < RTOL64, err.max()
 
 
-@pytest.mark.parametrize("L", [2, 4])
-def test_sshex8_laplacian_apply_fp32(cuda, L):
+@pytest.mark.parametrize("L,n", [(2, (3, 2, 2)), (3, (3, 2, 2)), (4, (3, 2, 2)), (6, (2, 2, 1)), (8, (1, 2, 2))])
+def test_sshex8_laplacian_apply_fp32(cuda, L, n):
+    """The float apply with the default kernel of each level (L = 6, 8: warp kernel)."""
     import torch
 
-    m = SSMesh(3, 2, 2, L, perturb=0.1, seed=1)
+    m = SSMesh(*n, L, perturb=0.1, seed=1)
     sp = SSMeshDevice(m, L)
     el = m.elements(L)
     fff_aos = O.fff_fill(el[m.macro_corner_lidx(L)], m.points)
