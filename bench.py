@@ -689,8 +689,9 @@ def profile_zoo():
     the BLAS / CG / Chebyshev / precision-bridge vector kernels on 40M-entry vectors,
     the Dirichlet copy, the symmetric CRS and 3x3 BSR SpMV and the matrix-free hex8
     Laplacian on a 96^3 hex8 mesh (912,673 nodes), the L=2 thread-per-element and
-    L=3 staged float sshex8 kernels on 96^3 / 64^3 macro meshes, and the dense
-    coarse-level mat-vec (1536 unknowns)."""
+    L=3 staged float sshex8 kernels on 96^3 / 64^3 macro meshes, the elasticity applies
+    of the L=2 and hex8 levels of the 64x16x16 cantilever, and the dense coarse-level
+    mat-vec (1536 unknowns)."""
     import ctypes
 
     import torch
@@ -773,6 +774,19 @@ def profile_zoo():
         for _ in range(2):
             ops.apply(xs, ys)
         del ops, sps, xs, ys
+    # elasticity on the levels of the 64x16x16 cantilever hierarchy below L=4: L=2 and the hex8
+    # macro mesh (SIMT kernels, FP32 and FP64; compute bound)
+    for L in (2, 1):
+        me = SSMesh(64, 16, 16, L, box=((0, 4), (0, 1), (0, 1)))
+        He = S.Hierarchy(me, dirichlet_faces=("x0",), device=dev, vec=3, coarsen_macro=False)
+        ctx_e = S.context()
+        for dt in (torch.float32, torch.float64):
+            ope = S.elasticity_op(ctx_e, He.spaces[0], He.adj, He.det, 1.0, 10.0, He.dirichlet[0], dt)
+            u = torch.rand(3 * me.n_nodes(L), dtype=dt, device=dev)
+            v = torch.zeros_like(u)
+            for _ in range(2):
+                S.apply(ope, u, v)
+        del He
     # dense coarse-level solve (1536 unknowns): a hex8 Poisson level of 15 x 15 x 5 elements
     mc = SSMesh(15, 15, 5, 1)
     Hc = S.Hierarchy(mc, dirichlet_faces=("x0",), device=dev, coarsen_macro=False)
