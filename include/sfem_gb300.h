@@ -100,6 +100,16 @@ int sfem_gb300_linear_elasticity_apply(int element_type, ptrdiff_t nelements, sf
                                        double mu, double lambda, int real_type, const void *u, void *out,
                                        void *stream);
 
+/* Stored element matrices (no reference counterpart; the reference rebuilds them per apply):
+ * K[e] (24 x 24 row-major, row/column = component * 8 + corner, real_type) of every macro
+ * element from the level's sub-adjugate, and out += K u with them.  Used on coarse levels
+ * (hex8, L <= 2), where building the matrix costs more than applying it. */
+int sfem_gb300_linear_elasticity_element_matrices(int element_type, ptrdiff_t nelements, ptrdiff_t jacobian_stride,
+                                                  const float *adjugate, const float *determinant, double mu,
+                                                  double lambda, int real_type, void *K, void *stream);
+int sfem_gb300_linear_elasticity_apply_em(int element_type, ptrdiff_t nelements, sfem_gb300_idx_t **elements,
+                                          const void *K, int real_type, const void *u, void *out, void *stream);
+
 /* FP32 sshex8 kernel choice (no reference counterpart): -1 default, 0 the SIMT warp
  * kernel, 1 the tcgen05 kernel (L = 4: element-matrix contraction on the tensor cores in
  * 3xTF32, FP32-level accuracy; the default at L = 4).  sfem_gb300_elasticity_status
@@ -341,7 +351,9 @@ int sfem_gb300_laplacian_op_create(void *context, int real_type, int element_typ
                                    sfem_gb300_idx_t **elements, ptrdiff_t fff_stride, const float *fff,
                                    ptrdiff_t n_nodes, ptrdiff_t n_dirichlet, const int32_t *dirichlet_nodes,
                                    void **op);
-/* Function-level linear elasticity (3 dofs/node, all components fixed on Dirichlet nodes). */
+/* Function-level linear elasticity (3 dofs/node, all components fixed on Dirichlet nodes).
+ * On hex8 and L <= 2 levels the element matrices are built once here, from the geometry
+ * as it is at creation, and applied from memory (sfem_gb300_linear_elasticity_apply_em). */
 int sfem_gb300_elasticity_op_create(void *context, int real_type, int element_type, ptrdiff_t nelements,
                                     sfem_gb300_idx_t **elements, ptrdiff_t jacobian_stride, const float *adjugate,
                                     const float *determinant, double mu, double lambda, ptrdiff_t n_nodes,

@@ -149,11 +149,33 @@ __device__ __forceinline__ void load_grad_table(T *Is) {
 // memory, stages the (L+1)^3 x 3 micro-grid values, lanes apply K per micro
 // element with shared-memory accumulation, then scatter (owned interior nodes
 // plain, shared surface nodes atomic).  HEX8 = plain hex8 mesh in hex8 corner order.
-template <typename T, int L, bool HEX8>
+// Element matrices of every macro element of a level (sub-adjugate at level L), stored
+// row-major [e][(i, a)][(j, b)]: one warp per element.
+template <typename T>
+__global__ void __launch_bounds__(64) elasticity_element_matrices_kernel(ptrdiff_t nelements, int L, ptrdiff_t stride,
+                                                                         const float *adjugate,
+                                                                         const float *determinant, T mu, T lambda,
+                                                                         T *__restrict__ Kout) {
+    __shared__ T Ws[2][81];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    T Ir[2][9];
+    load_grad_regs<T>(lane, Ir);
+    for (ptrdiff_t e = (ptrdiff_t)blockIdx.x * 2 + warp; e < nelements; e += (ptrdiff_t)gridDim.x * 2) {
+        T adj[9], AA[9], inv_det;
+        load_sub_adjugate<T>(adjugate, determinant, stride, e, L, adj, AA, inv_det);
+        build_K_warp_sym<T>(adj, AA, inv_det, mu, lambda, Ir, Ws[warp], Kout + 576 * e, 24, lane);
+    }
+}
+
+// STORED: the element matrices come from Kg (elasticity_element_matrices_kernel) instead
+// of being built from the sub-adjugate (used on coarse levels, where building a 24x24
+// matrix costs more than applying it to the 8 or 1 micro elements).
+template <typename T, int L, bool HEX8, bool STORED = false>
 __global__ void __launch_bounds__(64) elasticity_apply_warp_kernel(ptrdiff_t nelements, const idx_t *const *elements,
                                                                    ptrdiff_t stride, const float *adjugate,
                                                                    const float *determinant, T mu, T lambda,
-                                                                   const T *__restrict__ x, T *__restrict__ y) {
+                                                                   const T *__restrict__ x, T *__restrict__ y,
+                                                                   const T *__restrict__ Kg = nullptr) {
     constexpr int N1 = L + 1;
     constexpr int NXE = N1 * N1 * N1;
     constexpr int NM = L * L * L;
@@ -168,11 +190,17 @@ __global__ void __launch_bounds__(64) elasticity_apply_warp_kernel(ptrdiff_t nel
     T *xw = xs[warp];
     T *yw = ys[warp];
     T Ir[2][9];
-    load_grad_regs<T>(lane, Ir);
+    if constexpr (!STORED) load_grad_regs<T>(lane, Ir);
     for (ptrdiff_t e = (ptrdiff_t)blockIdx.x * WPB + warp; e < nelements; e += (ptrdiff_t)gridDim.x * WPB) {
-        T adj[9], AA[9], inv_det;
-        load_sub_adjugate<T>(adjugate, determinant, stride, e, L, adj, AA, inv_det);
-        build_K_warp_sym<T>(adj, AA, inv_det, mu, lambda, Ir, Ws[warp], K, 24, lane);
+        if constexpr (STORED) {
+            const T *src = Kg + 576 * e;
+            for (int k = lane; k < 576; k += 32) K[k] = src[k];
+            __syncwarp();
+        } else {
+            T adj[9], AA[9], inv_det;
+            load_sub_adjugate<T>(adjugate, determinant, stride, e, L, adj, AA, inv_det);
+            build_K_warp_sym<T>(adj, AA, inv_det, mu, lambda, Ir, Ws[warp], K, 24, lane);
+        }
         idx_t gi[NR];
 #pragma unroll
         for (int r = 0; r < NR; r++) {
@@ -885,6 +913,68 @@ extern "C" int sfem_gb300_linear_elasticity_apply(int element_type, ptrdiff_t ne
         return elasticity_apply_tpl<double>(element_type, nelements, elements, jacobian_stride, adjugate, determinant,
                                             mu, lambda, (const double *)u, (double *)out, s);
     return set_error("sfem_gb300_linear_elasticity_apply: unsupported real type %d", real_type);
+}
+
+template <typename T>
+static int elasticity_apply_em_tpl(int element_type, ptrdiff_t nelements, idx_t **elements, const T *K, const T *x,
+                                   T *y, cudaStream_t s) {
+    if (nelements <= 0) return SFEM_GB300_SUCCESS;
+    const int blocks = grid_for((nelements + 1) / 2, 1, kNumSMs * 64);
+    if (element_type == SFEM_GB300_HEX8) {
+        elasticity_apply_warp_kernel<T, 1, true, true><<<blocks, 64, 0, s>>>(nelements, elements, 0, nullptr, nullptr,
+                                                                             T(0), T(0), x, y, K);
+        return check_launch("sfem_gb300_linear_elasticity_apply_em(HEX8)");
+    }
+    const int L = element_type - SFEM_GB300_SSHEX8_BASE;
+#define SFEM_EL_EM_CASE(LL)                                                                                      \
+    case LL:                                                                                                     \
+        elasticity_apply_warp_kernel<T, LL, false, true><<<blocks, 64, 0, s>>>(nelements, elements, 0, nullptr, \
+                                                                               nullptr, T(0), T(0), x, y, K);   \
+        return check_launch("sfem_gb300_linear_elasticity_apply_em(SSHEX8)");
+    switch (L) {
+        SFEM_EL_EM_CASE(1)
+        SFEM_EL_EM_CASE(2)
+        SFEM_EL_EM_CASE(3)
+        SFEM_EL_EM_CASE(4)
+        default:
+            return set_error("sfem_gb300_linear_elasticity_apply_em: unsupported element type %d", element_type);
+    }
+#undef SFEM_EL_EM_CASE
+}
+
+extern "C" int sfem_gb300_linear_elasticity_element_matrices(int element_type, ptrdiff_t nelements,
+                                                             ptrdiff_t jacobian_stride, const float *adjugate,
+                                                             const float *determinant, double mu, double lambda,
+                                                             int real_type, void *K, void *stream) {
+    if (nelements <= 0) return SFEM_GB300_SUCCESS;
+    const int L = element_type == SFEM_GB300_HEX8 ? 1 : element_type - SFEM_GB300_SSHEX8_BASE;
+    if (L < 1 || L > 16)
+        return set_error("sfem_gb300_linear_elasticity_element_matrices: unsupported element type %d", element_type);
+    const cudaStream_t s = stream_of(stream);
+    const int blocks = grid_for((nelements + 1) / 2, 1, kNumSMs * 64);
+    if (real_type == SFEM_GB300_FLOAT32)
+        elasticity_element_matrices_kernel<float><<<blocks, 64, 0, s>>>(nelements, L, jacobian_stride, adjugate,
+                                                                        determinant, (float)mu, (float)lambda,
+                                                                        (float *)K);
+    else if (real_type == SFEM_GB300_FLOAT64 || real_type == SFEM_GB300_REAL_DEFAULT)
+        elasticity_element_matrices_kernel<double><<<blocks, 64, 0, s>>>(nelements, L, jacobian_stride, adjugate,
+                                                                         determinant, mu, lambda, (double *)K);
+    else
+        return set_error("sfem_gb300_linear_elasticity_element_matrices: unsupported real type %d", real_type);
+    return check_launch("sfem_gb300_linear_elasticity_element_matrices");
+}
+
+extern "C" int sfem_gb300_linear_elasticity_apply_em(int element_type, ptrdiff_t nelements, idx_t **elements,
+                                                     const void *K, int real_type, const void *u, void *out,
+                                                     void *stream) {
+    const cudaStream_t s = stream_of(stream);
+    if (real_type == SFEM_GB300_FLOAT32)
+        return elasticity_apply_em_tpl<float>(element_type, nelements, elements, (const float *)K, (const float *)u,
+                                              (float *)out, s);
+    if (real_type == SFEM_GB300_FLOAT64 || real_type == SFEM_GB300_REAL_DEFAULT)
+        return elasticity_apply_em_tpl<double>(element_type, nelements, elements, (const double *)K,
+                                               (const double *)u, (double *)out, s);
+    return set_error("sfem_gb300_linear_elasticity_apply_em: unsupported real type %d", real_type);
 }
 
 extern "C" int sfem_gb300_set_elasticity_kernel(int variant) {

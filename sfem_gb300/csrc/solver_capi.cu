@@ -50,9 +50,29 @@ public:
     double mu{1}, lambda{1};
     const idx_t *dirichlet{nullptr};
     int contraction{real_type_v<T>};  // FLOAT32_BF16TC: tensor-core BF16 element contraction
+    DeviceBuffer<T> em;                // stored element matrices (coarse levels), built by prepare()
+    bool stored() const {
+        const bool coarse = element_type == SFEM_GB300_HEX8 ||
+                            (element_type >= SFEM_GB300_SSHEX8(1) && element_type <= SFEM_GB300_SSHEX8(2));
+        return coarse && contraction == real_type_v<T>;
+    }
+    // called at creation and whenever the geometry or the contraction changes (outside any capture)
+    int prepare() {
+        if (!stored()) return 0;
+        SFEM_GB300_CHECK(em.resize(576 * nelements));
+        return sfem_gb300_linear_elasticity_element_matrices(element_type, nelements, jac_stride, adjugate,
+                                                             determinant, mu, lambda, real_type_v<T>, em.ptr,
+                                                             ctx->sp());
+    }
     int apply(const T *x, T *y) override {
-        SFEM_GB300_CHECK(sfem_gb300_linear_elasticity_apply(element_type, nelements, elements, jac_stride, adjugate,
-                                                            determinant, mu, lambda, contraction, x, y, ctx->sp()));
+        if (stored() && em.n == 576 * nelements) {
+            SFEM_GB300_CHECK(sfem_gb300_linear_elasticity_apply_em(element_type, nelements, elements, em.ptr,
+                                                                   real_type_v<T>, x, y, ctx->sp()));
+        } else {
+            SFEM_GB300_CHECK(sfem_gb300_linear_elasticity_apply(element_type, nelements, elements, jac_stride,
+                                                                adjugate, determinant, mu, lambda, contraction, x, y,
+                                                                ctx->sp()));
+        }
         for (int c = 0; c < 3; c++)
             SFEM_GB300_CHECK(
                     sfem_gb300_constraint_nodes_copy(real_type_v<T>, n_dirichlet, dirichlet, 3, c, x, y, ctx->sp()));
@@ -293,15 +313,22 @@ int sfem_gb300_elasticity_op_create(void *context, int real_type, int element_ty
         op->n_dirichlet = n_dirichlet;
         op->dirichlet = dirichlet_nodes;
     };
+    int rc = 0;
     if (is_f32(real_type)) {
         auto op = std::make_shared<ElasticityOp<float>>();
         fill(op);
         if (real_type == SFEM_GB300_FLOAT32_BF16TC) op->contraction = SFEM_GB300_FLOAT32_BF16TC;
+        rc = op->prepare();
         h->f = op;
     } else {
         auto op = std::make_shared<ElasticityOp<double>>();
         fill(op);
+        rc = op->prepare();
         h->d = op;
+    }
+    if (rc) {
+        delete h;
+        return rc;
     }
     *out = h;
     return SFEM_GB300_SUCCESS;

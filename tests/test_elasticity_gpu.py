@@ -76,6 +76,38 @@ def test_elasticity_apply_fp32_coarse_levels(cuda, L):
     assert err.max() < 2e-5, err.max()
 
 
+@pytest.mark.parametrize("dtype_name,tol", [("float64", 1e-13), ("float32", 2e-5)])
+@pytest.mark.parametrize("L", [1, 2, 3, 4])
+def test_elasticity_stored_element_matrices(cuda, L, dtype_name, tol):
+    """Element matrices stored once (coarse-level path) then applied: same operator as the
+    oracle's, FP64 to 1e-13 and FP32 to 2e-5 of the row scale."""
+    import torch
+
+    m, sp, el, adj, det, adj_d, det_d = _setup(cuda, L, seed=5)
+    n = m.n_nodes(L)
+    dt = getattr(torch, dtype_name)
+    rt = capi.FLOAT64 if dtype_name == "float64" else capi.FLOAT32
+    rng = np.random.default_rng(20 + L)
+    u = rng.standard_normal(3 * n)
+    y0 = rng.standard_normal(3 * n)
+    ref = O.linear_elasticity_apply(L if L > 1 else 0, el, adj, det, MU, LAM, u, out=y0.copy())
+    lib = capi.load()
+    E = m.n_elements
+    K = torch.empty(576 * E, dtype=dt, device=cuda)
+    capi.check(lib.sfem_gb300_linear_elasticity_element_matrices(sp.element_type, capi.i64(E), capi.i64(E),
+                                                                  capi.vp(adj_d), capi.vp(det_d), ctypes_d(MU),
+                                                                  ctypes_d(LAM), rt, capi.vp(K), None), "matrices")
+    yd = torch.from_numpy(y0).to(dt).to(cuda)
+    ud = torch.from_numpy(u).to(dt).to(cuda)
+    capi.check(lib.sfem_gb300_linear_elasticity_apply_em(sp.element_type, capi.i64(E), sp.elements_ptrs.ptr,
+                                                         capi.vp(K), rt, capi.vp(ud), capi.vp(yd), None), "apply_em")
+    err = np.abs(yd.double().cpu().numpy() - ref) / (_scale(L, el, adj, det, u) + np.abs(y0))
+    assert err.max() < tol, err.max()
+    # the stored matrices are symmetric (built from the six distinct blocks)
+    Kh = K.double().cpu().numpy().reshape(E, 24, 24)
+    assert np.abs(Kh - Kh.transpose(0, 2, 1)).max() <= 1e-6 * np.abs(Kh).max()
+
+
 def ctypes_d(v):
     import ctypes
 
