@@ -54,7 +54,9 @@ public:
     bool stored() const {
         const bool coarse = element_type == SFEM_GB300_HEX8 ||
                             (element_type >= SFEM_GB300_SSHEX8(1) && element_type <= SFEM_GB300_SSHEX8(2));
-        return coarse && contraction == real_type_v<T>;
+        // at most 4 GiB of matrices (576 values per element); larger meshes build them per apply
+        const bool fits = (double)nelements * 576 * sizeof(T) <= 4.0 * 1024 * 1024 * 1024;
+        return coarse && fits && contraction == real_type_v<T>;
     }
     // called at creation and whenever the geometry or the contraction changes (outside any capture)
     int prepare() {
