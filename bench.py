@@ -565,8 +565,9 @@ def run_ours(args):
     value /= 1e9
 
     # end-to-end through the C ABI with host buffers: every step copies its x from pinned
-    # host memory, resets y, applies (cu_laplacian_apply on an explicit stream) and copies y
-    # back to pinned host memory.  Consecutive steps overlap on three streams (host-to-
+    # host memory, resets y, applies (the operator's FP32 apply from its packed tiles,
+    # sfem_gb300_sshex8_laplacian_apply_packed, on an explicit stream) and copies y back to
+    # pinned host memory.  Consecutive steps overlap on three streams (host-to-
     # device, compute, device-to-host) with double-buffered device and host buffers.
     e2e_value, t_e2e = measure_e2e(op, x, N, max(20, args.steps), world, dev)
 

@@ -88,6 +88,24 @@ int cu_laplacian_diag(int element_type, ptrdiff_t nelements, sfem_gb300_idx_t **
  * setting (-1 if none was forced). */
 int sfem_gb300_set_laplacian_kernel(int variant);
 
+/* Packed tiles (no reference counterpart; an operator-creation step like the
+ * reference's FFF cache): the connectivity and FFF of sshex8 L = 4 repacked into
+ * one contiguous block per 32 consecutive macro elements ([(L+1)^3][el] int32 node
+ * ids, then [6][el] FFF floats; elements past the end: node 0, FFF 0) so the FP32
+ * apply fetches a tile's ids and metric with one bulk copy.
+ * sfem_gb300_sshex8_packed_bytes gives the block array's size (-1: unsupported
+ * type), sfem_gb300_sshex8_pack fills it (16-byte aligned),
+ * sfem_gb300_sshex8_laplacian_apply_packed computes y += A x (FP32 x / y) from it;
+ * the result equals cu_laplacian_apply's on the same connectivity and FFF up to FP32
+ * rounding order.  sfem_gb300_laplacian_status returns (and clears) 1 if a packed
+ * apply gave up waiting for its bulk copy, else 0. */
+ptrdiff_t sfem_gb300_sshex8_packed_bytes(int element_type, ptrdiff_t nelements);
+int sfem_gb300_sshex8_pack(int element_type, ptrdiff_t nelements, sfem_gb300_idx_t **elements, ptrdiff_t fff_stride,
+                           const float *fff, void *packed, void *stream);
+int sfem_gb300_sshex8_laplacian_apply_packed(int element_type, ptrdiff_t nelements, const void *packed,
+                                             int real_type_xy, const void *x, void *y, void *stream);
+int sfem_gb300_laplacian_status(void);
+
 /* ------------------------------------------------------- linear elasticity */
 
 /* out += K u for the affine hex8 / sshex8 linear-elasticity operator with
@@ -346,7 +364,10 @@ int sfem_gb300_context_create(void *stream, void **context);
 int sfem_gb300_handle_destroy(void *handle);
 
 /* Function-level Laplacian: y += A x, then y[c] = x[c] on Dirichlet nodes
- * (Function::apply + copy_constrained_dofs, frontend/sfem_Function.cpp:481-496). */
+ * (Function::apply + copy_constrained_dofs, frontend/sfem_Function.cpp:481-496).
+ * An FP32 sshex8 L = 4 operator packs the connectivity and FFF at creation
+ * (sfem_gb300_sshex8_pack) and applies from the packed tiles, so it keeps the
+ * geometry it was created with; other operators read `fff` at every apply. */
 int sfem_gb300_laplacian_op_create(void *context, int real_type, int element_type, ptrdiff_t nelements,
                                    sfem_gb300_idx_t **elements, ptrdiff_t fff_stride, const float *fff,
                                    ptrdiff_t n_nodes, ptrdiff_t n_dirichlet, const int32_t *dirichlet_nodes,

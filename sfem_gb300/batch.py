@@ -242,7 +242,7 @@ class BatchGroup:
         sp = self.spaces[k]
         d = torch.zeros(self.vec * sp.n_nodes, dtype=dtype, device=self.device)
         if self.kind == "poisson":
-            Laplacian(sp).set_fff(sp.fff).hessian_diag(d)
+            Laplacian(sp, packed=False).set_fff(sp.fff).hessian_diag(d)
         else:
             E = sp.n_elements
             capi.check(capi.load().sfem_gb300_linear_elasticity_block_diag(

@@ -52,6 +52,7 @@ def load(path: str | None = None):
     _lib = C.CDLL(str(p))
     _lib.sfem_gb300_last_error.restype = C.c_char_p
     _lib.sfem_gb300_version.restype = C.c_char_p
+    _lib.sfem_gb300_sshex8_packed_bytes.restype = C.c_ssize_t
     return _lib
 
 

@@ -5,11 +5,13 @@
 // operators/hex8/hex8_laplacian.cpp:309-345): one metric (FFF, 6 floats) per
 // macro element, sub-metric FFF/L for each of the L^3 micro elements, element
 // matrix A = sum_m f_m W_m with the exact Q1 integrals W_m, y += A x.
+#include <algorithm>
 #include <cstdio>
 #include <cstdlib>
 
 #include "common.cuh"
 #include "laplacian_kernels.cuh"
+#include "tcgen05.cuh"
 
 namespace sfem_gb300 {
 
@@ -735,6 +737,143 @@ __global__ void __launch_bounds__(32 * L, 2) sshex8_laplacian_apply_pipe_kernel(
     cp_async_wait_all();
 }
 
+// ------------------------------------------------------------------ packed tiles
+// Connectivity and metric repacked once per operator into one contiguous block per
+// tile of PK_TILE = 32 consecutive macro elements: [node][el] int32 ids followed by
+// [6][el] metric entries as float bits (elements past the end: node 0, metric 0), so
+// a CTA fetches its tile's ids and metric with one bulk copy (cp.async.bulk,
+// completion counted on an mbarrier) instead of 125 row segments of 128 bytes from
+// 125 SoA rows, each behind a row-pointer load.
+constexpr int PK_TILE = 32;
+constexpr int PK_L = 4;  // the level the packed path serves
+__host__ __device__ constexpr int pk_words(int L) { return PK_TILE * ((L + 1) * (L + 1) * (L + 1) + 6); }
+constexpr int LAP_WAIT_POLLS = 1 << 20;
+__device__ int g_lap_status;  // nonzero: a bulk-copy wait gave up
+
+__global__ void sshex8_pack_kernel(ptrdiff_t nelements, int nxe, const idx_t *const *elements, ptrdiff_t fff_stride,
+                                   const float *fff, int32_t *packed) {
+    const int words = PK_TILE * (nxe + 6);
+    const ptrdiff_t total = (nelements + PK_TILE - 1) / PK_TILE * words;
+    for (ptrdiff_t g = (ptrdiff_t)blockIdx.x * blockDim.x + threadIdx.x; g < total;
+         g += (ptrdiff_t)gridDim.x * blockDim.x) {
+        const ptrdiff_t t = g / words;
+        const int w = (int)(g - t * words);
+        const ptrdiff_t e = t * PK_TILE + w % PK_TILE;
+        int32_t val = 0;
+        if (e < nelements)
+            val = w < PK_TILE * nxe ? elements[w / PK_TILE][e]
+                                    : __float_as_int(fff[(w / PK_TILE - nxe) * fff_stride + e]);
+        packed[g] = val;
+    }
+}
+
+// Rows 0..3 of the micro element matrix (packed by pairs) from the macro metric f
+// already scaled by 1/L.
+__device__ __forceinline__ void lap_A2_from_metric(const float (&f)[6], float2 (&A2)[8][2]) {
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+#pragma unroll
+        for (int k = 0; k < 2; k++) {
+            float a0 = 0.f, a1 = 0.f;
+#pragma unroll
+            for (int m = 0; m < 6; m++) {
+                const double w0 = LapTable().w[(2 * k) * 8 + j][m];
+                const double w1 = LapTable().w[(2 * k + 1) * 8 + j][m];
+                if (w0 != 0.0) a0 += f[m] * (float)w0;
+                if (w1 != 0.0) a1 += f[m] * (float)w1;
+            }
+            A2[j][k] = make_float2(a0, a1);
+        }
+    }
+}
+
+// FP32 apply of one packed tile per CTA: bulk copy of the block, x gathered with
+// 4-byte cp.async (lanes = the tile's elements), two threads per element each running
+// half of the micro layers (the async tile kernel's arithmetic), atomic scatter.
+// Shared memory (dynamic, 35,968 B at L = 4: 6 CTAs per SM): the block, x [node][el],
+// the partial sums of the middle plane [p][el].
+template <int L>
+__global__ void __launch_bounds__(2 * PK_TILE, 6) sshex8_laplacian_apply_packed_kernel(
+        ptrdiff_t nelements, const int32_t *__restrict__ packed, const float *__restrict__ x,
+        float *__restrict__ y) {
+    constexpr int N1 = L + 1;
+    constexpr int NP = N1 * N1;
+    constexpr int NXE = NP * N1;
+    constexpr int H = L / 2;
+    constexpr int WORDS = pk_words(L);
+    extern __shared__ __align__(128) int32_t pk_smem[];
+    __shared__ __align__(8) uint64_t mbar;
+    const int32_t *sidx = pk_smem;
+    const float *smet = reinterpret_cast<const float *>(pk_smem + PK_TILE * NXE);
+    float *sx = reinterpret_cast<float *>(pk_smem + WORDS);
+    float *spart = sx + NXE * PK_TILE;
+    const int tid = threadIdx.x;
+    const ptrdiff_t t = blockIdx.x;
+    if (tid == 0) {
+        tc::mbar_init(&mbar, 1);
+        tc::mbar_arrive_expect_tx(&mbar, WORDS * 4);
+        tc::bulk_load(pk_smem, packed + t * WORDS, WORDS * 4, &mbar);
+    }
+    __syncthreads();
+    if (!__syncthreads_and(tc::mbar_wait(&mbar, 0, LAP_WAIT_POLLS))) {
+        // leave no copy in flight into this CTA's shared memory
+        if (tid == 0) {
+            atomicExch(&g_lap_status, 1);
+            tc::mbar_wait(&mbar, 0, LAP_WAIT_POLLS);
+        }
+        return;
+    }
+    const int nvalid = (int)((nelements - t * PK_TILE) < PK_TILE ? (nelements - t * PK_TILE) : PK_TILE);
+    // 1. gather x
+    for (int i = tid; i < NXE * PK_TILE; i += 2 * PK_TILE)
+        if (i % PK_TILE < nvalid) cp_async4(&sx[i], x + sidx[i]);
+    const int el = tid % PK_TILE;
+    const int half = tid / PK_TILE;  // warp-uniform layer group
+    float2 A2[8][2];
+    {
+        float f[6];
+        const float h = 1.f / (float)L;
+#pragma unroll
+        for (int m = 0; m < 6; m++) f[m] = el < nvalid ? smet[m * PK_TILE + el] * h : 0.f;
+        lap_A2_from_metric(f, A2);
+    }
+    cp_async_wait_all();
+    __syncthreads();
+    // 2. apply: thread group `half` runs layers half*H .. half*H + H - 1 upwards
+    float *col = sx + el;
+    const int z0 = half * H;
+    float lo[NP], up[NP];
+#pragma unroll
+    for (int p = 0; p < NP; p++) lo[p] = 0.f;
+#pragma unroll 1
+    for (int zi = z0; zi < z0 + H; zi++) {
+#pragma unroll
+        for (int p = 0; p < NP; p++) up[p] = 0.f;
+        lap_layer_f32x2<L, PK_TILE>(col + zi * NP * PK_TILE, A2, lo, up);
+        // plane zi is complete for this thread; the middle plane's lower part (from the
+        // upper group) is kept aside until every x read of it is done
+        float *dst = (zi == z0 && half > 0) ? spart + el : col + zi * NP * PK_TILE;
+#pragma unroll
+        for (int p = 0; p < NP; p++) {
+            dst[p * PK_TILE] = lo[p];
+            lo[p] = up[p];
+        }
+    }
+    if (half == 1) {
+#pragma unroll
+        for (int p = 0; p < NP; p++) col[(L * NP + p) * PK_TILE] = lo[p];
+    }
+    __syncthreads();
+    if (half == 0) {
+#pragma unroll
+        for (int p = 0; p < NP; p++) col[(H * NP + p) * PK_TILE] = lo[p] + spart[p * PK_TILE + el];
+    }
+    __syncthreads();
+    // 3. scatter
+    for (int i = tid; i < NXE * PK_TILE; i += 2 * PK_TILE)
+        if (i % PK_TILE < nvalid) atomicAdd(&y[sidx[i]], sx[i]);
+}
+
 // Diagonal: node value = sum over the micro elements of this macro element that
 // contain it of A[a][a] (a = the node's corner in that micro element).
 template <typename T, int L>
@@ -1005,4 +1144,60 @@ extern "C" int sfem_gb300_set_laplacian_kernel(int variant) {
     __atomic_store_n(&g_laplacian_variant, variant < 0 ? 0 : variant, __ATOMIC_RELAXED);
     __atomic_store_n(&g_laplacian_variant_forced, variant < 0 ? 0 : 1, __ATOMIC_RELAXED);
     return prev;
+}
+
+// ------------------------------------------------------------------ packed tiles (C ABI)
+
+extern "C" ptrdiff_t sfem_gb300_sshex8_packed_bytes(int element_type, ptrdiff_t nelements) {
+    if (element_type != SFEM_GB300_SSHEX8(PK_L) || nelements < 0) return -1;
+    return (nelements + PK_TILE - 1) / PK_TILE * (ptrdiff_t)pk_words(PK_L) * (ptrdiff_t)sizeof(int32_t);
+}
+
+extern "C" int sfem_gb300_sshex8_pack(int element_type, ptrdiff_t nelements, idx_t **elements, ptrdiff_t fff_stride,
+                                      const float *fff, void *packed, void *stream) {
+    if (element_type != SFEM_GB300_SSHEX8(PK_L))
+        return set_error("sfem_gb300_sshex8_pack: element type %d is not sshex8 L = %d", element_type, PK_L);
+    if (nelements <= 0) return SFEM_GB300_SUCCESS;
+    if (reinterpret_cast<uintptr_t>(packed) & 15) return set_error("sfem_gb300_sshex8_pack: packed is not 16-byte aligned");
+    constexpr int nxe = (PK_L + 1) * (PK_L + 1) * (PK_L + 1);
+    const ptrdiff_t total = (nelements + PK_TILE - 1) / PK_TILE * (ptrdiff_t)pk_words(PK_L);
+    sshex8_pack_kernel<<<grid_for(total, 256), 256, 0, stream_of(stream)>>>(nelements, nxe, elements, fff_stride, fff,
+                                                                           (int32_t *)packed);
+    return check_launch("sfem_gb300_sshex8_pack");
+}
+
+extern "C" int sfem_gb300_sshex8_laplacian_apply_packed(int element_type, ptrdiff_t nelements, const void *packed,
+                                                        int real_type_xy, const void *x, void *y, void *stream) {
+    if (element_type != SFEM_GB300_SSHEX8(PK_L))
+        return set_error("sfem_gb300_sshex8_laplacian_apply_packed: element type %d is not sshex8 L = %d",
+                         element_type, PK_L);
+    if (real_type_xy != SFEM_GB300_FLOAT32)
+        return set_error("sfem_gb300_sshex8_laplacian_apply_packed: real type %d (FP32 only)", real_type_xy);
+    if (nelements <= 0) return SFEM_GB300_SUCCESS;
+    if (reinterpret_cast<uintptr_t>(packed) & 15)
+        return set_error("sfem_gb300_sshex8_laplacian_apply_packed: packed is not 16-byte aligned");
+    const ptrdiff_t ntiles = (nelements + PK_TILE - 1) / PK_TILE;
+    if (ntiles > 0x7fffffff) return set_error("sfem_gb300_sshex8_laplacian_apply_packed: too many tiles");
+    constexpr int NXE = (PK_L + 1) * (PK_L + 1) * (PK_L + 1);
+    constexpr size_t smem = ((size_t)pk_words(PK_L) + (size_t)NXE * PK_TILE + (size_t)(PK_L + 1) * (PK_L + 1) * PK_TILE) *
+                            sizeof(float);
+    static bool attr = false;  // shared-memory opt-in, once
+    if (!attr) {
+        cudaFuncSetAttribute(sshex8_laplacian_apply_packed_kernel<PK_L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem);
+        attr = true;
+    }
+    sshex8_laplacian_apply_packed_kernel<PK_L><<<(unsigned)ntiles, 2 * PK_TILE, smem, stream_of(stream)>>>(
+            nelements, (const int32_t *)packed, (const float *)x, (float *)y);
+    return check_launch("sfem_gb300_sshex8_laplacian_apply_packed");
+}
+
+extern "C" int sfem_gb300_laplacian_status(void) {
+    int st = 0;
+    if (cudaMemcpyFromSymbol(&st, g_lap_status, sizeof(int)) != cudaSuccess) return -1;
+    if (st) {
+        const int zero = 0;
+        cudaMemcpyToSymbol(g_lap_status, &zero, sizeof(int));
+    }
+    return st;
 }

@@ -29,9 +29,24 @@ public:
     idx_t **elements{nullptr};
     const float *fff{nullptr};
     const idx_t *dirichlet{nullptr};
+    // FP32 sshex8 L = 4: connectivity + FFF repacked per 32-element tile, built at creation
+    // (the operator keeps the geometry it was created with, as the reference's op keeps its FFF)
+    DeviceBuffer<int32_t> packed;
+    int prepare() {
+        if (real_type_v<T> != SFEM_GB300_FLOAT32) return 0;
+        const ptrdiff_t nb = sfem_gb300_sshex8_packed_bytes(element_type, nelements);
+        if (nb <= 0) return 0;
+        SFEM_GB300_CHECK(packed.resize(nb / (ptrdiff_t)sizeof(int32_t)));
+        return sfem_gb300_sshex8_pack(element_type, nelements, elements, fff_stride, fff, packed.ptr, ctx->sp());
+    }
     int apply(const T *x, T *y) override {
-        SFEM_GB300_CHECK(cu_laplacian_apply(element_type, nelements, elements, fff_stride, fff, real_type_v<T>, x, y,
-                                            ctx->sp()));
+        if (packed.n > 0) {
+            SFEM_GB300_CHECK(sfem_gb300_sshex8_laplacian_apply_packed(element_type, nelements, packed.ptr,
+                                                                      real_type_v<T>, x, y, ctx->sp()));
+        } else {
+            SFEM_GB300_CHECK(cu_laplacian_apply(element_type, nelements, elements, fff_stride, fff, real_type_v<T>, x,
+                                                y, ctx->sp()));
+        }
         return sfem_gb300_constraint_nodes_copy(real_type_v<T>, n_dirichlet, dirichlet, 1, 0, x, y, ctx->sp());
     }
     ptrdiff_t rows() const override { return n_nodes; }
@@ -279,14 +294,20 @@ int sfem_gb300_laplacian_op_create(void *context, int real_type, int element_typ
         op->n_dirichlet = n_dirichlet;
         op->dirichlet = dirichlet_nodes;
     };
+    int rc = 0;
     if (is_f32(real_type)) {
         auto op = std::make_shared<LaplacianOp<float>>();
         fill(op);
+        rc = op->prepare();
         h->f = op;
     } else {
         auto op = std::make_shared<LaplacianOp<double>>();
         fill(op);
         h->d = op;
+    }
+    if (rc) {
+        delete h;
+        return rc;
     }
     *out = h;
     return SFEM_GB300_SUCCESS;

@@ -230,7 +230,7 @@ def fine_inv_diag(H, dtype):
 
     sp = H.spaces[0]
     d = torch.zeros(sp.n_nodes, dtype=dtype, device=H.device)
-    Laplacian(sp).set_fff(H.fff).hessian_diag(d)
+    Laplacian(sp, packed=False).set_fff(H.fff).hessian_diag(d)
     d[H.dirichlet[0].long()] = 1
     return 1.0 / d
 

@@ -61,10 +61,14 @@ class SSMeshDevice:
 class Laplacian:
     """Matrix-free Laplacian op on the GPU (mirror of ``GPULaplacian``)."""
 
-    def __init__(self, space: SSMeshDevice, coefficient=None):
+    def __init__(self, space: SSMeshDevice, coefficient=None, packed=True):
         self.space = space
         self.coefficient = coefficient
         self.fff = None
+        # FP32 applies of sshex8 L = 2 / 4 read the connectivity + metric repacked into
+        # one contiguous block per 32 macro elements (built with the metric)
+        self.packed = bool(packed)
+        self.packed_blocks = None
 
     def initialize(self, stream=None):
         import torch
@@ -79,6 +83,21 @@ class Laplacian:
             # per-macro-element coefficient k_e scales the metric exactly
             k = torch.as_tensor(self.coefficient, dtype=torch.float32, device=self.space.device)
             self.fff *= k[None, :]
+        return self._pack()
+
+    def _pack(self):
+        import torch
+
+        self.packed_blocks = None
+        lib = capi.load()
+        E = self.space.n_elements
+        nbytes = lib.sfem_gb300_sshex8_packed_bytes(self.space.element_type, capi.i64(E)) if self.packed else -1
+        if nbytes > 0:
+            self.packed_blocks = torch.empty(nbytes // 4, dtype=torch.int32, device=self.space.device)
+            capi.check(lib.sfem_gb300_sshex8_pack(self.space.element_type, capi.i64(E), self.space.elements_ptrs.ptr,
+                                                  capi.i64(self.fff.shape[1]), capi.vp(self.fff),
+                                                  capi.vp(self.packed_blocks), None),
+                       "sfem_gb300_sshex8_pack")
         return self
 
     def set_fff(self, fff_soa):
@@ -86,11 +105,19 @@ class Laplacian:
         import torch
 
         self.fff = torch.as_tensor(fff_soa, dtype=torch.float32, device=self.space.device).contiguous()
-        return self
+        return self._pack()
 
     def apply(self, x, out, stream=None):
         """out += A x (x, out: float32 or float64 CUDA tensors)."""
         E = self.space.n_elements
+        rt = capi.real_type_of(x)
+        if self.packed_blocks is not None and rt == capi.FLOAT32:
+            capi.check(
+                capi.load().sfem_gb300_sshex8_laplacian_apply_packed(self.space.element_type, capi.i64(E),
+                                                                     capi.vp(self.packed_blocks), rt, capi.vp(x),
+                                                                     capi.vp(out), stream),
+                "sfem_gb300_sshex8_laplacian_apply_packed")
+            return out
         capi.check(
             capi.load().cu_laplacian_apply(self.space.element_type, capi.i64(E), self.space.elements_ptrs.ptr,
                                            capi.i64(E), capi.vp(self.fff), capi.real_type_of(x), capi.vp(x),

@@ -266,7 +266,7 @@ class Hierarchy:
         self.dirichlet = [sp.dirichlet_nodes(dirichlet_faces) if dirichlet_faces else
                           torch.zeros(0, dtype=torch.int32, device=self.device) for sp in self.spaces]
         # geometry: one metric / adjugate per macro element for all sshex8 levels
-        lap = Laplacian(self.spaces[0], coefficient=coefficient).initialize()
+        lap = Laplacian(self.spaces[0], coefficient=coefficient, packed=False).initialize()
         self.fff = lap.fff
         self.adj, self.det = self._adjugate(self.spaces[0])
         for sp in self.spaces[:self.n_sshex8_levels]:
@@ -276,7 +276,7 @@ class Hierarchy:
             if k is not None:
                 cx, cy, cz = sp.lvl.shape
                 k = coarsen_coefficient(k, (cz, cy, cx))
-            sp.fff = Laplacian(sp, coefficient=None if k is None else k.reshape(-1)).initialize().fff
+            sp.fff = Laplacian(sp, coefficient=None if k is None else k.reshape(-1), packed=False).initialize().fff
             sp.adj, sp.det = self._adjugate(sp)
 
     def _adjugate(self, sp):
@@ -320,7 +320,7 @@ def build_poisson_mg(ctx, H: Hierarchy, dtype, smoother="chebyshev3", sweeps=2, 
     for k, sp in enumerate(H.spaces):
         op = laplacian_op(ctx, sp, sp.fff, H.dirichlet[k], dtype)
         ops.append(op)
-        lap = Laplacian(sp).set_fff(sp.fff)
+        lap = Laplacian(sp, packed=False).set_fff(sp.fff)
         diag = torch.zeros(sp.n_nodes, dtype=dtype, device=H.device)
         lap.hessian_diag(diag)
         diag[H.dirichlet[k].long()] = 1

@@ -105,6 +105,93 @@ def test_sshex8_laplacian_fp32_kernels(cuda, variant, L, aligned):
     assert err.max() < RTOL32, (variant, L, aligned, err.max())
 
 
+@pytest.mark.parametrize("n", [(5, 4, 3), (9, 8, 7), (1, 1, 1), (36, 36, 36)])
+@pytest.mark.parametrize("aligned", [True, False])
+def test_sshex8_laplacian_packed(cuda, n, aligned):
+    """Packed tiles (L = 4): pack from SoA rows (row stride E or E + 1) and apply in FP32;
+    element counts 60 (32 + 28: a ragged last tile), 504, 1 and 46,656."""
+    import torch
+
+    L = 4
+    m = SSMesh(*n, L, perturb=0.1, seed=6)
+    el = m.elements(L)
+    E = m.n_elements
+    fff_aos = O.fff_fill(el[m.macro_corner_lidx(L)], m.points)
+    stride = E if aligned else E + 1
+    fbuf = torch.zeros((6, stride), dtype=torch.float32, device=cuda)
+    fbuf[:, :E] = torch.from_numpy(fff_aos.T.copy()).to(cuda)
+    buf = torch.zeros((el.shape[0], stride), dtype=torch.int32, device=cuda)
+    buf[:, :E] = torch.from_numpy(el).to(cuda)
+    rows = capi.DevicePtrArray(buf)
+    lib = capi.load()
+    nbytes = lib.sfem_gb300_sshex8_packed_bytes(capi.SSHEX8(L), capi.i64(E))
+    nxe = el.shape[0]
+    assert nbytes == (E + 31) // 32 * 32 * (nxe + 6) * 4
+    packed = torch.empty(nbytes // 4, dtype=torch.int32, device=cuda)
+    capi.check(lib.sfem_gb300_sshex8_pack(capi.SSHEX8(L), capi.i64(E), rows.ptr, capi.i64(stride), capi.vp(fbuf),
+                                          capi.vp(packed), None), "pack")
+    # layout: tile t = [node][el] ids, then [6][el] metric bits; padding node 0, metric 0
+    blk = packed.view(-1, 32 * (nxe + 6)).cpu().numpy()
+    ids = blk[:, :32 * nxe].reshape(-1, nxe, 32).transpose(0, 2, 1).reshape(-1, nxe)
+    assert np.array_equal(ids[:E], el.T) and not ids[E:].any()
+    met = blk[:, 32 * nxe:].reshape(-1, 6, 32).transpose(0, 2, 1).reshape(-1, 6).view(np.float32)
+    assert np.array_equal(met[:E], fff_aos.astype(np.float32)) and not met[E:].any()
+    x = np.random.default_rng(7).standard_normal(m.n_nodes(L))
+    y0 = np.random.default_rng(8).standard_normal(m.n_nodes(L))
+    ref = O.sshex8_laplacian_apply(L, el, fff_aos, x, out=y0.copy())
+    xd = torch.from_numpy(x).float().to(cuda)
+    yd = torch.from_numpy(y0).float().to(cuda)
+    capi.check(lib.sfem_gb300_sshex8_laplacian_apply_packed(capi.SSHEX8(L), capi.i64(E), capi.vp(packed),
+                                                            capi.FLOAT32, capi.vp(xd), capi.vp(yd), None),
+               "apply_packed")
+    torch.cuda.synchronize()
+    assert lib.sfem_gb300_laplacian_status() == 0
+    scale = _row_scale_lap(L, el, fff_aos, x) + np.abs(y0)
+    err = np.abs(yd.double().cpu().numpy() - ref) / scale
+    assert err.max() < RTOL32, (n, aligned, err.max())
+
+
+def test_sshex8_laplacian_packed_operator(cuda):
+    """The operator's FP32 apply goes through the packed blocks; FP64 keeps the SoA rows."""
+    import torch
+
+    L = 4
+    m = SSMesh(3, 2, 2, L, perturb=0.1, seed=9)
+    sp = SSMeshDevice(m, L)
+    el = m.elements(L)
+    fff_aos = O.fff_fill(el[m.macro_corner_lidx(L)], m.points)
+    op = Laplacian(sp, packed=True).set_fff(torch.from_numpy(fff_aos.T.copy()))
+    assert op.packed_blocks is not None
+    x = np.random.default_rng(10).standard_normal(m.n_nodes(L))
+    ref = O.sshex8_laplacian_apply(L, el, fff_aos, x)
+    y32 = torch.zeros(m.n_nodes(L), dtype=torch.float32, device=cuda)
+    op.apply(torch.from_numpy(x).float().to(cuda), y32)
+    y64 = torch.zeros(m.n_nodes(L), dtype=torch.float64, device=cuda)
+    op.apply(torch.from_numpy(x).to(cuda), y64)
+    scale = _row_scale_lap(L, el, fff_aos, x)
+    assert (np.abs(y32.double().cpu().numpy() - ref) / scale).max() < RTOL32
+    assert (np.abs(y64.cpu().numpy() - ref) / scale).max() < RTOL64
+
+
+def test_sshex8_laplacian_packed_bad_inputs(cuda):
+    import torch
+
+    lib = capi.load()
+    assert lib.sfem_gb300_sshex8_packed_bytes(capi.SSHEX8(3), capi.i64(10)) == -1
+    assert lib.sfem_gb300_sshex8_packed_bytes(capi.SSHEX8(2), capi.i64(10)) == -1
+    assert lib.sfem_gb300_sshex8_packed_bytes(capi.SSHEX8(4), capi.i64(0)) == 0
+    buf = torch.zeros(64, dtype=torch.int32, device=cuda)
+    x = torch.zeros(8, dtype=torch.float64, device=cuda)
+    # FP64 vectors are refused with a message (the packed path is FP32 only)
+    assert lib.sfem_gb300_sshex8_laplacian_apply_packed(capi.SSHEX8(4), capi.i64(1), capi.vp(buf), capi.FLOAT64,
+                                                        capi.vp(x), capi.vp(x), None) == 1
+    assert "FP32" in capi.last_error()
+    # a block array that is not 16-byte aligned is refused before any launch
+    assert lib.sfem_gb300_sshex8_laplacian_apply_packed(capi.SSHEX8(4), capi.i64(1), capi.c_void(buf.data_ptr() + 4),
+                                                        capi.FLOAT32, capi.vp(x), capi.vp(x), None) == 1
+    assert "aligned" in capi.last_error()
+
+
 def test_hex8_laplacian_apply_and_diag(cuda):
     import torch
 
