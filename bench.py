@@ -41,10 +41,10 @@ NX = 48
 LEVEL = 4
 METRIC = "sshex8 Laplacian apply GDoF/s (FP32, L=4, 48^3 macro); solve times to FP64 residual in 'solve'"
 NOMINAL_FP64_TFLOPS = 1.25  # GB300 nominal FP64 (no measured figure in the peaks file)
-# dram__bytes_read.sum + dram__bytes_write.sum of one launch of the default float
-# kernel on this workload (ncu --set full, cold cache: 115.5 MB read + 5.3 MB
-# written), from profiles/sshex8_laplacian_apply_async_fp32_L4_48cube.md
-TRAFFIC_BYTES_PER_LAUNCH = 120.8e6
+# dram__bytes_read.sum + dram__bytes_write.sum of one launch of the float kernel of
+# the step on this workload (ncu --set full, cold cache, mean of two launches:
+# 115.5 MB read + 5.65 MB written), from profiles/sshex8_laplacian_apply_packed_fp32_L4_48cube.md
+TRAFFIC_BYTES_PER_LAUNCH = 121.15e6
 SEED = 0
 PERTURB = 0.1
 
