@@ -819,6 +819,157 @@ __global__ void __launch_bounds__(128, ETC_CTAS_PER_SM) elasticity_apply_tf32x3_
     if (warp == 0) tc::tmem_dealloc(tmem, ETC_TMEM_COLS);
 }
 
+// Any level 5 <= L <= 16 (no compile-time kernel): one CTA per macro element, warp 0
+// builds K, the (L+1)^3 x 3 values of u and out in dynamic shared memory (FP64 up to
+// L = 12, FP32 up to L = 16 within 227 KB), micro elements over the threads (u read
+// once per micro element, 24 rows, shared-memory atomics), node ids read again for
+// the scatter.
+constexpr int EL_MAX_L = 16;
+template <typename T>
+__host__ __device__ constexpr size_t el_cta_smem_bytes(int L) {
+    return (576 + 96 + 6 * (size_t)(L + 1) * (L + 1) * (L + 1)) * sizeof(T);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) elasticity_apply_cta_kernel(int L, ptrdiff_t nelements,
+                                                                   const idx_t *const *elements, ptrdiff_t stride,
+                                                                   const float *adjugate, const float *determinant,
+                                                                   T mu, T lambda, const T *__restrict__ x,
+                                                                   T *__restrict__ y) {
+    extern __shared__ __align__(16) unsigned char el_cta_smem[];
+    const int N1 = L + 1, NXE = N1 * N1 * N1, NM = L * L * L;
+    T *K = reinterpret_cast<T *>(el_cta_smem);
+    T *Wsm = K + 576;
+    T *xs = Wsm + 96;
+    T *ys = xs + 3 * NXE;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    T Ir[2][9];
+    if (warp == 0) load_grad_regs<T>(lane, Ir);
+    for (ptrdiff_t e = blockIdx.x; e < nelements; e += gridDim.x) {
+        if (warp == 0) {
+            T adj[9], AA[9], inv_det;
+            load_sub_adjugate<T>(adjugate, determinant, stride, e, L, adj, AA, inv_det);
+            build_K_warp_sym<T>(adj, AA, inv_det, mu, lambda, Ir, Wsm, K, 24, lane);
+        }
+        for (int l = threadIdx.x; l < NXE; l += blockDim.x) {
+            const ptrdiff_t g = elements[l][e];
+#pragma unroll
+            for (int d = 0; d < 3; d++) {
+                xs[d * NXE + l] = x[3 * g + d];
+                ys[d * NXE + l] = 0;
+            }
+        }
+        __syncthreads();
+        for (int m = threadIdx.x; m < NM; m += blockDim.x) {
+            const int xi = m % L, yi = (m / L) % L, zi = m / (L * L);
+            int v[8];
+            T u[24];
+#pragma unroll
+            for (int c = 0; c < 8; c++) {
+                v[c] = lidx(L, xi + c8x(c), yi + c8y(c), zi + c8z(c));
+#pragma unroll
+                for (int d = 0; d < 3; d++) u[d * 8 + c] = xs[d * NXE + v[c]];
+            }
+#pragma unroll 4
+            for (int i = 0; i < 24; i++) {
+                T acc = 0;
+#pragma unroll
+                for (int j = 0; j < 24; j++) acc += K[i * 24 + j] * u[j];
+                atomicAdd(&ys[(i / 8) * NXE + v[i % 8]], acc);
+            }
+        }
+        __syncthreads();
+        for (int l = threadIdx.x; l < NXE; l += blockDim.x) {
+            const int xi = l % N1, yi = (l / N1) % N1, zi = l / (N1 * N1);
+            const bool interior = xi > 0 && xi < L && yi > 0 && yi < L && zi > 0 && zi < L;
+            const ptrdiff_t g = elements[l][e];
+#pragma unroll
+            for (int d = 0; d < 3; d++) {
+                if (interior)
+                    y[3 * g + d] += ys[d * NXE + l];
+                else
+                    atomicAdd(&y[3 * g + d], ys[d * NXE + l]);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// Block diagonal at any level (runtime L), warp per macro element as the compile-time kernel.
+template <typename T>
+__global__ void __launch_bounds__(64) elasticity_block_diag_any_kernel(int L, ptrdiff_t nelements,
+                                                                       const idx_t *const *elements, ptrdiff_t stride,
+                                                                       const float *adjugate, const float *determinant,
+                                                                       T mu, T lambda, T *diag3, T *block6) {
+    const int N1 = L + 1, NXE = N1 * N1 * N1;
+    constexpr int WPB = 2;
+    __shared__ T Bs[WPB][8][6];
+    __shared__ T Ks[WPB][576];
+    __shared__ T Is[576];
+    __shared__ T Ws[WPB][81];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int bi[6] = {0, 0, 0, 1, 1, 2}, bj[6] = {0, 1, 2, 1, 2, 2};
+    load_grad_table<T>(Is);
+    for (ptrdiff_t e = (ptrdiff_t)blockIdx.x * WPB + warp; e < nelements; e += (ptrdiff_t)gridDim.x * WPB) {
+        T adj[9], AA[9], inv_det;
+        load_sub_adjugate<T>(adjugate, determinant, stride, e, L, adj, AA, inv_det);
+        build_K_warp<T>(adj, AA, inv_det, mu, lambda, Is, Ws[warp], Ks[warp], 24, lane);
+        for (int k = lane; k < 48; k += 32) {
+            const int a = k / 6, c = k % 6;
+            Bs[warp][a][c] = Ks[warp][(bi[c] * 8 + a) * 24 + bj[c] * 8 + a];
+        }
+        __syncwarp();
+        for (int l = lane; l < NXE; l += 32) {
+            const int xi = l % N1, yi = (l / N1) % N1, zi = l / (N1 * N1);
+            T sacc[6] = {0, 0, 0, 0, 0, 0};
+#pragma unroll
+            for (int a = 0; a < 8; a++) {
+                const bool ok = (c8x(a) ? xi > 0 : xi < L) && (c8y(a) ? yi > 0 : yi < L) && (c8z(a) ? zi > 0 : zi < L);
+                if (ok)
+#pragma unroll
+                    for (int c = 0; c < 6; c++) sacc[c] += Bs[warp][a][c];
+            }
+            const ptrdiff_t g = elements[l][e];
+            const bool interior = xi > 0 && xi < L && yi > 0 && yi < L && zi > 0 && zi < L;
+            if (diag3) {
+                const T dv[3] = {sacc[0], sacc[3], sacc[5]};
+                for (int d = 0; d < 3; d++) {
+                    if (interior)
+                        diag3[3 * g + d] += dv[d];
+                    else
+                        atomicAdd(&diag3[3 * g + d], dv[d]);
+                }
+            }
+            if (block6) {
+                for (int c = 0; c < 6; c++) {
+                    if (interior)
+                        block6[6 * g + c] += sacc[c];
+                    else
+                        atomicAdd(&block6[6 * g + c], sacc[c]);
+                }
+            }
+        }
+        __syncwarp();
+    }
+}
+
+template <typename T>
+static int launch_el_cta(int L, ptrdiff_t nelements, idx_t **elements, ptrdiff_t stride, const float *adj,
+                         const float *det, T mu, T lambda, const T *x, T *y, cudaStream_t s) {
+    const size_t smem = el_cta_smem_bytes<T>(L);
+    if (smem > 227 * 1024)
+        return set_error("sfem_gb300_linear_elasticity_apply: level %d needs %zu bytes of shared memory in %s", L,
+                         smem, sizeof(T) == 8 ? "FP64" : "FP32");
+    static size_t attr = 0;  // largest shared-memory opt-in so far (per T)
+    if (smem > 48 * 1024 && smem > attr) {
+        cudaFuncSetAttribute(elasticity_apply_cta_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        attr = smem;
+    }
+    const int grid = (int)std::min<ptrdiff_t>(nelements, (ptrdiff_t)kNumSMs * 8);
+    elasticity_apply_cta_kernel<T><<<grid, 256, smem, s>>>(L, nelements, elements, stride, adj, det, mu, lambda, x, y);
+    return check_launch("sfem_gb300_linear_elasticity_apply(SSHEX8, CTA per element)");
+}
+
 static int g_elasticity_kernel = -1;  // -1 default (tcgen05 at L = 4), 0 SIMT warp kernel, 1 tcgen05 3xTF32
 
 static int elasticity_apply_tf32x3(ptrdiff_t nelements, idx_t **elements, ptrdiff_t stride, const float *adj,
@@ -860,6 +1011,8 @@ static int elasticity_apply_tpl(int element_type, ptrdiff_t nelements, idx_t **e
         SFEM_EL_CASE(3)
         SFEM_EL_CASE(4)
         default:
+            if (L >= 5 && L <= EL_MAX_L)
+                return launch_el_cta<T>(L, nelements, elements, stride, adj, det, mu, lambda, x, y, s);
             return set_error("sfem_gb300_linear_elasticity_apply: unsupported element type %d", element_type);
     }
 #undef SFEM_EL_CASE
@@ -887,6 +1040,11 @@ static int elasticity_diag_tpl(int element_type, ptrdiff_t nelements, idx_t **el
         SFEM_EL_CASE(3)
         SFEM_EL_CASE(4)
         default:
+            if (L >= 5 && L <= EL_MAX_L) {
+                elasticity_block_diag_any_kernel<T><<<blocks, 64, 0, s>>>(L, nelements, elements, stride, adj, det, mu,
+                                                                          lambda, diag3, block6);
+                return check_launch("sfem_gb300_linear_elasticity_block_diag(SSHEX8, any level)");
+            }
             return set_error("sfem_gb300_linear_elasticity_block_diag: unsupported element type %d", element_type);
     }
 #undef SFEM_EL_CASE

@@ -914,6 +914,116 @@ __global__ void __launch_bounds__(128) sshex8_laplacian_diag_kernel(ptrdiff_t ne
     }
 }
 
+// Any level 2 <= L <= LAP_MAX_L without a compile-time kernel (5, 7, 9..16): one CTA
+// per macro element, the (L+1)^3 values of x and y in dynamic shared memory
+// (2 (L+1)^3 T: 78.6 KB for FP64 at L = 16), micro elements spread over the
+// threads with shared-memory atomics, node ids read again for the scatter
+// (interior nodes plain read-modify-write, surface nodes atomics).
+constexpr int LAP_MAX_L = 16;
+template <typename T>
+__global__ void __launch_bounds__(256) sshex8_laplacian_apply_cta_kernel(int L, ptrdiff_t nelements,
+                                                                         const idx_t *const *elements,
+                                                                         ptrdiff_t fff_stride, const float *fff,
+                                                                         const T *x, T *y) {
+    extern __shared__ __align__(16) unsigned char lap_cta_smem[];
+    const int N1 = L + 1, NXE = N1 * N1 * N1, NM = L * L * L;
+    T *xs = reinterpret_cast<T *>(lap_cta_smem);
+    T *ys = xs + NXE;
+    T *As = ys + NXE;
+    const T h = T(1) / T(L);
+    for (ptrdiff_t e = blockIdx.x; e < nelements; e += gridDim.x) {
+        if (threadIdx.x < 64) {
+            T a = 0;
+            for (int m = 0; m < 6; m++) a += (T)fff[m * fff_stride + e] * h * lap_w<T>(threadIdx.x, m);
+            As[threadIdx.x] = a;
+        }
+        for (int l = threadIdx.x; l < NXE; l += blockDim.x) {
+            xs[l] = x[elements[l][e]];
+            ys[l] = 0;
+        }
+        __syncthreads();
+        for (int m = threadIdx.x; m < NM; m += blockDim.x) {
+            const int xi = m % L, yi = (m / L) % L, zi = m / (L * L);
+            int v[8];
+            T u[8];
+#pragma unroll
+            for (int c = 0; c < 8; c++) {
+                v[c] = lidx(L, xi + c8x(c), yi + c8y(c), zi + c8z(c));
+                u[c] = xs[v[c]];
+            }
+#pragma unroll
+            for (int i = 0; i < 8; i++) {
+                T acc = 0;
+#pragma unroll
+                for (int j = 0; j < 8; j++) acc += As[i * 8 + j] * u[j];
+                atomicAdd(&ys[v[i]], acc);
+            }
+        }
+        __syncthreads();
+        for (int l = threadIdx.x; l < NXE; l += blockDim.x) {
+            const int xi = l % N1, yi = (l / N1) % N1, zi = l / (N1 * N1);
+            const bool interior = xi > 0 && xi < L && yi > 0 && yi < L && zi > 0 && zi < L;
+            const idx_t g = elements[l][e];
+            if (interior)
+                y[g] += ys[l];
+            else
+                atomicAdd(&y[g], ys[l]);
+        }
+        __syncthreads();
+    }
+}
+
+// Diagonal at any level (runtime L), warp per macro element as the compile-time kernel.
+template <typename T>
+__global__ void __launch_bounds__(128) sshex8_laplacian_diag_any_kernel(int L, ptrdiff_t nelements,
+                                                                        const idx_t *const *elements,
+                                                                        ptrdiff_t fff_stride, const float *fff, T *diag) {
+    const int N1 = L + 1, NXE = N1 * N1 * N1;
+    constexpr int WPB = 4;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const T h = T(1) / T(L);
+    for (ptrdiff_t e = (ptrdiff_t)blockIdx.x * WPB + warp; e < nelements; e += (ptrdiff_t)gridDim.x * WPB) {
+        T Ad[8];
+#pragma unroll
+        for (int a = 0; a < 8; a++) {
+            T s = 0;
+#pragma unroll
+            for (int m = 0; m < 6; m++) s += (T)fff[m * fff_stride + e] * h * lap_w<T>(a * 9, m);
+            Ad[a] = s;
+        }
+        for (int l = lane; l < NXE; l += 32) {
+            const int xi = l % N1, yi = (l / N1) % N1, zi = l / (N1 * N1);
+            T s = 0;
+#pragma unroll
+            for (int a = 0; a < 8; a++) {
+                const bool ok = (c8x(a) ? xi > 0 : xi < L) && (c8y(a) ? yi > 0 : yi < L) && (c8z(a) ? zi > 0 : zi < L);
+                if (ok) s += Ad[a];
+            }
+            const bool interior = xi > 0 && xi < L && yi > 0 && yi < L && zi > 0 && zi < L;
+            const idx_t g = elements[l][e];
+            if (interior)
+                diag[g] += s;
+            else
+                atomicAdd(&diag[g], s);
+        }
+    }
+}
+
+template <typename T>
+static int launch_lap_cta(int L, ptrdiff_t nelements, idx_t **elements, ptrdiff_t fff_stride, const float *fff,
+                          const T *x, T *y, cudaStream_t s) {
+    const size_t smem = (2 * (size_t)(L + 1) * (L + 1) * (L + 1) + 64) * sizeof(T);
+    static size_t attr = 0;  // largest shared-memory opt-in so far (per T)
+    if (smem > 48 * 1024 && smem > attr) {
+        cudaFuncSetAttribute(sshex8_laplacian_apply_cta_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem);
+        attr = smem;
+    }
+    const int grid = (int)std::min<ptrdiff_t>(nelements, (ptrdiff_t)kNumSMs * 8);
+    sshex8_laplacian_apply_cta_kernel<T><<<grid, 256, smem, s>>>(L, nelements, elements, fff_stride, fff, x, y);
+    return check_launch("cu_laplacian_apply(SSHEX8, CTA per element)");
+}
+
 // ------------------------------------------------------------------ dispatch
 
 // Kernel variant override for benchmarking (SFEM_GB300_LAPLACIAN_KERNEL or
@@ -1051,6 +1161,7 @@ static int laplacian_apply_tpl(int element_type, ptrdiff_t nelements, idx_t **el
         SFEM_LAP_CASE(6)
         SFEM_LAP_CASE(8)
         default:
+            if (L >= 2 && L <= LAP_MAX_L) return launch_lap_cta<T>(L, nelements, elements, fff_stride, fff, x, y, s);
             return set_error("cu_laplacian_apply: unsupported element type %d", element_type);
     }
 #undef SFEM_LAP_CASE
@@ -1078,6 +1189,11 @@ static int laplacian_diag_tpl(int element_type, ptrdiff_t nelements, idx_t **ele
         SFEM_LAP_CASE(6)
         SFEM_LAP_CASE(8)
         default:
+            if (L >= 2 && L <= LAP_MAX_L) {
+                sshex8_laplacian_diag_any_kernel<T><<<blocks, 128, 0, s>>>(L, nelements, elements, fff_stride, fff,
+                                                                           diag);
+                return check_launch("cu_laplacian_diag(SSHEX8, any level)");
+            }
             return set_error("cu_laplacian_diag: unsupported element type %d", element_type);
     }
 #undef SFEM_LAP_CASE

@@ -32,7 +32,7 @@ def _scale(L, el, adj, det, u):
     return a + 4 * np.abs(d3) * np.abs(u)
 
 
-@pytest.mark.parametrize("L", [1, 2, 3, 4])
+@pytest.mark.parametrize("L", [1, 2, 3, 4, 5, 8])
 def test_elasticity_apply_fp64(cuda, L):
     import torch
 
@@ -74,6 +74,31 @@ def test_elasticity_apply_fp32_coarse_levels(cuda, L):
                "elasticity apply")
     err = np.abs(yd.double().cpu().numpy() - ref) / _scale(L, el, adj, det, u)
     assert err.max() < 2e-5, err.max()
+
+
+@pytest.mark.parametrize("L,n", [(6, (2, 1, 1)), (16, (1, 1, 1))])
+def test_elasticity_apply_fp32_high_levels(cuda, L, n):
+    """Levels without a compile-time kernel (CTA per macro element) in FP32; FP64 at
+    L = 16 needs more shared memory than a CTA has and is refused with a message."""
+    import torch
+
+    m, sp, el, adj, det, adj_d, det_d = _setup(cuda, L, n=n)
+    nn = m.n_nodes(L)
+    u = np.random.default_rng(30 + L).standard_normal(3 * nn)
+    ref = O.linear_elasticity_apply(L, el, adj, det, MU, LAM, u)
+    yd = torch.zeros(3 * nn, dtype=torch.float32, device=cuda)
+    ud = torch.from_numpy(u).float().to(cuda)
+    lib = capi.load()
+    args = (sp.element_type, capi.i64(m.n_elements), sp.elements_ptrs.ptr, capi.i64(m.n_elements), capi.vp(adj_d),
+            capi.vp(det_d), ctypes_d(MU), ctypes_d(LAM))
+    capi.check(lib.sfem_gb300_linear_elasticity_apply(*args, capi.FLOAT32, capi.vp(ud), capi.vp(yd), None), "apply")
+    err = np.abs(yd.double().cpu().numpy() - ref) / _scale(L, el, adj, det, u)
+    assert err.max() < 2e-5, err.max()
+    if L == 16:
+        y64 = torch.zeros(3 * nn, dtype=torch.float64, device=cuda)
+        u64 = torch.from_numpy(u).to(cuda)
+        assert lib.sfem_gb300_linear_elasticity_apply(*args, capi.FLOAT64, capi.vp(u64), capi.vp(y64), None) == 1
+        assert "shared memory" in capi.last_error()
 
 
 @pytest.mark.parametrize("dtype_name,tol", [("float64", 1e-13), ("float32", 2e-5)])
@@ -152,7 +177,7 @@ def test_elasticity_reference_signature_and_fp32(cuda, fp32_kernel, shape):
         capi.vp(yd), capi.vp(yd), capi.vp(yd), None) == 1
 
 
-@pytest.mark.parametrize("L", [1, 2, 4])
+@pytest.mark.parametrize("L", [1, 2, 4, 8])
 def test_elasticity_block_diag(cuda, L):
     import torch
 

@@ -29,7 +29,8 @@ def _row_scale_lap(L, el, fff_aos, x):
     return np.abs(ax) + 2 * d * np.abs(x)
 
 
-@pytest.mark.parametrize("L,n", [(2, (3, 2, 2)), (3, (2, 3, 2)), (4, (3, 3, 2)), (6, (2, 2, 1)), (8, (1, 2, 2))])
+@pytest.mark.parametrize("L,n", [(2, (3, 2, 2)), (3, (2, 3, 2)), (4, (3, 3, 2)), (5, (2, 1, 2)), (6, (2, 2, 1)),
+                                 (8, (1, 2, 2)), (12, (1, 1, 2)), (16, (2, 1, 1))])
 def test_sshex8_laplacian_apply_fp64(cuda, L, n):
     import torch
 
@@ -51,9 +52,11 @@ def test_sshex8_laplacian_apply_fp64(cuda, L, n):
     assert err.max() < RTOL64, err.max()
 
 
-@pytest.mark.parametrize("L,n", [(2, (3, 2, 2)), (3, (3, 2, 2)), (4, (3, 2, 2)), (6, (2, 2, 1)), (8, (1, 2, 2))])
+@pytest.mark.parametrize("L,n", [(2, (3, 2, 2)), (3, (3, 2, 2)), (4, (3, 2, 2)), (6, (2, 2, 1)), (7, (1, 2, 1)),
+                                 (8, (1, 2, 2)), (16, (1, 1, 2))])
 def test_sshex8_laplacian_apply_fp32(cuda, L, n):
-    """The float apply with the default kernel of each level (L = 6, 8: warp kernel)."""
+    """The float apply with the default kernel of each level (L = 6, 8: warp kernel;
+    7, 16: CTA per element)."""
     import torch
 
     m = SSMesh(*n, L, perturb=0.1, seed=1)
@@ -212,7 +215,7 @@ def test_hex8_laplacian_apply_and_diag(cuda):
     assert np.abs(dd.cpu().numpy() - d_ref).max() <= 1e-13 * np.abs(d_ref).max()
 
 
-@pytest.mark.parametrize("L", [2, 3, 4])
+@pytest.mark.parametrize("L", [2, 3, 4, 5, 16])
 def test_sshex8_laplacian_diag(cuda, L):
     import torch
 
@@ -251,7 +254,7 @@ def test_empty_and_bad_inputs(cuda):
     assert lib.cu_laplacian_apply(capi.SSHEX8(4), capi.i64(0), sp.elements_ptrs.ptr, capi.i64(0), None,
                                   capi.FLOAT64, capi.vp(y), capi.vp(y), None) == 0
     # unsupported level: failure with a message, no abort
-    assert lib.cu_laplacian_apply(capi.SSHEX8(5), capi.i64(1), sp.elements_ptrs.ptr, capi.i64(1), None,
+    assert lib.cu_laplacian_apply(capi.SSHEX8(17), capi.i64(1), sp.elements_ptrs.ptr, capi.i64(1), None,
                                   capi.FLOAT64, capi.vp(y), capi.vp(y), None) == 1
     assert "unsupported" in capi.last_error()
     assert lib.cu_laplacian_apply(capi.SSHEX8(4), capi.i64(1), sp.elements_ptrs.ptr, capi.i64(1), None,

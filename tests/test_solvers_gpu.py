@@ -117,6 +117,31 @@ def test_sshex8_mg_pcg_fp64(cuda, smoother):
     _check_solution(apply, b, x.cpu().numpy(), x_star, rtol=1e-10, xtol=1e-7)
 
 
+def test_sshex8_L16_mg_pcg_fp64(cuda):
+    """Level 16 (hierarchy 16, 8, 4, 2, 1): the CTA-per-element apply at L = 16, the
+    transfers 16 <-> 8, and FP64 MG-PCG to the true residual 1e-10."""
+    import torch
+
+    L = 16
+    m = SSMesh(2, 2, 2, L, perturb=0.1, seed=5)
+    assert m.levels == [16, 8, 4, 2, 1]
+    H = S.Hierarchy(m, dirichlet_faces=("x0",), device=cuda)
+    fff = H.fff.cpu().numpy().T.copy()
+    dn = H.dirichlet[0].cpu().numpy()
+    apply, d = _oracle_poisson(m, L, fff, dn)
+    b = _rhs(m, L, dn, seed=6)
+    x_star, _ = OS.cg(apply, b, precond=lambda r: r / d, rtol=1e-14, max_it=20000)
+    ctx = S.context()
+    mg, op = S.build_poisson_mg(ctx, H, torch.float64, smoother="chebyshev3", sweeps=2)
+    solver = S.cg(ctx, op, mg, rtol=1e-11, max_it=100, residual_norm=True)
+    bd = torch.from_numpy(b).to(cuda)
+    x = torch.zeros_like(bd)
+    assert S.solve(solver, bd, x) == 0
+    it, _ = S.stats(solver)
+    assert it <= 30, it
+    _check_solution(apply, b, x.cpu().numpy(), x_star, rtol=1e-10, xtol=1e-7)
+
+
 @pytest.mark.parametrize("mixed", [False, True])
 def test_mg_with_macro_coarse_levels(cuda, mixed):
     """Poisson MG-PCG whose hierarchy continues below the macro mesh with plain hex8
@@ -278,6 +303,45 @@ def test_elasticity_mg_pcg_and_mixed(cuda, coarsen):
     assert S.solve(solver, bd, x3) == 0
     res3 = np.linalg.norm(b - apply(x3.cpu().numpy())) / np.linalg.norm(b)
     assert res3 < 1e-10, res3
+
+
+def test_elasticity_L8_mg(cuda):
+    """Level 8 elasticity (hierarchy 8, 4, 2, 1; CTA-per-element apply and runtime-level
+    block diagonal at L = 8): FP64 flexible MG-PCG and FP64 FCG over the FP32 multigrid,
+    both to the true residual 1e-10."""
+    import torch
+
+    L = 8
+    mu, lam = 1.0, 10.0
+    m = SSMesh(2, 1, 1, L, box=((0, 2), (0, 1), (0, 1)), perturb=0.05, seed=8)
+    H = S.Hierarchy(m, dirichlet_faces=("x0",), device=cuda, vec=3)
+    adj = H.adj.cpu().numpy().T.copy()
+    det = H.det.cpu().numpy().copy()
+    el = m.elements(L)
+    dn = H.dirichlet[0].cpu().numpy()
+    n = m.n_nodes(L)
+
+    def apply(u):
+        y = O.linear_elasticity_apply(L, el, adj, det, mu, lam, u)
+        for c in range(3):
+            y[3 * dn + c] = u[3 * dn + c]
+        return y
+
+    b = np.zeros(3 * n)
+    b[2::3] = -1.0
+    for c in range(3):
+        b[3 * dn + c] = 0
+    ctx = S.context()
+    mg, op = S.build_elasticity_mg(ctx, H, torch.float64, mu=mu, lam=lam)
+    bd = torch.from_numpy(b).to(cuda)
+    x = torch.zeros_like(bd)
+    assert S.solve(S.cg(ctx, op, mg, rtol=5e-11, max_it=300, residual_norm=True, flexible=True), bd, x) == 0
+    assert np.linalg.norm(b - apply(x.cpu().numpy())) / np.linalg.norm(b) < 1e-10
+    mg32, _ = S.build_elasticity_mg(ctx, H, torch.float32, mu=mu, lam=lam, eig_max=mg.eigs)
+    x2 = torch.zeros_like(bd)
+    fcg = S.cg(ctx, op, S.mixed_precond(ctx, mg32), rtol=5e-11, max_it=300, residual_norm=True, flexible=True)
+    assert S.solve(fcg, bd, x2) == 0
+    assert np.linalg.norm(b - apply(x2.cpu().numpy())) / np.linalg.norm(b) < 1e-10
 
 
 def test_cg_options_true_residual_and_check_every(cuda):
