@@ -99,6 +99,16 @@ int sfem_gb300_set_laplacian_kernel(int variant);
  * the result equals cu_laplacian_apply's on the same connectivity and FFF up to FP32
  * rounding order.  sfem_gb300_laplacian_status returns (and clears) 1 if a packed
  * apply gave up waiting for its bulk copy, else 0. */
+/* Stored element matrices (the reference's "ss:em" Laplacian,
+ * frontend/ops/sfem_SemiStructuredEMLaplacian.cpp:77-117: sshex8_laplacian_element_matrix,
+ * operators/sshex8/sshex8_laplacian.cpp:595-634, + sshex8_stencil_element_matrix_apply):
+ * em[e * 64 + i * 8 + j] = the micro element matrix of macro element e (FFF / L, hex8
+ * corner order) in real_type, and y += A x from them (any sshex8 level 1..16). */
+int sfem_gb300_sshex8_laplacian_element_matrix(int element_type, ptrdiff_t nelements, ptrdiff_t fff_stride,
+                                               const float *fff, int real_type, void *em, void *stream);
+int sfem_gb300_sshex8_laplacian_apply_em(int element_type, ptrdiff_t nelements, sfem_gb300_idx_t **elements,
+                                         const void *em, int real_type, const void *x, void *y, void *stream);
+
 ptrdiff_t sfem_gb300_sshex8_packed_bytes(int element_type, ptrdiff_t nelements);
 int sfem_gb300_sshex8_pack(int element_type, ptrdiff_t nelements, sfem_gb300_idx_t **elements, ptrdiff_t fff_stride,
                            const float *fff, void *packed, void *stream);

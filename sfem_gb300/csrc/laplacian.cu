@@ -139,7 +139,7 @@ template <typename T, int L>
 __global__ void __launch_bounds__(128) sshex8_laplacian_apply_warp_kernel(ptrdiff_t nelements,
                                                                           const idx_t *const *elements,
                                                                           ptrdiff_t fff_stride, const float *fff,
-                                                                          const T *x, T *y) {
+                                                                          const T *x, T *y, const T *Ag = nullptr) {
     constexpr int N1 = L + 1;
     constexpr int NXE = N1 * N1 * N1;
     constexpr int NM = L * L * L;
@@ -158,17 +158,22 @@ __global__ void __launch_bounds__(128) sshex8_laplacian_apply_warp_kernel(ptrdif
     __syncthreads();
 
     for (ptrdiff_t e = (ptrdiff_t)blockIdx.x * WPB + warp; e < nelements; e += (ptrdiff_t)gridDim.x * WPB) {
-        T f = 0;
-        if (lane < 6) f = (T)fff[lane * fff_stride + e] * h;
-        T sub[6];
+        if (Ag) {
+            // stored micro element matrix of this macro element (row-major 8 x 8)
+            for (int k = lane; k < 64; k += 32) Aw[k] = Ag[64 * e + k];
+        } else {
+            T f = 0;
+            if (lane < 6) f = (T)fff[lane * fff_stride + e] * h;
+            T sub[6];
 #pragma unroll
-        for (int m = 0; m < 6; m++) sub[m] = __shfl_sync(0xffffffffu, f, m);
+            for (int m = 0; m < 6; m++) sub[m] = __shfl_sync(0xffffffffu, f, m);
 #pragma unroll
-        for (int k = lane; k < 64; k += 32) {
-            T a = 0;
+            for (int k = lane; k < 64; k += 32) {
+                T a = 0;
 #pragma unroll
-            for (int m = 0; m < 6; m++) a += sub[m] * Wt[k * 6 + m];
-            Aw[k] = a;
+                for (int m = 0; m < 6; m++) a += sub[m] * Wt[k * 6 + m];
+                Aw[k] = a;
+            }
         }
 
         idx_t gi[NR];
@@ -924,7 +929,7 @@ template <typename T>
 __global__ void __launch_bounds__(256) sshex8_laplacian_apply_cta_kernel(int L, ptrdiff_t nelements,
                                                                          const idx_t *const *elements,
                                                                          ptrdiff_t fff_stride, const float *fff,
-                                                                         const T *x, T *y) {
+                                                                         const T *x, T *y, const T *Ag = nullptr) {
     extern __shared__ __align__(16) unsigned char lap_cta_smem[];
     const int N1 = L + 1, NXE = N1 * N1 * N1, NM = L * L * L;
     T *xs = reinterpret_cast<T *>(lap_cta_smem);
@@ -934,7 +939,10 @@ __global__ void __launch_bounds__(256) sshex8_laplacian_apply_cta_kernel(int L, 
     for (ptrdiff_t e = blockIdx.x; e < nelements; e += gridDim.x) {
         if (threadIdx.x < 64) {
             T a = 0;
-            for (int m = 0; m < 6; m++) a += (T)fff[m * fff_stride + e] * h * lap_w<T>(threadIdx.x, m);
+            if (Ag)
+                a = Ag[64 * e + threadIdx.x];
+            else
+                for (int m = 0; m < 6; m++) a += (T)fff[m * fff_stride + e] * h * lap_w<T>(threadIdx.x, m);
             As[threadIdx.x] = a;
         }
         for (int l = threadIdx.x; l < NXE; l += blockDim.x) {
@@ -1011,7 +1019,7 @@ __global__ void __launch_bounds__(128) sshex8_laplacian_diag_any_kernel(int L, p
 
 template <typename T>
 static int launch_lap_cta(int L, ptrdiff_t nelements, idx_t **elements, ptrdiff_t fff_stride, const float *fff,
-                          const T *x, T *y, cudaStream_t s) {
+                          const T *x, T *y, cudaStream_t s, const T *Ag = nullptr) {
     const size_t smem = (2 * (size_t)(L + 1) * (L + 1) * (L + 1) + 64) * sizeof(T);
     static size_t attr = 0;  // largest shared-memory opt-in so far (per T)
     if (smem > 48 * 1024 && smem > attr) {
@@ -1020,7 +1028,7 @@ static int launch_lap_cta(int L, ptrdiff_t nelements, idx_t **elements, ptrdiff_
         attr = smem;
     }
     const int grid = (int)std::min<ptrdiff_t>(nelements, (ptrdiff_t)kNumSMs * 8);
-    sshex8_laplacian_apply_cta_kernel<T><<<grid, 256, smem, s>>>(L, nelements, elements, fff_stride, fff, x, y);
+    sshex8_laplacian_apply_cta_kernel<T><<<grid, 256, smem, s>>>(L, nelements, elements, fff_stride, fff, x, y, Ag);
     return check_launch("cu_laplacian_apply(SSHEX8, CTA per element)");
 }
 
@@ -1316,4 +1324,88 @@ extern "C" int sfem_gb300_laplacian_status(void) {
         cudaMemcpyToSymbol(g_lap_status, &zero, sizeof(int));
     }
     return st;
+}
+
+// ------------------------------------------------------------------ stored element matrices
+
+// em[e][i][j] = A_ij of the micro elements of macro element e (metric / L), row-major 8 x 8
+// in hex8 corner order (the layout of sshex8_laplacian_element_matrix's `values`).
+template <typename T>
+__global__ void sshex8_laplacian_element_matrix_kernel(ptrdiff_t nelements, int L, ptrdiff_t fff_stride,
+                                                       const float *fff, T *em) {
+    const T h = T(1) / T(L);
+    for (ptrdiff_t t = (ptrdiff_t)blockIdx.x * blockDim.x + threadIdx.x; t < nelements * 64;
+         t += (ptrdiff_t)gridDim.x * blockDim.x) {
+        const ptrdiff_t e = t / 64;
+        const int k = (int)(t % 64);
+        T a = 0;
+        for (int m = 0; m < 6; m++) a += (T)fff[m * fff_stride + e] * h * lap_w<T>(k, m);
+        em[t] = a;
+    }
+}
+
+template <typename T>
+static int laplacian_apply_em_tpl(int L, ptrdiff_t nelements, idx_t **elements, const T *em, const T *x, T *y,
+                                  cudaStream_t s) {
+    const int blocks = grid_for((nelements + 3) / 4, 1, kNumSMs * 64);
+#define SFEM_LAP_EM_CASE(LL)                                                                                   \
+    case LL:                                                                                                   \
+        sshex8_laplacian_apply_warp_kernel<T, LL><<<blocks, 128, 0, s>>>(nelements, elements, 0, nullptr, x, y, em); \
+        return check_launch("sfem_gb300_sshex8_laplacian_apply_em");
+    switch (L) {
+        SFEM_LAP_EM_CASE(1)
+        SFEM_LAP_EM_CASE(2)
+        SFEM_LAP_EM_CASE(3)
+        SFEM_LAP_EM_CASE(4)
+        SFEM_LAP_EM_CASE(6)
+        SFEM_LAP_EM_CASE(8)
+        default:
+            return launch_lap_cta<T>(L, nelements, elements, 0, nullptr, x, y, s, em);
+    }
+#undef SFEM_LAP_EM_CASE
+}
+
+extern "C" int sfem_gb300_sshex8_laplacian_element_matrix(int element_type, ptrdiff_t nelements, ptrdiff_t fff_stride,
+                                                          const float *fff, int real_type, void *em, void *stream) {
+    const int L = element_type - SFEM_GB300_SSHEX8_BASE;
+    if (L < 1 || L > LAP_MAX_L)
+        return set_error("sfem_gb300_sshex8_laplacian_element_matrix: unsupported element type %d", element_type);
+    if (nelements <= 0) return SFEM_GB300_SUCCESS;
+    const cudaStream_t s = stream_of(stream);
+    const int grid = grid_for(nelements * 64, 256);
+    switch (real_type) {
+        case SFEM_GB300_REAL_DEFAULT:
+        case SFEM_GB300_FLOAT64:
+            sshex8_laplacian_element_matrix_kernel<double><<<grid, 256, 0, s>>>(nelements, L, fff_stride, fff,
+                                                                                 (double *)em);
+            break;
+        case SFEM_GB300_FLOAT32:
+            sshex8_laplacian_element_matrix_kernel<float><<<grid, 256, 0, s>>>(nelements, L, fff_stride, fff,
+                                                                                (float *)em);
+            break;
+        default:
+            return set_error("sfem_gb300_sshex8_laplacian_element_matrix: unsupported real type %d", real_type);
+    }
+    return check_launch("sfem_gb300_sshex8_laplacian_element_matrix");
+}
+
+extern "C" int sfem_gb300_sshex8_laplacian_apply_em(int element_type, ptrdiff_t nelements, idx_t **elements,
+                                                    const void *em, int real_type, const void *x, void *y,
+                                                    void *stream) {
+    const int L = element_type - SFEM_GB300_SSHEX8_BASE;
+    if (L < 1 || L > LAP_MAX_L)
+        return set_error("sfem_gb300_sshex8_laplacian_apply_em: unsupported element type %d", element_type);
+    if (nelements <= 0) return SFEM_GB300_SUCCESS;
+    const cudaStream_t s = stream_of(stream);
+    switch (real_type) {
+        case SFEM_GB300_REAL_DEFAULT:
+        case SFEM_GB300_FLOAT64:
+            return laplacian_apply_em_tpl<double>(L, nelements, elements, (const double *)em, (const double *)x,
+                                                  (double *)y, s);
+        case SFEM_GB300_FLOAT32:
+            return laplacian_apply_em_tpl<float>(L, nelements, elements, (const float *)em, (const float *)x,
+                                                 (float *)y, s);
+        default:
+            return set_error("sfem_gb300_sshex8_laplacian_apply_em: unsupported real type %d", real_type);
+    }
 }

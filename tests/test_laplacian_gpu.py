@@ -259,3 +259,35 @@ def test_empty_and_bad_inputs(cuda):
     assert "unsupported" in capi.last_error()
     assert lib.cu_laplacian_apply(capi.SSHEX8(4), capi.i64(1), sp.elements_ptrs.ptr, capi.i64(1), None,
                                   7, capi.vp(y), capi.vp(y), None) == 1
+
+
+@pytest.mark.parametrize("dtype_name,tol", [("float64", 1e-13), ("float32", 2e-5)])
+@pytest.mark.parametrize("L,n", [(1, (3, 2, 2)), (4, (3, 2, 2)), (5, (2, 1, 1)), (8, (1, 2, 1))])
+def test_sshex8_laplacian_stored_element_matrices(cuda, dtype_name, tol, L, n):
+    """ss:em form: the stored 8 x 8 micro element matrices equal the oracle's, and the
+    apply from them equals the oracle apply."""
+    import torch
+
+    dt = getattr(torch, dtype_name)
+    rt = capi.FLOAT64 if dt == torch.float64 else capi.FLOAT32
+    m = SSMesh(*n, L, perturb=0.1, seed=3)
+    sp = SSMeshDevice(m, L)
+    el = m.elements(L)
+    fff_aos = O.fff_fill(el[m.macro_corner_lidx(L)], m.points)
+    E = m.n_elements
+    fff = torch.from_numpy(fff_aos.T.copy()).to(cuda)
+    lib = capi.load()
+    em = torch.empty(E * 64, dtype=dt, device=cuda)
+    capi.check(lib.sfem_gb300_sshex8_laplacian_element_matrix(capi.SSHEX8(L), capi.i64(E), capi.i64(E), capi.vp(fff),
+                                                              rt, capi.vp(em), None), "element matrices")
+    ref_em = np.stack([O.laplacian_matrix(fff_aos[e].astype(np.float64) / L).reshape(64) for e in range(E)])
+    assert np.abs(em.double().cpu().numpy().reshape(E, 64) - ref_em).max() <= (1e-14 if tol < 1e-10 else 1e-6) * np.abs(ref_em).max()
+    x = np.random.default_rng(11).standard_normal(m.n_nodes(L))
+    ref = O.sshex8_laplacian_apply(L, el, fff_aos, x) if L > 1 else O.hex8_laplacian_apply(m.hex8_elements(), fff_aos, x)
+    y = torch.zeros(m.n_nodes(L), dtype=dt, device=cuda)
+    elp = sp.elements_ptrs if L > 1 else capi.DevicePtrArray(torch.from_numpy(np.ascontiguousarray(el)).to(cuda))
+    capi.check(lib.sfem_gb300_sshex8_laplacian_apply_em(capi.SSHEX8(L), capi.i64(E), elp.ptr, capi.vp(em), rt,
+                                                        capi.vp(torch.from_numpy(x).to(dt).to(cuda)), capi.vp(y), None),
+               "apply_em")
+    scale = _row_scale_lap(L, el if L > 1 else m.hex8_elements(), fff_aos, x)
+    assert (np.abs(y.double().cpu().numpy() - ref) / scale).max() < tol
