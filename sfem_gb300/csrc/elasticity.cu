@@ -13,6 +13,8 @@
 
 #include <algorithm>
 #include <cstdlib>
+#include <atomic>
+#include <mutex>
 
 #include "common.cuh"
 #include "tcgen05.cuh"
@@ -960,10 +962,10 @@ static int launch_el_cta(int L, ptrdiff_t nelements, idx_t **elements, ptrdiff_t
     if (smem > 227 * 1024)
         return set_error("sfem_gb300_linear_elasticity_apply: level %d needs %zu bytes of shared memory in %s", L,
                          smem, sizeof(T) == 8 ? "FP64" : "FP32");
-    static size_t attr = 0;  // largest shared-memory opt-in so far (per T)
-    if (smem > 48 * 1024 && smem > attr) {
+    static std::atomic<size_t> attr{0};  // largest shared-memory opt-in so far (per T)
+    if (smem > 48 * 1024 && smem > attr.load(std::memory_order_relaxed)) {
         cudaFuncSetAttribute(elasticity_apply_cta_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        attr = smem;
+        attr.store(smem, std::memory_order_relaxed);  // a racing caller at worst repeats the opt-in
     }
     const int grid = (int)std::min<ptrdiff_t>(nelements, (ptrdiff_t)kNumSMs * 8);
     elasticity_apply_cta_kernel<T><<<grid, 256, smem, s>>>(L, nelements, elements, stride, adj, det, mu, lambda, x, y);
@@ -974,11 +976,10 @@ static int g_elasticity_kernel = -1;  // -1 default (tcgen05 at L = 4), 0 SIMT w
 
 static int elasticity_apply_tf32x3(ptrdiff_t nelements, idx_t **elements, ptrdiff_t stride, const float *adj,
                                    const float *det, float mu, float lambda, const float *x, float *y, cudaStream_t s) {
-    static bool attr = false;
-    if (!attr) {
+    static std::once_flag attr;
+    std::call_once(attr, [] {
         cudaFuncSetAttribute(elasticity_apply_tf32x3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, ETC_SMEM);
-        attr = true;
-    }
+    });
     const ptrdiff_t pairs = (nelements + 1) / 2;
     const int grid = (int)std::min<ptrdiff_t>(pairs, (ptrdiff_t)kNumSMs * ETC_CTAS_PER_SM);
     elasticity_apply_tf32x3_kernel<<<grid, 128, ETC_SMEM, s>>>(nelements, elements, stride, adj, det, mu, lambda, x, y);

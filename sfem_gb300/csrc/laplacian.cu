@@ -8,6 +8,8 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstdlib>
+#include <atomic>
+#include <mutex>
 
 #include "common.cuh"
 #include "laplacian_kernels.cuh"
@@ -1040,11 +1042,11 @@ template <typename T>
 static int launch_lap_cta(int L, ptrdiff_t nelements, idx_t **elements, ptrdiff_t fff_stride, const float *fff,
                           const T *x, T *y, cudaStream_t s, const T *Ag = nullptr) {
     const size_t smem = (2 * (size_t)(L + 1) * (L + 1) * (L + 1) + 64) * sizeof(T);
-    static size_t attr = 0;  // largest shared-memory opt-in so far (per T)
-    if (smem > 48 * 1024 && smem > attr) {
+    static std::atomic<size_t> attr{0};  // largest shared-memory opt-in so far (per T)
+    if (smem > 48 * 1024 && smem > attr.load(std::memory_order_relaxed)) {
         cudaFuncSetAttribute(sshex8_laplacian_apply_cta_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smem);
-        attr = smem;
+        attr.store(smem, std::memory_order_relaxed);  // a racing caller at worst repeats the opt-in
     }
     const int grid = (int)std::min<ptrdiff_t>(nelements, (ptrdiff_t)kNumSMs * 8);
     sshex8_laplacian_apply_cta_kernel<T><<<grid, 256, smem, s>>>(L, nelements, elements, fff_stride, fff, x, y, Ag);
@@ -1350,12 +1352,11 @@ static int sshex8_apply_packed_impl(int element_type, ptrdiff_t nelements, const
     constexpr int NXE = (PK_L + 1) * (PK_L + 1) * (PK_L + 1);
     constexpr size_t smem = ((size_t)pk_words(PK_L) + (size_t)NXE * PK_TILE + (size_t)(PK_L + 1) * (PK_L + 1) * PK_TILE) *
                             sizeof(float);
-    static bool attr = false;  // shared-memory opt-in, once
-    if (!attr) {
+    static std::once_flag attr;  // shared-memory opt-in, once
+    std::call_once(attr, [] {
         cudaFuncSetAttribute(sshex8_laplacian_apply_packed_kernel<PK_L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smem);
-        attr = true;
-    }
+    });
     sshex8_laplacian_apply_packed_kernel<PK_L><<<(unsigned)ntiles, 2 * PK_TILE, smem, stream_of(stream)>>>(
             nelements, (const int32_t *)packed, (const float *)x, (float *)y, n_constrained, constrained);
     return check_launch("sfem_gb300_sshex8_laplacian_apply_packed");
