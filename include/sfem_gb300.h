@@ -116,18 +116,6 @@ int sfem_gb300_sshex8_laplacian_apply_packed(int element_type, ptrdiff_t nelemen
                                              int real_type_xy, const void *x, void *y, void *stream);
 int sfem_gb300_laplacian_status(void);
 
-/* Function-level form with Dirichlet rows fused (frontend/sfem_Function.cpp:481-496:
- * apply, then copy_constrained_dofs): pack_constrained marks the ids of the n_constrained
- * nodes (device array, ids < n_nodes) in the blocks; apply_packed_constrained skips their
- * element contributions and writes y[c] = x[c] in the same launch (y += A x elsewhere). */
-int sfem_gb300_sshex8_pack_constrained(int element_type, ptrdiff_t nelements, sfem_gb300_idx_t **elements,
-                                       ptrdiff_t fff_stride, const float *fff, ptrdiff_t n_nodes,
-                                       ptrdiff_t n_constrained, const sfem_gb300_idx_t *constrained, void *packed,
-                                       void *stream);
-int sfem_gb300_sshex8_laplacian_apply_packed_constrained(int element_type, ptrdiff_t nelements, const void *packed,
-                                                         ptrdiff_t n_constrained, const sfem_gb300_idx_t *constrained,
-                                                         int real_type_xy, const void *x, void *y, void *stream);
-
 /* ------------------------------------------------------- linear elasticity */
 
 /* out += K u for the affine hex8 / sshex8 linear-elasticity operator with

@@ -757,11 +757,8 @@ __host__ __device__ constexpr int pk_words(int L) { return PK_TILE * ((L + 1) * 
 constexpr int LAP_WAIT_POLLS = 1 << 20;
 __device__ int g_lap_status;  // nonzero: a bulk-copy wait gave up
 
-// constrained (optional, one byte per node): ids of constrained nodes get the sign bit
-// (PK_CONSTRAINED), which the apply masks off for the gather and skips in the scatter
-constexpr uint32_t PK_CONSTRAINED = 0x80000000u;
 __global__ void sshex8_pack_kernel(ptrdiff_t nelements, int nxe, const idx_t *const *elements, ptrdiff_t fff_stride,
-                                   const float *fff, const uint8_t *constrained, int32_t *packed) {
+                                   const float *fff, int32_t *packed) {
     const int words = PK_TILE * (nxe + 6);
     const ptrdiff_t total = (nelements + PK_TILE - 1) / PK_TILE * words;
     for (ptrdiff_t g = (ptrdiff_t)blockIdx.x * blockDim.x + threadIdx.x; g < total;
@@ -770,21 +767,11 @@ __global__ void sshex8_pack_kernel(ptrdiff_t nelements, int nxe, const idx_t *co
         const int w = (int)(g - t * words);
         const ptrdiff_t e = t * PK_TILE + w % PK_TILE;
         int32_t val = 0;
-        if (e < nelements) {
-            if (w < PK_TILE * nxe) {
-                val = elements[w / PK_TILE][e];
-                if (constrained && constrained[val]) val = (int32_t)((uint32_t)val | PK_CONSTRAINED);
-            } else {
-                val = __float_as_int(fff[(w / PK_TILE - nxe) * fff_stride + e]);
-            }
-        }
+        if (e < nelements)
+            val = w < PK_TILE * nxe ? elements[w / PK_TILE][e]
+                                    : __float_as_int(fff[(w / PK_TILE - nxe) * fff_stride + e]);
         packed[g] = val;
     }
-}
-
-__global__ void mark_nodes_kernel(ptrdiff_t n, const idx_t *nodes, uint8_t *mask) {
-    for (ptrdiff_t i = (ptrdiff_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (ptrdiff_t)gridDim.x * blockDim.x)
-        mask[nodes[i]] = 1;
 }
 
 // Rows 0..3 of the micro element matrix (packed by pairs) from the macro metric f
@@ -815,7 +802,7 @@ __device__ __forceinline__ void lap_A2_from_metric(const float (&f)[6], float2 (
 template <int L>
 __global__ void __launch_bounds__(2 * PK_TILE, 6) sshex8_laplacian_apply_packed_kernel(
         ptrdiff_t nelements, const int32_t *__restrict__ packed, const float *__restrict__ x,
-        float *__restrict__ y, ptrdiff_t n_constrained, const idx_t *__restrict__ constrained) {
+        float *__restrict__ y) {
     constexpr int N1 = L + 1;
     constexpr int NP = N1 * N1;
     constexpr int NXE = NP * N1;
@@ -846,7 +833,7 @@ __global__ void __launch_bounds__(2 * PK_TILE, 6) sshex8_laplacian_apply_packed_
     const int nvalid = (int)((nelements - t * PK_TILE) < PK_TILE ? (nelements - t * PK_TILE) : PK_TILE);
     // 1. gather x
     for (int i = tid; i < NXE * PK_TILE; i += 2 * PK_TILE)
-        if (i % PK_TILE < nvalid) cp_async4(&sx[i], x + (sidx[i] & 0x7fffffff));
+        if (i % PK_TILE < nvalid) cp_async4(&sx[i], x + sidx[i]);
     const int el = tid % PK_TILE;
     const int half = tid / PK_TILE;  // warp-uniform layer group
     float2 A2[8][2];
@@ -891,13 +878,7 @@ __global__ void __launch_bounds__(2 * PK_TILE, 6) sshex8_laplacian_apply_packed_
     __syncthreads();
     // 3. scatter
     for (int i = tid; i < NXE * PK_TILE; i += 2 * PK_TILE)
-        if (i % PK_TILE < nvalid && sidx[i] >= 0) atomicAdd(&y[sidx[i]], sx[i]);
-    // constrained rows: y[c] = x[c] (their element contributions were skipped above)
-    for (ptrdiff_t c = (ptrdiff_t)blockIdx.x * (2 * PK_TILE) + tid; c < n_constrained;
-         c += (ptrdiff_t)gridDim.x * (2 * PK_TILE)) {
-        const idx_t g = constrained[c];
-        y[g] = x[g];
-    }
+        if (i % PK_TILE < nvalid) atomicAdd(&y[sidx[i]], sx[i]);
 }
 
 // Diagonal: node value = sum over the micro elements of this macro element that
@@ -1298,47 +1279,21 @@ extern "C" ptrdiff_t sfem_gb300_sshex8_packed_bytes(int element_type, ptrdiff_t 
     return (nelements + PK_TILE - 1) / PK_TILE * (ptrdiff_t)pk_words(PK_L) * (ptrdiff_t)sizeof(int32_t);
 }
 
-static int sshex8_pack_impl(int element_type, ptrdiff_t nelements, idx_t **elements, ptrdiff_t fff_stride,
-                            const float *fff, ptrdiff_t n_nodes, ptrdiff_t n_constrained, const idx_t *constrained,
-                            void *packed, void *stream) {
+extern "C" int sfem_gb300_sshex8_pack(int element_type, ptrdiff_t nelements, idx_t **elements, ptrdiff_t fff_stride,
+                                      const float *fff, void *packed, void *stream) {
     if (element_type != SFEM_GB300_SSHEX8(PK_L))
         return set_error("sfem_gb300_sshex8_pack: element type %d is not sshex8 L = %d", element_type, PK_L);
     if (nelements <= 0) return SFEM_GB300_SUCCESS;
     if (reinterpret_cast<uintptr_t>(packed) & 15) return set_error("sfem_gb300_sshex8_pack: packed is not 16-byte aligned");
-    const cudaStream_t s = stream_of(stream);
-    uint8_t *mask = nullptr;
-    if (n_constrained > 0) {
-        if (n_nodes <= 0) return set_error("sfem_gb300_sshex8_pack_constrained: n_nodes must be positive");
-        if (cudaMallocAsync((void **)&mask, (size_t)n_nodes, s) != cudaSuccess)
-            return set_error("sfem_gb300_sshex8_pack_constrained: cannot allocate the node mask");
-        cudaMemsetAsync(mask, 0, (size_t)n_nodes, s);
-        mark_nodes_kernel<<<grid_for(n_constrained, 256), 256, 0, s>>>(n_constrained, constrained, mask);
-    }
     constexpr int nxe = (PK_L + 1) * (PK_L + 1) * (PK_L + 1);
     const ptrdiff_t total = (nelements + PK_TILE - 1) / PK_TILE * (ptrdiff_t)pk_words(PK_L);
-    sshex8_pack_kernel<<<grid_for(total, 256), 256, 0, s>>>(nelements, nxe, elements, fff_stride, fff, mask,
-                                                           (int32_t *)packed);
-    const int rc = check_launch("sfem_gb300_sshex8_pack");
-    if (mask) cudaFreeAsync(mask, s);
-    return rc;
+    sshex8_pack_kernel<<<grid_for(total, 256), 256, 0, stream_of(stream)>>>(nelements, nxe, elements, fff_stride, fff,
+                                                                           (int32_t *)packed);
+    return check_launch("sfem_gb300_sshex8_pack");
 }
 
-extern "C" int sfem_gb300_sshex8_pack(int element_type, ptrdiff_t nelements, idx_t **elements, ptrdiff_t fff_stride,
-                                      const float *fff, void *packed, void *stream) {
-    return sshex8_pack_impl(element_type, nelements, elements, fff_stride, fff, 0, 0, nullptr, packed, stream);
-}
-
-extern "C" int sfem_gb300_sshex8_pack_constrained(int element_type, ptrdiff_t nelements, idx_t **elements,
-                                                  ptrdiff_t fff_stride, const float *fff, ptrdiff_t n_nodes,
-                                                  ptrdiff_t n_constrained, const idx_t *constrained, void *packed,
-                                                  void *stream) {
-    return sshex8_pack_impl(element_type, nelements, elements, fff_stride, fff, n_nodes, n_constrained, constrained,
-                            packed, stream);
-}
-
-static int sshex8_apply_packed_impl(int element_type, ptrdiff_t nelements, const void *packed,
-                                    ptrdiff_t n_constrained, const idx_t *constrained, int real_type_xy,
-                                    const void *x, void *y, void *stream) {
+extern "C" int sfem_gb300_sshex8_laplacian_apply_packed(int element_type, ptrdiff_t nelements, const void *packed,
+                                                        int real_type_xy, const void *x, void *y, void *stream) {
     if (element_type != SFEM_GB300_SSHEX8(PK_L))
         return set_error("sfem_gb300_sshex8_laplacian_apply_packed: element type %d is not sshex8 L = %d",
                          element_type, PK_L);
@@ -1358,21 +1313,8 @@ static int sshex8_apply_packed_impl(int element_type, ptrdiff_t nelements, const
                              (int)smem);
     });
     sshex8_laplacian_apply_packed_kernel<PK_L><<<(unsigned)ntiles, 2 * PK_TILE, smem, stream_of(stream)>>>(
-            nelements, (const int32_t *)packed, (const float *)x, (float *)y, n_constrained, constrained);
+            nelements, (const int32_t *)packed, (const float *)x, (float *)y);
     return check_launch("sfem_gb300_sshex8_laplacian_apply_packed");
-}
-
-extern "C" int sfem_gb300_sshex8_laplacian_apply_packed(int element_type, ptrdiff_t nelements, const void *packed,
-                                                        int real_type_xy, const void *x, void *y, void *stream) {
-    return sshex8_apply_packed_impl(element_type, nelements, packed, 0, nullptr, real_type_xy, x, y, stream);
-}
-
-extern "C" int sfem_gb300_sshex8_laplacian_apply_packed_constrained(int element_type, ptrdiff_t nelements,
-                                                                    const void *packed, ptrdiff_t n_constrained,
-                                                                    const idx_t *constrained, int real_type_xy,
-                                                                    const void *x, void *y, void *stream) {
-    return sshex8_apply_packed_impl(element_type, nelements, packed, n_constrained, constrained, real_type_xy, x, y,
-                                    stream);
 }
 
 extern "C" int sfem_gb300_laplacian_status(void) {

@@ -37,15 +37,12 @@ public:
         const ptrdiff_t nb = sfem_gb300_sshex8_packed_bytes(element_type, nelements);
         if (nb <= 0) return 0;
         SFEM_GB300_CHECK(packed.resize(nb / (ptrdiff_t)sizeof(int32_t)));
-        return sfem_gb300_sshex8_pack_constrained(element_type, nelements, elements, fff_stride, fff, n_nodes,
-                                                  n_dirichlet, dirichlet, packed.ptr, ctx->sp());
+        return sfem_gb300_sshex8_pack(element_type, nelements, elements, fff_stride, fff, packed.ptr, ctx->sp());
     }
     int apply(const T *x, T *y) override {
         if (packed.n > 0) {
-            // Dirichlet rows fused into the apply (contributions skipped, y[c] = x[c])
-            return sfem_gb300_sshex8_laplacian_apply_packed_constrained(element_type, nelements, packed.ptr,
-                                                                        n_dirichlet, dirichlet, real_type_v<T>, x, y,
-                                                                        ctx->sp());
+            SFEM_GB300_CHECK(sfem_gb300_sshex8_laplacian_apply_packed(element_type, nelements, packed.ptr,
+                                                                      real_type_v<T>, x, y, ctx->sp()));
         } else {
             SFEM_GB300_CHECK(cu_laplacian_apply(element_type, nelements, elements, fff_stride, fff, real_type_v<T>, x,
                                                 y, ctx->sp()));

@@ -291,44 +291,3 @@ def test_sshex8_laplacian_stored_element_matrices(cuda, dtype_name, tol, L, n):
                "apply_em")
     scale = _row_scale_lap(L, el if L > 1 else m.hex8_elements(), fff_aos, x)
     assert (np.abs(y.double().cpu().numpy() - ref) / scale).max() < tol
-
-
-def test_sshex8_laplacian_packed_constrained(cuda):
-    """Dirichlet rows fused into the packed apply: y = y0 + A x on free rows, y[c] = x[c]
-    on constrained rows (apply + copy_constrained_dofs), element count 60 (ragged tile)."""
-    import torch
-
-    L = 4
-    m = SSMesh(5, 4, 3, L, perturb=0.1, seed=12)
-    sp = SSMeshDevice(m, L)
-    el = m.elements(L)
-    E = m.n_elements
-    n = m.n_nodes(L)
-    fff_aos = O.fff_fill(el[m.macro_corner_lidx(L)], m.points)
-    fff = torch.from_numpy(fff_aos.T.copy()).to(cuda)
-    dn = np.unique(np.concatenate([m.boundary_nodes("x0", L), m.boundary_nodes("z1", L)])).astype(np.int32)
-    dd = torch.from_numpy(dn).to(cuda)
-    lib = capi.load()
-    packed = torch.empty(lib.sfem_gb300_sshex8_packed_bytes(capi.SSHEX8(L), capi.i64(E)) // 4, dtype=torch.int32,
-                         device=cuda)
-    capi.check(lib.sfem_gb300_sshex8_pack_constrained(capi.SSHEX8(L), capi.i64(E), sp.elements_ptrs.ptr, capi.i64(E),
-                                                      capi.vp(fff), capi.i64(n), capi.i64(dn.size), capi.vp(dd),
-                                                      capi.vp(packed), None), "pack_constrained")
-    ids = packed.view(-1, 32 * (el.shape[0] + 6))[:, :32 * el.shape[0]].cpu().numpy()
-    marked = np.unique(ids[ids < 0] & 0x7FFFFFFF)
-    assert np.array_equal(marked, dn)
-    rng = np.random.default_rng(13)
-    x = rng.standard_normal(n)
-    y0 = rng.standard_normal(n)
-    ref = O.sshex8_laplacian_apply(L, el, fff_aos, x, out=y0.copy())
-    ref[dn] = x[dn]
-    xd = torch.from_numpy(x).float().to(cuda)
-    yd = torch.from_numpy(y0).float().to(cuda)
-    capi.check(lib.sfem_gb300_sshex8_laplacian_apply_packed_constrained(
-        capi.SSHEX8(L), capi.i64(E), capi.vp(packed), capi.i64(dn.size), capi.vp(dd), capi.FLOAT32, capi.vp(xd),
-        capi.vp(yd), None), "apply_packed_constrained")
-    got = yd.double().cpu().numpy()
-    assert np.array_equal(got[dn], xd.double().cpu().numpy()[dn])
-    free = np.setdiff1d(np.arange(n), dn)
-    scale = _row_scale_lap(L, el, fff_aos, x) + np.abs(y0)
-    assert (np.abs(got - ref) / scale)[free].max() < RTOL32
