@@ -60,6 +60,32 @@ def main():
         x_level1=x1, prolongate_1_2=hprol, count_2=cnt2, restrict_2_1=hrest, hex8_elements=h8,
         hex8_laplacian_apply=hlap, laplacian_matrix_e0=A, elasticity_matrix_e0=K)
     print("wrote", OUT / "sshex8_L4_2x2x1.npz")
+    # levels without a compile-time GPU kernel: Laplacian and elasticity at L = 5, 12, 16,
+    # transfers between 8 and 16
+    out = {}
+    for L, n, seed in ((5, (2, 1, 1), 21), (12, (1, 1, 1), 22), (16, (1, 1, 1), 23)):
+        m = SSMesh(*n, L, box=((0, n[0]), (0, 1), (0, 1)), perturb=0.15, seed=seed)
+        el = m.elements(L)
+        corners = el[m.macro_corner_lidx(L)]
+        fff = O.fff_fill(corners, m.points, use_ref=True)
+        adj, det = O.adjugate_fill(corners, m.points, use_ref=True)
+        nn = m.n_nodes(L)
+        x = rng.standard_normal(nn)
+        u = rng.standard_normal(3 * nn)
+        out.update({f"L{L}_elements": el, f"L{L}_points": m.points, f"L{L}_fff": fff, f"L{L}_adjugate": adj,
+                    f"L{L}_determinant": det, f"L{L}_x": x, f"L{L}_u": u,
+                    f"L{L}_laplacian_apply": O.sshex8_laplacian_apply(L, el, fff, x, use_ref=True),
+                    f"L{L}_elasticity_apply": O.linear_elasticity_apply(L, el, adj, det, 1.0, 10.0, u, use_ref=True)})
+        if L == 16:
+            e8 = m.elements(8)
+            n8 = m.n_nodes(8)
+            x8 = rng.standard_normal(n8)
+            cnt = O.incidence_count(16, el, nn, use_ref=True)
+            out.update({"L16_elements8": e8, "L16_x8": x8,
+                        "L16_prolongate_8_16": O.prolongate(8, e8, 16, el, 1, x8, nn, use_ref=True),
+                        "L16_restrict_16_8": O.restrict(16, el, cnt, 8, e8, 1, x, n8, use_ref=True)})
+    np.savez_compressed(OUT / "sshex8_high_levels.npz", mu=1.0, lam=10.0, **out)
+    print("wrote", OUT / "sshex8_high_levels.npz")
 
 
 if __name__ == "__main__":

@@ -190,3 +190,29 @@ def test_float32_configuration_apply():
     assert np.abs(a - b).max() <= 1e-5 * np.abs(a).max()
     zb = O.sshex8_laplacian_apply_f32(L, el, fff, z)
     assert abs(float(z.astype(np.float32) @ b) - float(x.astype(np.float32) @ zb)) <= 1e-4 * abs(float(z @ a))
+
+
+HIGH = Path(__file__).resolve().parent / "golden" / "sshex8_high_levels.npz"
+
+
+@pytest.mark.parametrize("L", [5, 12, 16])
+def test_oracle_matches_reference_golden_high_levels(L):
+    """The oracle restatement at levels 5, 12 and 16 (the GPU's CTA-per-element kernels'
+    reference) against outputs of the reference's own CPU kernels."""
+    g = np.load(HIGH)
+    el, fff, adj, det = g[f"L{L}_elements"], g[f"L{L}_fff"], g[f"L{L}_adjugate"], g[f"L{L}_determinant"]
+    x, u = g[f"L{L}_x"], g[f"L{L}_u"]
+    lap = O.sshex8_laplacian_apply(L, el, fff, x)
+    ref = g[f"L{L}_laplacian_apply"]
+    assert np.abs(lap - ref).max() <= 1e-13 * np.abs(ref).max()
+    ela = O.linear_elasticity_apply(L, el, adj, det, float(g["mu"]), float(g["lam"]), u)
+    ref = g[f"L{L}_elasticity_apply"]
+    assert np.abs(ela - ref).max() <= 1e-13 * np.abs(ref).max()
+    if L == 16:
+        e8, x8 = g["L16_elements8"], g["L16_x8"]
+        n = x.size
+        prol = O.prolongate(8, e8, 16, el, 1, x8, n)
+        assert np.abs(prol - g["L16_prolongate_8_16"]).max() <= 1e-14 * np.abs(prol).max()
+        cnt = O.incidence_count(16, el, n)
+        rest = O.restrict(16, el, cnt, 8, e8, 1, x, x8.size)
+        assert np.abs(rest - g["L16_restrict_16_8"]).max() <= 1e-13 * np.abs(rest).max()
