@@ -145,3 +145,28 @@ def test_bad_meshes(tmp_path):
         ssmesh_from_folder(tmp_path / "tet", 2)
     with pytest.raises(KeyError):
         HexSSMesh(m.elements, m.points, 2).boundary_nodes("left")
+
+
+def test_read_wide_types_and_comments(tmp_path):
+    """int64 ids and float64 coordinates named in the file names, comments and quoted
+    values in meta.yaml, boundary files named without their folder."""
+    m = read_sfem_mesh(FIXTURE)
+    d = tmp_path / "wide"
+    (d / "boundary_nodes").mkdir(parents=True)
+    for v in range(8):
+        m.elements[v].astype(np.int64).tofile(d / f"i{v}.int64.raw")
+    for k, name in enumerate("xyz"):
+        m.points[k].astype(np.float64).tofile(d / f"{name}.float64.raw")
+    m.boundary_nodes["left"].astype(np.int64).tofile(d / "boundary_nodes" / "left.int64.raw")
+    lines = ["# written by hand", "element_type: 'HEX8'  # quoted", f"n_elements: {m.n_elements}",
+             f"n_points: {m.n_nodes}", "rpath: true", "elements:"]
+    lines += [f"- i{v}: i{v}.int64.raw" for v in range(8)]
+    lines += ["points:"] + [f"- {n}: {n}.float64.raw" for n in "xyz"]
+    lines += ["boundary_nodes:", "- left: left.int64.raw"]
+    (d / "meta.yaml").write_text("\n".join(lines) + "\n")
+    r = read_sfem_mesh(d)
+    assert r.element_type == "HEX8"
+    assert np.array_equal(r.elements, m.elements) and np.array_equal(r.points, m.points)
+    assert np.array_equal(r.boundary_nodes["left"], m.boundary_nodes["left"])
+    hm = ssmesh_from_folder(d, 2)
+    assert hm.n_nodes(2) == 7 * 5 * 5 and hm.boundary_nodes("left", 2).size == 5 * 5
