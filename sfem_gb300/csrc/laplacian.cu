@@ -831,9 +831,14 @@ __global__ void __launch_bounds__(2 * PK_TILE, 6) sshex8_laplacian_apply_packed_
         return;
     }
     const int nvalid = (int)((nelements - t * PK_TILE) < PK_TILE ? (nelements - t * PK_TILE) : PK_TILE);
-    // 1. gather x
-    for (int i = tid; i < NXE * PK_TILE; i += 2 * PK_TILE)
-        if (i % PK_TILE < nvalid) cp_async4(&sx[i], x + sidx[i]);
+    // 1. gather x (full tiles without the per-node validity test)
+    if (nvalid == PK_TILE) {
+#pragma unroll 8
+        for (int i = tid; i < NXE * PK_TILE; i += 2 * PK_TILE) cp_async4(&sx[i], x + sidx[i]);
+    } else {
+        for (int i = tid; i < NXE * PK_TILE; i += 2 * PK_TILE)
+            if (i % PK_TILE < nvalid) cp_async4(&sx[i], x + sidx[i]);
+    }
     const int el = tid % PK_TILE;
     const int half = tid / PK_TILE;  // warp-uniform layer group
     float2 A2[8][2];
@@ -877,8 +882,13 @@ __global__ void __launch_bounds__(2 * PK_TILE, 6) sshex8_laplacian_apply_packed_
     }
     __syncthreads();
     // 3. scatter
-    for (int i = tid; i < NXE * PK_TILE; i += 2 * PK_TILE)
-        if (i % PK_TILE < nvalid) atomicAdd(&y[sidx[i]], sx[i]);
+    if (nvalid == PK_TILE) {
+#pragma unroll 8
+        for (int i = tid; i < NXE * PK_TILE; i += 2 * PK_TILE) atomicAdd(&y[sidx[i]], sx[i]);
+    } else {
+        for (int i = tid; i < NXE * PK_TILE; i += 2 * PK_TILE)
+            if (i % PK_TILE < nvalid) atomicAdd(&y[sidx[i]], sx[i]);
+    }
 }
 
 // Diagonal: node value = sum over the micro elements of this macro element that
