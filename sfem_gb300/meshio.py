@@ -430,3 +430,20 @@ def ssmesh_from_folder(folder, L: int) -> HexSSMesh:
     if m.element_type.upper() not in ("HEX8", "HEXAHEDRON", "HEX"):
         raise ValueError(f"{folder}: element type {m.element_type} (HEX8 meshes only)")
     return HexSSMesh(m.elements, m.points, L, boundary=m.boundary_nodes)
+
+
+def sshex8_to_hex8(elements: np.ndarray, L: int) -> np.ndarray:
+    """Micro hex8 connectivity ``[8, E * L^3]`` (standard corner order) of a level-``L``
+    sshex8 connectivity ``[(L+1)^3, E]``: micro element ``m = xi + L (yi + L zi)`` of
+    macro element ``e`` is column ``e * L^3 + m``.  With the fine points this is a plain
+    HEX8 mesh (e.g. to write with :func:`write_sfem_mesh` for the reference)."""
+    el = np.asarray(elements)
+    if el.shape[0] != (L + 1) ** 3:
+        raise ValueError(f"connectivity has {el.shape[0]} rows, level {L} needs {(L + 1) ** 3}")
+    zi, yi, xi = np.meshgrid(np.arange(L), np.arange(L), np.arange(L), indexing="ij")
+    xi, yi, zi = xi.reshape(-1), yi.reshape(-1), zi.reshape(-1)
+    out = np.empty((8, el.shape[1], L ** 3), dtype=np.int32)
+    for c in range(8):
+        dx, dy, dz = HEX8_CORNERS[c]
+        out[c] = el[sshex8_lidx(L, xi + dx, yi + dy, zi + dz)].T
+    return np.ascontiguousarray(out.reshape(8, -1))

@@ -170,3 +170,23 @@ def test_read_wide_types_and_comments(tmp_path):
     assert np.array_equal(r.boundary_nodes["left"], m.boundary_nodes["left"])
     hm = ssmesh_from_folder(d, 2)
     assert hm.n_nodes(2) == 7 * 5 * 5 and hm.boundary_nodes("left", 2).size == 5 * 5
+
+
+@pytest.mark.parametrize("L", [2, 4])
+def test_sshex8_to_hex8_micro_mesh(tmp_path, L):
+    """The micro hex8 mesh of an (affine) sshex8 level carries the same Laplacian, and
+    survives a write / read as a reference mesh folder."""
+    from sfem_gb300.meshio import sshex8_to_hex8
+
+    m = SSMesh(3, 2, 2, L, box=((0, 2), (0, 1), (0, 1)))
+    el = m.elements(L)
+    micro = sshex8_to_hex8(el, L)
+    assert micro.shape == (8, m.n_elements * L ** 3)
+    write_sfem_mesh(tmp_path / "micro", SfemMesh("HEX8", micro, m.points))
+    r = read_sfem_mesh(tmp_path / "micro")
+    assert np.array_equal(r.elements, micro)
+    x = np.random.default_rng(L).standard_normal(m.n_nodes(L))
+    fff_macro = O.fff_fill(el[m.macro_corner_lidx(L)], m.points)
+    y_ss = O.sshex8_laplacian_apply(L, el, fff_macro, x)
+    y_h8 = O.hex8_laplacian_apply(r.elements, O.fff_fill(r.elements, r.points), x)
+    assert np.abs(y_h8 - y_ss).max() <= 1e-6 * np.abs(y_ss).max()
