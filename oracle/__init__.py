@@ -22,6 +22,7 @@ from . import build as _build
 
 _lib = None
 _ref = None
+_ref_f32 = None
 
 c_int = C.c_int
 c_ptrdiff = C.c_ssize_t
@@ -65,6 +66,19 @@ def ref():
             return None
         _ref = C.CDLL(str(path))
     return _ref
+
+
+def ref_f32():
+    """The reference's sshex8 Laplacian built in its float32 number configuration, or None."""
+    global _ref_f32
+    if _ref_f32 is None:
+        path = _build.REF_LIB_F32
+        if not path.exists():
+            path = _build.build_ref_f32()
+        if path is None or not Path(path).exists():
+            return None
+        _ref_f32 = C.CDLL(str(path))
+    return _ref_f32
 
 
 # ---------------------------------------------------------------------------
@@ -143,6 +157,34 @@ def sshex8_laplacian_apply_f32(L, elements, fff_aos, u, out=None):
     ea = PtrArray(elements.astype(np.int32))
     f = _f32(fff_aos)
     lib().or_sshex8_laplacian_apply_f32(c_int(L), c_ptrdiff(E), ea.p, _ptr(f), _ptr(u), _ptr(out))
+    return out
+
+
+def sshex8_laplacian_stencil_apply(L, elements, fff_aos, u, out=None):
+    """values += A u in the reference's node-centric stencil form (FP64)."""
+    E = elements.shape[1]
+    u = _f64(u)
+    out = np.zeros_like(u) if out is None else out
+    ea = PtrArray(elements.astype(np.int32))
+    f = _f32(fff_aos)
+    lib().or_sshex8_laplacian_stencil_apply(c_int(L), c_ptrdiff(E), ea.p, _ptr(f), _ptr(u), _ptr(out))
+    return out
+
+
+def sshex8_laplacian_stencil_apply_f32(L, elements, fff_aos, u, out=None, use_ref=False):
+    """values += A u in the stencil form, float32 number configuration.  use_ref: the
+    reference's own affine_sshex8_laplacian_stencil_apply_fff built with real_t = float."""
+    E = elements.shape[1]
+    u = np.ascontiguousarray(u, dtype=np.float32)
+    out = np.zeros_like(u) if out is None else out
+    assert out.dtype == np.float32
+    ea = PtrArray(elements.astype(np.int32))
+    f = _f32(fff_aos)
+    if use_ref:
+        ref_f32().affine_sshex8_laplacian_stencil_apply_fff(c_int(L), c_ptrdiff(E), ea.p, _ptr(f), _ptr(u),
+                                                             _ptr(out))
+    else:
+        lib().or_sshex8_laplacian_stencil_apply_f32(c_int(L), c_ptrdiff(E), ea.p, _ptr(f), _ptr(u), _ptr(out))
     return out
 
 

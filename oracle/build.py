@@ -21,6 +21,9 @@ REF_ROOT = Path(os.environ.get("SFEM_REFERENCE_ROOT", "/root/reference"))
 
 ORACLE_LIB = HERE / "_build" / "liboracle.so"
 REF_LIB = HERE / "_ref" / "libsfem_ref.so"
+# the reference's Laplacian sources built again in its float32 number configuration
+REF_LIB_F32 = HERE / "_ref" / "libsfem_ref_f32.so"
+REF_SOURCES_F32 = ["operators/sshex8/sshex8_laplacian.cpp"]
 
 # reference sources on the operator path (read in place)
 REF_SOURCES = [
@@ -62,7 +65,7 @@ def build_oracle(force: bool = False) -> Path:
     srcs = [HERE / "src" / "oracle.c"]
     if force or _stale(ORACLE_LIB, srcs):
         ORACLE_LIB.parent.mkdir(parents=True, exist_ok=True)
-        _run(["gcc", "-O2", "-fopenmp", "-fPIC", "-shared", "-o", str(ORACLE_LIB)] + [str(s) for s in srcs] + ["-lm"])
+        _run(["gcc", "-O3", "-fopenmp", "-fPIC", "-shared", "-o", str(ORACLE_LIB)] + [str(s) for s in srcs] + ["-lm"])
     return ORACLE_LIB
 
 
@@ -93,6 +96,28 @@ def build_ref(force: bool = False):
     return REF_LIB
 
 
+def build_ref_f32(force: bool = False):
+    """The reference's sshex8 Laplacian sources with real/scalar/accumulator = float
+    (shim_f32 first on the include path) into oracle/_ref/libsfem_ref_f32.so."""
+    if not reference_available():
+        return None
+    srcs = [REF_ROOT / s for s in REF_SOURCES_F32] + [HERE / "ref" / "ref_f32_extras.cpp"]
+    if not (force or _stale(REF_LIB_F32, srcs)):
+        return REF_LIB_F32
+    objdir = HERE / "_ref" / "obj_f32"
+    objdir.mkdir(parents=True, exist_ok=True)
+    inc = ["-I" + str(HERE / "shim_f32"), "-I" + str(HERE / "shim")] + ["-I" + str(REF_ROOT / d) for d in REF_INCLUDES]
+    flags = ["g++", "-std=c++17", "-O2", "-fopenmp", "-fPIC", "-DNDEBUG", "-w"] + inc
+    objs = []
+    for src in srcs:
+        obj = objdir / (src.stem + ".o")
+        _run(flags + ["-c", str(src), "-o", str(obj)])
+        objs.append(obj)
+    _run(["g++", "-shared", "-fopenmp", "-o", str(REF_LIB_F32)] + [str(o) for o in objs])
+    return REF_LIB_F32
+
+
 if __name__ == "__main__":
     print(build_oracle(force=True))
     print(build_ref(force=True))
+    print(build_ref_f32(force=True))

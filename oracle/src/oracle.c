@@ -288,6 +288,263 @@ int or_sshex8_laplacian_apply_f32(int L, ptrdiff_t nelements, idx_t **elements, 
     return 0;
 }
 
+/* ------------------------------------------------------------------------ */
+/* Node-centric (stencil) form: the reference's CPU default                 */
+/* ------------------------------------------------------------------------ */
+
+/* Tap tables of the node-centric form, by node class (per axis: 0 = low face, 1 = inside,
+ * 2 = high face of the macro element; class = cz*9 + cy*3 + cx): the offsets d of the
+ * neighbours a node of that class couples to inside its macro element, and for each the
+ * element-matrix entries A[k][k+d] (k over the micro elements of this macro element that
+ * contain both nodes) whose sum is the coefficient.  Class 13 (inside) is the 27-point
+ * stencil; the other 26 are the partial stencils of the surface. */
+typedef struct {
+    int ntaps[27];
+    int off[27][27][3];
+    int nsum[27][27];
+    int a[27][27][8];
+} stencil_taps_t;
+
+static void stencil_taps(stencil_taps_t *t) {
+    memset(t, 0, sizeof(*t));
+    for (int cls = 0; cls < 27; cls++) {
+        const int c[3] = {cls % 3, (cls / 3) % 3, cls / 9};
+        for (int dz = -1; dz <= 1; dz++)
+            for (int dy = -1; dy <= 1; dy++)
+                for (int dx = -1; dx <= 1; dx++) {
+                    const int d[3] = {dx, dy, dz};
+                    int n = 0, idx[8];
+                    for (int k = 0; k < 8; k++) {
+                        int ok = 1;
+                        for (int ax = 0; ax < 3; ax++) {
+                            const int kk = C8[k][ax], jj = kk + d[ax];
+                            /* the micro element with the node at corner kk lies inside the macro
+                             * element: low face -> corner 0 only, high face -> corner 1 only */
+                            if (jj < 0 || jj > 1 || (c[ax] == 0 && kk != 0) || (c[ax] == 2 && kk != 1)) ok = 0;
+                        }
+                        if (!ok) continue;
+                        int j = 0;
+                        while (C8[j][0] != C8[k][0] + dx || C8[j][1] != C8[k][1] + dy || C8[j][2] != C8[k][2] + dz) j++;
+                        idx[n++] = k * 8 + j;
+                    }
+                    if (!n) continue;
+                    const int q = t->ntaps[cls]++;
+                    t->off[cls][q][0] = dx;
+                    t->off[cls][q][1] = dy;
+                    t->off[cls][q][2] = dz;
+                    t->nsum[cls][q] = n;
+                    for (int i = 0; i < n; i++) t->a[cls][q][i] = idx[i];
+                }
+    }
+}
+
+static inline int node_class(int L, int i) { return i == 0 ? 0 : (i == L ? 2 : 1); }
+
+/* class of every local node and the tap offsets as local-index differences */
+static void stencil_linear_offsets(int L, const stencil_taps_t *T, int *vcls, int offl[27][27]) {
+    const int N1 = L + 1;
+    for (int zi = 0; zi <= L; zi++)
+        for (int yi = 0; yi <= L; yi++)
+            for (int xi = 0; xi <= L; xi++)
+                vcls[lidx(L, xi, yi, zi)] = node_class(L, zi) * 9 + node_class(L, yi) * 3 + node_class(L, xi);
+    for (int cls = 0; cls < 27; cls++)
+        for (int q = 0; q < T->ntaps[cls]; q++)
+            offl[cls][q] = T->off[cls][q][0] + N1 * (T->off[cls][q][1] + N1 * T->off[cls][q][2]);
+}
+
+/* affine_sshex8_laplacian_stencil_apply_fff (operators/sshex8/sshex8_laplacian.cpp:698-769),
+ * values += A u.  Per macro element: sub-FFF = FFF / L (:19-28), element matrix A, the
+ * 27-point stencil of A (hex8_matrix_to_stencil, operators/stencil/stencil3.hpp:205)
+ * applied at every node strictly inside the macro element (sshex8_stencil,
+ * stencil3.hpp:167), the partial stencils of A at its surface nodes (the 26 cases of
+ * sshex8_surface_stencil, operators/stencil/sshex8_skeleton_stencil.hpp:1683-1720), then
+ * the (L+1)^3 results are added to values with atomics.  Coefficients are built once per
+ * macro element and class, as the reference does. */
+int or_sshex8_laplacian_stencil_apply(int L, ptrdiff_t nelements, idx_t **elements, const jacobian_t *fff,
+                                      const double *u, double *values) {
+    const int N1 = L + 1, nxe = N1 * N1 * N1;
+    stencil_taps_t *T = (stencil_taps_t *)malloc(sizeof(stencil_taps_t));
+    stencil_taps(T);
+    int *vcls = (int *)malloc(nxe * sizeof(int));
+    int offl[27][27];
+    stencil_linear_offsets(L, T, vcls, offl);
+#pragma omp parallel
+    {
+        double *eu = (double *)malloc(nxe * sizeof(double));
+        double *ev = (double *)malloc(nxe * sizeof(double));
+        idx_t *idx = (idx_t *)malloc(nxe * sizeof(idx_t));
+        double coef[27][27];
+#pragma omp for
+        for (ptrdiff_t e = 0; e < nelements; e++) {
+            double sub[6], A[64];
+            const double h = 1.0 / L;
+            for (int d = 0; d < 6; d++) sub[d] = (double)fff[e * 6 + d] * h;
+            or_hex8_laplacian_matrix(sub, A);
+            for (int cls = 0; cls < 27; cls++)
+                for (int q = 0; q < T->ntaps[cls]; q++) {
+                    double c = 0;
+                    for (int i = 0; i < T->nsum[cls][q]; i++) c += A[T->a[cls][q][i]];
+                    coef[cls][q] = c;
+                }
+            for (int v = 0; v < nxe; v++) {
+                idx[v] = elements[v][e];
+                eu[v] = u[idx[v]];
+            }
+            /* class by class, rows of nodes along x (the reference's stencil sweeps run
+             * along x too); fixed tap counts so the x loop unrolls and vectorises */
+            for (int cls = 0; cls < 27; cls++) {
+                const int cx = cls % 3, cy = (cls / 3) % 3, cz = cls / 9;
+                const int x0 = cx == 0 ? 0 : (cx == 1 ? 1 : L), x1 = cx == 1 ? L - 1 : x0;
+                const int y0 = cy == 0 ? 0 : (cy == 1 ? 1 : L), y1 = cy == 1 ? L - 1 : y0;
+                const int z0 = cz == 0 ? 0 : (cz == 1 ? 1 : L), z1 = cz == 1 ? L - 1 : z0;
+                const int nt = T->ntaps[cls];
+                const int *restrict o = offl[cls];
+                const double *restrict c = coef[cls];
+                const double *restrict xin = eu;
+                double *restrict yout = ev;
+                for (int zi = z0; zi <= z1; zi++)
+                    for (int yi = y0; yi <= y1; yi++) {
+                        const int row = lidx(L, 0, yi, zi);
+                        switch (nt) {
+                            case 27:
+                                for (int xi = x0; xi <= x1; xi++) {
+                                    double acc = 0;
+#pragma GCC unroll 27
+                                    for (int q = 0; q < 27; q++) acc += c[q] * xin[row + xi + o[q]];
+                                    yout[row + xi] = acc;
+                                }
+                                break;
+                            case 18:
+                                for (int xi = x0; xi <= x1; xi++) {
+                                    double acc = 0;
+#pragma GCC unroll 18
+                                    for (int q = 0; q < 18; q++) acc += c[q] * xin[row + xi + o[q]];
+                                    yout[row + xi] = acc;
+                                }
+                                break;
+                            case 12:
+                                for (int xi = x0; xi <= x1; xi++) {
+                                    double acc = 0;
+#pragma GCC unroll 12
+                                    for (int q = 0; q < 12; q++) acc += c[q] * xin[row + xi + o[q]];
+                                    yout[row + xi] = acc;
+                                }
+                                break;
+                            default:
+                                for (int xi = x0; xi <= x1; xi++) {
+                                    double acc = 0;
+                                    for (int q = 0; q < nt; q++) acc += c[q] * xin[row + xi + o[q]];
+                                    yout[row + xi] = acc;
+                                }
+                        }
+                    }
+            }
+            for (int v = 0; v < nxe; v++) atomic_add(&values[idx[v]], ev[v]);
+        }
+        free(eu);
+        free(ev);
+        free(idx);
+    }
+    free(vcls);
+    free(T);
+    return 0;
+}
+
+/* The same stencil apply in the reference's float32 number configuration
+ * (real, scalar and accumulator float, cmake/SFEMNumbers.cmake:5-10): element
+ * matrix rounded to float, stencil sums, products and sums in float. */
+int or_sshex8_laplacian_stencil_apply_f32(int L, ptrdiff_t nelements, idx_t **elements, const jacobian_t *fff,
+                                          const float *u, float *values) {
+    const int N1 = L + 1, nxe = N1 * N1 * N1;
+    stencil_taps_t *T = (stencil_taps_t *)malloc(sizeof(stencil_taps_t));
+    stencil_taps(T);
+    int *vcls = (int *)malloc(nxe * sizeof(int));
+    int offl[27][27];
+    stencil_linear_offsets(L, T, vcls, offl);
+#pragma omp parallel
+    {
+        float *eu = (float *)malloc(nxe * sizeof(float));
+        float *ev = (float *)malloc(nxe * sizeof(float));
+        idx_t *idx = (idx_t *)malloc(nxe * sizeof(idx_t));
+        float coef[27][27];
+#pragma omp for
+        for (ptrdiff_t e = 0; e < nelements; e++) {
+            double sub[6], Ad[64];
+            float A[64];
+            const float h = 1.0f / (float)L;
+            for (int d = 0; d < 6; d++) sub[d] = (double)(fff[e * 6 + d] * h);
+            or_hex8_laplacian_matrix(sub, Ad);
+            for (int k = 0; k < 64; k++) A[k] = (float)Ad[k];
+            for (int cls = 0; cls < 27; cls++)
+                for (int q = 0; q < T->ntaps[cls]; q++) {
+                    float c = 0;
+                    for (int i = 0; i < T->nsum[cls][q]; i++) c += A[T->a[cls][q][i]];
+                    coef[cls][q] = c;
+                }
+            for (int v = 0; v < nxe; v++) {
+                idx[v] = elements[v][e];
+                eu[v] = u[idx[v]];
+            }
+            /* class by class, rows of nodes along x (the reference's stencil sweeps run
+             * along x too); fixed tap counts so the x loop unrolls and vectorises */
+            for (int cls = 0; cls < 27; cls++) {
+                const int cx = cls % 3, cy = (cls / 3) % 3, cz = cls / 9;
+                const int x0 = cx == 0 ? 0 : (cx == 1 ? 1 : L), x1 = cx == 1 ? L - 1 : x0;
+                const int y0 = cy == 0 ? 0 : (cy == 1 ? 1 : L), y1 = cy == 1 ? L - 1 : y0;
+                const int z0 = cz == 0 ? 0 : (cz == 1 ? 1 : L), z1 = cz == 1 ? L - 1 : z0;
+                const int nt = T->ntaps[cls];
+                const int *restrict o = offl[cls];
+                const float *restrict c = coef[cls];
+                const float *restrict xin = eu;
+                float *restrict yout = ev;
+                for (int zi = z0; zi <= z1; zi++)
+                    for (int yi = y0; yi <= y1; yi++) {
+                        const int row = lidx(L, 0, yi, zi);
+                        switch (nt) {
+                            case 27:
+                                for (int xi = x0; xi <= x1; xi++) {
+                                    float acc = 0;
+#pragma GCC unroll 27
+                                    for (int q = 0; q < 27; q++) acc += c[q] * xin[row + xi + o[q]];
+                                    yout[row + xi] = acc;
+                                }
+                                break;
+                            case 18:
+                                for (int xi = x0; xi <= x1; xi++) {
+                                    float acc = 0;
+#pragma GCC unroll 18
+                                    for (int q = 0; q < 18; q++) acc += c[q] * xin[row + xi + o[q]];
+                                    yout[row + xi] = acc;
+                                }
+                                break;
+                            case 12:
+                                for (int xi = x0; xi <= x1; xi++) {
+                                    float acc = 0;
+#pragma GCC unroll 12
+                                    for (int q = 0; q < 12; q++) acc += c[q] * xin[row + xi + o[q]];
+                                    yout[row + xi] = acc;
+                                }
+                                break;
+                            default:
+                                for (int xi = x0; xi <= x1; xi++) {
+                                    float acc = 0;
+                                    for (int q = 0; q < nt; q++) acc += c[q] * xin[row + xi + o[q]];
+                                    yout[row + xi] = acc;
+                                }
+                        }
+                    }
+            }
+            for (int v = 0; v < nxe; v++) atomic_add_f(&values[idx[v]], ev[v]);
+        }
+        free(eu);
+        free(ev);
+        free(idx);
+    }
+    free(vcls);
+    free(T);
+    return 0;
+}
+
 /* hex8_laplacian_apply_opt (operators/hex8/hex8_laplacian.cpp:309-345);
  * elements in hex8 corner order. */
 int or_hex8_laplacian_apply(ptrdiff_t nelements, idx_t **elements, const jacobian_t *fff, const double *u,

@@ -86,7 +86,30 @@ def main():
                         "L16_restrict_16_8": O.restrict(16, el, cnt, 8, e8, 1, x, n8, use_ref=True)})
     np.savez_compressed(OUT / "sshex8_high_levels.npz", mu=1.0, lam=10.0, **out)
     print("wrote", OUT / "sshex8_high_levels.npz")
+    make_float32_stencil()
+
+
+def make_float32_stencil():
+    """affine_sshex8_laplacian_stencil_apply_fff built in the reference's float32 number
+    configuration (real, scalar, accumulator = float): the pin of the float32 stencil
+    restatement and of the CPU baseline the benchmark times."""
+    assert O.ref_f32() is not None, "reference kernels (float32 configuration) unavailable"
+    rng = np.random.default_rng(20261204)
+    out = {}
+    for L, n, seed in ((4, (3, 2, 2), 31), (2, (2, 2, 2), 32), (5, (2, 1, 1), 33)):
+        m = SSMesh(*n, L, box=((0, n[0]), (0, n[1]), (0, n[2])), perturb=0.15, seed=seed)
+        el = m.elements(L)
+        fff = O.fff_fill(el[m.macro_corner_lidx(L)], m.points, use_ref=True)
+        x = rng.standard_normal(m.n_nodes(L)).astype(np.float32)
+        out.update({f"L{L}_elements": el, f"L{L}_fff": fff, f"L{L}_x": x,
+                    f"L{L}_apply_f32": O.sshex8_laplacian_stencil_apply_f32(L, el, fff, x, use_ref=True),
+                    f"L{L}_apply_f64": O.sshex8_laplacian_apply(L, el, fff, x.astype(np.float64), use_ref=True)})
+    np.savez_compressed(OUT / "sshex8_stencil_float32.npz", **out)
+    print("wrote", OUT / "sshex8_stencil_float32.npz")
 
 
 if __name__ == "__main__":
-    main()
+    if len(sys.argv) > 1 and sys.argv[1] == "float32":
+        make_float32_stencil()
+    else:
+        main()

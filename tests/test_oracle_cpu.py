@@ -216,3 +216,47 @@ def test_oracle_matches_reference_golden_high_levels(L):
         cnt = O.incidence_count(16, el, n)
         rest = O.restrict(16, el, cnt, 8, e8, 1, x, x8.size)
         assert np.abs(rest - g["L16_restrict_16_8"]).max() <= 1e-13 * np.abs(rest).max()
+
+
+STENCIL_F32 = Path(__file__).resolve().parent / "golden" / "sshex8_stencil_float32.npz"
+
+
+def test_stencil_form_matches_reference_golden(gold):
+    """The node-centric (stencil) restatement of affine_sshex8_laplacian_stencil_apply_fff
+    against that reference function's own FP64 output (L = 4 fixture) and the high-level
+    fixtures (L = 5, 12, 16)."""
+    lap = O.sshex8_laplacian_stencil_apply(4, gold["elements"], gold["fff"], gold["x"])
+    assert _rel(lap, gold["laplacian_apply"]) < 1e-14
+    g = np.load(HIGH)
+    for L in (5, 12, 16):
+        lap = O.sshex8_laplacian_stencil_apply(L, g[f"L{L}_elements"], g[f"L{L}_fff"], g[f"L{L}_x"])
+        assert _rel(lap, g[f"L{L}_laplacian_apply"]) < 1e-14
+
+
+@pytest.mark.parametrize("L", [2, 4, 5])
+def test_stencil_form_float32_matches_reference_golden(L):
+    """The float32 stencil restatement (the benchmark's CPU baseline) against the
+    reference's stencil apply built with real_t = float, and the FP64 stencil apply
+    against the reference's FP64 output on the same input."""
+    g = np.load(STENCIL_F32)
+    el, fff, x = g[f"L{L}_elements"], g[f"L{L}_fff"], g[f"L{L}_x"]
+    y32 = O.sshex8_laplacian_stencil_apply_f32(L, el, fff, x)
+    ref32 = g[f"L{L}_apply_f32"]
+    assert y32.dtype == np.float32 and ref32.dtype == np.float32
+    # float rounding in a different summation order: a few float ulps of the row scale
+    assert np.abs(y32 - ref32).max() <= 2e-6 * np.abs(ref32).max()
+    y64 = O.sshex8_laplacian_stencil_apply(L, el, fff, x.astype(np.float64))
+    assert _rel(y64, g[f"L{L}_apply_f64"]) < 1e-14
+    assert np.abs(ref32 - g[f"L{L}_apply_f64"]).max() <= 2e-6 * np.abs(ref32).max()
+
+
+@pytest.mark.skipif(O.ref_f32() is None, reason="reference tree not present")
+def test_stencil_form_float32_matches_reference_direct():
+    """Directly against the reference's float32-configuration build on a fresh mesh."""
+    m = SSMesh(3, 2, 2, 4, perturb=0.12, seed=9)
+    el = m.elements(4)
+    fff = O.fff_fill(el[m.macro_corner_lidx(4)], m.points)
+    x = np.random.default_rng(5).standard_normal(m.n_nodes()).astype(np.float32)
+    ref = O.sshex8_laplacian_stencil_apply_f32(4, el, fff, x, use_ref=True)
+    ours = O.sshex8_laplacian_stencil_apply_f32(4, el, fff, x)
+    assert np.abs(ours - ref).max() <= 2e-6 * np.abs(ref).max()
