@@ -16,9 +16,13 @@ three streams (copy in, compute, copy out; double-buffered).
 against the mixed-precision solvers (Poisson 48^3 L=4, elasticity cantilever
 64x16x16 L=4), and the batched serving run (256 uneven problems).
 
-``--impl reference`` times the reference CPU implementation of the same apply
-in the same precision (the oracle port of affine_sshex8_laplacian_stencil_apply_fff
-in the reference's float32 number configuration, OpenMP, all host threads).
+``--impl reference`` times the reference's CPU algorithm for the same apply in the
+same precision: the oracle's restatement of affine_sshex8_laplacian_stencil_apply_fff
+(the reference's default CPU path: 27-point stencil inside each macro element, partial
+stencils on its surface) in the reference's float32 number configuration, OpenMP on
+every host core the process may use, OMP_PROC_BIND=true.  The restatement is pinned to
+the reference's own build of that function (FP64 and float32 configurations) by the
+CPU test suite.
 """
 
 from __future__ import annotations
@@ -26,6 +30,10 @@ from __future__ import annotations
 import argparse
 import json
 import os
+
+# thread binding of the OpenMP CPU baseline, as the reference's run scripts set it;
+# before any import that starts an OpenMP runtime
+os.environ.setdefault("OMP_PROC_BIND", "true")
 import subprocess
 import sys
 import threading
@@ -42,9 +50,8 @@ LEVEL = 4
 METRIC = "sshex8 Laplacian apply GDoF/s (FP32, L=4, 48^3 macro); solve times to FP64 residual in 'solve'"
 NOMINAL_FP64_TFLOPS = 1.25  # GB300 nominal FP64 (no measured figure in the peaks file)
 # dram__bytes_read.sum + dram__bytes_write.sum of one launch of the float kernel of
-# the step on this workload (ncu --set full, cold cache, mean of two launches:
-# 115.5 MB read + 5.65 MB written), from profiles/sshex8_laplacian_apply_packed_fp32_L4_48cube.md
-TRAFFIC_BYTES_PER_LAUNCH = 121.15e6
+# the step on this workload (ncu, cold cache), None until captured for the kernel in use
+TRAFFIC_BYTES_PER_LAUNCH = None
 SEED = 0
 PERTURB = 0.1
 
@@ -62,6 +69,9 @@ def parse():
     ap.add_argument("--no-learned", action="store_true")
     ap.add_argument("--profile-kernels", action="store_true",
                     help="launch each main kernel twice on the bench workloads and exit (an ncu target)")
+    ap.add_argument("--profile-apply", action="store_true",
+                    help="launch only the 48^3 L=4 Laplacian applies (FP32 stencil and element-matrix kernels, "
+                         "FP64 stencil kernel) twice each and exit (an ncu target)")
     ap.add_argument("--batch-problems", type=int, default=256)
     ap.add_argument("--profile-zoo", action="store_true",
                     help="launch every vector, SpMV and coarse-level kernel twice on inputs larger than L2: "
@@ -84,6 +94,32 @@ def workload_config(nx):
 
     m = SSMesh(nx, nx, nx, LEVEL, perturb=PERTURB, seed=SEED)
     return m
+
+
+L2_NOTE = ("flushed before every timed step, after the y reset: 512 MiB write, then 512 MiB read of another "
+           "buffer (the write's dirty lines leave L2 before the timed region)")
+
+
+def config_dict(m, world=1):
+    """The workload description both arms print (identical keys and values; `l2` is the
+    GPU arm's timing rule, the CPU arm's caches are described in its cpu_baseline)."""
+    return {"workload": "sshex8_laplacian_apply_L4_48cube", "nodes": m.n_nodes(), "macro_elements": m.n_elements,
+            "level": LEVEL, "perturb": PERTURB, "seed": SEED, "l2": L2_NOTE,
+            "parallelism": f"replicas{world}" if world > 1 else "single"}
+
+
+def stencil_fma_per_element(L):
+    """FMAs of the node-centric apply per macro element: 27 taps inside, 18 on faces,
+    12 on edges, 8 at corners (2,197 at L = 4)."""
+    return 27 * (L - 1) ** 3 + 18 * 6 * (L - 1) ** 2 + 12 * 12 * (L - 1) + 8 * 8
+
+
+def host_cores():
+    """Host threads this process may run on (its affinity mask)."""
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count()
 
 
 class ClockSampler:
@@ -158,7 +194,8 @@ def measured_peak_hbm():
 
 
 def cpu_apply_time(m, dtype, reps=3):
-    """Seconds per apply of the CPU oracle port (OpenMP, all host threads) on the full mesh."""
+    """Seconds per apply of the oracle's restatement of the reference's CPU stencil apply
+    (OpenMP, every host core of the affinity mask) on the full mesh."""
     import oracle as O
 
     el = m.elements(LEVEL)
@@ -166,9 +203,9 @@ def cpu_apply_time(m, dtype, reps=3):
     x = np.random.default_rng(1).standard_normal(m.n_nodes())
     if dtype == "f32":
         x = x.astype(np.float32)
-        fn = lambda out: O.sshex8_laplacian_apply_f32(LEVEL, el, fff, x, out=out)
+        fn = lambda out: O.sshex8_laplacian_stencil_apply_f32(LEVEL, el, fff, x, out=out)
     else:
-        fn = lambda out: O.sshex8_laplacian_apply(LEVEL, el, fff, x, out=out)
+        fn = lambda out: O.sshex8_laplacian_stencil_apply(LEVEL, el, fff, x, out=out)
     y = np.zeros_like(x)
     fn(y)  # warm-up
     t = time.perf_counter()
@@ -178,12 +215,17 @@ def cpu_apply_time(m, dtype, reps=3):
     return (time.perf_counter() - t) / reps
 
 
+CPU_KIND_NOTE = ("oracle restatement of affine_sshex8_laplacian_stencil_apply_fff "
+                 "(operators/sshex8/sshex8_laplacian.cpp:698-769; stencil form), float32 number configuration, "
+                 "OpenMP, OMP_PROC_BIND=true; pinned to the reference's own float32 build of that function")
+
+
 def cpu_baseline(m, reps=3):
-    """The CPU oracle apply (port of the reference CPU kernel, float32 configuration) on the host cores."""
+    """The reference's CPU stencil apply (oracle restatement, float32 configuration) on the host cores."""
     dt = cpu_apply_time(m, "f32", reps)
-    return {"value": m.n_nodes() / dt / 1e9, "unit": "GDoF/s", "cores": os.cpu_count(), "kind": "port",
-            "sample": f"{reps} FP32 applies of the full 48^3 L=4 mesh (oracle port of "
-                      f"affine_sshex8_laplacian_stencil_apply_fff, float32 number configuration, OpenMP)",
+    return {"value": m.n_nodes() / dt / 1e9, "unit": "GDoF/s", "cores": host_cores(), "kind": "port",
+            "sample": f"{reps} FP32 applies of the full 48^3 L=4 mesh, after one warm-up apply",
+            "algorithm": CPU_KIND_NOTE, "omp_proc_bind": os.environ.get("OMP_PROC_BIND"),
             "seconds_per_apply": dt}
 
 
@@ -199,22 +241,23 @@ def run_reference(args):
     x = np.random.default_rng(1).standard_normal(m.n_nodes()).astype(np.float32)
     y = np.zeros_like(x)
     for _ in range(max(1, args.warmup)):
-        O.sshex8_laplacian_apply_f32(LEVEL, el, fff, x, out=y)
+        O.sshex8_laplacian_stencil_apply_f32(LEVEL, el, fff, x, out=y)
     steps = max(1, min(args.steps, 20))  # bounded CPU sample
     t = time.perf_counter()
     for _ in range(steps):
         y[:] = 0
-        O.sshex8_laplacian_apply_f32(LEVEL, el, fff, x, out=y)
+        O.sshex8_laplacian_stencil_apply_f32(LEVEL, el, fff, x, out=y)
     dt = (time.perf_counter() - t) / steps
     v = m.n_nodes() / dt / 1e9
     line = {
         "impl": "reference", "metric": METRIC, "value": v,
         "unit": "GDoF/s", "n_gpus": world, "steps": steps, "warmup": args.warmup, "ms_per_step": dt * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "sshex8_laplacian_apply_L4_48cube", "nodes": m.n_nodes(), "macro_elements": m.n_elements},
-        "cpu_baseline": {"value": v, "unit": "GDoF/s", "cores": os.cpu_count(), "kind": "port",
-                         "sample": f"{steps} timed FP32 applies of the full mesh (oracle port of the reference "
-                                   f"CPU kernel in its float32 configuration, OpenMP)"},
+        "config": config_dict(m, world),
+        "cpu_baseline": {"value": v, "unit": "GDoF/s", "cores": host_cores(), "kind": "port",
+                         "sample": f"{steps} timed FP32 applies of the full 48^3 L=4 mesh",
+                         "algorithm": CPU_KIND_NOTE, "omp_proc_bind": os.environ.get("OMP_PROC_BIND"),
+                         "caches": "not flushed; one apply's data (~144 MB) exceeds the host caches"},
         "e2e": {"value": v, "unit": "GDoF/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -591,15 +634,13 @@ def run_ours(args):
     alg_bytes = 3 * 4 * N + (4 * (LEVEL + 1) ** 3 + 24) * E
     alg_bytes64 = 3 * 8 * N + (4 * (LEVEL + 1) ** 3 + 24) * E
     achieved = alg_bytes / t_kernel / 1e9
-    fp64_flops = 2 * 64 * (LEVEL ** 3) * E  # element-matrix form, 128 flop per micro element
+    fp64_flops = 2 * stencil_fma_per_element(LEVEL) * E  # node-centric form, 2 flop per tap
     line = {
         "metric": METRIC,
         "value": value, "unit": "GDoF/s", "n_gpus": world, "steps": args.steps, "warmup": max(3, args.warmup),
         "ms_per_step": t_kernel * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "sshex8_laplacian_apply_L4_48cube", "nodes": N, "macro_elements": E, "level": LEVEL,
-                   "perturb": PERTURB, "seed": SEED, "l2": "flushed before every timed step, after the y reset: 512 MiB write, then 512 MiB read of another buffer (the write's dirty lines leave L2 before the timed region)",
-                   "parallelism": f"replicas{world}" if world > 1 else "single"},
+        "config": config_dict(m, world),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": TRAFFIC_BYTES_PER_LAUNCH, "peak_kind": peak_kind, "algorithmic_bytes": alg_bytes},
         "e2e": {"value": e2e_value, "unit": "GDoF/s", "h2d_bytes_per_step": 4 * N, "d2h_bytes_per_step": 4 * N},
@@ -683,6 +724,32 @@ def profile_kernels():
             S.apply(ope, u, v)
     torch.cuda.synchronize()
     print("profile kernels: done")
+
+
+def profile_apply():
+    """Two launches each of the 48^3 L=4 Laplacian applies from packed tiles: the FP32
+    stencil kernel (the step), the FP32 element-matrix kernel and the FP64 stencil
+    kernel.  A small ncu target (about 150 MB of inputs, above the L2)."""
+    import torch
+
+    from sfem_gb300 import capi
+    from sfem_gb300.operators import Laplacian, SSMeshDevice
+
+    dev = torch.device("cuda:0")
+    lib = capi.load()
+    m = workload_config(NX)
+    op = Laplacian(SSMeshDevice(m, LEVEL, device=dev)).initialize()
+    N = m.n_nodes()
+    for dt, variant in ((torch.float32, -1), (torch.float32, 3), (torch.float64, -1)):
+        x = torch.randn(N, dtype=dt, device=dev)
+        y = torch.zeros_like(x)
+        prev = lib.sfem_gb300_set_laplacian_kernel(variant)
+        for _ in range(2):
+            y.zero_()
+            op.apply(x, y)
+        lib.sfem_gb300_set_laplacian_kernel(prev)
+    torch.cuda.synchronize()
+    print("profile apply: done")
 
 
 def profile_zoo():
@@ -849,6 +916,9 @@ def main():
     args = parse()
     if args.profile_kernels:
         profile_kernels()
+        return
+    if args.profile_apply:
+        profile_apply()
         return
     if args.profile_solves:
         profile_solves()

@@ -84,8 +84,9 @@ int cu_laplacian_diag(int element_type, ptrdiff_t nelements, sfem_gb300_idx_t **
  * counterpart): -1 per-level default, 0 shared-memory staged tile, 1 warp per
  * element, 2 thread per element in registers, 3 cp.async staged tile with two
  * threads per element, 4 persistent cp.async pipeline with one warp per micro
- * layer (3 and 4: even L; other levels use the staged tile).  Returns the previous
- * setting (-1 if none was forced). */
+ * layer (3 and 4: even L; other levels use the staged tile), 8 node-centric
+ * stencil form (L = 4; the FP64 default there, FP32 on request).  Returns the
+ * previous setting (-1 if none was forced). */
 int sfem_gb300_set_laplacian_kernel(int variant);
 
 /* Packed tiles (no reference counterpart; an operator-creation step like the
@@ -95,10 +96,16 @@ int sfem_gb300_set_laplacian_kernel(int variant);
  * apply fetches a tile's ids and metric with one bulk copy.
  * sfem_gb300_sshex8_packed_bytes gives the block array's size (-1: unsupported
  * type), sfem_gb300_sshex8_pack fills it (16-byte aligned),
- * sfem_gb300_sshex8_laplacian_apply_packed computes y += A x (FP32 x / y) from it;
- * the result equals cu_laplacian_apply's on the same connectivity and FFF up to FP32
- * rounding order.  sfem_gb300_laplacian_status returns (and clears) 1 if a packed
- * apply gave up waiting for its bulk copy, else 0. */
+ * sfem_gb300_sshex8_laplacian_apply_packed computes y += A x from it (FP32 x / y:
+ * element-matrix kernel, or the node-centric stencil kernel with variant 8; FP64
+ * x / y: stencil kernel); the result equals cu_laplacian_apply's on the same
+ * connectivity and FFF up to rounding order.  sfem_gb300_laplacian_status returns
+ * (and clears) 1 if a packed apply gave up waiting for its bulk copy (2 if the
+ * drain after that gave up too), else 0.
+ * sfem_gb300_set_tile_wait_polls (test knob, no reference counterpart) bounds the
+ * FIRST wait of every tile on its bulk copy (polls <= 0: the default bound) so a
+ * test can make it give up; the drain wait keeps its long bound.  Returns the
+ * previous bound. */
 /* Stored element matrices (the reference's "ss:em" Laplacian,
  * frontend/ops/sfem_SemiStructuredEMLaplacian.cpp:77-117: sshex8_laplacian_element_matrix,
  * operators/sshex8/sshex8_laplacian.cpp:595-634, + sshex8_stencil_element_matrix_apply):
@@ -115,6 +122,7 @@ int sfem_gb300_sshex8_pack(int element_type, ptrdiff_t nelements, sfem_gb300_idx
 int sfem_gb300_sshex8_laplacian_apply_packed(int element_type, ptrdiff_t nelements, const void *packed,
                                              int real_type_xy, const void *x, void *y, void *stream);
 int sfem_gb300_laplacian_status(void);
+int sfem_gb300_set_tile_wait_polls(int polls);
 
 /* ------------------------------------------------------- linear elasticity */
 

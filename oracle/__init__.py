@@ -238,6 +238,18 @@ def linear_elasticity_apply(L, elements, adj_aos, det, mu, lam, u, out=None, use
     return out
 
 
+def linear_elasticity_row_scale(L, elements, adj_aos, det, mu, lam, u):
+    """sum_j |K_ij| |u_j| (element by element): the scale of per-entry parity checks."""
+    E = elements.shape[1]
+    u = np.abs(_f64(u))
+    out = np.zeros_like(u)
+    ea = PtrArray(elements.astype(np.int32))
+    a, d = _f32(adj_aos), _f32(det)
+    lib().or_linear_elasticity_apply_abs(c_int(L), c_ptrdiff(E), ea.p, _ptr(a), _ptr(d), c_double(mu),
+                                         c_double(lam), _ptr(u), _ptr(out))
+    return out
+
+
 def linear_elasticity_block_diag(L, elements, adj_aos, det, mu, lam, n_nodes):
     E = elements.shape[1]
     d3 = np.zeros(3 * n_nodes)

@@ -635,8 +635,27 @@ static void sub_adjugate(const jacobian_t *adjugate, const jacobian_t *determina
  * u and out are interleaved with stride 3 (ux = u, uy = u+1, uz = u+2).
  * L == 0 selects a plain hex8 mesh (affine_hex8_linear_elasticity_apply_adjugate,
  * operators/hex8/hex8_linear_elasticity.cpp:458). */
+static int linear_elasticity_apply_impl(int L, ptrdiff_t nelements, idx_t **elements, const jacobian_t *adjugate,
+                                        const jacobian_t *determinant, double mu, double lambda, const double *u,
+                                        double *out, int absolute);
+
 int or_linear_elasticity_apply(int L, ptrdiff_t nelements, idx_t **elements, const jacobian_t *adjugate,
                                const jacobian_t *determinant, double mu, double lambda, const double *u, double *out) {
+    return linear_elasticity_apply_impl(L, nelements, elements, adjugate, determinant, mu, lambda, u, out, 0);
+}
+
+/* out += |K| u with every element-matrix entry replaced by its magnitude: with u = |x|
+ * this is the row scale sum_j |K_ij| |x_j| (summed element by element, so an upper
+ * bound of the assembled one) that floating-point parity is measured against. */
+int or_linear_elasticity_apply_abs(int L, ptrdiff_t nelements, idx_t **elements, const jacobian_t *adjugate,
+                                   const jacobian_t *determinant, double mu, double lambda, const double *u,
+                                   double *out) {
+    return linear_elasticity_apply_impl(L, nelements, elements, adjugate, determinant, mu, lambda, u, out, 1);
+}
+
+static int linear_elasticity_apply_impl(int L, ptrdiff_t nelements, idx_t **elements, const jacobian_t *adjugate,
+                                        const jacobian_t *determinant, double mu, double lambda, const double *u,
+                                        double *out, int absolute) {
     const int Lm = L > 0 ? L : 1;
     const int nxe = (Lm + 1) * (Lm + 1) * (Lm + 1);
 #pragma omp parallel
@@ -650,6 +669,8 @@ int or_linear_elasticity_apply(int L, ptrdiff_t nelements, idx_t **elements, con
             double adj[9], det;
             sub_adjugate(adjugate, determinant, e, Lm, adj, &det);
             or_hex8_linear_elasticity_matrix(mu, lambda, adj, det, K);
+            if (absolute)
+                for (int k = 0; k < 576; k++) K[k] = fabs(K[k]);
             if (L == 0) {
                 double ue[24], oe[24];
                 for (int v = 0; v < 8; v++)

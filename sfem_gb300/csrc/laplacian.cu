@@ -14,6 +14,7 @@
 #include "common.cuh"
 #include "laplacian_kernels.cuh"
 #include "tcgen05.cuh"
+#include "tiles.cuh"
 
 namespace sfem_gb300 {
 
@@ -441,15 +442,6 @@ __global__ void __launch_bounds__(TILE) sshex8_laplacian_apply_staged_kernel(ptr
 //     plane is summed after a barrier;
 //  4. the y values of the tile are scattered with atomics, one coalesced pass.
 // Shared layout [node][TILE] keeps every access conflict-free.
-__device__ __forceinline__ void cp_async4(void *smem, const void *gmem) {
-    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
-    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
 // Inversion symmetry of the affine element matrix: the point reflection
 // xi -> 1 - xi maps hex8 corner c to pi(c) = (0 6)(1 7)(2 4)(3 5) and leaves
@@ -745,16 +737,7 @@ __global__ void __launch_bounds__(32 * L, 2) sshex8_laplacian_apply_pipe_kernel(
 }
 
 // ------------------------------------------------------------------ packed tiles
-// Connectivity and metric repacked once per operator into one contiguous block per
-// tile of PK_TILE = 32 consecutive macro elements: [node][el] int32 ids followed by
-// [6][el] metric entries as float bits (elements past the end: node 0, metric 0), so
-// a CTA fetches its tile's ids and metric with one bulk copy (cp.async.bulk,
-// completion counted on an mbarrier) instead of 125 row segments of 128 bytes from
-// 125 SoA rows, each behind a row-pointer load.
-constexpr int PK_TILE = 32;
-constexpr int PK_L = 4;  // the level the packed path serves
-__host__ __device__ constexpr int pk_words(int L) { return PK_TILE * ((L + 1) * (L + 1) * (L + 1) + 6); }
-constexpr int LAP_WAIT_POLLS = 1 << 20;
+// (layout in tiles.cuh)
 __device__ int g_lap_status;  // nonzero: a bulk-copy wait gave up
 
 __global__ void sshex8_pack_kernel(ptrdiff_t nelements, int nxe, const idx_t *const *elements, ptrdiff_t fff_stride,
@@ -802,7 +785,7 @@ __device__ __forceinline__ void lap_A2_from_metric(const float (&f)[6], float2 (
 template <int L>
 __global__ void __launch_bounds__(2 * PK_TILE, 6) sshex8_laplacian_apply_packed_kernel(
         ptrdiff_t nelements, const int32_t *__restrict__ packed, const float *__restrict__ x,
-        float *__restrict__ y) {
+        float *__restrict__ y, int first_polls) {
     constexpr int N1 = L + 1;
     constexpr int NP = N1 * N1;
     constexpr int NXE = NP * N1;
@@ -822,11 +805,12 @@ __global__ void __launch_bounds__(2 * PK_TILE, 6) sshex8_laplacian_apply_packed_
         tc::bulk_load(pk_smem, packed + t * WORDS, WORDS * 4, &mbar);
     }
     __syncthreads();
-    if (!__syncthreads_and(tc::mbar_wait(&mbar, 0, LAP_WAIT_POLLS))) {
-        // leave no copy in flight into this CTA's shared memory
+    if (!__syncthreads_and(tc::mbar_wait(&mbar, 0, first_polls))) {
+        // leave no copy in flight into this CTA's shared memory: thread 0 drains the
+        // copy (with a far longer bound) before its CTA exits
         if (tid == 0) {
             atomicExch(&g_lap_status, 1);
-            tc::mbar_wait(&mbar, 0, LAP_WAIT_POLLS);
+            if (!tc::mbar_wait(&mbar, 0, LAP_DRAIN_POLLS)) atomicExch(&g_lap_status, 2);
         }
         return;
     }
@@ -1061,7 +1045,12 @@ static int laplacian_variant() {
     int v = __atomic_load_n(&g_laplacian_variant, __ATOMIC_RELAXED);
     if (v < 0) {
         const char *e = getenv("SFEM_GB300_LAPLACIAN_KERNEL");
-        v = (e && e[0] == 'w') ? 1 : (e && e[0] == 't') ? 2 : (e && e[0] == 'a') ? 3 : (e && e[0] == 'p') ? 4 : 0;
+        v = (e && e[0] == 'w')   ? 1
+            : (e && e[0] == 't') ? 2
+            : (e && e[0] == 'a') ? 3
+            : (e && e[0] == 'p') ? 4
+            : (e && e[0] == 's') ? 8
+                                 : 0;
         if (e && e[0]) __atomic_store_n(&g_laplacian_variant_forced, 1, __ATOMIC_RELAXED);
         __atomic_store_n(&g_laplacian_variant, v, __ATOMIC_RELAXED);
     }
@@ -1080,7 +1069,13 @@ static int laplacian_apply_tpl(int element_type, ptrdiff_t nelements, idx_t **el
     const int blocks = grid_for((nelements + 3) / 4, 1, kNumSMs * 64);
     // default per level (measured at 7.2M nodes): L=4 async tile, L=2 thread per element, else staged tile
     int variant = laplacian_variant();
-    if (__atomic_load_n(&g_laplacian_variant_forced, __ATOMIC_RELAXED) == 0) variant = (L == 4) ? 3 : (L == 2) ? 2 : 0;
+    const bool forced = __atomic_load_n(&g_laplacian_variant_forced, __ATOMIC_RELAXED) != 0;
+    if (!forced) variant = (L == 4) ? 8 : (L == 2) ? 2 : 0;
+    // node-centric stencil form (variant 8): the default where it is served.  FP64:
+    // 0.57 ms against 0.99 ms for the warp element-matrix kernel (about half the FP64
+    // operations); FP32: 49 us against 58 us for the async tile (48^3 macro, L = 4)
+    if (variant == 8 && sshex8_laplacian_stencil_supported(L))
+        return sshex8_laplacian_stencil_apply<T>(L, nelements, nullptr, elements, fff_stride, fff, x, y, s);
     // FP64 at L = 2, 3: few micro elements per macro element leave most lanes of the warp
     // kernel idle; the staged tile (one thread per element) keeps them busy
     if (sizeof(T) == 8 && (L == 2 || L == 3) && variant != 1) variant = 5;
@@ -1273,8 +1268,8 @@ extern "C" int cu_laplacian_diag(int element_type, ptrdiff_t nelements, idx_t **
 }
 
 extern "C" int sfem_gb300_set_laplacian_kernel(int variant) {
-    if (variant < -1 || variant > 7 || variant == 5)
-        return set_error("sfem_gb300_set_laplacian_kernel: variant must be -1..4, 6 or 7");
+    if (variant < -1 || variant > 8 || variant == 5)
+        return set_error("sfem_gb300_set_laplacian_kernel: variant must be -1..4, 6, 7 or 8");
     const int cur = laplacian_variant();
     const int prev = __atomic_load_n(&g_laplacian_variant_forced, __ATOMIC_RELAXED) ? cur : -1;
     __atomic_store_n(&g_laplacian_variant, variant < 0 ? 0 : variant, __ATOMIC_RELAXED);
@@ -1307,11 +1302,20 @@ extern "C" int sfem_gb300_sshex8_laplacian_apply_packed(int element_type, ptrdif
     if (element_type != SFEM_GB300_SSHEX8(PK_L))
         return set_error("sfem_gb300_sshex8_laplacian_apply_packed: element type %d is not sshex8 L = %d",
                          element_type, PK_L);
-    if (real_type_xy != SFEM_GB300_FLOAT32)
-        return set_error("sfem_gb300_sshex8_laplacian_apply_packed: real type %d (FP32 only)", real_type_xy);
     if (nelements <= 0) return SFEM_GB300_SUCCESS;
     if (reinterpret_cast<uintptr_t>(packed) & 15)
         return set_error("sfem_gb300_sshex8_laplacian_apply_packed: packed is not 16-byte aligned");
+    // FP64 always, FP32 with variant 8: the node-centric stencil kernel on the same blocks
+    if (real_type_xy == SFEM_GB300_FLOAT64 || real_type_xy == SFEM_GB300_REAL_DEFAULT)
+        return sshex8_laplacian_stencil_apply<double>(PK_L, nelements, (const int32_t *)packed, nullptr, 0, nullptr,
+                                                      (const double *)x, (double *)y, stream_of(stream));
+    if (real_type_xy != SFEM_GB300_FLOAT32)
+        return set_error("sfem_gb300_sshex8_laplacian_apply_packed: unsupported real type %d", real_type_xy);
+    // the stencil kernel unless another kernel was forced (packed element-matrix kernel:
+    // 50.8 us against 45.0 us on the 48^3 L = 4 mesh)
+    if (laplacian_variant() == 8 || !__atomic_load_n(&g_laplacian_variant_forced, __ATOMIC_RELAXED))
+        return sshex8_laplacian_stencil_apply<float>(PK_L, nelements, (const int32_t *)packed, nullptr, 0, nullptr,
+                                                     (const float *)x, (float *)y, stream_of(stream));
     const ptrdiff_t ntiles = (nelements + PK_TILE - 1) / PK_TILE;
     if (ntiles > 0x7fffffff) return set_error("sfem_gb300_sshex8_laplacian_apply_packed: too many tiles");
     constexpr int NXE = (PK_L + 1) * (PK_L + 1) * (PK_L + 1);
@@ -1323,7 +1327,7 @@ extern "C" int sfem_gb300_sshex8_laplacian_apply_packed(int element_type, ptrdif
                              (int)smem);
     });
     sshex8_laplacian_apply_packed_kernel<PK_L><<<(unsigned)ntiles, 2 * PK_TILE, smem, stream_of(stream)>>>(
-            nelements, (const int32_t *)packed, (const float *)x, (float *)y);
+            nelements, (const int32_t *)packed, (const float *)x, (float *)y, first_wait_polls());
     return check_launch("sfem_gb300_sshex8_laplacian_apply_packed");
 }
 
@@ -1334,7 +1338,9 @@ extern "C" int sfem_gb300_laplacian_status(void) {
         const int zero = 0;
         cudaMemcpyToSymbol(g_lap_status, &zero, sizeof(int));
     }
-    return st;
+    const int st2 = sshex8_laplacian_stencil_status();
+    if (st2 < 0) return -1;
+    return st > st2 ? st : st2;
 }
 
 // ------------------------------------------------------------------ stored element matrices

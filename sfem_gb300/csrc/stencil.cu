@@ -1,0 +1,343 @@
+// Node-centric (stencil) form of the affine sshex8 Laplacian apply, sm_103a.
+//
+// Reference: affine_sshex8_laplacian_stencil_apply_fff (operators/sshex8/sshex8_laplacian.cpp:698-769),
+// the reference's CPU default (operators/laplacian.cpp:195-205): per macro element the
+// 27-point stencil of the micro element matrix at the nodes inside the macro element
+// (sshex8_stencil, operators/stencil/stencil3.hpp:167) and partial stencils at its
+// surface nodes (sshex8_surface_stencil, operators/stencil/sshex8_skeleton_stencil.hpp:1683).
+//
+// Every output value is computed once, by one thread, as a gather over its (at most 27)
+// neighbours inside the macro element: no shared-memory accumulation and no element
+// matrix.  At L = 4 a macro element costs 2,197 FMA (27 x 27 inside, 54 x 18 on faces,
+// 36 x 12 on edges, 8 x 8 at corners) against 4,096 for the micro element-matrix form.
+//
+// Stencil coefficients.  With one metric G (the sub-FFF, 6 entries) per macro element the
+// micro element matrix is A = sum_pq G_pq int d_p phi_i d_q phi_j, each term a product of
+// one-dimensional integrals.  The coefficient coupling node i to node i + d is the sum of
+// A over the micro elements of this macro element that contain both nodes, which
+// factorises per axis: per axis the node is on the low face (LO), inside (MID) or on the
+// high face (HI) of the macro element, and the assembled 1D integral over the micro
+// intervals containing both i and i + delta is a compile-time constant of (class, delta).
+// So every coefficient is sum_m g_m W_m(class, d) with compile-time weights W.
+//
+// Thread mapping.  A CTA takes a tile of 32 consecutive macro elements (lane = element,
+// so every shared-memory access of a warp is conflict-free: [node][element] layout) and
+// four warps split the (L+1)^2 node columns (ix, iy); a warp walks each of its columns in
+// z with a three-plane register window and scatters every finished value with one
+// atomic add (a value inside the macro element has no other contributor, so the atomic
+// only serves the surface).  A warp handles columns of one class at a time, so its
+// coefficients are built once per class in registers.
+#include <algorithm>
+#include <atomic>
+#include <mutex>
+
+#include "common.cuh"
+#include "tcgen05.cuh"
+#include "tiles.cuh"
+
+namespace sfem_gb300 {
+namespace stencil {
+
+enum : int { LO = 0, MID = 1, HI = 2 };
+
+// int_0^1 of (test, trial) factor type t for linear basis psi_0 = 1 - s, psi_1 = s:
+// t = 0 mass psi_a psi_b, 1 stiffness psi'_a psi'_b, 2 psi'_a psi_b, 3 psi_a psi'_b
+__host__ __device__ constexpr double q1_1d(int t, int a, int b) {
+    return t == 0 ? (a == b ? 1.0 / 3.0 : 1.0 / 6.0)
+           : t == 1 ? (a == b ? 1.0 : -1.0)
+           : t == 2 ? (a ? 0.5 : -0.5)
+                    : (b ? 0.5 : -0.5);
+}
+
+// the same integral summed over the micro intervals of the macro element that contain
+// node i (class cls) and node i + delta: the right interval [i, i+1] (node i is its
+// local 0) exists unless i is on the high face, the left one [i-1, i] unless on the low face
+__host__ __device__ constexpr double q1_1d_assembled(int t, int cls, int delta) {
+    return delta == 1    ? (cls != HI ? q1_1d(t, 0, 1) : 0.0)
+           : delta == -1 ? (cls != LO ? q1_1d(t, 1, 0) : 0.0)
+                         : (cls != LO ? q1_1d(t, 1, 1) : 0.0) + (cls != HI ? q1_1d(t, 0, 0) : 0.0);
+}
+
+// factor type on `axis` of the term int d_p phi_i d_q phi_j
+__host__ __device__ constexpr int factor_type(int axis, int p, int q) {
+    return (axis == p && axis == q) ? 1 : axis == p ? 2 : axis == q ? 3 : 0;
+}
+
+__host__ __device__ constexpr double pq_product(int p, int q, int cx, int cy, int cz, int dx, int dy, int dz) {
+    return q1_1d_assembled(factor_type(0, p, q), cx, dx) * q1_1d_assembled(factor_type(1, p, q), cy, dy) *
+           q1_1d_assembled(factor_type(2, p, q), cz, dz);
+}
+
+// weight of metric entry m (00, 01, 02, 11, 12, 22) in the coefficient of offset d at a
+// node of class (cx, cy, cz); off-diagonal entries stand for G_pq and G_qp
+__host__ __device__ constexpr double weight(int m, int cx, int cy, int cz, int dx, int dy, int dz) {
+    return m == 0   ? pq_product(0, 0, cx, cy, cz, dx, dy, dz)
+           : m == 1 ? pq_product(0, 1, cx, cy, cz, dx, dy, dz) + pq_product(1, 0, cx, cy, cz, dx, dy, dz)
+           : m == 2 ? pq_product(0, 2, cx, cy, cz, dx, dy, dz) + pq_product(2, 0, cx, cy, cz, dx, dy, dz)
+           : m == 3 ? pq_product(1, 1, cx, cy, cz, dx, dy, dz)
+           : m == 4 ? pq_product(1, 2, cx, cy, cz, dx, dy, dz) + pq_product(2, 1, cx, cy, cz, dx, dy, dz)
+                    : pq_product(2, 2, cx, cy, cz, dx, dy, dz);
+}
+
+// a neighbour at offset d along an axis exists inside the macro element
+__host__ __device__ constexpr bool offset_ok(int cls, int d) { return d > 0 ? cls != HI : d < 0 ? cls != LO : true; }
+
+template <typename T>
+__device__ __forceinline__ T coefficient(const T (&g)[6], int cx, int cy, int cz, int dx, int dy, int dz) {
+    T c = T(0);
+#pragma unroll
+    for (int m = 0; m < 6; m++) {
+        const double w = weight(m, cx, cy, cz, dx, dy, dz);
+        if (w != 0.0) c = fma(g[m], (T)w, c);
+    }
+    return c;
+}
+
+template <typename T>
+__device__ __forceinline__ void cp_async_val(T *smem, const T *gmem);
+template <>
+__device__ __forceinline__ void cp_async_val<float>(float *smem, const float *gmem) {
+    cp_async4(smem, gmem);
+}
+template <>
+__device__ __forceinline__ void cp_async_val<double>(double *smem, const double *gmem) {
+    cp_async8(smem, gmem);
+}
+
+// the valid (dy, dx) neighbours of plane z of the column at `col` into w[dy+1][dx+1]
+template <typename T, int L, int TILE, int CX, int CY>
+__device__ __forceinline__ void load_plane(T (&w)[3][3], const T *__restrict__ col, int z) {
+    constexpr int N1 = L + 1, NP = N1 * N1;
+#pragma unroll
+    for (int j = 0; j < 3; j++)
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+            if (offset_ok(CY, j - 1) && offset_ok(CX, i - 1)) w[j][i] = col[(z * NP + (j - 1) * N1 + (i - 1)) * TILE];
+}
+
+// Columns [c0, c1) of class (CX, CY) for this lane's macro element.  Columns of a class
+// are numbered x fastest over the MID positions 1..L-1.
+template <typename T, int L, int TILE, int CX, int CY>
+__device__ __forceinline__ void columns(const T *__restrict__ sx, const int32_t *__restrict__ sidx,
+                                        const T (&g)[6], int c0, int c1, int lane, bool valid,
+                                        T *__restrict__ y) {
+    constexpr int N1 = L + 1, NP = N1 * N1;
+    // coefficients of the low (dz = 0, +1) and high (dz = -1, 0) z classes; a node inside
+    // in z takes dz = +1 from the low class, dz = -1 from the high class and the sum of
+    // both for dz = 0 (the assembled 1D integrals add up the same way)
+    T clo[3][3][2], chi[3][3][2], cmid[3][3];
+#pragma unroll
+    for (int j = 0; j < 3; j++)
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+            if (!(offset_ok(CY, j - 1) && offset_ok(CX, i - 1))) continue;
+            clo[j][i][0] = coefficient(g, CX, CY, LO, i - 1, j - 1, 0);
+            clo[j][i][1] = coefficient(g, CX, CY, LO, i - 1, j - 1, 1);
+            chi[j][i][0] = coefficient(g, CX, CY, HI, i - 1, j - 1, -1);
+            chi[j][i][1] = coefficient(g, CX, CY, HI, i - 1, j - 1, 0);
+            cmid[j][i] = clo[j][i][0] + chi[j][i][1];
+        }
+    for (int c = c0; c < c1; c++) {
+        const int ix = CX == LO ? 0 : CX == HI ? L : (CY == MID ? 1 + c % (L - 1) : 1 + c);
+        const int iy = CY == LO ? 0 : CY == HI ? L : (CX == MID ? 1 + c / (L - 1) : 1 + c);
+        const T *col = sx + (iy * N1 + ix) * TILE + lane;
+        const int32_t *icol = sidx + (iy * N1 + ix) * TILE + lane;
+        T w[3][3][3];
+        load_plane<T, L, TILE, CX, CY>(w[1], col, 0);
+        load_plane<T, L, TILE, CX, CY>(w[2], col, 1);
+#pragma unroll
+        for (int iz = 0; iz <= L; iz++) {
+            T a0 = T(0), a1 = T(0), a2 = T(0);
+#pragma unroll
+            for (int j = 0; j < 3; j++)
+#pragma unroll
+                for (int i = 0; i < 3; i++) {
+                    if (!(offset_ok(CY, j - 1) && offset_ok(CX, i - 1))) continue;
+                    if (iz > 0) a0 = fma(chi[j][i][0], w[0][j][i], a0);
+                    a1 = fma(iz == 0 ? clo[j][i][0] : iz == L ? chi[j][i][1] : cmid[j][i], w[1][j][i], a1);
+                    if (iz < L) a2 = fma(clo[j][i][1], w[2][j][i], a2);
+                }
+            const T v = (a0 + a1) + a2;
+            if (valid) atomicAdd(y + icol[iz * NP * TILE], v);
+            if (iz < L) {
+#pragma unroll
+                for (int j = 0; j < 3; j++)
+#pragma unroll
+                    for (int i = 0; i < 3; i++) {
+                        w[0][j][i] = w[1][j][i];
+                        w[1][j][i] = w[2][j][i];
+                    }
+                if (iz + 2 <= L) load_plane<T, L, TILE, CX, CY>(w[2], col, iz + 2);
+            }
+        }
+    }
+}
+
+constexpr int kWarps = 4;
+constexpr int kThreads = 32 * kWarps;
+
+// Shared memory of a tile: the ids [node][el] and metric [6][el] (the packed block
+// layout), then x [node][el].
+template <typename T, int L>
+__host__ __device__ constexpr size_t smem_bytes() {
+    return (size_t)pk_words(L) * 4 + (size_t)(L + 1) * (L + 1) * (L + 1) * PK_TILE * sizeof(T);
+}
+
+__device__ int g_status;  // nonzero: a bulk-copy wait gave up (2: its drain gave up too)
+
+// One CTA per tile of PK_TILE macro elements.  PACKED: ids and metric come as one bulk
+// copy of the tile's packed block; otherwise from the SoA rows elements[v][e] and the SoA
+// metric fff[m * fff_stride + e].
+template <typename T, int L, bool PACKED>
+__global__ void __launch_bounds__(kThreads) sshex8_laplacian_stencil_kernel(
+        ptrdiff_t nelements, const int32_t *__restrict__ packed, const idx_t *const *elements, ptrdiff_t fff_stride,
+        const float *__restrict__ fff, const T *__restrict__ x, T *__restrict__ y, int first_polls) {
+    constexpr int TILE = PK_TILE;
+    constexpr int N1 = L + 1;
+    constexpr int NXE = N1 * N1 * N1;
+    constexpr int WORDS = pk_words(L);
+    extern __shared__ __align__(128) unsigned char st_smem[];
+    __shared__ __align__(8) uint64_t mbar;
+    int32_t *sidx = reinterpret_cast<int32_t *>(st_smem);
+    const float *smet = reinterpret_cast<const float *>(sidx + NXE * TILE);
+    T *sx = reinterpret_cast<T *>(st_smem + (size_t)WORDS * 4);
+    const int tid = threadIdx.x;
+    const int lane = tid & 31, warp = tid >> 5;
+    const ptrdiff_t t = blockIdx.x;
+    const ptrdiff_t e0 = t * TILE;
+    const int nvalid = (int)((nelements - e0) < TILE ? (nelements - e0) : TILE);
+    const bool valid = lane < nvalid;
+    T g[6];
+    const T h = T(1) / T(L);
+    if (PACKED) {
+        if (tid == 0) {
+            tc::mbar_init(&mbar, 1);
+            tc::mbar_arrive_expect_tx(&mbar, WORDS * 4);
+            tc::bulk_load(st_smem, packed + t * WORDS, WORDS * 4, &mbar);
+        }
+        __syncthreads();
+        if (!__syncthreads_and(tc::mbar_wait(&mbar, 0, first_polls))) {
+            // leave no copy in flight into this CTA's shared memory
+            if (tid == 0) {
+                atomicExch(&g_status, 1);
+                if (!tc::mbar_wait(&mbar, 0, LAP_DRAIN_POLLS)) atomicExch(&g_status, 2);
+            }
+            return;
+        }
+#pragma unroll
+        for (int m = 0; m < 6; m++) g[m] = valid ? (T)smet[m * TILE + lane] * h : T(0);
+    } else {
+        __shared__ const idx_t *srow[NXE];
+        for (int v = tid; v < NXE; v += kThreads) srow[v] = elements[v];
+        __syncthreads();
+        constexpr int Q = TILE / 4;  // 16-byte chunks per row segment
+        for (int k = tid; k < NXE * Q; k += kThreads) {
+            const int v = k / Q, q = k % Q;
+            const idx_t *row = srow[v] + e0;
+            if (nvalid == TILE && ((reinterpret_cast<uintptr_t>(row) & 15) == 0)) {
+                cp_async16(&sidx[v * TILE + 4 * q], row + 4 * q);
+            } else {
+#pragma unroll
+                for (int r = 0; r < 4; r++)
+                    if (4 * q + r < nvalid) cp_async4(&sidx[v * TILE + 4 * q + r], row + 4 * q + r);
+            }
+        }
+#pragma unroll
+        for (int m = 0; m < 6; m++) g[m] = valid ? (T)__ldg(&fff[m * fff_stride + e0 + lane]) * h : T(0);
+        cp_async_wait_all();
+        __syncthreads();
+    }
+    // gather x of the tile's micro grids
+    if (nvalid == TILE) {
+#pragma unroll 4
+        for (int k = tid; k < NXE * TILE; k += kThreads) cp_async_val<T>(&sx[k], x + sidx[k]);
+    } else {
+        for (int k = tid; k < NXE * TILE; k += kThreads)
+            if (k % TILE < nvalid) cp_async_val<T>(&sx[k], x + sidx[k]);
+    }
+    cp_async_wait_all();
+    __syncthreads();
+    // node columns: two warps split the inside columns, two take the face and edge columns
+    constexpr int NIN = (L - 1) * (L - 1);
+    constexpr int HALF = (NIN + 1) / 2;
+    switch (warp) {
+        case 0:
+            columns<T, L, TILE, MID, MID>(sx, sidx, g, 0, HALF, lane, valid, y);
+            break;
+        case 1:
+            columns<T, L, TILE, MID, MID>(sx, sidx, g, HALF, NIN, lane, valid, y);
+            break;
+        case 2:
+            columns<T, L, TILE, LO, MID>(sx, sidx, g, 0, L - 1, lane, valid, y);
+            columns<T, L, TILE, HI, MID>(sx, sidx, g, 0, L - 1, lane, valid, y);
+            columns<T, L, TILE, LO, LO>(sx, sidx, g, 0, 1, lane, valid, y);
+            columns<T, L, TILE, HI, LO>(sx, sidx, g, 0, 1, lane, valid, y);
+            break;
+        default:
+            columns<T, L, TILE, MID, LO>(sx, sidx, g, 0, L - 1, lane, valid, y);
+            columns<T, L, TILE, MID, HI>(sx, sidx, g, 0, L - 1, lane, valid, y);
+            columns<T, L, TILE, LO, HI>(sx, sidx, g, 0, 1, lane, valid, y);
+            columns<T, L, TILE, HI, HI>(sx, sidx, g, 0, 1, lane, valid, y);
+            break;
+    }
+}
+
+template <typename T, int L, bool PACKED>
+static int launch(ptrdiff_t nelements, const int32_t *packed, idx_t **elements, ptrdiff_t fff_stride, const float *fff,
+                  const T *x, T *y, cudaStream_t s) {
+    const ptrdiff_t ntiles = (nelements + PK_TILE - 1) / PK_TILE;
+    if (ntiles > 0x7fffffff) return set_error("sshex8 Laplacian stencil apply: too many tiles");
+    constexpr size_t smem = smem_bytes<T, L>();
+    static std::once_flag attr;  // shared-memory opt-in, once per instantiation
+    std::call_once(attr, [] {
+        cudaFuncSetAttribute(sshex8_laplacian_stencil_kernel<T, L, PACKED>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    });
+    sshex8_laplacian_stencil_kernel<T, L, PACKED><<<(unsigned)ntiles, kThreads, smem, s>>>(
+            nelements, packed, elements, fff_stride, fff, x, y, first_wait_polls());
+    return check_launch("sshex8 Laplacian stencil apply");
+}
+
+}  // namespace stencil
+
+static std::atomic<int> g_first_wait_polls{LAP_WAIT_POLLS};
+int first_wait_polls() { return g_first_wait_polls.load(std::memory_order_relaxed); }
+
+// Levels served by the node-centric kernel.
+bool sshex8_laplacian_stencil_supported(int L) { return L == 4; }
+
+template <typename T>
+int sshex8_laplacian_stencil_apply(int L, ptrdiff_t nelements, const int32_t *packed, idx_t **elements,
+                                   ptrdiff_t fff_stride, const float *fff, const T *x, T *y, cudaStream_t s) {
+    if (nelements <= 0) return SFEM_GB300_SUCCESS;
+    if (L != 4) return set_error("sshex8 Laplacian stencil apply: level %d not served", L);
+    if (packed) {
+        if (reinterpret_cast<uintptr_t>(packed) & 15)
+            return set_error("sshex8 Laplacian stencil apply: packed block not 16-byte aligned");
+        return stencil::launch<T, 4, true>(nelements, packed, nullptr, 0, nullptr, x, y, s);
+    }
+    return stencil::launch<T, 4, false>(nelements, nullptr, elements, fff_stride, fff, x, y, s);
+}
+
+template int sshex8_laplacian_stencil_apply<float>(int, ptrdiff_t, const int32_t *, idx_t **, ptrdiff_t,
+                                                   const float *, const float *, float *, cudaStream_t);
+template int sshex8_laplacian_stencil_apply<double>(int, ptrdiff_t, const int32_t *, idx_t **, ptrdiff_t,
+                                                    const float *, const double *, double *, cudaStream_t);
+
+int sshex8_laplacian_stencil_status() {
+    int st = 0;
+    if (cudaMemcpyFromSymbol(&st, stencil::g_status, sizeof(int)) != cudaSuccess) return -1;
+    if (st) {
+        const int zero = 0;
+        cudaMemcpyToSymbol(stencil::g_status, &zero, sizeof(int));
+    }
+    return st;
+}
+
+}  // namespace sfem_gb300
+
+extern "C" int sfem_gb300_set_tile_wait_polls(int polls) {
+    const int prev = sfem_gb300::g_first_wait_polls.load();
+    sfem_gb300::g_first_wait_polls.store(polls <= 0 ? sfem_gb300::LAP_WAIT_POLLS : polls);
+    return prev;
+}

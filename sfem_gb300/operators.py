@@ -65,8 +65,8 @@ class Laplacian:
         self.space = space
         self.coefficient = coefficient
         self.fff = None
-        # FP32 applies of sshex8 L = 2 / 4 read the connectivity + metric repacked into
-        # one contiguous block per 32 macro elements (built with the metric)
+        # applies of sshex8 L = 4 read the connectivity + metric repacked into one
+        # contiguous block per 32 macro elements (built with the metric)
         self.packed = bool(packed)
         self.packed_blocks = None
 
@@ -111,7 +111,7 @@ class Laplacian:
         """out += A x (x, out: float32 or float64 CUDA tensors)."""
         E = self.space.n_elements
         rt = capi.real_type_of(x)
-        if self.packed_blocks is not None and rt == capi.FLOAT32:
+        if self.packed_blocks is not None and rt in (capi.FLOAT32, capi.FLOAT64):
             capi.check(
                 capi.load().sfem_gb300_sshex8_laplacian_apply_packed(self.space.element_type, capi.i64(E),
                                                                      capi.vp(self.packed_blocks), rt, capi.vp(x),

@@ -73,7 +73,7 @@ def test_sshex8_laplacian_apply_fp32(cuda, L, n):
     assert err.max() < RTOL32, err.max()
 
 
-@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 6, 7])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 6, 7, 8])
 @pytest.mark.parametrize("L", [2, 3, 4])
 @pytest.mark.parametrize("aligned", [True, False])
 def test_sshex8_laplacian_fp32_kernels(cuda, variant, L, aligned):
@@ -108,11 +108,51 @@ def test_sshex8_laplacian_fp32_kernels(cuda, variant, L, aligned):
     assert err.max() < RTOL32, (variant, L, aligned, err.max())
 
 
+@pytest.mark.parametrize("variant", [1, -1])
+@pytest.mark.parametrize("n", [(5, 4, 3), (1, 1, 1), (8, 5, 3)])
+@pytest.mark.parametrize("aligned", [True, False])
+def test_sshex8_laplacian_fp64_kernels(cuda, variant, n, aligned):
+    """FP64 at L = 4: the node-centric stencil kernel (default, -1) and the warp
+    element-matrix kernel (1), on ragged tiles (60 = 32 + 28, 1, 120 = 3 x 32 + 24) with
+    connectivity rows 16-byte aligned or not; 1e-13 of the row scale."""
+    import torch
+
+    L = 4
+    m = SSMesh(*n, L, perturb=0.1, seed=12)
+    el = m.elements(L)
+    E = m.n_elements
+    fff_aos = O.fff_fill(el[m.macro_corner_lidx(L)], m.points)
+    stride = E if aligned else E + 1
+    fbuf = torch.zeros((6, stride), dtype=torch.float32, device=cuda)
+    fbuf[:, :E] = torch.from_numpy(fff_aos.T.copy()).to(cuda)
+    buf = torch.zeros((el.shape[0], stride), dtype=torch.int32, device=cuda)
+    buf[:, :E] = torch.from_numpy(el).to(cuda)
+    rows = capi.DevicePtrArray(buf)
+    rng = np.random.default_rng(13)
+    x, y0 = rng.standard_normal(m.n_nodes(L)), rng.standard_normal(m.n_nodes(L))
+    ref = O.sshex8_laplacian_stencil_apply(L, el, fff_aos, x, out=y0.copy())
+    xd, yd = torch.from_numpy(x).to(cuda), torch.from_numpy(y0).to(cuda)
+    lib = capi.load()
+    prev = lib.sfem_gb300_set_laplacian_kernel(variant)
+    try:
+        capi.check(lib.cu_laplacian_apply(capi.SSHEX8(L), capi.i64(E), rows.ptr, capi.i64(stride), capi.vp(fbuf),
+                                          capi.FLOAT64, capi.vp(xd), capi.vp(yd), None), "apply")
+        torch.cuda.synchronize()
+    finally:
+        lib.sfem_gb300_set_laplacian_kernel(prev)
+    scale = _row_scale_lap(L, el, fff_aos, x) + np.abs(y0)
+    err = np.abs(yd.cpu().numpy() - ref) / scale
+    assert err.max() < RTOL64, (variant, n, aligned, err.max())
+
+
+@pytest.mark.parametrize("form", ["fp32_em", "fp32_stencil", "fp64_stencil"])
 @pytest.mark.parametrize("n", [(5, 4, 3), (9, 8, 7), (1, 1, 1), (36, 36, 36)])
 @pytest.mark.parametrize("aligned", [True, False])
-def test_sshex8_laplacian_packed(cuda, n, aligned):
-    """Packed tiles (L = 4): pack from SoA rows (row stride E or E + 1) and apply in FP32;
-    element counts 60 (32 + 28: a ragged last tile), 504, 1 and 46,656."""
+def test_sshex8_laplacian_packed(cuda, form, n, aligned):
+    """Packed tiles (L = 4): pack from SoA rows (row stride E or E + 1) and apply with the
+    FP32 stencil kernel (default), the FP32 element-matrix kernel (any other forced
+    variant) or FP64 (stencil kernel); element counts 60 (32 + 28: a ragged last tile),
+    504, 1 and 46,656."""
     import torch
 
     L = 4
@@ -142,20 +182,66 @@ def test_sshex8_laplacian_packed(cuda, n, aligned):
     x = np.random.default_rng(7).standard_normal(m.n_nodes(L))
     y0 = np.random.default_rng(8).standard_normal(m.n_nodes(L))
     ref = O.sshex8_laplacian_apply(L, el, fff_aos, x, out=y0.copy())
-    xd = torch.from_numpy(x).float().to(cuda)
-    yd = torch.from_numpy(y0).float().to(cuda)
-    capi.check(lib.sfem_gb300_sshex8_laplacian_apply_packed(capi.SSHEX8(L), capi.i64(E), capi.vp(packed),
-                                                            capi.FLOAT32, capi.vp(xd), capi.vp(yd), None),
-               "apply_packed")
-    torch.cuda.synchronize()
+    dt, rt, tol = (torch.float64, capi.FLOAT64, RTOL64) if form == "fp64_stencil" else (torch.float32, capi.FLOAT32, RTOL32)
+    xd = torch.from_numpy(x).to(dt).to(cuda)
+    yd = torch.from_numpy(y0).to(dt).to(cuda)
+    prev = lib.sfem_gb300_set_laplacian_kernel(3 if form == "fp32_em" else -1)
+    try:
+        capi.check(lib.sfem_gb300_sshex8_laplacian_apply_packed(capi.SSHEX8(L), capi.i64(E), capi.vp(packed),
+                                                                rt, capi.vp(xd), capi.vp(yd), None),
+                   "apply_packed")
+        torch.cuda.synchronize()
+    finally:
+        lib.sfem_gb300_set_laplacian_kernel(prev)
     assert lib.sfem_gb300_laplacian_status() == 0
     scale = _row_scale_lap(L, el, fff_aos, x) + np.abs(y0)
     err = np.abs(yd.double().cpu().numpy() - ref) / scale
-    assert err.max() < RTOL32, (n, aligned, err.max())
+    assert err.max() < tol, (form, n, aligned, err.max())
+
+
+@pytest.mark.parametrize("form", ["fp32_stencil", "fp32_em", "fp64_stencil"])
+def test_tile_wait_gives_up_and_reports(cuda, form):
+    """Failure detection without a fault: the first wait on each tile's bulk copy is
+    limited to one poll, so tiles give up before their copy has landed.  Each such CTA
+    records the status and drains its copy (normal long bound) before it exits; the
+    status is reported once, the context stays usable and the next apply is exact."""
+    import torch
+
+    L = 4
+    m = SSMesh(24, 24, 24, L, perturb=0.1, seed=14)
+    sp = SSMeshDevice(m, L)
+    el = m.elements(L)
+    fff_aos = O.fff_fill(el[m.macro_corner_lidx(L)], m.points)
+    op = Laplacian(sp, packed=True).set_fff(torch.from_numpy(fff_aos.T.copy()))
+    dt = torch.float64 if form == "fp64_stencil" else torch.float32
+    x = torch.from_numpy(np.random.default_rng(15).standard_normal(m.n_nodes(L))).to(dt).to(cuda)
+    y = torch.zeros_like(x)
+    lib = capi.load()
+    assert lib.sfem_gb300_laplacian_status() == 0
+    kprev = lib.sfem_gb300_set_laplacian_kernel(3 if form == "fp32_em" else -1)
+    try:
+        prev = lib.sfem_gb300_set_tile_wait_polls(1)
+        try:
+            op.apply(x, y)
+            torch.cuda.synchronize()
+        finally:
+            lib.sfem_gb300_set_tile_wait_polls(prev)
+        assert lib.sfem_gb300_laplacian_status() == 1  # gave up, drained, reported
+        assert lib.sfem_gb300_laplacian_status() == 0  # read and cleared
+        y.zero_()
+        op.apply(x, y)
+        torch.cuda.synchronize()
+    finally:
+        lib.sfem_gb300_set_laplacian_kernel(kprev)
+    assert lib.sfem_gb300_laplacian_status() == 0
+    ref = O.sshex8_laplacian_apply(L, el, fff_aos, x.double().cpu().numpy())
+    scale = _row_scale_lap(L, el, fff_aos, x.double().cpu().numpy())
+    tol = RTOL64 if dt == torch.float64 else RTOL32
+    assert (np.abs(y.double().cpu().numpy() - ref) / scale).max() < tol
 
 
 def test_sshex8_laplacian_packed_operator(cuda):
-    """The operator's FP32 apply goes through the packed blocks; FP64 keeps the SoA rows."""
+    """The operator's FP32 and FP64 applies go through the packed blocks."""
     import torch
 
     L = 4
@@ -185,10 +271,10 @@ def test_sshex8_laplacian_packed_bad_inputs(cuda):
     assert lib.sfem_gb300_sshex8_packed_bytes(capi.SSHEX8(4), capi.i64(0)) == 0
     buf = torch.zeros(64, dtype=torch.int32, device=cuda)
     x = torch.zeros(8, dtype=torch.float64, device=cuda)
-    # FP64 vectors are refused with a message (the packed path is FP32 only)
-    assert lib.sfem_gb300_sshex8_laplacian_apply_packed(capi.SSHEX8(4), capi.i64(1), capi.vp(buf), capi.FLOAT64,
+    # an unknown real type is refused with a message
+    assert lib.sfem_gb300_sshex8_laplacian_apply_packed(capi.SSHEX8(4), capi.i64(1), capi.vp(buf), 7,
                                                         capi.vp(x), capi.vp(x), None) == 1
-    assert "FP32" in capi.last_error()
+    assert "real type" in capi.last_error()
     # a block array that is not 16-byte aligned is refused before any launch
     assert lib.sfem_gb300_sshex8_laplacian_apply_packed(capi.SSHEX8(4), capi.i64(1), capi.c_void(buf.data_ptr() + 4),
                                                         capi.FLOAT32, capi.vp(x), capi.vp(x), None) == 1
