@@ -31,9 +31,16 @@ import argparse
 import json
 import os
 
+# host threads this process may use, read before any OpenMP runtime starts (with
+# OMP_PROC_BIND the runtime pins the calling thread to one core afterwards)
+try:
+    HOST_CORES = len(os.sched_getaffinity(0))
+except AttributeError:
+    HOST_CORES = os.cpu_count()
 # thread binding of the OpenMP CPU baseline, as the reference's run scripts set it;
 # before any import that starts an OpenMP runtime
 os.environ.setdefault("OMP_PROC_BIND", "true")
+os.environ.setdefault("OMP_NUM_THREADS", str(HOST_CORES))
 import subprocess
 import sys
 import threading
@@ -115,11 +122,9 @@ def stencil_fma_per_element(L):
 
 
 def host_cores():
-    """Host threads this process may run on (its affinity mask)."""
-    try:
-        return len(os.sched_getaffinity(0))
-    except AttributeError:
-        return os.cpu_count()
+    """Host threads the CPU baseline runs on: the process's affinity mask at start-up
+    (OMP_NUM_THREADS is set to it)."""
+    return int(os.environ.get("OMP_NUM_THREADS", HOST_CORES))
 
 
 class ClockSampler:

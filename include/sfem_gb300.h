@@ -103,8 +103,9 @@ int sfem_gb300_set_laplacian_kernel(int variant);
  * (and clears) 1 if a packed apply gave up waiting for its bulk copy (2 if the
  * drain after that gave up too), else 0.
  * sfem_gb300_set_tile_wait_polls (test knob, no reference counterpart) bounds the
- * FIRST wait of every tile on its bulk copy (polls <= 0: the default bound) so a
- * test can make it give up; the drain wait keeps its long bound.  Returns the
+ * FIRST wait of every tile on its bulk copy (0: give up without polling; < 0: the
+ * default bound) so a test can make it give up; the drain wait that follows keeps
+ * its long bound, so no copy is left in flight when the CTA exits.  Returns the
  * previous bound. */
 /* Stored element matrices (the reference's "ss:em" Laplacian,
  * frontend/ops/sfem_SemiStructuredEMLaplacian.cpp:77-117: sshex8_laplacian_element_matrix,

@@ -338,6 +338,6 @@ int sshex8_laplacian_stencil_status() {
 
 extern "C" int sfem_gb300_set_tile_wait_polls(int polls) {
     const int prev = sfem_gb300::g_first_wait_polls.load();
-    sfem_gb300::g_first_wait_polls.store(polls <= 0 ? sfem_gb300::LAP_WAIT_POLLS : polls);
+    sfem_gb300::g_first_wait_polls.store(polls < 0 ? sfem_gb300::LAP_WAIT_POLLS : polls);
     return prev;
 }

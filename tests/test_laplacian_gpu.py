@@ -202,9 +202,9 @@ def test_sshex8_laplacian_packed(cuda, form, n, aligned):
 @pytest.mark.parametrize("form", ["fp32_stencil", "fp32_em", "fp64_stencil"])
 def test_tile_wait_gives_up_and_reports(cuda, form):
     """Failure detection without a fault: the first wait on each tile's bulk copy is
-    limited to one poll, so tiles give up before their copy has landed.  Each such CTA
-    records the status and drains its copy (normal long bound) before it exits; the
-    status is reported once, the context stays usable and the next apply is exact."""
+    given no polls, so every tile gives up.  Each CTA records the status and drains
+    its copy (normal long bound) before it exits; the status is reported once, the
+    context stays usable and the next apply is exact."""
     import torch
 
     L = 4
@@ -220,7 +220,7 @@ def test_tile_wait_gives_up_and_reports(cuda, form):
     assert lib.sfem_gb300_laplacian_status() == 0
     kprev = lib.sfem_gb300_set_laplacian_kernel(3 if form == "fp32_em" else -1)
     try:
-        prev = lib.sfem_gb300_set_tile_wait_polls(1)
+        prev = lib.sfem_gb300_set_tile_wait_polls(0)
         try:
             op.apply(x, y)
             torch.cuda.synchronize()
