@@ -125,6 +125,20 @@ int sfem_gb300_sshex8_laplacian_apply_packed(int element_type, ptrdiff_t nelemen
 int sfem_gb300_laplacian_status(void);
 int sfem_gb300_set_tile_wait_polls(int polls);
 
+/* Compensated residual (no reference counterpart; the reference evaluates residuals
+ * in the working precision, drivers/mgsolve.cpp:315): r = b - A x for the FP64
+ * operator given by its stored micro element matrices (row-major (8 bs) x (8 bs) per
+ * macro element, row / column = component * 8 + corner: the layout of
+ * sfem_gb300_sshex8_laplacian_element_matrix and
+ * sfem_gb300_linear_elasticity_element_matrices), block_size 1 or 3 (interleaved
+ * components), with every product and sum of A x carried in double-double and the
+ * scatter to shared nodes kept error-free, then rounded to double; constrained rows
+ * get b - x.  `work` holds 2 n_dofs doubles.  Certifies residuals far below the plain
+ * FP64 evaluation floor (about 1e-16 of (|A||x|)_i per entry). */
+int sfem_gb300_residual_dd(int element_type, int block_size, ptrdiff_t nelements, sfem_gb300_idx_t **elements,
+                           const double *element_matrices, ptrdiff_t n_dofs, const double *x, const double *b,
+                           ptrdiff_t n_dirichlet, const int32_t *dirichlet, double *work, double *r, void *stream);
+
 /* ------------------------------------------------------- linear elasticity */
 
 /* out += K u for the affine hex8 / sshex8 linear-elasticity operator with

@@ -387,3 +387,96 @@ def patchconv_backward_weights(P, cin, cout, gout, x):
     lib().or_patchconv_backward_weights(c_ptrdiff(P), c_int(cin), c_int(cout), _ptr(_f32(gout)), _ptr(_f32(x)),
                                         _ptr(dW))
     return dW
+
+
+# ---------------------------------------------------------------------------
+# compensated residuals and the CPU multigrid-CG solve
+# ---------------------------------------------------------------------------
+def laplacian_residual_dd(L, elements, fff_aos, x, b):
+    """b - A x with A x summed in double-double (sshex8 L >= 2), rounded to double;
+    constrained rows are left to the caller."""
+    E = elements.shape[1]
+    x, b = _f64(x), _f64(b)
+    r = np.zeros_like(x)
+    ea = PtrArray(elements.astype(np.int32))
+    f = _f32(fff_aos)
+    assert lib().or_sshex8_laplacian_residual_dd(c_int(L), c_ptrdiff(E), ea.p, _ptr(f), _ptr(x), _ptr(b),
+                                                 c_ptrdiff(x.size), _ptr(r)) == 0
+    return r
+
+
+def elasticity_residual_dd(L, elements, adj_aos, det, mu, lam, x, b):
+    """b - K x with K x summed in double-double (interleaved xyz), rounded to double."""
+    E = elements.shape[1]
+    x, b = _f64(x), _f64(b)
+    r = np.zeros_like(x)
+    ea = PtrArray(elements.astype(np.int32))
+    a, d = _f32(adj_aos), _f32(det)
+    assert lib().or_linear_elasticity_residual_dd(c_int(L), c_ptrdiff(E), ea.p, _ptr(a), _ptr(d), c_double(mu),
+                                                  c_double(lam), _ptr(x), _ptr(b), c_ptrdiff(x.size), _ptr(r)) == 0
+    return r
+
+
+class _Level(C.Structure):
+    _fields_ = [("L", c_int), ("elements", c_void_p), ("hex8_elements", c_void_p), ("n_nodes", c_ptrdiff),
+                ("n_dirichlet", c_ptrdiff), ("dirichlet", c_void_p), ("count", c_void_p)]
+
+
+class _Problem(C.Structure):
+    _fields_ = [("kind", c_int), ("nelements", c_ptrdiff), ("geom", c_void_p), ("det", c_void_p), ("mu", c_double),
+                ("lam", c_double), ("nlevels", c_int), ("levels", C.POINTER(_Level)), ("sweeps", c_int),
+                ("scaled", c_int), ("scale_eig_max", c_double), ("coarse_rtol", c_double), ("rtol", c_double),
+                ("max_it", c_int), ("flexible", c_int)]
+
+
+class _Stats(C.Structure):
+    _fields_ = [("iterations", c_int), ("restarts", c_int), ("coarse_iterations", c_int),
+                ("true_rel_residual", c_double), ("setup_seconds", c_double), ("solve_seconds", c_double)]
+
+
+def mg_pcg_solve(mesh, kind, b, dirichlet_faces=("x0",), geom=None, det=None, mu=1.0, lam=10.0, sweeps=2,
+                 scaled=True, scale_eig_max=1.02, coarse_rtol=1e-8, rtol=1e-10, max_it=200, flexible=False):
+    """CPU multigrid-preconditioned CG (oracle/src/solve.c) on the derefinement levels of an
+    SSMesh (kind "laplacian" or "elasticity"); returns (x, stats dict).  geom: FFF AoS (or
+    adjugate AoS with det) of the macro elements; computed here when omitted."""
+    from sfem_gb300.mesh import derefinement_levels
+
+    L = mesh.L
+    keep = []
+    levels = []
+    for lv in derefinement_levels(L):
+        el = mesh.elements(lv)
+        pe = PtrArray(el.astype(np.int32))
+        keep.append(pe)
+        h8 = None
+        if lv == 1:
+            h8 = PtrArray(mesh.hex8_elements().astype(np.int32))
+            keep.append(h8)
+        n = mesh.n_nodes(lv)
+        dn = np.unique(np.concatenate([mesh.boundary_nodes(f, lv) for f in dirichlet_faces])).astype(np.int32)
+        cnt = incidence_count(lv, el, n)
+        keep += [dn, cnt]
+        levels.append(_Level(lv, pe.p.value, h8.p.value if h8 else None, n, dn.size, dn.ctypes.data,
+                             cnt.ctypes.data))
+    corners = mesh.elements(L)[mesh.macro_corner_lidx(L)]
+    if kind == "laplacian":
+        g = _f32(geom if geom is not None else fff_fill(corners, mesh.points))
+        d = None
+        k = 0
+    else:
+        if geom is None:
+            geom, det = adjugate_fill(corners, mesh.points)
+        g, d = _f32(geom), _f32(det)
+        k = 1
+    keep += [g, d]
+    arr = (_Level * len(levels))(*levels)
+    prob = _Problem(k, mesh.n_elements, g.ctypes.data, d.ctypes.data if d is not None else None, mu, lam,
+                    len(levels), arr, sweeps, int(scaled), scale_eig_max, coarse_rtol, rtol, max_it, int(flexible))
+    b = _f64(b)
+    x = np.zeros_like(b)
+    st = _Stats()
+    rc = lib().or_mg_pcg_solve(C.byref(prob), _ptr(b), _ptr(x), C.byref(st))
+    stats = {"rc": rc, "iterations": st.iterations, "restarts": st.restarts,
+             "coarse_iterations": st.coarse_iterations, "true_rel_residual": st.true_rel_residual,
+             "setup_seconds": st.setup_seconds, "solve_seconds": st.solve_seconds}
+    return x, stats

@@ -62,7 +62,7 @@ def _stale(target: Path, sources) -> bool:
 
 
 def build_oracle(force: bool = False) -> Path:
-    srcs = [HERE / "src" / "oracle.c"]
+    srcs = [HERE / "src" / "oracle.c", HERE / "src" / "solve.c"]
     if force or _stale(ORACLE_LIB, srcs):
         ORACLE_LIB.parent.mkdir(parents=True, exist_ok=True)
         _run(["gcc", "-O3", "-fopenmp", "-fPIC", "-shared", "-o", str(ORACLE_LIB)] + [str(s) for s in srcs] + ["-lm"])

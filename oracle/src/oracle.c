@@ -978,3 +978,118 @@ void or_patchconv_backward_weights(ptrdiff_t P, int cin, int cout, const float *
                 dW[(co * cin + ci) * 27 + o] += acc;
             }
 }
+
+/* ------------------------------------------------------------------------ */
+/* Compensated (double-double) residuals                                    */
+/* ------------------------------------------------------------------------ */
+
+/* Error-free transformations (Knuth's TwoSum; TwoProduct with a fused multiply-add):
+ * a + b = s + e and a * b = p + e exactly. */
+static inline void two_sum(double a, double b, double *s, double *e) {
+    const double x = a + b, bb = x - a;
+    *s = x;
+    *e = (a - (x - bb)) + (b - bb);
+}
+static inline void dd_add(double *hi, double *lo, double v) {
+    double s, e;
+    two_sum(*hi, v, &s, &e);
+    *hi = s;
+    *lo += e;
+}
+static inline void dd_fma(double *hi, double *lo, double a, double b) {
+    const double p = a * b, pe = fma(a, b, -p);
+    dd_add(hi, lo, p);
+    *lo += pe;
+}
+
+/* r = b - A x with the products and sums of A x carried in double-double: the
+ * residual of the FP64 operator (element matrices in double, as the apply) evaluated
+ * to about 1e-30 relative to |A||x| instead of 1e-16, so residuals far below the
+ * plain-FP64 evaluation floor can be measured.  Element contributions are formed in
+ * parallel and summed node by node in element order.  kind 0: sshex8 Laplacian from
+ * the FFF (L >= 2), kind 1: linear elasticity (3 interleaved components; L = 0 plain
+ * hex8).  Rows of the constrained dofs are left to the caller. */
+static int residual_dd(int kind, int L, ptrdiff_t nelements, idx_t **elements, const jacobian_t *geom,
+                       const jacobian_t *det, double mu, double lambda, const double *x, const double *b,
+                       ptrdiff_t ndofs, double *r) {
+    const int bs = kind == 1 ? 3 : 1;
+    const int Lm = L > 0 ? L : 1;
+    const int nxe = L > 0 ? (L + 1) * (L + 1) * (L + 1) : 8;
+    const int nloc = nxe * bs;
+    double *buf = (double *)malloc((size_t)nelements * nloc * 2 * sizeof(double));
+    if (!buf) return 1;
+#pragma omp parallel
+    {
+        double *K = (double *)malloc(576 * sizeof(double));
+#pragma omp for
+        for (ptrdiff_t e = 0; e < nelements; e++) {
+            double *hi = buf + (size_t)e * nloc * 2, *lo = hi + nloc;
+            for (int i = 0; i < nloc; i++) hi[i] = lo[i] = 0;
+            int ne = 8;
+            if (kind == 0) {
+                double sub[6];
+                for (int d = 0; d < 6; d++) sub[d] = (double)geom[e * 6 + d] * (1.0 / Lm);
+                or_hex8_laplacian_matrix(sub, K);
+            } else {
+                double adj[9], dt;
+                sub_adjugate(geom, det, e, Lm, adj, &dt);
+                or_hex8_linear_elasticity_matrix(mu, lambda, adj, dt, K);
+                ne = 24;
+            }
+            for (int zi = 0; zi < Lm; zi++)
+                for (int yi = 0; yi < Lm; yi++)
+                    for (int xi = 0; xi < Lm; xi++) {
+                        int lev[8];
+                        if (L > 0)
+                            sshex8_micro_nodes(L, xi, yi, zi, lev);
+                        else
+                            for (int c = 0; c < 8; c++) lev[c] = c;
+                        double ue[24];
+                        for (int c = 0; c < 8; c++)
+                            for (int d = 0; d < bs; d++)
+                                ue[d * 8 + c] = x[(ptrdiff_t)elements[lev[c]][e] * bs + d];
+                        for (int i = 0; i < ne; i++) {
+                            double h = 0, l = 0;
+                            for (int j = 0; j < ne; j++) dd_fma(&h, &l, K[i * ne + j], ue[j]);
+                            const int slot = lev[i % 8] * bs + i / 8;
+                            dd_add(&hi[slot], &lo[slot], h);
+                            lo[slot] += l;
+                        }
+                    }
+        }
+        free(K);
+    }
+    double *ahi = (double *)calloc(ndofs, sizeof(double)), *alo = (double *)calloc(ndofs, sizeof(double));
+    for (ptrdiff_t e = 0; e < nelements; e++) {
+        const double *hi = buf + (size_t)e * nloc * 2, *lo = hi + nloc;
+        for (int v = 0; v < nxe; v++) {
+            const ptrdiff_t g = elements[v][e];
+            for (int d = 0; d < bs; d++) {
+                dd_add(&ahi[g * bs + d], &alo[g * bs + d], hi[v * bs + d]);
+                alo[g * bs + d] += lo[v * bs + d];
+            }
+        }
+    }
+#pragma omp parallel for
+    for (ptrdiff_t i = 0; i < ndofs; i++) {
+        double h = b[i], l = 0;
+        dd_add(&h, &l, -ahi[i]);
+        l -= alo[i];
+        r[i] = h + l;
+    }
+    free(ahi);
+    free(alo);
+    free(buf);
+    return 0;
+}
+
+int or_sshex8_laplacian_residual_dd(int L, ptrdiff_t nelements, idx_t **elements, const jacobian_t *fff,
+                                    const double *x, const double *b, ptrdiff_t n, double *r) {
+    return residual_dd(0, L, nelements, elements, fff, NULL, 0, 0, x, b, n, r);
+}
+
+int or_linear_elasticity_residual_dd(int L, ptrdiff_t nelements, idx_t **elements, const jacobian_t *adjugate,
+                                     const jacobian_t *determinant, double mu, double lambda, const double *x,
+                                     const double *b, ptrdiff_t ndofs, double *r) {
+    return residual_dd(1, L, nelements, elements, adjugate, determinant, mu, lambda, x, b, ndofs, r);
+}

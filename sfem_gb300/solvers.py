@@ -413,3 +413,50 @@ def build_elasticity_mg(ctx, H: Hierarchy, dtype, mu=1.0, lam=10.0, sweeps=2, co
     if graph:
         mg_set_graph(mg, True)
     return mg, fine_op
+
+
+class CompensatedResidual:
+    """r = b - A x of the finest level's FP64 operator with A x accumulated in
+    double-double (``sfem_gb300_residual_dd``): the residual of an FP64 iterate to
+    about 1e-30 relative to (|A||x|)_i, where a plain FP64 evaluation is limited to
+    about 1e-16 (|A||x|)_i.  kind: "laplacian" (the hierarchy's FFF, coefficient
+    included) or "elasticity" (mu, lam)."""
+
+    def __init__(self, H: Hierarchy, kind="laplacian", mu=1.0, lam=10.0):
+        import torch
+
+        sp = H.spaces[0]
+        E = sp.n_elements
+        lib = _lib()
+        self.space, self.dirichlet = sp, H.dirichlet[0]
+        self.bs = 3 if kind == "elasticity" else 1
+        ne = 8 * self.bs
+        self.em = torch.empty(E * ne * ne, dtype=torch.float64, device=H.device)
+        if kind == "elasticity":
+            capi.check(lib.sfem_gb300_linear_elasticity_element_matrices(
+                sp.element_type, capi.i64(E), capi.i64(H.adj.shape[1]), capi.vp(H.adj), capi.vp(H.det),
+                c_double(mu), c_double(lam), capi.FLOAT64, capi.vp(self.em), None), "element matrices")
+        else:
+            capi.check(lib.sfem_gb300_sshex8_laplacian_element_matrix(
+                sp.element_type, capi.i64(E), capi.i64(H.fff.shape[1]), capi.vp(H.fff), capi.FLOAT64,
+                capi.vp(self.em), None), "element matrices")
+        # hex8 levels keep their corners in hex8 order; sshex8 levels in lidx order
+        self.elements = sp.elements_ptrs
+        self.n = self.bs * sp.n_nodes
+        self.work = torch.empty(2 * self.n, dtype=torch.float64, device=H.device)
+
+    def __call__(self, x, b, r=None):
+        import torch
+
+        r = torch.empty_like(b) if r is None else r
+        capi.check(_lib().sfem_gb300_residual_dd(
+            self.space.element_type, c_int(self.bs), capi.i64(self.space.n_elements), self.elements.ptr,
+            capi.vp(self.em), capi.i64(self.n), capi.vp(x), capi.vp(b), capi.i64(self.dirichlet.numel()),
+            capi.vp(self.dirichlet), capi.vp(self.work), capi.vp(r), None), "sfem_gb300_residual_dd")
+        return r
+
+    def relative(self, x, b):
+        import torch
+
+        r = self(x, b)
+        return float(torch.linalg.vector_norm(r) / torch.linalg.vector_norm(b))
