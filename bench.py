@@ -364,27 +364,37 @@ def _timed_solve(S, solver, b, x):
     return rc, time.perf_counter() - t0
 
 
-def refine_dd(S, res, inner, b, x, rtol, max_outer=8):
+def refine_dd(S, res, inner, b, x, rtol, max_outer=8, x_lo=None, stall=0.5):
     """Iterative refinement driven by the compensated residual: r = b - A x in
     double-double (``res``), stop when ||r|| / ||b|| <= rtol, else solve A e = r with
-    ``inner`` from e = 0 and update x += e in FP64.  Returns (relative residual, outer
-    steps, inner iterations)."""
+    ``inner`` from e = 0 and update x += e -- in FP64, or error-free into the
+    double-double solution (x, x_lo) when x_lo is given.  Also stops when a step fails
+    to cut the residual by the factor ``stall`` (the floor of an FP64 solution vector).
+    Returns (relative residual, outer steps, inner iterations, stalled)."""
     import torch
 
     nb = torch.linalg.vector_norm(b)
     e = torch.zeros_like(b)
-    r = res(x, b)
+    r = res(x, b, x_lo=x_lo)
     rel = float(torch.linalg.vector_norm(r) / nb)
     outer = inner_its = 0
+    stalled = False
     while rel > rtol and outer < max_outer:
         e.zero_()
         S.solve(inner, r, e)
         inner_its += S.stats(inner)[0]
-        x += e
-        res(x, b, r)
-        rel = float(torch.linalg.vector_norm(r) / nb)
+        if x_lo is None:
+            x += e
+        else:
+            S.dd_axpy(1.0, e, x, x_lo)
+        res(x, b, r, x_lo=x_lo)
+        new = float(torch.linalg.vector_norm(r) / nb)
         outer += 1
-    return rel, outer, inner_its
+        stalled = new > stall * rel
+        rel = new
+        if stalled:
+            break
+    return rel, outer, inner_its, stalled
 
 
 def _timed(fn):
@@ -586,12 +596,22 @@ def measure_elasticity_solves(dev, nx=64, ny=16, nz=16, rtol=1e-10, mu=1.0, lam=
                                   residual_norm=True, flexible=True)}
     sols = {}
     for name, inner in arms.items():
-        x = torch.zeros_like(b)
         refine_dd(S, res, inner, b, torch.zeros_like(b), rtol, max_outer=1)  # warm-up of both graphs
-        (rel, outer, its), sec = _timed(lambda: refine_dd(S, res, inner, b, x, rtol))
+        # the solution kept in double-double (x, x_lo): the refinement reaches rtol
+        x, xl = torch.zeros_like(b), torch.zeros_like(b)
+        (rel, outer, its, _), sec = _timed(lambda: refine_dd(S, res, inner, b, x, rtol, x_lo=xl))
         sols[name] = x
+        # the same refinement with a plain FP64 solution vector: it stops at the floor that
+        # rounding the solution to FP64 leaves (measured, both residual evaluations)
+        x64v = torch.zeros_like(b)
+        (rel64, outer64, its64, stalled), sec64 = _timed(lambda: refine_dd(S, res, inner, b, x64v, rtol))
         out[name] = {"seconds": sec, "outer_steps": outer, "iterations": its, "double_double_rel_residual": rel,
-                     "fp64_rel_residual": fp64_rel(x), "rc": int(rel > rtol)}
+                     "rc": int(rel > rtol), "solution": "double-double (x_hi + x_lo)",
+                     "rounded_solution_rel_residual": {"double_double": res.relative(x, b),
+                                                       "fp64_evaluation": fp64_rel(x)},
+                     "fp64_solution_vector": {"seconds": sec64, "outer_steps": outer64, "iterations": its64,
+                                              "double_double_rel_residual": rel64, "stalled": stalled,
+                                              "fp64_evaluation_rel_residual": fp64_rel(x64v)}}
     x64 = sols["plain_fp64_mg_pcg"]
     out["mixed_precond"]["solution_rel_diff_vs_plain_fp64"] = float(
         torch.linalg.vector_norm(sols["mixed_precond"] - x64) / torch.linalg.vector_norm(x64))

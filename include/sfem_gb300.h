@@ -133,11 +133,15 @@ int sfem_gb300_set_tile_wait_polls(int polls);
  * sfem_gb300_linear_elasticity_element_matrices), block_size 1 or 3 (interleaved
  * components), with every product and sum of A x carried in double-double and the
  * scatter to shared nodes kept error-free, then rounded to double; constrained rows
- * get b - x.  `work` holds 2 n_dofs doubles.  Certifies residuals far below the plain
- * FP64 evaluation floor (about 1e-16 of (|A||x|)_i per entry). */
+ * get b - x.  x may be an unevaluated sum x + x_lo (x_lo NULL: zero), so a solution
+ * kept in double-double is judged exactly.  `work` holds 2 n_dofs doubles.  Certifies
+ * residuals far below the plain FP64 evaluation floor (about 1e-16 of (|A||x|)_i per
+ * entry).  sfem_gb300_dd_axpy: (x_hi, x_lo) += alpha e with an error-free sum. */
 int sfem_gb300_residual_dd(int element_type, int block_size, ptrdiff_t nelements, sfem_gb300_idx_t **elements,
-                           const double *element_matrices, ptrdiff_t n_dofs, const double *x, const double *b,
-                           ptrdiff_t n_dirichlet, const int32_t *dirichlet, double *work, double *r, void *stream);
+                           const double *element_matrices, ptrdiff_t n_dofs, const double *x, const double *x_lo,
+                           const double *b, ptrdiff_t n_dirichlet, const int32_t *dirichlet, double *work, double *r,
+                           void *stream);
+int sfem_gb300_dd_axpy(ptrdiff_t n, double alpha, const double *e, double *x_hi, double *x_lo, void *stream);
 
 /* ------------------------------------------------------- linear elasticity */
 

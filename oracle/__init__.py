@@ -417,6 +417,20 @@ def elasticity_residual_dd(L, elements, adj_aos, det, mu, lam, x, b):
     return r
 
 
+def residual_dd_em(bs, L, elements, em, x, b, x_lo=None):
+    """b - A (x + x_lo) in double-double from given micro element matrices (the GPU's)."""
+    E = elements.shape[1]
+    x, b = _f64(x), _f64(b)
+    r = np.zeros_like(x)
+    ea = PtrArray(elements.astype(np.int32))
+    em = _f64(em)
+    xl = _f64(x_lo) if x_lo is not None else None
+    assert lib().or_residual_dd_em(c_int(bs), c_int(L), c_ptrdiff(E), ea.p, _ptr(em), _ptr(x),
+                                   _ptr(xl) if xl is not None else c_void_p(0), _ptr(b), c_ptrdiff(x.size),
+                                   _ptr(r)) == 0
+    return r
+
+
 class _Level(C.Structure):
     _fields_ = [("L", c_int), ("elements", c_void_p), ("hex8_elements", c_void_p), ("n_nodes", c_ptrdiff),
                 ("n_dirichlet", c_ptrdiff), ("dirichlet", c_void_p), ("count", c_void_p)]

@@ -1010,8 +1010,8 @@ static inline void dd_fma(double *hi, double *lo, double a, double b) {
  * the FFF (L >= 2), kind 1: linear elasticity (3 interleaved components; L = 0 plain
  * hex8).  Rows of the constrained dofs are left to the caller. */
 static int residual_dd(int kind, int L, ptrdiff_t nelements, idx_t **elements, const jacobian_t *geom,
-                       const jacobian_t *det, double mu, double lambda, const double *x, const double *b,
-                       ptrdiff_t ndofs, double *r) {
+                       const jacobian_t *det, double mu, double lambda, const double *em, const double *x,
+                       const double *x_lo, const double *b, ptrdiff_t ndofs, double *r) {
     const int bs = kind == 1 ? 3 : 1;
     const int Lm = L > 0 ? L : 1;
     const int nxe = L > 0 ? (L + 1) * (L + 1) * (L + 1) : 8;
@@ -1025,8 +1025,10 @@ static int residual_dd(int kind, int L, ptrdiff_t nelements, idx_t **elements, c
         for (ptrdiff_t e = 0; e < nelements; e++) {
             double *hi = buf + (size_t)e * nloc * 2, *lo = hi + nloc;
             for (int i = 0; i < nloc; i++) hi[i] = lo[i] = 0;
-            int ne = 8;
-            if (kind == 0) {
+            const int ne = kind == 1 ? 24 : 8;
+            if (em) {
+                memcpy(K, em + (size_t)e * ne * ne, (size_t)ne * ne * sizeof(double));
+            } else if (kind == 0) {
                 double sub[6];
                 for (int d = 0; d < 6; d++) sub[d] = (double)geom[e * 6 + d] * (1.0 / Lm);
                 or_hex8_laplacian_matrix(sub, K);
@@ -1034,7 +1036,6 @@ static int residual_dd(int kind, int L, ptrdiff_t nelements, idx_t **elements, c
                 double adj[9], dt;
                 sub_adjugate(geom, det, e, Lm, adj, &dt);
                 or_hex8_linear_elasticity_matrix(mu, lambda, adj, dt, K);
-                ne = 24;
             }
             for (int zi = 0; zi < Lm; zi++)
                 for (int yi = 0; yi < Lm; yi++)
@@ -1044,13 +1045,19 @@ static int residual_dd(int kind, int L, ptrdiff_t nelements, idx_t **elements, c
                             sshex8_micro_nodes(L, xi, yi, zi, lev);
                         else
                             for (int c = 0; c < 8; c++) lev[c] = c;
-                        double ue[24];
+                        double ue[24], ul[24];
                         for (int c = 0; c < 8; c++)
-                            for (int d = 0; d < bs; d++)
-                                ue[d * 8 + c] = x[(ptrdiff_t)elements[lev[c]][e] * bs + d];
+                            for (int d = 0; d < bs; d++) {
+                                const ptrdiff_t q = (ptrdiff_t)elements[lev[c]][e] * bs + d;
+                                ue[d * 8 + c] = x[q];
+                                ul[d * 8 + c] = x_lo ? x_lo[q] : 0.0;
+                            }
                         for (int i = 0; i < ne; i++) {
                             double h = 0, l = 0;
-                            for (int j = 0; j < ne; j++) dd_fma(&h, &l, K[i * ne + j], ue[j]);
+                            for (int j = 0; j < ne; j++) {
+                                dd_fma(&h, &l, K[i * ne + j], ue[j]);
+                                l = fma(K[i * ne + j], ul[j], l);
+                            }
                             const int slot = lev[i % 8] * bs + i / 8;
                             dd_add(&hi[slot], &lo[slot], h);
                             lo[slot] += l;
@@ -1085,11 +1092,18 @@ static int residual_dd(int kind, int L, ptrdiff_t nelements, idx_t **elements, c
 
 int or_sshex8_laplacian_residual_dd(int L, ptrdiff_t nelements, idx_t **elements, const jacobian_t *fff,
                                     const double *x, const double *b, ptrdiff_t n, double *r) {
-    return residual_dd(0, L, nelements, elements, fff, NULL, 0, 0, x, b, n, r);
+    return residual_dd(0, L, nelements, elements, fff, NULL, 0, 0, NULL, x, NULL, b, n, r);
 }
 
 int or_linear_elasticity_residual_dd(int L, ptrdiff_t nelements, idx_t **elements, const jacobian_t *adjugate,
                                      const jacobian_t *determinant, double mu, double lambda, const double *x,
                                      const double *b, ptrdiff_t ndofs, double *r) {
-    return residual_dd(1, L, nelements, elements, adjugate, determinant, mu, lambda, x, b, ndofs, r);
+    return residual_dd(1, L, nelements, elements, adjugate, determinant, mu, lambda, NULL, x, NULL, b, ndofs, r);
+}
+
+/* The same from given micro element matrices em[e][(8 bs)^2] (bs 1: kind 0, bs 3: kind 1)
+ * and a solution given as x + x_lo (x_lo may be NULL). */
+int or_residual_dd_em(int bs, int L, ptrdiff_t nelements, idx_t **elements, const double *em, const double *x,
+                      const double *x_lo, const double *b, ptrdiff_t ndofs, double *r) {
+    return residual_dd(bs == 3 ? 1 : 0, L, nelements, elements, NULL, NULL, 0, 0, em, x, x_lo, b, ndofs, r);
 }

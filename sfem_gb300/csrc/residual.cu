@@ -49,7 +49,8 @@ template <int BS>
 __global__ void __launch_bounds__(128) residual_dd_scatter_kernel(int L, ptrdiff_t nelements,
                                                                   const idx_t *const *elements,
                                                                   const double *__restrict__ em,
-                                                                  const double *__restrict__ x, double *hi,
+                                                                  const double *__restrict__ x,
+                                                                  const double *__restrict__ x_lo, double *hi,
                                                                   double *lo) {
     constexpr int NE = 8 * BS;
     extern __shared__ __align__(16) unsigned char rdd_smem[];
@@ -57,7 +58,8 @@ __global__ void __launch_bounds__(128) residual_dd_scatter_kernel(int L, ptrdiff
     const int Lm = L > 0 ? L : 1;
     const int nxe = L > 0 ? (L + 1) * (L + 1) * (L + 1) : 8;
     double *xe = K + NE * NE;
-    idx_t *ids = reinterpret_cast<idx_t *>(xe + nxe * BS);
+    double *xl = xe + nxe * BS;
+    idx_t *ids = reinterpret_cast<idx_t *>(xl + nxe * BS);
     const int nm = Lm * Lm * Lm;
     for (ptrdiff_t e = blockIdx.x; e < nelements; e += gridDim.x) {
         for (int k = threadIdx.x; k < NE * NE; k += blockDim.x) K[k] = em[e * NE * NE + k];
@@ -65,13 +67,20 @@ __global__ void __launch_bounds__(128) residual_dd_scatter_kernel(int L, ptrdiff
             const idx_t g = elements[v][e];
             ids[v] = g;
 #pragma unroll
-            for (int d = 0; d < BS; d++) xe[v * BS + d] = x[(ptrdiff_t)g * BS + d];
+            for (int d = 0; d < BS; d++) {
+                xe[v * BS + d] = x[(ptrdiff_t)g * BS + d];
+                xl[v * BS + d] = x_lo ? x_lo[(ptrdiff_t)g * BS + d] : 0.0;
+            }
         }
         __syncthreads();
         for (int w = threadIdx.x; w < nm * NE; w += blockDim.x) {
             const int m = w / NE, i = w % NE;
             double h = 0, l = 0;
-            for (int j = 0; j < NE; j++) dd_fma(h, l, K[i * NE + j], xe[micro_node(L, m, j % 8) * BS + j / 8]);
+            for (int j = 0; j < NE; j++) {
+                const int q = micro_node(L, m, j % 8) * BS + j / 8;
+                dd_fma(h, l, K[i * NE + j], xe[q]);
+                l = fma(K[i * NE + j], xl[q], l);  // the low part of x: its product's error is negligible
+            }
             const ptrdiff_t dof = (ptrdiff_t)ids[micro_node(L, m, i % 8)] * BS + i / 8;
             const double old = atomicAdd(&hi[dof], h);
             double s, err;
@@ -92,11 +101,21 @@ __global__ void residual_dd_finish_kernel(ptrdiff_t n, const double *__restrict_
 }
 
 __global__ void residual_dd_dirichlet_kernel(ptrdiff_t nd, const int32_t *nodes, int bs, const double *b,
-                                             const double *x, double *r) {
+                                             const double *x, const double *x_lo, double *r) {
     for (ptrdiff_t k = blockIdx.x * (ptrdiff_t)blockDim.x + threadIdx.x; k < nd * bs;
          k += (ptrdiff_t)gridDim.x * blockDim.x) {
         const ptrdiff_t dof = (ptrdiff_t)nodes[k / bs] * bs + k % bs;
-        r[dof] = b[dof] - x[dof];
+        r[dof] = (b[dof] - x[dof]) - (x_lo ? x_lo[dof] : 0.0);
+    }
+}
+
+// (x_hi, x_lo) += e with TwoSum: the solution kept as an unevaluated double-double sum
+__global__ void dd_axpy_kernel(ptrdiff_t n, double alpha, const double *__restrict__ e, double *x_hi, double *x_lo) {
+    for (ptrdiff_t i = blockIdx.x * (ptrdiff_t)blockDim.x + threadIdx.x; i < n; i += (ptrdiff_t)gridDim.x * blockDim.x) {
+        double s, err;
+        two_sum(x_hi[i], alpha * e[i], s, err);
+        x_hi[i] = s;
+        x_lo[i] += err;
     }
 }
 
@@ -107,8 +126,8 @@ using namespace sfem_gb300;
 
 extern "C" int sfem_gb300_residual_dd(int element_type, int block_size, ptrdiff_t nelements, idx_t **elements,
                                       const double *element_matrices, ptrdiff_t n_dofs, const double *x,
-                                      const double *b, ptrdiff_t n_dirichlet, const int32_t *dirichlet, double *work,
-                                      double *r, void *stream) {
+                                      const double *x_lo, const double *b, ptrdiff_t n_dirichlet,
+                                      const int32_t *dirichlet, double *work, double *r, void *stream) {
     const cudaStream_t s = stream_of(stream);
     int L;
     if (element_type == SFEM_GB300_HEX8)
@@ -126,7 +145,7 @@ extern "C" int sfem_gb300_residual_dd(int element_type, int block_size, ptrdiff_
     if (nelements > 0) {
         const int ne = 8 * block_size;
         const int nxe = L > 0 ? (L + 1) * (L + 1) * (L + 1) : 8;
-        const size_t smem = (size_t)ne * ne * sizeof(double) + (size_t)nxe * block_size * sizeof(double) +
+        const size_t smem = (size_t)ne * ne * sizeof(double) + 2 * (size_t)nxe * block_size * sizeof(double) +
                             (size_t)nxe * sizeof(idx_t);
         if (smem > 200 * 1024) return set_error("sfem_gb300_residual_dd: level %d too large", L);
         const int grid = (int)std::min<ptrdiff_t>(nelements, (ptrdiff_t)kNumSMs * 8);
@@ -134,14 +153,14 @@ extern "C" int sfem_gb300_residual_dd(int element_type, int block_size, ptrdiff_
             if (smem > 48 * 1024)
                 cudaFuncSetAttribute(residual_dd_scatter_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)smem);
-            residual_dd_scatter_kernel<1><<<grid, 128, smem, s>>>(L, nelements, elements, element_matrices, x, hi,
-                                                                   lo);
+            residual_dd_scatter_kernel<1><<<grid, 128, smem, s>>>(L, nelements, elements, element_matrices, x, x_lo,
+                                                                   hi, lo);
         } else {
             if (smem > 48 * 1024)
                 cudaFuncSetAttribute(residual_dd_scatter_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)smem);
-            residual_dd_scatter_kernel<3><<<grid, 128, smem, s>>>(L, nelements, elements, element_matrices, x, hi,
-                                                                   lo);
+            residual_dd_scatter_kernel<3><<<grid, 128, smem, s>>>(L, nelements, elements, element_matrices, x, x_lo,
+                                                                   hi, lo);
         }
         if (check_launch("sfem_gb300_residual_dd (scatter)")) return SFEM_GB300_FAILURE;
     }
@@ -151,8 +170,15 @@ extern "C" int sfem_gb300_residual_dd(int element_type, int block_size, ptrdiff_
     }
     if (n_dirichlet > 0) {
         residual_dd_dirichlet_kernel<<<grid_for(n_dirichlet * block_size, 256), 256, 0, s>>>(n_dirichlet, dirichlet,
-                                                                                             block_size, b, x, r);
+                                                                                             block_size, b, x, x_lo, r);
         return check_launch("sfem_gb300_residual_dd (constraints)");
     }
     return SFEM_GB300_SUCCESS;
+}
+
+extern "C" int sfem_gb300_dd_axpy(ptrdiff_t n, double alpha, const double *e, double *x_hi, double *x_lo,
+                                  void *stream) {
+    if (n <= 0) return SFEM_GB300_SUCCESS;
+    dd_axpy_kernel<<<grid_for(n, 256), 256, 0, stream_of(stream)>>>(n, alpha, e, x_hi, x_lo);
+    return check_launch("sfem_gb300_dd_axpy");
 }

@@ -445,18 +445,26 @@ class CompensatedResidual:
         self.n = self.bs * sp.n_nodes
         self.work = torch.empty(2 * self.n, dtype=torch.float64, device=H.device)
 
-    def __call__(self, x, b, r=None):
+    def __call__(self, x, b, r=None, x_lo=None):
+        """b - A (x + x_lo) (x_lo: the low part of a double-double solution, or None)."""
         import torch
 
         r = torch.empty_like(b) if r is None else r
         capi.check(_lib().sfem_gb300_residual_dd(
             self.space.element_type, c_int(self.bs), capi.i64(self.space.n_elements), self.elements.ptr,
-            capi.vp(self.em), capi.i64(self.n), capi.vp(x), capi.vp(b), capi.i64(self.dirichlet.numel()),
-            capi.vp(self.dirichlet), capi.vp(self.work), capi.vp(r), None), "sfem_gb300_residual_dd")
+            capi.vp(self.em), capi.i64(self.n), capi.vp(x), capi.vp(x_lo), capi.vp(b),
+            capi.i64(self.dirichlet.numel()), capi.vp(self.dirichlet), capi.vp(self.work), capi.vp(r), None),
+            "sfem_gb300_residual_dd")
         return r
 
-    def relative(self, x, b):
+    def relative(self, x, b, x_lo=None):
         import torch
 
-        r = self(x, b)
+        r = self(x, b, x_lo=x_lo)
         return float(torch.linalg.vector_norm(r) / torch.linalg.vector_norm(b))
+
+
+def dd_axpy(alpha, e, x_hi, x_lo):
+    """(x_hi, x_lo) += alpha e, error-free (the solution of a refinement kept in double-double)."""
+    capi.check(_lib().sfem_gb300_dd_axpy(capi.i64(e.numel()), c_double(alpha), capi.vp(e), capi.vp(x_hi),
+                                         capi.vp(x_lo), None), "sfem_gb300_dd_axpy")
