@@ -172,6 +172,33 @@ int sfem_gb300_linear_elasticity_apply_em(int element_type, ptrdiff_t nelements,
 int sfem_gb300_set_elasticity_kernel(int variant);
 int sfem_gb300_elasticity_status(void);
 
+/* The reference's linear-elasticity entry points under its names and argument order
+ * (operators/cuda/cu_linear_elasticity.hpp:15-60): interleaved xyz vectors, SoA float
+ * adjugate (9 x jacobian_stride) and determinant.
+ *  - cu_linear_elasticity_apply: y += K x, HEX8 or SSHEX8(L) (:15-26);
+ *  - cu_linear_elasticity_diag: diag += diag(K) (3 per node, :28-38);
+ *  - cu_linear_elasticity_block_diag_sym_aos: out += the symmetric 3 x 3 node blocks
+ *    (6 per node: 00, 01, 02, 11, 12, 22, :55-65);
+ *  - cu_linear_elasticity_bsr: values += K on a block sparse row pattern with 3 x 3
+ *    row-major blocks (HEX8, as the reference, :41-53; fails if an element node pair is
+ *    missing from the pattern). */
+int cu_linear_elasticity_apply(int element_type, ptrdiff_t nelements, sfem_gb300_idx_t **elements,
+                               ptrdiff_t jacobian_stride, const void *jacobian_adjugate,
+                               const void *jacobian_determinant, double mu, double lambda, int real_type,
+                               const void *x, void *y, void *stream);
+int cu_linear_elasticity_diag(int element_type, ptrdiff_t nelements, sfem_gb300_idx_t **elements,
+                              ptrdiff_t jacobian_stride, const void *jacobian_adjugate,
+                              const void *jacobian_determinant, double mu, double lambda, int real_type, void *diag,
+                              void *stream);
+int cu_linear_elasticity_block_diag_sym_aos(int element_type, ptrdiff_t nelements, sfem_gb300_idx_t **elements,
+                                            ptrdiff_t jacobian_stride, const void *jacobian_adjugate,
+                                            const void *jacobian_determinant, double mu, double lambda,
+                                            int real_type, void *out, void *stream);
+int cu_linear_elasticity_bsr(int element_type, ptrdiff_t nelements, sfem_gb300_idx_t **elements,
+                             ptrdiff_t jacobian_stride, const void *jacobian_adjugate, const void *jacobian_determinant,
+                             double mu, double lambda, int real_type, const int32_t *rowptr, const int32_t *colidx,
+                             void *values, void *stream);
+
 /* The reference's exact sshex8 entry point (operators/sshex8/cuda/cu_sshex8_linear_elasticity.cu:1730-1748);
  * only the interleaved layout (u_stride = out_stride = 3, uy = ux + 1, uz = ux + 2) is accepted. */
 int cu_affine_sshex8_linear_elasticity_apply(int level, ptrdiff_t nelements, sfem_gb300_idx_t **elements,
@@ -254,6 +281,24 @@ int sfem_gb300_bsr_sym_spmv(int real_type, int block_size, ptrdiff_t nblock_rows
 int sfem_gb300_hex8_laplacian_crs_sym(ptrdiff_t nelements, sfem_gb300_idx_t **elements, ptrdiff_t fff_stride,
                                       const float *fff, const int32_t *rowptr, const int32_t *colidx, int real_type,
                                       void *diag, void *offdiag, void *stream);
+
+/* values += the hex8 Laplacian on a full CRS graph (both triangles; elements in hex8
+ * corner order).  Fails if an element coupling is missing from the graph.  The
+ * reference's hex8_laplacian_crs (operators/hex8/hex8_laplacian.cpp:223) on the GPU. */
+int sfem_gb300_hex8_laplacian_crs(ptrdiff_t nelements, sfem_gb300_idx_t **elements, ptrdiff_t fff_stride,
+                                  const float *fff, const int32_t *rowptr, const int32_t *colidx, int real_type,
+                                  void *values, void *stream);
+
+/* The reference's Laplacian assembly entry points under its names and argument order
+ * (operators/cuda/cu_laplacian.hpp:32-53): element_type HEX8 (the reference's CUDA
+ * crs_sym serves HEX8 only; its crs serves tetrahedra only, which are out of scope here,
+ * so cu_laplacian_crs serves HEX8 instead); others return FAILURE with a message. */
+int cu_laplacian_crs(int element_type, ptrdiff_t nelements, sfem_gb300_idx_t **elements, ptrdiff_t fff_stride,
+                     const void *fff, const int32_t *rowptr, const int32_t *colidx, int real_type, void *values,
+                     void *stream);
+int cu_laplacian_crs_sym(int element_type, ptrdiff_t nelements, sfem_gb300_idx_t **elements, ptrdiff_t fff_stride,
+                         const void *fff, const int32_t *rowptr, const int32_t *colidx, int real_type, void *diag,
+                         void *offdiag, void *stream);
 
 /* ------------------------------------------------------------ vector BLAS */
 /* Device-vector kernels of the BLAS<T> seam (algebra/sfem_tpl_blas.hpp:11-35;

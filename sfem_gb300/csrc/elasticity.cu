@@ -1051,9 +1051,97 @@ static int elasticity_diag_tpl(int element_type, ptrdiff_t nelements, idx_t **el
 #undef SFEM_EL_CASE
 }
 
+// position of column `col` in CRS row `row` (sorted columns), -1 if absent
+__device__ __forceinline__ idx_t bsr_find_col(const idx_t *rowptr, const idx_t *colidx, idx_t row, idx_t col) {
+    idx_t lo = rowptr[row], hi = rowptr[row + 1] - 1;
+    while (lo <= hi) {
+        const idx_t mid = (lo + hi) >> 1;
+        const idx_t c = colidx[mid];
+        if (c == col) return mid;
+        if (c < col)
+            lo = mid + 1;
+        else
+            hi = mid - 1;
+    }
+    return -1;
+}
+
+// Assembly of the hex8 (or one sshex8 micro level's macro) elasticity matrix into a block
+// sparse row pattern with 3 x 3 row-major blocks (affine_hex8_linear_elasticity_bsr,
+// operators/hex8/hex8_linear_elasticity.hpp:74-110; cu_affine_hex8_linear_elasticity_bsr,
+// operators/hex8/cuda/cu_hex8_linear_elasticity.cu:265): one warp per element builds K in
+// shared memory, lanes add its 8 x 8 node blocks into the pattern (values +=).
+template <typename T>
+__global__ void __launch_bounds__(64) elasticity_bsr_kernel(ptrdiff_t nelements, const idx_t *const *elements,
+                                                            ptrdiff_t stride, const float *adjugate,
+                                                            const float *determinant, T mu, T lambda,
+                                                            const idx_t *rowptr, const idx_t *colidx, T *values,
+                                                            int *missing) {
+    __shared__ T Ws[2][81];
+    __shared__ T Ks[2][576];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    T Ir[2][9];
+    load_grad_regs<T>(lane, Ir);
+    for (ptrdiff_t e = (ptrdiff_t)blockIdx.x * 2 + warp; e < nelements; e += (ptrdiff_t)gridDim.x * 2) {
+        T adj[9], AA[9], inv_det;
+        load_sub_adjugate<T>(adjugate, determinant, stride, e, 1, adj, AA, inv_det);
+        build_K_warp_sym<T>(adj, AA, inv_det, mu, lambda, Ir, Ws[warp], Ks[warp], 24, lane);
+        for (int ab = lane; ab < 64; ab += 32) {
+            const int a = ab >> 3, b = ab & 7;
+            const idx_t k = bsr_find_col(rowptr, colidx, elements[a][e], elements[b][e]);
+            if (k < 0) {
+                atomicAdd(missing, 1);
+                continue;
+            }
+#pragma unroll
+            for (int i = 0; i < 3; i++)
+#pragma unroll
+                for (int j = 0; j < 3; j++) atomicAdd(&values[(ptrdiff_t)k * 9 + i * 3 + j], Ks[warp][(i * 8 + a) * 24 + j * 8 + b]);
+        }
+        __syncwarp();
+    }
+}
+
 }  // namespace sfem_gb300
 
 using namespace sfem_gb300;
+
+extern "C" int cu_linear_elasticity_bsr(int element_type, ptrdiff_t nelements, idx_t **elements,
+                                        ptrdiff_t jacobian_stride, const void *jacobian_adjugate,
+                                        const void *jacobian_determinant, double mu, double lambda, int real_type,
+                                        const int32_t *rowptr, const int32_t *colidx, void *values, void *stream) {
+    if (element_type != SFEM_GB300_HEX8)
+        return set_error("cu_linear_elasticity_bsr: element type %d (HEX8 only, as the reference)", element_type);
+    if (nelements <= 0) return SFEM_GB300_SUCCESS;
+    const cudaStream_t s = stream_of(stream);
+    int *missing = nullptr;
+    if (cudaMallocAsync((void **)&missing, sizeof(int), s) != cudaSuccess)
+        return set_error("cu_linear_elasticity_bsr: allocation failed");
+    cudaMemsetAsync(missing, 0, sizeof(int), s);
+    const int blocks = grid_for((nelements + 1) / 2, 1, kNumSMs * 32);
+    if (real_type == SFEM_GB300_FLOAT32)
+        elasticity_bsr_kernel<float><<<blocks, 64, 0, s>>>(nelements, elements, jacobian_stride,
+                                                           (const float *)jacobian_adjugate,
+                                                           (const float *)jacobian_determinant, (float)mu,
+                                                           (float)lambda, rowptr, colidx, (float *)values, missing);
+    else if (real_type == SFEM_GB300_FLOAT64 || real_type == SFEM_GB300_REAL_DEFAULT)
+        elasticity_bsr_kernel<double><<<blocks, 64, 0, s>>>(nelements, elements, jacobian_stride,
+                                                            (const float *)jacobian_adjugate,
+                                                            (const float *)jacobian_determinant, mu, lambda, rowptr,
+                                                            colidx, (double *)values, missing);
+    else {
+        cudaFreeAsync(missing, s);
+        return set_error("cu_linear_elasticity_bsr: unsupported real type %d", real_type);
+    }
+    const int lerr = check_launch("cu_linear_elasticity_bsr");
+    int h_missing = 0;
+    cudaMemcpyAsync(&h_missing, missing, sizeof(int), cudaMemcpyDeviceToHost, s);
+    cudaStreamSynchronize(s);
+    cudaFreeAsync(missing, s);
+    if (lerr) return SFEM_GB300_FAILURE;
+    if (h_missing) return set_error("cu_linear_elasticity_bsr: %d element node pairs missing from the pattern", h_missing);
+    return SFEM_GB300_SUCCESS;
+}
 
 extern "C" int sfem_gb300_linear_elasticity_apply(int element_type, ptrdiff_t nelements, idx_t **elements,
                                                   ptrdiff_t jacobian_stride, const float *adjugate,

@@ -161,6 +161,35 @@ __global__ void hex8_laplacian_crs_sym_kernel(ptrdiff_t nelements, const idx_t *
     }
 }
 
+// hex8 Laplacian -> full CRS (every coupling, both triangles), one thread per element
+// (hex8_laplacian_crs, operators/hex8/hex8_laplacian.cpp:223).
+template <typename T>
+__global__ void hex8_laplacian_crs_kernel(ptrdiff_t nelements, const idx_t *const *elements, ptrdiff_t fff_stride,
+                                          const float *fff, const idx_t *rowptr, const idx_t *colidx, T *values,
+                                          int *missing) {
+    for (ptrdiff_t e = blockIdx.x * (ptrdiff_t)blockDim.x + threadIdx.x; e < nelements;
+         e += (ptrdiff_t)gridDim.x * blockDim.x) {
+        idx_t ev[8];
+        T f[6];
+#pragma unroll
+        for (int v = 0; v < 8; v++) ev[v] = elements[v][e];
+#pragma unroll
+        for (int m = 0; m < 6; m++) f[m] = (T)fff[m * fff_stride + e];
+        for (int i = 0; i < 8; i++) {
+            for (int j = 0; j < 8; j++) {
+                T a = 0;
+#pragma unroll
+                for (int m = 0; m < 6; m++) a += f[m] * lap_w<T>(i * 8 + j, m);
+                const idx_t k = find_col(rowptr, colidx, ev[i], ev[j]);
+                if (k < 0)
+                    atomicAdd(missing, 1);
+                else
+                    atomicAdd(&values[k], a);
+            }
+        }
+    }
+}
+
 template <typename T>
 static int crs_sym_spmv_tpl(ptrdiff_t n, const idx_t *rowptr, const idx_t *colidx, const void *diag,
                             const void *offdiag, double scale, const void *x, void *y, cudaStream_t s) {
@@ -245,5 +274,33 @@ extern "C" int sfem_gb300_hex8_laplacian_crs_sym(ptrdiff_t nelements, idx_t **el
     cudaFreeAsync(missing, s);
     if (check_launch("sfem_gb300_hex8_laplacian_crs_sym")) return SFEM_GB300_FAILURE;
     if (h_missing) return set_error("sfem_gb300_hex8_laplacian_crs_sym: %d element couplings missing from the graph", h_missing);
+    return SFEM_GB300_SUCCESS;
+}
+
+extern "C" int sfem_gb300_hex8_laplacian_crs(ptrdiff_t nelements, idx_t **elements, ptrdiff_t fff_stride,
+                                             const float *fff, const int32_t *rowptr, const int32_t *colidx,
+                                             int real_type, void *values, void *stream) {
+    if (nelements <= 0) return SFEM_GB300_SUCCESS;
+    if (real_type != SFEM_GB300_FLOAT32 && real_type != SFEM_GB300_FLOAT64 && real_type != SFEM_GB300_REAL_DEFAULT)
+        return set_error("sfem_gb300_hex8_laplacian_crs: unsupported real type %d", real_type);
+    const cudaStream_t s = stream_of(stream);
+    int *missing = nullptr;
+    if (cudaMallocAsync((void **)&missing, sizeof(int), s) != cudaSuccess)
+        return set_error("sfem_gb300_hex8_laplacian_crs: allocation failed");
+    cudaMemsetAsync(missing, 0, sizeof(int), s);
+    const int g = grid_for(nelements, 128, kNumSMs * 16);
+    if (real_type == SFEM_GB300_FLOAT32)
+        hex8_laplacian_crs_kernel<float><<<g, 128, 0, s>>>(nelements, elements, fff_stride, fff, rowptr, colidx,
+                                                           (float *)values, missing);
+    else
+        hex8_laplacian_crs_kernel<double><<<g, 128, 0, s>>>(nelements, elements, fff_stride, fff, rowptr, colidx,
+                                                            (double *)values, missing);
+    const int lerr = check_launch("sfem_gb300_hex8_laplacian_crs");
+    int h_missing = 0;
+    cudaMemcpyAsync(&h_missing, missing, sizeof(int), cudaMemcpyDeviceToHost, s);
+    cudaStreamSynchronize(s);
+    cudaFreeAsync(missing, s);
+    if (lerr) return SFEM_GB300_FAILURE;
+    if (h_missing) return set_error("sfem_gb300_hex8_laplacian_crs: %d element couplings missing from the graph", h_missing);
     return SFEM_GB300_SUCCESS;
 }

@@ -274,6 +274,21 @@ def upper_crs_graph(elements: np.ndarray, n_nodes: int):
     return rowptr, c.astype(np.int32)
 
 
+def full_crs_graph(elements: np.ndarray, n_nodes: int):
+    """Node-to-node CRS graph with both triangles and the diagonal (sorted columns): the
+    pattern of the full CRS and BSR assembly (the reference's node-to-node graph)."""
+    nv, E = elements.shape
+    el = elements.astype(np.int64)
+    r = np.repeat(el, nv, axis=0).reshape(-1)
+    c = np.tile(el, (nv, 1)).reshape(-1)
+    key = np.unique(r * n_nodes + c)
+    r, c = key // n_nodes, key % n_nodes
+    rowptr = np.zeros(n_nodes + 1, dtype=np.int64)
+    np.add.at(rowptr, r + 1, 1)
+    rowptr = np.cumsum(rowptr).astype(np.int32)
+    return rowptr, c.astype(np.int32)
+
+
 def _coarse_axis(n: int) -> np.ndarray:
     """Finer-grid indices kept on a 2x coarser axis of n elements: the even ones,
     plus the last index when n is odd (the last coarse element then spans one

@@ -99,3 +99,108 @@ def test_bsr_sym_spmv(cuda, bs, sym):
                                                    None), "bsr")
     torch.cuda.synchronize()
     assert np.abs(y.cpu().numpy() - ref).max() <= 1e-12 * np.abs(ref).max()
+
+
+def _csr_matvec(rowptr, colidx, vals, x, bs=1):
+    n = rowptr.size - 1
+    y = np.zeros(n * bs)
+    blocks = vals.reshape(-1, bs, bs)
+    for i in range(n):
+        for k in range(rowptr[i], rowptr[i + 1]):
+            y[i * bs:(i + 1) * bs] += blocks[k] @ x[colidx[k] * bs:(colidx[k] + 1) * bs]
+    return y
+
+
+def test_reference_named_laplacian_assembly(cuda):
+    """cu_laplacian_crs (full graph) and cu_laplacian_crs_sym under the reference's names:
+    the assembled matrices reproduce the matrix-free oracle apply; other element types
+    are refused with a message."""
+    import torch
+
+    from sfem_gb300.mesh import full_crs_graph
+
+    m = SSMesh(5, 4, 3, 1, perturb=0.2, seed=4)
+    el = m.hex8_elements()
+    n = m.n_nodes(1)
+    fff = O.fff_fill(el, m.points)
+    sp = SSMeshDevice(m, 1, device=cuda)
+    fff_d = _t(fff.T, cuda)
+    E = m.n_elements
+    lib = capi.load()
+    x = np.random.default_rng(1).standard_normal(n)
+    y_mf = O.hex8_laplacian_apply(el, fff, x)
+    rowptr, colidx = full_crs_graph(el, n)
+    rp, ci = _t(rowptr, cuda), _t(colidx, cuda)
+    vals = torch.zeros(colidx.size, dtype=torch.float64, device=cuda)
+    capi.check(lib.cu_laplacian_crs(capi.HEX8, capi.i64(E), sp.elements_ptrs.ptr, capi.i64(E), capi.vp(fff_d),
+                                    capi.vp(rp), capi.vp(ci), capi.FLOAT64, capi.vp(vals), None), "cu_laplacian_crs")
+    y = _csr_matvec(rowptr, colidx, vals.cpu().numpy(), x)
+    assert np.abs(y - y_mf).max() <= 1e-12 * np.abs(y_mf).max()
+    urp, uci = upper_crs_graph(el, n)
+    urp_d, uci_d = _t(urp, cuda), _t(uci, cuda)
+    diag = torch.zeros(n, dtype=torch.float64, device=cuda)
+    off = torch.zeros(uci.size, dtype=torch.float64, device=cuda)
+    capi.check(lib.cu_laplacian_crs_sym(capi.HEX8, capi.i64(E), sp.elements_ptrs.ptr, capi.i64(E), capi.vp(fff_d),
+                                        capi.vp(urp_d), capi.vp(uci_d), capi.FLOAT64, capi.vp(diag), capi.vp(off),
+                                        None), "cu_laplacian_crs_sym")
+    y2 = O.crs_sym_spmv(urp, uci, diag.cpu().numpy(), off.cpu().numpy(), x)
+    assert np.abs(y2 - y_mf).max() <= 1e-12 * np.abs(y_mf).max()
+    assert lib.cu_laplacian_crs(capi.SSHEX8(2), capi.i64(E), sp.elements_ptrs.ptr, capi.i64(E), capi.vp(fff_d),
+                                capi.vp(rp), capi.vp(ci), capi.FLOAT64, capi.vp(vals), None) == 1
+    assert "HEX8" in capi.last_error()
+
+
+def test_reference_named_elasticity_entry_points(cuda):
+    """cu_linear_elasticity_apply / _diag / _block_diag_sym_aos / _bsr against the oracle
+    (hex8 and sshex8 L = 2; BSR on hex8 as the reference)."""
+    import torch
+
+    from sfem_gb300.mesh import full_crs_graph
+
+    mu, lam = 1.0, 10.0
+    lib = capi.load()
+    for L in (1, 2):
+        m = SSMesh(4, 3, 2, L, box=((0, 4), (0, 1), (0, 1)), perturb=0.1, seed=L)
+        sp = SSMeshDevice(m, L, device=cuda)
+        el = m.hex8_elements() if L == 1 else m.elements(L)
+        corners = el if L == 1 else el[m.macro_corner_lidx(L)]
+        adj, det = O.adjugate_fill(corners, m.points)
+        adj_d, det_d = _t(adj.T, cuda), _t(det, cuda)
+        n = m.n_nodes(L)
+        E = m.n_elements
+        et = capi.HEX8 if L == 1 else capi.SSHEX8(L)
+        Lo = 0 if L == 1 else L
+        u = np.random.default_rng(2).standard_normal(3 * n)
+        ref = O.linear_elasticity_apply(Lo, el, adj, det, mu, lam, u)
+        y = torch.zeros(3 * n, dtype=torch.float64, device=cuda)
+        capi.check(lib.cu_linear_elasticity_apply(et, capi.i64(E), sp.elements_ptrs.ptr, capi.i64(E), capi.vp(adj_d),
+                                                  capi.vp(det_d), D(mu), D(lam), capi.FLOAT64, capi.vp(_t(u, cuda)),
+                                                  capi.vp(y), None), "apply")
+        scale = O.linear_elasticity_row_scale(Lo, el, adj, det, mu, lam, u)
+        assert (np.abs(y.cpu().numpy() - ref) / scale).max() < 1e-13
+        d3_ref, b6_ref = O.linear_elasticity_block_diag(Lo, el, adj, det, mu, lam, n)
+        d3 = torch.zeros(3 * n, dtype=torch.float64, device=cuda)
+        b6 = torch.zeros(6 * n, dtype=torch.float64, device=cuda)
+        capi.check(lib.cu_linear_elasticity_diag(et, capi.i64(E), sp.elements_ptrs.ptr, capi.i64(E), capi.vp(adj_d),
+                                                 capi.vp(det_d), D(mu), D(lam), capi.FLOAT64, capi.vp(d3), None), "diag")
+        capi.check(lib.cu_linear_elasticity_block_diag_sym_aos(et, capi.i64(E), sp.elements_ptrs.ptr, capi.i64(E),
+                                                               capi.vp(adj_d), capi.vp(det_d), D(mu), D(lam),
+                                                               capi.FLOAT64, capi.vp(b6), None), "block diag")
+        assert np.abs(d3.cpu().numpy() - d3_ref).max() <= 1e-13 * np.abs(d3_ref).max()
+        assert np.abs(b6.cpu().numpy() - b6_ref).max() <= 1e-13 * np.abs(b6_ref).max()
+        if L == 1:
+            rowptr, colidx = full_crs_graph(el, n)
+            rp, ci = _t(rowptr, cuda), _t(colidx, cuda)
+            vals = torch.zeros(colidx.size * 9, dtype=torch.float64, device=cuda)
+            capi.check(lib.cu_linear_elasticity_bsr(et, capi.i64(E), sp.elements_ptrs.ptr, capi.i64(E),
+                                                    capi.vp(adj_d), capi.vp(det_d), D(mu), D(lam), capi.FLOAT64,
+                                                    capi.vp(rp), capi.vp(ci), capi.vp(vals), None), "bsr")
+            yb = _csr_matvec(rowptr, colidx, vals.cpu().numpy(), u, bs=3)
+            assert (np.abs(yb - ref) / scale).max() < 1e-13
+            # symmetric blocks: the (i, j) block is the transpose of (j, i)
+            V = vals.cpu().numpy().reshape(-1, 3, 3)
+            k = 5
+            row = np.searchsorted(rowptr, k, side="right") - 1
+            col = colidx[k]
+            kt = rowptr[col] + np.searchsorted(colidx[rowptr[col]:rowptr[col + 1]], row)
+            assert np.abs(V[k] - V[kt].T).max() <= 1e-15 * np.abs(V).max()
