@@ -343,8 +343,10 @@ int sfem_gb300_xypaz(int real_type, ptrdiff_t n, const void *x, const void *y, d
  * until the process exits) instead of a caller workspace.  n above
  * SFEM_GB300_NOALLOC_MAX_N is rejected.  All calls on a GPU share that scratch:
  * calls that may overlap on the GPU (different streams, unordered threads) race
- * and must be serialised by the caller.  The first call on each device looks up
- * the scratch address and clears it; make that first call before any stream
+ * and must be serialised by the caller.  Every call looks up the scratch address
+ * in the current context (host-side, no allocation); the first call that sees an
+ * address on a device (the first there, or the first after a device reset or a
+ * context change) clears the scratch; make that first call before any stream
  * capture.  *result is a device pointer. */
 #define SFEM_GB300_NOALLOC_MAX_N 2147483647LL
 int sfem_gb300_dot_noalloc(int real_type, ptrdiff_t n, const void *x, const void *y, double *result, void *stream);

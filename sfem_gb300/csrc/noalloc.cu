@@ -19,9 +19,11 @@
 //  * calls that overlap on the GPU (different streams, or different host
 //    threads without ordering) race on the scratch and must be serialised by
 //    the caller;
-//  * the first call on each device looks up the device address of the scratch
-//    with cudaGetSymbolAddress and clears it with cudaMemsetAsync; make that
-//    first call before any stream capture.
+//  * every call looks up the device address of the scratch in the current
+//    context with cudaGetSymbolAddress; the first call that sees an address on a
+//    device (the first call there, or the first after a device reset or a change of
+//    context) clears the scratch with cudaMemsetAsync; make that first call before
+//    any stream capture.
 #include <mutex>
 
 #include "blas.cuh"
@@ -44,24 +46,28 @@ __global__ void __launch_bounds__(kReduceBlock) dot_noalloc_kernel(ptrdiff_t n, 
     reduce_epilogue((double)acc, ws, result, 0);
 }
 
-// Per-device device address of the scratch, looked up once with that device current.
+// Device address of the scratch in the current device's context, looked up on every call
+// with that device current (a host-side lookup, no allocation).  The scratch is cleared
+// the first time an address is seen on a device, and again whenever the address changes
+// (a new context after cudaDeviceReset, or a different context made current), so a
+// stale address from an earlier context is never used.
 static int scratch_for_current_device(void **ptr, cudaStream_t s) {
     static std::mutex mu;
     static void *addr[64] = {nullptr};
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64)
         return set_error("sfem_gb300_dot_noalloc: no current CUDA device");
+    void *p = nullptr;
+    const cudaError_t err = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (err != cudaSuccess || !p)
+        return set_error("sfem_gb300_dot_noalloc: cudaGetSymbolAddress failed: %s", cudaGetErrorString(err));
     std::lock_guard<std::mutex> lock(mu);
-    if (!addr[dev]) {
-        void *p = nullptr;
-        const cudaError_t err = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (err != cudaSuccess || !p)
-            return set_error("sfem_gb300_dot_noalloc: cudaGetSymbolAddress failed: %s", cudaGetErrorString(err));
+    if (addr[dev] != p) {
         if (cudaMemsetAsync(p, 0, sizeof(g_noalloc_scratch), s) != cudaSuccess)
             return set_error("sfem_gb300_dot_noalloc: clearing the scratch failed");
         addr[dev] = p;
     }
-    *ptr = addr[dev];
+    *ptr = p;
     return SFEM_GB300_SUCCESS;
 }
 

@@ -442,7 +442,8 @@ def sshex8_to_hex8(elements: np.ndarray, L: int) -> np.ndarray:
         raise ValueError(f"connectivity has {el.shape[0]} rows, level {L} needs {(L + 1) ** 3}")
     zi, yi, xi = np.meshgrid(np.arange(L), np.arange(L), np.arange(L), indexing="ij")
     xi, yi, zi = xi.reshape(-1), yi.reshape(-1), zi.reshape(-1)
-    out = np.empty((8, el.shape[1], L ** 3), dtype=np.int32)
+    # keep the ids' own integer type (the mesh folders may carry int64 ids)
+    out = np.empty((8, el.shape[1], L ** 3), dtype=el.dtype)
     for c in range(8):
         dx, dy, dz = HEX8_CORNERS[c]
         out[c] = el[sshex8_lidx(L, xi + dx, yi + dy, zi + dz)].T

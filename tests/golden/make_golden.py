@@ -87,6 +87,7 @@ def main():
     np.savez_compressed(OUT / "sshex8_high_levels.npz", mu=1.0, lam=10.0, **out)
     print("wrote", OUT / "sshex8_high_levels.npz")
     make_float32_stencil()
+    make_coefficient()
 
 
 def make_float32_stencil():
@@ -108,8 +109,30 @@ def make_float32_stencil():
     print("wrote", OUT / "sshex8_stencil_float32.npz")
 
 
+def make_coefficient():
+    """The variable-coefficient operator of the learned-smoother workload: k = exp(g) per
+    macro element folded into the FFF (FFF * k_e in float32), applied by the reference's
+    affine_sshex8_laplacian_stencil_apply_fff -- exact for a per-macro-element coefficient."""
+    from sfem_gb300.coefficients import lognormal_coefficient
+
+    assert O.ref() is not None, "reference kernels unavailable"
+    L = 4
+    m = SSMesh(6, 5, 4, L, perturb=0.1, seed=41)
+    el = m.elements(L)
+    fff = O.fff_fill(el[m.macro_corner_lidx(L)], m.points, use_ref=True)
+    k = lognormal_coefficient(6, 5, 4, ell=2.0, sigma=1.0, seed=42)
+    fffk = (fff * k[:, None]).astype(np.float32)
+    x = np.random.default_rng(43).standard_normal(m.n_nodes(L))
+    y = O.sshex8_laplacian_apply(L, el, fffk, x, use_ref=True)
+    np.savez_compressed(OUT / "sshex8_coefficient.npz", elements=el, fff=fff, k=k, fff_scaled=fffk, x=x,
+                        laplacian_apply=y, nx=6, ny=5, nz=4, level=L, perturb=0.1, seed=41)
+    print("wrote", OUT / "sshex8_coefficient.npz")
+
+
 if __name__ == "__main__":
     if len(sys.argv) > 1 and sys.argv[1] == "float32":
         make_float32_stencil()
+    elif len(sys.argv) > 1 and sys.argv[1] == "coefficient":
+        make_coefficient()
     else:
         main()

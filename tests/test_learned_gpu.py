@@ -139,8 +139,7 @@ def test_fused_tensor_core_correction_matches_layer_kernels(cuda, dtype_name, va
 
 def test_learned_smoother_pipeline_small(cuda):
     """Harvest -> train (own BF16 kernels) -> FCG with the learned correction on a fresh
-    coefficient draw: the loss drops, the solve reaches 1e-10 true residual, and the
-    trained correction does not cost iterations against the same MG without it."""
+    coefficient draw: the loss drops and the solve reaches 1e-10 true residual."""
     from sfem_gb300 import learned
 
     res = learned.run_experiment(nx=8, draws=4, n_pairs=8000, epochs=8, eval_draws=1, device=str(cuda),
@@ -149,7 +148,23 @@ def test_learned_smoother_pipeline_small(cuda):
     row = res["eval"][0]
     for name in ("chebyshev3", "learned"):
         assert row[name]["rc"] == 0 and row[name]["true_rel_residual"] < 1e-10, row
-    assert row["learned"]["iterations"] <= row["chebyshev3"]["iterations"] + 1, row
+
+
+def test_learned_smoother_gains_iterations(cuda):
+    """What the trained network buys: on fresh coefficient draws of a 16^3 L=4 problem
+    with k = exp(g) (sigma 1, correlation length 4 macro elements), FCG with the learned
+    correction needs strictly fewer iterations than the same multigrid without it, both
+    in FP64 and through the FP32 precision bridge, and every arm reaches 1e-10."""
+    from sfem_gb300 import learned
+
+    res = learned.run_experiment(nx=16, draws=16, n_pairs=30000, epochs=12, eval_draws=2, device=str(cuda),
+                                 placement="before", fallback_sweeps=1)
+    assert res["loss_last"] < 0.8 * res["loss_first"]
+    for row in res["eval"]:
+        for name in ("chebyshev3", "learned", "mixed", "mixed_learned"):
+            assert row[name]["rc"] == 0 and row[name]["true_rel_residual"] < 1e-10, (name, row)
+        assert row["learned"]["iterations"] < row["chebyshev3"]["iterations"], row
+        assert row["mixed_learned"]["iterations"] < row["mixed"]["iterations"], row
 
 
 def test_fallback_switch_recaptures_graph(cuda):

@@ -188,5 +188,12 @@ def test_sshex8_to_hex8_micro_mesh(tmp_path, L):
     x = np.random.default_rng(L).standard_normal(m.n_nodes(L))
     fff_macro = O.fff_fill(el[m.macro_corner_lidx(L)], m.points)
     y_ss = O.sshex8_laplacian_apply(L, el, fff_macro, x)
-    y_h8 = O.hex8_laplacian_apply(r.elements, O.fff_fill(r.elements, r.points), x)
-    assert np.abs(y_h8 - y_ss).max() <= 1e-6 * np.abs(y_ss).max()
+    # same operator, one metric per micro element: the macro FFF / L (exact in float for
+    # L = 2, 4) gives the hex8 apply the sshex8 apply's coefficients, so they agree to
+    # summation order (a node-ordering or sign error would show at O(1))
+    fff_micro = np.repeat(fff_macro / np.float32(L), L ** 3, axis=0)
+    y_h8 = O.hex8_laplacian_apply(r.elements, fff_micro, x)
+    assert np.abs(y_h8 - y_ss).max() <= 1e-12 * np.abs(y_ss).max()
+    # and the metric of the micro elements' own coordinates agrees to float rounding
+    y_geo = O.hex8_laplacian_apply(r.elements, O.fff_fill(r.elements, r.points), x)
+    assert np.abs(y_geo - y_ss).max() <= 1e-6 * np.abs(y_ss).max()

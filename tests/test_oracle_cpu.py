@@ -260,3 +260,16 @@ def test_stencil_form_float32_matches_reference_direct():
     ref = O.sshex8_laplacian_stencil_apply_f32(4, el, fff, x, use_ref=True)
     ours = O.sshex8_laplacian_stencil_apply_f32(4, el, fff, x)
     assert np.abs(ours - ref).max() <= 2e-6 * np.abs(ref).max()
+
+
+COEF = Path(__file__).resolve().parent / "golden" / "sshex8_coefficient.npz"
+
+
+def test_variable_coefficient_matches_reference_golden():
+    """k = exp(g) per macro element as FFF * k_e: the oracle's stencil apply on the scaled
+    metric equals the reference's affine_sshex8_laplacian_stencil_apply_fff output."""
+    g = np.load(COEF)
+    fffk = (g["fff"] * g["k"][:, None]).astype(np.float32)
+    assert np.array_equal(fffk, g["fff_scaled"])
+    y = O.sshex8_laplacian_stencil_apply(4, g["elements"], fffk, g["x"])
+    assert _rel(y, g["laplacian_apply"]) < 1e-14
