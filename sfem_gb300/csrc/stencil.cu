@@ -83,13 +83,56 @@ __host__ __device__ constexpr double weight(int m, int cx, int cy, int cz, int d
 // a neighbour at offset d along an axis exists inside the macro element
 __host__ __device__ constexpr bool offset_ok(int cls, int d) { return d > 0 ? cls != HI : d < 0 ? cls != LO : true; }
 
-template <typename T>
-__device__ __forceinline__ T coefficient(const T (&g)[6], int cx, int cy, int cz, int dx, int dy, int dz) {
-    T c = T(0);
+// What one lane holds: the value of one macro element (float, double) or of two
+// (float2, the packed FP32x2 arithmetic of sm_100+), with the matching node-id type.
+template <typename V>
+struct Lanes;
+template <>
+struct Lanes<float> {
+    using S = float;
+    using I = int32_t;
+    static __device__ __forceinline__ float zero() { return 0.f; }
+    static __device__ __forceinline__ float splat(double w) { return (float)w; }
+    static __device__ __forceinline__ float fma(float a, float b, float c) { return fmaf(a, b, c); }
+    static __device__ __forceinline__ float add(float a, float b) { return a + b; }
+    static __device__ __forceinline__ float scale(float a, float h) { return a * h; }
+    static __device__ __forceinline__ void scatter(float *y, I id, float v, unsigned valid) {
+        if (valid & 1u) atomicAdd(y + id, v);
+    }
+};
+template <>
+struct Lanes<double> {
+    using S = double;
+    using I = int32_t;
+    static __device__ __forceinline__ double zero() { return 0.0; }
+    static __device__ __forceinline__ double splat(double w) { return w; }
+    static __device__ __forceinline__ double fma(double a, double b, double c) { return ::fma(a, b, c); }
+    static __device__ __forceinline__ double add(double a, double b) { return a + b; }
+    static __device__ __forceinline__ void scatter(double *y, I id, double v, unsigned valid) {
+        if (valid & 1u) atomicAdd(y + id, v);
+    }
+};
+template <>
+struct Lanes<float2> {
+    using S = float;
+    using I = int2;
+    static __device__ __forceinline__ float2 zero() { return make_float2(0.f, 0.f); }
+    static __device__ __forceinline__ float2 splat(double w) { return make_float2((float)w, (float)w); }
+    static __device__ __forceinline__ float2 fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+    static __device__ __forceinline__ float2 add(float2 a, float2 b) { return __fadd2_rn(a, b); }
+    static __device__ __forceinline__ void scatter(float *y, I id, float2 v, unsigned valid) {
+        if (valid & 1u) atomicAdd(y + id.x, v.x);
+        if (valid & 2u) atomicAdd(y + id.y, v.y);
+    }
+};
+
+template <typename V>
+__device__ __forceinline__ V coefficient(const V (&g)[6], int cx, int cy, int cz, int dx, int dy, int dz) {
+    V c = Lanes<V>::zero();
 #pragma unroll
     for (int m = 0; m < 6; m++) {
         const double w = weight(m, cx, cy, cz, dx, dy, dz);
-        if (w != 0.0) c = fma(g[m], (T)w, c);
+        if (w != 0.0) c = Lanes<V>::fma(g[m], Lanes<V>::splat(w), c);
     }
     return c;
 }
@@ -105,28 +148,31 @@ __device__ __forceinline__ void cp_async_val<double>(double *smem, const double 
     cp_async8(smem, gmem);
 }
 
-// the valid (dy, dx) neighbours of plane z of the column at `col` into w[dy+1][dx+1]
-template <typename T, int L, int TILE, int CX, int CY>
-__device__ __forceinline__ void load_plane(T (&w)[3][3], const T *__restrict__ col, int z) {
+// the valid (dy, dx) neighbours of plane z of the column at `col` into w[dy+1][dx+1];
+// consecutive nodes are NS values apart
+template <typename V, int L, int NS, int CX, int CY>
+__device__ __forceinline__ void load_plane(V (&w)[3][3], const V *__restrict__ col, int z) {
     constexpr int N1 = L + 1, NP = N1 * N1;
 #pragma unroll
     for (int j = 0; j < 3; j++)
 #pragma unroll
         for (int i = 0; i < 3; i++)
-            if (offset_ok(CY, j - 1) && offset_ok(CX, i - 1)) w[j][i] = col[(z * NP + (j - 1) * N1 + (i - 1)) * TILE];
+            if (offset_ok(CY, j - 1) && offset_ok(CX, i - 1)) w[j][i] = col[(z * NP + (j - 1) * N1 + (i - 1)) * NS];
 }
 
-// Columns [c0, c1) of class (CX, CY) for this lane's macro element.  Columns of a class
-// are numbered x fastest over the MID positions 1..L-1.
-template <typename T, int L, int TILE, int CX, int CY>
-__device__ __forceinline__ void columns(const T *__restrict__ sx, const int32_t *__restrict__ sidx,
-                                        const T (&g)[6], int c0, int c1, int lane, bool valid,
-                                        T *__restrict__ y) {
+// Columns [c0, c1) of class (CX, CY) for this lane's macro element(s).  Columns of a
+// class are numbered x fastest over the MID positions 1..L-1.  sx and sidx point at the
+// lane's values / ids of node 0; node v is v * NS further.
+template <typename V, int L, int NS, int CX, int CY>
+__device__ __forceinline__ void columns(const V *__restrict__ sx, const typename Lanes<V>::I *__restrict__ sidx,
+                                        const V (&g)[6], int c0, int c1, unsigned valid,
+                                        typename Lanes<V>::S *__restrict__ y) {
+    using Op = Lanes<V>;
     constexpr int N1 = L + 1, NP = N1 * N1;
     // coefficients of the low (dz = 0, +1) and high (dz = -1, 0) z classes; a node inside
     // in z takes dz = +1 from the low class, dz = -1 from the high class and the sum of
     // both for dz = 0 (the assembled 1D integrals add up the same way)
-    T clo[3][3][2], chi[3][3][2], cmid[3][3];
+    V clo[3][3][2], chi[3][3][2], cmid[3][3];
 #pragma unroll
     for (int j = 0; j < 3; j++)
 #pragma unroll
@@ -136,7 +182,7 @@ __device__ __forceinline__ void columns(const T *__restrict__ sx, const int32_t 
             clo[j][i][1] = coefficient(g, CX, CY, LO, i - 1, j - 1, 1);
             chi[j][i][0] = coefficient(g, CX, CY, HI, i - 1, j - 1, -1);
             chi[j][i][1] = coefficient(g, CX, CY, HI, i - 1, j - 1, 0);
-            cmid[j][i] = clo[j][i][0] + chi[j][i][1];
+            cmid[j][i] = Op::add(clo[j][i][0], chi[j][i][1]);
         }
     // kept as a loop: unrolling the columns (every shared-memory address a fixed offset)
     // raised the FP32 kernel to 80 registers and 58 us against 47 us on the 48^3 L = 4 mesh
@@ -144,25 +190,25 @@ __device__ __forceinline__ void columns(const T *__restrict__ sx, const int32_t 
     for (int c = c0; c < c1; c++) {
         const int ix = CX == LO ? 0 : CX == HI ? L : (CY == MID ? 1 + c % (L - 1) : 1 + c);
         const int iy = CY == LO ? 0 : CY == HI ? L : (CX == MID ? 1 + c / (L - 1) : 1 + c);
-        const T *col = sx + (iy * N1 + ix) * TILE + lane;
-        const int32_t *icol = sidx + (iy * N1 + ix) * TILE + lane;
-        T w[3][3][3];
-        load_plane<T, L, TILE, CX, CY>(w[1], col, 0);
-        load_plane<T, L, TILE, CX, CY>(w[2], col, 1);
+        const V *col = sx + (iy * N1 + ix) * NS;
+        const typename Op::I *icol = sidx + (iy * N1 + ix) * NS;
+        V w[3][3][3];
+        load_plane<V, L, NS, CX, CY>(w[1], col, 0);
+        load_plane<V, L, NS, CX, CY>(w[2], col, 1);
 #pragma unroll
         for (int iz = 0; iz <= L; iz++) {
-            T a0 = T(0), a1 = T(0), a2 = T(0);
+            V a0 = Op::zero(), a1 = Op::zero(), a2 = Op::zero();
 #pragma unroll
             for (int j = 0; j < 3; j++)
 #pragma unroll
                 for (int i = 0; i < 3; i++) {
                     if (!(offset_ok(CY, j - 1) && offset_ok(CX, i - 1))) continue;
-                    if (iz > 0) a0 = fma(chi[j][i][0], w[0][j][i], a0);
-                    a1 = fma(iz == 0 ? clo[j][i][0] : iz == L ? chi[j][i][1] : cmid[j][i], w[1][j][i], a1);
-                    if (iz < L) a2 = fma(clo[j][i][1], w[2][j][i], a2);
+                    if (iz > 0) a0 = Op::fma(chi[j][i][0], w[0][j][i], a0);
+                    a1 = Op::fma(iz == 0 ? clo[j][i][0] : iz == L ? chi[j][i][1] : cmid[j][i], w[1][j][i], a1);
+                    if (iz < L) a2 = Op::fma(clo[j][i][1], w[2][j][i], a2);
                 }
-            const T v = (a0 + a1) + a2;
-            if (valid) atomicAdd(y + icol[iz * NP * TILE], v);
+            const V v = Op::add(Op::add(a0, a1), a2);
+            if (valid) Op::scatter(y, icol[iz * NP * NS], v, valid);
             if (iz < L) {
 #pragma unroll
                 for (int j = 0; j < 3; j++)
@@ -171,9 +217,38 @@ __device__ __forceinline__ void columns(const T *__restrict__ sx, const int32_t 
                         w[0][j][i] = w[1][j][i];
                         w[1][j][i] = w[2][j][i];
                     }
-                if (iz + 2 <= L) load_plane<T, L, TILE, CX, CY>(w[2], col, iz + 2);
+                if (iz + 2 <= L) load_plane<V, L, NS, CX, CY>(w[2], col, iz + 2);
             }
         }
+    }
+}
+
+// The four warps' column schedule: two warps split the inside columns, two take the
+// face, edge and corner columns.
+template <typename V, int L, int NS>
+__device__ __forceinline__ void all_columns(int warp, const V *sx, const typename Lanes<V>::I *sidx, const V (&g)[6],
+                                            unsigned valid, typename Lanes<V>::S *y) {
+    constexpr int NIN = (L - 1) * (L - 1);
+    constexpr int HALF = (NIN + 1) / 2;
+    switch (warp) {
+        case 0:
+            columns<V, L, NS, MID, MID>(sx, sidx, g, 0, HALF, valid, y);
+            break;
+        case 1:
+            columns<V, L, NS, MID, MID>(sx, sidx, g, HALF, NIN, valid, y);
+            break;
+        case 2:
+            columns<V, L, NS, LO, MID>(sx, sidx, g, 0, L - 1, valid, y);
+            columns<V, L, NS, HI, MID>(sx, sidx, g, 0, L - 1, valid, y);
+            columns<V, L, NS, LO, LO>(sx, sidx, g, 0, 1, valid, y);
+            columns<V, L, NS, HI, LO>(sx, sidx, g, 0, 1, valid, y);
+            break;
+        default:
+            columns<V, L, NS, MID, LO>(sx, sidx, g, 0, L - 1, valid, y);
+            columns<V, L, NS, MID, HI>(sx, sidx, g, 0, L - 1, valid, y);
+            columns<V, L, NS, LO, HI>(sx, sidx, g, 0, 1, valid, y);
+            columns<V, L, NS, HI, HI>(sx, sidx, g, 0, 1, valid, y);
+            break;
     }
 }
 
@@ -261,29 +336,82 @@ __global__ void __launch_bounds__(kThreads) sshex8_laplacian_stencil_kernel(
     }
     cp_async_wait_all();
     __syncthreads();
-    // node columns: two warps split the inside columns, two take the face and edge columns
-    constexpr int NIN = (L - 1) * (L - 1);
-    constexpr int HALF = (NIN + 1) / 2;
-    switch (warp) {
-        case 0:
-            columns<T, L, TILE, MID, MID>(sx, sidx, g, 0, HALF, lane, valid, y);
-            break;
-        case 1:
-            columns<T, L, TILE, MID, MID>(sx, sidx, g, HALF, NIN, lane, valid, y);
-            break;
-        case 2:
-            columns<T, L, TILE, LO, MID>(sx, sidx, g, 0, L - 1, lane, valid, y);
-            columns<T, L, TILE, HI, MID>(sx, sidx, g, 0, L - 1, lane, valid, y);
-            columns<T, L, TILE, LO, LO>(sx, sidx, g, 0, 1, lane, valid, y);
-            columns<T, L, TILE, HI, LO>(sx, sidx, g, 0, 1, lane, valid, y);
-            break;
-        default:
-            columns<T, L, TILE, MID, LO>(sx, sidx, g, 0, L - 1, lane, valid, y);
-            columns<T, L, TILE, MID, HI>(sx, sidx, g, 0, L - 1, lane, valid, y);
-            columns<T, L, TILE, LO, HI>(sx, sidx, g, 0, 1, lane, valid, y);
-            columns<T, L, TILE, HI, HI>(sx, sidx, g, 0, 1, lane, valid, y);
-            break;
+    all_columns<T, L, TILE>(warp, sx + lane, sidx + lane, g, valid ? 1u : 0u, y);
+}
+
+// FP32 with two macro elements per lane: a CTA takes two consecutive packed tiles (64
+// elements, one bulk copy), lane l owns elements 2 (l mod 16) and 2 (l mod 16) + 1 of
+// tile l / 16 and computes both with packed FP32x2 arithmetic (__ffma2_rn) from 8-byte
+// shared-memory loads: half the FMA and load instructions per element of the one-element
+// form, twice the registers.  Shared memory: the two blocks, then x [tile][node][32].
+template <int L>
+__global__ void __launch_bounds__(kThreads, 3) sshex8_laplacian_stencil2_kernel(ptrdiff_t nelements,
+                                                                                const int32_t *__restrict__ packed,
+                                                                                const float *__restrict__ x,
+                                                                                float *__restrict__ y,
+                                                                                int first_polls) {
+    constexpr int N1 = L + 1;
+    constexpr int NXE = N1 * N1 * N1;
+    constexpr int WORDS = pk_words(L);
+    extern __shared__ __align__(128) unsigned char st_smem[];
+    __shared__ __align__(8) uint64_t mbar;
+    int32_t *blk = reinterpret_cast<int32_t *>(st_smem);
+    float *sx = reinterpret_cast<float *>(st_smem + (size_t)2 * WORDS * 4);
+    const int tid = threadIdx.x;
+    const ptrdiff_t ntiles = (nelements + PK_TILE - 1) / PK_TILE;
+    const ptrdiff_t t0 = 2 * (ptrdiff_t)blockIdx.x;
+    const int nblk = (t0 + 1 < ntiles) ? 2 : 1;
+    if (tid == 0) {
+        tc::mbar_init(&mbar, 1);
+        tc::mbar_arrive_expect_tx(&mbar, nblk * WORDS * 4);
+        tc::bulk_load(st_smem, packed + t0 * WORDS, nblk * WORDS * 4, &mbar);
     }
+    __syncthreads();
+    if (!__syncthreads_and(tc::mbar_wait(&mbar, 0, first_polls))) {
+        if (tid == 0) {
+            atomicExch(&g_status, 1);
+            if (!tc::mbar_wait(&mbar, 0, LAP_DRAIN_POLLS)) atomicExch(&g_status, 2);
+        }
+        return;
+    }
+    // gather x of both tiles' micro grids
+    for (int k = tid; k < nblk * NXE * PK_TILE; k += kThreads) {
+        const int b = k / (NXE * PK_TILE), r = k - b * (NXE * PK_TILE);
+        if ((t0 + b) * PK_TILE + r % PK_TILE < nelements) cp_async4(&sx[k], x + blk[b * WORDS + r]);
+    }
+    const int lane = tid & 31, warp = tid >> 5;
+    const int b = lane >> 4, q = lane & 15;
+    const ptrdiff_t e0 = (t0 + b) * PK_TILE + 2 * q;
+    const unsigned valid = (e0 < nelements ? 1u : 0u) | (e0 + 1 < nelements ? 2u : 0u);
+    float2 g[6];
+    const float h = 1.f / (float)L;
+    const float2 *met = reinterpret_cast<const float2 *>(blk + b * WORDS + PK_TILE * NXE) + q;
+#pragma unroll
+    for (int m = 0; m < 6; m++) {
+        const float2 f = valid ? met[m * (PK_TILE / 2)] : make_float2(0.f, 0.f);
+        g[m] = make_float2(f.x * h, f.y * h);
+    }
+    cp_async_wait_all();
+    __syncthreads();
+    const float2 *sx2 = reinterpret_cast<const float2 *>(sx) + (size_t)b * NXE * (PK_TILE / 2) + q;
+    const int2 *sid2 = reinterpret_cast<const int2 *>(blk + b * WORDS) + q;
+    all_columns<float2, L, PK_TILE / 2>(warp, sx2, sid2, g, valid, y);
+}
+
+static int launch_pairs(ptrdiff_t nelements, const int32_t *packed, const float *x, float *y, cudaStream_t s) {
+    constexpr int L = 4;
+    const ptrdiff_t ntiles = (nelements + PK_TILE - 1) / PK_TILE;
+    const ptrdiff_t nctas = (ntiles + 1) / 2;
+    if (nctas > 0x7fffffff) return set_error("sshex8 Laplacian stencil apply: too many tiles");
+    constexpr size_t smem = (size_t)2 * pk_words(L) * 4 + (size_t)2 * (L + 1) * (L + 1) * (L + 1) * PK_TILE * 4;
+    static std::once_flag attr;
+    std::call_once(attr, [] {
+        cudaFuncSetAttribute(sshex8_laplacian_stencil2_kernel<L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem);
+    });
+    sshex8_laplacian_stencil2_kernel<L><<<(unsigned)nctas, kThreads, smem, s>>>(nelements, packed, x, y,
+                                                                             first_wait_polls());
+    return check_launch("sshex8 Laplacian stencil apply (two elements per lane)");
 }
 
 template <typename T, int L, bool PACKED>
@@ -321,6 +449,15 @@ int sshex8_laplacian_stencil_apply(int L, ptrdiff_t nelements, const int32_t *pa
         return stencil::launch<T, 4, true>(nelements, packed, nullptr, 0, nullptr, x, y, s);
     }
     return stencil::launch<T, 4, false>(nelements, nullptr, elements, fff_stride, fff, x, y, s);
+}
+
+int sshex8_laplacian_stencil_apply_pairs(int L, ptrdiff_t nelements, const int32_t *packed, const float *x,
+                                         float *y, cudaStream_t s) {
+    if (nelements <= 0) return SFEM_GB300_SUCCESS;
+    if (L != 4) return set_error("sshex8 Laplacian stencil apply: level %d not served", L);
+    if (reinterpret_cast<uintptr_t>(packed) & 15)
+        return set_error("sshex8 Laplacian stencil apply: packed block not 16-byte aligned");
+    return stencil::launch_pairs(nelements, packed, x, y, s);
 }
 
 template int sshex8_laplacian_stencil_apply<float>(int, ptrdiff_t, const int32_t *, idx_t **, ptrdiff_t,
