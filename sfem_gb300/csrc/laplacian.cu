@@ -1050,7 +1050,6 @@ static int laplacian_variant() {
             : (e && e[0] == 'a') ? 3
             : (e && e[0] == 'p') ? 4
             : (e && e[0] == 's') ? 8
-            : (e && e[0] == '2') ? 9
                                  : 0;
         if (e && e[0]) __atomic_store_n(&g_laplacian_variant_forced, 1, __ATOMIC_RELAXED);
         __atomic_store_n(&g_laplacian_variant, v, __ATOMIC_RELAXED);
@@ -1269,8 +1268,8 @@ extern "C" int cu_laplacian_diag(int element_type, ptrdiff_t nelements, idx_t **
 }
 
 extern "C" int sfem_gb300_set_laplacian_kernel(int variant) {
-    if (variant < -1 || variant > 9 || variant == 5)
-        return set_error("sfem_gb300_set_laplacian_kernel: variant must be -1..4 or 6..9");
+    if (variant < -1 || variant > 8 || variant == 5)
+        return set_error("sfem_gb300_set_laplacian_kernel: variant must be -1..4, 6, 7 or 8");
     const int cur = laplacian_variant();
     const int prev = __atomic_load_n(&g_laplacian_variant_forced, __ATOMIC_RELAXED) ? cur : -1;
     __atomic_store_n(&g_laplacian_variant, variant < 0 ? 0 : variant, __ATOMIC_RELAXED);
@@ -1314,9 +1313,6 @@ extern "C" int sfem_gb300_sshex8_laplacian_apply_packed(int element_type, ptrdif
         return set_error("sfem_gb300_sshex8_laplacian_apply_packed: unsupported real type %d", real_type_xy);
     // the stencil kernel unless another kernel was forced (packed element-matrix kernel:
     // 50.8 us against 45.0 us on the 48^3 L = 4 mesh)
-    if (laplacian_variant() == 9)
-        return sshex8_laplacian_stencil_apply_pairs(PK_L, nelements, (const int32_t *)packed, (const float *)x,
-                                                    (float *)y, stream_of(stream));
     if (laplacian_variant() == 8 || !__atomic_load_n(&g_laplacian_variant_forced, __ATOMIC_RELAXED))
         return sshex8_laplacian_stencil_apply<float>(PK_L, nelements, (const int32_t *)packed, nullptr, 0, nullptr,
                                                      (const float *)x, (float *)y, stream_of(stream));

@@ -83,8 +83,10 @@ __host__ __device__ constexpr double weight(int m, int cx, int cy, int cz, int d
 // a neighbour at offset d along an axis exists inside the macro element
 __host__ __device__ constexpr bool offset_ok(int cls, int d) { return d > 0 ? cls != HI : d < 0 ? cls != LO : true; }
 
-// What one lane holds: the value of one macro element (float, double) or of two
-// (float2, the packed FP32x2 arithmetic of sm_100+), with the matching node-id type.
+// What one lane holds: the value of one macro element and its node-id type.  (Two
+// elements per lane with packed FP32x2 arithmetic and 8-byte shared loads was built
+// and measured slower: 63.8 against 45.6 us on the 48^3 L = 4 mesh -- more
+// instructions for the packed pairs, 148 registers, 12 warps per SM.)
 template <typename V>
 struct Lanes;
 template <>
@@ -112,20 +114,6 @@ struct Lanes<double> {
         if (valid & 1u) atomicAdd(y + id, v);
     }
 };
-template <>
-struct Lanes<float2> {
-    using S = float;
-    using I = int2;
-    static __device__ __forceinline__ float2 zero() { return make_float2(0.f, 0.f); }
-    static __device__ __forceinline__ float2 splat(double w) { return make_float2((float)w, (float)w); }
-    static __device__ __forceinline__ float2 fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
-    static __device__ __forceinline__ float2 add(float2 a, float2 b) { return __fadd2_rn(a, b); }
-    static __device__ __forceinline__ void scatter(float *y, I id, float2 v, unsigned valid) {
-        if (valid & 1u) atomicAdd(y + id.x, v.x);
-        if (valid & 2u) atomicAdd(y + id.y, v.y);
-    }
-};
-
 template <typename V>
 __device__ __forceinline__ V coefficient(const V (&g)[6], int cx, int cy, int cz, int dx, int dy, int dz) {
     V c = Lanes<V>::zero();
@@ -339,81 +327,6 @@ __global__ void __launch_bounds__(kThreads) sshex8_laplacian_stencil_kernel(
     all_columns<T, L, TILE>(warp, sx + lane, sidx + lane, g, valid ? 1u : 0u, y);
 }
 
-// FP32 with two macro elements per lane: a CTA takes two consecutive packed tiles (64
-// elements, one bulk copy), lane l owns elements 2 (l mod 16) and 2 (l mod 16) + 1 of
-// tile l / 16 and computes both with packed FP32x2 arithmetic (__ffma2_rn) from 8-byte
-// shared-memory loads: half the FMA and load instructions per element of the one-element
-// form, twice the registers.  Shared memory: the two blocks, then x [tile][node][32].
-template <int L>
-__global__ void __launch_bounds__(kThreads, 3) sshex8_laplacian_stencil2_kernel(ptrdiff_t nelements,
-                                                                                const int32_t *__restrict__ packed,
-                                                                                const float *__restrict__ x,
-                                                                                float *__restrict__ y,
-                                                                                int first_polls) {
-    constexpr int N1 = L + 1;
-    constexpr int NXE = N1 * N1 * N1;
-    constexpr int WORDS = pk_words(L);
-    extern __shared__ __align__(128) unsigned char st_smem[];
-    __shared__ __align__(8) uint64_t mbar;
-    int32_t *blk = reinterpret_cast<int32_t *>(st_smem);
-    float *sx = reinterpret_cast<float *>(st_smem + (size_t)2 * WORDS * 4);
-    const int tid = threadIdx.x;
-    const ptrdiff_t ntiles = (nelements + PK_TILE - 1) / PK_TILE;
-    const ptrdiff_t t0 = 2 * (ptrdiff_t)blockIdx.x;
-    const int nblk = (t0 + 1 < ntiles) ? 2 : 1;
-    if (tid == 0) {
-        tc::mbar_init(&mbar, 1);
-        tc::mbar_arrive_expect_tx(&mbar, nblk * WORDS * 4);
-        tc::bulk_load(st_smem, packed + t0 * WORDS, nblk * WORDS * 4, &mbar);
-    }
-    __syncthreads();
-    if (!__syncthreads_and(tc::mbar_wait(&mbar, 0, first_polls))) {
-        if (tid == 0) {
-            atomicExch(&g_status, 1);
-            if (!tc::mbar_wait(&mbar, 0, LAP_DRAIN_POLLS)) atomicExch(&g_status, 2);
-        }
-        return;
-    }
-    // gather x of both tiles' micro grids
-    for (int k = tid; k < nblk * NXE * PK_TILE; k += kThreads) {
-        const int b = k / (NXE * PK_TILE), r = k - b * (NXE * PK_TILE);
-        if ((t0 + b) * PK_TILE + r % PK_TILE < nelements) cp_async4(&sx[k], x + blk[b * WORDS + r]);
-    }
-    const int lane = tid & 31, warp = tid >> 5;
-    const int b = lane >> 4, q = lane & 15;
-    const ptrdiff_t e0 = (t0 + b) * PK_TILE + 2 * q;
-    const unsigned valid = (e0 < nelements ? 1u : 0u) | (e0 + 1 < nelements ? 2u : 0u);
-    float2 g[6];
-    const float h = 1.f / (float)L;
-    const float2 *met = reinterpret_cast<const float2 *>(blk + b * WORDS + PK_TILE * NXE) + q;
-#pragma unroll
-    for (int m = 0; m < 6; m++) {
-        const float2 f = valid ? met[m * (PK_TILE / 2)] : make_float2(0.f, 0.f);
-        g[m] = make_float2(f.x * h, f.y * h);
-    }
-    cp_async_wait_all();
-    __syncthreads();
-    const float2 *sx2 = reinterpret_cast<const float2 *>(sx) + (size_t)b * NXE * (PK_TILE / 2) + q;
-    const int2 *sid2 = reinterpret_cast<const int2 *>(blk + b * WORDS) + q;
-    all_columns<float2, L, PK_TILE / 2>(warp, sx2, sid2, g, valid, y);
-}
-
-static int launch_pairs(ptrdiff_t nelements, const int32_t *packed, const float *x, float *y, cudaStream_t s) {
-    constexpr int L = 4;
-    const ptrdiff_t ntiles = (nelements + PK_TILE - 1) / PK_TILE;
-    const ptrdiff_t nctas = (ntiles + 1) / 2;
-    if (nctas > 0x7fffffff) return set_error("sshex8 Laplacian stencil apply: too many tiles");
-    constexpr size_t smem = (size_t)2 * pk_words(L) * 4 + (size_t)2 * (L + 1) * (L + 1) * (L + 1) * PK_TILE * 4;
-    static std::once_flag attr;
-    std::call_once(attr, [] {
-        cudaFuncSetAttribute(sshex8_laplacian_stencil2_kernel<L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)smem);
-    });
-    sshex8_laplacian_stencil2_kernel<L><<<(unsigned)nctas, kThreads, smem, s>>>(nelements, packed, x, y,
-                                                                             first_wait_polls());
-    return check_launch("sshex8 Laplacian stencil apply (two elements per lane)");
-}
-
 template <typename T, int L, bool PACKED>
 static int launch(ptrdiff_t nelements, const int32_t *packed, idx_t **elements, ptrdiff_t fff_stride, const float *fff,
                   const T *x, T *y, cudaStream_t s) {
@@ -449,15 +362,6 @@ int sshex8_laplacian_stencil_apply(int L, ptrdiff_t nelements, const int32_t *pa
         return stencil::launch<T, 4, true>(nelements, packed, nullptr, 0, nullptr, x, y, s);
     }
     return stencil::launch<T, 4, false>(nelements, nullptr, elements, fff_stride, fff, x, y, s);
-}
-
-int sshex8_laplacian_stencil_apply_pairs(int L, ptrdiff_t nelements, const int32_t *packed, const float *x,
-                                         float *y, cudaStream_t s) {
-    if (nelements <= 0) return SFEM_GB300_SUCCESS;
-    if (L != 4) return set_error("sshex8 Laplacian stencil apply: level %d not served", L);
-    if (reinterpret_cast<uintptr_t>(packed) & 15)
-        return set_error("sshex8 Laplacian stencil apply: packed block not 16-byte aligned");
-    return stencil::launch_pairs(nelements, packed, x, y, s);
 }
 
 template int sshex8_laplacian_stencil_apply<float>(int, ptrdiff_t, const int32_t *, idx_t **, ptrdiff_t,

@@ -51,9 +51,6 @@ bool sshex8_laplacian_stencil_supported(int L);
 template <typename T>
 int sshex8_laplacian_stencil_apply(int L, ptrdiff_t nelements, const int32_t *packed, idx_t **elements,
                                    ptrdiff_t fff_stride, const float *fff, const T *x, T *y, cudaStream_t s);
-// FP32 from packed tiles with two macro elements per lane (packed FP32x2 arithmetic)
-int sshex8_laplacian_stencil_apply_pairs(int L, ptrdiff_t nelements, const int32_t *packed, const float *x,
-                                         float *y, cudaStream_t s);
 // status of the stencil kernels' bulk-copy waits since the last call (read and cleared)
 int sshex8_laplacian_stencil_status();
 }  // namespace sfem_gb300

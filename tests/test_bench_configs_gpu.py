@@ -73,7 +73,7 @@ def test_cube48_fp64_apply(cuda, cube48, form):
     assert err.max() < RTOL64, (form, err.max())
 
 
-@pytest.mark.parametrize("form", ["packed_element_matrix", "packed_stencil", "packed_stencil_pairs", "soa_default"])
+@pytest.mark.parametrize("form", ["packed_element_matrix", "packed_stencil", "soa_default"])
 def test_cube48_fp32_apply(cuda, cube48, form):
     """FP32 on the 48^3 L = 4 mesh: the benchmark's step (packed tiles, stencil kernel),
     the packed element-matrix kernel and cu_laplacian_apply's float default (stencil
@@ -86,7 +86,7 @@ def test_cube48_fp32_apply(cuda, cube48, form):
     y = torch.zeros_like(x)
     sp = c["sp"]
     E = sp.n_elements
-    prev = lib.sfem_gb300_set_laplacian_kernel({"packed_element_matrix": 3, "packed_stencil_pairs": 9}.get(form, -1))
+    prev = lib.sfem_gb300_set_laplacian_kernel(3 if form == "packed_element_matrix" else -1)
     try:
         if form.startswith("packed"):
             c["op"].apply(x, y)

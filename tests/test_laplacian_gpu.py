@@ -145,16 +145,14 @@ def test_sshex8_laplacian_fp64_kernels(cuda, variant, n, aligned):
     assert err.max() < RTOL64, (variant, n, aligned, err.max())
 
 
-@pytest.mark.parametrize("form", ["fp32_em", "fp32_stencil", "fp32_stencil_pairs", "fp64_stencil"])
+@pytest.mark.parametrize("form", ["fp32_em", "fp32_stencil", "fp64_stencil"])
 @pytest.mark.parametrize("n", [(5, 4, 3), (9, 8, 7), (1, 1, 1), (36, 36, 36), (2, 16, 1), (3, 11, 1)])
 @pytest.mark.parametrize("aligned", [True, False])
 def test_sshex8_laplacian_packed(cuda, form, n, aligned):
     """Packed tiles (L = 4): pack from SoA rows (row stride E or E + 1) and apply with the
-    FP32 stencil kernel (default), the FP32 stencil kernel with two elements per lane
-    (variant 9, CTAs of two tiles), the FP32 element-matrix kernel (any other forced
+    FP32 stencil kernel (default), the FP32 element-matrix kernel (any other forced
     variant) or FP64 (stencil kernel); element counts 60 (32 + 28: a ragged last tile),
-    504, 1, 46,656, 32 (one tile: the pair CTA's second tile absent) and 33 (a pair CTA
-    whose second tile holds one element)."""
+    504, 1, 46,656, 32 (one full tile) and 33 (a last tile of one element)."""
     import torch
 
     L = 4
@@ -187,7 +185,7 @@ def test_sshex8_laplacian_packed(cuda, form, n, aligned):
     dt, rt, tol = (torch.float64, capi.FLOAT64, RTOL64) if form == "fp64_stencil" else (torch.float32, capi.FLOAT32, RTOL32)
     xd = torch.from_numpy(x).to(dt).to(cuda)
     yd = torch.from_numpy(y0).to(dt).to(cuda)
-    variant = {"fp32_em": 3, "fp32_stencil_pairs": 9}.get(form, -1)
+    variant = 3 if form == "fp32_em" else -1
     prev = lib.sfem_gb300_set_laplacian_kernel(variant)
     try:
         capi.check(lib.sfem_gb300_sshex8_laplacian_apply_packed(capi.SSHEX8(L), capi.i64(E), capi.vp(packed),
@@ -202,7 +200,7 @@ def test_sshex8_laplacian_packed(cuda, form, n, aligned):
     assert err.max() < tol, (form, n, aligned, err.max())
 
 
-@pytest.mark.parametrize("form", ["fp32_stencil", "fp32_stencil_pairs", "fp32_em", "fp64_stencil"])
+@pytest.mark.parametrize("form", ["fp32_stencil", "fp32_em", "fp64_stencil"])
 def test_tile_wait_gives_up_and_reports(cuda, form):
     """Failure detection without a fault: the first wait on each tile's bulk copy is
     given no polls, so every tile gives up.  Each CTA records the status and drains
@@ -221,7 +219,7 @@ def test_tile_wait_gives_up_and_reports(cuda, form):
     y = torch.zeros_like(x)
     lib = capi.load()
     assert lib.sfem_gb300_laplacian_status() == 0
-    kprev = lib.sfem_gb300_set_laplacian_kernel({"fp32_em": 3, "fp32_stencil_pairs": 9}.get(form, -1))
+    kprev = lib.sfem_gb300_set_laplacian_kernel(3 if form == "fp32_em" else -1)
     try:
         prev = lib.sfem_gb300_set_tile_wait_polls(0)
         try:
