@@ -114,15 +114,91 @@ struct Lanes<double> {
         if (valid & 1u) atomicAdd(y + id, v);
     }
 };
-template <typename V>
-__device__ __forceinline__ V coefficient(const V (&g)[6], int cx, int cy, int cz, int dx, int dy, int dz) {
+// The affine micro element matrix A (hex8 corner order) is symmetric and invariant
+// under the point reflection xi -> 1 - xi (corner c -> pi(c) = (0 6)(1 7)(2 4)(3 5):
+// A[pi k][pi j] = A[k][j]), so its 64 entries take 20 distinct values.  Each warp builds
+// five of them per element from the sub-metric (compile-time Q1 weights), the CTA shares
+// them in shared memory, and a stencil coefficient is the sum of the entries A[k][k+d]
+// over the micro elements of this macro element containing both nodes: 530 operations
+// per tile and lane for all node classes instead of 1,042 with every coefficient
+// expanded in the six metric entries.
+__host__ __device__ constexpr int reflect8(int c) {
+    return c == 0 ? 6 : c == 1 ? 7 : c == 2 ? 4 : c == 3 ? 5 : c == 4 ? 2 : c == 5 ? 3 : c == 6 ? 0 : 1;
+}
+__host__ __device__ constexpr int min2(int a, int b) { return a < b ? a : b; }
+__host__ __device__ constexpr int canon_key(int k, int j) {
+    return min2(min2(k * 8 + j, j * 8 + k), min2(reflect8(k) * 8 + reflect8(j), reflect8(j) * 8 + reflect8(k)));
+}
+constexpr int kUnique = 20;
+struct UniqueEntries {
+    int of[64];   // unique index of entry (k, j)
+    int rep[kUnique];  // key k * 8 + j of a representative of each unique index
+    constexpr UniqueEntries() : of(), rep() {
+        int n = 0;
+        for (int key = 0; key < 64; key++) {
+            if (canon_key(key / 8, key % 8) != key) continue;
+            rep[n] = key;
+            for (int q = 0; q < 64; q++)
+                if (canon_key(q / 8, q % 8) == key) of[q] = n;
+            n++;
+        }
+    }
+};
+static_assert(UniqueEntries().rep[kUnique - 1] > 0, "20 distinct entries");
+static_assert(kUnique == 5 * 4, "five entries for each of the four warps");
+
+__host__ __device__ constexpr int corner_of(int x, int y, int z) { return z * 4 + (y ? (x ? 2 : 3) : (x ? 1 : 0)); }
+
+// unique index of A[k][k + d] for corner k, or -1 when that micro element of a node of
+// class (cx, cy, cz) is outside the macro element or k + d is not one of its corners
+__host__ __device__ constexpr int stencil_term(int k, int cx, int cy, int cz, int dx, int dy, int dz) {
+    const int c[3] = {c8x(k), c8y(k), c8z(k)}, cl[3] = {cx, cy, cz}, d[3] = {dx, dy, dz};
+    int jj[3] = {0, 0, 0};
+    for (int ax = 0; ax < 3; ax++) {
+        jj[ax] = c[ax] + d[ax];
+        if (jj[ax] < 0 || jj[ax] > 1) return -1;
+        if ((cl[ax] == LO && c[ax] != 0) || (cl[ax] == HI && c[ax] != 1)) return -1;
+    }
+    constexpr UniqueEntries t{};
+    return t.of[k * 8 + corner_of(jj[0], jj[1], jj[2])];
+}
+
+// the coefficient from the shared entries a[u * NS] (u = unique index)
+template <typename V, int NS>
+__device__ __forceinline__ V coefficient(const V *__restrict__ a, int cx, int cy, int cz, int dx, int dy, int dz) {
+    V c = Lanes<V>::zero();
+    bool first = true;
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        const int u = stencil_term(k, cx, cy, cz, dx, dy, dz);
+        if (u < 0) continue;
+        c = first ? a[u * NS] : Lanes<V>::add(c, a[u * NS]);
+        first = false;
+    }
+    return c;
+}
+
+// unique entry U of the micro element matrix from the sub-metric g
+template <typename V, int U>
+__device__ __forceinline__ V unique_entry(const V (&g)[6]) {
+    constexpr int key = UniqueEntries().rep[U];
     V c = Lanes<V>::zero();
 #pragma unroll
     for (int m = 0; m < 6; m++) {
-        const double w = weight(m, cx, cy, cz, dx, dy, dz);
+        const double w = lap_weight(key / 8, key % 8, m);
         if (w != 0.0) c = Lanes<V>::fma(g[m], Lanes<V>::splat(w), c);
     }
     return c;
+}
+
+// warp W's share of the entries: U = W, W + 4, ... into a[U * NS]
+template <typename V, int NS, int W>
+__device__ __forceinline__ void store_entries(const V (&g)[6], V *a) {
+    a[W * NS] = unique_entry<V, W>(g);
+    a[(W + 4) * NS] = unique_entry<V, W + 4>(g);
+    a[(W + 8) * NS] = unique_entry<V, W + 8>(g);
+    a[(W + 12) * NS] = unique_entry<V, W + 12>(g);
+    a[(W + 16) * NS] = unique_entry<V, W + 16>(g);
 }
 
 template <typename T>
@@ -153,7 +229,7 @@ __device__ __forceinline__ void load_plane(V (&w)[3][3], const V *__restrict__ c
 // lane's values / ids of node 0; node v is v * NS further.
 template <typename V, int L, int NS, int CX, int CY>
 __device__ __forceinline__ void columns(const V *__restrict__ sx, const typename Lanes<V>::I *__restrict__ sidx,
-                                        const V (&g)[6], int c0, int c1, unsigned valid,
+                                        const V *__restrict__ sa, int c0, int c1, unsigned valid,
                                         typename Lanes<V>::S *__restrict__ y) {
     using Op = Lanes<V>;
     constexpr int N1 = L + 1, NP = N1 * N1;
@@ -166,10 +242,10 @@ __device__ __forceinline__ void columns(const V *__restrict__ sx, const typename
 #pragma unroll
         for (int i = 0; i < 3; i++) {
             if (!(offset_ok(CY, j - 1) && offset_ok(CX, i - 1))) continue;
-            clo[j][i][0] = coefficient(g, CX, CY, LO, i - 1, j - 1, 0);
-            clo[j][i][1] = coefficient(g, CX, CY, LO, i - 1, j - 1, 1);
-            chi[j][i][0] = coefficient(g, CX, CY, HI, i - 1, j - 1, -1);
-            chi[j][i][1] = coefficient(g, CX, CY, HI, i - 1, j - 1, 0);
+            clo[j][i][0] = coefficient<V, NS>(sa, CX, CY, LO, i - 1, j - 1, 0);
+            clo[j][i][1] = coefficient<V, NS>(sa, CX, CY, LO, i - 1, j - 1, 1);
+            chi[j][i][0] = coefficient<V, NS>(sa, CX, CY, HI, i - 1, j - 1, -1);
+            chi[j][i][1] = coefficient<V, NS>(sa, CX, CY, HI, i - 1, j - 1, 0);
             cmid[j][i] = Op::add(clo[j][i][0], chi[j][i][1]);
         }
     // kept as a loop: unrolling the columns (every shared-memory address a fixed offset)
@@ -214,28 +290,28 @@ __device__ __forceinline__ void columns(const V *__restrict__ sx, const typename
 // The four warps' column schedule: two warps split the inside columns, two take the
 // face, edge and corner columns.
 template <typename V, int L, int NS>
-__device__ __forceinline__ void all_columns(int warp, const V *sx, const typename Lanes<V>::I *sidx, const V (&g)[6],
+__device__ __forceinline__ void all_columns(int warp, const V *sx, const typename Lanes<V>::I *sidx, const V *sa,
                                             unsigned valid, typename Lanes<V>::S *y) {
     constexpr int NIN = (L - 1) * (L - 1);
     constexpr int HALF = (NIN + 1) / 2;
     switch (warp) {
         case 0:
-            columns<V, L, NS, MID, MID>(sx, sidx, g, 0, HALF, valid, y);
+            columns<V, L, NS, MID, MID>(sx, sidx, sa, 0, HALF, valid, y);
             break;
         case 1:
-            columns<V, L, NS, MID, MID>(sx, sidx, g, HALF, NIN, valid, y);
+            columns<V, L, NS, MID, MID>(sx, sidx, sa, HALF, NIN, valid, y);
             break;
         case 2:
-            columns<V, L, NS, LO, MID>(sx, sidx, g, 0, L - 1, valid, y);
-            columns<V, L, NS, HI, MID>(sx, sidx, g, 0, L - 1, valid, y);
-            columns<V, L, NS, LO, LO>(sx, sidx, g, 0, 1, valid, y);
-            columns<V, L, NS, HI, LO>(sx, sidx, g, 0, 1, valid, y);
+            columns<V, L, NS, LO, MID>(sx, sidx, sa, 0, L - 1, valid, y);
+            columns<V, L, NS, HI, MID>(sx, sidx, sa, 0, L - 1, valid, y);
+            columns<V, L, NS, LO, LO>(sx, sidx, sa, 0, 1, valid, y);
+            columns<V, L, NS, HI, LO>(sx, sidx, sa, 0, 1, valid, y);
             break;
         default:
-            columns<V, L, NS, MID, LO>(sx, sidx, g, 0, L - 1, valid, y);
-            columns<V, L, NS, MID, HI>(sx, sidx, g, 0, L - 1, valid, y);
-            columns<V, L, NS, LO, HI>(sx, sidx, g, 0, 1, valid, y);
-            columns<V, L, NS, HI, HI>(sx, sidx, g, 0, 1, valid, y);
+            columns<V, L, NS, MID, LO>(sx, sidx, sa, 0, L - 1, valid, y);
+            columns<V, L, NS, MID, HI>(sx, sidx, sa, 0, L - 1, valid, y);
+            columns<V, L, NS, LO, HI>(sx, sidx, sa, 0, 1, valid, y);
+            columns<V, L, NS, HI, HI>(sx, sidx, sa, 0, 1, valid, y);
             break;
     }
 }
@@ -244,10 +320,10 @@ constexpr int kWarps = 4;
 constexpr int kThreads = 32 * kWarps;
 
 // Shared memory of a tile: the ids [node][el] and metric [6][el] (the packed block
-// layout), then x [node][el].
+// layout), then x [node][el], then the 20 distinct element-matrix entries [u][el].
 template <typename T, int L>
 __host__ __device__ constexpr size_t smem_bytes() {
-    return (size_t)pk_words(L) * 4 + (size_t)(L + 1) * (L + 1) * (L + 1) * PK_TILE * sizeof(T);
+    return (size_t)pk_words(L) * 4 + ((size_t)(L + 1) * (L + 1) * (L + 1) + kUnique) * PK_TILE * sizeof(T);
 }
 
 __device__ int g_status;  // nonzero: a bulk-copy wait gave up (2: its drain gave up too)
@@ -322,9 +398,17 @@ __global__ void __launch_bounds__(kThreads) sshex8_laplacian_stencil_kernel(
         for (int k = tid; k < NXE * TILE; k += kThreads)
             if (k % TILE < nvalid) cp_async_val<T>(&sx[k], x + sidx[k]);
     }
+    // the distinct element-matrix entries, five per warp, while the gathers are in flight
+    T *sa = sx + NXE * TILE;
+    switch (warp) {
+        case 0: store_entries<T, TILE, 0>(g, sa + lane); break;
+        case 1: store_entries<T, TILE, 1>(g, sa + lane); break;
+        case 2: store_entries<T, TILE, 2>(g, sa + lane); break;
+        default: store_entries<T, TILE, 3>(g, sa + lane); break;
+    }
     cp_async_wait_all();
     __syncthreads();
-    all_columns<T, L, TILE>(warp, sx + lane, sidx + lane, g, valid ? 1u : 0u, y);
+    all_columns<T, L, TILE>(warp, sx + lane, sidx + lane, sa + lane, valid ? 1u : 0u, y);
 }
 
 template <typename T, int L, bool PACKED>
