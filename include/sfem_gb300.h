@@ -96,9 +96,9 @@ int sfem_gb300_set_laplacian_kernel(int variant);
  * apply fetches a tile's ids and metric with one bulk copy.
  * sfem_gb300_sshex8_packed_bytes gives the block array's size (-1: unsupported
  * type), sfem_gb300_sshex8_pack fills it (16-byte aligned),
- * sfem_gb300_sshex8_laplacian_apply_packed computes y += A x from it (FP32 x / y:
- * element-matrix kernel, or the node-centric stencil kernel with variant 8; FP64
- * x / y: stencil kernel); the result equals cu_laplacian_apply's on the same
+ * sfem_gb300_sshex8_laplacian_apply_packed computes y += A x from it (FP32 and
+ * FP64 x / y: the node-centric stencil kernel; FP32 with kernel variant 3 forced:
+ * the element-matrix kernel); the result equals cu_laplacian_apply's on the same
  * connectivity and FFF up to rounding order.  sfem_gb300_laplacian_status returns
  * (and clears) 1 if a packed apply gave up waiting for its bulk copy (2 if the
  * drain after that gave up too), else 0.
