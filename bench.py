@@ -704,7 +704,7 @@ def measure_batch(dev, count=256, seed=0):
     rc, lat, its, sec = bs.solve(b, x)
     tr = bs.true_residuals(b, x)
     kinds = [p.kind for p in bs.problems]
-    return {
+    out = {
         "problems": count, "dofs": int(bs.n), "groups": len(bs.groups), "rc": int(rc), "seconds": sec,
         "solves_per_s": count / sec,
         "latency_p50_s": float(np.percentile(lat, 50)), "latency_p99_s": float(np.percentile(lat, 99)),
@@ -714,6 +714,57 @@ def measure_batch(dev, count=256, seed=0):
         "setup_seconds": setup, "autotune_seconds": tune,
         "autotune": [{"chunk": c[0], "threads": c[1], "ctas_per_sm": c[2], "ms_per_chunk": t} for c, t in table],
         "tuned": list(bs.tuned),
+    }
+    # staggered arrivals: Poisson process over the first half of the simultaneous solve's
+    # time, in a seeded random order; latency from each problem's own release
+    rng = np.random.default_rng(seed + 1)
+    gaps = rng.exponential(1.0, count)
+    release = np.cumsum(gaps) / gaps.sum() * 0.5 * sec
+    release = release[rng.permutation(count)] - release.min()
+    x = torch.zeros_like(b)
+    rc2, lat2, its2, sec2 = bs.solve(b, x, release=release)
+    tr2 = bs.true_residuals(b, x)
+    out["staggered"] = {
+        "arrivals": "Poisson process over [0, 0.5 x the simultaneous solve time], seeded, random order",
+        "last_release_s": float(release.max()), "rc": int(rc2), "seconds": sec2, "solves_per_s": count / sec2,
+        "latency_from_release_p50_s": float(np.percentile(lat2, 50)),
+        "latency_from_release_p99_s": float(np.percentile(lat2, 99)),
+        "max_true_rel_residual": float(tr2.max()), "all_converged": bool(rc2 == 0 and (tr2 <= 1.5e-10).all()),
+    }
+    del bs, b, x
+    torch.cuda.empty_cache()
+    out["sequential_gpu"] = measure_batch_sequential(dev, probs, stride=8)
+    return out
+
+
+def measure_batch_sequential(dev, probs, stride=8):
+    """The same mixed solver run one problem at a time (a batch of one: FP64 flexible CG,
+    FP32 multigrid, graph-replayed chunks) on every ``stride``-th problem of the batched
+    draw; solve time only (setup excluded, as for the batch)."""
+    import torch
+
+    from sfem_gb300.batch import BatchSolver
+
+    sample = probs[::stride]
+    times, ok = [], True
+    for p in sample:
+        bs = BatchSolver([p], device=dev)
+        b = bs.rhs()
+        x = torch.zeros_like(b)
+        torch.cuda.synchronize()
+        rc, _, _, sec = bs.solve(b, x)
+        ok = ok and rc == 0 and bool((bs.true_residuals(b, x) <= 1.5e-10).all())
+        times.append(sec)
+        del bs, b, x
+    t = np.asarray(times)
+    # served back to back in draw order, every problem submitted at t = 0
+    done = np.cumsum(t)
+    return {
+        "sample": f"every {stride}th of the {len(probs)} problems ({len(sample)} solves), same problems and rhs",
+        "all_converged": bool(ok), "seconds_sum": float(t.sum()), "solves_per_s": len(t) / float(t.sum()),
+        "solve_s_p50": float(np.percentile(t, 50)), "solve_s_p99": float(np.percentile(t, 99)),
+        "queue_latency_p50_s_scaled_to_all": float(np.percentile(done, 50)) * stride,
+        "queue_latency_p99_s_scaled_to_all": float(np.percentile(done, 99)) * stride,
     }
 
 

@@ -600,6 +600,12 @@ int sfem_gb300_batch_solve_set_launch(void *solver, int check_every);
  * converged, the iteration count at that check, total seconds. */
 int sfem_gb300_batch_solve_run(void *solver, const double *b, double *x, double *latency_s,
                                int *iterations_per_problem, double *seconds);
+/* The same with staggered arrivals: release_s[p] (host) is problem p's release time in
+ * seconds from the start of the call.  A problem keeps its start state until the first
+ * chunk boundary after its release, then iterates; latency_s and the iteration counts
+ * are counted from its release. */
+int sfem_gb300_batch_solve_run_released(void *solver, const double *b, double *x, const double *release_s,
+                                        double *latency_s, int *iterations_per_problem, double *seconds);
 /* Mean milliseconds of `reps` replays of the captured chunk starting from x (x is
  * modified): the autotuner's measurement. */
 int sfem_gb300_batch_solve_time_chunk(void *solver, const double *b, double *x, int reps, double *ms);

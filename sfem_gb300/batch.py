@@ -378,16 +378,27 @@ class BatchSolver:
         self.tuned = best
         return table
 
-    def solve(self, b, x):
+    def solve(self, b, x, release=None):
         """Solve every problem to ||b_p - A_p x_p|| <= rtol ||b_p|| (FP64, zero start).
-        Returns (rc, per-problem latency s, per-problem iterations, seconds)."""
+        ``release`` (seconds from the start of the call, one per problem in batch order)
+        staggers the arrivals: a problem iterates from the first chunk boundary after its
+        release.  Returns (rc, per-problem latency s from release, per-problem
+        iterations, seconds)."""
         P = self.n_problems
         lat = np.zeros(P)
         its = np.zeros(P, dtype=np.int32)
         sec = c_double(0)
-        rc = capi.load().sfem_gb300_batch_solve_run(self.solver.ptr, capi.vp(b), capi.vp(x),
-                                                    lat.ctypes.data_as(C.c_void_p), its.ctypes.data_as(C.c_void_p),
-                                                    C.byref(sec))
+        lib = capi.load()
+        if release is None:
+            rc = lib.sfem_gb300_batch_solve_run(self.solver.ptr, capi.vp(b), capi.vp(x), lat.ctypes.data_as(C.c_void_p),
+                                                its.ctypes.data_as(C.c_void_p), C.byref(sec))
+        else:
+            rel = np.ascontiguousarray(release, dtype=np.float64)
+            if rel.shape != (P,):
+                raise ValueError(f"release: {P} times expected, got shape {rel.shape}")
+            rc = lib.sfem_gb300_batch_solve_run_released(self.solver.ptr, capi.vp(b), capi.vp(x),
+                                                         rel.ctypes.data_as(C.c_void_p), lat.ctypes.data_as(C.c_void_p),
+                                                         its.ctypes.data_as(C.c_void_p), C.byref(sec))
         return rc, lat, its, sec.value
 
     def true_residuals(self, b, x):

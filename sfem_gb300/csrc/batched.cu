@@ -421,6 +421,13 @@ public:
                                                                          flex ? scal(4) : nullptr, active.ptr, zz,
                                                                          p.ptr);
         }
+        if (pre && flex && (k & 1)) {
+            // An odd number of buffer swaps: move the latest z back into the buffer the
+            // chunk started with, so every chunk starts from the same (zz, zp) pair -- a
+            // captured chunk replays with the pointers it was captured with.
+            SFEM_GB300_CUDA(cudaMemcpyAsync(zp, zz, n * sizeof(T), cudaMemcpyDeviceToDevice, s));
+            std::swap(zz, zp);
+        }
         return check_launch("BatchCG iterate");
     }
     int apply(const T *b, T *x) override {
@@ -536,7 +543,11 @@ public:
         }
         return on_stream([&] { return cg->iterate(check_every, x); });
     }
-    int solve(const double *b, double *x) {
+    // release_s (host, optional): release time of every problem in seconds from the start
+    // of the solve.  A problem joins the iteration at the first chunk boundary after its
+    // release (until then it keeps its start state: the CG update kernels skip inactive
+    // problems); its latency is counted from its release.
+    int solve(const double *b, double *x, const double *release_s = nullptr) {
         const int P = lay->P;
         if (!stream) SFEM_GB300_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
         SFEM_GB300_CUDA(cudaStreamSynchronize(ctx->stream));  // caller's work on b, x is done
@@ -549,31 +560,78 @@ public:
             SFEM_GB300_CUDA(cudaStreamSynchronize(stream));
             SFEM_GB300_CHECK(capture(x));
         }
-        std::vector<int> h_active(P, 1), prev(P, 1);
+        std::vector<int> h_active(P, 1), prev(P, 1), started(P, 1), released(P, 1), it0(P, 0);
         h_latency.assign(P, -1.0);
         h_iters.assign(P, -1);
+        auto elapsed = [](std::chrono::steady_clock::time_point a) {
+            return std::chrono::duration<double>(std::chrono::steady_clock::now() - a).count();
+        };
         const auto t0 = std::chrono::steady_clock::now();
         SFEM_GB300_CHECK(on_stream([&] { return cg->start(b, x); }));
-        int n_active = P;
-        for (iterations = 0; iterations < max_it && n_active > 0;) {
+        int n_pending = 0;
+        if (release_s) {
+            // the start state of every problem is kept; only the released ones iterate
+            SFEM_GB300_CUDA(cudaMemcpyAsync(started.data(), cg->active.ptr, P * sizeof(int), cudaMemcpyDeviceToHost,
+                                            stream));
+            SFEM_GB300_CUDA(cudaStreamSynchronize(stream));
+            for (int q = 0; q < P; q++) {
+                released[q] = release_s[q] <= 0.0;
+                h_active[q] = started[q] && released[q];
+                n_pending += !released[q];
+            }
+            SFEM_GB300_CUDA(cudaMemcpyAsync(cg->active.ptr, h_active.data(), P * sizeof(int), cudaMemcpyHostToDevice,
+                                            stream));
+            prev = h_active;
+        }
+        int n_active = 0;
+        for (int q = 0; q < P; q++) n_active += h_active[q] != 0;
+        for (iterations = 0; iterations < max_it && (n_active > 0 || n_pending > 0);) {
+            if (n_pending > 0) {
+                // join the problems released by now; with nothing to iterate, wait for the next release
+                double now = elapsed(t0);
+                if (n_active == 0) {
+                    double next = 1e300;
+                    for (int q = 0; q < P; q++)
+                        if (!released[q]) next = std::min(next, release_s[q]);
+                    while (now < next) now = elapsed(t0);
+                }
+                bool changed = false;
+                for (int q = 0; q < P; q++) {
+                    if (released[q] || release_s[q] > now) continue;
+                    released[q] = 1;
+                    n_pending--;
+                    it0[q] = iterations;
+                    if (started[q]) {
+                        h_active[q] = 1;
+                        n_active++;
+                    }
+                    changed = true;
+                }
+                if (changed)
+                    SFEM_GB300_CUDA(cudaMemcpyAsync(cg->active.ptr, h_active.data(), P * sizeof(int),
+                                                    cudaMemcpyHostToDevice, stream));
+                prev = h_active;
+                if (n_active == 0) continue;
+            }
             SFEM_GB300_CHECK(chunk(x));
             iterations += check_every;
             SFEM_GB300_CUDA(cudaMemcpyAsync(h_active.data(), cg->active.ptr, P * sizeof(int), cudaMemcpyDeviceToHost,
                                             stream));
             SFEM_GB300_CUDA(cudaStreamSynchronize(stream));
-            const double now = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+            const double now = elapsed(t0);
             n_active = 0;
             for (int q = 0; q < P; q++) {
                 if (prev[q] && !h_active[q]) {
-                    h_latency[q] = now;
-                    h_iters[q] = iterations;
+                    h_latency[q] = now - (release_s ? std::max(release_s[q], 0.0) : 0.0);
+                    h_iters[q] = iterations - it0[q];
                 }
                 n_active += h_active[q] != 0;
             }
             prev = h_active;
         }
-        seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-        if (n_active) return set_error("BatchSolve: %d problems not converged in %d iterations", n_active, max_it);
+        seconds = elapsed(t0);
+        if (n_active || n_pending)
+            return set_error("BatchSolve: %d problems not converged in %d iterations", n_active + n_pending, max_it);
         return 0;
     }
 };
@@ -784,16 +842,22 @@ extern "C" int sfem_gb300_batch_solve_set_launch(void *solver, int check_every) 
     return SFEM_GB300_SUCCESS;
 }
 
-extern "C" int sfem_gb300_batch_solve_run(void *solver, const double *b, double *x, double *latency_s,
-                                          int *iterations_per_problem, double *seconds) {
+extern "C" int sfem_gb300_batch_solve_run_released(void *solver, const double *b, double *x,
+                                                   const double *release_s, double *latency_s,
+                                                   int *iterations_per_problem, double *seconds) {
     auto bs = std::static_pointer_cast<BatchSolve>(H(solver)->impl);
-    const int rc = bs->solve(b, x);
+    const int rc = bs->solve(b, x, release_s);
     const int P = bs->lay->P;
     if (latency_s && (int)bs->h_latency.size() == P) std::memcpy(latency_s, bs->h_latency.data(), P * sizeof(double));
     if (iterations_per_problem && (int)bs->h_iters.size() == P)
         std::memcpy(iterations_per_problem, bs->h_iters.data(), P * sizeof(int));
     if (seconds) *seconds = bs->seconds;
     return rc;
+}
+
+extern "C" int sfem_gb300_batch_solve_run(void *solver, const double *b, double *x, double *latency_s,
+                                          int *iterations_per_problem, double *seconds) {
+    return sfem_gb300_batch_solve_run_released(solver, b, x, nullptr, latency_s, iterations_per_problem, seconds);
 }
 
 extern "C" int sfem_gb300_batch_solve_time_chunk(void *solver, const double *b, double *x, int reps, double *ms) {

@@ -573,10 +573,14 @@ public:
 
 // Dense direct solve for a small coarsest level (no reference counterpart; the
 // reference runs an iterative coarse solver).  The operator's n x n matrix is
-// built by n applies to unit vectors, inverted once on the host by Cholesky,
-// and applied as x += A^-1 b with one dense matrix-vector kernel: no iteration
-// count, no host synchronisation.
+// built on the device by n applies to unit vectors (one column each, no host round
+// trip), inverted once on the device in FP64 (Gauss-Jordan, Dirichlet couplings
+// folded back, dense.cu), and applied as x += A^-1 b with one dense matrix-vector
+// kernel: no iteration count, no host synchronisation.
 int dense_symv_add(int real_type, ptrdiff_t n, const void *M, const void *b, void *x, void *stream);
+int dense_unit_vector(int real_type, ptrdiff_t n, ptrdiff_t j, void *e, void *stream);
+int dense_inverse(int real_type, ptrdiff_t n, ptrdiff_t ld, const void *cols, double *A, double *S, double *rc,
+                  int *flags, void *inv, void *stream);
 
 template <typename T>
 class DenseCoarseSolver final : public Solver<T> {
@@ -588,85 +592,18 @@ public:
     int setup() {
         const ptrdiff_t n = op->rows();
         if (n > kMaxN) return set_error("DenseCoarseSolver: %td unknowns exceed the dense limit %td", n, kMaxN);
-        DeviceBuffer<T> e(n), col(n);
-        std::vector<T> hcol(n);
-        std::vector<double> A((size_t)n * n), Linv((size_t)n * n, 0.0);
+        const ptrdiff_t ld = (n + 7) / 8 * 8;  // columns start 32-byte aligned
+        DeviceBuffer<T> e(n), cols(ld * n);
+        DeviceBuffer<double> A(n * n), S(n * n), rc(2 * n);
+        DeviceBuffer<int> flags(n + 1);
+        SFEM_GB300_CHECK(blas.zeros(ld * n, cols.ptr));
         for (ptrdiff_t j = 0; j < n; j++) {
-            blas.zeros(n, e.ptr);
-            const T one = 1;
-            SFEM_GB300_CUDA(cudaMemcpyAsync(e.ptr + j, &one, sizeof(T), cudaMemcpyHostToDevice, blas.ctx->stream));
-            blas.zeros(n, col.ptr);
-            SFEM_GB300_CHECK(op->apply(e.ptr, col.ptr));
-            SFEM_GB300_CUDA(cudaMemcpyAsync(hcol.data(), col.ptr, n * sizeof(T), cudaMemcpyDeviceToHost,
-                                            blas.ctx->stream));
-            SFEM_GB300_CUDA(cudaStreamSynchronize(blas.ctx->stream));
-            for (ptrdiff_t i = 0; i < n; i++) A[(size_t)i * n + j] = (double)hcol[i];
-        }
-        // Dirichlet dofs appear as identity rows (the operator copies constrained
-        // entries) while their columns keep the couplings: M = [[A_II, A_ID], [0, I]].
-        // Factor the SPD part (constrained columns zeroed) and fold the couplings
-        // back in afterwards: M^-1 = S^-1 (I - N), N = the zeroed couplings.
-        std::vector<ptrdiff_t> constrained;
-        std::vector<double> coupling;  // column d's couplings, per constrained dof
-        for (ptrdiff_t i = 0; i < n; i++) {
-            bool identity = A[(size_t)i * n + i] == 1.0;
-            for (ptrdiff_t j = 0; j < n && identity; j++)
-                if (j != i && A[(size_t)i * n + j] != 0.0) identity = false;
-            if (!identity) continue;
-            constrained.push_back(i);
-            for (ptrdiff_t k = 0; k < n; k++) {
-                coupling.push_back(k != i ? A[(size_t)k * n + i] : 0.0);
-                if (k != i) A[(size_t)k * n + i] = 0.0;
-            }
-        }
-        // symmetrise (the assembled operator is symmetric up to rounding), Cholesky A = L L^T
-        for (ptrdiff_t i = 0; i < n; i++)
-            for (ptrdiff_t j = 0; j < i; j++) {
-                const double v = 0.5 * (A[(size_t)i * n + j] + A[(size_t)j * n + i]);
-                A[(size_t)i * n + j] = A[(size_t)j * n + i] = v;
-            }
-        for (ptrdiff_t j = 0; j < n; j++) {
-            double d = A[(size_t)j * n + j];
-            for (ptrdiff_t k = 0; k < j; k++) d -= A[(size_t)j * n + k] * A[(size_t)j * n + k];
-            if (!(d > 0)) return set_error("DenseCoarseSolver: matrix not positive definite (pivot %td)", j);
-            d = std::sqrt(d);
-            A[(size_t)j * n + j] = d;
-            for (ptrdiff_t i = j + 1; i < n; i++) {
-                double v = A[(size_t)i * n + j];
-                for (ptrdiff_t k = 0; k < j; k++) v -= A[(size_t)i * n + k] * A[(size_t)j * n + k];
-                A[(size_t)i * n + j] = v / d;
-            }
-        }
-        // L^-1 (lower triangular), then A^-1 = L^-T L^-1
-        for (ptrdiff_t j = 0; j < n; j++) {
-            Linv[(size_t)j * n + j] = 1.0 / A[(size_t)j * n + j];
-            for (ptrdiff_t i = j + 1; i < n; i++) {
-                double v = 0;
-                for (ptrdiff_t k = j; k < i; k++) v -= A[(size_t)i * n + k] * Linv[(size_t)k * n + j];
-                Linv[(size_t)i * n + j] = v / A[(size_t)i * n + i];
-            }
-        }
-        std::vector<double> Sinv((size_t)n * n);
-        for (ptrdiff_t i = 0; i < n; i++)
-            for (ptrdiff_t j = 0; j <= i; j++) {
-                double v = 0;
-                for (ptrdiff_t k = i; k < n; k++) v += Linv[(size_t)k * n + i] * Linv[(size_t)k * n + j];
-                Sinv[(size_t)i * n + j] = Sinv[(size_t)j * n + i] = v;
-            }
-        std::vector<T> Ainv((size_t)n * n);
-        for (size_t k = 0; k < Sinv.size(); k++) Ainv[k] = (T)Sinv[k];
-        for (size_t c = 0; c < constrained.size(); c++) {
-            const ptrdiff_t d = constrained[c];
-            const double *cp = &coupling[c * (size_t)n];
-            for (ptrdiff_t r = 0; r < n; r++) {
-                double v = Sinv[(size_t)r * n + d];
-                for (ptrdiff_t k = 0; k < n; k++) v -= Sinv[(size_t)r * n + k] * cp[k];
-                Ainv[(size_t)r * n + d] = (T)v;
-            }
+            SFEM_GB300_CHECK(dense_unit_vector(real_type_v<T>, n, j, e.ptr, blas.ctx->sp()));
+            SFEM_GB300_CHECK(op->apply(e.ptr, cols.ptr + j * ld));
         }
         SFEM_GB300_CHECK(inv.resize(n * n));
-        SFEM_GB300_CUDA(cudaMemcpy(inv.ptr, Ainv.data(), (size_t)n * n * sizeof(T), cudaMemcpyHostToDevice));
-        return 0;
+        return dense_inverse(real_type_v<T>, n, ld, cols.ptr, A.ptr, S.ptr, rc.ptr, flags.ptr, inv.ptr,
+                             blas.ctx->sp());
     }
     int apply(const T *b, T *x) override {
         this->iterations_ = 1;

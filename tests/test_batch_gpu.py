@@ -96,3 +96,26 @@ def test_batch_autotune_and_dot(cuda, batch):
     ref = torch.stack([torch.dot(b[s0:s1], y[s0:s1]) for s0, s1 in
                        zip(batch.dof_offsets[:-1], batch.dof_offsets[1:])])
     torch.testing.assert_close(out, ref, rtol=1e-12, atol=1e-12)
+
+
+def test_batch_staggered_release(cuda, batch):
+    """Problems released one after another (reverse batch order over 60 ms): each joins at
+    the first chunk boundary after its release, converges to 1e-10, its latency counts from
+    its own release, and it takes the iterations it takes when all start together (to a
+    chunk: the checks fall on chunk boundaries)."""
+    import torch
+
+    b = batch.rhs()
+    x0 = torch.zeros_like(b)
+    rc, _, its_all, _ = batch.solve(b, x0)
+    assert rc == 0, capi.last_error()
+    P = batch.n_problems
+    release = np.linspace(0.06, 0.0, P)
+    x = torch.zeros_like(b)
+    rc, lat, its, sec = batch.solve(b, x, release=release)
+    assert rc == 0, capi.last_error()
+    assert (lat > 0).all() and (lat + release <= sec + 1e-9).all()
+    assert (its >= 1).all() and np.abs(its - its_all).max() <= batch.check_every, (its, its_all)
+    assert (batch.true_residuals(b, x) <= 1.5e-10).all()
+    with pytest.raises(ValueError):
+        batch.solve(b, x, release=release[:-1])

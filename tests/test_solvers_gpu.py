@@ -368,10 +368,34 @@ def test_cg_options_true_residual_and_check_every(cuda):
     assert its[0] <= its[1] < its[0] + 7
 
 
+@pytest.mark.parametrize("dtype", ["float64", "float32"])
+def test_dense_coarse_inverse_729(cuda, dtype):
+    """The device-built dense inverse on a 729-unknown hex8 Poisson level (9^3 nodes, one
+    Dirichlet face): A (A^-1 b) = b, b nonzero on the constrained dofs too."""
+    import torch
+
+    dt = getattr(torch, dtype)
+    m = SSMesh(8, 8, 8, 4, perturb=0.05, seed=3)
+    H = S.Hierarchy(m, dirichlet_faces=("x0",), device=cuda, coarsen_macro=True, min_coarse_nodes=700)
+    cs = H.spaces[-1]
+    assert cs.n_nodes == 729
+    ctx = S.context()
+    cop = S.laplacian_op(ctx, cs, cs.fff, H.dirichlet[-1], dt)
+    ds = S.dense_solver(ctx, cop)
+    bc = torch.randn(cs.n_nodes, dtype=torch.float64, device=cuda).to(dt)
+    xc = torch.zeros_like(bc)
+    S.solve(ds, bc, xc)
+    r = torch.zeros_like(bc)
+    S.apply(cop, xc, r)
+    tol = 1e-10 if dtype == "float64" else 2e-4
+    assert float(torch.linalg.vector_norm(r - bc) / torch.linalg.vector_norm(bc)) < tol
+
+
 @pytest.mark.parametrize("kind", ["poisson", "elasticity"])
 def test_dense_coarse_and_graph_vcycle(cuda, kind):
-    """Dense Cholesky coarse solve + CUDA-graph V-cycle: the coarse solve is exact, the
-    graph replay reproduces the eager V-cycle, and FCG converges to the oracle residual."""
+    """Dense coarse solve (inverse built on the device) + CUDA-graph V-cycle: the coarse
+    solve is exact, the graph replay reproduces the eager V-cycle, and FCG converges to
+    the oracle residual."""
     import torch
 
     L = 4
