@@ -83,11 +83,11 @@ def parse():
                          "FP64 stencil kernel) twice each and exit (an ncu target)")
     ap.add_argument("--batch-problems", type=int, default=256)
     ap.add_argument("--profile-zoo", action="store_true",
-                    help="launch every vector, SpMV and coarse-level kernel twice on inputs larger than L2: "
-                         "the target of the per-kernel roofline table in profiles/")
+                    help="launch every vector, SpMV and coarse-level kernel twice on inputs larger than L2 "
+                         "(a target for per-kernel ncu captures)")
     ap.add_argument("--profile-solves", action="store_true",
                     help="run one mixed + learned Poisson solve (32^3 L=4, k = exp(g)) and one mixed elasticity "
-                         "solve (64x16x16 L=4): the target of the solver launch-list captures in profiles/")
+                         "solve (64x16x16 L=4) (a target for solver launch-list captures)")
     return ap.parse_args()
 
 
@@ -880,8 +880,8 @@ def run_ours(args):
 def profile_kernels():
     """Two launches of each main kernel on the bench workloads (48^3 L=4 Laplacian FP32 /
     FP64 apply, level 2 <-> 4 transfers, the fused learned correction on the 48^3
-    patches, 64x16x16 L=4 elasticity FP32 / FP64): the target of the ncu captures
-    summarised in profiles/."""
+    patches, 64x16x16 L=4 elasticity FP32 / FP64): a target for per-kernel ncu
+    captures."""
     import ctypes
 
     import torch

@@ -61,7 +61,10 @@ def ref():
     if _ref is None:
         path = _build.REF_LIB
         if not path.exists():
-            path = _build.build_ref()
+            try:
+                path = _build.build_ref()
+            except RuntimeError:  # no reference tree on this machine
+                return None
         if path is None or not Path(path).exists():
             return None
         _ref = C.CDLL(str(path))
@@ -74,7 +77,10 @@ def ref_f32():
     if _ref_f32 is None:
         path = _build.REF_LIB_F32
         if not path.exists():
-            path = _build.build_ref_f32()
+            try:
+                path = _build.build_ref_f32()
+            except RuntimeError:  # no reference tree on this machine
+                return None
         if path is None or not Path(path).exists():
             return None
         _ref_f32 = C.CDLL(str(path))

@@ -5,8 +5,9 @@
 * ``build_ref()`` compiles the reference's own CPU operator sources, read in
   place from the reference tree (never copied), together with the small type
   shim in ``oracle/shim`` and the wrapper ``oracle/ref/ref_extras.cpp`` into
-  ``oracle/_ref/libsfem_ref.so``.  It is skipped when the reference tree is
-  absent (e.g. on a machine that only runs the tests).
+  ``oracle/_ref/libsfem_ref.so``.  The reference tree comes from the ``root``
+  argument or ``$SFEM_REFERENCE_ROOT``; without either (a machine that only runs the
+  tests) it raises with what to set.
 """
 
 from __future__ import annotations
@@ -17,7 +18,6 @@ from concurrent.futures import ThreadPoolExecutor
 from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
-REF_ROOT = Path(os.environ.get("SFEM_REFERENCE_ROOT", "/root/reference"))
 
 ORACLE_LIB = HERE / "_build" / "liboracle.so"
 REF_LIB = HERE / "_ref" / "libsfem_ref.so"
@@ -69,13 +69,19 @@ def build_oracle(force: bool = False) -> Path:
     return ORACLE_LIB
 
 
-def reference_available() -> bool:
-    return (REF_ROOT / "operators" / "sshex8" / "sshex8_laplacian.cpp").exists()
+def reference_root(root=None) -> Path:
+    """The reference tree to compile from: ``root``, else ``$SFEM_REFERENCE_ROOT``."""
+    r = root if root is not None else os.environ.get("SFEM_REFERENCE_ROOT")
+    if not r:
+        raise RuntimeError("no reference tree given: pass root=... or set SFEM_REFERENCE_ROOT to the sfem checkout")
+    path = Path(r)
+    if not (path / "operators" / "sshex8" / "sshex8_laplacian.cpp").exists():
+        raise RuntimeError(f"{path} is not an sfem tree (operators/sshex8/sshex8_laplacian.cpp missing)")
+    return path
 
 
-def build_ref(force: bool = False):
-    if not reference_available():
-        return None
+def build_ref(force: bool = False, root=None):
+    REF_ROOT = reference_root(root)
     srcs = [REF_ROOT / s for s in REF_SOURCES] + [HERE / "ref" / "ref_extras.cpp"]
     if not (force or _stale(REF_LIB, srcs)):
         return REF_LIB
@@ -96,11 +102,10 @@ def build_ref(force: bool = False):
     return REF_LIB
 
 
-def build_ref_f32(force: bool = False):
+def build_ref_f32(force: bool = False, root=None):
     """The reference's sshex8 Laplacian sources with real/scalar/accumulator = float
     (shim_f32 first on the include path) into oracle/_ref/libsfem_ref_f32.so."""
-    if not reference_available():
-        return None
+    REF_ROOT = reference_root(root)
     srcs = [REF_ROOT / s for s in REF_SOURCES_F32] + [HERE / "ref" / "ref_f32_extras.cpp"]
     if not (force or _stale(REF_LIB_F32, srcs)):
         return REF_LIB_F32
@@ -118,6 +123,9 @@ def build_ref_f32(force: bool = False):
 
 
 if __name__ == "__main__":
+    import sys
+
+    root = sys.argv[1] if len(sys.argv) > 1 else None  # else $SFEM_REFERENCE_ROOT
     print(build_oracle(force=True))
-    print(build_ref(force=True))
-    print(build_ref_f32(force=True))
+    print(build_ref(force=True, root=root))
+    print(build_ref_f32(force=True, root=root))

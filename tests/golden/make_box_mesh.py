@@ -7,16 +7,25 @@ PyYAML is not installed here, so a stand-in ``yaml`` module with a block-style
 writes for these metas) is put on the path for that run; every raw array is the
 reference script's own output.
 
-    python tests/golden/make_box_mesh.py
+    python tests/golden/make_box_mesh.py REFERENCE_ROOT   (or SFEM_REFERENCE_ROOT set)
 """
 
+import os
 import shutil
 import subprocess
 import sys
 import tempfile
 from pathlib import Path
 
-REF = Path("/root/reference/python/sfem/mesh")
+def _reference_mesh_dir() -> Path:
+    """python/sfem/mesh of the reference tree: the first argument, else $SFEM_REFERENCE_ROOT."""
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("SFEM_REFERENCE_ROOT")
+    if not root:
+        raise SystemExit("usage: make_box_mesh.py REFERENCE_ROOT (or set SFEM_REFERENCE_ROOT)")
+    return Path(root) / "python" / "sfem" / "mesh"
+
+
+REF = _reference_mesh_dir() if __name__ == "__main__" else None
 OUT = Path(__file__).resolve().parent / "box_mesh_hex8"
 
 YAML_STUB = '''
