@@ -128,6 +128,25 @@ __global__ void constraint_copy_kernel(ptrdiff_t nn, const idx_t *__restrict__ n
     }
 }
 
+// every component of the constrained nodes in one launch: dst[node*block + c] = src[...], c < block
+template <typename T>
+__global__ void constraint_copy_block_kernel(ptrdiff_t nn, const idx_t *__restrict__ nodes, int block,
+                                             const T *__restrict__ src, T *__restrict__ dst) {
+    for (ptrdiff_t i = blockIdx.x * (ptrdiff_t)blockDim.x + threadIdx.x; i < nn * block;
+         i += (ptrdiff_t)gridDim.x * blockDim.x) {
+        const ptrdiff_t k = (ptrdiff_t)nodes[i / block] * block + i % block;
+        dst[k] = src[k];
+    }
+}
+
+template <typename T>
+__global__ void constraint_value_block_kernel(ptrdiff_t nn, const idx_t *__restrict__ nodes, int block, T value,
+                                              T *__restrict__ x) {
+    for (ptrdiff_t i = blockIdx.x * (ptrdiff_t)blockDim.x + threadIdx.x; i < nn * block;
+         i += (ptrdiff_t)gridDim.x * blockDim.x)
+        x[(ptrdiff_t)nodes[i / block] * block + i % block] = value;
+}
+
 template <typename T>
 __global__ void constraint_value_kernel(ptrdiff_t nn, const idx_t *__restrict__ nodes, int block, int comp, T value,
                                         T *__restrict__ x) {
@@ -351,6 +370,30 @@ extern "C" int sfem_gb300_constraint_nodes_to_value(int real_type, ptrdiff_t n_n
                        SFEM_EW_LAUNCH(constraint_value_kernel, n, nodes, block_size, component, (T)value, (T *)x));
     return check_launch("sfem_gb300_constraint_nodes_to_value");
 }
+
+namespace sfem_gb300 {
+int constraint_copy_block(int real_type, ptrdiff_t n_nodes, const int32_t *nodes, int block_size, const void *src,
+                          void *dest, void *stream) {
+    const ptrdiff_t n = n_nodes * block_size;
+    if (n <= 0) return SFEM_GB300_SUCCESS;
+    SFEM_DISPATCH_REAL(real_type, "constraint_copy_block",
+                       SFEM_EW_LAUNCH(constraint_copy_block_kernel, n_nodes, nodes, block_size, (const T *)src,
+                                      (T *)dest),
+                       SFEM_EW_LAUNCH(constraint_copy_block_kernel, n_nodes, nodes, block_size, (const T *)src,
+                                      (T *)dest));
+    return check_launch("constraint_copy_block");
+}
+
+int constraint_value_block(int real_type, ptrdiff_t n_nodes, const int32_t *nodes, int block_size, double value,
+                           void *x, void *stream) {
+    const ptrdiff_t n = n_nodes * block_size;
+    if (n <= 0) return SFEM_GB300_SUCCESS;
+    SFEM_DISPATCH_REAL(real_type, "constraint_value_block",
+                       SFEM_EW_LAUNCH(constraint_value_block_kernel, n_nodes, nodes, block_size, (T)value, (T *)x),
+                       SFEM_EW_LAUNCH(constraint_value_block_kernel, n_nodes, nodes, block_size, (T)value, (T *)x));
+    return check_launch("constraint_value_block");
+}
+}  // namespace sfem_gb300
 
 extern "C" int sfem_gb300_convert(ptrdiff_t n, int src_type, const void *src, int dst_type, void *dst, void *stream) {
     if (n <= 0) return SFEM_GB300_SUCCESS;

@@ -90,9 +90,7 @@ public:
                                                                 adjugate, determinant, mu, lambda, contraction, x, y,
                                                                 ctx->sp()));
         }
-        for (int c = 0; c < 3; c++)
-            SFEM_GB300_CHECK(
-                    sfem_gb300_constraint_nodes_copy(real_type_v<T>, n_dirichlet, dirichlet, 3, c, x, y, ctx->sp()));
+        SFEM_GB300_CHECK(constraint_copy_block(real_type_v<T>, n_dirichlet, dirichlet, 3, x, y, ctx->sp()));
         return 0;
     }
     ptrdiff_t rows() const override { return 3 * n_nodes; }
@@ -112,9 +110,7 @@ public:
     int apply(const T *x, T *y) override {
         SFEM_GB300_CHECK(sfem_gb300_sshex8_prolongate(nelements, from_level, from_elements, to_level, to_elements, vec,
                                                       real_type_v<T>, x, y, ctx->sp()));
-        for (int c = 0; c < vec; c++)
-            SFEM_GB300_CHECK(
-                    sfem_gb300_constraint_nodes_to_value(real_type_v<T>, n_dirichlet, dirichlet, vec, c, 0.0, y, ctx->sp()));
+        SFEM_GB300_CHECK(constraint_value_block(real_type_v<T>, n_dirichlet, dirichlet, vec, 0.0, y, ctx->sp()));
         return 0;
     }
     ptrdiff_t rows() const override { return vec * n_to; }
@@ -135,9 +131,7 @@ public:
     const idx_t *dirichlet{nullptr};
     int apply(const T *x, T *y) override {
         SFEM_GB300_CHECK(sfem_gb300_crs_transfer(real_type_v<T>, nrows, vec, rowptr, colidx, weights, x, y, ctx->sp()));
-        for (int c = 0; c < vec; c++)
-            SFEM_GB300_CHECK(
-                    sfem_gb300_constraint_nodes_to_value(real_type_v<T>, n_dirichlet, dirichlet, vec, c, 0.0, y, ctx->sp()));
+        SFEM_GB300_CHECK(constraint_value_block(real_type_v<T>, n_dirichlet, dirichlet, vec, 0.0, y, ctx->sp()));
         return 0;
     }
     ptrdiff_t rows() const override { return vec * nrows; }
@@ -159,9 +153,7 @@ public:
     int apply(const T *x, T *y) override {
         SFEM_GB300_CHECK(sfem_gb300_sshex8_restrict(nelements, from_level, from_elements, count, to_level, to_elements,
                                                     vec, real_type_v<T>, x, y, ctx->sp()));
-        for (int c = 0; c < vec; c++)
-            SFEM_GB300_CHECK(
-                    sfem_gb300_constraint_nodes_to_value(real_type_v<T>, n_dirichlet, dirichlet, vec, c, 0.0, y, ctx->sp()));
+        SFEM_GB300_CHECK(constraint_value_block(real_type_v<T>, n_dirichlet, dirichlet, vec, 0.0, y, ctx->sp()));
         return 0;
     }
     ptrdiff_t rows() const override { return vec * n_to; }

@@ -45,6 +45,13 @@ constexpr int real_type_v = sizeof(T) == 8 ? SFEM_GB300_FLOAT64 : SFEM_GB300_FLO
 
 int set_error(const char *fmt, ...);
 
+// Dirichlet dofs of every block component in one launch (the per-component C entry points
+// sfem_gb300_constraint_nodes_copy / _to_value launch once per component)
+int constraint_copy_block(int real_type, ptrdiff_t n_nodes, const int32_t *nodes, int block_size, const void *src,
+                          void *dest, void *stream);
+int constraint_value_block(int real_type, ptrdiff_t n_nodes, const int32_t *nodes, int block_size, double value,
+                           void *x, void *stream);
+
 // -------------------------------------------------------------------------- buffers
 
 // Owning device buffer.
