@@ -1070,10 +1070,12 @@ static int laplacian_apply_tpl(int element_type, ptrdiff_t nelements, idx_t **el
     // default per level (measured at 7.2M nodes): L=4 async tile, L=2 thread per element, else staged tile
     int variant = laplacian_variant();
     const bool forced = __atomic_load_n(&g_laplacian_variant_forced, __ATOMIC_RELAXED) != 0;
-    if (!forced) variant = (L == 4) ? 8 : (L == 2) ? 2 : 0;
-    // node-centric stencil form (variant 8): the default where it is served.  FP64:
-    // 0.57 ms against 0.99 ms for the warp element-matrix kernel (about half the FP64
-    // operations); FP32: 49 us against 58 us for the async tile (48^3 macro, L = 4)
+    if (!forced) variant = (L == 3 || L == 4 || (L == 2 && sizeof(T) == 8)) ? 8 : (L == 2) ? 2 : 0;
+    // node-centric stencil form (variant 8): the default where it is faster (7.2M nodes,
+    // L2 flushed).  L = 4: FP64 0.53 ms against 0.99 ms for the warp element-matrix
+    // kernel (about half the FP64 operations), FP32 45 us against 58 us for the async
+    // tile.  L = 3: FP64 0.63 against 0.96 ms, FP32 51 against 80 us for the staged tile.
+    // L = 2: FP64 0.97 against 1.04 ms; FP32 keeps the thread-per-element kernel.
     if (variant == 8 && sshex8_laplacian_stencil_supported(L))
         return sshex8_laplacian_stencil_apply<T>(L, nelements, nullptr, elements, fff_stride, fff, x, y, s);
     // FP64 at L = 2, 3: few micro elements per macro element leave most lanes of the warp

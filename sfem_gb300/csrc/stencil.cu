@@ -294,6 +294,29 @@ __device__ __forceinline__ void all_columns(int warp, const V *sx, const typenam
                                             unsigned valid, typename Lanes<V>::S *y) {
     constexpr int NIN = (L - 1) * (L - 1);
     constexpr int HALF = (NIN + 1) / 2;
+    if constexpr (L == 2) {
+        // nine columns of one node class each: 2 / 2 / 2 / 3 per warp
+        switch (warp) {
+            case 0:
+                columns<V, L, NS, MID, MID>(sx, sidx, sa, 0, 1, valid, y);
+                columns<V, L, NS, LO, LO>(sx, sidx, sa, 0, 1, valid, y);
+                break;
+            case 1:
+                columns<V, L, NS, LO, MID>(sx, sidx, sa, 0, 1, valid, y);
+                columns<V, L, NS, HI, MID>(sx, sidx, sa, 0, 1, valid, y);
+                break;
+            case 2:
+                columns<V, L, NS, MID, LO>(sx, sidx, sa, 0, 1, valid, y);
+                columns<V, L, NS, MID, HI>(sx, sidx, sa, 0, 1, valid, y);
+                break;
+            default:
+                columns<V, L, NS, HI, LO>(sx, sidx, sa, 0, 1, valid, y);
+                columns<V, L, NS, LO, HI>(sx, sidx, sa, 0, 1, valid, y);
+                columns<V, L, NS, HI, HI>(sx, sidx, sa, 0, 1, valid, y);
+                break;
+        }
+        return;
+    }
     switch (warp) {
         case 0:
             columns<V, L, NS, MID, MID>(sx, sidx, sa, 0, HALF, valid, y);
@@ -432,20 +455,28 @@ static int launch(ptrdiff_t nelements, const int32_t *packed, idx_t **elements, 
 static std::atomic<int> g_first_wait_polls{LAP_WAIT_POLLS};
 int first_wait_polls() { return g_first_wait_polls.load(std::memory_order_relaxed); }
 
-// Levels served by the node-centric kernel.
-bool sshex8_laplacian_stencil_supported(int L) { return L == 4; }
+// Levels served by the node-centric kernel (packed tiles: L = 4 only).
+bool sshex8_laplacian_stencil_supported(int L) { return L >= 2 && L <= 4; }
 
 template <typename T>
 int sshex8_laplacian_stencil_apply(int L, ptrdiff_t nelements, const int32_t *packed, idx_t **elements,
                                    ptrdiff_t fff_stride, const float *fff, const T *x, T *y, cudaStream_t s) {
     if (nelements <= 0) return SFEM_GB300_SUCCESS;
-    if (L != 4) return set_error("sshex8 Laplacian stencil apply: level %d not served", L);
+    if (!sshex8_laplacian_stencil_supported(L)) return set_error("sshex8 Laplacian stencil apply: level %d not served", L);
     if (packed) {
+        if (L != PK_L) return set_error("sshex8 Laplacian stencil apply: packed tiles hold level %d, not %d", PK_L, L);
         if (reinterpret_cast<uintptr_t>(packed) & 15)
             return set_error("sshex8 Laplacian stencil apply: packed block not 16-byte aligned");
         return stencil::launch<T, 4, true>(nelements, packed, nullptr, 0, nullptr, x, y, s);
     }
-    return stencil::launch<T, 4, false>(nelements, nullptr, elements, fff_stride, fff, x, y, s);
+    switch (L) {
+        case 2:
+            return stencil::launch<T, 2, false>(nelements, nullptr, elements, fff_stride, fff, x, y, s);
+        case 3:
+            return stencil::launch<T, 3, false>(nelements, nullptr, elements, fff_stride, fff, x, y, s);
+        default:
+            return stencil::launch<T, 4, false>(nelements, nullptr, elements, fff_stride, fff, x, y, s);
+    }
 }
 
 template int sshex8_laplacian_stencil_apply<float>(int, ptrdiff_t, const int32_t *, idx_t **, ptrdiff_t,

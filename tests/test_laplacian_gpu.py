@@ -108,16 +108,16 @@ def test_sshex8_laplacian_fp32_kernels(cuda, variant, L, aligned):
     assert err.max() < RTOL32, (variant, L, aligned, err.max())
 
 
-@pytest.mark.parametrize("variant", [1, -1])
+@pytest.mark.parametrize("variant", [1, -1, 8])
+@pytest.mark.parametrize("L", [2, 3, 4])
 @pytest.mark.parametrize("n", [(5, 4, 3), (1, 1, 1), (8, 5, 3)])
 @pytest.mark.parametrize("aligned", [True, False])
-def test_sshex8_laplacian_fp64_kernels(cuda, variant, n, aligned):
-    """FP64 at L = 4: the node-centric stencil kernel (default, -1) and the warp
-    element-matrix kernel (1), on ragged tiles (60 = 32 + 28, 1, 120 = 3 x 32 + 24) with
-    connectivity rows 16-byte aligned or not; 1e-13 of the row scale."""
+def test_sshex8_laplacian_fp64_kernels(cuda, variant, L, n, aligned):
+    """FP64 at L = 2, 3, 4: the default kernel (-1), the node-centric stencil kernel (8)
+    and the warp element-matrix kernel (1), on ragged tiles (60 = 32 + 28, 1, 120 = 3 x
+    32 + 24) with connectivity rows 16-byte aligned or not; 1e-13 of the row scale."""
     import torch
 
-    L = 4
     m = SSMesh(*n, L, perturb=0.1, seed=12)
     el = m.elements(L)
     E = m.n_elements
