@@ -712,8 +712,11 @@ def measure_batch(dev, count=256, seed=0):
         "all_converged": bool(rc == 0 and (tr <= 1.5e-10).all()),
         "poisson": kinds.count("poisson"), "elasticity": kinds.count("elasticity"),
         "setup_seconds": setup, "autotune_seconds": tune,
-        "autotune": [{"chunk": c[0], "threads": c[1], "ctas_per_sm": c[2], "ms_per_chunk": t} for c, t in table],
-        "tuned": list(bs.tuned),
+        "autotune": [{"chunk": c[0], "threads": c[1], "ctas_per_sm": c[2], "kernels": k, "ms_per_chunk": t}
+                     for c, k, t in table],
+        "autotune_kernels": "laplacian: -1 per-level default, 0 staged 64-element tiles, 2 thread per element, "
+                            "8 stencil tiles; elasticity: -1 tcgen05 at L=4, 0 SIMT",
+        "tuned": list(bs.tuned), "tuned_kernels": bs.tuned_kernels,
     }
     # staggered arrivals: Poisson process over the first half of the simultaneous solve's
     # time, in a seeded random order; latency from each problem's own release

@@ -361,21 +361,67 @@ class BatchSolver:
                                                                  C.byref(ms)), "batch_solve_time_chunk")
         return ms.value
 
-    def autotune(self, b, candidates=None, reps=1):
-        """Pick (chunk, threads, CTAs per SM) of the batched vector kernels by timing a
-        captured chunk of CG iterations on a scratch iterate; returns the timing table."""
+    # element-kernel tile shapes the autotuner tries: the FP32 sshex8 Laplacian
+    # (sfem_gb300_set_laplacian_kernel: -1 per-level default, 0 staged tiles of 64
+    # elements with one thread each, 2 one thread per element, 8 node-centric stencil
+    # tiles of 32 elements x 4 warps) and the FP32 elasticity kernel
+    # (sfem_gb300_set_elasticity_kernel: -1 default = tcgen05 pairs at L = 4, 0 SIMT warp
+    # per element)
+    KERNEL_CANDIDATES = {"laplacian": (-1, 0, 2, 8), "elasticity": (-1, 0)}
+
+    def _set_kernels(self, kernels):
+        """Select the element kernels; returns the previous selection."""
+        lib = capi.load()
+        prev = {"laplacian": lib.sfem_gb300_set_laplacian_kernel(int(kernels["laplacian"]))}
+        old_e = getattr(self, "_elasticity_kernel", -1)
+        capi.check(lib.sfem_gb300_set_elasticity_kernel(int(kernels["elasticity"])), "set_elasticity_kernel")
+        self._elasticity_kernel = int(kernels["elasticity"])
+        prev["elasticity"] = old_e
+        return prev
+
+    def autotune(self, b, candidates=None, reps=1, kernels=None):
+        """Pick the element kernels (tile shapes) of the group operators and the launch
+        shape (chunk, threads per CTA, CTAs per SM) of the batched vector kernels by
+        timing a captured chunk of CG iterations on a scratch iterate: first each
+        operator family's kernel candidates at the first launch shape, then the launch
+        shapes with the chosen kernels.  Returns the timing table."""
         import torch
 
         if candidates is None:
             candidates = [(2048, 256, 8), (4096, 256, 8), (8192, 512, 4), (4096, 128, 16)]
+        if kernels is None:
+            kernels = self.KERNEL_CANDIDATES
         table = []
-        for cand in candidates:
-            self.set_launch(*cand)
-            xs = torch.zeros_like(b)
-            table.append((cand, self.time_chunk(b, xs, reps)))
-        best = min(table, key=lambda t: t[1])[0]
-        self.set_launch(*best)
-        self.tuned = best
+        best = {"laplacian": -1, "elasticity": -1}
+        self.set_launch(*candidates[0])
+        saved = None
+        try:
+            for family, kind in (("laplacian", "poisson"), ("elasticity", "elasticity")):
+                if not any(g.kind == kind for g in self.groups) or len(kernels[family]) < 2:
+                    continue
+                timed = []
+                for v in kernels[family]:
+                    prev = self._set_kernels({**best, family: v})
+                    saved = saved or prev
+                    xs = torch.zeros_like(b)
+                    t = self.time_chunk(b, xs, reps)
+                    timed.append((t, v))
+                    table.append((candidates[0], {**best, family: v}, t))
+                best[family] = min(timed)[1]
+            prev = self._set_kernels(best)
+            saved = saved or prev
+            for cand in candidates:
+                self.set_launch(*cand)
+                xs = torch.zeros_like(b)
+                table.append((cand, dict(best), self.time_chunk(b, xs, reps)))
+        finally:
+            if saved is not None:
+                self._set_kernels(saved)
+        launch_rows = [t for t in table if t[1] == best]
+        best_launch = min(launch_rows, key=lambda t: t[2])[0]
+        self.set_launch(*best_launch)
+        self.tuned = best_launch
+        self.tuned_kernels = dict(best)
         return table
 
     def solve(self, b, x, release=None):
@@ -389,6 +435,15 @@ class BatchSolver:
         its = np.zeros(P, dtype=np.int32)
         sec = c_double(0)
         lib = capi.load()
+        prev = self._set_kernels(self.tuned_kernels) if getattr(self, "tuned_kernels", None) else None
+        try:
+            rc = self._run(lib, b, x, release, P, lat, its, sec)
+        finally:
+            if prev is not None:
+                self._set_kernels(prev)
+        return rc, lat, its, sec.value
+
+    def _run(self, lib, b, x, release, P, lat, its, sec):
         if release is None:
             rc = lib.sfem_gb300_batch_solve_run(self.solver.ptr, capi.vp(b), capi.vp(x), lat.ctypes.data_as(C.c_void_p),
                                                 its.ctypes.data_as(C.c_void_p), C.byref(sec))
@@ -399,7 +454,7 @@ class BatchSolver:
             rc = lib.sfem_gb300_batch_solve_run_released(self.solver.ptr, capi.vp(b), capi.vp(x),
                                                          rel.ctypes.data_as(C.c_void_p), lat.ctypes.data_as(C.c_void_p),
                                                          its.ctypes.data_as(C.c_void_p), C.byref(sec))
-        return rc, lat, its, sec.value
+        return rc
 
     def true_residuals(self, b, x):
         """||b_p - A_p x_p|| / ||b_p|| per problem with the FP64 operators (device)."""

@@ -1030,15 +1030,17 @@ static int launch_lap_cta(int L, ptrdiff_t nelements, idx_t **elements, ptrdiff_
 
 // ------------------------------------------------------------------ dispatch
 
-// Kernel variant override for benchmarking (SFEM_GB300_LAPLACIAN_KERNEL or
-// sfem_gb300_set_laplacian_kernel); without one, float applies pick per level
-// (L=4 async tile, L=2 thread per element, L=3 staged tile).
+// Kernel variant override for benchmarking and the batched autotuner
+// (SFEM_GB300_LAPLACIAN_KERNEL or sfem_gb300_set_laplacian_kernel); without one the
+// applies pick per level: the node-centric stencil kernel (8) at L = 3, 4 and, in
+// FP64, at L = 2; the thread-per-element kernel (2) for float at L = 2.
 // "staged" (0) = shared-memory staged tile kernel for float, L <= 4;
 // "warp" (1) = warp per element; "thread" (2) = registers-only thread per element;
 // "async" (3) = cp.async staged tile, two threads per element, packed FP32x2 FMAs (even L);
 // "pipe" (4) = persistent CTAs, cp.async pipeline across tiles, one warp per micro layer (even L);
 // 6 = the async tile with four threads per element (one micro layer each, L = 4);
-// 7 = the async tile of 64 elements (128 threads per CTA, L = 4).
+// 7 = the async tile of 64 elements (128 threads per CTA, L = 4);
+// "stencil" (8) = node-centric stencil tiles of 32 elements (stencil.cu), L = 2..4.
 static int g_laplacian_variant = -1;
 static int g_laplacian_variant_forced = 0;  // set by sfem_gb300_set_laplacian_kernel
 static int laplacian_variant() {

@@ -80,10 +80,17 @@ def test_batch_autotune_and_dot(cuda, batch):
     import torch
 
     b = batch.rhs()
-    table = batch.autotune(b, candidates=[(1024, 128, 8), (4096, 256, 8)], reps=1)
+    lib = capi.load()
+    before = lib.sfem_gb300_set_laplacian_kernel(-1)
+    table = batch.autotune(b, candidates=[(1024, 128, 8), (4096, 256, 8)], reps=1,
+                           kernels={"laplacian": (-1, 8), "elasticity": (-1, 0)})
     assert any(g.spaces[-1].is_macro_coarse for g in batch.groups)
-    assert len(table) == 2 and all(t > 0 for _, t in table)
-    assert batch.tuned in [c for c, _ in table]
+    # two Laplacian and two elasticity kernel candidates, then both launch shapes
+    assert len(table) == 6 and all(t > 0 for *_, t in table)
+    assert batch.tuned_kernels["laplacian"] in (-1, 8) and batch.tuned_kernels["elasticity"] in (-1, 0)
+    assert batch.tuned in [c for c, k, _ in table if k == batch.tuned_kernels]
+    # the process-wide kernel choice is restored after tuning
+    assert lib.sfem_gb300_set_laplacian_kernel(before) == -1
     x = torch.zeros_like(b)
     rc, lat, its, sec = batch.solve(b, x)
     assert rc == 0, capi.last_error()
