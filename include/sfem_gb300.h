@@ -606,6 +606,19 @@ int sfem_gb300_batch_solve_run(void *solver, const double *b, double *x, double 
  * are counted from its release. */
 int sfem_gb300_batch_solve_run_released(void *solver, const double *b, double *x, const double *release_s,
                                         double *latency_s, int *iterations_per_problem, double *seconds);
+/* Non-blocking driver, for several batched solvers (each with its own context) that
+ * advance independently on their own streams: begin captures the chunk if needed and
+ * starts the CG; step launches one chunk and the copy of the active mask; poll returns
+ * 2 while that mask is in flight (SFEM_GB300_FAILURE on an error), else 0 with the mask
+ * in active[P] (may be NULL), the
+ * number of active problems and the iterations done.  A problem has converged when its
+ * flag drops to 0; step again only after poll returned 0 with problems still active. */
+int sfem_gb300_batch_solve_begin(void *solver, const double *b, double *x);
+/* Stream priority of the solver's own stream: level 0 the default, each level one step
+ * higher, clamped to the device's priority range (not while a chunk is in flight). */
+int sfem_gb300_batch_solve_set_priority(void *solver, int level);
+int sfem_gb300_batch_solve_step(void *solver);
+int sfem_gb300_batch_solve_poll(void *solver, int *active, int *n_active, int *iterations);
 /* Mean milliseconds of `reps` replays of the captured chunk starting from x (x is
  * modified): the autotuner's measurement. */
 int sfem_gb300_batch_solve_time_chunk(void *solver, const double *b, double *x, int reps, double *ms);

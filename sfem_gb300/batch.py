@@ -469,3 +469,94 @@ class BatchSolver:
         capi.check(lib.sfem_gb300_batch_dot(self.layout.ptr, capi.FLOAT64, capi.vp(r), capi.vp(r), capi.vp(rr)), "dot")
         capi.check(lib.sfem_gb300_batch_dot(self.layout.ptr, capi.FLOAT64, capi.vp(b), capi.vp(b), capi.vp(bb)), "dot")
         return (rr.sqrt() / bb.sqrt()).cpu().numpy()
+
+
+class ConcurrentBatchSolver:
+    """The problems of a :class:`BatchSolver`, one batched solver per group (its own
+    context, stream and captured chunk of CG iterations), advanced independently by one
+    host loop: a group launches its next chunk as soon as the convergence mask of its
+    last chunk has arrived (``sfem_gb300_batch_solve_begin / step / poll``).  Kernels of
+    different groups overlap on the GPU, and a group of small problems finishes on its
+    own cadence instead of the slowest group's."""
+
+    PRIORITY_LEVELS = 6  # stream priority steps used (clamped to the device's range)
+
+    def __init__(self, problems, device="cuda:0", launch=None, kernels=None, coarse_min_nodes=27, prioritize=True,
+                 **kw):
+        keyf = lambda p: (p.kind, p.level, coarse_depth(p.n, coarse_min_nodes))
+        keys = sorted({keyf(p) for p in problems})
+        self.subs = [BatchSolver([p for p in problems if keyf(p) == k], device=device,
+                                 coarse_min_nodes=coarse_min_nodes, **kw) for k in keys]
+        if launch is not None:
+            for s in self.subs:
+                s.set_launch(*launch)
+        # the smaller a group's total dofs, the higher its stream priority: its chunks
+        # are short, and running them first is what takes its problems out of the queue
+        self.priority = [0] * len(self.subs)
+        if prioritize and len(self.subs) > 1:
+            order = sorted(range(len(self.subs)), key=lambda i: self.subs[i].n)
+            top = self.PRIORITY_LEVELS - 1
+            for rank, i in enumerate(order):
+                self.priority[i] = top - (rank * self.PRIORITY_LEVELS) // len(self.subs)
+                capi.check(capi.load().sfem_gb300_batch_solve_set_priority(self.subs[i].solver.ptr,
+                                                                           C.c_int(self.priority[i])),
+                           "batch_solve_set_priority")
+        self.kernels = dict(kernels) if kernels else None
+        self.problems = [p for s in self.subs for p in s.problems]
+        self.offsets = np.cumsum([0] + [s.n_problems for s in self.subs])
+
+    @property
+    def n_problems(self):
+        return len(self.problems)
+
+    def rhs(self):
+        """One right-hand side per group (in group order)."""
+        return [s.rhs() for s in self.subs]
+
+    def solve(self, bs, xs):
+        """Solve every group's problems to ||b_p - A_p x_p|| <= rtol ||b_p|| (zero start),
+        all submitted at once.  Returns (per-problem latency s, per-problem iterations,
+        seconds); a problem's latency is when the host saw its group's mask drop it."""
+        import time
+
+        lib = capi.load()
+        P = self.n_problems
+        lat = np.zeros(P)
+        its = np.zeros(P, dtype=np.int32)
+        n = len(self.subs)
+        masks = [np.zeros(s.n_problems, dtype=np.int32) for s in self.subs]
+        prev = [None] * n
+        done = [False] * n
+        saved = self.subs[0]._set_kernels(self.kernels) if self.kernels else None
+        try:
+            t0 = time.perf_counter()
+            for s, b, x in zip(self.subs, bs, xs):
+                capi.check(lib.sfem_gb300_batch_solve_begin(s.solver.ptr, capi.vp(b), capi.vp(x)), "batch_solve_begin")
+            n_act, it = C.c_int(0), C.c_int(0)
+            while not all(done):
+                for i, s in enumerate(self.subs):
+                    if done[i]:
+                        continue
+                    rc = lib.sfem_gb300_batch_solve_poll(s.solver.ptr, masks[i].ctypes.data_as(C.c_void_p),
+                                                         C.byref(n_act), C.byref(it))
+                    if rc == 2:  # this group's chunk is still running
+                        continue
+                    capi.check(rc, "batch_solve_poll")
+                    now = time.perf_counter() - t0
+                    if prev[i] is not None:
+                        conv = (prev[i] != 0) & (masks[i] == 0)
+                        lat[self.offsets[i]:self.offsets[i + 1]][conv] = now
+                        its[self.offsets[i]:self.offsets[i + 1]][conv] = it.value
+                    prev[i] = masks[i].copy()
+                    if n_act.value == 0:
+                        done[i] = True
+                        continue
+                    capi.check(lib.sfem_gb300_batch_solve_step(s.solver.ptr), "batch_solve_step")
+            seconds = time.perf_counter() - t0
+        finally:
+            if saved is not None:
+                self.subs[0]._set_kernels(saved)
+        return lat, its, seconds
+
+    def true_residuals(self, bs, xs):
+        return np.concatenate([s.true_residuals(b, x) for s, b, x in zip(self.subs, bs, xs)])

@@ -20,6 +20,7 @@
 //    the per-problem active mask once per chunk;
 //  * the work-list chunk, the CTA shape of the vector kernels and the chunk length
 //    are picked by an autotuner that times the captured chunk for each candidate.
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstring>
@@ -501,9 +502,37 @@ public:
     std::vector<int> h_iters;
     int iterations{0};
     double seconds{0};
+    // non-blocking driver (begin / step / poll): pinned copy of the active mask, the
+    // event that marks its arrival
+    int *h_mask{nullptr};
+    cudaEvent_t mask_ready{nullptr};
+    bool pending{false};
+    double *run_x{nullptr};
+    int priority{0};  // CUDA stream priority of this solver's stream (0: the default)
+
+    int make_stream() {
+        if (stream) return 0;
+        SFEM_GB300_CUDA(cudaStreamCreateWithPriority(&stream, cudaStreamNonBlocking, priority));
+        return 0;
+    }
+    // level 0: default priority; each level up one step higher, clamped to the device's range
+    int set_priority(int level) {
+        if (pending) return set_error("BatchSolve: priority change while a chunk is in flight");
+        int least = 0, greatest = 0;
+        SFEM_GB300_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        priority = std::max(greatest, least - std::max(level, 0));
+        if (stream) {
+            SFEM_GB300_CUDA(cudaStreamSynchronize(stream));
+            SFEM_GB300_CUDA(cudaStreamDestroy(stream));
+            stream = nullptr;
+        }
+        return make_stream();
+    }
 
     ~BatchSolve() {
         exec_reset();
+        if (mask_ready) cudaEventDestroy(mask_ready);
+        if (h_mask) cudaFreeHost(h_mask);
         if (stream) cudaStreamDestroy(stream);
     }
     void exec_reset() {
@@ -543,13 +572,66 @@ public:
         }
         return on_stream([&] { return cg->iterate(check_every, x); });
     }
+    // Capture (if needed) and start the CG on this solver's own stream; then step() launches
+    // one chunk and the copy of the active mask without waiting, and poll() reports whether
+    // that mask has arrived.  Several solvers on their own streams (and contexts) advance
+    // independently: a host loop steps each one whose last mask has arrived.
+    int begin(const double *b, double *x) {
+        const int P = lay->P;
+        SFEM_GB300_CHECK(make_stream());
+        if (!h_mask) SFEM_GB300_CUDA(cudaMallocHost(&h_mask, (size_t)P * sizeof(int)));
+        if (!mask_ready) SFEM_GB300_CUDA(cudaEventCreateWithFlags(&mask_ready, cudaEventDisableTiming));
+        SFEM_GB300_CUDA(cudaStreamSynchronize(ctx->stream));
+        if (use_graph && (!exec || g_x != x)) {
+            DeviceBuffer<double> xs(cg->rows());
+            SFEM_GB300_CUDA(cudaMemcpyAsync(xs.ptr, x, cg->rows() * sizeof(double), cudaMemcpyDeviceToDevice, stream));
+            SFEM_GB300_CHECK(on_stream([&] { return cg->start(b, xs.ptr); }));
+            SFEM_GB300_CHECK(on_stream([&] { return cg->iterate(1, xs.ptr); }));
+            SFEM_GB300_CUDA(cudaStreamSynchronize(stream));
+            SFEM_GB300_CHECK(capture(x));
+        }
+        SFEM_GB300_CHECK(on_stream([&] { return cg->start(b, x); }));
+        SFEM_GB300_CUDA(cudaMemcpyAsync(h_mask, cg->active.ptr, P * sizeof(int), cudaMemcpyDeviceToHost, stream));
+        SFEM_GB300_CUDA(cudaEventRecord(mask_ready, stream));
+        pending = true;
+        iterations = 0;
+        run_x = x;
+        return 0;
+    }
+    int step() {
+        if (pending) return set_error("BatchSolve: step before the previous mask arrived");
+        if (iterations >= max_it) return set_error("BatchSolve: no convergence in %d iterations", max_it);
+        SFEM_GB300_CHECK(chunk(run_x));
+        iterations += check_every;
+        SFEM_GB300_CUDA(cudaMemcpyAsync(h_mask, cg->active.ptr, lay->P * sizeof(int), cudaMemcpyDeviceToHost, stream));
+        SFEM_GB300_CUDA(cudaEventRecord(mask_ready, stream));
+        pending = true;
+        return 0;
+    }
+    // 0: the mask of the last step (or of begin) is in `active`; kPollNotReady: not yet
+    static constexpr int kPollNotReady = 2;
+    int poll(int *active, int *n_active) {
+        if (!pending) return set_error("BatchSolve: poll without a step");
+        const cudaError_t e = cudaEventQuery(mask_ready);
+        if (e == cudaErrorNotReady) return kPollNotReady;
+        if (e != cudaSuccess) return set_error("BatchSolve: %s", cudaGetErrorString(e));
+        pending = false;
+        int n = 0;
+        for (int q = 0; q < lay->P; q++) {
+            if (active) active[q] = h_mask[q];
+            n += h_mask[q] != 0;
+        }
+        if (n_active) *n_active = n;
+        return 0;
+    }
+
     // release_s (host, optional): release time of every problem in seconds from the start
     // of the solve.  A problem joins the iteration at the first chunk boundary after its
     // release (until then it keeps its start state: the CG update kernels skip inactive
     // problems); its latency is counted from its release.
     int solve(const double *b, double *x, const double *release_s = nullptr) {
         const int P = lay->P;
-        if (!stream) SFEM_GB300_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+        SFEM_GB300_CHECK(make_stream());
         SFEM_GB300_CUDA(cudaStreamSynchronize(ctx->stream));  // caller's work on b, x is done
         if (use_graph && (!exec || g_x != x)) {
             // eager warm-up on a scratch iterate sizes every lazily allocated buffer
@@ -855,6 +937,25 @@ extern "C" int sfem_gb300_batch_solve_run_released(void *solver, const double *b
     return rc;
 }
 
+extern "C" int sfem_gb300_batch_solve_set_priority(void *solver, int level) {
+    return std::static_pointer_cast<BatchSolve>(H(solver)->impl)->set_priority(level);
+}
+
+extern "C" int sfem_gb300_batch_solve_begin(void *solver, const double *b, double *x) {
+    return std::static_pointer_cast<BatchSolve>(H(solver)->impl)->begin(b, x);
+}
+
+extern "C" int sfem_gb300_batch_solve_step(void *solver) {
+    return std::static_pointer_cast<BatchSolve>(H(solver)->impl)->step();
+}
+
+extern "C" int sfem_gb300_batch_solve_poll(void *solver, int *active, int *n_active, int *iterations) {
+    auto bs = std::static_pointer_cast<BatchSolve>(H(solver)->impl);
+    const int rc = bs->poll(active, n_active);
+    if (iterations) *iterations = bs->iterations;
+    return rc;
+}
+
 extern "C" int sfem_gb300_batch_solve_run(void *solver, const double *b, double *x, double *latency_s,
                                           int *iterations_per_problem, double *seconds) {
     return sfem_gb300_batch_solve_run_released(solver, b, x, nullptr, latency_s, iterations_per_problem, seconds);
@@ -862,7 +963,7 @@ extern "C" int sfem_gb300_batch_solve_run(void *solver, const double *b, double 
 
 extern "C" int sfem_gb300_batch_solve_time_chunk(void *solver, const double *b, double *x, int reps, double *ms) {
     auto bs = std::static_pointer_cast<BatchSolve>(H(solver)->impl);
-    if (!bs->stream) SFEM_GB300_CUDA(cudaStreamCreateWithFlags(&bs->stream, cudaStreamNonBlocking));
+    SFEM_GB300_CHECK(bs->make_stream());
     SFEM_GB300_CUDA(cudaStreamSynchronize(bs->ctx->stream));
     bs->use_graph = true;
     SFEM_GB300_CHECK(bs->on_stream([&] { return bs->cg->start(b, x); }));

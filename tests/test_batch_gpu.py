@@ -7,7 +7,7 @@ import pytest
 
 import oracle as O
 from sfem_gb300 import capi
-from sfem_gb300.batch import BatchSolver, ProblemSpec
+from sfem_gb300.batch import BatchSolver, ConcurrentBatchSolver, ProblemSpec
 from sfem_gb300.mesh import SSMesh
 
 pytestmark = pytest.mark.gpu
@@ -126,3 +126,36 @@ def test_batch_staggered_release(cuda, batch):
     assert (batch.true_residuals(b, x) <= 1.5e-10).all()
     with pytest.raises(ValueError):
         batch.solve(b, x, release=release[:-1])
+
+
+def test_concurrent_groups(cuda, batch):
+    """One batched solver per group on its own stream, advanced by the non-blocking
+    begin / step / poll driver: every problem converges to 1e-10 (oracle residual on its
+    own mesh), with the iterations the lockstep batch takes (to a chunk), and no group
+    waits for another's chunks."""
+    import torch
+
+    cs = ConcurrentBatchSolver(PROBLEMS, device=cuda, coarse_iterations=20)
+    assert len(cs.subs) == len(batch.groups) and sorted(map(str, cs.problems)) == sorted(map(str, batch.problems))
+    # the smallest group gets the highest stream priority level, the largest the lowest
+    sizes = [s.n for s in cs.subs]
+    assert cs.priority[int(np.argmin(sizes))] == max(cs.priority) > cs.priority[int(np.argmax(sizes))] == 0
+    bs = cs.rhs()
+    xs = [torch.zeros_like(b) for b in bs]
+    lat, its, sec = cs.solve(bs, xs)
+    assert (lat > 0).all() and lat.max() <= sec + 1e-9 and (its >= 1).all()
+    assert (cs.true_residuals(bs, xs) <= 1.5e-10).all()
+    b0 = batch.rhs()
+    x0 = torch.zeros_like(b0)
+    rc, _, its_lock, _ = batch.solve(b0, x0)
+    assert rc == 0, capi.last_error()
+    order = {str(p): i for i, p in enumerate(batch.problems)}
+    its_lock = np.array([its_lock[order[str(p)]] for p in cs.problems])
+    assert np.abs(its - its_lock).max() <= batch.check_every, (its, its_lock)
+    for i in (0, len(cs.problems) - 1):
+        k = next(j for j in range(len(cs.subs)) if cs.offsets[j] <= i < cs.offsets[j + 1])
+        s = cs.subs[k]
+        q = i - cs.offsets[k]
+        sl = slice(s.dof_offsets[q], s.dof_offsets[q + 1])
+        res = _oracle_residual(cs.problems[i], bs[k].cpu().numpy()[sl], xs[k].cpu().numpy()[sl])
+        assert res <= 2e-10, (cs.problems[i], res)
