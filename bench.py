@@ -973,10 +973,13 @@ def profile_kernels():
 def profile_apply():
     """Two launches each of the 48^3 L=4 Laplacian applies from packed tiles: the FP32
     stencil kernel (the step), the FP32 element-matrix kernel and the FP64 stencil
-    kernel.  A small ncu target (about 150 MB of inputs, above the L2)."""
+    kernel; then two each of the FP32 and FP64 stencil applies at L=3 from SoA rows on
+    a 64^3 macro mesh (7,189,057 nodes).  A small ncu target (about 150 MB of inputs per
+    apply, above the L2)."""
     import torch
 
     from sfem_gb300 import capi
+    from sfem_gb300.mesh import SSMesh
     from sfem_gb300.operators import Laplacian, SSMeshDevice
 
     dev = torch.device("cuda:0")
@@ -992,6 +995,15 @@ def profile_apply():
             y.zero_()
             op.apply(x, y)
         lib.sfem_gb300_set_laplacian_kernel(prev)
+    del op
+    m3 = SSMesh(64, 64, 64, 3, perturb=PERTURB, seed=SEED)
+    op3 = Laplacian(SSMeshDevice(m3, 3, device=dev), packed=False).initialize()
+    for dt in (torch.float32, torch.float64):
+        x = torch.randn(m3.n_nodes(3), dtype=dt, device=dev)
+        y = torch.zeros_like(x)
+        for _ in range(2):
+            y.zero_()
+            op3.apply(x, y)
     torch.cuda.synchronize()
     print("profile apply: done")
 
