@@ -85,20 +85,20 @@ int cu_laplacian_diag(int element_type, ptrdiff_t nelements, sfem_gb300_idx_t **
  * element, 2 thread per element in registers, 3 cp.async staged tile with two
  * threads per element, 4 persistent cp.async pipeline with one warp per micro
  * layer (3 and 4: even L; other levels use the staged tile), 8 node-centric
- * stencil form (L = 4; the FP64 default there, FP32 on request).  Returns the
- * previous setting (-1 if none was forced). */
+ * stencil form (L = 2, 3, 4; the default at L = 3, 4 and in FP64 at L = 2).
+ * Returns the previous setting (-1 if none was forced). */
 int sfem_gb300_set_laplacian_kernel(int variant);
 
 /* Packed tiles (no reference counterpart; an operator-creation step like the
- * reference's FFF cache): the connectivity and FFF of sshex8 L = 4 repacked into
- * one contiguous block per 32 consecutive macro elements ([(L+1)^3][el] int32 node
- * ids, then [6][el] FFF floats; elements past the end: node 0, FFF 0) so the FP32
+ * reference's FFF cache): the connectivity and FFF of sshex8 L = 3 or 4 repacked
+ * into one contiguous block per 32 consecutive macro elements ([(L+1)^3][el] int32
+ * node ids, then [6][el] FFF floats; elements past the end: node 0, FFF 0) so an
  * apply fetches a tile's ids and metric with one bulk copy.
  * sfem_gb300_sshex8_packed_bytes gives the block array's size (-1: unsupported
  * type), sfem_gb300_sshex8_pack fills it (16-byte aligned),
  * sfem_gb300_sshex8_laplacian_apply_packed computes y += A x from it (FP32 and
- * FP64 x / y: the node-centric stencil kernel; FP32 with kernel variant 3 forced:
- * the element-matrix kernel); the result equals cu_laplacian_apply's on the same
+ * FP64 x / y: the node-centric stencil kernel; FP32 at L = 4 with another kernel
+ * variant forced: the element-matrix kernel); the result equals cu_laplacian_apply's on the same
  * connectivity and FFF up to rounding order.  sfem_gb300_laplacian_status returns
  * (and clears) 1 if a packed apply gave up waiting for its bulk copy (2 if the
  * drain after that gave up too), else 0.

@@ -1283,19 +1283,25 @@ extern "C" int sfem_gb300_set_laplacian_kernel(int variant) {
 
 // ------------------------------------------------------------------ packed tiles (C ABI)
 
+// levels served from packed tiles: 4 (stencil or element-matrix kernel) and 3 (stencil)
+static int packed_level(int element_type) {
+    return element_type == SFEM_GB300_SSHEX8(PK_L) ? PK_L : element_type == SFEM_GB300_SSHEX8(3) ? 3 : -1;
+}
+
 extern "C" ptrdiff_t sfem_gb300_sshex8_packed_bytes(int element_type, ptrdiff_t nelements) {
-    if (element_type != SFEM_GB300_SSHEX8(PK_L) || nelements < 0) return -1;
-    return (nelements + PK_TILE - 1) / PK_TILE * (ptrdiff_t)pk_words(PK_L) * (ptrdiff_t)sizeof(int32_t);
+    const int L = packed_level(element_type);
+    if (L < 0 || nelements < 0) return -1;
+    return (nelements + PK_TILE - 1) / PK_TILE * (ptrdiff_t)pk_words(L) * (ptrdiff_t)sizeof(int32_t);
 }
 
 extern "C" int sfem_gb300_sshex8_pack(int element_type, ptrdiff_t nelements, idx_t **elements, ptrdiff_t fff_stride,
                                       const float *fff, void *packed, void *stream) {
-    if (element_type != SFEM_GB300_SSHEX8(PK_L))
-        return set_error("sfem_gb300_sshex8_pack: element type %d is not sshex8 L = %d", element_type, PK_L);
+    const int L = packed_level(element_type);
+    if (L < 0) return set_error("sfem_gb300_sshex8_pack: element type %d is not sshex8 L = 3 or 4", element_type);
     if (nelements <= 0) return SFEM_GB300_SUCCESS;
     if (reinterpret_cast<uintptr_t>(packed) & 15) return set_error("sfem_gb300_sshex8_pack: packed is not 16-byte aligned");
-    constexpr int nxe = (PK_L + 1) * (PK_L + 1) * (PK_L + 1);
-    const ptrdiff_t total = (nelements + PK_TILE - 1) / PK_TILE * (ptrdiff_t)pk_words(PK_L);
+    const int nxe = (L + 1) * (L + 1) * (L + 1);
+    const ptrdiff_t total = (nelements + PK_TILE - 1) / PK_TILE * (ptrdiff_t)pk_words(L);
     sshex8_pack_kernel<<<grid_for(total, 256), 256, 0, stream_of(stream)>>>(nelements, nxe, elements, fff_stride, fff,
                                                                            (int32_t *)packed);
     return check_launch("sfem_gb300_sshex8_pack");
@@ -1303,22 +1309,23 @@ extern "C" int sfem_gb300_sshex8_pack(int element_type, ptrdiff_t nelements, idx
 
 extern "C" int sfem_gb300_sshex8_laplacian_apply_packed(int element_type, ptrdiff_t nelements, const void *packed,
                                                         int real_type_xy, const void *x, void *y, void *stream) {
-    if (element_type != SFEM_GB300_SSHEX8(PK_L))
-        return set_error("sfem_gb300_sshex8_laplacian_apply_packed: element type %d is not sshex8 L = %d",
-                         element_type, PK_L);
+    const int L = packed_level(element_type);
+    if (L < 0)
+        return set_error("sfem_gb300_sshex8_laplacian_apply_packed: element type %d is not sshex8 L = 3 or 4",
+                         element_type);
     if (nelements <= 0) return SFEM_GB300_SUCCESS;
     if (reinterpret_cast<uintptr_t>(packed) & 15)
         return set_error("sfem_gb300_sshex8_laplacian_apply_packed: packed is not 16-byte aligned");
-    // FP64 always, FP32 with variant 8: the node-centric stencil kernel on the same blocks
+    // FP64 always, FP32 with variant 8 or at L = 3: the node-centric stencil kernel on the blocks
     if (real_type_xy == SFEM_GB300_FLOAT64 || real_type_xy == SFEM_GB300_REAL_DEFAULT)
-        return sshex8_laplacian_stencil_apply<double>(PK_L, nelements, (const int32_t *)packed, nullptr, 0, nullptr,
+        return sshex8_laplacian_stencil_apply<double>(L, nelements, (const int32_t *)packed, nullptr, 0, nullptr,
                                                       (const double *)x, (double *)y, stream_of(stream));
     if (real_type_xy != SFEM_GB300_FLOAT32)
         return set_error("sfem_gb300_sshex8_laplacian_apply_packed: unsupported real type %d", real_type_xy);
-    // the stencil kernel unless another kernel was forced (packed element-matrix kernel:
-    // 50.8 us against 45.0 us on the 48^3 L = 4 mesh)
-    if (laplacian_variant() == 8 || !__atomic_load_n(&g_laplacian_variant_forced, __ATOMIC_RELAXED))
-        return sshex8_laplacian_stencil_apply<float>(PK_L, nelements, (const int32_t *)packed, nullptr, 0, nullptr,
+    // the stencil kernel unless another kernel was forced at L = 4 (packed element-matrix
+    // kernel: 50.8 us against 45.0 us on the 48^3 L = 4 mesh)
+    if (L != PK_L || laplacian_variant() == 8 || !__atomic_load_n(&g_laplacian_variant_forced, __ATOMIC_RELAXED))
+        return sshex8_laplacian_stencil_apply<float>(L, nelements, (const int32_t *)packed, nullptr, 0, nullptr,
                                                      (const float *)x, (float *)y, stream_of(stream));
     const ptrdiff_t ntiles = (nelements + PK_TILE - 1) / PK_TILE;
     if (ntiles > 0x7fffffff) return set_error("sfem_gb300_sshex8_laplacian_apply_packed: too many tiles");

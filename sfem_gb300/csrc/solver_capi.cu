@@ -29,7 +29,7 @@ public:
     idx_t **elements{nullptr};
     const float *fff{nullptr};
     const idx_t *dirichlet{nullptr};
-    // FP32 sshex8 L = 4: connectivity + FFF repacked per 32-element tile, built at creation
+    // FP32 sshex8 L = 3, 4: connectivity + FFF repacked per 32-element tile, built at creation
     // (the operator keeps the geometry it was created with, as the reference's op keeps its FFF)
     DeviceBuffer<int32_t> packed;
     int prepare() {

@@ -362,6 +362,7 @@ __global__ void __launch_bounds__(kThreads) sshex8_laplacian_stencil_kernel(
     constexpr int N1 = L + 1;
     constexpr int NXE = N1 * N1 * N1;
     constexpr int WORDS = pk_words(L);
+    static_assert(WORDS * 4 % 16 == 0, "a tile's bulk copy is a whole number of 16-byte units");
     extern __shared__ __align__(128) unsigned char st_smem[];
     __shared__ __align__(8) uint64_t mbar;
     int32_t *sidx = reinterpret_cast<int32_t *>(st_smem);
@@ -464,9 +465,10 @@ int sshex8_laplacian_stencil_apply(int L, ptrdiff_t nelements, const int32_t *pa
     if (nelements <= 0) return SFEM_GB300_SUCCESS;
     if (!sshex8_laplacian_stencil_supported(L)) return set_error("sshex8 Laplacian stencil apply: level %d not served", L);
     if (packed) {
-        if (L != PK_L) return set_error("sshex8 Laplacian stencil apply: packed tiles hold level %d, not %d", PK_L, L);
         if (reinterpret_cast<uintptr_t>(packed) & 15)
             return set_error("sshex8 Laplacian stencil apply: packed block not 16-byte aligned");
+        if (L == 3) return stencil::launch<T, 3, true>(nelements, packed, nullptr, 0, nullptr, x, y, s);
+        if (L != PK_L) return set_error("sshex8 Laplacian stencil apply: no packed tiles at level %d", L);
         return stencil::launch<T, 4, true>(nelements, packed, nullptr, 0, nullptr, x, y, s);
     }
     switch (L) {

@@ -26,7 +26,7 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 // a CTA fetches its tile's ids and metric with one bulk copy (cp.async.bulk,
 // completion counted on an mbarrier) instead of (L+1)^3 row segments from SoA rows.
 constexpr int PK_TILE = 32;
-constexpr int PK_L = 4;  // the level the packed path serves
+constexpr int PK_L = 4;  // the packed element-matrix kernel's level (the stencil kernel also packs L = 3)
 __host__ __device__ constexpr int pk_words(int L) { return PK_TILE * ((L + 1) * (L + 1) * (L + 1) + 6); }
 // polls of a tile's bulk-copy mbarrier before a kernel gives up and reports it
 constexpr int LAP_WAIT_POLLS = 1 << 20;

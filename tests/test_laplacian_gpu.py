@@ -148,14 +148,16 @@ def test_sshex8_laplacian_fp64_kernels(cuda, variant, L, n, aligned):
 @pytest.mark.parametrize("form", ["fp32_em", "fp32_stencil", "fp64_stencil"])
 @pytest.mark.parametrize("n", [(5, 4, 3), (9, 8, 7), (1, 1, 1), (36, 36, 36), (2, 16, 1), (3, 11, 1)])
 @pytest.mark.parametrize("aligned", [True, False])
-def test_sshex8_laplacian_packed(cuda, form, n, aligned):
-    """Packed tiles (L = 4): pack from SoA rows (row stride E or E + 1) and apply with the
-    FP32 stencil kernel (default), the FP32 element-matrix kernel (any other forced
-    variant) or FP64 (stencil kernel); element counts 60 (32 + 28: a ragged last tile),
-    504, 1, 46,656, 32 (one full tile) and 33 (a last tile of one element)."""
+@pytest.mark.parametrize("L", [4, 3])
+def test_sshex8_laplacian_packed(cuda, form, n, aligned, L):
+    """Packed tiles (L = 4 and 3): pack from SoA rows (row stride E or E + 1) and apply
+    with the FP32 stencil kernel (default), the FP32 element-matrix kernel (L = 4, any
+    other forced variant) or FP64 (stencil kernel); element counts 60 (32 + 28: a ragged
+    last tile), 504, 1, 46,656, 32 (one full tile) and 33 (a last tile of one element)."""
     import torch
 
-    L = 4
+    if form == "fp32_em" and L != 4:
+        pytest.skip("the element-matrix packed kernel serves L = 4")
     m = SSMesh(*n, L, perturb=0.1, seed=6)
     el = m.elements(L)
     E = m.n_elements
@@ -267,8 +269,10 @@ def test_sshex8_laplacian_packed_bad_inputs(cuda):
     import torch
 
     lib = capi.load()
-    assert lib.sfem_gb300_sshex8_packed_bytes(capi.SSHEX8(3), capi.i64(10)) == -1
+    # packed tiles serve L = 3 and 4 only
     assert lib.sfem_gb300_sshex8_packed_bytes(capi.SSHEX8(2), capi.i64(10)) == -1
+    assert lib.sfem_gb300_sshex8_packed_bytes(capi.SSHEX8(5), capi.i64(10)) == -1
+    assert lib.sfem_gb300_sshex8_packed_bytes(capi.SSHEX8(3), capi.i64(10)) == 32 * (64 + 6) * 4
     assert lib.sfem_gb300_sshex8_packed_bytes(capi.SSHEX8(4), capi.i64(0)) == 0
     buf = torch.zeros(64, dtype=torch.int32, device=cuda)
     x = torch.zeros(8, dtype=torch.float64, device=cuda)
