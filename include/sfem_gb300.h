@@ -89,6 +89,16 @@ int cu_laplacian_diag(int element_type, ptrdiff_t nelements, sfem_gb300_idx_t **
  * Returns the previous setting (-1 if none was forced). */
 int sfem_gb300_set_laplacian_kernel(int variant);
 
+/* Non-affine sshex8 Laplacian, y += A x (replaces sshex8_laplacian_apply,
+ * operators/sshex8/sshex8_laplacian.cpp:39-182, on the GPU): macro elements with the
+ * trilinear geometry of their 8 corner nodes (points_x/y/z: device float arrays, the
+ * reference's SoA geom_t** points), every micro element integrated with the six-point
+ * face-centre rule at the FFF of the macro map.  element_type SSHEX8(L), 1 <= L <= 16;
+ * FP32 or FP64 x / y; a correctness path (one CTA per macro element), not tuned. */
+int sfem_gb300_sshex8_laplacian_apply_nonaffine(int element_type, ptrdiff_t nelements, sfem_gb300_idx_t **elements,
+                                                const float *points_x, const float *points_y, const float *points_z,
+                                                int real_type_xy, const void *x, void *y, void *stream);
+
 /* Packed tiles (no reference counterpart; an operator-creation step like the
  * reference's FFF cache): the connectivity and FFF of sshex8 L = 3 or 4 repacked
  * into one contiguous block per 32 consecutive macro elements ([(L+1)^3][el] int32

@@ -109,6 +109,22 @@ def fff_fill(corners, points, use_ref=False):
     return out
 
 
+def sshex8_laplacian_apply_nonaffine(L, elements, points, u, out=None, use_ref=False):
+    """values += A u for the non-affine sshex8 Laplacian (six-point rule per micro element,
+    FFF of the trilinear macro map at every point).  use_ref: the reference's own
+    sshex8_laplacian_apply (operators/sshex8/sshex8_laplacian.cpp:39-182)."""
+    E = elements.shape[1]
+    u = _f64(u)
+    out = np.zeros_like(u) if out is None else out
+    ea, pa = PtrArray(elements.astype(np.int32)), PtrArray(_f32(points))
+    if use_ref:
+        rc = ref().sshex8_laplacian_apply(c_int(L), c_ptrdiff(E), ea.p, pa.p, _ptr(u), _ptr(out))
+    else:
+        rc = lib().or_sshex8_laplacian_apply_nonaffine(c_int(L), c_ptrdiff(E), ea.p, pa.p, _ptr(u), _ptr(out))
+    assert rc == 0, rc
+    return out
+
+
 def adjugate_fill(corners, points, use_ref=False):
     L = ref() if use_ref else lib()
     fn = L.ref_hex8_adjugate_and_det_fill if use_ref else L.or_hex8_adjugate_and_det_fill

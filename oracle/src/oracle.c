@@ -1107,3 +1107,84 @@ int or_residual_dd_em(int bs, int L, ptrdiff_t nelements, idx_t **elements, cons
                       const double *x_lo, const double *b, ptrdiff_t ndofs, double *r) {
     return residual_dd(bs == 3 ? 1 : 0, L, nelements, elements, NULL, NULL, 0, 0, em, x, x_lo, b, ndofs, r);
 }
+
+/* ------------------------------------------------------------------------ */
+/* Non-affine sshex8 Laplacian                                               */
+/* ------------------------------------------------------------------------ */
+
+/* sshex8_laplacian_apply (operators/sshex8/sshex8_laplacian.cpp:39-182), values += A u
+ * for macro elements whose geometry is the trilinear map of their 8 corner nodes.
+ * Per micro element (xi, yi, zi): the six-point rule at the face centres of the micro
+ * reference cube, weights 1/6 (q6, operators/hex8/hex8_quadrature.hpp:4-15); at each
+ * point the FFF of the macro map at the macro coordinates ((xi, yi, zi) + q) / L, scaled
+ * by h = 1/L to the micro element (hex8_sub_fff_0, :19-28), and
+ * v_i += w grad phi_i(q) . (G grad u(q)) (what hex8_laplacian_apply_fff evaluates,
+ * operators/hex8/hex8_laplacian_inline_cpu.hpp:6). */
+static const double OR_Q6[6][3] = {{0.0, 0.5, 0.5}, {0.5, 0.0, 0.5}, {0.5, 0.5, 0.0},
+                                   {0.5, 0.5, 1.0}, {0.5, 1.0, 0.5}, {1.0, 0.5, 0.5}};
+
+int or_sshex8_laplacian_apply_nonaffine(int L, ptrdiff_t nelements, idx_t **elements, geom_t **points,
+                                        const double *u, double *values) {
+    if (L < 1 || L > 16) return -1;
+    const int N1 = L + 1, nxe = N1 * N1 * N1;
+#pragma omp parallel
+    {
+        double *eu = (double *)malloc(nxe * sizeof(double));
+        double *ev = (double *)malloc(nxe * sizeof(double));
+        idx_t *idx = (idx_t *)malloc(nxe * sizeof(idx_t));
+#pragma omp for
+        for (ptrdiff_t e = 0; e < nelements; e++) {
+            double x[8], y[8], z[8];
+            for (int c = 0; c < 8; c++) {
+                const idx_t n = elements[lidx(L, C8[c][0] * L, C8[c][1] * L, C8[c][2] * L)][e];
+                x[c] = points[0][n];
+                y[c] = points[1][n];
+                z[c] = points[2][n];
+            }
+            for (int v = 0; v < nxe; v++) {
+                idx[v] = elements[v][e];
+                eu[v] = u[idx[v]];
+                ev[v] = 0;
+            }
+            const double h = 1.0 / L;
+            for (int zi = 0; zi < L; zi++)
+                for (int yi = 0; yi < L; yi++)
+                    for (int xi = 0; xi < L; xi++) {
+                        int lev[8];
+                        double ue[8], ve[8] = {0};
+                        for (int c = 0; c < 8; c++) {
+                            lev[c] = lidx(L, xi + C8[c][0], yi + C8[c][1], zi + C8[c][2]);
+                            ue[c] = eu[lev[c]];
+                        }
+                        for (int k = 0; k < 6; k++) {
+                            double J[3][3], f[6], dphi[8][3], gu[3] = {0, 0, 0}, t[3];
+                            hex8_jacobian(x, y, z, h * (xi + OR_Q6[k][0]), h * (yi + OR_Q6[k][1]),
+                                          h * (zi + OR_Q6[k][2]), J);
+                            fff_from_jacobian(J, f);
+                            const double G[3][3] = {{f[0] * h, f[1] * h, f[2] * h},
+                                                    {f[1] * h, f[3] * h, f[4] * h},
+                                                    {f[2] * h, f[4] * h, f[5] * h}};
+                            for (int c = 0; c < 8; c++) {
+                                double w[3], dw[3];
+                                for (int d = 0; d < 3; d++) {
+                                    w[d] = C8[c][d] ? OR_Q6[k][d] : 1 - OR_Q6[k][d];
+                                    dw[d] = C8[c][d] ? 1.0 : -1.0;
+                                }
+                                dphi[c][0] = dw[0] * w[1] * w[2];
+                                dphi[c][1] = w[0] * dw[1] * w[2];
+                                dphi[c][2] = w[0] * w[1] * dw[2];
+                                for (int p = 0; p < 3; p++) gu[p] += dphi[c][p] * ue[c];
+                            }
+                            for (int p = 0; p < 3; p++) t[p] = (G[p][0] * gu[0] + G[p][1] * gu[1] + G[p][2] * gu[2]) / 6.0;
+                            for (int c = 0; c < 8; c++) ve[c] += dphi[c][0] * t[0] + dphi[c][1] * t[1] + dphi[c][2] * t[2];
+                        }
+                        for (int c = 0; c < 8; c++) ev[lev[c]] += ve[c];
+                    }
+            for (int v = 0; v < nxe; v++) atomic_add(&values[idx[v]], ev[v]);
+        }
+        free(eu);
+        free(ev);
+        free(idx);
+    }
+    return 0;
+}

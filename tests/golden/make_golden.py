@@ -129,10 +129,29 @@ def make_coefficient():
     print("wrote", OUT / "sshex8_coefficient.npz")
 
 
+def make_nonaffine():
+    """The non-affine sshex8 Laplacian: the reference's sshex8_laplacian_apply
+    (operators/sshex8/sshex8_laplacian.cpp:39-182; six-point rule per micro element, FFF
+    of the trilinear macro map at every point) on perturbed macro meshes at L = 2 and 4."""
+    assert O.ref() is not None, "reference kernels unavailable"
+    out = {}
+    for L, n, seed in ((2, (4, 3, 2), 51), (4, (3, 2, 2), 52)):
+        m = SSMesh(*n, L, perturb=0.2, seed=seed)
+        el = m.elements(L)
+        x = np.random.default_rng(seed + 100).standard_normal(m.n_nodes(L))
+        y = O.sshex8_laplacian_apply_nonaffine(L, el, m.points, x, use_ref=True)
+        out.update({f"L{L}_elements": el, f"L{L}_points": m.points.astype(np.float32), f"L{L}_x": x,
+                    f"L{L}_apply": y, f"L{L}_shape": np.array(n), f"L{L}_seed": seed})
+    np.savez_compressed(OUT / "sshex8_nonaffine.npz", perturb=0.2, **out)
+    print("wrote", OUT / "sshex8_nonaffine.npz")
+
+
 if __name__ == "__main__":
     if len(sys.argv) > 1 and sys.argv[1] == "float32":
         make_float32_stencil()
     elif len(sys.argv) > 1 and sys.argv[1] == "coefficient":
         make_coefficient()
+    elif len(sys.argv) > 1 and sys.argv[1] == "nonaffine":
+        make_nonaffine()
     else:
         main()
