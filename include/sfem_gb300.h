@@ -209,8 +209,10 @@ int cu_linear_elasticity_bsr(int element_type, ptrdiff_t nelements, sfem_gb300_i
                              double mu, double lambda, int real_type, const int32_t *rowptr, const int32_t *colidx,
                              void *values, void *stream);
 
-/* The reference's exact sshex8 entry point (operators/sshex8/cuda/cu_sshex8_linear_elasticity.cu:1730-1748);
- * only the interleaved layout (u_stride = out_stride = 3, uy = ux + 1, uz = ux + 2) is accepted. */
+/* The reference's exact sshex8 entry point (operators/sshex8/cuda/cu_sshex8_linear_elasticity.cu:1730-1748):
+ * component d of node g at u{x,y,z}[g * u_stride] and out{x,y,z}[g * out_stride].  The
+ * interleaved layout (stride 3, uy = ux + 1, uz = ux + 2) runs the tuned kernels; any
+ * other (separate arrays, padded strides) the CTA-per-macro-element kernel, L = 1..16. */
 int cu_affine_sshex8_linear_elasticity_apply(int level, ptrdiff_t nelements, sfem_gb300_idx_t **elements,
                                              ptrdiff_t jacobian_stride, const void *jacobian_adjugate,
                                              const void *jacobian_determinant, double mu, double lambda,

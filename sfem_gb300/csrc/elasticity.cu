@@ -832,12 +832,20 @@ __host__ __device__ constexpr size_t el_cta_smem_bytes(int L) {
     return (576 + 96 + 6 * (size_t)(L + 1) * (L + 1) * (L + 1)) * sizeof(T);
 }
 
+// three components of a nodal vector: component d of node g at c[d][g * stride]
+// (interleaved xyz: c = {u, u + 1, u + 2}, stride 3; separate arrays: stride 1)
+template <typename P>
+struct Comp3 {
+    P c[3];
+    ptrdiff_t stride;
+};
+
 template <typename T>
 __global__ void __launch_bounds__(256) elasticity_apply_cta_kernel(int L, ptrdiff_t nelements,
                                                                    const idx_t *const *elements, ptrdiff_t stride,
                                                                    const float *adjugate, const float *determinant,
-                                                                   T mu, T lambda, const T *__restrict__ x,
-                                                                   T *__restrict__ y) {
+                                                                   T mu, T lambda, Comp3<const T *> x,
+                                                                   Comp3<T *> y) {
     extern __shared__ __align__(16) unsigned char el_cta_smem[];
     const int N1 = L + 1, NXE = N1 * N1 * N1, NM = L * L * L;
     T *K = reinterpret_cast<T *>(el_cta_smem);
@@ -857,7 +865,7 @@ __global__ void __launch_bounds__(256) elasticity_apply_cta_kernel(int L, ptrdif
             const ptrdiff_t g = elements[l][e];
 #pragma unroll
             for (int d = 0; d < 3; d++) {
-                xs[d * NXE + l] = x[3 * g + d];
+                xs[d * NXE + l] = x.c[d][g * x.stride];
                 ys[d * NXE + l] = 0;
             }
         }
@@ -888,9 +896,9 @@ __global__ void __launch_bounds__(256) elasticity_apply_cta_kernel(int L, ptrdif
 #pragma unroll
             for (int d = 0; d < 3; d++) {
                 if (interior)
-                    y[3 * g + d] += ys[d * NXE + l];
+                    y.c[d][g * y.stride] += ys[d * NXE + l];
                 else
-                    atomicAdd(&y[3 * g + d], ys[d * NXE + l]);
+                    atomicAdd(&y.c[d][g * y.stride], ys[d * NXE + l]);
             }
         }
         __syncthreads();
@@ -956,8 +964,8 @@ __global__ void __launch_bounds__(64) elasticity_block_diag_any_kernel(int L, pt
 }
 
 template <typename T>
-static int launch_el_cta(int L, ptrdiff_t nelements, idx_t **elements, ptrdiff_t stride, const float *adj,
-                         const float *det, T mu, T lambda, const T *x, T *y, cudaStream_t s) {
+static int launch_el_cta_views(int L, ptrdiff_t nelements, idx_t **elements, ptrdiff_t stride, const float *adj,
+                               const float *det, T mu, T lambda, Comp3<const T *> xv, Comp3<T *> yv, cudaStream_t s) {
     const size_t smem = el_cta_smem_bytes<T>(L);
     if (smem > 227 * 1024)
         return set_error("sfem_gb300_linear_elasticity_apply: level %d needs %zu bytes of shared memory in %s", L,
@@ -968,8 +976,15 @@ static int launch_el_cta(int L, ptrdiff_t nelements, idx_t **elements, ptrdiff_t
         attr.store(smem, std::memory_order_relaxed);  // a racing caller at worst repeats the opt-in
     }
     const int grid = (int)std::min<ptrdiff_t>(nelements, (ptrdiff_t)kNumSMs * 8);
-    elasticity_apply_cta_kernel<T><<<grid, 256, smem, s>>>(L, nelements, elements, stride, adj, det, mu, lambda, x, y);
+    elasticity_apply_cta_kernel<T><<<grid, 256, smem, s>>>(L, nelements, elements, stride, adj, det, mu, lambda, xv, yv);
     return check_launch("sfem_gb300_linear_elasticity_apply(SSHEX8, CTA per element)");
+}
+
+template <typename T>
+static int launch_el_cta(int L, ptrdiff_t nelements, idx_t **elements, ptrdiff_t stride, const float *adj,
+                         const float *det, T mu, T lambda, const T *x, T *y, cudaStream_t s) {
+    return launch_el_cta_views<T>(L, nelements, elements, stride, adj, det, mu, lambda,
+                                  Comp3<const T *>{{x, x + 1, x + 2}, 3}, Comp3<T *>{{y, y + 1, y + 2}, 3}, s);
 }
 
 static int g_elasticity_kernel = -1;  // -1 default (tcgen05 at L = 4), 0 SIMT warp kernel, 1 tcgen05 3xTF32
@@ -1246,15 +1261,35 @@ extern "C" int cu_affine_sshex8_linear_elasticity_apply(int level, ptrdiff_t nel
                                                         int real_type, ptrdiff_t u_stride, const void *ux,
                                                         const void *uy, const void *uz, ptrdiff_t out_stride,
                                                         void *outx, void *outy, void *outz, void *stream) {
-    // Interleaved xyz vectors only: ux = u, uy = u + 1, uz = u + 2 with stride 3.
+    // interleaved xyz vectors (ux = u, uy = u + 1, uz = u + 2, stride 3): the tuned kernels;
+    // any other layout (separate component arrays, other strides): the CTA-per-element
+    // kernel reading and writing through the component pointers and strides
     const size_t es = (real_type == SFEM_GB300_FLOAT32 || real_type == SFEM_GB300_FLOAT32_BF16TC) ? 4 : 8;
-    if (u_stride != 3 || out_stride != 3 || (const char *)uy != (const char *)ux + es ||
-        (const char *)uz != (const char *)ux + 2 * es || (char *)outy != (char *)outx + es ||
-        (char *)outz != (char *)outx + 2 * es)
-        return set_error("cu_affine_sshex8_linear_elasticity_apply: only interleaved (stride 3) vectors are supported");
-    return sfem_gb300_linear_elasticity_apply(SFEM_GB300_SSHEX8(level), nelements, elements, jacobian_stride,
-                                              (const float *)jacobian_adjugate, (const float *)jacobian_determinant, mu,
-                                              lambda, real_type, ux, outx, stream);
+    if (u_stride == 3 && out_stride == 3 && (const char *)uy == (const char *)ux + es &&
+        (const char *)uz == (const char *)ux + 2 * es && (char *)outy == (char *)outx + es &&
+        (char *)outz == (char *)outx + 2 * es)
+        return sfem_gb300_linear_elasticity_apply(SFEM_GB300_SSHEX8(level), nelements, elements, jacobian_stride,
+                                                  (const float *)jacobian_adjugate, (const float *)jacobian_determinant,
+                                                  mu, lambda, real_type, ux, outx, stream);
+    if (level < 1 || level > EL_MAX_L)
+        return set_error("cu_affine_sshex8_linear_elasticity_apply: level %d (1..%d)", level, EL_MAX_L);
+    if (u_stride < 1 || out_stride < 1)
+        return set_error("cu_affine_sshex8_linear_elasticity_apply: strides must be positive");
+    if (nelements <= 0) return SFEM_GB300_SUCCESS;
+    const cudaStream_t s = stream_of(stream);
+    const float *adj = (const float *)jacobian_adjugate, *det = (const float *)jacobian_determinant;
+    if (es == 4)
+        return launch_el_cta_views<float>(level, nelements, elements, jacobian_stride, adj, det, (float)mu,
+                                          (float)lambda,
+                                          Comp3<const float *>{{(const float *)ux, (const float *)uy, (const float *)uz},
+                                                               u_stride},
+                                          Comp3<float *>{{(float *)outx, (float *)outy, (float *)outz}, out_stride}, s);
+    if (real_type != SFEM_GB300_FLOAT64 && real_type != SFEM_GB300_REAL_DEFAULT)
+        return set_error("cu_affine_sshex8_linear_elasticity_apply: unsupported real type %d", real_type);
+    return launch_el_cta_views<double>(
+            level, nelements, elements, jacobian_stride, adj, det, mu, lambda,
+            Comp3<const double *>{{(const double *)ux, (const double *)uy, (const double *)uz}, u_stride},
+            Comp3<double *>{{(double *)outx, (double *)outy, (double *)outz}, out_stride}, s);
 }
 
 extern "C" int sfem_gb300_linear_elasticity_block_diag(int element_type, ptrdiff_t nelements, idx_t **elements,

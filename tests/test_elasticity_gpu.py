@@ -170,11 +170,34 @@ def test_elasticity_reference_signature_and_fp32(cuda, fp32_kernel, shape):
         assert err.max() < tol, (dt, rt, err.max())
     capi.check(lib.sfem_gb300_set_elasticity_kernel(-1), "variant")
     assert lib.sfem_gb300_elasticity_status() == 0
-    # non-interleaved layouts are rejected with a message
-    assert lib.cu_affine_sshex8_linear_elasticity_apply(
-        L, capi.i64(m.n_elements), sp.elements_ptrs.ptr, capi.i64(m.n_elements), capi.vp(adj_d), capi.vp(det_d),
-        ctypes_d(MU), ctypes_d(LAM), capi.FLOAT64, capi.i64(1), capi.vp(yd), capi.vp(yd), capi.vp(yd), capi.i64(1),
-        capi.vp(yd), capi.vp(yd), capi.vp(yd), None) == 1
+    # other layouts, as the reference's signature allows: separate component arrays
+    # (stride 1) and interleaved with a padding slot (stride 4); the padding stays untouched
+    for dt, rt, tol in ((torch.float64, capi.FLOAT64, 1e-13), (torch.float32, capi.FLOAT32, 2e-5)):
+        for stride in (1, 4):
+            if stride == 1:
+                us = [torch.from_numpy(u[d::3].copy()).to(cuda).to(dt) for d in range(3)]
+                ys = [torch.zeros(n, dtype=dt, device=cuda) for _ in range(3)]
+                uptr, yptr = [capi.vp(t) for t in us], [capi.vp(t) for t in ys]
+            else:
+                ub = torch.full((n, 4), 7.0, dtype=dt, device=cuda)
+                ub[:, :3] = torch.from_numpy(u.reshape(n, 3)).to(cuda).to(dt)
+                yb = torch.full((n, 4), -3.0, dtype=dt, device=cuda)
+                yb[:, :3] = 0
+                es = ub.element_size()
+                uptr = [capi.c_void(ub.data_ptr() + d * es) for d in range(3)]
+                yptr = [capi.c_void(yb.data_ptr() + d * es) for d in range(3)]
+            capi.check(lib.cu_affine_sshex8_linear_elasticity_apply(
+                L, capi.i64(m.n_elements), sp.elements_ptrs.ptr, capi.i64(m.n_elements), capi.vp(adj_d),
+                capi.vp(det_d), ctypes_d(MU), ctypes_d(LAM), rt, capi.i64(stride), *uptr, capi.i64(stride), *yptr,
+                None), "cu_affine_sshex8_linear_elasticity_apply (strided)")
+            torch.cuda.synchronize()
+            if stride == 1:
+                got = torch.stack(ys, dim=1).reshape(-1)
+            else:
+                assert bool((yb[:, 3] == -3.0).all())
+                got = yb[:, :3].reshape(-1)
+            err = np.abs(got.double().cpu().numpy() - ref) / _scale(L, el, adj, det, u)
+            assert err.max() < tol, (dt, stride, err.max())
 
 
 @pytest.mark.parametrize("L", [1, 2, 4, 8])
