@@ -125,6 +125,19 @@ def sshex8_laplacian_apply_nonaffine(L, elements, points, u, out=None, use_ref=F
     return out
 
 
+def sshex8_laplacian_apply_affine_points_ref(L, elements, points, u, out=None):
+    """values += A u by the reference's affine_sshex8_laplacian_apply
+    (operators/sshex8/sshex8_laplacian.cpp:184-330): the affine form with the metric
+    computed from the corner points at the element centre (fixture generation only)."""
+    E = elements.shape[1]
+    u = _f64(u)
+    out = np.zeros_like(u) if out is None else out
+    ea, pa = PtrArray(elements.astype(np.int32)), PtrArray(_f32(points))
+    rc = ref().affine_sshex8_laplacian_apply(c_int(L), c_ptrdiff(E), ea.p, pa.p, _ptr(u), _ptr(out))
+    assert rc == 0, rc
+    return out
+
+
 def adjugate_fill(corners, points, use_ref=False):
     L = ref() if use_ref else lib()
     fn = L.ref_hex8_adjugate_and_det_fill if use_ref else L.or_hex8_adjugate_and_det_fill

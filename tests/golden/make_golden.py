@@ -132,7 +132,8 @@ def make_coefficient():
 def make_nonaffine():
     """The non-affine sshex8 Laplacian: the reference's sshex8_laplacian_apply
     (operators/sshex8/sshex8_laplacian.cpp:39-182; six-point rule per micro element, FFF
-    of the trilinear macro map at every point) on perturbed macro meshes at L = 2 and 4."""
+    of the trilinear macro map at every point) on perturbed macro meshes at L = 2 and 4,
+    and the reference's affine_sshex8_laplacian_apply (:184-330) on the same meshes."""
     assert O.ref() is not None, "reference kernels unavailable"
     out = {}
     for L, n, seed in ((2, (4, 3, 2), 51), (4, (3, 2, 2), 52)):
@@ -140,8 +141,11 @@ def make_nonaffine():
         el = m.elements(L)
         x = np.random.default_rng(seed + 100).standard_normal(m.n_nodes(L))
         y = O.sshex8_laplacian_apply_nonaffine(L, el, m.points, x, use_ref=True)
+        # the reference's affine form from the corner points (FFF at the element centre,
+        # sshex8_laplacian.cpp:184-330) on the same mesh
+        ya = O.sshex8_laplacian_apply_affine_points_ref(L, el, m.points, x)
         out.update({f"L{L}_elements": el, f"L{L}_points": m.points.astype(np.float32), f"L{L}_x": x,
-                    f"L{L}_apply": y, f"L{L}_shape": np.array(n), f"L{L}_seed": seed})
+                    f"L{L}_apply": y, f"L{L}_affine_apply": ya, f"L{L}_shape": np.array(n), f"L{L}_seed": seed})
     np.savez_compressed(OUT / "sshex8_nonaffine.npz", perturb=0.2, **out)
     print("wrote", OUT / "sshex8_nonaffine.npz")
 

@@ -305,3 +305,17 @@ def test_nonaffine_laplacian_matches_reference_directly():
     ours = O.sshex8_laplacian_apply_nonaffine(3, el, m.points, x)
     ref = O.sshex8_laplacian_apply_nonaffine(3, el, m.points, x, use_ref=True)
     assert _rel(ours, ref) < 1e-14
+
+
+@pytest.mark.parametrize("L", [2, 4])
+def test_affine_points_form_matches_reference_golden(L):
+    """The reference's affine_sshex8_laplacian_apply (sshex8_laplacian.cpp:184-330: the
+    metric computed from the corner points at the element centre, kept in double) and the
+    affine form this library computes from the float32 FFF cache (the reference's default
+    affine_sshex8_laplacian_stencil_apply_fff input) are the same operator: they agree to
+    the float32 rounding of the metric (6e-8 relative), on perturbed meshes."""
+    g = np.load(NONAFFINE)
+    el, pts, x = g[f"L{L}_elements"], g[f"L{L}_points"], g[f"L{L}_x"]
+    m = SSMesh(*g[f"L{L}_shape"], L)
+    ours = O.sshex8_laplacian_stencil_apply(L, el, O.fff_fill(el[m.macro_corner_lidx(L)], pts), x)
+    assert _rel(ours, g[f"L{L}_affine_apply"]) < 1e-7
