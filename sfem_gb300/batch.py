@@ -471,6 +471,21 @@ class BatchSolver:
         return (rr.sqrt() / bb.sqrt()).cpu().numpy()
 
 
+def stream_priority_levels(sizes, levels=6):
+    """Stream priority level per group (0 = the default, higher = scheduled first): the
+    groups ranked by size, the smallest on the top level (levels - 1), the largest on 0,
+    the ranks in between spread over the levels (equal sizes keep their order).  One
+    group: level 0."""
+    n = len(sizes)
+    out = [0] * n
+    if n < 2:
+        return out
+    order = sorted(range(n), key=lambda i: sizes[i])
+    for rank, i in enumerate(order):
+        out[i] = (levels - 1) - (rank * (levels - 1)) // (n - 1)
+    return out
+
+
 class ConcurrentBatchSolver:
     """The problems of a :class:`BatchSolver`, one batched solver per group (its own
     context, stream and captured chunk of CG iterations), advanced independently by one
@@ -492,14 +507,11 @@ class ConcurrentBatchSolver:
                 s.set_launch(*launch)
         # the smaller a group's total dofs, the higher its stream priority: its chunks
         # are short, and running them first is what takes its problems out of the queue
-        self.priority = [0] * len(self.subs)
-        if prioritize and len(self.subs) > 1:
-            order = sorted(range(len(self.subs)), key=lambda i: self.subs[i].n)
-            top = self.PRIORITY_LEVELS - 1
-            for rank, i in enumerate(order):
-                self.priority[i] = top - (rank * self.PRIORITY_LEVELS) // len(self.subs)
-                capi.check(capi.load().sfem_gb300_batch_solve_set_priority(self.subs[i].solver.ptr,
-                                                                           C.c_int(self.priority[i])),
+        self.priority = (stream_priority_levels([g.n for g in self.subs], self.PRIORITY_LEVELS) if prioritize
+                         else [0] * len(self.subs))
+        for sub, level in zip(self.subs, self.priority):
+            if level:
+                capi.check(capi.load().sfem_gb300_batch_solve_set_priority(sub.solver.ptr, C.c_int(level)),
                            "batch_solve_set_priority")
         self.kernels = dict(kernels) if kernels else None
         self.problems = [p for s in self.subs for p in s.problems]
