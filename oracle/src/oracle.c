@@ -352,6 +352,59 @@ static void stencil_linear_offsets(int L, const stencil_taps_t *T, int *vcls, in
             offl[cls][q] = T->off[cls][q][0] + N1 * (T->off[cls][q][1] + N1 * T->off[cls][q][2]);
 }
 
+/* L = 4 (the benchmark level): one function per node class with every loop bound a
+ * compile-time constant (nodes of the class, and its taps dz, dy, dx in that order, the
+ * order of the tap tables), so the compiler unrolls them into straight-line code with
+ * fixed offsets on the 5x5x5 micro grid.  c27: the class's coefficients as a full 3x3x3
+ * block indexed (dz+1)*9 + (dy+1)*3 + (dx+1); a tap that does not exist is never read. */
+#define OR_LO(c) ((c) == 0 ? 0 : ((c) == 1 ? 1 : 4))
+#define OR_HI(c) ((c) == 1 ? 3 : OR_LO(c))
+#define OR_D0(c) ((c) == 0 ? 0 : -1)
+#define OR_D1(c) ((c) == 2 ? 0 : 1)
+#define OR_L4_CLASS(REAL, P, CX, CY, CZ)                                                                   \
+    static inline void P##_##CX##CY##CZ(const REAL *restrict c27, const REAL *restrict in,                \
+                                        REAL *restrict out) {                                             \
+        for (int z = OR_LO(CZ); z <= OR_HI(CZ); z++)                                                       \
+            for (int y = OR_LO(CY); y <= OR_HI(CY); y++)                                                   \
+                for (int x = OR_LO(CX); x <= OR_HI(CX); x++) {                                             \
+                    REAL acc = 0;                                                                          \
+                    for (int dz = OR_D0(CZ); dz <= OR_D1(CZ); dz++)                                        \
+                        for (int dy = OR_D0(CY); dy <= OR_D1(CY); dy++)                                    \
+                            for (int dx = OR_D0(CX); dx <= OR_D1(CX); dx++)                                \
+                                acc += c27[(dz + 1) * 9 + (dy + 1) * 3 + (dx + 1)] *                       \
+                                       in[(z + dz) * 25 + (y + dy) * 5 + x + dx];                          \
+                    out[z * 25 + y * 5 + x] = acc;                                                         \
+                }                                                                                          \
+    }
+#define OR_L4_CLASSES_Z(REAL, P, CZ)                                                                       \
+    OR_L4_CLASS(REAL, P, 0, 0, CZ) OR_L4_CLASS(REAL, P, 1, 0, CZ) OR_L4_CLASS(REAL, P, 2, 0, CZ)            \
+    OR_L4_CLASS(REAL, P, 0, 1, CZ) OR_L4_CLASS(REAL, P, 1, 1, CZ) OR_L4_CLASS(REAL, P, 2, 1, CZ)            \
+    OR_L4_CLASS(REAL, P, 0, 2, CZ) OR_L4_CLASS(REAL, P, 1, 2, CZ) OR_L4_CLASS(REAL, P, 2, 2, CZ)
+#define OR_L4_ALL(REAL, P)                                                                                 \
+    OR_L4_CLASSES_Z(REAL, P, 0) OR_L4_CLASSES_Z(REAL, P, 1) OR_L4_CLASSES_Z(REAL, P, 2)                     \
+    static inline void P##_apply(const REAL (*full)[27], const REAL *restrict in, REAL *restrict out) {    \
+        P##_000(full[0], in, out);  P##_100(full[1], in, out);  P##_200(full[2], in, out);                 \
+        P##_010(full[3], in, out);  P##_110(full[4], in, out);  P##_210(full[5], in, out);                 \
+        P##_020(full[6], in, out);  P##_120(full[7], in, out);  P##_220(full[8], in, out);                 \
+        P##_001(full[9], in, out);  P##_101(full[10], in, out); P##_201(full[11], in, out);                \
+        P##_011(full[12], in, out); P##_111(full[13], in, out); P##_211(full[14], in, out);                \
+        P##_021(full[15], in, out); P##_121(full[16], in, out); P##_221(full[17], in, out);                \
+        P##_002(full[18], in, out); P##_102(full[19], in, out); P##_202(full[20], in, out);                \
+        P##_012(full[21], in, out); P##_112(full[22], in, out); P##_212(full[23], in, out);                \
+        P##_022(full[24], in, out); P##_122(full[25], in, out); P##_222(full[26], in, out);                \
+    }
+OR_L4_ALL(double, or_l4d)
+OR_L4_ALL(float, or_l4f)
+
+/* full 3x3x3 coefficient blocks of every class from the tap tables */
+#define OR_FULL_COEF(coef, full, T)                                                          \
+    for (int cls = 0; cls < 27; cls++) {                                                     \
+        for (int k = 0; k < 27; k++) (full)[cls][k] = 0;                                     \
+        for (int q = 0; q < (T)->ntaps[cls]; q++)                                            \
+            (full)[cls][((T)->off[cls][q][2] + 1) * 9 + ((T)->off[cls][q][1] + 1) * 3 +      \
+                       ((T)->off[cls][q][0] + 1)] = (coef)[cls][q];                          \
+    }
+
 /* affine_sshex8_laplacian_stencil_apply_fff (operators/sshex8/sshex8_laplacian.cpp:698-769),
  * values += A u.  Per macro element: sub-FFF = FFF / L (:19-28), element matrix A, the
  * 27-point stencil of A (hex8_matrix_to_stencil, operators/stencil/stencil3.hpp:205)
@@ -390,6 +443,11 @@ int or_sshex8_laplacian_stencil_apply(int L, ptrdiff_t nelements, idx_t **elemen
                 idx[v] = elements[v][e];
                 eu[v] = u[idx[v]];
             }
+            if (L == 4) {
+                double full[27][27];
+                OR_FULL_COEF(coef, full, T);
+                or_l4d_apply((const double(*)[27])full, eu, ev);
+            } else
             /* class by class, rows of nodes along x (the reference's stencil sweeps run
              * along x too); fixed tap counts so the x loop unrolls and vectorises */
             for (int cls = 0; cls < 27; cls++) {
@@ -485,6 +543,11 @@ int or_sshex8_laplacian_stencil_apply_f32(int L, ptrdiff_t nelements, idx_t **el
                 idx[v] = elements[v][e];
                 eu[v] = u[idx[v]];
             }
+            if (L == 4) {
+                float full[27][27];
+                OR_FULL_COEF(coef, full, T);
+                or_l4f_apply((const float(*)[27])full, eu, ev);
+            } else
             /* class by class, rows of nodes along x (the reference's stencil sweeps run
              * along x too); fixed tap counts so the x loop unrolls and vectorises */
             for (int cls = 0; cls < 27; cls++) {
