@@ -301,6 +301,7 @@ int or_sshex8_laplacian_apply_f32(int L, ptrdiff_t nelements, idx_t **elements, 
 typedef struct {
     int ntaps[27];
     int off[27][27][3];
+    int pos[27][27];  /* (dz+1)*9 + (dy+1)*3 + (dx+1): the tap's slot in a full 3x3x3 block */
     int nsum[27][27];
     int a[27][27][8];
 } stencil_taps_t;
@@ -332,6 +333,7 @@ static void stencil_taps(stencil_taps_t *t) {
                     t->off[cls][q][0] = dx;
                     t->off[cls][q][1] = dy;
                     t->off[cls][q][2] = dz;
+                    t->pos[cls][q] = (dz + 1) * 9 + (dy + 1) * 3 + (dx + 1);
                     t->nsum[cls][q] = n;
                     for (int i = 0; i < n; i++) t->a[cls][q][i] = idx[i];
                 }
@@ -396,15 +398,6 @@ static void stencil_linear_offsets(int L, const stencil_taps_t *T, int *vcls, in
 OR_L4_ALL(double, or_l4d)
 OR_L4_ALL(float, or_l4f)
 
-/* full 3x3x3 coefficient blocks of every class from the tap tables */
-#define OR_FULL_COEF(coef, full, T)                                                          \
-    for (int cls = 0; cls < 27; cls++) {                                                     \
-        for (int k = 0; k < 27; k++) (full)[cls][k] = 0;                                     \
-        for (int q = 0; q < (T)->ntaps[cls]; q++)                                            \
-            (full)[cls][((T)->off[cls][q][2] + 1) * 9 + ((T)->off[cls][q][1] + 1) * 3 +      \
-                       ((T)->off[cls][q][0] + 1)] = (coef)[cls][q];                          \
-    }
-
 /* affine_sshex8_laplacian_stencil_apply_fff (operators/sshex8/sshex8_laplacian.cpp:698-769),
  * values += A u.  Per macro element: sub-FFF = FFF / L (:19-28), element matrix A, the
  * 27-point stencil of A (hex8_matrix_to_stencil, operators/stencil/stencil3.hpp:205)
@@ -427,6 +420,8 @@ int or_sshex8_laplacian_stencil_apply(int L, ptrdiff_t nelements, idx_t **elemen
         double *ev = (double *)malloc(nxe * sizeof(double));
         idx_t *idx = (idx_t *)malloc(nxe * sizeof(idx_t));
         double coef[27][27];
+        double full[27][27];
+        memset(full, 0, sizeof(full));  /* slots of taps that do not exist stay zero */
 #pragma omp for
         for (ptrdiff_t e = 0; e < nelements; e++) {
             double sub[6], A[64];
@@ -438,14 +433,13 @@ int or_sshex8_laplacian_stencil_apply(int L, ptrdiff_t nelements, idx_t **elemen
                     double c = 0;
                     for (int i = 0; i < T->nsum[cls][q]; i++) c += A[T->a[cls][q][i]];
                     coef[cls][q] = c;
+                    full[cls][T->pos[cls][q]] = c;
                 }
             for (int v = 0; v < nxe; v++) {
                 idx[v] = elements[v][e];
                 eu[v] = u[idx[v]];
             }
             if (L == 4) {
-                double full[27][27];
-                OR_FULL_COEF(coef, full, T);
                 or_l4d_apply((const double(*)[27])full, eu, ev);
             } else
             /* class by class, rows of nodes along x (the reference's stencil sweeps run
@@ -525,6 +519,8 @@ int or_sshex8_laplacian_stencil_apply_f32(int L, ptrdiff_t nelements, idx_t **el
         float *ev = (float *)malloc(nxe * sizeof(float));
         idx_t *idx = (idx_t *)malloc(nxe * sizeof(idx_t));
         float coef[27][27];
+        float full[27][27];
+        memset(full, 0, sizeof(full));  /* slots of taps that do not exist stay zero */
 #pragma omp for
         for (ptrdiff_t e = 0; e < nelements; e++) {
             double sub[6], Ad[64];
@@ -538,14 +534,13 @@ int or_sshex8_laplacian_stencil_apply_f32(int L, ptrdiff_t nelements, idx_t **el
                     float c = 0;
                     for (int i = 0; i < T->nsum[cls][q]; i++) c += A[T->a[cls][q][i]];
                     coef[cls][q] = c;
+                    full[cls][T->pos[cls][q]] = c;
                 }
             for (int v = 0; v < nxe; v++) {
                 idx[v] = elements[v][e];
                 eu[v] = u[idx[v]];
             }
             if (L == 4) {
-                float full[27][27];
-                OR_FULL_COEF(coef, full, T);
                 or_l4f_apply((const float(*)[27])full, eu, ev);
             } else
             /* class by class, rows of nodes along x (the reference's stencil sweeps run
