@@ -354,36 +354,37 @@ static void stencil_linear_offsets(int L, const stencil_taps_t *T, int *vcls, in
             offl[cls][q] = T->off[cls][q][0] + N1 * (T->off[cls][q][1] + N1 * T->off[cls][q][2]);
 }
 
-/* L = 4 (the benchmark level): one function per node class with every loop bound a
- * compile-time constant (nodes of the class, and its taps dz, dy, dx in that order, the
- * order of the tap tables), so the compiler unrolls them into straight-line code with
- * fixed offsets on the 5x5x5 micro grid.  c27: the class's coefficients as a full 3x3x3
- * block indexed (dz+1)*9 + (dy+1)*3 + (dx+1); a tap that does not exist is never read. */
-#define OR_LO(c) ((c) == 0 ? 0 : ((c) == 1 ? 1 : 4))
-#define OR_HI(c) ((c) == 1 ? 3 : OR_LO(c))
+/* L = 2, 3, 4: one function per node class with every loop bound a compile-time
+ * constant (nodes of the class, and its taps dz, dy, dx in that order, the order of the
+ * tap tables), so the compiler unrolls them into straight-line code with fixed offsets
+ * on the (L+1)^3 micro grid.  c27: the class's coefficients as a full 3x3x3 block indexed
+ * (dz+1)*9 + (dy+1)*3 + (dx+1); a tap that does not exist is never read. */
+#define OR_LO(LL, c) ((c) == 0 ? 0 : ((c) == 1 ? 1 : (LL)))
+#define OR_HI(LL, c) ((c) == 1 ? (LL) - 1 : OR_LO(LL, c))
 #define OR_D0(c) ((c) == 0 ? 0 : -1)
 #define OR_D1(c) ((c) == 2 ? 0 : 1)
-#define OR_L4_CLASS(REAL, P, CX, CY, CZ)                                                                   \
+#define OR_CLASS(REAL, P, LL, CX, CY, CZ)                                                                  \
     static inline void P##_##CX##CY##CZ(const REAL *restrict c27, const REAL *restrict in,                \
                                         REAL *restrict out) {                                             \
-        for (int z = OR_LO(CZ); z <= OR_HI(CZ); z++)                                                       \
-            for (int y = OR_LO(CY); y <= OR_HI(CY); y++)                                                   \
-                for (int x = OR_LO(CX); x <= OR_HI(CX); x++) {                                             \
+        enum { N1_ = (LL) + 1, NP_ = N1_ * N1_ };                                                          \
+        for (int z = OR_LO(LL, CZ); z <= OR_HI(LL, CZ); z++)                                               \
+            for (int y = OR_LO(LL, CY); y <= OR_HI(LL, CY); y++)                                           \
+                for (int x = OR_LO(LL, CX); x <= OR_HI(LL, CX); x++) {                                     \
                     REAL acc = 0;                                                                          \
                     for (int dz = OR_D0(CZ); dz <= OR_D1(CZ); dz++)                                        \
                         for (int dy = OR_D0(CY); dy <= OR_D1(CY); dy++)                                    \
                             for (int dx = OR_D0(CX); dx <= OR_D1(CX); dx++)                                \
                                 acc += c27[(dz + 1) * 9 + (dy + 1) * 3 + (dx + 1)] *                       \
-                                       in[(z + dz) * 25 + (y + dy) * 5 + x + dx];                          \
-                    out[z * 25 + y * 5 + x] = acc;                                                         \
+                                       in[(z + dz) * NP_ + (y + dy) * N1_ + x + dx];                       \
+                    out[z * NP_ + y * N1_ + x] = acc;                                                      \
                 }                                                                                          \
     }
-#define OR_L4_CLASSES_Z(REAL, P, CZ)                                                                       \
-    OR_L4_CLASS(REAL, P, 0, 0, CZ) OR_L4_CLASS(REAL, P, 1, 0, CZ) OR_L4_CLASS(REAL, P, 2, 0, CZ)            \
-    OR_L4_CLASS(REAL, P, 0, 1, CZ) OR_L4_CLASS(REAL, P, 1, 1, CZ) OR_L4_CLASS(REAL, P, 2, 1, CZ)            \
-    OR_L4_CLASS(REAL, P, 0, 2, CZ) OR_L4_CLASS(REAL, P, 1, 2, CZ) OR_L4_CLASS(REAL, P, 2, 2, CZ)
-#define OR_L4_ALL(REAL, P)                                                                                 \
-    OR_L4_CLASSES_Z(REAL, P, 0) OR_L4_CLASSES_Z(REAL, P, 1) OR_L4_CLASSES_Z(REAL, P, 2)                     \
+#define OR_CLASSES_Z(REAL, P, LL, CZ)                                                                      \
+    OR_CLASS(REAL, P, LL, 0, 0, CZ) OR_CLASS(REAL, P, LL, 1, 0, CZ) OR_CLASS(REAL, P, LL, 2, 0, CZ)         \
+    OR_CLASS(REAL, P, LL, 0, 1, CZ) OR_CLASS(REAL, P, LL, 1, 1, CZ) OR_CLASS(REAL, P, LL, 2, 1, CZ)         \
+    OR_CLASS(REAL, P, LL, 0, 2, CZ) OR_CLASS(REAL, P, LL, 1, 2, CZ) OR_CLASS(REAL, P, LL, 2, 2, CZ)
+#define OR_ALL(REAL, P, LL)                                                                                \
+    OR_CLASSES_Z(REAL, P, LL, 0) OR_CLASSES_Z(REAL, P, LL, 1) OR_CLASSES_Z(REAL, P, LL, 2)                  \
     static inline void P##_apply(const REAL (*full)[27], const REAL *restrict in, REAL *restrict out) {    \
         P##_000(full[0], in, out);  P##_100(full[1], in, out);  P##_200(full[2], in, out);                 \
         P##_010(full[3], in, out);  P##_110(full[4], in, out);  P##_210(full[5], in, out);                 \
@@ -395,8 +396,12 @@ static void stencil_linear_offsets(int L, const stencil_taps_t *T, int *vcls, in
         P##_012(full[21], in, out); P##_112(full[22], in, out); P##_212(full[23], in, out);                \
         P##_022(full[24], in, out); P##_122(full[25], in, out); P##_222(full[26], in, out);                \
     }
-OR_L4_ALL(double, or_l4d)
-OR_L4_ALL(float, or_l4f)
+OR_ALL(double, or_l2d, 2)
+OR_ALL(float, or_l2f, 2)
+OR_ALL(double, or_l3d, 3)
+OR_ALL(float, or_l3f, 3)
+OR_ALL(double, or_l4d, 4)
+OR_ALL(float, or_l4f, 4)
 
 /* affine_sshex8_laplacian_stencil_apply_fff (operators/sshex8/sshex8_laplacian.cpp:698-769),
  * values += A u.  Per macro element: sub-FFF = FFF / L (:19-28), element matrix A, the
@@ -439,8 +444,14 @@ int or_sshex8_laplacian_stencil_apply(int L, ptrdiff_t nelements, idx_t **elemen
                 idx[v] = elements[v][e];
                 eu[v] = u[idx[v]];
             }
-            if (L == 4) {
-                or_l4d_apply((const double(*)[27])full, eu, ev);
+            if (L >= 2 && L <= 4) {
+                const double(*cf)[27] = (const double(*)[27])full;
+                if (L == 4)
+                    or_l4d_apply(cf, eu, ev);
+                else if (L == 3)
+                    or_l3d_apply(cf, eu, ev);
+                else
+                    or_l2d_apply(cf, eu, ev);
             } else
             /* class by class, rows of nodes along x (the reference's stencil sweeps run
              * along x too); fixed tap counts so the x loop unrolls and vectorises */
@@ -540,8 +551,14 @@ int or_sshex8_laplacian_stencil_apply_f32(int L, ptrdiff_t nelements, idx_t **el
                 idx[v] = elements[v][e];
                 eu[v] = u[idx[v]];
             }
-            if (L == 4) {
-                or_l4f_apply((const float(*)[27])full, eu, ev);
+            if (L >= 2 && L <= 4) {
+                const float(*cf)[27] = (const float(*)[27])full;
+                if (L == 4)
+                    or_l4f_apply(cf, eu, ev);
+                else if (L == 3)
+                    or_l3f_apply(cf, eu, ev);
+                else
+                    or_l2f_apply(cf, eu, ev);
             } else
             /* class by class, rows of nodes along x (the reference's stencil sweeps run
              * along x too); fixed tap counts so the x loop unrolls and vectorises */
