@@ -319,3 +319,19 @@ def test_affine_points_form_matches_reference_golden(L):
     m = SSMesh(*g[f"L{L}_shape"], L)
     ours = O.sshex8_laplacian_stencil_apply(L, el, O.fff_fill(el[m.macro_corner_lidx(L)], pts), x)
     assert _rel(ours, g[f"L{L}_affine_apply"]) < 1e-7
+
+
+def test_reference_root_is_explicit(tmp_path, monkeypatch):
+    """The reference tree comes from an argument or SFEM_REFERENCE_ROOT, with a clear error
+    when neither names an sfem checkout."""
+    from oracle import build as ob
+
+    monkeypatch.delenv("SFEM_REFERENCE_ROOT", raising=False)
+    with pytest.raises(RuntimeError, match="SFEM_REFERENCE_ROOT"):
+        ob.reference_root()
+    with pytest.raises(RuntimeError, match="not an sfem tree"):
+        ob.reference_root(str(tmp_path))
+    (tmp_path / "operators" / "sshex8").mkdir(parents=True)
+    (tmp_path / "operators" / "sshex8" / "sshex8_laplacian.cpp").write_text("")
+    monkeypatch.setenv("SFEM_REFERENCE_ROOT", str(tmp_path))
+    assert ob.reference_root() == tmp_path
